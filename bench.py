@@ -1,0 +1,395 @@
+#!/usr/bin/env python
+"""Benchmark of the HJM exposure / CVA path on one GB300 (path-steps per second).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload fp64|mixed] [--no-extras]
+
+Default workload (``fp64``): the plain FP64 valuation of one payer swap
+(notional 1e6, fixed 2.5%, 10y semiannual) on 1,048,576 paths x 1,000 Euler
+steps (dt = 0.01) of the 3-factor HJM model on the 51-tenor Nelson-Siegel
+curve, with EE, PFE(97.5%) on the 21 reset dates and CVA (hazard 2%,
+recovery 40%).  ``mixed``: the same at 4,194,304 paths in mixed precision.
+One step = one valuation (path kernel + reductions + PFE selection).  The
+timed region holds K steps, each followed by a 256 MiB device write that
+evicts L2 (the path kernel reads no input from HBM; its normals are made in
+registers).  ``value`` is device-resident throughput (CUDA events on the
+launching stream); ``e2e`` repeats the workload through the C ABI call with
+host buffers (hjm_run), copies included.  Unless --no-extras, rank 0 also
+reports the mixed-precision run against the FP64 run on identical normals,
+the measured FMA peaks (roofline denominators) and the CPU baseline (the
+oracle port on all host cores, on a bounded sample of the same workload).
+
+``--impl reference`` times the reference algorithm's CPU implementation (the
+oracle port, all host threads) on the same workload and prints the same line
+with "impl": "reference".  Under torchrun only rank 0 runs it.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "HJM path-steps/s and CVA+deltas time: FP32-mixed vs FP64 on 1 GB300 @1e-4 rel"
+UNIT = "path-steps/s"
+N_STEPS, DT, SEED = 1000, 0.01, 1234
+WORKLOADS = {
+    "fp64": {"precision": "fp64", "n_paths": 1_048_576, "dtype": "f64",
+             "name": "hjm-3f-51tenor-payer-irs-10y-fp64-1048576paths-1000steps"},
+    "mixed": {"precision": "mixed", "n_paths": 4_194_304, "dtype": "f32+f64",
+              "name": "hjm-3f-51tenor-payer-irs-10y-mixed-4194304paths-1000steps"},
+}
+FLUSH_BYTES = 256 << 20
+
+
+def env_rank():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)),
+            int(os.environ.get("WORLD_SIZE", 1)))
+
+
+def algorithmic_flops_per_path(n_tenor: int, n_steps: int, stride: int) -> int:
+    """Flops the method needs per path: the Euler update of the stochastic curve,
+    4 FMAs + 1 subtraction = 9 flops per tenor per evolved step (the first block
+    holds the curve at spot and does no arithmetic), plus one addition per
+    discount accumulation of a tenor that is still to be sampled.  Pricing,
+    normals and reductions are not counted, so the fraction is a lower bound."""
+    B = n_steps // stride
+    evolved = n_steps - stride
+    acc = stride * sum(B - b for b in range(1, B))
+    return evolved * 9 * n_tenor + acc
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.file = None
+
+    def start(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.file, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self) -> dict | None:
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.file.flush()
+        rows = [r.split(",") for r in Path(self.file.name).read_text().strip().splitlines() if r.count(",") >= 8]
+        os.unlink(self.file.name)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["active_mask", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i - 4] for r in rows for i in range(5, 9) if r[i].strip().lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def profiled_traffic(kernel_key: str) -> float | None:
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
+    f = ROOT / "profiles" / "path_kernel_ncu.md"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.startswith(f"traffic_bytes_per_launch[{kernel_key}]:"):
+            try:
+                return float(line.split(":", 1)[1].strip().split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def cpu_oracle_sample(target_s: float, n_threads: int) -> dict:
+    """The oracle port on all host cores, on a bounded sample of the workload."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    import numpy as np
+    import oracle_lib as O
+    from cva_hjm_cuda_gb300.market import Market, Swap
+
+    mk, sw = Market(), Swap()
+    lib = O.oracle()
+    ee = np.zeros(51)
+
+    def run(n):
+        t0 = time.perf_counter()
+        rc = lib.oracle_run_mt(51, mk.dtau, DT, N_STEPS, mk.spot, mk.vol.ravel(), mk.drift, sw.accrual, sw.notional,
+                               sw.strike, sw.sign, n, SEED, 0, n_threads, ee)
+        assert rc == 0
+        return time.perf_counter() - t0
+
+    n = 4 * n_threads
+    dt = run(n)
+    while dt < 0.3:
+        n *= 4
+        dt = run(n)
+    n = max(n_threads, int(n * target_s / dt))
+    return {"n_paths": n, "run": run}
+
+
+def cpu_model() -> str:
+    try:
+        for line in Path("/proc/cpuinfo").read_text().splitlines():
+            if line.lower().startswith(("model name", "cpu part", "hardware")):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+
+    return platform.processor() or platform.machine()
+
+
+# ---------------------------------------------------------------------------
+def run_reference(args) -> None:
+    rank, _, world = env_rank()
+    if rank != 0:
+        return
+    n_threads = os.cpu_count() or 1
+    wl = WORKLOADS[args.workload]
+    sample = cpu_oracle_sample(target_s=2.0, n_threads=n_threads)
+    n = sample["n_paths"]
+    for _ in range(args.warmup):
+        sample["run"](n)
+    times = [sample["run"](n) for _ in range(args.steps)]
+    total = sum(times)
+    value = n * N_STEPS * args.steps / total
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": wl["name"], "sample_paths_per_step": n, "n_steps": N_STEPS, "dt": DT,
+                   "n_tenor": 51, "l2": "n/a (host CPU)"},
+        "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": n_threads, "kind": "port",
+                         "sample": f"{n} paths x {N_STEPS} steps per step (FP64, the workload's first {n} paths)",
+                         "cpu": cpu_model()},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args) -> None:
+    import numpy as np
+    import torch
+
+    from cva_hjm_cuda_gb300 import HJMEngine, Market, RunConfig, Swap
+
+    rank, local_rank, world = env_rank()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local_rank)
+    wl = WORKLOADS[args.workload]
+    n_paths = args.paths or wl["n_paths"]
+    prec = wl["precision"]
+    mk, sw = Market(), Swap()
+    stride = int(round(mk.dtau / DT))
+    eng = HJMEngine(local_rank)
+    stream = torch.cuda.current_stream()
+    eng.set_stream(stream.cuda_stream)
+    eng.set_market(mk)
+    eng.set_swap(sw)
+    # weak scaling across ranks: rank r owns paths [r*n, (r+1)*n)
+    cfg = RunConfig(n_paths=n_paths, n_steps=N_STEPS, dt=DT, seed=SEED, path_offset=rank * n_paths)
+    flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+
+    for _ in range(args.warmup):
+        eng.enqueue(cfg, prec)
+        flush.zero_()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    launches = 0
+    for _ in range(args.steps):
+        eng.enqueue(cfg, prec)
+        launches += eng.stats()["kernels"]
+        flush.zero_()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    elapsed = e0.elapsed_time(e1) / 1e3
+    if dist:
+        t = torch.tensor([elapsed], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+    value = world * n_paths * N_STEPS * args.steps / elapsed
+    hist = eng.timing_history(min(args.steps, 64))
+    path_ms = float(hist[:, 0].mean())
+    step_dev_ms = float(hist[:, 3].mean())
+    res = eng.fetch()
+
+    # e2e: the C ABI call with host buffers (market/product arrays in, results out)
+    e2e_times = []
+    for i in range(args.steps):
+        t0 = time.perf_counter()
+        eng.set_market(mk)
+        eng.set_swap(sw)
+        eng.run(cfg, prec)
+        e2e_times.append(time.perf_counter() - t0)
+        flush.zero_()
+        torch.cuda.synchronize()
+    st = eng.stats()
+    h2d = st["h2d_bytes"] + 8 * (mk.spot.size + mk.vol.size + mk.drift.size + sw.accrual.size)
+    e2e_value = world * n_paths * N_STEPS * args.steps / sum(e2e_times)
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    flops = algorithmic_flops_per_path(mk.n_tenor, N_STEPS, stride) * n_paths
+    extras = {}
+    peak_key = "fp64" if prec == "fp64" else "mixed"
+    peak = None
+    if not args.no_extras:
+        peak64 = max(eng.fma_peak_tflops("fp64") for _ in range(2))
+        peak32 = max(eng.fma_peak_tflops("mixed") for _ in range(2))
+        peak = peak64 if peak_key == "fp64" else peak32
+        extras["measured_fma_peak_tflops"] = {"fp64": peak64, "fp32": peak32,
+                                             "how": "hjm_measure_fma_peak: 8 independent FMA chains per thread, "
+                                                    "8 CTAs x 256 threads per SM, best of 3 (2 flops per FMA)"}
+    achieved = flops / (path_ms * 1e-3) / 1e12
+    traffic = profiled_traffic(f"{prec}-{n_paths}")
+    roofline = {"bound": "fp64_pipe" if prec == "fp64" else "fp32_pipe", "achieved": achieved, "peak": peak,
+                "unit": "TFLOP/s", "frac": (achieved / peak) if peak else None, "traffic": traffic,
+                "kernel": f"path_kernel<51,{'double' if prec == 'fp64' else 'float'},false>",
+                "algorithmic_flops_per_launch": flops, "avg_launch_ms": path_ms,
+                "peak_source": "measured live by bench.py (FMA microkernel, this GPU)",
+                "hbm_peak_gbs_measured": _measured_hbm()}
+
+    if not args.no_extras and prec == "fp64":
+        extras["mixed"] = mixed_vs_fp64(eng, mk, sw, args, stream, flush, value)
+    if not args.no_extras:
+        cb = cpu_oracle_sample(target_s=3.0, n_threads=os.cpu_count() or 1)
+        n_cpu = cb["n_paths"]
+        t_cpu = cb["run"](n_cpu)
+        cpu_baseline = {"value": n_cpu * N_STEPS / t_cpu, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+                        "sample": f"first {n_cpu} paths x {N_STEPS} steps, FP64, oracle port, all host threads",
+                        "cpu": cpu_model()}
+    else:
+        cpu_baseline = None
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": wl["dtype"], "data": "synthetic",
+        "config": {"workload": wl["name"], "n_paths_per_gpu": n_paths, "n_steps": N_STEPS, "dt": DT, "n_tenor": 51,
+                   "factors": 3, "sampled_dates": N_STEPS // stride, "pfe_quantile": 0.975, "hazard": 0.02,
+                   "recovery": 0.4, "seed": SEED, "parallelism": f"replicas{world}" if world > 1 else "single",
+                   "l2": f"flushed between steps ({FLUSH_BYTES >> 20} MiB device write, inside the timed region)"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(st["d2h_bytes"]), "call": "hjm_set_market + hjm_set_swap + hjm_run"},
+        "gpu_launches": launches,
+        "roofline": roofline,
+        "cpu_baseline": cpu_baseline,
+        "clocks": clk,
+        "device_ms_per_step": step_dev_ms,
+        "result": {"cva": res.cva, "cva_stderr": res.cva_stderr, "ee_0": float(res.ee[0]),
+                   "pfe_0": float(res.pfe[0]) if res.pfe is not None else None},
+    }
+    line.update(extras)
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def _measured_hbm():
+    f = ROOT / "MEASURED_PEAKS.json"
+    try:
+        return json.loads(f.read_text()).get("hbm_gbs")
+    except (OSError, ValueError):
+        return None
+
+
+def mixed_vs_fp64(eng, mk, sw, args, stream, flush, fp64_value) -> dict:
+    """Mixed precision at 4,194,304 paths: throughput, and its error against the
+    FP64 valuation of the same paths (identical normals)."""
+    import numpy as np
+    import torch
+
+    from cva_hjm_cuda_gb300 import RunConfig
+
+    n = WORKLOADS["mixed"]["n_paths"]
+    cfg = RunConfig(n_paths=n, n_steps=N_STEPS, dt=DT, seed=SEED)
+    for _ in range(args.warmup):
+        eng.enqueue(cfg, "mixed")
+        flush.zero_()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        eng.enqueue(cfg, "mixed")
+        flush.zero_()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    el = e0.elapsed_time(e1) / 1e3
+    hist = eng.timing_history(min(args.steps, 64))
+    mx = eng.fetch()
+    f64 = eng.run(cfg, "fp64")
+    f64_ms = float(eng.timing_history(1)[0, 0])
+    rel = np.abs(mx.ee[:20] - f64.ee[:20]) / f64.ee[:20]
+    value = n * N_STEPS * args.steps / el
+    return {
+        "value": value, "unit": UNIT, "n_paths": n, "ms_per_step": 1e3 * el / args.steps,
+        "path_kernel_ms": float(hist[:, 0].mean()),
+        "speedup_vs_fp64_path_steps_per_s": value / fp64_value,
+        "fp64_same_paths_path_kernel_ms": f64_ms,
+        "ee_rel_err_vs_fp64_per_date": [float(x) for x in rel],
+        "ee_max_rel_err_vs_fp64": float(rel.max()),
+        "cva": mx.cva, "cva_fp64": f64.cva, "cva_rel_err_vs_fp64": abs(mx.cva - f64.cva) / f64.cva,
+        "cva_stderr": mx.cva_stderr,
+        "pfe_max_rel_err_vs_fp64": float(np.max(np.abs(mx.pfe[:20] - f64.pfe[:20]) / f64.pfe[:20])),
+    }
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="fp64")
+    ap.add_argument("--paths", type=int, default=0, help="override the workload's path count (profiling only)")
+    ap.add_argument("--no-extras", action="store_true", help="only the headline workload")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,695 @@
+// hjm_capi.cu -- the C ABI of libhjmcva.so (declared in include/hjm_cva.h).
+//
+// Host orchestration that replaces __calculateExposureMultiGPU
+// (simulation_gpu.cu:956-1241): instead of eight cudaMallocs, a cuRAND buffer,
+// 2,500 launches with a device synchronisation after each and a host-side
+// reduction, one context keeps grow-only device buffers, and one valuation is
+// a fixed sequence of launches on one stream (path kernel, column reduction,
+// finalisation, optional PFE selection) followed by one small copy-out.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/hjm_cva.h"
+#include "hjm_kernels.h"
+
+using namespace hjm;
+
+namespace {
+
+thread_local std::string g_thread_error;
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t need)
+    {
+        if (need <= bytes) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMalloc(&p, need);
+        if (e == cudaSuccess) bytes = need;
+        return e;
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+};
+
+}  // namespace
+
+struct hjm_ctx {
+    int device = 0;
+    int n_sms = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    std::string err;
+
+    // market
+    bool have_market = false;
+    bool have_poly = false;
+    int nt = 0;
+    double dtau = 0.5;
+    std::vector<double> spot, vol, drift;
+    double coef[HJM_N_VOL_COEF] = {0};
+
+    // product: cash flow of date i = D_i * (payA[i] * L_i - payB[i])
+    bool have_product = false;
+    std::vector<double> payA, payB;
+
+    bool keep_exposures = false;
+
+    // device buffers
+    DevBuf partials, sums, result, estore, sel, hist, ext, ext_raw, wide, scratch;
+
+    // last valuation
+    bool have_result = false;
+    int64_t last_n_paths = 0;
+    int last_n_dates = 0;
+    bool last_mixed = false;
+    bool last_stored = false;
+    bool last_pfe = false;
+    int64_t last_ld = 0;
+    int64_t stat_launches = 0, stat_h2d = 0, stat_d2h = 0;
+    // ring of event quadruples, one per valuation: before the path kernel,
+    // after it, after the reductions, after the PFE selection
+    static constexpr int kRing = 64;
+    cudaEvent_t ring[kRing][4] = {};
+    int64_t n_enqueued = 0;
+    cudaEvent_t* ev = nullptr;  // the quadruple of the current valuation
+};
+
+static hjm_status fail(hjm_ctx* ctx, hjm_status st, const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (ctx)
+        ctx->err = buf;
+    else
+        g_thread_error = buf;
+    return st;
+}
+
+#define HJM_CUDA(ctx, call)                                                                                 \
+    do {                                                                                                    \
+        cudaError_t e_ = (call);                                                                            \
+        if (e_ != cudaSuccess)                                                                              \
+            return fail((ctx), e_ == cudaErrorMemoryAllocation ? HJM_ERR_OUT_OF_MEMORY : HJM_ERR_CUDA,      \
+                        "%s failed: %s", #call, cudaGetErrorString(e_));                                    \
+    } while (0)
+
+#define HJM_CHECK_CTX(ctx)                                                                                  \
+    do {                                                                                                    \
+        if (!(ctx)) return fail(nullptr, HJM_ERR_INVALID_ARGUMENT, "null context");                        \
+    } while (0)
+
+static bool finite_all(const double* a, size_t n)
+{
+    for (size_t i = 0; i < n; ++i)
+        if (!std::isfinite(a[i])) return false;
+    return true;
+}
+
+// Every hjm_* function below is declared extern "C" in hjm_cva.h, so its
+// definition has C linkage.
+const char* hjm_version(void) { return "hjmcva 0.1.0 (sm_103a)"; }
+
+const char* hjm_last_error(const hjm_ctx* ctx) { return ctx ? ctx->err.c_str() : g_thread_error.c_str(); }
+
+hjm_status hjm_ctx_create(int device, hjm_ctx** out)
+{
+    if (!out) return fail(nullptr, HJM_ERR_INVALID_ARGUMENT, "out is null");
+    *out = nullptr;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n <= 0)
+        return fail(nullptr, HJM_ERR_NO_DEVICE, "no CUDA device: %s", cudaGetErrorString(e));
+    if (device < 0 || device >= n)
+        return fail(nullptr, HJM_ERR_INVALID_ARGUMENT, "device %d out of range [0, %d)", device, n);
+    e = cudaSetDevice(device);
+    if (e != cudaSuccess) return fail(nullptr, HJM_ERR_CUDA, "cudaSetDevice(%d): %s", device, cudaGetErrorString(e));
+    cudaDeviceProp prop;
+    e = cudaGetDeviceProperties(&prop, device);
+    if (e != cudaSuccess) return fail(nullptr, HJM_ERR_CUDA, "cudaGetDeviceProperties: %s", cudaGetErrorString(e));
+    if (prop.major < 10)
+        return fail(nullptr, HJM_ERR_UNSUPPORTED, "device %d is sm_%d%d; this library is built for sm_103a", device,
+                    prop.major, prop.minor);
+    hjm_ctx* c = new hjm_ctx();
+    c->device = device;
+    c->n_sms = prop.multiProcessorCount;
+    e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete c;
+        return fail(nullptr, HJM_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
+    }
+    c->stream = c->own_stream;
+    for (auto& q : c->ring)
+        for (auto& ev : q) {
+            e = cudaEventCreate(&ev);
+            if (e != cudaSuccess) {
+                hjm_ctx_destroy(c);
+                return fail(nullptr, HJM_ERR_CUDA, "cudaEventCreate: %s", cudaGetErrorString(e));
+            }
+        }
+    c->ev = c->ring[0];
+    *out = c;
+    return HJM_OK;
+}
+
+hjm_status hjm_ctx_destroy(hjm_ctx* ctx)
+{
+    if (!ctx) return HJM_OK;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    for (DevBuf* b : {&ctx->partials, &ctx->sums, &ctx->result, &ctx->estore, &ctx->sel, &ctx->hist, &ctx->ext,
+                      &ctx->ext_raw, &ctx->wide, &ctx->scratch})
+        b->release();
+    for (auto& q : ctx->ring)
+        for (auto& ev : q)
+            if (ev) cudaEventDestroy(ev);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    delete ctx;
+    return HJM_OK;
+}
+
+hjm_status hjm_ctx_set_stream(hjm_ctx* ctx, void* cuda_stream)
+{
+    HJM_CHECK_CTX(ctx);
+    ctx->stream = cuda_stream ? (cudaStream_t)cuda_stream : ctx->own_stream;
+    return HJM_OK;
+}
+
+hjm_status hjm_ctx_keep_exposures(hjm_ctx* ctx, int32_t keep)
+{
+    HJM_CHECK_CTX(ctx);
+    ctx->keep_exposures = keep != 0;
+    return HJM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// inputs
+// ---------------------------------------------------------------------------
+static void trapezoid_drift(const std::vector<double>& vol, int nt, double dtau, std::vector<double>& drift)
+{
+    drift.assign(nt, 0.0);
+    for (int k = 0; k < HJM_N_FACTOR; ++k) {
+        const double* s = vol.data() + (size_t)k * nt;
+        double integral = 0.0;
+        for (int i = 0; i < nt; ++i) {
+            if (i > 0) integral += 0.5 * (s[i] + s[i - 1]) * dtau;
+            drift[i] += s[i] * integral;
+        }
+    }
+}
+
+hjm_status hjm_set_market(hjm_ctx* ctx, int32_t n_tenor, double dtau, const double* spot_host,
+                          const double* vol_host, int32_t n_factor, const double* drift_host)
+{
+    HJM_CHECK_CTX(ctx);
+    if (n_tenor < 2 || n_tenor > HJM_MAX_TENOR)
+        return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "n_tenor %d outside [2, %d]", n_tenor, HJM_MAX_TENOR);
+    if (!path_tenor_supported(n_tenor))
+        return fail(ctx, HJM_ERR_UNSUPPORTED, "n_tenor %d: path kernels are built for 51 and 61 tenors", n_tenor);
+    if (n_factor != HJM_N_FACTOR)
+        return fail(ctx, HJM_ERR_UNSUPPORTED, "n_factor %d: the model has %d factors", n_factor, HJM_N_FACTOR);
+    if (!(dtau > 0.0) || !std::isfinite(dtau)) return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "dtau must be > 0");
+    if (!spot_host || !vol_host) return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "spot and vol must not be null");
+    if (!finite_all(spot_host, n_tenor) || !finite_all(vol_host, (size_t)n_tenor * n_factor) ||
+        (drift_host && !finite_all(drift_host, n_tenor)))
+        return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "market inputs must be finite");
+    ctx->nt = n_tenor;
+    ctx->dtau = dtau;
+    ctx->spot.assign(spot_host, spot_host + n_tenor);
+    ctx->vol.assign(vol_host, vol_host + (size_t)n_tenor * n_factor);
+    if (drift_host)
+        ctx->drift.assign(drift_host, drift_host + n_tenor);
+    else
+        trapezoid_drift(ctx->vol, n_tenor, dtau, ctx->drift);
+    ctx->have_market = true;
+    ctx->have_poly = false;
+    if (ctx->have_product && (int)ctx->payA.size() != n_tenor) ctx->have_product = false;
+    return HJM_OK;
+}
+
+hjm_status hjm_set_market_poly(hjm_ctx* ctx, int32_t n_tenor, double dtau, const double* spot_host,
+                               const double* vol_coef_host)
+{
+    HJM_CHECK_CTX(ctx);
+    if (!vol_coef_host) return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "vol_coef must not be null");
+    if (!finite_all(vol_coef_host, HJM_N_VOL_COEF))
+        return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "volatility coefficients must be finite");
+    if (n_tenor < 2 || n_tenor > HJM_MAX_TENOR)
+        return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "n_tenor %d outside [2, %d]", n_tenor, HJM_MAX_TENOR);
+    std::vector<double> vol((size_t)HJM_N_FACTOR * n_tenor);
+    for (int k = 0; k < HJM_N_FACTOR; ++k)
+        for (int t = 0; t < n_tenor; ++t) {
+            const double T = dtau * t;
+            vol[(size_t)k * n_tenor + t] =
+                vol_coef_host[k * 3 + 0] + vol_coef_host[k * 3 + 1] * T + vol_coef_host[k * 3 + 2] * T * T;
+        }
+    hjm_status st = hjm_set_market(ctx, n_tenor, dtau, spot_host, vol.data(), HJM_N_FACTOR, nullptr);
+    if (st != HJM_OK) return st;
+    std::memcpy(ctx->coef, vol_coef_host, sizeof(ctx->coef));
+    ctx->have_poly = true;
+    return HJM_OK;
+}
+
+hjm_status hjm_set_swap(hjm_ctx* ctx, double notional, double fixed_rate, const double* accrual_host, int32_t payer)
+{
+    HJM_CHECK_CTX(ctx);
+    if (!ctx->have_market) return fail(ctx, HJM_ERR_NOT_CONFIGURED, "hjm_set_market must come first");
+    if (!accrual_host) return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "accrual must not be null");
+    if (!std::isfinite(notional) || !std::isfinite(fixed_rate) || !finite_all(accrual_host, ctx->nt))
+        return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "swap inputs must be finite");
+    const double sign = payer ? 1.0 : -1.0;
+    ctx->payA.assign(ctx->nt, 0.0);
+    ctx->payB.assign(ctx->nt, 0.0);
+    for (int i = 0; i < ctx->nt; ++i) {
+        ctx->payA[i] = sign * notional * accrual_host[i];
+        ctx->payB[i] = sign * notional * accrual_host[i] * fixed_rate;
+    }
+    ctx->have_product = true;
+    return HJM_OK;
+}
+
+hjm_status hjm_set_netting_set(hjm_ctx* ctx, int32_t n_swaps, const double* notional_host,
+                               const double* fixed_rate_host, const int32_t* n_periods_host,
+                               const int32_t* payer_host)
+{
+    HJM_CHECK_CTX(ctx);
+    if (!ctx->have_market) return fail(ctx, HJM_ERR_NOT_CONFIGURED, "hjm_set_market must come first");
+    if (n_swaps <= 0 || !notional_host || !fixed_rate_host || !n_periods_host || !payer_host)
+        return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "netting set needs n_swaps > 0 and four non-null arrays");
+    ctx->payA.assign(ctx->nt, 0.0);
+    ctx->payB.assign(ctx->nt, 0.0);
+    for (int s = 0; s < n_swaps; ++s) {
+        const int np = n_periods_host[s];
+        if (np < 1 || np > ctx->nt - 1)
+            return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "swap %d: n_periods %d outside [1, %d]", s, np, ctx->nt - 1);
+        if (!std::isfinite(notional_host[s]) || !std::isfinite(fixed_rate_host[s]))
+            return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "swap %d: non-finite notional or rate", s);
+        const double sign = payer_host[s] ? 1.0 : -1.0;
+        for (int i = 1; i <= np; ++i) {
+            ctx->payA[i] += sign * notional_host[s] * ctx->dtau;
+            ctx->payB[i] += sign * notional_host[s] * ctx->dtau * fixed_rate_host[s];
+        }
+    }
+    ctx->have_product = true;
+    return HJM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// valuation
+// ---------------------------------------------------------------------------
+struct RunShape {
+    int stride = 0, B = 0;
+};
+
+static hjm_status check_run(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, double dt, int32_t precision,
+                            double hazard, double recovery, double pfe_q, RunShape& sh)
+{
+    if (!ctx->have_market) return fail(ctx, HJM_ERR_NOT_CONFIGURED, "no market: call hjm_set_market");
+    if (!ctx->have_product) return fail(ctx, HJM_ERR_NOT_CONFIGURED, "no product: call hjm_set_swap");
+    if (n_paths <= 0 || n_paths > (int64_t)1 << 31)
+        return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "n_paths %lld outside [1, 2^31]", (long long)n_paths);
+    if (!(dt > 0.0) || !std::isfinite(dt)) return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "dt must be > 0");
+    if (precision != HJM_PRECISION_FP64 && precision != HJM_PRECISION_MIXED)
+        return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "unknown precision %d", precision);
+    if (!(hazard >= 0.0) || !std::isfinite(hazard) || !(recovery >= 0.0 && recovery <= 1.0))
+        return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "hazard must be >= 0 and recovery in [0, 1]");
+    if (!(pfe_q < 1.0) || std::isnan(pfe_q))
+        return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "pfe_quantile must be < 1 (<= 0 disables PFE)");
+    // stride = dtau / dt; the reference truncates (int)(dtau/dt) (simulation_gpu.cu:383);
+    // here it must be an integer up to rounding
+    const double r = ctx->dtau / dt;
+    const long st = std::lround(r);
+    if (st < 1 || std::fabs(r - (double)st) > 1e-9 * r)
+        return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "dtau/dt = %.17g is not an integer number of steps", r);
+    if (n_steps <= 0 || n_steps % st != 0)
+        return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "n_steps %d is not a positive multiple of the block length %ld",
+                    n_steps, st);
+    const int B = n_steps / (int)st;
+    if (B > ctx->nt - 1)
+        return fail(ctx, HJM_ERR_INVALID_ARGUMENT,
+                    "%d sampled dates need %d tenors; the grid has %d (n_steps * dt must not exceed the last tenor)",
+                    B, B + 1, ctx->nt);
+    const size_t smem = path_smem(ctx->nt, B, precision == HJM_PRECISION_MIXED);
+    if (smem > 227 * 1024) return fail(ctx, HJM_ERR_UNSUPPORTED, "shared memory %zu B exceeds 227 KB", smem);
+    sh.stride = (int)st;
+    sh.B = B;
+    return HJM_OK;
+}
+
+// Deterministic curve p (no noise) in FP64: p_n = spot for the first block,
+// then p_{n+1}[t] = p_n[t] + (mu[t] dt + (dF/dtau) dt) (simulation_cpu.h:37-54
+// with zero normals); its samples and discount integrals per tenor.
+static void deterministic_curve(const hjm_ctx* ctx, int stride, int B, double dt, double* psamp, double* psum)
+{
+    const int nt = ctx->nt;
+    std::vector<double> p(ctx->spot), pn(nt), acc(nt, 0.0);
+    for (int i = 0; i < kMaxTenor; ++i) psamp[i] = psum[i] = 0.0;
+    for (int s = 0; s < stride; ++s)
+        for (int t = 0; t < nt; ++t) acc[t] += p[t];
+    psamp[1] = p[1];
+    psum[1] = acc[1];
+    for (int b = 1; b < B; ++b) {
+        for (int s = 0; s < stride; ++s) {
+            for (int t = 0; t < nt; ++t) {
+                const double dF = (t == nt - 1) ? p[t] - p[t - 1] : p[t + 1] - p[t];
+                double dfbar = ctx->drift[t] * dt;
+                dfbar += (dF / ctx->dtau) * dt;
+                pn[t] = p[t] + dfbar;
+            }
+            for (int t = 0; t < nt; ++t) {
+                p[t] = pn[t];
+                acc[t] += p[t];
+            }
+        }
+        psamp[b + 1] = p[b + 1];
+        psum[b + 1] = acc[b + 1];
+    }
+}
+
+template <typename T>
+static void fill_params(const hjm_ctx* ctx, const RunShape& sh, int64_t n_paths, double dt, uint64_t seed,
+                        uint64_t path_offset, double hazard, double recovery, int64_t ld, bool store,
+                        PathParams<T>& P, FinalParams& F)
+{
+    std::memset(&P, 0, sizeof(P));
+    std::memset(&F, 0, sizeof(F));
+    const int nt = ctx->nt;
+    const double sq = std::sqrt(dt);
+    for (int k = 0; k < kFactors; ++k)
+        for (int t = 0; t < nt; ++t) P.sv[k][t] = (T)(sq * ctx->vol[(size_t)k * nt + t]);
+    deterministic_curve(ctx, sh.stride, sh.B, dt, P.psamp, P.psum);
+    for (int i = 0; i < nt; ++i) {
+        P.payA[i] = ctx->payA[i];
+        P.payB[i] = ctx->payB[i];
+    }
+    for (int j = 1; j <= sh.B; ++j) {
+        const double t0 = (j - 1) * ctx->dtau, t1 = j * ctx->dtau;
+        const double e0 = std::exp(-hazard * t0), e1 = std::exp(-hazard * t1);
+        P.cvaw[j] = (1.0 - recovery) * (e0 - e1);
+        F.cvaw[j] = P.cvaw[j];
+        F.dcvaw[j] = (1.0 - recovery) * (-t0 * e0 + t1 * e1);
+    }
+    P.c = (T)(dt / ctx->dtau);
+    P.dt = dt;
+    P.m = 1.0 / ctx->dtau;
+    P.key0 = (uint32_t)seed;
+    P.key1 = (uint32_t)(seed >> 32);
+    P.path_offset = path_offset;
+    P.n_paths = n_paths;
+    P.ld = ld;
+    P.n_blocks = sh.B;
+    P.stride = sh.stride;
+    P.store_exposures = store ? 1 : 0;
+    F.n_paths = n_paths;
+    F.n_blocks = sh.B;
+}
+
+static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, double dt, uint64_t seed,
+                               uint64_t path_offset, int32_t precision, double hazard, double recovery, double pfe_q,
+                               const double* ext_dev)
+{
+    RunShape sh;
+    hjm_status st = check_run(ctx, n_paths, n_steps, dt, precision, hazard, recovery, pfe_q, sh);
+    if (st != HJM_OK) return st;
+    HJM_CUDA(ctx, cudaSetDevice(ctx->device));
+    const bool mixed = precision == HJM_PRECISION_MIXED;
+    const bool want_pfe = pfe_q > 0.0;
+    const bool store = want_pfe || ctx->keep_exposures;
+    const int n_dates = sh.B + 1;
+    const int R = sh.B + 3;
+    const int64_t n_ctas = (n_paths + kCta - 1) / kCta;
+    const int64_t ld = (n_paths + 3) / 4 * 4;
+    const size_t esize = mixed ? 4 : 8;
+
+    HJM_CUDA(ctx, ctx->partials.ensure(sizeof(double) * (size_t)n_ctas * R));
+    HJM_CUDA(ctx, ctx->sums.ensure(sizeof(double) * kMaxTenor * 2));
+    HJM_CUDA(ctx, ctx->result.ensure(sizeof(double) * kResLen));
+    if (store) HJM_CUDA(ctx, ctx->estore.ensure(esize * (size_t)n_dates * (size_t)ld));
+    if (want_pfe) {
+        HJM_CUDA(ctx, ctx->sel.ensure(sizeof(SelState) * kMaxTenor));
+        HJM_CUDA(ctx, ctx->hist.ensure(sizeof(uint32_t) * 256 * kMaxTenor));
+    }
+    cudaStream_t s = ctx->stream;
+    ctx->have_result = false;
+    HJM_CUDA(ctx, cudaMemsetAsync(ctx->result.p, 0, sizeof(double) * kResLen, s));
+
+    FinalParams F;
+    ctx->ev = ctx->ring[ctx->n_enqueued % hjm_ctx::kRing];
+    ctx->n_enqueued++;
+    ctx->stat_launches = 3;  // path kernel, column reduction, finalisation
+    ctx->stat_h2d = (mixed ? sizeof(PathParams<float>) : sizeof(PathParams<double>)) + sizeof(FinalParams);
+    ctx->stat_d2h = 0;
+    HJM_CUDA(ctx, cudaEventRecord(ctx->ev[0], s));
+    if (mixed) {
+        PathParams<float> P;
+        fill_params<float>(ctx, sh, n_paths, dt, seed, path_offset, hazard, recovery, ld, store, P, F);
+        HJM_CUDA(ctx, launch_path_mixed(ctx->nt, P, ext_dev, (double*)ctx->partials.p,
+                                        store ? (float*)ctx->estore.p : nullptr, s));
+    } else {
+        PathParams<double> P;
+        fill_params<double>(ctx, sh, n_paths, dt, seed, path_offset, hazard, recovery, ld, store, P, F);
+        HJM_CUDA(ctx, launch_path_fp64(ctx->nt, P, ext_dev, (double*)ctx->partials.p,
+                                       store ? (double*)ctx->estore.p : nullptr, s));
+    }
+    HJM_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
+    HJM_CUDA(ctx, launch_reduce((const double*)ctx->partials.p, n_ctas, R, (double*)ctx->sums.p, F,
+                                (double*)ctx->result.p, s));
+    HJM_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
+    if (want_pfe) {
+        const int64_t k = std::min<int64_t>(std::max<int64_t>((int64_t)std::ceil(pfe_q * (double)n_paths - 1e-7), 1),
+                                            n_paths);
+        HJM_CUDA(ctx, launch_pfe(ctx->estore.p, !mixed, ld, n_paths, n_dates, (uint64_t)(k - 1),
+                                 (SelState*)ctx->sel.p, (uint32_t*)ctx->hist.p, (double*)ctx->result.p, ctx->n_sms,
+                                 s));
+        ctx->stat_launches += 2 + 2 * (mixed ? 4 : 8);  // init, 8-bit digit passes (histogram + scan), write
+    }
+    HJM_CUDA(ctx, cudaEventRecord(ctx->ev[3], s));
+    ctx->last_n_paths = n_paths;
+    ctx->last_n_dates = n_dates;
+    ctx->last_mixed = mixed;
+    ctx->last_stored = store;
+    ctx->last_pfe = want_pfe;
+    ctx->last_ld = ld;
+    ctx->have_result = true;
+    return HJM_OK;
+}
+
+hjm_status hjm_enqueue(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, double dt, uint64_t seed,
+                       uint64_t path_offset, int32_t precision, double hazard_rate, double recovery,
+                       double pfe_quantile)
+{
+    HJM_CHECK_CTX(ctx);
+    return enqueue_impl(ctx, n_paths, n_steps, dt, seed, path_offset, precision, hazard_rate, recovery, pfe_quantile,
+                        nullptr);
+}
+
+hjm_status hjm_fetch_results(hjm_ctx* ctx, double* ee_out, double* pfe_out, double* cva_out)
+{
+    HJM_CHECK_CTX(ctx);
+    if (!ctx->have_result) return fail(ctx, HJM_ERR_NOT_CONFIGURED, "no valuation has been enqueued");
+    double res[kResLen];
+    HJM_CUDA(ctx, cudaSetDevice(ctx->device));
+    HJM_CUDA(ctx, cudaMemcpyAsync(res, ctx->result.p, sizeof(res), cudaMemcpyDeviceToHost, ctx->stream));
+    HJM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->stat_d2h += (int64_t)sizeof(res);
+    if (ee_out)
+        for (int j = 0; j < ctx->nt; ++j) ee_out[j] = res[kResEE + j];
+    if (pfe_out)
+        for (int j = 0; j < ctx->nt; ++j) pfe_out[j] = ctx->last_pfe ? res[kResPFE + j] : 0.0;
+    if (cva_out) {
+        cva_out[HJM_CVA_VALUE] = res[kResCVA];
+        cva_out[HJM_CVA_STDERR] = res[kResCVAStderr];
+        cva_out[HJM_CVA_DHAZARD] = res[kResDCVADHazard];
+    }
+    return HJM_OK;
+}
+
+hjm_status hjm_run(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, double dt, uint64_t seed, uint64_t path_offset,
+                   int32_t precision, double hazard_rate, double recovery, double pfe_quantile, double* ee_out,
+                   double* pfe_out, double* cva_out)
+{
+    HJM_CHECK_CTX(ctx);
+    if (!ee_out && !pfe_out && !cva_out) return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "no output requested");
+    const double q = pfe_out ? pfe_quantile : 0.0;
+    hjm_status st = enqueue_impl(ctx, n_paths, n_steps, dt, seed, path_offset, precision, hazard_rate, recovery, q,
+                                 nullptr);
+    if (st != HJM_OK) return st;
+    return hjm_fetch_results(ctx, ee_out, pfe_out, cva_out);
+}
+
+hjm_status hjm_run_with_normals(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, double dt, const double* normals_host,
+                                int32_t precision, double hazard_rate, double recovery, double pfe_quantile,
+                                double* ee_out, double* pfe_out, double* cva_out)
+{
+    HJM_CHECK_CTX(ctx);
+    if (!normals_host) return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "normals must not be null");
+    if (n_paths <= 0 || n_steps <= 0) return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "n_paths and n_steps must be > 0");
+    const size_t count = (size_t)n_paths * (size_t)n_steps * 3;
+    if (count > ((size_t)1 << 33)) return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "normals buffer too large");
+    HJM_CUDA(ctx, cudaSetDevice(ctx->device));
+    HJM_CUDA(ctx, ctx->ext_raw.ensure(sizeof(double) * count));
+    HJM_CUDA(ctx, ctx->ext.ensure(sizeof(double) * count));
+    HJM_CUDA(ctx, cudaMemcpyAsync(ctx->ext_raw.p, normals_host, sizeof(double) * count, cudaMemcpyHostToDevice,
+                                  ctx->stream));
+    HJM_CUDA(ctx, launch_transpose_normals((const double*)ctx->ext_raw.p, n_paths, n_steps, (double*)ctx->ext.p,
+                                           ctx->stream));
+    const double q = pfe_out ? pfe_quantile : 0.0;
+    hjm_status st = enqueue_impl(ctx, n_paths, n_steps, dt, 0, 0, precision, hazard_rate, recovery, q,
+                                 (const double*)ctx->ext.p);
+    if (st != HJM_OK) return st;
+    ctx->stat_launches += 1;
+    ctx->stat_h2d += (int64_t)(sizeof(double) * count);
+    return hjm_fetch_results(ctx, ee_out, pfe_out, cva_out);
+}
+
+hjm_status hjm_get_exposures(hjm_ctx* ctx, double* out_host, int64_t capacity)
+{
+    HJM_CHECK_CTX(ctx);
+    if (!ctx->have_result || !ctx->last_stored)
+        return fail(ctx, HJM_ERR_NOT_CONFIGURED,
+                    "no stored exposures: run with a PFE quantile or after hjm_ctx_keep_exposures(ctx, 1)");
+    const int64_t need = ctx->last_n_paths * (int64_t)ctx->last_n_dates;
+    if (!out_host || capacity < need)
+        return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "exposure buffer holds %lld values, %lld needed",
+                    (long long)capacity, (long long)need);
+    HJM_CUDA(ctx, cudaSetDevice(ctx->device));
+    HJM_CUDA(ctx, ctx->wide.ensure(sizeof(double) * (size_t)need));
+    HJM_CUDA(ctx, launch_widen_exposures(ctx->estore.p, !ctx->last_mixed, ctx->last_ld, ctx->last_n_paths,
+                                         ctx->last_n_dates, (double*)ctx->wide.p, ctx->stream));
+    HJM_CUDA(ctx, cudaMemcpyAsync(out_host, ctx->wide.p, sizeof(double) * (size_t)need, cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    HJM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return HJM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// diagnostics
+// ---------------------------------------------------------------------------
+hjm_status hjm_dump_normals(hjm_ctx* ctx, int64_t n_paths, uint64_t path_offset, int32_t n_steps, uint64_t seed,
+                            double* out_host)
+{
+    HJM_CHECK_CTX(ctx);
+    if (n_paths <= 0 || n_steps <= 0 || !out_host)
+        return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "n_paths, n_steps must be > 0 and out non-null");
+    const size_t count = (size_t)n_paths * (size_t)n_steps * 3;
+    if (count > ((size_t)1 << 33)) return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "normals buffer too large");
+    HJM_CUDA(ctx, cudaSetDevice(ctx->device));
+    HJM_CUDA(ctx, ctx->scratch.ensure(sizeof(double) * count));
+    HJM_CUDA(ctx, launch_dump_normals(n_paths, path_offset, n_steps, (uint32_t)seed, (uint32_t)(seed >> 32),
+                                      (double*)ctx->scratch.p, ctx->stream));
+    HJM_CUDA(ctx, cudaMemcpyAsync(out_host, ctx->scratch.p, sizeof(double) * count, cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    HJM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return HJM_OK;
+}
+
+hjm_status hjm_philox_words(hjm_ctx* ctx, int64_t n_paths, uint64_t path_offset, uint32_t step, uint64_t seed,
+                            uint32_t* out_host)
+{
+    HJM_CHECK_CTX(ctx);
+    if (n_paths <= 0 || n_paths > ((int64_t)1 << 28) || !out_host)
+        return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "n_paths must be in [1, 2^28] and out non-null");
+    HJM_CUDA(ctx, cudaSetDevice(ctx->device));
+    HJM_CUDA(ctx, ctx->scratch.ensure(sizeof(uint32_t) * 4 * (size_t)n_paths));
+    HJM_CUDA(ctx, launch_philox_words(n_paths, path_offset, step, (uint32_t)seed, (uint32_t)(seed >> 32),
+                                      (uint32_t*)ctx->scratch.p, ctx->stream));
+    HJM_CUDA(ctx, cudaMemcpyAsync(out_host, ctx->scratch.p, sizeof(uint32_t) * 4 * (size_t)n_paths,
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+    HJM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return HJM_OK;
+}
+
+hjm_status hjm_last_timings(hjm_ctx* ctx, double* ms_out)
+{
+    HJM_CHECK_CTX(ctx);
+    if (!ms_out) return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "ms_out must not be null");
+    if (!ctx->have_result) return fail(ctx, HJM_ERR_NOT_CONFIGURED, "no valuation has been enqueued");
+    HJM_CUDA(ctx, cudaEventSynchronize(ctx->ev[3]));
+    float a = 0, b = 0, c = 0, d = 0;
+    HJM_CUDA(ctx, cudaEventElapsedTime(&a, ctx->ev[0], ctx->ev[1]));
+    HJM_CUDA(ctx, cudaEventElapsedTime(&b, ctx->ev[1], ctx->ev[2]));
+    HJM_CUDA(ctx, cudaEventElapsedTime(&c, ctx->ev[2], ctx->ev[3]));
+    HJM_CUDA(ctx, cudaEventElapsedTime(&d, ctx->ev[0], ctx->ev[3]));
+    ms_out[0] = a;
+    ms_out[1] = b;
+    ms_out[2] = c;
+    ms_out[3] = d;
+    return HJM_OK;
+}
+
+hjm_status hjm_timing_history(hjm_ctx* ctx, int32_t n, double* ms_out)
+{
+    HJM_CHECK_CTX(ctx);
+    if (!ms_out || n <= 0) return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "need n > 0 and ms_out non-null");
+    if (n > hjm_ctx::kRing || n > ctx->n_enqueued)
+        return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "history holds min(%d, %lld) valuations, %d requested",
+                    hjm_ctx::kRing, (long long)ctx->n_enqueued, n);
+    HJM_CUDA(ctx, cudaSetDevice(ctx->device));
+    for (int i = 0; i < n; ++i) {
+        const int64_t idx = ctx->n_enqueued - n + i;
+        cudaEvent_t* q = ctx->ring[idx % hjm_ctx::kRing];
+        HJM_CUDA(ctx, cudaEventSynchronize(q[3]));
+        float a = 0, b = 0, c = 0, d = 0;
+        HJM_CUDA(ctx, cudaEventElapsedTime(&a, q[0], q[1]));
+        HJM_CUDA(ctx, cudaEventElapsedTime(&b, q[1], q[2]));
+        HJM_CUDA(ctx, cudaEventElapsedTime(&c, q[2], q[3]));
+        HJM_CUDA(ctx, cudaEventElapsedTime(&d, q[0], q[3]));
+        ms_out[4 * i + 0] = a;
+        ms_out[4 * i + 1] = b;
+        ms_out[4 * i + 2] = c;
+        ms_out[4 * i + 3] = d;
+    }
+    return HJM_OK;
+}
+
+hjm_status hjm_last_stats(hjm_ctx* ctx, int64_t* stats_out)
+{
+    HJM_CHECK_CTX(ctx);
+    if (!stats_out) return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "stats_out must not be null");
+    stats_out[0] = ctx->stat_launches;
+    stats_out[1] = ctx->stat_h2d;
+    stats_out[2] = ctx->stat_d2h;
+    return HJM_OK;
+}
+
+hjm_status hjm_measure_fma_peak(hjm_ctx* ctx, int32_t precision, double* tflops_out)
+{
+    HJM_CHECK_CTX(ctx);
+    if (!tflops_out) return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "tflops_out must not be null");
+    HJM_CUDA(ctx, cudaSetDevice(ctx->device));
+    HJM_CUDA(ctx, measure_fma_peak(precision == HJM_PRECISION_FP64, ctx->stream, ctx->n_sms, tflops_out));
+    return HJM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// adjoint
+// ---------------------------------------------------------------------------
+hjm_status hjm_run_adjoint(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, double dt, uint64_t seed,
+                           uint64_t path_offset, double hazard_rate, double recovery, int32_t checkpoint_every,
+                           double* cva_out, double* dcva_dspot_out, double* dcva_ddrift_out,
+                           double* dcva_dvolcoef_out)
+{
+    HJM_CHECK_CTX(ctx);
+    (void)n_paths; (void)n_steps; (void)dt; (void)seed; (void)path_offset; (void)hazard_rate; (void)recovery;
+    (void)checkpoint_every; (void)cva_out; (void)dcva_dspot_out; (void)dcva_ddrift_out; (void)dcva_dvolcoef_out;
+    return fail(ctx, HJM_ERR_UNSUPPORTED, "adjoint not built yet");
+}
+

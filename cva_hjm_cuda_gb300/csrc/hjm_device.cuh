@@ -1,0 +1,111 @@
+// hjm_device.cuh -- shared device definitions of the GB300 HJM exposure engine.
+//
+// Counter-based normals (Philox4x32-10 + Box-Muller, generated in registers,
+// replacing the pre-generated cuRAND buffer of simulation_gpu.cu:195-216 and
+// :1057-1071), the kernel parameter block, and small warp helpers.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace hjm {
+
+constexpr int kMaxTenor = 64;   // tenor-grid capacity of every parameter array
+constexpr int kFactors = 3;     // PCA factors (VOL_DIM, simulation_gpu.cu:34)
+constexpr int kCta = 128;       // threads per CTA of the path kernel: one path per thread
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), published multipliers and
+// Weyl increments.  Host and device compile the same function.
+// ---------------------------------------------------------------------------
+__host__ __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0, uint32_t k1)
+{
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+#ifdef __CUDA_ARCH__
+        const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
+        const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
+#else
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c.x, p1 = (uint64_t)0xCD9E8D57u * c.z;
+        const uint32_t lo0 = (uint32_t)p0, hi0 = (uint32_t)(p0 >> 32);
+        const uint32_t lo1 = (uint32_t)p1, hi1 = (uint32_t)(p1 >> 32);
+#endif
+        c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return c;
+}
+
+// Counter of the normals of (path, step): (step, stream 0, path lo, path hi).
+__host__ __device__ __forceinline__ uint4 normals_counter(uint64_t path, uint32_t step)
+{
+    return make_uint4(step, 0u, (uint32_t)path, (uint32_t)(path >> 32));
+}
+
+#ifdef __CUDACC__
+// Three N(0,1) draws for one path-step: Box-Muller on the two uniform pairs
+// a = (word >> 8) * 2^-24 in [0, 1) (exact in FP32); radius from log(1 - a),
+// angle pi * (2a - 1).  FP32 with the SFU intrinsics: the normals are inputs
+// of both precision modes (the FP64 mode promotes them exactly), and the
+// oracle consumes these very values through hjm_dump_normals.
+__device__ __forceinline__ void normals3(uint4 w, float& z0, float& z1, float& z2)
+{
+    const float a0 = (float)(w.x >> 8) * 0x1p-24f;
+    const float a1 = (float)(w.y >> 8) * 0x1p-24f;
+    const float a2 = (float)(w.z >> 8) * 0x1p-24f;
+    const float a3 = (float)(w.w >> 8) * 0x1p-24f;
+    const float pi = 3.14159265358979323846f;
+    const float r0 = sqrtf(-2.0f * __logf(1.0f - a0));
+    const float r1 = sqrtf(-2.0f * __logf(1.0f - a2));
+    float s0, c0;
+    __sincosf(pi * (2.0f * a1 - 1.0f), &s0, &c0);
+    const float c1 = __cosf(pi * (2.0f * a3 - 1.0f));
+    z0 = r0 * c0;
+    z1 = r0 * s0;
+    z2 = r1 * c1;
+}
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+#endif
+
+// ---------------------------------------------------------------------------
+// Kernel parameter block, passed by value (constant bank): every per-tenor
+// coefficient is read as an FMA operand straight from the constant bank with a
+// compile-time offset once the tenor loop is unrolled.  Replaces the
+// __constant__ symbols of simulation_gpu.cu:109-119 and keeps launches
+// re-entrant.
+//
+// Curve split.  f_n = p_n + h_n, where p_n is the deterministic curve
+// (p_n = spot for the first block, then p_{n+1} = A p_n + mu dt) computed on
+// the host in FP64, and h_n the stochastic part,
+//   h_{n+1}[t] = h_n[t] + sum_k sv[k][t] phi_{n+1,k} + c (h_n[t+1] - h_n[t]),
+// with the backward difference at the last tenor (simulation_cpu.h:96-108)
+// and c = dt/dtau.  Linear, so the split is exact in exact arithmetic.
+// ---------------------------------------------------------------------------
+template <typename T>
+struct PathParams {
+    T sv[kFactors][kMaxTenor];   // sqrt(dt) * sigma_k(tau_t)
+    double psamp[kMaxTenor];     // p at the sampling of tenor i: p_{stride*i-1}[i]
+    double psum[kMaxTenor];      // sum_{n < stride*i} p_n[i]
+    double payA[kMaxTenor];      // cash flow of date i: D_i * (payA[i] * L_i - payB[i])
+    double payB[kMaxTenor];
+    double cvaw[kMaxTenor];      // (1-R)(exp(-l t_{j-1}) - exp(-l t_j)); cvaw[0] = 0
+    T c;                         // dt / dtau
+    double dt;
+    double m;                    // 1 / dtau: LIBOR from the sampled forward, m (e^{f/m} - 1)
+    uint32_t key0, key1;         // Philox key = seed
+    uint64_t path_offset;        // global index of this launch's first path
+    int64_t n_paths;
+    int64_t ld;                  // row stride (elements) of the exposure store
+    int n_blocks;                // sampled dates B = n_steps / stride
+    int stride;                  // Euler steps per block (dtau / dt)
+    int store_exposures;         // write per-path exposures [date][path]
+};
+
+}  // namespace hjm

@@ -1,0 +1,556 @@
+// hjm_forward.cu -- fused Monte Carlo path kernel, reductions and PFE selection.
+//
+// One launch of path_kernel replaces the reference's whole GPU pipeline
+// (simulation_gpu.cu:956-1179): cuRAND normal buffer (:1057-1071), 2,500
+// single-step launches each followed by cudaDeviceSynchronize (:724-796, or
+// the 50-step kernel4 variant :471-669), the exposure kernel (:803-882) and
+// the cuBLAS gemv column sum (:889-933).  One thread owns one Monte Carlo
+// path for its whole life: the curve sits in registers, normals come from
+// Philox in registers, the numeraire of each 0.5y block end is priced on the
+// spot, and the per-path exposure profile is reduced inside the CTA.
+//
+// Semantics follow the reference CPU path (simulation_cpu.h:188-296), which
+// the reference's shared-memory GPU kernel also reproduces (xls RMSE 0.0):
+//   * block 0 (steps 0..stride-1) holds the curve at spot (simulation_cpu.h:212);
+//   * after block b the numeraire of tenor i = b+1 is sampled: forward f[i] and
+//     discount exp(-dt * sum of f[i] over all steps so far) (simulation_cpu.h:248-250);
+//   * cash flow of date i: D_i * N * alpha_i * (L_i - K), L = m (e^{f/m} - 1);
+//     exposure E_j = max(sum_{i>j} cf_i, 0) (simulation_cpu.h:279-295).
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "hjm_device.cuh"
+#include "hjm_kernels.h"
+
+namespace hjm {
+
+// Static selection of a register-array element by a runtime index (uniform
+// across the warp): keeps the arrays in registers.
+template <int NT, typename T>
+__device__ __forceinline__ T select_reg(const T (&a)[NT], int i)
+{
+    T r = a[0];
+#pragma unroll
+    for (int t = 1; t < NT; ++t) r = (t == i) ? a[t] : r;
+    return r;
+}
+
+template <typename T>
+struct Prec;
+template <>
+struct Prec<double> {
+    static constexpr bool kMixed = false;
+};
+template <>
+struct Prec<float> {
+    static constexpr bool kMixed = true;
+};
+
+// Shared-memory layout of path_kernel (dynamic), per CTA of kCta threads,
+// column tid private to its thread until the epilogue:
+//   cf_s   [B+1][kCta] T       cash flows of the sampled dates
+//   acc_s  [B+1][kCta] double  FP64 discount accumulators       (mixed only)
+//   work_s [max(NT, B+1)][kCta] T   block partial staging (mixed), then exposures
+//   red_s  [2 * kCta/32] double CVA statistics
+__host__ __device__ inline size_t path_smem_bytes(int nt, int n_blocks, bool mixed)
+{
+    const size_t te = mixed ? 4 : 8;
+    const size_t rows = (size_t)n_blocks + 1;
+    size_t b = rows * kCta * te;                       // cf_s
+    if (mixed) b += rows * kCta * 8;                   // acc_s
+    const size_t wrows = (mixed && (size_t)nt > rows) ? (size_t)nt : rows;
+    b = (b + 127) & ~(size_t)127;
+    b += wrows * kCta * te;                            // work_s
+    b += 2 * (kCta / 32) * 8;                          // red_s
+    return b;
+}
+
+template <int NT, typename T, bool EXT>
+__global__ void __launch_bounds__(kCta, Prec<T>::kMixed ? 3 : 1)
+    path_kernel(const __grid_constant__ PathParams<T> P, const double* __restrict__ ext,
+                double* __restrict__ partials, T* __restrict__ estore)
+{
+    constexpr bool kMixed = Prec<T>::kMixed;
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int tid = threadIdx.x;
+    const int B = P.n_blocks;
+    const int rows = B + 1;
+    T* cf_s = reinterpret_cast<T*>(smem);
+    double* acc_s = reinterpret_cast<double*>(smem + (size_t)rows * kCta * sizeof(T));
+    size_t off = (size_t)rows * kCta * sizeof(T) + (kMixed ? (size_t)rows * kCta * 8 : 0);
+    off = (off + 127) & ~(size_t)127;
+    T* work_s = reinterpret_cast<T*>(smem + off);
+    const int wrows = (kMixed && NT > rows) ? NT : rows;
+    double* red_s = reinterpret_cast<double*>(smem + off + (size_t)wrows * kCta * sizeof(T));
+
+    const int64_t cta_base = (int64_t)blockIdx.x * kCta;
+    const int64_t lp = cta_base + tid;            // path index within this launch
+    const bool active = lp < P.n_paths;
+    const uint64_t gpath = P.path_offset + (uint64_t)lp;
+
+    // stochastic part of the curve; zero through block 0 (spot hold)
+    T h[NT];
+#pragma unroll
+    for (int t = 0; t < NT; ++t) h[t] = T(0);
+
+    // discount accumulators of the stochastic part:
+    //   FP64: acc[t] directly; mixed: FP32 block partials pb[t] folded into acc_s
+    double acc[kMixed ? 1 : NT];
+    T pb[kMixed ? NT : 1];
+#pragma unroll
+    for (int t = 0; t < (kMixed ? 1 : NT); ++t) acc[t] = 0.0;
+#pragma unroll
+    for (int t = 0; t < (kMixed ? NT : 1); ++t) pb[t] = T(0);
+    if (kMixed)
+        for (int i = 0; i < rows; ++i) acc_s[i * kCta + tid] = 0.0;
+
+    // price date i from the sampled numeraire (x_i, D_i)
+    auto sample = [&](int i) {
+        const T hi = select_reg<NT, T>(h, i);
+        double a_h;
+        if constexpr (kMixed) {
+            a_h = acc_s[i * kCta + tid];
+        } else {
+            a_h = select_reg<NT, double>(acc, i);
+        }
+        const double x = P.psamp[i] + (double)hi;
+        const double a = P.psum[i] + a_h;
+        T cf;
+        if constexpr (kMixed) {
+            const float D = expf((float)(-a * P.dt));
+            const float mm = (float)P.m;
+            const float L = mm * expm1f((float)x / mm);
+            cf = D * ((float)P.payA[i] * L - (float)P.payB[i]);
+        } else {
+            const double D = exp(-a * P.dt);
+            const double L = P.m * (exp(x / P.m) - 1.0);
+            cf = D * (P.payA[i] * L - P.payB[i]);
+        }
+        cf_s[i * kCta + tid] = cf;
+    };
+
+    sample(1);
+    const T c = P.c;
+    for (int b = 1; b < B; ++b) {
+        for (int s = 0; s < P.stride; ++s) {
+            const int n = b * P.stride + s;
+            T phi0, phi1, phi2;
+            if constexpr (EXT) {
+                const size_t np = (size_t)P.n_paths;
+                const size_t base = (size_t)n * 3 * np + (size_t)(active ? lp : 0);
+                phi0 = (T)__ldg(ext + base);
+                phi1 = (T)__ldg(ext + base + np);
+                phi2 = (T)__ldg(ext + base + 2 * np);
+            } else {
+                const uint4 w = philox4x32_10(normals_counter(gpath, (uint32_t)n), P.key0, P.key1);
+                float z0, z1, z2;
+                normals3(w, z0, z1, z2);
+                phi0 = (T)z0;
+                phi1 = (T)z1;
+                phi2 = (T)z2;
+            }
+            // Musiela Euler step of the stochastic part (simulation_cpu.h:37-54
+            // with the drift moved into the deterministic part): 5 FMA-pipe
+            // operations per tenor, coefficients from the constant bank.
+            T hn[NT];
+#pragma unroll
+            for (int t = 0; t < NT; ++t) {
+                T x = fma(P.sv[0][t], phi0, h[t]);
+                x = fma(P.sv[1][t], phi1, x);
+                x = fma(P.sv[2][t], phi2, x);
+                const T d = (t < NT - 1) ? (h[t + 1] - h[t]) : (h[t] - h[t - 1]);
+                hn[t] = fma(c, d, x);
+            }
+#pragma unroll
+            for (int t = 0; t < NT; ++t) h[t] = hn[t];
+            if constexpr (kMixed) {
+#pragma unroll
+                for (int t = 1; t < NT; ++t) pb[t] += h[t];
+            } else {
+                // only tenors that are still to be sampled: (b, B]
+#pragma unroll
+                for (int t = 1; t < NT; ++t)
+                    if (t > b && t <= B) acc[t] += h[t];
+            }
+        }
+        if constexpr (kMixed) {
+            // fold the FP32 block partials of the tenors still to be sampled
+            // into the FP64 accumulators
+#pragma unroll
+            for (int t = 1; t < NT; ++t) {
+                work_s[t * kCta + tid] = pb[t];
+                pb[t] = T(0);
+            }
+            for (int t = b + 1; t <= B; ++t) acc_s[t * kCta + tid] += (double)work_s[t * kCta + tid];
+        }
+        sample(b + 1);
+    }
+
+    // exposure profile E_j = max(sum_{i>j} cf_i, 0), FP64 suffix sums, and the
+    // path's CVA contribution sum_j cvaw[j] E_j
+    T* e_s = work_s;
+    double v = 0.0, cva_c = 0.0;
+    e_s[B * kCta + tid] = T(0);
+    for (int j = B - 1; j >= 0; --j) {
+        v += (double)cf_s[(j + 1) * kCta + tid];
+        double e = (v > 0.0) ? v : 0.0;
+        if (!active) e = 0.0;
+        e_s[j * kCta + tid] = (T)e;
+        cva_c = fma(P.cvaw[j], e, cva_c);
+    }
+    __syncthreads();
+
+    // CTA partial sums: dates 0..B, then sum c and sum c^2
+    const int warp = tid >> 5, lane = tid & 31;
+    const int R = B + 3;
+    for (int j = warp; j <= B; j += kCta / 32) {
+        double s = 0.0;
+#pragma unroll
+        for (int q = 0; q < kCta / 32; ++q) s += (double)e_s[j * kCta + lane + 32 * q];
+        s = warp_sum(s);
+        if (lane == 0) partials[(size_t)blockIdx.x * R + j] = s;
+    }
+    {
+        const double s1 = warp_sum(cva_c), s2 = warp_sum(cva_c * cva_c);
+        if (lane == 0) {
+            red_s[warp] = s1;
+            red_s[kCta / 32 + warp] = s2;
+        }
+    }
+    if (P.store_exposures) {
+        // date rows of this CTA's paths, smem -> HBM with the bulk-copy (TMA) engine
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    if (tid == 0) {
+        double s1 = 0.0, s2 = 0.0;
+        for (int w = 0; w < kCta / 32; ++w) {
+            s1 += red_s[w];
+            s2 += red_s[kCta / 32 + w];
+        }
+        partials[(size_t)blockIdx.x * R + B + 1] = s1;
+        partials[(size_t)blockIdx.x * R + B + 2] = s2;
+        if (P.store_exposures) {
+            const int64_t cnt = (P.n_paths - cta_base < kCta) ? (P.n_paths - cta_base) : kCta;
+            constexpr int kVec = 16 / (int)sizeof(T);
+            const uint32_t bytes = (uint32_t)(((cnt + kVec - 1) / kVec) * kVec * sizeof(T));
+            for (int j = 0; j <= B; ++j) {
+                T* dst = estore + (size_t)j * (size_t)P.ld + (size_t)cta_base;
+                const uint32_t src = (uint32_t)__cvta_generic_to_shared(e_s + (size_t)j * kCta);
+                asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
+                             :: "l"(dst), "r"(src), "r"(bytes) : "memory");
+            }
+            asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+            asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Deterministic column sums of the CTA partials (Neumaier-compensated FP64):
+// one CTA per column, fixed assignment of rows to threads, fixed tree order.
+// Replaces the cuBLAS gemv with a ones vector (simulation_gpu.cu:889-933) and
+// the host vAdd/saxpy (simulation_gpu.cu:941-951, 1157-1179).
+// ---------------------------------------------------------------------------
+constexpr int kReduceThreads = 256;
+
+__device__ __forceinline__ void neumaier_add(double& s, double& comp, double x)
+{
+    const double t = s + x;
+    comp += (fabs(s) >= fabs(x)) ? ((s - t) + x) : ((x - t) + s);
+    s = t;
+}
+
+__global__ void __launch_bounds__(kReduceThreads)
+    reduce_columns(const double* __restrict__ partials, int64_t n_rows, int R, double* __restrict__ sums)
+{
+    __shared__ double ss[kReduceThreads], cs[kReduceThreads];
+    const int col = blockIdx.x;
+    double s = 0.0, comp = 0.0;
+    for (int64_t r = threadIdx.x; r < n_rows; r += kReduceThreads) neumaier_add(s, comp, partials[(size_t)r * R + col]);
+    ss[threadIdx.x] = s;
+    cs[threadIdx.x] = comp;
+    __syncthreads();
+    for (int w = kReduceThreads / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            double a = ss[threadIdx.x], ca = cs[threadIdx.x] + cs[threadIdx.x + w];
+            neumaier_add(a, ca, ss[threadIdx.x + w]);
+            ss[threadIdx.x] = a;
+            cs[threadIdx.x] = ca;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) sums[col] = ss[0] + cs[0];
+}
+
+// EE, CVA, its standard error and dCVA/dhazard from the column sums.
+__global__ void finalize_results(const double* __restrict__ sums, FinalParams F, double* __restrict__ result)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int B = F.n_blocks;
+    const double inv_n = 1.0 / (double)F.n_paths;
+    double cva = 0.0, dcva = 0.0;
+    for (int j = 0; j < kMaxTenor; ++j) {
+        const double ee = (j <= B) ? sums[j] * inv_n : 0.0;
+        result[kResEE + j] = ee;
+        cva += F.cvaw[j] * ee;
+        dcva += F.dcvaw[j] * ee;
+    }
+    const double s1 = sums[B + 1], s2 = sums[B + 2];
+    const double n = (double)F.n_paths;
+    const double var = (n > 1.0) ? fmax((s2 - s1 * s1 / n) / (n - 1.0), 0.0) : 0.0;
+    result[kResCVA] = cva;
+    result[kResCVAStderr] = sqrt(var / n);
+    result[kResDCVADHazard] = dcva;
+    result[kResCVAPathMean] = s1 * inv_n;
+}
+
+// ---------------------------------------------------------------------------
+// PFE: exact k-th smallest exposure of every date column by most-significant-
+// digit radix selection on the IEEE bit patterns (exposures are >= +0, so the
+// unsigned order of the bits is the numeric order).  8-bit digits; each pass
+// histograms the candidates that match the prefix found so far.
+// ---------------------------------------------------------------------------
+template <typename K>
+__global__ void pfe_hist(const K* __restrict__ keys, int64_t ld, int64_t n, const SelState* __restrict__ st,
+                         uint32_t* __restrict__ hist, int shift)
+{
+    __shared__ uint32_t h[256];
+    const int date = blockIdx.y;
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    const uint64_t prefix = st[date].prefix, mask = st[date].mask;
+    const K* col = keys + (size_t)date * (size_t)ld;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
+        const int64_t i = base + threadIdx.x;
+        bool take = false;
+        uint32_t digit = 0;
+        if (i < n) {
+            const uint64_t k = (uint64_t)col[i];
+            take = (k & mask) == prefix;
+            digit = (uint32_t)(k >> shift) & 0xFFu;
+        }
+        // warp-aggregated increments: one atomic per distinct digit per warp
+        const uint32_t active = __ballot_sync(0xffffffffu, take);
+        if (take) {
+            const uint32_t peers = __match_any_sync(active, digit);
+            if ((threadIdx.x & 31) == (__ffs(peers) - 1)) atomicAdd(&h[digit], (uint32_t)__popc(peers));
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 256; i += blockDim.x)
+        if (h[i]) atomicAdd(&hist[date * 256 + i], h[i]);
+}
+
+__global__ void pfe_scan(SelState* __restrict__ st, uint32_t* __restrict__ hist, int shift)
+{
+    const int date = blockIdx.x;
+    if (threadIdx.x == 0) {
+        uint64_t k = st[date].k;
+        uint32_t* hd = hist + date * 256;
+        int d = 0;
+        for (; d < 255; ++d) {
+            if (k < hd[d]) break;
+            k -= hd[d];
+        }
+        st[date].prefix |= (uint64_t)d << shift;
+        st[date].mask |= (uint64_t)0xFF << shift;
+        st[date].k = k;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) hist[date * 256 + i] = 0;
+}
+
+template <typename K>
+__global__ void pfe_write(const SelState* __restrict__ st, int n_dates, double* __restrict__ result)
+{
+    const int j = threadIdx.x;
+    if (j < kMaxTenor) {
+        double v = 0.0;
+        if (j < n_dates) {
+            if (sizeof(K) == 8) {
+                v = __longlong_as_double((long long)st[j].prefix);
+            } else {
+                v = (double)__uint_as_float((uint32_t)st[j].prefix);
+            }
+        }
+        result[kResPFE + j] = v;
+    }
+}
+
+__global__ void pfe_init(SelState* __restrict__ st, int n_dates, uint64_t k0)
+{
+    const int j = threadIdx.x;
+    if (j < n_dates) {
+        st[j].prefix = 0;
+        st[j].mask = 0;
+        st[j].k = k0;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Diagnostics: the device's normals and raw Philox words; layout transposes.
+// ---------------------------------------------------------------------------
+__global__ void dump_normals_kernel(int64_t n_paths, uint64_t path_offset, int n_steps, uint32_t k0, uint32_t k1,
+                                    double* __restrict__ out)
+{
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= n_paths * (int64_t)n_steps) return;
+    const int64_t p = idx / n_steps;
+    const int n = (int)(idx % n_steps);
+    const uint4 w = philox4x32_10(normals_counter(path_offset + (uint64_t)p, (uint32_t)n), k0, k1);
+    float z0, z1, z2;
+    normals3(w, z0, z1, z2);
+    out[idx * 3 + 0] = (double)z0;
+    out[idx * 3 + 1] = (double)z1;
+    out[idx * 3 + 2] = (double)z2;
+}
+
+__global__ void philox_words_kernel(int64_t n_paths, uint64_t path_offset, uint32_t step, uint32_t k0, uint32_t k1,
+                                    uint32_t* __restrict__ out)
+{
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n_paths) return;
+    const uint4 w = philox4x32_10(normals_counter(path_offset + (uint64_t)p, step), k0, k1);
+    out[p * 4 + 0] = w.x;
+    out[p * 4 + 1] = w.y;
+    out[p * 4 + 2] = w.z;
+    out[p * 4 + 3] = w.w;
+}
+
+// [path][step][3] -> [step][3][path] so that the path kernel reads coalesced
+__global__ void transpose_normals_kernel(const double* __restrict__ in, int64_t n_paths, int n_steps,
+                                         double* __restrict__ out)
+{
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t total = n_paths * (int64_t)n_steps * 3;
+    if (idx >= total) return;
+    const int64_t p = idx % n_paths;
+    const int64_t rest = idx / n_paths;  // = n * 3 + k
+    out[idx] = in[(size_t)p * n_steps * 3 + (size_t)rest];
+}
+
+// [date][ld] of T -> [date][n_paths] of double
+template <typename T>
+__global__ void widen_exposures_kernel(const T* __restrict__ in, int64_t ld, int64_t n_paths, int n_dates,
+                                       double* __restrict__ out)
+{
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= n_paths * (int64_t)n_dates) return;
+    const int64_t j = idx / n_paths, p = idx % n_paths;
+    out[idx] = (double)in[(size_t)j * ld + p];
+}
+
+// ---------------------------------------------------------------------------
+// Host launchers
+// ---------------------------------------------------------------------------
+template <int NT, typename T, bool EXT>
+static cudaError_t launch_path_t(const PathParams<T>& P, const double* ext, double* partials, T* estore,
+                                 cudaStream_t s)
+{
+    const size_t smem = path_smem_bytes(NT, P.n_blocks, Prec<T>::kMixed);
+    auto k = path_kernel<NT, T, EXT>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const int64_t grid = (P.n_paths + kCta - 1) / kCta;
+    k<<<(unsigned)grid, kCta, smem, s>>>(P, ext, partials, estore);
+    return cudaGetLastError();
+}
+
+template <typename T>
+static cudaError_t launch_path_nt(int nt, const PathParams<T>& P, const double* ext, double* partials, T* estore,
+                                  cudaStream_t s)
+{
+    if (nt == 51) return ext ? launch_path_t<51, T, true>(P, ext, partials, estore, s)
+                             : launch_path_t<51, T, false>(P, ext, partials, estore, s);
+    if (nt == 61) return ext ? launch_path_t<61, T, true>(P, ext, partials, estore, s)
+                             : launch_path_t<61, T, false>(P, ext, partials, estore, s);
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_path_fp64(int nt, const PathParams<double>& P, const double* ext, double* partials,
+                             double* estore, cudaStream_t s)
+{
+    return launch_path_nt<double>(nt, P, ext, partials, estore, s);
+}
+
+cudaError_t launch_path_mixed(int nt, const PathParams<float>& P, const double* ext, double* partials,
+                              float* estore, cudaStream_t s)
+{
+    return launch_path_nt<float>(nt, P, ext, partials, estore, s);
+}
+
+bool path_tenor_supported(int nt) { return nt == 51 || nt == 61; }
+
+size_t path_smem(int nt, int n_blocks, bool mixed) { return path_smem_bytes(nt, n_blocks, mixed); }
+
+cudaError_t launch_reduce(const double* partials, int64_t n_rows, int R, double* sums, const FinalParams& F,
+                          double* result, cudaStream_t s)
+{
+    reduce_columns<<<R, kReduceThreads, 0, s>>>(partials, n_rows, R, sums);
+    finalize_results<<<1, 32, 0, s>>>(sums, F, result);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pfe(const void* estore, bool fp64_keys, int64_t ld, int64_t n_paths, int n_dates, uint64_t k0,
+                       SelState* st, uint32_t* hist, double* result, int n_sms, cudaStream_t s)
+{
+    pfe_init<<<1, kMaxTenor, 0, s>>>(st, n_dates, k0);
+    cudaMemsetAsync(hist, 0, sizeof(uint32_t) * 256 * (size_t)n_dates, s);
+    int64_t gx = (n_paths + 1023) / 1024;
+    const int64_t cap = (int64_t)n_sms * 8;
+    if (gx > cap) gx = cap;
+    if (gx < 1) gx = 1;
+    const dim3 grid((unsigned)gx, (unsigned)n_dates);
+    const int bits = fp64_keys ? 64 : 32;
+    for (int shift = bits - 8; shift >= 0; shift -= 8) {
+        if (fp64_keys)
+            pfe_hist<uint64_t><<<grid, 256, 0, s>>>((const uint64_t*)estore, ld, n_paths, st, hist, shift);
+        else
+            pfe_hist<uint32_t><<<grid, 256, 0, s>>>((const uint32_t*)estore, ld, n_paths, st, hist, shift);
+        pfe_scan<<<n_dates, 256, 0, s>>>(st, hist, shift);
+    }
+    if (fp64_keys)
+        pfe_write<uint64_t><<<1, kMaxTenor, 0, s>>>(st, n_dates, result);
+    else
+        pfe_write<uint32_t><<<1, kMaxTenor, 0, s>>>(st, n_dates, result);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dump_normals(int64_t n_paths, uint64_t path_offset, int n_steps, uint32_t k0, uint32_t k1,
+                                double* out, cudaStream_t s)
+{
+    const int64_t total = n_paths * (int64_t)n_steps;
+    dump_normals_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(n_paths, path_offset, n_steps, k0, k1, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_philox_words(int64_t n_paths, uint64_t path_offset, uint32_t step, uint32_t k0, uint32_t k1,
+                                uint32_t* out, cudaStream_t s)
+{
+    philox_words_kernel<<<(unsigned)((n_paths + 255) / 256), 256, 0, s>>>(n_paths, path_offset, step, k0, k1, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_transpose_normals(const double* in, int64_t n_paths, int n_steps, double* out, cudaStream_t s)
+{
+    const int64_t total = n_paths * (int64_t)n_steps * 3;
+    transpose_normals_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(in, n_paths, n_steps, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_widen_exposures(const void* in, bool fp64, int64_t ld, int64_t n_paths, int n_dates, double* out,
+                                   cudaStream_t s)
+{
+    const int64_t total = n_paths * (int64_t)n_dates;
+    const unsigned g = (unsigned)((total + 255) / 256);
+    if (fp64)
+        widen_exposures_kernel<double><<<g, 256, 0, s>>>((const double*)in, ld, n_paths, n_dates, out);
+    else
+        widen_exposures_kernel<float><<<g, 256, 0, s>>>((const float*)in, ld, n_paths, n_dates, out);
+    return cudaGetLastError();
+}
+
+}  // namespace hjm

@@ -1,0 +1,53 @@
+// hjm_kernels.h -- host-side launchers of the device kernels (internal).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+#include "hjm_device.cuh"
+
+namespace hjm {
+
+// Device result block (doubles)
+constexpr int kResEE = 0;                       // [kMaxTenor]
+constexpr int kResPFE = kMaxTenor;              // [kMaxTenor]
+constexpr int kResCVA = 2 * kMaxTenor;
+constexpr int kResCVAStderr = kResCVA + 1;
+constexpr int kResDCVADHazard = kResCVA + 2;
+constexpr int kResCVAPathMean = kResCVA + 3;    // mean of per-path CVA contributions
+constexpr int kResLen = kResCVA + 8;
+
+struct FinalParams {
+    double cvaw[kMaxTenor];    // CVA weights per date
+    double dcvaw[kMaxTenor];   // d(weights)/d(hazard)
+    int64_t n_paths;
+    int n_blocks;
+};
+
+struct SelState {
+    uint64_t prefix, mask, k;
+};
+
+cudaError_t launch_path_fp64(int nt, const PathParams<double>& P, const double* ext, double* partials,
+                             double* estore, cudaStream_t s);
+cudaError_t launch_path_mixed(int nt, const PathParams<float>& P, const double* ext, double* partials,
+                              float* estore, cudaStream_t s);
+bool path_tenor_supported(int nt);
+size_t path_smem(int nt, int n_blocks, bool mixed);
+
+cudaError_t launch_reduce(const double* partials, int64_t n_rows, int R, double* sums, const FinalParams& F,
+                          double* result, cudaStream_t s);
+cudaError_t launch_pfe(const void* estore, bool fp64_keys, int64_t ld, int64_t n_paths, int n_dates, uint64_t k0,
+                       SelState* st, uint32_t* hist, double* result, int n_sms, cudaStream_t s);
+cudaError_t launch_dump_normals(int64_t n_paths, uint64_t path_offset, int n_steps, uint32_t k0, uint32_t k1,
+                                double* out, cudaStream_t s);
+cudaError_t launch_philox_words(int64_t n_paths, uint64_t path_offset, uint32_t step, uint32_t k0, uint32_t k1,
+                                uint32_t* out, cudaStream_t s);
+cudaError_t launch_transpose_normals(const double* in, int64_t n_paths, int n_steps, double* out, cudaStream_t s);
+cudaError_t launch_widen_exposures(const void* in, bool fp64, int64_t ld, int64_t n_paths, int n_dates, double* out,
+                                   cudaStream_t s);
+cudaError_t measure_fma_peak(bool fp64, cudaStream_t s, int n_sms, double* tflops);
+
+}  // namespace hjm

@@ -1,0 +1,217 @@
+"""Host-side mirror of the reference's exposure interface, over the C ABI.
+
+``calculate_exposure_gpu`` mirrors the reference's
+``calculateExposureMultiGPU(expected_exposure, payOff, accrual, spot_rates,
+drift, volatilities, scale, num_gpus, simN, dt)`` (simulation_gpu.h:12,14):
+same inputs, same 51-point EE output, same print-and-continue behaviour is
+left to the C++ drop-in; this Python form raises instead.  ``HJMEngine`` is
+the full interface: market and product set-up, FP64 / mixed-precision
+valuation with EE, PFE and CVA, external normals, exposures, diagnostics and
+the adjoint.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from .market import Market, RunConfig, Swap
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+@dataclass
+class Valuation:
+    ee: np.ndarray             # [n_tenor] EE(t_j), zero beyond the last sampled date
+    pfe: np.ndarray | None     # [n_tenor] PFE(t_j) or None
+    cva: float
+    cva_stderr: float
+    dcva_dhazard: float
+    n_dates: int               # sampled dates + 1
+
+
+@dataclass
+class Sensitivities:
+    cva: float
+    cva_stderr: float
+    dcva_dspot: np.ndarray     # [n_tenor]
+    dcva_ddrift: np.ndarray    # [n_tenor]
+    dcva_dvolcoef: np.ndarray  # [3, 3]: factor k, power d of T
+    dcva_dhazard: float
+
+
+class HJMEngine:
+    """One device context (stream, buffers, market, product)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = _lib.load()
+        h = C.c_void_p()
+        _lib.check(self.lib.hjm_ctx_create(device, C.byref(h)), None)
+        self.ctx = h
+        self.n_tenor = 0
+        self.dtau = 0.5
+        self._last_dates = 0
+        self._last_paths = 0
+
+    def close(self) -> None:
+        if getattr(self, "ctx", None):
+            self.lib.hjm_ctx_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # interpreter shutdown
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, status: int) -> None:
+        _lib.check(status, self.ctx)
+
+    # ---------------------------------------------------------------- set-up
+    def set_stream(self, cuda_stream: int | None) -> None:
+        self._check(self.lib.hjm_ctx_set_stream(self.ctx, C.c_void_p(cuda_stream or 0)))
+
+    def keep_exposures(self, keep: bool = True) -> None:
+        self._check(self.lib.hjm_ctx_keep_exposures(self.ctx, 1 if keep else 0))
+
+    def set_market(self, market: Market, drift: bool = True) -> None:
+        spot, vol = _f64(market.spot), _f64(market.vol).ravel()
+        d = _f64(market.drift) if drift else None
+        self._check(self.lib.hjm_set_market(self.ctx, market.n_tenor, market.dtau, _dptr(spot), _dptr(vol), 3,
+                                            _dptr(d) if d is not None else None))
+        self.n_tenor, self.dtau = market.n_tenor, market.dtau
+
+    def set_market_poly(self, n_tenor: int, dtau: float, spot, vol_coeffs) -> None:
+        spot = _f64(spot)
+        coef = _f64(vol_coeffs).reshape(9)
+        self._check(self.lib.hjm_set_market_poly(self.ctx, n_tenor, dtau, _dptr(spot), _dptr(coef)))
+        self.n_tenor, self.dtau = n_tenor, dtau
+
+    def set_swap(self, swap: Swap) -> None:
+        acc = _f64(swap.accrual)
+        self._check(self.lib.hjm_set_swap(self.ctx, swap.notional, swap.strike, _dptr(acc), 1 if swap.payer else 0))
+
+    def set_netting_set(self, notional, fixed_rate, n_periods, payer) -> None:
+        n = len(notional)
+        notional, fixed_rate = _f64(notional), _f64(fixed_rate)
+        n_periods = np.ascontiguousarray(n_periods, dtype=np.int32)
+        payer = np.ascontiguousarray(payer, dtype=np.int32)
+        ip = C.POINTER(C.c_int32)
+        self._check(self.lib.hjm_set_netting_set(self.ctx, n, _dptr(notional), _dptr(fixed_rate),
+                                                 n_periods.ctypes.data_as(ip), payer.ctypes.data_as(ip)))
+
+    # ------------------------------------------------------------- valuation
+    def run(self, cfg: RunConfig, precision: str = "fp64", pfe: bool = True) -> Valuation:
+        nt = self.n_tenor
+        ee, pf, cva = np.zeros(nt), np.zeros(nt), np.zeros(3)
+        self._check(self.lib.hjm_run(self.ctx, cfg.n_paths, cfg.n_steps, cfg.dt, cfg.seed, cfg.path_offset,
+                                     _lib.PRECISION[precision], cfg.hazard, cfg.recovery, cfg.pfe_quantile,
+                                     _dptr(ee), _dptr(pf) if pfe else None, _dptr(cva)))
+        self._last_paths = cfg.n_paths
+        self._last_dates = cfg.n_steps // int(round(self.dtau / cfg.dt)) + 1
+        return Valuation(ee, pf if pfe else None, float(cva[0]), float(cva[1]), float(cva[2]), self._last_dates)
+
+    def enqueue(self, cfg: RunConfig, precision: str = "fp64", pfe: bool = True) -> None:
+        self._check(self.lib.hjm_enqueue(self.ctx, cfg.n_paths, cfg.n_steps, cfg.dt, cfg.seed, cfg.path_offset,
+                                         _lib.PRECISION[precision], cfg.hazard, cfg.recovery,
+                                         cfg.pfe_quantile if pfe else 0.0))
+        self._last_paths = cfg.n_paths
+        self._last_dates = cfg.n_steps // int(round(self.dtau / cfg.dt)) + 1
+
+    def fetch(self, pfe: bool = True) -> Valuation:
+        nt = self.n_tenor
+        ee, pf, cva = np.zeros(nt), np.zeros(nt), np.zeros(3)
+        self._check(self.lib.hjm_fetch_results(self.ctx, _dptr(ee), _dptr(pf), _dptr(cva)))
+        return Valuation(ee, pf if pfe else None, float(cva[0]), float(cva[1]), float(cva[2]), self._last_dates)
+
+    def run_with_normals(self, normals: np.ndarray, n_steps: int, dt: float, precision: str = "fp64",
+                         hazard: float = 0.02, recovery: float = 0.4, pfe_quantile: float = 0.975,
+                         pfe: bool = True) -> Valuation:
+        normals = _f64(normals)
+        n_paths = normals.shape[0]
+        if normals.shape != (n_paths, n_steps, 3):
+            raise ValueError(f"normals must be [n_paths][{n_steps}][3], got {normals.shape}")
+        nt = self.n_tenor
+        ee, pf, cva = np.zeros(nt), np.zeros(nt), np.zeros(3)
+        self._check(self.lib.hjm_run_with_normals(self.ctx, n_paths, n_steps, dt, _dptr(normals),
+                                                  _lib.PRECISION[precision], hazard, recovery, pfe_quantile,
+                                                  _dptr(ee), _dptr(pf) if pfe else None, _dptr(cva)))
+        self._last_paths = n_paths
+        self._last_dates = n_steps // int(round(self.dtau / dt)) + 1
+        return Valuation(ee, pf if pfe else None, float(cva[0]), float(cva[1]), float(cva[2]), self._last_dates)
+
+    def exposures(self) -> np.ndarray:
+        """Per-path exposures of the last valuation, [n_dates][n_paths]."""
+        out = np.zeros((self._last_dates, self._last_paths))
+        self._check(self.lib.hjm_get_exposures(self.ctx, _dptr(out), out.size))
+        return out
+
+    # ---------------------------------------------------------- sensitivities
+    def run_adjoint(self, cfg: RunConfig, checkpoint_every: int = 32) -> Sensitivities:
+        nt = self.n_tenor
+        cva = np.zeros(3)
+        dspot, ddrift, dcoef = np.zeros(nt), np.zeros(nt), np.zeros(9)
+        self._check(self.lib.hjm_run_adjoint(self.ctx, cfg.n_paths, cfg.n_steps, cfg.dt, cfg.seed, cfg.path_offset,
+                                             cfg.hazard, cfg.recovery, checkpoint_every, _dptr(cva), _dptr(dspot),
+                                             _dptr(ddrift), _dptr(dcoef)))
+        return Sensitivities(float(cva[0]), float(cva[1]), dspot, ddrift, dcoef.reshape(3, 3), float(cva[2]))
+
+    # ------------------------------------------------------------ diagnostics
+    def dump_normals(self, n_paths: int, n_steps: int, seed: int, path_offset: int = 0) -> np.ndarray:
+        out = np.zeros((n_paths, n_steps, 3))
+        self._check(self.lib.hjm_dump_normals(self.ctx, n_paths, path_offset, n_steps, seed, _dptr(out)))
+        return out
+
+    def philox_words(self, n_paths: int, step: int, seed: int, path_offset: int = 0) -> np.ndarray:
+        out = np.zeros((n_paths, 4), dtype=np.uint32)
+        self._check(self.lib.hjm_philox_words(self.ctx, n_paths, path_offset, step, seed,
+                                              out.ctypes.data_as(C.POINTER(C.c_uint32))))
+        return out
+
+    def timings(self) -> dict:
+        ms = np.zeros(4)
+        self._check(self.lib.hjm_last_timings(self.ctx, _dptr(ms)))
+        return {"path_ms": ms[0], "reduce_ms": ms[1], "pfe_ms": ms[2], "total_ms": ms[3]}
+
+    def timing_history(self, n: int) -> np.ndarray:
+        """[n][4] device ms of the last n valuations: path kernel, reductions, PFE, total."""
+        ms = np.zeros((n, 4))
+        self._check(self.lib.hjm_timing_history(self.ctx, n, _dptr(ms)))
+        return ms
+
+    def stats(self) -> dict:
+        v = np.zeros(3, dtype=np.int64)
+        self._check(self.lib.hjm_last_stats(self.ctx, v.ctypes.data_as(C.POINTER(C.c_int64))))
+        return {"kernels": int(v[0]), "h2d_bytes": int(v[1]), "d2h_bytes": int(v[2])}
+
+    def fma_peak_tflops(self, precision: str = "fp64") -> float:
+        v = C.c_double(0.0)
+        self._check(self.lib.hjm_measure_fma_peak(self.ctx, _lib.PRECISION[precision], C.byref(v)))
+        return v.value
+
+
+def calculate_exposure_gpu(expected_exposure: np.ndarray, notional: float, K: float, expiry: float, dtau: float,
+                           accrual, spot_rates, drift, volatilities, scale: float, num_gpus: int, simN: int,
+                           dt: float) -> None:
+    """The reference's calculateExposureMultiGPU (double overload) through the
+    C++ drop-in of libhjmcva.so; writes the 51-point EE into expected_exposure."""
+    lib = _lib.load()
+    if expected_exposure.dtype != np.float64 or expected_exposure.size < 51:
+        raise ValueError("expected_exposure must be a float64 array of 51 values")
+    a, s, d, v = (_f64(x) for x in (accrual, spot_rates, drift, volatilities))
+    lib.hjm_dropin_calculate_exposure_fp64(_dptr(expected_exposure), notional, K, expiry, dtau, _dptr(a), _dptr(s),
+                                           _dptr(d), _dptr(v), num_gpus, simN, dt)

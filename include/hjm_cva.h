@@ -1,0 +1,182 @@
+/*
+ * hjm_cva.h -- C ABI of the GB300 HJM exposure / CVA engine (libhjmcva.so).
+ *
+ * This is the boundary that replaces the reference's GPU entry point
+ * (mahsanchez/cva_hjm_cuda simulation_gpu.h:12,14 -> simulation_gpu.cu:956-1250,
+ * __calculateExposureMultiGPU).  The C++ drop-in for those two overloads is
+ * declared in hjm_dropin.h and is implemented on top of these functions.
+ *
+ * Conventions
+ *   - Every function returns an hjm_status; nothing throws across the ABI.
+ *     hjm_last_error(ctx) gives the message of the last failure on ctx
+ *     (ctx may be NULL for failures of hjm_ctx_create).
+ *   - Pointers named *_host are host memory owned by the caller.
+ *   - A context owns one device, one CUDA stream and its device buffers.
+ *     Calls on one context must not overlap; distinct contexts are
+ *     independent and may be driven from different threads.  (The reference
+ *     writes global __constant__ symbols and is not re-entrant,
+ *     simulation_gpu.cu:109-119, 1032-1035.)
+ *   - Arrays on the tenor grid have n_tenor entries, 2 <= n_tenor <= 64.
+ *     Volatility tables are factor-major, vol[k * n_tenor + t], three factors
+ *     (simulation_gpu_testing.cpp:47-63; VOL_DIM = 3 in simulation_gpu.cu:34).
+ *   - Paths are numbered globally: path p uses the Philox4x32-10 counter
+ *     (step, 0, p lo, p hi) under key (seed lo, seed hi), so a run over paths
+ *     [path_offset, path_offset + n_paths) draws exactly the normals those
+ *     paths draw in any larger run.
+ */
+#ifndef HJM_CVA_H
+#define HJM_CVA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HJM_MAX_TENOR 64
+#define HJM_N_FACTOR 3
+#define HJM_N_VOL_COEF 9 /* three factors x polynomial degree <= 2 */
+
+typedef struct hjm_ctx hjm_ctx;
+
+typedef enum hjm_status {
+    HJM_OK = 0,
+    HJM_ERR_INVALID_ARGUMENT = 1,
+    HJM_ERR_UNSUPPORTED = 2,
+    HJM_ERR_CUDA = 3,
+    HJM_ERR_OUT_OF_MEMORY = 4,
+    HJM_ERR_NOT_CONFIGURED = 5,
+    HJM_ERR_NO_DEVICE = 6
+} hjm_status;
+
+typedef enum hjm_precision {
+    /* curve evolution, swap pricing and reductions in FP64 */
+    HJM_PRECISION_FP64 = 0,
+    /* curve evolution and swap pricing in FP32; the deterministic drift
+     * integral, the discount accumulation and the EE/CVA reductions in FP64 */
+    HJM_PRECISION_MIXED = 1
+} hjm_precision;
+
+/* Output layout of hjm_run / hjm_run_with_normals: cva_out[0..3] */
+#define HJM_CVA_VALUE 0
+#define HJM_CVA_STDERR 1    /* Monte Carlo standard error of the CVA estimate */
+#define HJM_CVA_DHAZARD 2   /* dCVA / d(hazard rate), exact from EE */
+#define HJM_CVA_OUT_LEN 3
+
+/* ---- library / context --------------------------------------------------- */
+const char* hjm_version(void);
+/* Message of the last failure on ctx (or of the calling thread when ctx is NULL). */
+const char* hjm_last_error(const hjm_ctx* ctx);
+
+/* Create a context on CUDA device `device`.  Replaces the per-GPU set-up of
+ * simulation_gpu.cu:989-1043 (allocation, generator, constant uploads). */
+hjm_status hjm_ctx_create(int device, hjm_ctx** out);
+hjm_status hjm_ctx_destroy(hjm_ctx* ctx);
+/* Launch on a caller-owned cudaStream_t instead of the context's own stream
+ * (NULL restores the context's stream). */
+hjm_status hjm_ctx_set_stream(hjm_ctx* ctx, void* cuda_stream);
+
+/* Keep the per-path exposures of every valuation on the device (for
+ * hjm_get_exposures); they are always kept when a PFE is requested. */
+hjm_status hjm_ctx_keep_exposures(hjm_ctx* ctx, int32_t keep);
+
+/* ---- inputs --------------------------------------------------------------- */
+/* Market: spot forward curve, volatility factors, and the drift.  With
+ * drift_host == NULL the Musiela no-arbitrage drift is computed in FP64 by the
+ * trapezoid rule on the tenor grid.  Replaces the cudaMemcpyToSymbol uploads of
+ * simulation_gpu.cu:1032-1035 (spot, drift, volatilities). */
+hjm_status hjm_set_market(hjm_ctx* ctx, int32_t n_tenor, double dtau, const double* spot_host,
+                          const double* vol_host, int32_t n_factor, const double* drift_host);
+
+/* One interest-rate swap (product.h:4-18 InterestRateSwap: notional, K, and
+ * the accrual table of simulation_gpu.cu:1032).  payer != 0 pays fixed:
+ * cash flow D * N * alpha * (L - K); a receiver swap has the opposite sign. */
+hjm_status hjm_set_swap(hjm_ctx* ctx, double notional, double fixed_rate, const double* accrual_host,
+                        int32_t payer);
+
+/* A netting set of n_swaps swaps on the tenor grid, netted before max(., 0).
+ * Swap s accrues dtau on periods 1..n_periods[s].  Generalises the single
+ * swap of simulation_cpu.h:269-296. */
+hjm_status hjm_set_netting_set(hjm_ctx* ctx, int32_t n_swaps, const double* notional_host,
+                               const double* fixed_rate_host, const int32_t* n_periods_host,
+                               const int32_t* payer_host);
+
+/* ---- forward valuation ---------------------------------------------------- */
+/* Simulate n_paths paths of n_steps Euler steps of size dt (n_steps must be a
+ * multiple of stride = dtau / dt; the reference's block loop,
+ * simulation_cpu.h:413, simulation_gpu.cu:594-669), price the product at the
+ * end of every block, and reduce.
+ *   ee_out      [n_tenor]  expected exposure EE(t_j), t_j = j * dtau (zero
+ *                          beyond the last sampled date) -- the reference's
+ *                          expected_exposure output (simulation_gpu.cu:1177-1179)
+ *   pfe_out     [n_tenor]  PFE(t_j) at pfe_quantile (may be NULL; then
+ *                          pfe_quantile is ignored)
+ *   cva_out     [HJM_CVA_OUT_LEN]  CVA, its MC standard error, dCVA/dhazard,
+ *               CVA = (1-R) sum_j EE(t_j) (exp(-l t_{j-1}) - exp(-l t_j)).
+ * Host buffers; blocks until the results are on the host. */
+hjm_status hjm_run(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, double dt, uint64_t seed,
+                   uint64_t path_offset, int32_t precision, double hazard_rate, double recovery,
+                   double pfe_quantile, double* ee_out, double* pfe_out, double* cva_out);
+
+/* The same valuation, enqueued on the context's stream without any host copy
+ * or synchronisation; results stay on the device until hjm_fetch_results. */
+hjm_status hjm_enqueue(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, double dt, uint64_t seed,
+                       uint64_t path_offset, int32_t precision, double hazard_rate, double recovery,
+                       double pfe_quantile);
+hjm_status hjm_fetch_results(hjm_ctx* ctx, double* ee_out, double* pfe_out, double* cva_out);
+
+/* The valuation on caller-supplied normals, normals_host[path][step][3]
+ * (the reference's layout, simulation_cpu.h:205-207, simulation_gpu.cu:410).
+ * Used to feed the reference's own draws to the kernels. */
+hjm_status hjm_run_with_normals(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, double dt,
+                                const double* normals_host, int32_t precision, double hazard_rate,
+                                double recovery, double pfe_quantile, double* ee_out,
+                                double* pfe_out, double* cva_out);
+
+/* Exposures of the last valuation, date-major: out[j * n_paths + p] for
+ * j = 0 .. n_dates-1 with n_dates = n_steps / stride + 1 (the exposure
+ * matrix of simulation_gpu.cu:1003 / simulation_cpu.h:362, transposed). */
+hjm_status hjm_get_exposures(hjm_ctx* ctx, double* out_host, int64_t capacity);
+
+/* ---- sensitivities ---------------------------------------------------------- */
+/* Pathwise adjoint of the CVA: dCVA/d(initial forwards) [n_tenor],
+ * dCVA/d(drift table) [n_tenor], dCVA/d(polynomial volatility coefficients)
+ * [HJM_N_VOL_COEF] (diffusion and trapezoid-drift paths; coefficient (k,d)
+ * multiplies T^d in factor k), and dCVA/d(hazard).  Curve states are
+ * checkpointed every checkpoint_every steps (0 = none) and recomputed in the
+ * reverse sweep.  Requires a market set through hjm_set_market_poly. */
+hjm_status hjm_set_market_poly(hjm_ctx* ctx, int32_t n_tenor, double dtau, const double* spot_host,
+                               const double* vol_coef_host /* [3][3] */);
+hjm_status hjm_run_adjoint(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, double dt, uint64_t seed,
+                           uint64_t path_offset, double hazard_rate, double recovery,
+                           int32_t checkpoint_every, double* cva_out, double* dcva_dspot_out,
+                           double* dcva_ddrift_out, double* dcva_dvolcoef_out);
+
+/* ---- diagnostics ------------------------------------------------------------- */
+/* The device's normals for paths [path_offset, path_offset+n_paths) and steps
+ * [0, n_steps): out[path][step][3], exactly the values the path kernel uses. */
+hjm_status hjm_dump_normals(hjm_ctx* ctx, int64_t n_paths, uint64_t path_offset, int32_t n_steps,
+                            uint64_t seed, double* out_host);
+/* Raw Philox4x32-10 words for counter (step, 0, p lo, p hi), key = seed:
+ * out[p * 4 + i]. */
+hjm_status hjm_philox_words(hjm_ctx* ctx, int64_t n_paths, uint64_t path_offset, uint32_t step,
+                            uint64_t seed, uint32_t* out_host);
+/* Device times of the last valuation (ms): [0] path kernel, [1] reductions,
+ * [2] PFE selection, [3] whole enqueue. */
+hjm_status hjm_last_timings(hjm_ctx* ctx, double* ms_out /* [4] */);
+/* The same four device times for each of the last n valuations (n <= 64),
+ * oldest first: ms_out[4 * i + k]. */
+hjm_status hjm_timing_history(hjm_ctx* ctx, int32_t n, double* ms_out /* [4 * n] */);
+/* Counters of the last valuation: [0] kernels launched, [1] bytes copied
+ * host -> device (kernel parameter blocks and caller arrays), [2] bytes copied
+ * device -> host (results). */
+hjm_status hjm_last_stats(hjm_ctx* ctx, int64_t* stats_out /* [3] */);
+/* Sustained FMA throughput of this device in TFLOP/s (2 flops per FMA) for
+ * precision HJM_PRECISION_FP64 (DFMA) or HJM_PRECISION_MIXED (FFMA). */
+hjm_status hjm_measure_fma_peak(hjm_ctx* ctx, int32_t precision, double* tflops_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HJM_CVA_H */
