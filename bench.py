@@ -209,7 +209,9 @@ def run_ours(args) -> None:
     mk, sw = Market(), Swap()
     stride = int(round(mk.dtau / DT))
     eng = HJMEngine(local_rank)
-    stream = torch.cuda.current_stream()
+    # a dedicated (non-default) stream: the engine and the timing events share it
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     eng.set_stream(stream.cuda_stream)
     eng.set_market(mk)
     eng.set_swap(sw)
