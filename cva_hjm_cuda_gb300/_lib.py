@@ -32,8 +32,9 @@ EXPORTED = [
     "hjm_ctx_keep_exposures", "hjm_set_market", "hjm_set_swap", "hjm_set_netting_set", "hjm_run",
     "hjm_enqueue", "hjm_fetch_results", "hjm_run_with_normals", "hjm_get_exposures", "hjm_set_market_poly",
     "hjm_run_adjoint", "hjm_dump_normals", "hjm_philox_words", "hjm_last_timings", "hjm_timing_history", "hjm_last_stats", "hjm_measure_fma_peak",
-    "hjm_dropin_calculate_exposure_fp64", "hjm_dropin_calculate_exposure_fp32",
+    "hjm_dropin_calculate_exposure_fp64", "hjm_dropin_calculate_exposure_fp32", "hjm_run_static",
 ]
+STATIC_MAX_PATHS = 1048576
 
 _lock = threading.Lock()
 _lib: C.CDLL | None = None
@@ -71,6 +72,9 @@ def _declare(lib: C.CDLL) -> None:
         "hjm_timing_history": (st, [_vp, C.c_int32, _dp]),
         "hjm_last_stats": (st, [_vp, C.POINTER(C.c_int64)]),
         "hjm_measure_fma_peak": (st, [_vp, C.c_int32, _dp]),
+        "hjm_run_static": (st, [_vp, C.c_int32, C.c_double, _dp, _dp, _dp, C.c_double, C.c_double, _dp, C.c_int32,
+                                C.c_int64, C.c_int32, C.c_double, C.c_uint64, C.c_uint64, C.c_int32, C.c_double,
+                                C.c_double, _dp, _dp]),
         "hjm_dropin_calculate_exposure_fp64": (None, [_dp, C.c_double, C.c_double, C.c_double, C.c_double, _dp, _dp,
                                                       _dp, _dp, C.c_int, C.c_int, C.c_double]),
         "hjm_dropin_calculate_exposure_fp32": (None, [C.POINTER(C.c_float), C.c_float, C.c_float, C.c_float,

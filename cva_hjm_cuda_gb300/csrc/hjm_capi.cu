@@ -49,6 +49,12 @@ struct DevBuf {
 
 }  // namespace
 
+namespace hjm {
+// Lets the allocation-free entry point (hjm_static.cu) report a failure
+// through hjm_last_error(NULL); internal to the library.
+__attribute__((visibility("hidden"))) void set_thread_error(const char* msg) { g_thread_error = msg; }
+}  // namespace hjm
+
 struct hjm_ctx {
     int device = 0;
     int n_sms = 0;

@@ -153,6 +153,29 @@ hjm_status hjm_run_adjoint(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, doubl
                            int32_t checkpoint_every, double* cva_out, double* dcva_dspot_out,
                            double* dcva_ddrift_out, double* dcva_dvolcoef_out);
 
+/* ---- allocation-free valuation ------------------------------------------------ */
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory after start-up -- a host whose pool allocator owns the whole GPU, a
+ * plugin loaded into such a process, a latency-bound loop that cannot take
+ * the device-wide synchronisation a cudaMalloc/cudaFree may cause.  No
+ * context: all inputs are host arrays (as for hjm_set_market / hjm_set_swap /
+ * hjm_run), the work is enqueued on cuda_stream (NULL = the legacy default
+ * stream) and the call returns when ee_out [n_tenor] and cva_out
+ * [HJM_CVA_OUT_LEN] hold the results.  Its scratch is a fixed 4.2 MB static
+ * device array that each GPU loading the library keeps until exit; it calls
+ * no cudaMalloc, cudaFree or allocating library routine.  Limits: at most
+ * HJM_STATIC_MAX_PATHS paths per call (larger runs fail with
+ * HJM_ERR_INVALID_ARGUMENT), EE and CVA only (no PFE).  The first call on a
+ * device looks up the scratch address (cudaGetSymbolAddress): make that first
+ * call before any stream capture.  All calls share the scratch, so calls that
+ * overlap on the GPU race; serialise them.  Errors: hjm_last_error(NULL). */
+#define HJM_STATIC_MAX_PATHS 1048576
+hjm_status hjm_run_static(void* cuda_stream, int32_t n_tenor, double dtau, const double* spot_host,
+                          const double* vol_host, const double* drift_host, double notional, double fixed_rate,
+                          const double* accrual_host, int32_t payer, int64_t n_paths, int32_t n_steps, double dt,
+                          uint64_t seed, uint64_t path_offset, int32_t precision, double hazard_rate,
+                          double recovery, double* ee_out, double* cva_out);
+
 /* ---- diagnostics ------------------------------------------------------------- */
 /* The device's normals for paths [path_offset, path_offset+n_paths) and steps
  * [0, n_steps): out[path][step][3], exactly the values the path kernel uses. */

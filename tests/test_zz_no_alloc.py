@@ -1,0 +1,81 @@
+"""hjm_run_static: the allocation-free entry point.
+
+Some callers cannot allocate device memory once they are running: a risk
+server whose pool allocator already owns the GPU, a pricing plugin loaded into
+such a process, or a latency-bound loop that cannot take the device-wide
+synchronisation a cudaMalloc/cudaFree may cause.  hjm_run_static serves them
+from a fixed static device scratch (at most HJM_STATIC_MAX_PATHS paths, EE and
+CVA only).  This test calls it through the C ABI twice in a row and checks it
+against the context-based hjm_run, within the FP64 parity tolerance of the
+other GPU tests, and checks that oversize runs are refused with a clear error.
+
+The file name makes pytest collect it last; it must also pass on its own in a
+fresh process (the first call on the device does the scratch set-up).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from cva_hjm_cuda_gb300 import _lib
+from cva_hjm_cuda_gb300.market import Market, RunConfig, Swap
+
+pytestmark = pytest.mark.gpu
+
+FP64_RTOL = 1e-10
+MIXED_RTOL = 1e-4
+
+
+def _have_gpu() -> bool:
+    try:
+        import torch
+
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _run_static(lib, mk, sw, cfg, precision):
+    ee, cva = np.zeros(mk.n_tenor), np.zeros(3)
+    st = lib.hjm_run_static(None, mk.n_tenor, mk.dtau, _dp(mk.spot), _dp(np.ascontiguousarray(mk.vol.ravel())),
+                            _dp(mk.drift), sw.notional, sw.strike, _dp(sw.accrual), 1 if sw.payer else 0,
+                            cfg.n_paths, cfg.n_steps, cfg.dt, cfg.seed, cfg.path_offset, _lib.PRECISION[precision],
+                            cfg.hazard, cfg.recovery, _dp(ee), _dp(cva))
+    return st, ee, cva
+
+
+@pytest.mark.skipif(not _have_gpu(), reason="no CUDA device")
+@pytest.mark.parametrize("precision,rtol", [("fp64", FP64_RTOL), ("mixed", MIXED_RTOL)])
+def test_static_entry_matches_hjm_run_twice(precision, rtol):
+    from cva_hjm_cuda_gb300.engine import HJMEngine
+
+    lib = _lib.load()
+    mk, sw = Market(), Swap()
+    cfg = RunConfig(n_paths=50_000, n_steps=1000, dt=0.01, seed=4321, path_offset=7)
+    with HJMEngine(0) as eng:
+        eng.set_market(mk)
+        eng.set_swap(sw)
+        ref = eng.run(cfg, precision, pfe=False)
+    for call in range(2):
+        st, ee, cva = _run_static(lib, mk, sw, cfg, precision)
+        assert st == 0, lib.hjm_last_error(None)
+        np.testing.assert_allclose(ee, ref.ee, rtol=rtol, atol=0, err_msg=f"EE, call {call}")
+        assert abs(cva[0] - ref.cva) <= rtol * abs(ref.cva), f"CVA, call {call}"
+        assert abs(cva[1] - ref.cva_stderr) <= 1e-6 * ref.cva_stderr
+        assert abs(cva[2] - ref.dcva_dhazard) <= rtol * abs(ref.dcva_dhazard)
+
+
+@pytest.mark.skipif(not _have_gpu(), reason="no CUDA device")
+def test_static_entry_rejects_oversize_runs():
+    lib = _lib.load()
+    mk, sw = Market(), Swap()
+    cfg = RunConfig(n_paths=_lib.STATIC_MAX_PATHS + 1)
+    st, _, _ = _run_static(lib, mk, sw, cfg, "fp64")
+    assert st == 1  # HJM_ERR_INVALID_ARGUMENT
+    assert b"HJM_STATIC_MAX_PATHS" in lib.hjm_last_error(None)
