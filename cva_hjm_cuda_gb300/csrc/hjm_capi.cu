@@ -77,7 +77,7 @@ struct hjm_ctx {
     bool keep_exposures = false;
 
     // device buffers
-    DevBuf partials, sums, result, estore, sel, hist, ext, ext_raw, wide, scratch;
+    DevBuf partials, sums, result, estore, sel, hist, ext, ext_raw, wide, scratch, ck_h, ck_a;
 
     // last valuation
     bool have_result = false;
@@ -182,7 +182,7 @@ hjm_status hjm_ctx_destroy(hjm_ctx* ctx)
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     for (DevBuf* b : {&ctx->partials, &ctx->sums, &ctx->result, &ctx->estore, &ctx->sel, &ctx->hist, &ctx->ext,
-                      &ctx->ext_raw, &ctx->wide, &ctx->scratch})
+                      &ctx->ext_raw, &ctx->wide, &ctx->scratch, &ctx->ck_h, &ctx->ck_a})
         b->release();
     for (auto& q : ctx->ring)
         for (auto& ev : q)
@@ -446,7 +446,7 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
     const size_t esize = mixed ? 4 : 8;
 
     HJM_CUDA(ctx, ctx->partials.ensure(sizeof(double) * (size_t)n_ctas * R));
-    HJM_CUDA(ctx, ctx->sums.ensure(sizeof(double) * kMaxTenor * 2));
+    HJM_CUDA(ctx, ctx->sums.ensure(sizeof(double) * kMaxTenor * 4));
     HJM_CUDA(ctx, ctx->result.ensure(sizeof(double) * kResLen));
     if (store) HJM_CUDA(ctx, ctx->estore.ensure(esize * (size_t)n_dates * (size_t)ld));
     if (want_pfe) {
@@ -694,8 +694,98 @@ hjm_status hjm_run_adjoint(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, doubl
                            double* dcva_dvolcoef_out)
 {
     HJM_CHECK_CTX(ctx);
-    (void)n_paths; (void)n_steps; (void)dt; (void)seed; (void)path_offset; (void)hazard_rate; (void)recovery;
-    (void)checkpoint_every; (void)cva_out; (void)dcva_dspot_out; (void)dcva_ddrift_out; (void)dcva_dvolcoef_out;
-    return fail(ctx, HJM_ERR_UNSUPPORTED, "adjoint not built yet");
+    RunShape sh;
+    hjm_status st = check_run(ctx, n_paths, n_steps, dt, HJM_PRECISION_MIXED, hazard_rate, recovery, 0.0, sh);
+    if (st != HJM_OK) return st;
+    if (checkpoint_every < 0 || checkpoint_every > sh.stride)
+        return fail(ctx, HJM_ERR_UNSUPPORTED, "checkpoint_every %d: must be 0 (none) or in [1, %d] (the block length)",
+                    checkpoint_every, sh.stride);
+    if (dcva_dvolcoef_out && !ctx->have_poly)
+        return fail(ctx, HJM_ERR_NOT_CONFIGURED,
+                    "volatility-coefficient sensitivities need a polynomial market (hjm_set_market_poly)");
+    const int nt = ctx->nt, B = sh.B;
+    const int R = adjoint_columns(nt, B);
+    const size_t smem = adjoint_smem(nt, B);
+    if (smem > 227 * 1024) return fail(ctx, HJM_ERR_UNSUPPORTED, "adjoint shared memory %zu B exceeds 227 KB", smem);
+    HJM_CUDA(ctx, cudaSetDevice(ctx->device));
+    const int64_t n_ctas = (n_paths + kCta - 1) / kCta;
+    const int64_t ld = (n_paths + 3) / 4 * 4;
+    const int E = n_steps - sh.stride;
+    const int K = checkpoint_every;
+    const int S = K > 0 ? (E + K - 1) / K : 0;
+    HJM_CUDA(ctx, ctx->partials.ensure(sizeof(double) * (size_t)n_ctas * R));
+    HJM_CUDA(ctx, ctx->sums.ensure(sizeof(double) * kMaxTenor * 4));
+    HJM_CUDA(ctx, ctx->result.ensure(sizeof(double) * kResLen));
+    if (K > 0) {
+        HJM_CUDA(ctx, ctx->ck_h.ensure(sizeof(float) * (size_t)S * nt * (size_t)ld));
+        HJM_CUDA(ctx, ctx->ck_a.ensure(sizeof(double) * (size_t)S * (size_t)ld));
+    }
+    AdjParams A;
+    FinalParams F;
+    std::memset(&A, 0, sizeof(A));
+    fill_params<float>(ctx, sh, n_paths, dt, seed, path_offset, hazard_rate, recovery, 0, false, A.P, F);
+    for (int t = 0; t < nt; ++t) {
+        const double T = ctx->dtau * t;
+        A.tau[t] = (float)T;
+        A.tau2[t] = (float)(T * T);
+    }
+    A.ckpt_every = K;
+    A.ck_ld = ld;
+    cudaStream_t s = ctx->stream;
+    ctx->ev = ctx->ring[ctx->n_enqueued % hjm_ctx::kRing];
+    ctx->n_enqueued++;
+    HJM_CUDA(ctx, cudaMemsetAsync(ctx->result.p, 0, sizeof(double) * kResLen, s));
+    HJM_CUDA(ctx, cudaEventRecord(ctx->ev[0], s));
+    HJM_CUDA(ctx, launch_adjoint(nt, A, (double*)ctx->partials.p, K > 0 ? (float*)ctx->ck_h.p : nullptr,
+                                 K > 0 ? (double*)ctx->ck_a.p : nullptr, s));
+    HJM_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
+    HJM_CUDA(ctx, launch_reduce((const double*)ctx->partials.p, n_ctas, R, (double*)ctx->sums.p, F,
+                                (double*)ctx->result.p, s));
+    HJM_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
+    HJM_CUDA(ctx, cudaEventRecord(ctx->ev[3], s));
+    ctx->stat_launches = 3;
+    ctx->stat_h2d = sizeof(AdjParams) + sizeof(FinalParams);
+    std::vector<double> res(kResLen), sums(R);
+    HJM_CUDA(ctx, cudaMemcpyAsync(res.data(), ctx->result.p, sizeof(double) * kResLen, cudaMemcpyDeviceToHost, s));
+    HJM_CUDA(ctx, cudaMemcpyAsync(sums.data(), ctx->sums.p, sizeof(double) * R, cudaMemcpyDeviceToHost, s));
+    HJM_CUDA(ctx, cudaStreamSynchronize(s));
+    ctx->stat_d2h = (int64_t)sizeof(double) * (kResLen + R);
+    ctx->have_result = false;  // the exposure-valuation result buffers are not this run's
+    const double inv_n = 1.0 / (double)n_paths;
+    if (cva_out) {
+        cva_out[HJM_CVA_VALUE] = res[kResCVA];
+        cva_out[HJM_CVA_STDERR] = res[kResCVAStderr];
+        cva_out[HJM_CVA_DHAZARD] = res[kResDCVADHazard];
+    }
+    std::vector<double> dmu(nt);
+    for (int t = 0; t < nt; ++t) dmu[t] = dt * sums[B + 3 + nt + t] * inv_n;
+    if (dcva_dspot_out)
+        for (int t = 0; t < nt; ++t) dcva_dspot_out[t] = sums[B + 3 + t] * inv_n;
+    if (dcva_ddrift_out)
+        for (int t = 0; t < nt; ++t) dcva_ddrift_out[t] = dmu[t];
+    if (dcva_dvolcoef_out) {
+        // diffusion part, then the trapezoid drift's dependence on the coefficients:
+        // mu_i = sum_k sigma_k(tau_i) I_k(i), I_k(i) = sum_{j<=i} (sigma_k(tau_j)+sigma_k(tau_{j-1}))/2 dtau
+        // d mu_i / d c_{k,d} = tau_i^d I_k(i) + sigma_k(tau_i) J_d(i),  J_d(i) = sum_{j<=i} (tau_j^d+tau_{j-1}^d)/2 dtau
+        const double sq = std::sqrt(dt);
+        for (int k = 0; k < HJM_N_FACTOR; ++k) {
+            const double* sig = ctx->vol.data() + (size_t)k * nt;
+            for (int d = 0; d < 3; ++d) {
+                double v = sq * sums[B + 3 + 2 * nt + k * 3 + d] * inv_n;
+                double I = 0.0, J = 0.0;
+                for (int i = 0; i < nt; ++i) {
+                    const double ti = ctx->dtau * i;
+                    if (i > 0) {
+                        const double tp = ctx->dtau * (i - 1);
+                        I += 0.5 * (sig[i] + sig[i - 1]) * ctx->dtau;
+                        J += 0.5 * (std::pow(ti, d) + std::pow(tp, d)) * ctx->dtau;
+                    }
+                    v += dmu[i] * (std::pow(ti, d) * I + sig[i] * J);
+                }
+                dcva_dvolcoef_out[k * 3 + d] = v;
+            }
+        }
+    }
+    return HJM_OK;
 }
 

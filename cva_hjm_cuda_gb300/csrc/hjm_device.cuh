@@ -108,4 +108,60 @@ struct PathParams {
     int store_exposures;         // write per-path exposures [date][path]
 };
 
+#ifdef __CUDACC__
+// The three normals of (path, step): Philox in registers, or read from a
+// caller-supplied buffer laid out [step][3][path] (coalesced across threads).
+template <typename T, bool EXT>
+__device__ __forceinline__ void draw_phi(const double* __restrict__ ext, uint64_t gpath, int64_t lp, int64_t n_paths,
+                                         int n, uint32_t key0, uint32_t key1, T& phi0, T& phi1, T& phi2)
+{
+    if constexpr (EXT) {
+        const size_t np = (size_t)n_paths;
+        const size_t base = (size_t)n * 3 * np + (size_t)lp;
+        phi0 = (T)__ldg(ext + base);
+        phi1 = (T)__ldg(ext + base + np);
+        phi2 = (T)__ldg(ext + base + 2 * np);
+    } else {
+        const uint4 w = philox4x32_10(normals_counter(gpath, (uint32_t)n), key0, key1);
+        float z0, z1, z2;
+        normals3(w, z0, z1, z2);
+        phi0 = (T)z0;
+        phi1 = (T)z1;
+        phi2 = (T)z2;
+    }
+}
+
+// One Musiela Euler step of the stochastic part of the curve
+// (simulation_cpu.h:37-54 with the drift moved into the deterministic part):
+//   h[t] <- h[t] + sum_k sv[k][t] phi_k + c (h[t+1] - h[t])   (backward difference
+// at the last tenor, simulation_cpu.h:96-108); 5 FMA-pipe instructions per
+// tenor with every coefficient read from the constant bank.
+template <int NT, typename T>
+__device__ __forceinline__ void euler_step(T (&h)[NT], const PathParams<T>& P, T c, T phi0, T phi1, T phi2)
+{
+    T hn[NT];
+#pragma unroll
+    for (int t = 0; t < NT; ++t) {
+        T x = fma(P.sv[0][t], phi0, h[t]);
+        x = fma(P.sv[1][t], phi1, x);
+        x = fma(P.sv[2][t], phi2, x);
+        const T d = (t < NT - 1) ? (h[t + 1] - h[t]) : (h[t] - h[t - 1]);
+        hn[t] = fma(c, d, x);
+    }
+#pragma unroll
+    for (int t = 0; t < NT; ++t) h[t] = hn[t];
+}
+
+// Static selection of a register-array element by a runtime index (uniform
+// across the warp): keeps the arrays in registers.
+template <int NT, typename T>
+__device__ __forceinline__ T select_reg(const T (&a)[NT], int i)
+{
+    T r = a[0];
+#pragma unroll
+    for (int t = 1; t < NT; ++t) r = (t == i) ? a[t] : r;
+    return r;
+}
+#endif
+
 }  // namespace hjm

@@ -25,17 +25,6 @@
 
 namespace hjm {
 
-// Static selection of a register-array element by a runtime index (uniform
-// across the warp): keeps the arrays in registers.
-template <int NT, typename T>
-__device__ __forceinline__ T select_reg(const T (&a)[NT], int i)
-{
-    T r = a[0];
-#pragma unroll
-    for (int t = 1; t < NT; ++t) r = (t == i) ? a[t] : r;
-    return r;
-}
-
 template <typename T>
 struct Prec;
 template <>
@@ -136,34 +125,8 @@ __global__ void __launch_bounds__(kCta, Prec<T>::kMixed ? 3 : 1)
         for (int s = 0; s < P.stride; ++s) {
             const int n = b * P.stride + s;
             T phi0, phi1, phi2;
-            if constexpr (EXT) {
-                const size_t np = (size_t)P.n_paths;
-                const size_t base = (size_t)n * 3 * np + (size_t)(active ? lp : 0);
-                phi0 = (T)__ldg(ext + base);
-                phi1 = (T)__ldg(ext + base + np);
-                phi2 = (T)__ldg(ext + base + 2 * np);
-            } else {
-                const uint4 w = philox4x32_10(normals_counter(gpath, (uint32_t)n), P.key0, P.key1);
-                float z0, z1, z2;
-                normals3(w, z0, z1, z2);
-                phi0 = (T)z0;
-                phi1 = (T)z1;
-                phi2 = (T)z2;
-            }
-            // Musiela Euler step of the stochastic part (simulation_cpu.h:37-54
-            // with the drift moved into the deterministic part): 5 FMA-pipe
-            // operations per tenor, coefficients from the constant bank.
-            T hn[NT];
-#pragma unroll
-            for (int t = 0; t < NT; ++t) {
-                T x = fma(P.sv[0][t], phi0, h[t]);
-                x = fma(P.sv[1][t], phi1, x);
-                x = fma(P.sv[2][t], phi2, x);
-                const T d = (t < NT - 1) ? (h[t + 1] - h[t]) : (h[t] - h[t - 1]);
-                hn[t] = fma(c, d, x);
-            }
-#pragma unroll
-            for (int t = 0; t < NT; ++t) h[t] = hn[t];
+            draw_phi<T, EXT>(ext, gpath, active ? lp : 0, P.n_paths, n, P.key0, P.key1, phi0, phi1, phi2);
+            euler_step<NT, T>(h, P, c, phi0, phi1, phi2);
             if constexpr (kMixed) {
 #pragma unroll
                 for (int t = 1; t < NT; ++t) pb[t] += h[t];
