@@ -292,6 +292,8 @@ def run_ours(args) -> None:
 
     if not args.no_extras and prec == "fp64":
         extras["mixed"] = mixed_vs_fp64(eng, mk, sw, args, stream, flush, value)
+        extras["adjoint"] = adjoint_cost(eng, args, flush)
+        extras["netting"] = netting_set_run(eng, args, flush)
     if not args.no_extras:
         cb = cpu_oracle_sample(target_s=3.0, n_threads=os.cpu_count() or 1)
         n_cpu = cb["n_paths"]
@@ -373,6 +375,91 @@ def mixed_vs_fp64(eng, mk, sw, args, stream, flush, fp64_value) -> dict:
         "cva_stderr": mx.cva_stderr,
         "pfe_max_rel_err_vs_fp64": float(np.max(np.abs(mx.pfe[:20] - f64.pfe[:20]) / f64.pfe[:20])),
     }
+
+
+def adjoint_cost(eng, args, flush) -> dict:
+    """Config 4: CVA plus its sensitivities to the 51 initial forwards, the drift
+    table, the 9 volatility coefficients and the hazard rate, by the pathwise
+    adjoint (1,048,576 paths, FP32 forward with FP64 accumulators, checkpoints
+    every 32 steps), against one CVA valuation of the same paths."""
+    import numpy as np
+    import torch
+
+    from cva_hjm_cuda_gb300 import RunConfig
+    from cva_hjm_cuda_gb300.market import DEFAULT_VOL_COEFFS, Swap, nelson_siegel_curve, tenor_grid
+
+    n = 1_048_576
+    eng.set_market_poly(51, 0.5, nelson_siegel_curve(tenor_grid(51, 0.5)), DEFAULT_VOL_COEFFS)
+    eng.set_swap(Swap())
+    cfg = RunConfig(n_paths=n, n_steps=N_STEPS, dt=DT, seed=SEED)
+    out = {"n_paths": n, "n_sensitivities": 51 + 51 + 9 + 1}
+    for label, k in (("checkpoint_32", 32), ("no_checkpoint", 0)):
+        for _ in range(args.warmup):
+            eng.run_adjoint(cfg, checkpoint_every=k)
+        ms = []
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            sens = eng.run_adjoint(cfg, checkpoint_every=k)
+            ms.append(float(eng.timing_history(1)[0, 3]))
+        out[label] = {"ms": statistics.median(ms)}
+    for _ in range(args.warmup):
+        eng.run(cfg, "mixed", pfe=False)
+    ms = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        v = eng.run(cfg, "mixed", pfe=False)
+        ms.append(float(eng.timing_history(1)[0, 3]))
+    one = statistics.median(ms)
+    out["one_cva_valuation_ms"] = one
+    for label in ("checkpoint_32", "no_checkpoint"):
+        out[label]["cost_in_valuations"] = out[label]["ms"] / one
+    # one-sided bump-and-revalue of the 51 forwards, 9 coefficients and the hazard
+    out["bump_and_revalue_valuations"] = 1 + 51 + 9 + 1
+    out["cva"] = sens.cva
+    out["cva_same_paths_forward"] = v.cva
+    out["dcva_dspot_sum"] = float(np.sum(sens.dcva_dspot))
+    out["dcva_dhazard"] = sens.dcva_dhazard
+    return out
+
+
+def netting_set_run(eng, args, flush) -> dict:
+    """Config 5: 64 payer/receiver swaps (maturities 1-30y) on a 61-tenor curve,
+    3,000 steps, 2,097,152 paths, mixed precision: the netted EE/PFE/CVA
+    valuation and the adjoint, each one fused launch (plus reductions)."""
+    import numpy as np
+    import torch
+
+    from cva_hjm_cuda_gb300 import RunConfig
+    from cva_hjm_cuda_gb300.market import DEFAULT_VOL_COEFFS, nelson_siegel_curve, random_netting_set, tenor_grid
+
+    n, steps = 2_097_152, 3000
+    ns = random_netting_set(64, seed=20261203)
+    eng.set_market_poly(61, 0.5, nelson_siegel_curve(tenor_grid(61, 0.5)), DEFAULT_VOL_COEFFS)
+    eng.set_netting_set(ns)
+    cfg = RunConfig(n_paths=n, n_steps=steps, dt=DT, seed=SEED)
+    for _ in range(args.warmup):
+        eng.enqueue(cfg, "mixed")
+    torch.cuda.synchronize()
+    for _ in range(args.steps):
+        eng.enqueue(cfg, "mixed")
+    v = eng.fetch()
+    hist = eng.timing_history(min(args.steps, 64))
+    val_ms = float(np.median(hist[:, 3]))
+    eng.run_adjoint(cfg, checkpoint_every=32)
+    ms = []
+    for _ in range(max(1, args.steps // 2)):
+        flush.zero_()
+        torch.cuda.synchronize()
+        sens = eng.run_adjoint(cfg, checkpoint_every=32)
+        ms.append(float(eng.timing_history(1)[0, 3]))
+    adj_ms = statistics.median(ms)
+    return {"n_paths": n, "n_steps": steps, "n_tenor": 61, "n_swaps": len(ns), "dates": steps // 50,
+            "valuation_ms": val_ms, "path_steps_per_s": n * steps / (val_ms * 1e-3),
+            "path_kernel_ms": float(np.median(hist[:, 0])), "cva": v.cva, "cva_stderr": v.cva_stderr,
+            "adjoint_ms_checkpoint_32": adj_ms, "adjoint_cost_in_valuations": adj_ms / val_ms,
+            "adjoint_cva": sens.cva}
 
 
 def main() -> None:

@@ -105,7 +105,10 @@ class HJMEngine:
         acc = _f64(swap.accrual)
         self._check(self.lib.hjm_set_swap(self.ctx, swap.notional, swap.strike, _dptr(acc), 1 if swap.payer else 0))
 
-    def set_netting_set(self, notional, fixed_rate, n_periods, payer) -> None:
+    def set_netting_set(self, netting=None, notional=None, fixed_rate=None, n_periods=None, payer=None) -> None:
+        if netting is not None:
+            notional, fixed_rate, n_periods, payer = (netting.notional, netting.fixed_rate, netting.n_periods,
+                                                      netting.payer)
         n = len(notional)
         notional, fixed_rate = _f64(notional), _f64(fixed_rate)
         n_periods = np.ascontiguousarray(n_periods, dtype=np.int32)

@@ -125,9 +125,42 @@ class RunConfig:
     pfe_quantile: float = 0.975
     path_offset: int = 0
 
-    @property
-    def stride(self) -> int:
-        return int(round(0.5 / self.dt))
+
+@dataclass
+class NettingSet:
+    """Swaps on the tenor grid, netted before max(., 0): swap s pays (payer) or
+    receives fixed_rate[s] on notional[s], accruing dtau on periods 1..n_periods[s]."""
+
+    notional: np.ndarray
+    fixed_rate: np.ndarray
+    n_periods: np.ndarray
+    payer: np.ndarray
+
+    def __len__(self) -> int:
+        return len(self.notional)
+
+    def payoff_vectors(self, n_tenor: int, dtau: float = 0.5) -> tuple[np.ndarray, np.ndarray]:
+        """Per-date (payA, payB): the netted cash flow of date i is D_i (payA_i L_i - payB_i)."""
+        a, b = np.zeros(n_tenor), np.zeros(n_tenor)
+        for n, k, m, p in zip(self.notional, self.fixed_rate, self.n_periods, self.payer):
+            sgn = 1.0 if p else -1.0
+            a[1 : m + 1] += sgn * n * dtau
+            b[1 : m + 1] += sgn * n * dtau * k
+        return a, b
+
+
+def random_netting_set(n_swaps: int = 64, seed: int = 20261203, max_years: float = 30.0,
+                       dtau: float = 0.5) -> NettingSet:
+    """Maturities uniform on [1, max_years] snapped to the dtau grid, notionals
+    log-uniform on [1e5, 1e7], fixed rates uniform on [1 %, 4 %], payer/receiver
+    50/50, from a fixed seed."""
+    rng = np.random.default_rng(seed)
+    mat = rng.uniform(1.0, max_years, n_swaps)
+    n_periods = np.clip(np.rint(mat / dtau).astype(np.int32), 1, int(round(max_years / dtau)))
+    notional = np.exp(rng.uniform(np.log(1e5), np.log(1e7), n_swaps))
+    fixed = rng.uniform(0.01, 0.04, n_swaps)
+    payer = (rng.uniform(size=n_swaps) < 0.5).astype(np.int32)
+    return NettingSet(notional, fixed, n_periods, payer)
 
 
 def quantile_rank(q: float, n: int) -> int:

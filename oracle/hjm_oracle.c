@@ -126,6 +126,10 @@ typedef struct {
     double dtau, dt;
     const double *spot, *vol, *drift, *accrual;
     double notional, strike, sign;
+    /* netting set (new, not in the reference): cash flow of date i is
+     * D_i * (payA[i] * L_i - payB[i]), payA = sum of signed notional x accrual,
+     * payB = the same times each swap's fixed rate; NULL = the single swap */
+    const double *payA, *payB;
 } oracle_model;
 
 /* One path: simulation_cpu.h:188-262 called from the block loop at :413-436,
@@ -172,7 +176,10 @@ static void simulate_path(const oracle_model* M, const double* normals_path,
         double forward_rate = numer_x[t];
         double discount_factor = numer_y[t];
         double libor = m * (exp(forward_rate / m) - 1.0);
-        cash_flows[t] = discount_factor * M->notional * M->accrual[t] * ((libor - M->strike) * M->sign);
+        if (M->payA)
+            cash_flows[t] = discount_factor * (M->payA[t] * libor - M->payB[t]);
+        else
+            cash_flows[t] = discount_factor * M->notional * M->accrual[t] * ((libor - M->strike) * M->sign);
     }
     for (int t = 0; t < nt; ++t) {
         double sum = 0.0;
@@ -192,6 +199,7 @@ static int model_init(oracle_model* M, int n_tenor, double dtau, double dt, int 
     M->nt = n_tenor; M->dtau = dtau; M->dt = dt; M->n_steps = n_steps;
     M->spot = spot; M->vol = vol; M->drift = drift; M->accrual = accrual;
     M->notional = notional; M->strike = strike; M->sign = sign;
+    M->payA = NULL; M->payB = NULL;
     return 0;
 }
 
@@ -205,6 +213,23 @@ int oracle_exposure_paths(int n_tenor, double dtau, double dt, int n_steps,
     oracle_model M;
     int rc = model_init(&M, n_tenor, dtau, dt, n_steps, spot, vol, drift, accrual, notional, strike, sign);
     if (rc) return rc;
+    double cf[ORACLE_MAX_TENOR];
+    for (int p = 0; p < n_paths; ++p)
+        simulate_path(&M, normals + (size_t)p * n_steps * 3, exposures + (size_t)p * n_tenor, cf);
+    return 0;
+}
+
+/* The same valuation for a netting set given by its per-date payoff vectors. */
+int oracle_exposure_paths_netting(int n_tenor, double dtau, double dt, int n_steps,
+                                  const double* spot, const double* vol, const double* drift,
+                                  const double* payA, const double* payB,
+                                  int n_paths, const double* normals, double* exposures)
+{
+    oracle_model M;
+    int rc = model_init(&M, n_tenor, dtau, dt, n_steps, spot, vol, drift, payA, 0.0, 0.0, 1.0);
+    if (rc) return rc;
+    M.payA = payA;
+    M.payB = payB;
     double cf[ORACLE_MAX_TENOR];
     for (int p = 0; p < n_paths; ++p)
         simulate_path(&M, normals + (size_t)p * n_steps * 3, exposures + (size_t)p * n_tenor, cf);

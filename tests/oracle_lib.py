@@ -44,6 +44,10 @@ def oracle() -> C.CDLL:
             C.c_int, C.c_double, C.c_double, C.c_int, _dp, _dp, _dp, _dp,
             C.c_double, C.c_double, C.c_double, C.c_int, _dp, _dp,
         ]
+        lib.oracle_exposure_paths_netting.restype = C.c_int
+        lib.oracle_exposure_paths_netting.argtypes = [
+            C.c_int, C.c_double, C.c_double, C.c_int, _dp, _dp, _dp, _dp, _dp, C.c_int, _dp, _dp,
+        ]
         lib.oracle_expected_exposure.restype = None
         lib.oracle_expected_exposure.argtypes = [_dp, C.c_int, C.c_int, _dp]
         lib.oracle_trapezoid_drift.restype = None
@@ -109,6 +113,21 @@ def exposure_paths(market, swap, n_steps: int, dt: float, normals: np.ndarray) -
     )
     if rc != 0:
         raise ValueError(f"oracle_exposure_paths rejected its arguments (rc={rc})")
+    return out
+
+
+def exposure_paths_netting(market, payA, payB, n_steps: int, dt: float, normals: np.ndarray) -> np.ndarray:
+    """Per-path netted exposures for per-date payoff vectors (cash flow D (payA L - payB))."""
+    normals = np.ascontiguousarray(normals, dtype=np.float64)
+    n_paths = normals.shape[0]
+    out = np.zeros((n_paths, market.n_tenor), dtype=np.float64)
+    rc = oracle().oracle_exposure_paths_netting(
+        market.n_tenor, market.dtau, dt, n_steps, market.spot, market.vol.ravel(), market.drift,
+        np.ascontiguousarray(payA, dtype=np.float64), np.ascontiguousarray(payB, dtype=np.float64),
+        n_paths, normals.ravel(), out.ravel(),
+    )
+    if rc != 0:
+        raise ValueError(f"oracle_exposure_paths_netting rejected its arguments (rc={rc})")
     return out
 
 
