@@ -176,7 +176,7 @@ __global__ void __launch_bounds__(kCta, 2)
                 }
             }
             float phi0, phi1, phi2;
-            draw_phi<float, false>(nullptr, gpath, lp, P.n_paths, n, P.key0, P.key1, phi0, phi1, phi2);
+            draw_phi<float, false>(nullptr, gpath, lp, P.n_paths, n, P.rk0, P.rk1, phi0, phi1, phi2);
             euler_step<NT, float>(h, P, c, phi0, phi1, phi2);
 #pragma unroll
             for (int t = 1; t < NT; ++t) pb[t] += h[t];
@@ -281,7 +281,7 @@ __global__ void __launch_bounds__(kCta, 2)
             const double a0 = active ? ck_a[(size_t)sg * ld + lp] : 0.0;
             for (int n = n0; n < n1; ++n) {
                 float phi0, phi1, phi2;
-                draw_phi<float, false>(nullptr, gpath, lp, P.n_paths, n, P.key0, P.key1, phi0, phi1, phi2);
+                draw_phi<float, false>(nullptr, gpath, lp, P.n_paths, n, P.rk0, P.rk1, phi0, phi1, phi2);
                 euler_step<NT, float>(hr, P, c, phi0, phi1, phi2);
 #pragma unroll
                 for (int t = 1; t < NT; ++t) pbr[t] += hr[t];
@@ -335,7 +335,7 @@ __global__ void __launch_bounds__(kCta, 2)
             }
             const float m0 = m0a + m0b, m1 = m1a + m1b, m2 = m2a + m2b;
             float phi0, phi1, phi2;
-            draw_phi<float, false>(nullptr, gpath, lp, P.n_paths, n, P.key0, P.key1, phi0, phi1, phi2);
+            draw_phi<float, false>(nullptr, gpath, lp, P.n_paths, n, P.rk0, P.rk1, phi0, phi1, phi2);
             cbb[0] = fmaf(phi0, m0, cbb[0]);
             cbb[1] = fmaf(phi0, m1, cbb[1]);
             cbb[2] = fmaf(phi0, m2, cbb[2]);

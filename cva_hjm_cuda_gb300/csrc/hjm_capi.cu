@@ -418,6 +418,8 @@ static void fill_params(const hjm_ctx* ctx, const RunShape& sh, int64_t n_paths,
     P.m = 1.0 / ctx->dtau;
     P.key0 = (uint32_t)seed;
     P.key1 = (uint32_t)(seed >> 32);
+    philox_round_keys(P.key0, P.key1, P.rk0, P.rk1);
+    P.inv_c = ctx->dtau / dt;
     P.path_offset = path_offset;
     P.n_paths = n_paths;
     P.ld = ld;
@@ -441,7 +443,8 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
     const bool store = want_pfe || ctx->keep_exposures;
     const int n_dates = sh.B + 1;
     const int R = sh.B + 3;
-    const int64_t n_ctas = (n_paths + kCta - 1) / kCta;
+    const int cta = path_cta(mixed);
+    const int64_t n_ctas = (n_paths + cta - 1) / cta;
     const int64_t ld = (n_paths + 3) / 4 * 4;
     const size_t esize = mixed ? 4 : 8;
 

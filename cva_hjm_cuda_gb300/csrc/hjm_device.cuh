@@ -37,6 +37,33 @@ __host__ __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0, ui
     return c;
 }
 
+#ifdef __CUDACC__
+// The same generator with the ten round keys precomputed on the host (they
+// depend on the seed only, so every thread shares them): the key schedule
+// drops out of the per-thread work and each round is two 32x32->64
+// multiplies and two three-input XORs with a constant-bank operand.
+__device__ __forceinline__ uint4 philox4x32_10_rk(uint4 c, const uint32_t* rk0, const uint32_t* rk1)
+{
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c.x;
+        const uint64_t p1 = (uint64_t)0xCD9E8D57u * c.z;
+        c = make_uint4((uint32_t)(p1 >> 32) ^ c.y ^ rk0[r], (uint32_t)p1, (uint32_t)(p0 >> 32) ^ c.w ^ rk1[r],
+                       (uint32_t)p0);
+    }
+    return c;
+}
+#endif
+
+// Round keys of Philox4x32-10 for a seed: round r uses (k0 + r W0, k1 + r W1).
+__host__ __device__ __forceinline__ void philox_round_keys(uint32_t k0, uint32_t k1, uint32_t* rk0, uint32_t* rk1)
+{
+    for (int r = 0; r < 10; ++r) {
+        rk0[r] = k0 + (uint32_t)r * 0x9E3779B9u;
+        rk1[r] = k1 + (uint32_t)r * 0xBB67AE85u;
+    }
+}
+
 // Counter of the normals of (path, step): (step, stream 0, path lo, path hi).
 __host__ __device__ __forceinline__ uint4 normals_counter(uint64_t path, uint32_t step)
 {
@@ -100,6 +127,8 @@ struct PathParams {
     double dt;
     double m;                    // 1 / dtau: LIBOR from the sampled forward, m (e^{f/m} - 1)
     uint32_t key0, key1;         // Philox key = seed
+    uint32_t rk0[10], rk1[10];   // its round keys
+    double inv_c;                // dtau / dt (FP64 block-sum recovery)
     uint64_t path_offset;        // global index of this launch's first path
     int64_t n_paths;
     int64_t ld;                  // row stride (elements) of the exposure store
@@ -113,7 +142,7 @@ struct PathParams {
 // caller-supplied buffer laid out [step][3][path] (coalesced across threads).
 template <typename T, bool EXT>
 __device__ __forceinline__ void draw_phi(const double* __restrict__ ext, uint64_t gpath, int64_t lp, int64_t n_paths,
-                                         int n, uint32_t key0, uint32_t key1, T& phi0, T& phi1, T& phi2)
+                                         int n, const uint32_t* rk0, const uint32_t* rk1, T& phi0, T& phi1, T& phi2)
 {
     if constexpr (EXT) {
         const size_t np = (size_t)n_paths;
@@ -122,7 +151,7 @@ __device__ __forceinline__ void draw_phi(const double* __restrict__ ext, uint64_
         phi1 = (T)__ldg(ext + base + np);
         phi2 = (T)__ldg(ext + base + 2 * np);
     } else {
-        const uint4 w = philox4x32_10(normals_counter(gpath, (uint32_t)n), key0, key1);
+        const uint4 w = philox4x32_10_rk(normals_counter(gpath, (uint32_t)n), rk0, rk1);
         float z0, z1, z2;
         normals3(w, z0, z1, z2);
         phi0 = (T)z0;

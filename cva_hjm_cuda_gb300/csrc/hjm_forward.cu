@@ -30,47 +30,66 @@ struct Prec;
 template <>
 struct Prec<double> {
     static constexpr bool kMixed = false;
+    static constexpr int kThreads = 64;   // FP64: more shared memory per path, fewer paths per CTA
 };
 template <>
 struct Prec<float> {
     static constexpr bool kMixed = true;
+    static constexpr int kThreads = kCta;
 };
 
 // Shared-memory layout of path_kernel (dynamic), per CTA of kCta threads,
 // column tid private to its thread until the epilogue:
 //   cf_s   [B+1][kCta] T       cash flows of the sampled dates
-//   acc_s  [B+1][kCta] double  FP64 discount accumulators       (mixed only)
-//   work_s [max(NT, B+1)][kCta] T   block partial staging (mixed), then exposures
+//   acc_s  [B+1][kCta] double  FP64 discount sums of the stochastic part per tenor
+//   work_s mixed: [max(NT, B+1)][kCta] float   block-partial staging, then exposures
+//          FP64:  [2(B+2)][kCta] double        curve at block start / end, then exposures
 //   red_s  [2 * kCta/32] double CVA statistics
+__host__ __device__ inline int path_threads(bool mixed) { return mixed ? Prec<float>::kThreads : Prec<double>::kThreads; }
+
 __host__ __device__ inline size_t path_smem_bytes(int nt, int n_blocks, bool mixed)
 {
+    const size_t kCta = (size_t)path_threads(mixed);
     const size_t te = mixed ? 4 : 8;
     const size_t rows = (size_t)n_blocks + 1;
     size_t b = rows * kCta * te;                       // cf_s
-    if (mixed) b += rows * kCta * 8;                   // acc_s
-    const size_t wrows = (mixed && (size_t)nt > rows) ? (size_t)nt : rows;
+    b = (b + 7) & ~(size_t)7;
+    b += rows * kCta * 8;                              // acc_s
+    const size_t wrows = mixed ? ((size_t)nt > rows ? (size_t)nt : rows) : 2 * (rows + 1);
     b = (b + 127) & ~(size_t)127;
     b += wrows * kCta * te;                            // work_s
     b += 2 * (kCta / 32) * 8;                          // red_s
     return b;
 }
 
+// FP64 mode: discount sums by block-sum recovery.  Over one block of Euler
+// steps n = n0 .. n0+stride-1 the states h_n = A h_{n-1} + S phi_n sum to
+//     (I - A) H = S Phi - A (h_end - h_start),   H = sum_n h_n, Phi = sum_n phi_n,
+// and (I - A) H [t] = c (H[t] - H[t+1]) for t below the last tenor.  So with
+// one tenor accumulated directly (H[B], the last tenor still to be sampled),
+//     H[t] = H[t+1] + (sum_k sv[k][t] Phi_k - (A d)[t]) / c,  d = h_end - h_start,
+// gives every block sum the discount needs in O(B) FP64 operations per block
+// instead of one FP64 addition per tenor per step (the FP64 pipe is the bound).
+// Exact in exact arithmetic; in FP64 the recovered sums differ from step-by-
+// step accumulation by ~1e-14 relative.
 template <int NT, typename T, bool EXT>
-__global__ void __launch_bounds__(kCta, Prec<T>::kMixed ? 3 : 1)
+__global__ void __launch_bounds__(Prec<T>::kThreads, Prec<T>::kMixed ? 3 : 4)
     path_kernel(const __grid_constant__ PathParams<T> P, const double* __restrict__ ext,
                 double* __restrict__ partials, T* __restrict__ estore)
 {
     constexpr bool kMixed = Prec<T>::kMixed;
+    constexpr int kCta = Prec<T>::kThreads;  // paths per CTA
     extern __shared__ __align__(128) unsigned char smem[];
     const int tid = threadIdx.x;
     const int B = P.n_blocks;
     const int rows = B + 1;
     T* cf_s = reinterpret_cast<T*>(smem);
-    double* acc_s = reinterpret_cast<double*>(smem + (size_t)rows * kCta * sizeof(T));
-    size_t off = (size_t)rows * kCta * sizeof(T) + (kMixed ? (size_t)rows * kCta * 8 : 0);
+    size_t off = ((size_t)rows * kCta * sizeof(T) + 7) & ~(size_t)7;
+    double* acc_s = reinterpret_cast<double*>(smem + off);
+    off += (size_t)rows * kCta * 8;
     off = (off + 127) & ~(size_t)127;
     T* work_s = reinterpret_cast<T*>(smem + off);
-    const int wrows = (kMixed && NT > rows) ? NT : rows;
+    const int wrows = kMixed ? (NT > rows ? NT : rows) : 2 * (rows + 1);
     double* red_s = reinterpret_cast<double*>(smem + off + (size_t)wrows * kCta * sizeof(T));
 
     const int64_t cta_base = (int64_t)blockIdx.x * kCta;
@@ -82,29 +101,23 @@ __global__ void __launch_bounds__(kCta, Prec<T>::kMixed ? 3 : 1)
     T h[NT];
 #pragma unroll
     for (int t = 0; t < NT; ++t) h[t] = T(0);
+    for (int i = 0; i < rows; ++i) acc_s[i * kCta + tid] = 0.0;
 
-    // discount accumulators of the stochastic part:
-    //   FP64: acc[t] directly; mixed: FP32 block partials pb[t] folded into acc_s
-    double acc[kMixed ? 1 : NT];
+    // mixed: FP32 block partials of the discount sums, folded into acc_s per block
     T pb[kMixed ? NT : 1];
 #pragma unroll
-    for (int t = 0; t < (kMixed ? 1 : NT); ++t) acc[t] = 0.0;
-#pragma unroll
     for (int t = 0; t < (kMixed ? NT : 1); ++t) pb[t] = T(0);
-    if (kMixed)
-        for (int i = 0; i < rows; ++i) acc_s[i * kCta + tid] = 0.0;
+    // FP64: curve at the start / end of the block, tenors 0 .. B+1
+    double* hs_s = reinterpret_cast<double*>(work_s);
+    double* he_s = hs_s + (size_t)(rows + 1) * kCta;
+    if (!kMixed)
+        for (int t = 0; t <= B + 1; ++t) hs_s[t * kCta + tid] = 0.0;
 
     // price date i from the sampled numeraire (x_i, D_i)
     auto sample = [&](int i) {
         const T hi = select_reg<NT, T>(h, i);
-        double a_h;
-        if constexpr (kMixed) {
-            a_h = acc_s[i * kCta + tid];
-        } else {
-            a_h = select_reg<NT, double>(acc, i);
-        }
         const double x = P.psamp[i] + (double)hi;
-        const double a = P.psum[i] + a_h;
+        const double a = P.psum[i] + acc_s[i * kCta + tid];
         T cf;
         if constexpr (kMixed) {
             const float D = expf((float)(-a * P.dt));
@@ -122,19 +135,26 @@ __global__ void __launch_bounds__(kCta, Prec<T>::kMixed ? 3 : 1)
     sample(1);
     const T c = P.c;
     for (int b = 1; b < B; ++b) {
+        double f0 = 0.0, f1 = 0.0, f2 = 0.0, hb = 0.0;  // FP64 mode: block sums of phi_k and of h[B]
         for (int s = 0; s < P.stride; ++s) {
             const int n = b * P.stride + s;
             T phi0, phi1, phi2;
-            draw_phi<T, EXT>(ext, gpath, active ? lp : 0, P.n_paths, n, P.key0, P.key1, phi0, phi1, phi2);
+            draw_phi<T, EXT>(ext, gpath, active ? lp : 0, P.n_paths, n, P.rk0, P.rk1, phi0, phi1, phi2);
             euler_step<NT, T>(h, P, c, phi0, phi1, phi2);
             if constexpr (kMixed) {
+                // only the groups of 8 tenors that meet (b, B] (uniform branches)
 #pragma unroll
-                for (int t = 1; t < NT; ++t) pb[t] += h[t];
+                for (int g = 0; g < NT; g += 8) {
+                    if (g + 7 > b && g <= B) {
+#pragma unroll
+                        for (int t = (g == 0 ? 1 : g); t < g + 8 && t < NT; ++t) pb[t] += h[t];
+                    }
+                }
             } else {
-                // only tenors that are still to be sampled: (b, B]
-#pragma unroll
-                for (int t = 1; t < NT; ++t)
-                    if (t > b && t <= B) acc[t] += h[t];
+                f0 += (double)phi0;
+                f1 += (double)phi1;
+                f2 += (double)phi2;
+                hb += (double)select_reg<NT, T>(h, B);
             }
         }
         if constexpr (kMixed) {
@@ -146,6 +166,25 @@ __global__ void __launch_bounds__(kCta, Prec<T>::kMixed ? 3 : 1)
                 pb[t] = T(0);
             }
             for (int t = b + 1; t <= B; ++t) acc_s[t * kCta + tid] += (double)work_s[t * kCta + tid];
+        } else {
+            // stage the block-end curve, then recover the block sums of tenors (b, B]
+#pragma unroll
+            for (int t = 0; t < NT; ++t)
+                if (t <= B + 1) he_s[t * kCta + tid] = (double)h[t];
+            double Hn = hb;
+            acc_s[B * kCta + tid] += Hn;
+            double dn = he_s[B * kCta + tid] - hs_s[B * kCta + tid];
+            for (int t = B - 1; t > b; --t) {
+                const double d = he_s[t * kCta + tid] - hs_s[t * kCta + tid];
+                const double xi = fma((double)P.sv[2][t], f2, fma((double)P.sv[1][t], f1, (double)P.sv[0][t] * f0));
+                const double ad = fma((double)c, dn - d, d);
+                Hn = fma(xi - ad, P.inv_c, Hn);
+                acc_s[t * kCta + tid] += Hn;
+                dn = d;
+            }
+            double* tmp = hs_s;
+            hs_s = he_s;
+            he_s = tmp;
         }
         sample(b + 1);
     }
@@ -417,8 +456,9 @@ static cudaError_t launch_path_t(const PathParams<T>& P, const double* ext, doub
     auto k = path_kernel<NT, T, EXT>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    const int64_t grid = (P.n_paths + kCta - 1) / kCta;
-    k<<<(unsigned)grid, kCta, smem, s>>>(P, ext, partials, estore);
+    constexpr int cta = Prec<T>::kThreads;
+    const int64_t grid = (P.n_paths + cta - 1) / cta;
+    k<<<(unsigned)grid, cta, smem, s>>>(P, ext, partials, estore);
     return cudaGetLastError();
 }
 
@@ -448,6 +488,8 @@ cudaError_t launch_path_mixed(int nt, const PathParams<float>& P, const double* 
 bool path_tenor_supported(int nt) { return nt == 51 || nt == 61; }
 
 size_t path_smem(int nt, int n_blocks, bool mixed) { return path_smem_bytes(nt, n_blocks, mixed); }
+
+int path_cta(bool mixed) { return path_threads(mixed); }
 
 cudaError_t launch_reduce(const double* partials, int64_t n_rows, int R, double* sums, const FinalParams& F,
                           double* result, cudaStream_t s)

@@ -36,6 +36,7 @@ cudaError_t launch_path_mixed(int nt, const PathParams<float>& P, const double* 
                               float* estore, cudaStream_t s);
 bool path_tenor_supported(int nt);
 size_t path_smem(int nt, int n_blocks, bool mixed);
+int path_cta(bool mixed);  // paths per CTA of the path kernel (one partial-sum row each)
 
 cudaError_t launch_reduce(const double* partials, int64_t n_rows, int R, double* sums, const FinalParams& F,
                           double* result, cudaStream_t s);

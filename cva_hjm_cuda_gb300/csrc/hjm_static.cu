@@ -44,7 +44,8 @@ void set_thread_error(const char* msg);  // hjm_capi.cu: the message hjm_last_er
 
 namespace {
 
-constexpr int64_t kStaticCtas = (HJM_STATIC_MAX_PATHS + kCta - 1) / kCta;
+constexpr int kMinCta = 64;  // the smallest CTA of the path kernels (FP64)
+constexpr int64_t kStaticCtas = (HJM_STATIC_MAX_PATHS + kMinCta - 1) / kMinCta;
 constexpr int kStaticCols = kMaxTenor;                  // partial row: dates + 2 <= 64 doubles
 constexpr size_t kPartialsDoubles = (size_t)kStaticCtas * kStaticCols;
 constexpr size_t kSumsOffset = kPartialsDoubles;        // 2 * kMaxTenor doubles
@@ -68,7 +69,7 @@ hjm_status static_fail(hjm_status st, const char* fmt, ...)
 
 }  // namespace
 
-// The scratch: 4.2 MB of FP64 per device (HJM_STATIC_MAX_PATHS / 128 CTA rows
+// The scratch: 8.4 MB of FP64 per device (HJM_STATIC_MAX_PATHS / 64 CTA rows
 // of 64 partial sums, plus column sums and the result block).
 static __device__ __align__(256) double g_hjm_static_scratch[kScratchDoubles];
 
@@ -156,6 +157,8 @@ static void static_params(int nt, double dtau, const double* spot, const double*
     P.m = 1.0 / dtau;
     P.key0 = (uint32_t)seed;
     P.key1 = (uint32_t)(seed >> 32);
+    philox_round_keys(P.key0, P.key1, P.rk0, P.rk1);
+    P.inv_c = dtau / dt;
     P.path_offset = path_offset;
     P.n_paths = n_paths;
     P.ld = 0;
@@ -210,7 +213,8 @@ hjm_status hjm_run_static(void* cuda_stream, int32_t n_tenor, double dtau, const
         return static_fail(HJM_ERR_INVALID_ARGUMENT, "%d sampled dates need %d tenors; the grid has %d", B, B + 1,
                            n_tenor);
     const int R = B + 3;
-    const int64_t n_ctas = (n_paths + kCta - 1) / kCta;
+    const int cta = path_cta(precision == HJM_PRECISION_MIXED);
+    const int64_t n_ctas = (n_paths + cta - 1) / cta;
     if (R > kStaticCols || n_ctas > kStaticCtas)
         return static_fail(HJM_ERR_INVALID_ARGUMENT, "run exceeds the static scratch");
 

@@ -161,7 +161,7 @@ hjm_status hjm_run_adjoint(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, doubl
  * context: all inputs are host arrays (as for hjm_set_market / hjm_set_swap /
  * hjm_run), the work is enqueued on cuda_stream (NULL = the legacy default
  * stream) and the call returns when ee_out [n_tenor] and cva_out
- * [HJM_CVA_OUT_LEN] hold the results.  Its scratch is a fixed 4.2 MB static
+ * [HJM_CVA_OUT_LEN] hold the results.  Its scratch is a fixed 8.4 MB static
  * device array that each GPU loading the library keeps until exit; it calls
  * no cudaMalloc, cudaFree or allocating library routine.  Limits: at most
  * HJM_STATIC_MAX_PATHS paths per call (larger runs fail with
