@@ -464,13 +464,15 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
     ctx->ev = ctx->ring[ctx->n_enqueued % hjm_ctx::kRing];
     ctx->n_enqueued++;
     ctx->stat_launches = 3;  // path kernel, column reduction, finalisation
-    ctx->stat_h2d = (mixed ? sizeof(PathParams<float>) : sizeof(PathParams<double>)) + sizeof(FinalParams);
+    ctx->stat_h2d = (mixed ? sizeof(MixedParams) : sizeof(PathParams<double>)) + sizeof(FinalParams);
     ctx->stat_d2h = 0;
     HJM_CUDA(ctx, cudaEventRecord(ctx->ev[0], s));
     if (mixed) {
         PathParams<float> P;
         fill_params<float>(ctx, sh, n_paths, dt, seed, path_offset, hazard, recovery, ld, store, P, F);
-        HJM_CUDA(ctx, launch_path_mixed(ctx->nt, P, ext_dev, (double*)ctx->partials.p,
+        MixedParams M;
+        pack_mixed_params(ctx->nt, P, M);
+        HJM_CUDA(ctx, launch_path_mixed(ctx->nt, M, ext_dev, (double*)ctx->partials.p,
                                         store ? (float*)ctx->estore.p : nullptr, s));
     } else {
         PathParams<double> P;

@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstring>
 
 #include "hjm_device.cuh"
 #include "hjm_kernels.h"
@@ -247,6 +248,225 @@ __global__ void __launch_bounds__(Prec<T>::kThreads, Prec<T>::kMixed ? 3 : 4)
             asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
         }
     }
+}
+
+// ---------------------------------------------------------------------------
+// Mixed precision with packed FP32x2 arithmetic.  The curve of one path is held
+// as H = ceil(NT/2) float2 pairs, pair p = {h[p], h[p+H]}: the upwind neighbour
+// h[t+1] of every tenor lies in the same component of pair p+1, so each packed
+// FMA (__ffma2_rn) advances two tenors and the Euler step costs half the issue
+// slots of the scalar form.  Only the seam pair (p = H-1, whose .x neighbour is
+// pair 0's .y), the pair holding the last tenor (backward difference) and the
+// padding tenor of an odd grid take scalar fix-ups.  Every element sees exactly
+// the scalar kernel's operations (fma(sv, phi, h) three times, one rounded
+// difference, fma(c, d, x)), so the results are bit-identical to it.
+// ---------------------------------------------------------------------------
+template <int NT>
+struct PairGrid {
+    static constexpr int H = (NT + 1) / 2;  // pairs
+    static constexpr int L = NT - 1;        // last tenor
+};
+
+template <int NT>
+__device__ __forceinline__ void euler_step_pairs(float2 (&h)[PairGrid<NT>::H], const MixedParams& M, float phi0,
+                                                 float phi1, float phi2)
+{
+    constexpr int H = PairGrid<NT>::H, L = PairGrid<NT>::L;
+    const float2 f0 = make_float2(phi0, phi0), f1 = make_float2(phi1, phi1), f2 = make_float2(phi2, phi2);
+    const float2 m1 = make_float2(-1.0f, -1.0f);
+    float2 hn[H];
+#pragma unroll
+    for (int p = 0; p < H; ++p) {
+        float2 x = __ffma2_rn(M.svp[0][p], f0, h[p]);
+        x = __ffma2_rn(M.svp[1][p], f1, x);
+        x = __ffma2_rn(M.svp[2][p], f2, x);
+        const int q = H + p;  // tenor held in .y
+        float2 d;
+        if (p + 1 < H && q < L) {
+            d = __ffma2_rn(m1, h[p], h[p + 1]);  // h[t+1] - h[t] for both tenors, one rounding each
+        } else {
+            d.x = ((p + 1 < H) ? h[p + 1].x : h[0].y) - h[p].x;
+            if (q < L)
+                d.y = h[p + 1].y - h[p].y;
+            else if (q == L)
+                d.y = h[p].y - h[p - 1].y;  // backward difference at the last tenor
+            else
+                d.y = 0.0f;                 // padding tenor of an odd grid: stays zero
+        }
+        hn[p] = __ffma2_rn(M.cp, d, x);
+    }
+#pragma unroll
+    for (int p = 0; p < H; ++p) h[p] = hn[p];
+}
+
+template <int NT>
+__device__ __forceinline__ float select_pair(const float2 (&h)[PairGrid<NT>::H], int i)
+{
+    constexpr int H = PairGrid<NT>::H;
+    float r = 0.0f;
+#pragma unroll
+    for (int p = 0; p < H; ++p) {
+        r = (p == i) ? h[p].x : r;
+        r = (p + H == i) ? h[p].y : r;
+    }
+    return r;
+}
+
+// Mixed-precision discount sums: FP32 block sums by the same recovery as the
+// FP64 kernel, but anchored at tenor 1 and run upwards,
+//     H[t+1] = H[t] - (sum_k sv[k][t] Phi_k - (A d)[t]) / c,   t = 1 .. B-1,
+// so a block costs O(B) scalar FP32 operations and four additions per step
+// (Phi_k and H[1]) instead of an addition per tenor per step; the FP32 block
+// sums are then folded into FP64 per tenor.  The recovered sums differ from
+// step-by-step FP32 accumulation by ~1e-6 relative (the FP32 rounding of the
+// Euler steps divided by c), far inside the mixed-precision tolerance.
+//
+// Shared memory per thread: acc (B+1) FP64 discount sums, whose slot i holds
+// date i's cash flow once tenor i is sampled; hs (B+2) FP32 curve at the block
+// start, reused for the exposure tile at the end.
+template <int NT, bool EXT>
+__global__ void __launch_bounds__(kCta, 4)
+    path_kernel_mixed(const __grid_constant__ MixedParams M, const double* __restrict__ ext,
+                      double* __restrict__ partials, float* __restrict__ estore)
+{
+    constexpr int H = PairGrid<NT>::H;
+    const PathParams<float>& P = M.P;
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int tid = threadIdx.x;
+    const int B = P.n_blocks;
+    const int rows = B + 1;
+    double* acc_s = reinterpret_cast<double*>(smem);                       // [B+1][kCta]
+    float* hs_s = reinterpret_cast<float*>(smem + (size_t)rows * kCta * 8);  // [B+2][kCta]
+    double* red_s = reinterpret_cast<double*>(smem + (size_t)rows * kCta * 8 + (size_t)(rows + 1) * kCta * 4);
+
+    const int64_t cta_base = (int64_t)blockIdx.x * kCta;
+    const int64_t lp = cta_base + tid;
+    const bool active = lp < P.n_paths;
+    const uint64_t gpath = P.path_offset + (uint64_t)lp;
+
+    float2 h[H];
+#pragma unroll
+    for (int p = 0; p < H; ++p) h[p] = make_float2(0.f, 0.f);
+    for (int i = 0; i < rows; ++i) acc_s[i * kCta + tid] = 0.0;
+    for (int t = 0; t <= B + 1; ++t) hs_s[t * kCta + tid] = 0.f;
+
+    // tenor t of the packed curve (t static after unrolling)
+    auto ht = [&](int t) -> float { return t < H ? h[t].x : h[t - H].y; };
+
+    auto sample = [&](int i) {
+        const double x = P.psamp[i] + (double)select_pair<NT>(h, i);
+        const double a = P.psum[i] + acc_s[i * kCta + tid];
+        const float D = expf((float)(-a * P.dt));
+        const float mm = (float)P.m;
+        const float L = mm * expm1f((float)x / mm);
+        acc_s[i * kCta + tid] = (double)(D * ((float)P.payA[i] * L - (float)P.payB[i]));  // cash flow of date i
+    };
+
+    sample(1);
+    const float c = P.c, inv_c = (float)P.inv_c;
+    for (int b = 1; b < B; ++b) {
+        float F0 = 0.f, F1 = 0.f, F2 = 0.f, H1 = 0.f;  // block sums of phi_k and of h[1]
+        for (int s = 0; s < P.stride; ++s) {
+            const int n = b * P.stride + s;
+            float phi0, phi1, phi2;
+            draw_phi<float, EXT>(ext, gpath, active ? lp : 0, P.n_paths, n, P.rk0, P.rk1, phi0, phi1, phi2);
+            euler_step_pairs<NT>(h, M, phi0, phi1, phi2);
+            F0 += phi0;
+            F1 += phi1;
+            F2 += phi2;
+            H1 += h[1].x;
+        }
+        // recover the block sums of tenors 2 .. B upwards from H[1]; fold (b, B] into FP64
+        float Hn = H1;
+        float d = ht(1) - hs_s[1 * kCta + tid];
+#pragma unroll
+        for (int t = 1; t < NT - 1; ++t) {
+            if (t >= B) break;
+            const float dn = ht(t + 1) - hs_s[(t + 1) * kCta + tid];
+            const float xi = fmaf(P.sv[2][t], F2, fmaf(P.sv[1][t], F1, P.sv[0][t] * F0));
+            const float ad = fmaf(c, dn - d, d);
+            Hn = fmaf(ad - xi, inv_c, Hn);  // H[t+1]
+            if (t + 1 > b) acc_s[(t + 1) * kCta + tid] += (double)Hn;
+            d = dn;
+        }
+        // the block-end curve is the next block's start (tenors 1 .. B+1)
+#pragma unroll
+        for (int t = 1; t < NT; ++t)
+            if (t <= B + 1) hs_s[t * kCta + tid] = ht(t);
+        sample(b + 1);
+    }
+
+    float* e_s = hs_s;  // [B+1][kCta] exposures
+    double v = 0.0, cva_c = 0.0;
+    e_s[B * kCta + tid] = 0.f;
+    for (int j = B - 1; j >= 0; --j) {
+        v += acc_s[(j + 1) * kCta + tid];
+        double e = (v > 0.0) ? v : 0.0;
+        if (!active) e = 0.0;
+        e_s[j * kCta + tid] = (float)e;
+        cva_c = fma(P.cvaw[j], e, cva_c);
+    }
+    __syncthreads();
+
+    const int warp = tid >> 5, lane = tid & 31;
+    const int R = B + 3;
+    for (int j = warp; j <= B; j += kCta / 32) {
+        double sum = 0.0;
+#pragma unroll
+        for (int q = 0; q < kCta / 32; ++q) sum += (double)e_s[j * kCta + lane + 32 * q];
+        sum = warp_sum(sum);
+        if (lane == 0) partials[(size_t)blockIdx.x * R + j] = sum;
+    }
+    {
+        const double s1 = warp_sum(cva_c), s2 = warp_sum(cva_c * cva_c);
+        if (lane == 0) {
+            red_s[warp] = s1;
+            red_s[kCta / 32 + warp] = s2;
+        }
+    }
+    if (P.store_exposures) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+        double s1 = 0.0, s2 = 0.0;
+        for (int w = 0; w < kCta / 32; ++w) {
+            s1 += red_s[w];
+            s2 += red_s[kCta / 32 + w];
+        }
+        partials[(size_t)blockIdx.x * R + B + 1] = s1;
+        partials[(size_t)blockIdx.x * R + B + 2] = s2;
+        if (P.store_exposures) {
+            const int64_t cnt = (P.n_paths - cta_base < kCta) ? (P.n_paths - cta_base) : kCta;
+            const uint32_t bytes = (uint32_t)(((cnt + 3) / 4) * 4 * sizeof(float));
+            for (int j = 0; j <= B; ++j) {
+                float* dst = estore + (size_t)j * (size_t)P.ld + (size_t)cta_base;
+                const uint32_t src = (uint32_t)__cvta_generic_to_shared(e_s + (size_t)j * kCta);
+                asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
+                             :: "l"(dst), "r"(src), "r"(bytes) : "memory");
+            }
+            asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+            asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+        }
+    }
+}
+
+__host__ __device__ inline size_t mixed_smem_bytes(int nt, int n_blocks)
+{
+    (void)nt;
+    const size_t rows = (size_t)n_blocks + 1;
+    return rows * kCta * 8 + (rows + 1) * kCta * 4 + 2 * (kCta / 32) * 8;
+}
+
+void pack_mixed_params(int nt, const PathParams<float>& P, MixedParams& M)
+{
+    std::memset(&M, 0, sizeof(M));
+    M.P = P;
+    const int H = (nt + 1) / 2;
+    for (int k = 0; k < kFactors; ++k)
+        for (int p = 0; p < H; ++p) {
+            M.svp[k][p].x = P.sv[k][p];
+            M.svp[k][p].y = (H + p < nt) ? P.sv[k][H + p] : 0.0f;
+        }
+    M.cp = make_float2(P.c, P.c);
 }
 
 // ---------------------------------------------------------------------------
@@ -479,15 +699,35 @@ cudaError_t launch_path_fp64(int nt, const PathParams<double>& P, const double* 
     return launch_path_nt<double>(nt, P, ext, partials, estore, s);
 }
 
-cudaError_t launch_path_mixed(int nt, const PathParams<float>& P, const double* ext, double* partials,
-                              float* estore, cudaStream_t s)
+template <int NT, bool EXT>
+static cudaError_t launch_mixed_t(const MixedParams& M, const double* ext, double* partials, float* estore,
+                                  cudaStream_t s)
 {
-    return launch_path_nt<float>(nt, P, ext, partials, estore, s);
+    const size_t smem = mixed_smem_bytes(NT, M.P.n_blocks);
+    auto k = path_kernel_mixed<NT, EXT>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const int64_t grid = (M.P.n_paths + kCta - 1) / kCta;
+    k<<<(unsigned)grid, kCta, smem, s>>>(M, ext, partials, estore);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_path_mixed(int nt, const MixedParams& M, const double* ext, double* partials, float* estore,
+                              cudaStream_t s)
+{
+    if (nt == 51) return ext ? launch_mixed_t<51, true>(M, ext, partials, estore, s)
+                             : launch_mixed_t<51, false>(M, ext, partials, estore, s);
+    if (nt == 61) return ext ? launch_mixed_t<61, true>(M, ext, partials, estore, s)
+                             : launch_mixed_t<61, false>(M, ext, partials, estore, s);
+    return cudaErrorInvalidValue;
 }
 
 bool path_tenor_supported(int nt) { return nt == 51 || nt == 61; }
 
-size_t path_smem(int nt, int n_blocks, bool mixed) { return path_smem_bytes(nt, n_blocks, mixed); }
+size_t path_smem(int nt, int n_blocks, bool mixed)
+{
+    return mixed ? mixed_smem_bytes(nt, n_blocks) : path_smem_bytes(nt, n_blocks, false);
+}
 
 int path_cta(bool mixed) { return path_threads(mixed); }
 

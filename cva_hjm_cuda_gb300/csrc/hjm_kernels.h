@@ -30,10 +30,21 @@ struct SelState {
     uint64_t prefix, mask, k;
 };
 
+// Mixed-precision path kernel parameters: the FP32 parameter block plus the
+// volatility coefficients packed in tenor pairs {tenor p, tenor p + ceil(NT/2)}
+// for the packed FP32x2 FMA (two tenors per instruction).
+struct MixedParams {
+    PathParams<float> P;
+    float2 svp[kFactors][kMaxTenor / 2];
+    float2 cp;  // {c, c}
+};
+
+
 cudaError_t launch_path_fp64(int nt, const PathParams<double>& P, const double* ext, double* partials,
                              double* estore, cudaStream_t s);
-cudaError_t launch_path_mixed(int nt, const PathParams<float>& P, const double* ext, double* partials,
-                              float* estore, cudaStream_t s);
+cudaError_t launch_path_mixed(int nt, const MixedParams& M, const double* ext, double* partials, float* estore,
+                              cudaStream_t s);
+void pack_mixed_params(int nt, const PathParams<float>& P, MixedParams& M);
 bool path_tenor_supported(int nt);
 size_t path_smem(int nt, int n_blocks, bool mixed);
 int path_cta(bool mixed);  // paths per CTA of the path kernel (one partial-sum row each)
