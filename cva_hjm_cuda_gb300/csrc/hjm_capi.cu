@@ -713,7 +713,7 @@ hjm_status hjm_run_adjoint(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, doubl
     const size_t smem = adjoint_smem(nt, B);
     if (smem > 227 * 1024) return fail(ctx, HJM_ERR_UNSUPPORTED, "adjoint shared memory %zu B exceeds 227 KB", smem);
     HJM_CUDA(ctx, cudaSetDevice(ctx->device));
-    const int64_t n_ctas = (n_paths + kCta - 1) / kCta;
+    const int64_t n_ctas = (n_paths + adjoint_cta() - 1) / adjoint_cta();
     const int64_t ld = (n_paths + 3) / 4 * 4;
     const int E = n_steps - sh.stride;
     const int K = checkpoint_every;
@@ -728,11 +728,17 @@ hjm_status hjm_run_adjoint(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, doubl
     AdjParams A;
     FinalParams F;
     std::memset(&A, 0, sizeof(A));
-    fill_params<float>(ctx, sh, n_paths, dt, seed, path_offset, hazard_rate, recovery, 0, false, A.P, F);
-    for (int t = 0; t < nt; ++t) {
-        const double T = ctx->dtau * t;
-        A.tau[t] = (float)T;
-        A.tau2[t] = (float)(T * T);
+    {
+        PathParams<float> P;
+        fill_params<float>(ctx, sh, n_paths, dt, seed, path_offset, hazard_rate, recovery, 0, false, P, F);
+        pack_mixed_params(nt, P, A.M);
+    }
+    const int Hp = (nt + 1) / 2;
+    for (int p = 0; p < Hp; ++p) {
+        const double T0 = ctx->dtau * p, T1 = ctx->dtau * (p + Hp);
+        const bool pad = p + Hp >= nt;
+        A.taup[p] = make_float2((float)T0, pad ? 0.f : (float)T1);
+        A.tau2p[p] = make_float2((float)(T0 * T0), pad ? 0.f : (float)(T1 * T1));
     }
     A.ckpt_every = K;
     A.ck_ld = ld;

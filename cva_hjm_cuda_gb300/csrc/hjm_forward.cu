@@ -23,6 +23,7 @@
 
 #include "hjm_device.cuh"
 #include "hjm_kernels.h"
+#include "hjm_pairs.cuh"
 
 namespace hjm {
 
@@ -261,57 +262,6 @@ __global__ void __launch_bounds__(Prec<T>::kThreads, Prec<T>::kMixed ? 3 : 4)
 // the scalar kernel's operations (fma(sv, phi, h) three times, one rounded
 // difference, fma(c, d, x)), so the results are bit-identical to it.
 // ---------------------------------------------------------------------------
-template <int NT>
-struct PairGrid {
-    static constexpr int H = (NT + 1) / 2;  // pairs
-    static constexpr int L = NT - 1;        // last tenor
-};
-
-template <int NT>
-__device__ __forceinline__ void euler_step_pairs(float2 (&h)[PairGrid<NT>::H], const MixedParams& M, float phi0,
-                                                 float phi1, float phi2)
-{
-    constexpr int H = PairGrid<NT>::H, L = PairGrid<NT>::L;
-    const float2 f0 = make_float2(phi0, phi0), f1 = make_float2(phi1, phi1), f2 = make_float2(phi2, phi2);
-    const float2 m1 = make_float2(-1.0f, -1.0f);
-    float2 hn[H];
-#pragma unroll
-    for (int p = 0; p < H; ++p) {
-        float2 x = __ffma2_rn(M.svp[0][p], f0, h[p]);
-        x = __ffma2_rn(M.svp[1][p], f1, x);
-        x = __ffma2_rn(M.svp[2][p], f2, x);
-        const int q = H + p;  // tenor held in .y
-        float2 d;
-        if (p + 1 < H && q < L) {
-            d = __ffma2_rn(m1, h[p], h[p + 1]);  // h[t+1] - h[t] for both tenors, one rounding each
-        } else {
-            d.x = ((p + 1 < H) ? h[p + 1].x : h[0].y) - h[p].x;
-            if (q < L)
-                d.y = h[p + 1].y - h[p].y;
-            else if (q == L)
-                d.y = h[p].y - h[p - 1].y;  // backward difference at the last tenor
-            else
-                d.y = 0.0f;                 // padding tenor of an odd grid: stays zero
-        }
-        hn[p] = __ffma2_rn(M.cp, d, x);
-    }
-#pragma unroll
-    for (int p = 0; p < H; ++p) h[p] = hn[p];
-}
-
-template <int NT>
-__device__ __forceinline__ float select_pair(const float2 (&h)[PairGrid<NT>::H], int i)
-{
-    constexpr int H = PairGrid<NT>::H;
-    float r = 0.0f;
-#pragma unroll
-    for (int p = 0; p < H; ++p) {
-        r = (p == i) ? h[p].x : r;
-        r = (p + H == i) ? h[p].y : r;
-    }
-    return r;
-}
-
 // Mixed-precision discount sums: FP32 block sums by the same recovery as the
 // FP64 kernel, but anchored at tenor 1 and run upwards,
 //     H[t+1] = H[t] - (sum_k sv[k][t] Phi_k - (A d)[t]) / c,   t = 1 .. B-1,
@@ -363,7 +313,6 @@ __global__ void __launch_bounds__(kCta, 4)
     };
 
     sample(1);
-    const float c = P.c, inv_c = (float)P.inv_c;
     for (int b = 1; b < B; ++b) {
         float F0 = 0.f, F1 = 0.f, F2 = 0.f, H1 = 0.f;  // block sums of phi_k and of h[1]
         for (int s = 0; s < P.stride; ++s) {
@@ -377,18 +326,9 @@ __global__ void __launch_bounds__(kCta, 4)
             H1 += h[1].x;
         }
         // recover the block sums of tenors 2 .. B upwards from H[1]; fold (b, B] into FP64
-        float Hn = H1;
-        float d = ht(1) - hs_s[1 * kCta + tid];
-#pragma unroll
-        for (int t = 1; t < NT - 1; ++t) {
-            if (t >= B) break;
-            const float dn = ht(t + 1) - hs_s[(t + 1) * kCta + tid];
-            const float xi = fmaf(P.sv[2][t], F2, fmaf(P.sv[1][t], F1, P.sv[0][t] * F0));
-            const float ad = fmaf(c, dn - d, d);
-            Hn = fmaf(ad - xi, inv_c, Hn);  // H[t+1]
-            if (t + 1 > b) acc_s[(t + 1) * kCta + tid] += (double)Hn;
-            d = dn;
-        }
+        recover_sums_up<NT>(h, hs_s, tid, kCta, P, F0, F1, F2, H1, B, [&](int t, float Ht) {
+            if (t > b) acc_s[t * kCta + tid] += (double)Ht;
+        });
         // the block-end curve is the next block's start (tenors 1 .. B+1)
 #pragma unroll
         for (int t = 1; t < NT; ++t)

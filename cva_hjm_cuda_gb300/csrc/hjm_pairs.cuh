@@ -1,0 +1,137 @@
+// hjm_pairs.cuh -- packed FP32x2 helpers shared by the mixed-precision path
+// kernel and the adjoint kernel.
+//
+// The curve of one path is held as H = ceil(NT/2) float2 pairs, pair p =
+// {h[p], h[p+H]}; both upwind neighbours (h[t+1] in the Euler step, g[t-1] in
+// its adjoint) of nearly every tenor lie in the same component of the next or
+// previous pair, so one packed FMA (__ffma2_rn) serves two tenors.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "hjm_device.cuh"
+#include "hjm_kernels.h"
+
+namespace hjm {
+
+template <int NT>
+struct PairGrid {
+    static constexpr int H = (NT + 1) / 2;  // pairs
+    static constexpr int L = NT - 1;        // last tenor
+};
+
+template <int NT>
+__device__ __forceinline__ void euler_step_pairs(float2 (&h)[PairGrid<NT>::H], const MixedParams& M, float phi0,
+                                                 float phi1, float phi2)
+{
+    constexpr int H = PairGrid<NT>::H, L = PairGrid<NT>::L;
+    const float2 f0 = make_float2(phi0, phi0), f1 = make_float2(phi1, phi1), f2 = make_float2(phi2, phi2);
+    const float2 m1 = make_float2(-1.0f, -1.0f);
+    float2 hn[H];
+#pragma unroll
+    for (int p = 0; p < H; ++p) {
+        float2 x = __ffma2_rn(M.svp[0][p], f0, h[p]);
+        x = __ffma2_rn(M.svp[1][p], f1, x);
+        x = __ffma2_rn(M.svp[2][p], f2, x);
+        const int q = H + p;  // tenor held in .y
+        float2 d;
+        if (p + 1 < H && q < L) {
+            d = __ffma2_rn(m1, h[p], h[p + 1]);  // h[t+1] - h[t] for both tenors, one rounding each
+        } else {
+            d.x = ((p + 1 < H) ? h[p + 1].x : h[0].y) - h[p].x;
+            if (q < L)
+                d.y = h[p + 1].y - h[p].y;
+            else if (q == L)
+                d.y = h[p].y - h[p - 1].y;  // backward difference at the last tenor
+            else
+                d.y = 0.0f;                 // padding tenor of an odd grid: stays zero
+        }
+        hn[p] = __ffma2_rn(M.cp, d, x);
+    }
+#pragma unroll
+    for (int p = 0; p < H; ++p) h[p] = hn[p];
+}
+
+template <int NT>
+__device__ __forceinline__ float select_pair(const float2 (&h)[PairGrid<NT>::H], int i)
+{
+    constexpr int H = PairGrid<NT>::H;
+    float r = 0.0f;
+#pragma unroll
+    for (int p = 0; p < H; ++p) {
+        r = (p == i) ? h[p].x : r;
+        r = (p + H == i) ? h[p].y : r;
+    }
+    return r;
+}
+
+// Tenor t (compile-time after unrolling) of a packed curve.
+template <int NT>
+__device__ __forceinline__ float pair_tenor(const float2 (&h)[PairGrid<NT>::H], int t)
+{
+    constexpr int H = PairGrid<NT>::H;
+    return t < H ? h[t].x : h[t - H].y;
+}
+
+// Block-sum recovery in FP32, upwards from the anchor tenor 1.  Over a run of
+// Euler steps, with Phi_k the sums of the normals, H1 the sum of h[1] and
+// d = h_now - h_start (h_start in hs_s, thread column tid, stride cta),
+//     H[t+1] = H[t] + ((A d)[t] - sum_k sv[k][t] Phi_k) / c,   t = 1 .. tmax-1,
+// and fold(t, H[t]) is called for t = 2 .. tmax (tmax <= NT-1).
+template <int NT, typename Fold>
+__device__ __forceinline__ void recover_sums_up(const float2 (&h)[PairGrid<NT>::H], const float* hs_s, int tid,
+                                                int cta, const PathParams<float>& P, float F0, float F1, float F2,
+                                                float H1, int tmax, Fold fold)
+{
+    const float c = P.c, inv_c = (float)P.inv_c;
+    float Hn = H1;
+    float d = pair_tenor<NT>(h, 1) - hs_s[1 * cta + tid];
+#pragma unroll
+    for (int t = 1; t < NT - 1; ++t) {
+        if (t >= tmax) break;
+        const float dn = pair_tenor<NT>(h, t + 1) - hs_s[(t + 1) * cta + tid];
+        const float xi = fmaf(P.sv[2][t], F2, fmaf(P.sv[1][t], F1, P.sv[0][t] * F0));
+        const float ad = fmaf(c, dn - d, d);
+        Hn = fmaf(ad - xi, inv_c, Hn);
+        fold(t + 1, Hn);
+        d = dn;
+    }
+}
+
+// g <- A^T g on the packed adjoint state (A: the upwind convection of the Euler
+// step).  Per tenor, with L the last tenor:
+//   t = 0:          (1 - c) g[0]
+//   1 <= t <= L-2:  g[t] + c (g[t-1] - g[t])
+//   t = L-1:        g[t] + c (g[t-1] - g[t]) - c g[L]
+//   t = L:          g[L] + c (g[L] + g[L-1])
+template <int NT>
+__device__ __forceinline__ void adjoint_convection_pairs(float2 (&g)[PairGrid<NT>::H], float2 cp)
+{
+    constexpr int H = PairGrid<NT>::H, L = PairGrid<NT>::L;
+    const float c = cp.x;
+    const float2 m1 = make_float2(-1.0f, -1.0f);
+    float2 gn[H];
+#pragma unroll
+    for (int p = 0; p < H; ++p) {
+        const int q = H + p;
+        if (p >= 1 && q < L - 1) {
+            gn[p] = __ffma2_rn(cp, __ffma2_rn(m1, g[p], g[p - 1]), g[p]);
+        } else {
+            gn[p].x = (p == 0) ? fmaf(-c, g[0].x, g[0].x) : fmaf(c, g[p - 1].x - g[p].x, g[p].x);
+            const float gprev = (p == 0) ? g[H - 1].x : g[p - 1].y;  // tenor q-1
+            if (q < L - 1) {
+                gn[p].y = fmaf(c, gprev - g[p].y, g[p].y);
+            } else if (q == L - 1) {
+                gn[p].y = fmaf(-c, g[p + 1].y, fmaf(c, gprev - g[p].y, g[p].y));
+            } else if (q == L) {
+                gn[p].y = fmaf(c, g[p].y + gprev, g[p].y);
+            } else {
+                gn[p].y = 0.0f;  // padding tenor
+            }
+        }
+    }
+#pragma unroll
+    for (int p = 0; p < H; ++p) g[p] = gn[p];
+}
+
+}  // namespace hjm

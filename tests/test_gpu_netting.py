@@ -79,7 +79,7 @@ def test_netting_adjoint_vs_fp64_finite_differences(engine):
     engine.set_netting_set(ns)
     sens = engine.run_adjoint(cfg, checkpoint_every=32)
     v = engine.run(cfg, "mixed", pfe=False)
-    assert sens.cva == pytest.approx(v.cva, rel=1e-5)
+    assert sens.cva == v.cva
     gmax = np.max(np.abs(sens.dcva_dspot))
     for t in (2, 10, 30, 45, 60):
         h = 1e-5
