@@ -42,10 +42,16 @@ METRIC = "HJM path-steps/s and CVA+deltas time: FP32-mixed vs FP64 on 1 GB300 @1
 UNIT = "path-steps/s"
 N_STEPS, DT, SEED = 1000, 0.01, 1234
 WORKLOADS = {
-    "fp64": {"precision": "fp64", "n_paths": 1_048_576, "dtype": "f64",
+    "fp64": {"precision": "fp64", "n_paths": 1_048_576, "dtype": "f64", "n_tenor": 51, "n_steps": 1000,
              "name": "hjm-3f-51tenor-payer-irs-10y-fp64-1048576paths-1000steps"},
-    "mixed": {"precision": "mixed", "n_paths": 4_194_304, "dtype": "f32+f64",
+    "mixed": {"precision": "mixed", "n_paths": 4_194_304, "dtype": "f32+f64", "n_tenor": 51, "n_steps": 1000,
               "name": "hjm-3f-51tenor-payer-irs-10y-mixed-4194304paths-1000steps"},
+    # CVA plus 112 sensitivities by the pathwise adjoint, checkpoints every 32 steps
+    "adjoint": {"precision": "mixed", "n_paths": 1_048_576, "dtype": "f32+f64", "n_tenor": 51, "n_steps": 1000,
+                "name": "hjm-3f-51tenor-payer-irs-10y-adjoint-ckpt32-1048576paths-1000steps"},
+    # 64-swap netting set on a 61-tenor curve, mixed precision
+    "netting": {"precision": "mixed", "n_paths": 2_097_152, "dtype": "f32+f64", "n_tenor": 61, "n_steps": 3000,
+                "name": "hjm-3f-61tenor-netting64-30y-mixed-2097152paths-3000steps"},
 }
 FLUSH_BYTES = 256 << 20
 
@@ -206,21 +212,39 @@ def run_ours(args) -> None:
     wl = WORKLOADS[args.workload]
     n_paths = args.paths or wl["n_paths"]
     prec = wl["precision"]
-    mk, sw = Market(), Swap()
+    n_steps = wl["n_steps"]
+    mk, sw = Market(n_tenor=wl["n_tenor"]), Swap(n_tenor=wl["n_tenor"])
     stride = int(round(mk.dtau / DT))
     eng = HJMEngine(local_rank)
     # a dedicated (non-default) stream: the engine and the timing events share it
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     eng.set_stream(stream.cuda_stream)
-    eng.set_market(mk)
-    eng.set_swap(sw)
+    is_adjoint = args.workload == "adjoint"
+    if args.workload == "netting":
+        from cva_hjm_cuda_gb300.market import random_netting_set
+
+        netting = random_netting_set(64, seed=20261203)
+        set_product = lambda: eng.set_netting_set(netting)  # noqa: E731
+    else:
+        set_product = lambda: eng.set_swap(sw)  # noqa: E731
+    if is_adjoint:
+        eng.set_market_poly(mk.n_tenor, mk.dtau, mk.spot, mk.vol_coeffs)
+    else:
+        eng.set_market(mk)
+    set_product()
     # weak scaling across ranks: rank r owns paths [r*n, (r+1)*n)
-    cfg = RunConfig(n_paths=n_paths, n_steps=N_STEPS, dt=DT, seed=SEED, path_offset=rank * n_paths)
+    cfg = RunConfig(n_paths=n_paths, n_steps=n_steps, dt=DT, seed=SEED, path_offset=rank * n_paths)
     flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
 
+    def one_step():
+        if is_adjoint:
+            eng.run_adjoint(cfg, checkpoint_every=32)  # synchronises: results are copied out
+        else:
+            eng.enqueue(cfg, prec)
+
     for _ in range(args.warmup):
-        eng.enqueue(cfg, prec)
+        one_step()
         flush.zero_()
     torch.cuda.synchronize()
     if dist:
@@ -232,7 +256,7 @@ def run_ours(args) -> None:
     e0.record(stream)
     launches = 0
     for _ in range(args.steps):
-        eng.enqueue(cfg, prec)
+        one_step()
         launches += eng.stats()["kernels"]
         flush.zero_()
     e1.record(stream)
@@ -245,32 +269,40 @@ def run_ours(args) -> None:
         t = torch.tensor([elapsed], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         elapsed = float(t.item())
-    value = world * n_paths * N_STEPS * args.steps / elapsed
+    value = world * n_paths * n_steps * args.steps / elapsed
     hist = eng.timing_history(min(args.steps, 64))
     path_ms = float(hist[:, 0].mean())
     step_dev_ms = float(hist[:, 3].mean())
-    res = eng.fetch()
+    if is_adjoint:
+        res = None
+    else:
+        res = eng.fetch()
 
     # e2e: the C ABI call with host buffers (market/product arrays in, results out)
     e2e_times = []
     for i in range(args.steps):
         t0 = time.perf_counter()
-        eng.set_market(mk)
-        eng.set_swap(sw)
-        eng.run(cfg, prec)
+        if is_adjoint:
+            eng.set_market_poly(mk.n_tenor, mk.dtau, mk.spot, mk.vol_coeffs)
+            set_product()
+            sens = eng.run_adjoint(cfg, checkpoint_every=32)
+        else:
+            eng.set_market(mk)
+            set_product()
+            eng.run(cfg, prec)
         e2e_times.append(time.perf_counter() - t0)
         flush.zero_()
         torch.cuda.synchronize()
     st = eng.stats()
     h2d = st["h2d_bytes"] + 8 * (mk.spot.size + mk.vol.size + mk.drift.size + sw.accrual.size)
-    e2e_value = world * n_paths * N_STEPS * args.steps / sum(e2e_times)
+    e2e_value = world * n_paths * n_steps * args.steps / sum(e2e_times)
 
     if rank != 0:
         if dist:
             dist.destroy_process_group()
         return
 
-    flops = algorithmic_flops_per_path(mk.n_tenor, N_STEPS, stride) * n_paths
+    flops = algorithmic_flops_per_path(mk.n_tenor, n_steps, stride) * n_paths * (2 if is_adjoint else 1)
     extras = {}
     peak_key = "fp64" if prec == "fp64" else "mixed"
     peak = None
@@ -285,7 +317,9 @@ def run_ours(args) -> None:
     traffic = profiled_traffic(f"{prec}-{n_paths}")
     roofline = {"bound": "fp64_pipe" if prec == "fp64" else "fp32_pipe", "achieved": achieved, "peak": peak,
                 "unit": "TFLOP/s", "frac": (achieved / peak) if peak else None, "traffic": traffic,
-                "kernel": f"path_kernel<51,{'double' if prec == 'fp64' else 'float'},false>",
+                "kernel": ("adjoint_kernel<51,true>" if is_adjoint else
+                           f"path_kernel<{mk.n_tenor},double,false>" if prec == "fp64" else
+                           f"path_kernel_mixed<{mk.n_tenor},false>"),
                 "algorithmic_flops_per_launch": flops, "avg_launch_ms": path_ms,
                 "peak_source": "measured live by bench.py (FMA microkernel, this GPU)",
                 "hbm_peak_gbs_measured": _measured_hbm()}
@@ -308,8 +342,9 @@ def run_ours(args) -> None:
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": wl["dtype"], "data": "synthetic",
-        "config": {"workload": wl["name"], "n_paths_per_gpu": n_paths, "n_steps": N_STEPS, "dt": DT, "n_tenor": 51,
-                   "factors": 3, "sampled_dates": N_STEPS // stride, "pfe_quantile": 0.975, "hazard": 0.02,
+        "config": {"workload": wl["name"], "n_paths_per_gpu": n_paths, "n_steps": n_steps, "dt": DT,
+                   "n_tenor": mk.n_tenor, "factors": 3, "sampled_dates": n_steps // stride,
+                   "pfe_quantile": None if is_adjoint else 0.975, "hazard": 0.02,
                    "recovery": 0.4, "seed": SEED, "parallelism": f"replicas{world}" if world > 1 else "single",
                    "l2": f"flushed between steps ({FLUSH_BYTES >> 20} MiB device write, inside the timed region)"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
@@ -319,8 +354,10 @@ def run_ours(args) -> None:
         "cpu_baseline": cpu_baseline,
         "clocks": clk,
         "device_ms_per_step": step_dev_ms,
-        "result": {"cva": res.cva, "cva_stderr": res.cva_stderr, "ee_0": float(res.ee[0]),
-                   "pfe_0": float(res.pfe[0]) if res.pfe is not None else None},
+        "result": ({"cva": sens.cva, "cva_stderr": sens.cva_stderr, "dcva_dhazard": sens.dcva_dhazard}
+                   if is_adjoint else
+                   {"cva": res.cva, "cva_stderr": res.cva_stderr, "ee_0": float(res.ee[0]),
+                    "pfe_0": float(res.pfe[0]) if res.pfe is not None else None}),
     }
     line.update(extras)
     print(json.dumps(line), flush=True)

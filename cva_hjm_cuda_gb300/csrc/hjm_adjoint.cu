@@ -17,14 +17,19 @@
 // so seeds_n[i] = abar_i for n <= n_i and xbar_i at n = n_i, with
 //     cfbar_i = sum_{j<i} w_j [V_j > 0],  V_j = sum_{i>j} cf_i,
 //     xbar_i = cfbar_i D_i payA_i e^{x_i/m},  abar_i = -dt D_i cfbar_i (payA_i L_i - payB_i).
-// The Jacobian A does not depend on the state, so the same g serves p and h,
-// and the sweep needs no forward state beyond the per-date seeds:
-//     dCVA/dspot      = g_{stride-1} + (stride-1) abar          (block 0 holds spot)
-//     dCVA/dmu[t]     = dt sum_{n >= stride} g_n[t]
-//     dCVA/dS[t][k]   = sum_n g_n[t] phi_{n,k}
-// and with sigma_k(T) = sum_d c_{k,d} T^d the volatility coefficients need only
-// the three moments M_d(n) = sum_t g_n[t] tau_t^d per step:
-//     dCVA/dc_{k,d} (diffusion) = sqrt(dt) sum_n phi_{n,k} M_d(n).
+// The Jacobian A does not depend on the state.  Two consequences shape the kernel:
+//  * h does not depend on the initial curve or the drift, so dCVA/dspot and
+//    dCVA/dmu follow from the path means of the per-date seeds (E xbar_i,
+//    E abar_i) through the adjoint of the deterministic curve p, which the host
+//    runs in FP64; the kernel only reduces those 2B means.
+//  * the volatility coefficients (sigma_k(T) = sum_d c_{k,d} T^d) need, per step,
+//    the three moments M_d(n) = sum_t g_n[t] tau_t^d:
+//        dCVA/dc_{k,d} (diffusion) = sqrt(dt) sum_n phi_{n,k} M_d(n),
+//    and because A 1 = 1, A tau = tau + c dtau 1 and A tau^2 = tau^2 + 2 c dtau tau
+//    + c dtau^2 1 - 2 c dtau^2 e_L, the moments of A^T g follow from those of g
+//    and g[L] in O(1):  M0' = M0,  M1' = M1 + c dtau M0,
+//        M2' = M2 + 2 c dtau M1 + c dtau^2 M0 - 2 c dtau^2 g[L].
+//    The per-tenor state g is still swept (A^T on packed pairs) for g[L].
 // The drift's own dependence on the coefficients (trapezoid rule) is chained
 // on the host.  The normals are regenerated from their Philox counters.
 //
@@ -49,12 +54,11 @@ namespace hjm {
 constexpr int kAdjCta = 64;  // paths per CTA of the adjoint kernel
 
 // Shared memory per thread (thread-private columns, stride kAdjCta):
-//   acc_s  max(B+1 f64, NT f32)  FP64 discount sums, slot i then cash flow i;
-//                                 reused as mu_s (NT f32 drift adjoints) in the sweep
+//   acc_s  (B+1) f64   FP64 discount sums, slot i then cash flow i
 //   hs_s   (B+2) f32   curve at the block start (forward), exposures (forward
 //                      epilogue), curve at the segment start (recompute)
-//   xs_s   (B+1) f32   K = 0: x_i then xbar_i;  K > 0: cfbar_i
-//   ds_s   (B+1) f32   K = 0: D_i then abar_i
+//   xs_s   (B+1) f32   K = 0: x_i then xbar_i;  K > 0: cfbar_i then xbar_i
+//   ds_s   (B+1) f32   K = 0: D_i then abar_i;   K > 0: abar_i
 //   cb_s   9 f64       diffusion coefficient adjoints
 //   red_s  (kAdjCta/32) * R f64   CTA reduction
 struct AdjLayout {
@@ -66,10 +70,10 @@ __host__ __device__ inline size_t align128(size_t x) { return (x + 127) & ~(size
 __host__ __device__ inline AdjLayout adj_layout(int nt, int B, int R)
 {
     AdjLayout L;
+    (void)nt;
     const size_t rows = (size_t)B + 1;
-    const size_t a = rows * 8 > (size_t)nt * 4 ? rows * 8 : (size_t)nt * 4;
     L.acc = 0;
-    L.hs = align128(a * kAdjCta);
+    L.hs = align128(rows * 8 * kAdjCta);
     L.xs = align128(L.hs + (rows + 1) * kAdjCta * 4);
     L.ds = align128(L.xs + rows * kAdjCta * 4);
     L.cb = align128(L.ds + rows * kAdjCta * 4);
@@ -114,7 +118,7 @@ __device__ __forceinline__ void pair_add(float2 (&v)[PairGrid<NT>::H], int i, fl
 }
 
 template <int NT, bool CKPT>
-__global__ void __launch_bounds__(kAdjCta, 4)
+__global__ void __launch_bounds__(kAdjCta, 6)
     adjoint_kernel(const __grid_constant__ AdjParams A, double* __restrict__ partials, float* __restrict__ ck_h,
                    double* __restrict__ ck_a)
 {
@@ -126,10 +130,9 @@ __global__ void __launch_bounds__(kAdjCta, 4)
     const int tid = threadIdx.x;
     const int B = P.n_blocks;
     const int rows = B + 1;
-    const int R = B + 3 + 2 * NT + 9;
+    const int R = 3 * B + 12;
     const AdjLayout Ly = adj_layout(NT, B, R);
     double* acc_s = reinterpret_cast<double*>(smem + Ly.acc);
-    float* mu_s = reinterpret_cast<float*>(smem + Ly.acc);
     float* hs_s = reinterpret_cast<float*>(smem + Ly.hs);
     float* xs_s = reinterpret_cast<float*>(smem + Ly.xs);
     float* ds_s = reinterpret_cast<float*>(smem + Ly.ds);
@@ -260,21 +263,22 @@ __global__ void __launch_bounds__(kAdjCta, 4)
             }
         }
     }
-    __syncthreads();  // acc_s becomes mu_s
 
     // ---------------------------------------------------------------- reverse
-    for (int t = 0; t < NT; ++t) mu_s[t * kCtaA + tid] = 0.f;
     for (int q = 0; q < 9; ++q) cb_s[q * kCtaA + tid] = 0.0;
-    float2 g[H], inj[H], mub[H];
+    float2 g[H], inj[H];
 #pragma unroll
     for (int p = 0; p < H; ++p) {
         g[p] = make_float2(0.f, 0.f);
         inj[p] = make_float2(0.f, 0.f);
-        mub[p] = make_float2(0.f, 0.f);
     }
     float cbb[9];
 #pragma unroll
     for (int q = 0; q < 9; ++q) cbb[q] = 0.f;
+    // moments of g and of the injected discount seeds
+    float M0 = 0.f, M1 = 0.f, M2 = 0.f, I0 = 0.f, I1 = 0.f, I2 = 0.f;
+    const float dtau = (float)(1.0 / P.m);
+    const float k1 = P.c * dtau, k2 = P.c * dtau * dtau;
 
     const int E = n_steps - stride;
     const int S = (E + K - 1) / K;
@@ -315,6 +319,8 @@ __global__ void __launch_bounds__(kAdjCta, 4)
                     const double a = P.psum[i] + a0 + part;
                     const float D = expf((float)(-a * P.dt));
                     date_seeds(P, i, x, D, xs_s[i * kCtaA + tid], sx, sa);
+                    xs_s[i * kCtaA + tid] = sx;  // the seeds replace cfbar (no longer needed)
+                    ds_s[i * kCtaA + tid] = sa;
                     idate = i;
                 }
             }
@@ -334,17 +340,19 @@ __global__ void __launch_bounds__(kAdjCta, 4)
                 }
                 pair_set<NT>(inj, i, ab);
                 pair_add<NT>(g, i, xb);
+                const float ti = dtau * (float)i;
+                I0 += ab;
+                I1 = fmaf(ab, ti, I1);
+                I2 = fmaf(ab, ti * ti, I2);
+                M0 += xb;
+                M1 = fmaf(xb, ti, M1);
+                M2 = fmaf(xb, ti * ti, M2);
             }
-            float2 m0 = make_float2(0.f, 0.f), m1 = m0, m2 = m0;
 #pragma unroll
-            for (int p = 0; p < H; ++p) {
-                g[p] = __fadd2_rn(g[p], inj[p]);
-                mub[p] = __fadd2_rn(mub[p], g[p]);
-                m0 = __fadd2_rn(m0, g[p]);
-                m1 = __ffma2_rn(g[p], A.taup[p], m1);
-                m2 = __ffma2_rn(g[p], A.tau2p[p], m2);
-            }
-            const float M0 = m0.x + m0.y, M1 = m1.x + m1.y, M2 = m2.x + m2.y;
+            for (int p = 0; p < H; ++p) g[p] = __fadd2_rn(g[p], inj[p]);
+            M0 += I0;
+            M1 += I1;
+            M2 += I2;
             float phi0, phi1, phi2;
             draw_phi<float, false>(nullptr, gpath, lp, P.n_paths, n, P.rk0, P.rk1, phi0, phi1, phi2);
             cbb[0] = fmaf(phi0, M0, cbb[0]);
@@ -356,75 +364,60 @@ __global__ void __launch_bounds__(kAdjCta, 4)
             cbb[6] = fmaf(phi2, M0, cbb[6]);
             cbb[7] = fmaf(phi2, M1, cbb[7]);
             cbb[8] = fmaf(phi2, M2, cbb[8]);
+            // moments of A^T g from those of g and its last tenor, then the sweep itself
+            const float gL = pair_tenor<NT>(g, NT - 1);
+            M2 = fmaf(-2.f * k2, gL, fmaf(k2, M0, fmaf(2.f * k1, M1, M2)));
+            M1 = fmaf(k1, M0, M1);
             adjoint_convection_pairs<NT>(g, M.cp);
         }
         // fold the segment's FP32 partials
-#pragma unroll
-        for (int p = 0; p < H; ++p) {
-            mu_s[p * kCtaA + tid] += mub[p].x;
-            if (p + H < NT) mu_s[(p + H) * kCtaA + tid] += mub[p].y;
-            mub[p] = make_float2(0.f, 0.f);
-        }
 #pragma unroll
         for (int q = 0; q < 9; ++q) {
             cb_s[q * kCtaA + tid] += (double)cbb[q];
             cbb[q] = 0.f;
         }
     }
-    // seeds of step stride-1 (date 1 is deterministic: h = 0 through block 0)
-    {
+    // seeds of date 1 (deterministic: h = 0 through block 0), for the seed means
+    if (CKPT) {
+        const float D1 = expf((float)(-P.psum[1] * P.dt));
         float xb, ab;
-        if (CKPT) {
-            const float D1 = expf((float)(-P.psum[1] * P.dt));
-            date_seeds(P, 1, P.psamp[1], D1, xs_s[1 * kCtaA + tid], xb, ab);
-        } else {
-            xb = xs_s[1 * kCtaA + tid];
-            ab = ds_s[1 * kCtaA + tid];
-        }
-        pair_set<NT>(inj, 1, ab);
-        pair_add<NT>(g, 1, xb);
-    }
-    // dCVA/dspot = g_{stride-1} + (stride - 1) * abar  (steps 0 .. stride-2 read spot directly)
-    const float2 sm1 = make_float2((float)(stride - 1), (float)(stride - 1));
-#pragma unroll
-    for (int p = 0; p < H; ++p) {
-        g[p] = __fadd2_rn(g[p], inj[p]);
-        g[p] = __ffma2_rn(sm1, inj[p], g[p]);
-        if (!active) g[p] = make_float2(0.f, 0.f);
+        date_seeds(P, 1, P.psamp[1], D1, xs_s[1 * kCtaA + tid], xb, ab);
+        xs_s[1 * kCtaA + tid] = xb;
+        ds_s[1 * kCtaA + tid] = ab;
     }
 
     // ---------------------------------------------------------------- CTA reduction
-    // columns: [0..B] EE, B+1/B+2 CVA stats (written above),
-    // B+3 .. B+2+NT spot, then NT drift, then 9 coefficient columns
-    const int cs = B + 3, cm = B + 3 + NT, cc = B + 3 + 2 * NT;
+    // columns: [0..B] EE, B+1/B+2 CVA stats (written above), then
+    // E xbar_i (i = 1..B), E abar_i (i = 1..B), and the 9 coefficient columns
+    const int cx = B + 3, ca = 2 * B + 3, cc = 3 * B + 3;
     double* wred = red_s;  // [warp][R]
-#pragma unroll
-    for (int t = 0; t < NT; ++t) {
-        const double sum = warp_sum((double)pair_tenor<NT>(g, t));
-        if (lane == 0) wred[warp * R + cs + t] = sum;
-    }
-    for (int t = 0; t < NT; ++t) {
-        const double sum = warp_sum(active ? (double)mu_s[t * kCtaA + tid] : 0.0);
-        if (lane == 0) wred[warp * R + cm + t] = sum;
+    for (int i = 1; i <= B; ++i) {
+        const double sx_ = warp_sum(active ? (double)xs_s[i * kCtaA + tid] : 0.0);
+        const double sa_ = warp_sum(active ? (double)ds_s[i * kCtaA + tid] : 0.0);
+        if (lane == 0) {
+            wred[warp * R + cx + i - 1] = sx_;
+            wred[warp * R + ca + i - 1] = sa_;
+        }
     }
     for (int q = 0; q < 9; ++q) {
         const double sum = warp_sum(active ? cb_s[q * kCtaA + tid] : 0.0);
         if (lane == 0) wred[warp * R + cc + q] = sum;
     }
     __syncthreads();
-    for (int col = cs + tid; col < R; col += kCtaA) {
+    for (int col = cx + tid; col < R; col += kCtaA) {
         double sum = 0.0;
         for (int w = 0; w < kCtaA / 32; ++w) sum += wred[w * R + col];
         partials[(size_t)blockIdx.x * R + col] = sum;
     }
 }
 
-size_t adjoint_smem(int nt, int n_blocks)
-{
-    return adj_layout(nt, n_blocks, n_blocks + 3 + 2 * nt + 9).total;
-}
+size_t adjoint_smem(int nt, int n_blocks) { return adj_layout(nt, n_blocks, 3 * n_blocks + 12).total; }
 
-int adjoint_columns(int nt, int n_blocks) { return n_blocks + 3 + 2 * nt + 9; }
+int adjoint_columns(int nt, int n_blocks)
+{
+    (void)nt;
+    return 3 * n_blocks + 12;
+}
 
 int adjoint_cta() { return kAdjCta; }
 

@@ -733,13 +733,6 @@ hjm_status hjm_run_adjoint(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, doubl
         fill_params<float>(ctx, sh, n_paths, dt, seed, path_offset, hazard_rate, recovery, 0, false, P, F);
         pack_mixed_params(nt, P, A.M);
     }
-    const int Hp = (nt + 1) / 2;
-    for (int p = 0; p < Hp; ++p) {
-        const double T0 = ctx->dtau * p, T1 = ctx->dtau * (p + Hp);
-        const bool pad = p + Hp >= nt;
-        A.taup[p] = make_float2((float)T0, pad ? 0.f : (float)T1);
-        A.tau2p[p] = make_float2((float)(T0 * T0), pad ? 0.f : (float)(T1 * T1));
-    }
     A.ckpt_every = K;
     A.ck_ld = ld;
     cudaStream_t s = ctx->stream;
@@ -768,10 +761,34 @@ hjm_status hjm_run_adjoint(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, doubl
         cva_out[HJM_CVA_STDERR] = res[kResCVAStderr];
         cva_out[HJM_CVA_DHAZARD] = res[kResDCVADHazard];
     }
-    std::vector<double> dmu(nt);
-    for (int t = 0; t < nt; ++t) dmu[t] = dt * sums[B + 3 + nt + t] * inv_n;
+    // dCVA/dspot and dCVA/dmu: the path means of the per-date seeds through the
+    // FP64 adjoint of the deterministic curve (p_n = spot for the first block,
+    // p_n = A p_{n-1} + dt mu after; date i reads p_{n_i}[i] and sum_{n<=n_i} p_n[i]).
+    std::vector<double> xbar(B + 1, 0.0), abar(B + 1, 0.0);
+    for (int i = 1; i <= B; ++i) {
+        xbar[i] = sums[B + 3 + i - 1] * inv_n;
+        abar[i] = sums[2 * B + 3 + i - 1] * inv_n;
+    }
+    std::vector<double> q(nt, 0.0), qn(nt), dmu(nt, 0.0), inj(nt, 0.0);
+    const double c = dt / ctx->dtau;
+    const int L = nt - 1;
+    for (int n = n_steps - 1; n >= sh.stride - 1; --n) {
+        if ((n + 1) % sh.stride == 0) {  // step n samples date i
+            const int i = (n + 1) / sh.stride;
+            inj[i] = abar[i];
+            q[i] += xbar[i];
+        }
+        for (int t = 0; t < nt; ++t) q[t] += inj[t];
+        if (n < sh.stride) break;  // q = adjoint of p_{stride-1} = spot
+        for (int t = 0; t < nt; ++t) dmu[t] += dt * q[t];
+        qn[0] = (1.0 - c) * q[0];
+        for (int t = 1; t <= L - 2; ++t) qn[t] = q[t] + c * (q[t - 1] - q[t]);
+        qn[L - 1] = q[L - 1] + c * (q[L - 2] - q[L - 1]) - c * q[L];
+        qn[L] = q[L] + c * (q[L] + q[L - 1]);
+        q.swap(qn);
+    }
     if (dcva_dspot_out)
-        for (int t = 0; t < nt; ++t) dcva_dspot_out[t] = sums[B + 3 + t] * inv_n;
+        for (int t = 0; t < nt; ++t) dcva_dspot_out[t] = q[t] + (double)(sh.stride - 1) * inj[t];
     if (dcva_ddrift_out)
         for (int t = 0; t < nt; ++t) dcva_ddrift_out[t] = dmu[t];
     if (dcva_dvolcoef_out) {
@@ -782,7 +799,7 @@ hjm_status hjm_run_adjoint(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, doubl
         for (int k = 0; k < HJM_N_FACTOR; ++k) {
             const double* sig = ctx->vol.data() + (size_t)k * nt;
             for (int d = 0; d < 3; ++d) {
-                double v = sq * sums[B + 3 + 2 * nt + k * 3 + d] * inv_n;
+                double v = sq * sums[3 * B + 3 + k * 3 + d] * inv_n;
                 double I = 0.0, J = 0.0;
                 for (int i = 0; i < nt; ++i) {
                     const double ti = ctx->dtau * i;

@@ -63,12 +63,9 @@ cudaError_t launch_widen_exposures(const void* in, bool fp64, int64_t ld, int64_
 cudaError_t measure_fma_peak(bool fp64, cudaStream_t s, int n_sms, double* tflops);
 
 // Adjoint kernel parameters: the mixed-precision path parameters plus the
-// polynomial basis of the volatility coefficients in tenor pairs and the
 // checkpoint layout.
 struct AdjParams {
     MixedParams M;
-    float2 taup[kMaxTenor / 2];    // {tau_p, tau_{p+H}}
-    float2 tau2p[kMaxTenor / 2];   // their squares
     int ckpt_every;                // 0: no checkpoints; else K in [1, stride]
     int64_t ck_ld;                 // row stride of the checkpoint arrays
 };
