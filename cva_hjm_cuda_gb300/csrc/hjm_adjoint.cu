@@ -117,7 +117,7 @@ __device__ __forceinline__ void pair_add(float2 (&v)[PairGrid<NT>::H], int i, fl
     }
 }
 
-template <int NT, bool CKPT>
+template <int NT, bool CKPT, bool POLY>
 __global__ void __launch_bounds__(kAdjCta, 6)
     adjoint_kernel(const __grid_constant__ AdjParams A, double* __restrict__ partials, float* __restrict__ ck_h,
                    double* __restrict__ ck_a)
@@ -149,28 +149,31 @@ __global__ void __launch_bounds__(kAdjCta, 6)
 
     // ---------------------------------------------------------------- forward
     // The same arithmetic as path_kernel_mixed, plus what the sweep needs.
-    float2 h[H];
-#pragma unroll
-    for (int p = 0; p < H; ++p) h[p] = make_float2(0.f, 0.f);
+    MixedPath<NT, POLY> x;
+    x.reset();
     for (int i = 0; i < rows; ++i) acc_s[i * kCtaA + tid] = 0.0;
     for (int t = 0; t <= B + 1; ++t) hs_s[t * kCtaA + tid] = 0.f;
 
     auto sample = [&](int i) {
-        const double x = P.psamp[i] + (double)select_pair<NT>(h, i);
+        const double xv = P.psamp[i] + (double)x.value(P, i);
         const double a = P.psum[i] + acc_s[i * kCtaA + tid];
         const float D = expf((float)(-a * P.dt));
         const float mm = (float)P.m;
-        const float L = mm * expm1f((float)x / mm);
+        const float L = mm * expm1f((float)xv / mm);
         acc_s[i * kCtaA + tid] = (double)(D * ((float)P.payA[i] * L - (float)P.payB[i]));
         if (!CKPT) {
-            xs_s[i * kCtaA + tid] = (float)x;
+            xs_s[i * kCtaA + tid] = (float)xv;
             ds_s[i * kCtaA + tid] = D;
         }
     };
 
+    // checkpoint rows: the NT tenors of the curve (POLY: its convected part),
+    // then S, U, W
+    constexpr int kCkRows = NT + 3;
     sample(1);
     for (int b = 1; b < B; ++b) {
-        float F0 = 0.f, F1 = 0.f, F2 = 0.f, H1 = 0.f;
+        BlockSums bs;
+        bs.reset();
         for (int s = 0; s < stride; ++s) {
             const int n = b * stride + s;
             if (CKPT && ((n - stride) % K) == 0) {
@@ -181,30 +184,29 @@ __global__ void __launch_bounds__(kAdjCta, 6)
                 const int inext = b + 1;
                 double part = 0.0;
                 if (s > 0)
-                    recover_sums_up<NT>(h, hs_s, tid, kCtaA, P, F0, F1, F2, H1, inext, [&](int t, float Ht) {
+                    block_sums_up<NT, POLY>(x, hs_s, tid, kCtaA, P, bs, inext, [&](int t, float Ht) {
                         if (t == inext) part = (double)Ht;
                     });
-                if (inext == 1) part = (double)H1;
                 if (active) {
 #pragma unroll
-                    for (int t = 0; t < NT; ++t) ck_h[((size_t)ck * NT + t) * ld + lp] = pair_tenor<NT>(h, t);
+                    for (int t = 0; t < NT; ++t) ck_h[((size_t)ck * kCkRows + t) * ld + lp] = pair_tenor<NT>(x.h, t);
+                    ck_h[((size_t)ck * kCkRows + NT) * ld + lp] = x.S;
+                    ck_h[((size_t)ck * kCkRows + NT + 1) * ld + lp] = x.U;
+                    ck_h[((size_t)ck * kCkRows + NT + 2) * ld + lp] = x.W;
                     ck_a[(size_t)ck * ld + lp] = acc_s[inext * kCtaA + tid] + part;
                 }
             }
             float phi0, phi1, phi2;
             draw_phi<float, false>(nullptr, gpath, lp, P.n_paths, n, P.rk0, P.rk1, phi0, phi1, phi2);
-            euler_step_pairs<NT>(h, M, phi0, phi1, phi2);
-            F0 += phi0;
-            F1 += phi1;
-            F2 += phi2;
-            H1 += h[1].x;
+            x.step(M, phi0, phi1, phi2);
+            bs.add(x, phi0, phi1, phi2);
         }
-        recover_sums_up<NT>(h, hs_s, tid, kCtaA, P, F0, F1, F2, H1, B, [&](int t, float Ht) {
+        block_sums_up<NT, POLY>(x, hs_s, tid, kCtaA, P, bs, B, [&](int t, float Ht) {
             if (t > b) acc_s[t * kCtaA + tid] += (double)Ht;
         });
 #pragma unroll
         for (int t = 1; t < NT; ++t)
-            if (t <= B + 1) hs_s[t * kCtaA + tid] = pair_tenor<NT>(h, t);
+            if (t <= B + 1) hs_s[t * kCtaA + tid] = pair_tenor<NT>(x.h, t);
         sample(b + 1);
     }
 
@@ -290,35 +292,37 @@ __global__ void __launch_bounds__(kAdjCta, 6)
         if (CKPT) {
             // recompute the segment from its checkpoint; rebuild the seeds of
             // the date sampled inside it (at most one, since K <= stride)
-            float2 hr[H];
+            MixedPath<NT, POLY> xr;
+            const size_t base = (size_t)sg * kCkRows;
 #pragma unroll
             for (int p = 0; p < H; ++p) {
-                hr[p].x = active ? ck_h[((size_t)sg * NT + p) * ld + lp] : 0.f;
-                hr[p].y = (active && p + H < NT) ? ck_h[((size_t)sg * NT + p + H) * ld + lp] : 0.f;
+                xr.h[p].x = active ? ck_h[(base + p) * ld + lp] : 0.f;
+                xr.h[p].y = (active && p + H < NT) ? ck_h[(base + p + H) * ld + lp] : 0.f;
             }
+            xr.S = active ? ck_h[(base + NT) * ld + lp] : 0.f;
+            xr.U = active ? ck_h[(base + NT + 1) * ld + lp] : 0.f;
+            xr.W = active ? ck_h[(base + NT + 2) * ld + lp] : 0.f;
 #pragma unroll
             for (int t = 1; t < NT; ++t)
-                if (t <= B + 1) hs_s[t * kCtaA + tid] = pair_tenor<NT>(hr, t);
+                if (t <= B + 1) hs_s[t * kCtaA + tid] = pair_tenor<NT>(xr.h, t);
             const double a0 = active ? ck_a[(size_t)sg * ld + lp] : 0.0;
-            float F0 = 0.f, F1 = 0.f, F2 = 0.f, H1 = 0.f;
+            BlockSums bs;
+            bs.reset();
             for (int n = n0; n < n1; ++n) {
                 float phi0, phi1, phi2;
                 draw_phi<float, false>(nullptr, gpath, lp, P.n_paths, n, P.rk0, P.rk1, phi0, phi1, phi2);
-                euler_step_pairs<NT>(hr, M, phi0, phi1, phi2);
-                F0 += phi0;
-                F1 += phi1;
-                F2 += phi2;
-                H1 += hr[1].x;
+                xr.step(M, phi0, phi1, phi2);
+                bs.add(xr, phi0, phi1, phi2);
                 if ((n + 1) % stride == 0) {
                     const int i = (n + 1) / stride;
-                    double part = (i == 1) ? (double)H1 : 0.0;
-                    recover_sums_up<NT>(hr, hs_s, tid, kCtaA, P, F0, F1, F2, H1, i, [&](int t, float Ht) {
+                    double part = 0.0;
+                    block_sums_up<NT, POLY>(xr, hs_s, tid, kCtaA, P, bs, i, [&](int t, float Ht) {
                         if (t == i) part = (double)Ht;
                     });
-                    const double x = P.psamp[i] + (double)select_pair<NT>(hr, i);
+                    const double xv = P.psamp[i] + (double)xr.value(P, i);
                     const double a = P.psum[i] + a0 + part;
                     const float D = expf((float)(-a * P.dt));
-                    date_seeds(P, i, x, D, xs_s[i * kCtaA + tid], sx, sa);
+                    date_seeds(P, i, xv, D, xs_s[i * kCtaA + tid], sx, sa);
                     xs_s[i * kCtaA + tid] = sx;  // the seeds replace cfbar (no longer needed)
                     ds_s[i * kCtaA + tid] = sa;
                     idate = i;
@@ -421,11 +425,11 @@ int adjoint_columns(int nt, int n_blocks)
 
 int adjoint_cta() { return kAdjCta; }
 
-template <int NT, bool CKPT>
+template <int NT, bool CKPT, bool POLY>
 static cudaError_t launch_adj_t(const AdjParams& A, double* partials, float* ck_h, double* ck_a, cudaStream_t s)
 {
     const size_t smem = adjoint_smem(NT, A.M.P.n_blocks);
-    auto k = adjoint_kernel<NT, CKPT>;
+    auto k = adjoint_kernel<NT, CKPT, POLY>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const int64_t grid = (A.M.P.n_paths + kAdjCta - 1) / kAdjCta;
@@ -433,13 +437,22 @@ static cudaError_t launch_adj_t(const AdjParams& A, double* partials, float* ck_
     return cudaGetLastError();
 }
 
-cudaError_t launch_adjoint(int nt, const AdjParams& A, double* partials, float* ck_h, double* ck_a, cudaStream_t s)
+template <int NT>
+static cudaError_t launch_adj_nt(const AdjParams& A, bool poly, double* partials, float* ck_h, double* ck_a,
+                                 cudaStream_t s)
 {
     const bool ck = A.ckpt_every > 0;
-    if (nt == 51) return ck ? launch_adj_t<51, true>(A, partials, ck_h, ck_a, s)
-                            : launch_adj_t<51, false>(A, partials, ck_h, ck_a, s);
-    if (nt == 61) return ck ? launch_adj_t<61, true>(A, partials, ck_h, ck_a, s)
-                            : launch_adj_t<61, false>(A, partials, ck_h, ck_a, s);
+    if (poly) return ck ? launch_adj_t<NT, true, true>(A, partials, ck_h, ck_a, s)
+                        : launch_adj_t<NT, false, true>(A, partials, ck_h, ck_a, s);
+    return ck ? launch_adj_t<NT, true, false>(A, partials, ck_h, ck_a, s)
+              : launch_adj_t<NT, false, false>(A, partials, ck_h, ck_a, s);
+}
+
+cudaError_t launch_adjoint(int nt, const AdjParams& A, bool poly, double* partials, float* ck_h, double* ck_a,
+                           cudaStream_t s)
+{
+    if (nt == 51) return launch_adj_nt<51>(A, poly, partials, ck_h, ck_a, s);
+    if (nt == 61) return launch_adj_nt<61>(A, poly, partials, ck_h, ck_a, s);
     return cudaErrorInvalidValue;
 }
 

@@ -64,7 +64,9 @@ struct hjm_ctx {
 
     // market
     bool have_market = false;
-    bool have_poly = false;
+    bool have_poly = false;       // coefficients given by hjm_set_market_poly (sensitivities)
+    bool poly_path = false;       // the kernels run the polynomial decomposition (coef)
+    bool allow_poly_path = true;  // hjm_ctx_set_vol_decomposition
     int nt = 0;
     double dtau = 0.5;
     std::vector<double> spot, vol, drift;
@@ -206,9 +208,54 @@ hjm_status hjm_ctx_keep_exposures(hjm_ctx* ctx, int32_t keep)
     return HJM_OK;
 }
 
+hjm_status hjm_ctx_set_vol_decomposition(hjm_ctx* ctx, int32_t enable)
+{
+    HJM_CHECK_CTX(ctx);
+    ctx->allow_poly_path = enable != 0;
+    return HJM_OK;
+}
+
+hjm_status hjm_ctx_vol_decomposition(hjm_ctx* ctx, int32_t* active)
+{
+    HJM_CHECK_CTX(ctx);
+    if (!active) return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "active must not be null");
+    *active = (ctx->have_market && ctx->poly_path && ctx->allow_poly_path) ? 1 : 0;
+    return HJM_OK;
+}
+
 // ---------------------------------------------------------------------------
 // inputs
 // ---------------------------------------------------------------------------
+// Is every factor row of the volatility table a polynomial of degree <= 2 in
+// T = dtau t?  The quadratic through the rows' values at t = 0, mid, last
+// (Lagrange form) must reproduce every entry to 1e-12 of the row's largest
+// magnitude; its monomial coefficients go to coef[k * 3 + d].
+static bool fit_quadratic_vols(const std::vector<double>& vol, int nt, double dtau, double* coef)
+{
+    if (nt < 3) return false;
+    const int i0 = 0, i1 = (nt - 1) / 2, i2 = nt - 1;
+    const double x0 = dtau * i0, x1 = dtau * i1, x2 = dtau * i2;
+    for (int k = 0; k < HJM_N_FACTOR; ++k) {
+        const double* v = vol.data() + (size_t)k * nt;
+        // Lagrange basis l_j(x) = prod (x - x_m) / (x_j - x_m) expanded in 1, x, x^2
+        const double d0 = (x0 - x1) * (x0 - x2), d1 = (x1 - x0) * (x1 - x2), d2 = (x2 - x0) * (x2 - x1);
+        const double w0 = v[i0] / d0, w1 = v[i1] / d1, w2 = v[i2] / d2;
+        const double c2 = w0 + w1 + w2;
+        const double c1 = -(w0 * (x1 + x2) + w1 * (x0 + x2) + w2 * (x0 + x1));
+        const double c0 = w0 * x1 * x2 + w1 * x0 * x2 + w2 * x0 * x1;
+        double scale = 0.0;
+        for (int t = 0; t < nt; ++t) scale = std::max(scale, std::fabs(v[t]));
+        for (int t = 0; t < nt; ++t) {
+            const double T = dtau * t;
+            if (std::fabs(c0 + c1 * T + c2 * T * T - v[t]) > 1e-12 * scale) return false;
+        }
+        coef[k * 3 + 0] = c0;
+        coef[k * 3 + 1] = c1;
+        coef[k * 3 + 2] = c2;
+    }
+    return true;
+}
+
 static void trapezoid_drift(const std::vector<double>& vol, int nt, double dtau, std::vector<double>& drift)
 {
     drift.assign(nt, 0.0);
@@ -247,6 +294,7 @@ hjm_status hjm_set_market(hjm_ctx* ctx, int32_t n_tenor, double dtau, const doub
         trapezoid_drift(ctx->vol, n_tenor, dtau, ctx->drift);
     ctx->have_market = true;
     ctx->have_poly = false;
+    ctx->poly_path = fit_quadratic_vols(ctx->vol, n_tenor, dtau, ctx->coef);
     if (ctx->have_product && (int)ctx->payA.size() != n_tenor) ctx->have_product = false;
     return HJM_OK;
 }
@@ -271,6 +319,7 @@ hjm_status hjm_set_market_poly(hjm_ctx* ctx, int32_t n_tenor, double dtau, const
     if (st != HJM_OK) return st;
     std::memcpy(ctx->coef, vol_coef_host, sizeof(ctx->coef));
     ctx->have_poly = true;
+    ctx->poly_path = true;
     return HJM_OK;
 }
 
@@ -390,6 +439,8 @@ static void deterministic_curve(const hjm_ctx* ctx, int stride, int B, double dt
     }
 }
 
+static bool use_poly_path(const hjm_ctx* ctx) { return ctx->poly_path && ctx->allow_poly_path; }
+
 template <typename T>
 static void fill_params(const hjm_ctx* ctx, const RunShape& sh, int64_t n_paths, double dt, uint64_t seed,
                         uint64_t path_offset, double hazard, double recovery, int64_t ld, bool store,
@@ -413,6 +464,12 @@ static void fill_params(const hjm_ctx* ctx, const RunShape& sh, int64_t n_paths,
         F.cvaw[j] = P.cvaw[j];
         F.dcvaw[j] = (1.0 - recovery) * (-t0 * e0 + t1 * e1);
     }
+    if (use_poly_path(ctx))
+        for (int k = 0; k < kFactors; ++k)
+            for (int d = 0; d < 3; ++d) P.svc[k][d] = sq * ctx->coef[k * 3 + d];
+    P.k1 = (dt / ctx->dtau) * ctx->dtau;
+    P.k2 = (dt / ctx->dtau) * ctx->dtau * ctx->dtau;
+    for (int t = 0; t < nt; ++t) P.tau[t] = (T)(ctx->dtau * t);
     P.c = (T)(dt / ctx->dtau);
     P.dt = dt;
     P.m = 1.0 / ctx->dtau;
@@ -472,12 +529,12 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
         fill_params<float>(ctx, sh, n_paths, dt, seed, path_offset, hazard, recovery, ld, store, P, F);
         MixedParams M;
         pack_mixed_params(ctx->nt, P, M);
-        HJM_CUDA(ctx, launch_path_mixed(ctx->nt, M, ext_dev, (double*)ctx->partials.p,
+        HJM_CUDA(ctx, launch_path_mixed(ctx->nt, M, use_poly_path(ctx), ext_dev, (double*)ctx->partials.p,
                                         store ? (float*)ctx->estore.p : nullptr, s));
     } else {
         PathParams<double> P;
         fill_params<double>(ctx, sh, n_paths, dt, seed, path_offset, hazard, recovery, ld, store, P, F);
-        HJM_CUDA(ctx, launch_path_fp64(ctx->nt, P, ext_dev, (double*)ctx->partials.p,
+        HJM_CUDA(ctx, launch_path_fp64(ctx->nt, P, use_poly_path(ctx), ext_dev, (double*)ctx->partials.p,
                                        store ? (double*)ctx->estore.p : nullptr, s));
     }
     HJM_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
@@ -722,7 +779,7 @@ hjm_status hjm_run_adjoint(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, doubl
     HJM_CUDA(ctx, ctx->sums.ensure(sizeof(double) * kMaxTenor * 4));
     HJM_CUDA(ctx, ctx->result.ensure(sizeof(double) * kResLen));
     if (K > 0) {
-        HJM_CUDA(ctx, ctx->ck_h.ensure(sizeof(float) * (size_t)S * nt * (size_t)ld));
+        HJM_CUDA(ctx, ctx->ck_h.ensure(sizeof(float) * (size_t)S * (nt + 3) * (size_t)ld));
         HJM_CUDA(ctx, ctx->ck_a.ensure(sizeof(double) * (size_t)S * (size_t)ld));
     }
     AdjParams A;
@@ -740,7 +797,7 @@ hjm_status hjm_run_adjoint(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, doubl
     ctx->n_enqueued++;
     HJM_CUDA(ctx, cudaMemsetAsync(ctx->result.p, 0, sizeof(double) * kResLen, s));
     HJM_CUDA(ctx, cudaEventRecord(ctx->ev[0], s));
-    HJM_CUDA(ctx, launch_adjoint(nt, A, (double*)ctx->partials.p, K > 0 ? (float*)ctx->ck_h.p : nullptr,
+    HJM_CUDA(ctx, launch_adjoint(nt, A, use_poly_path(ctx), (double*)ctx->partials.p, K > 0 ? (float*)ctx->ck_h.p : nullptr,
                                  K > 0 ? (double*)ctx->ck_a.p : nullptr, s));
     HJM_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
     HJM_CUDA(ctx, launch_reduce((const double*)ctx->partials.p, n_ctas, R, (double*)ctx->sums.p, F,

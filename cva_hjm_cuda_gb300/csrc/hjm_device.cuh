@@ -135,6 +135,11 @@ struct PathParams {
     int n_blocks;                // sampled dates B = n_steps / stride
     int stride;                  // Euler steps per block (dtau / dt)
     int store_exposures;         // write per-path exposures [date][path]
+    // Polynomial volatility factors, sqrt(dt) sigma_k(T) = sum_d svc[k][d] T^d
+    // (degree <= 2): used by the kernels' polynomial form only.
+    double svc[kFactors][3];
+    double k1, k2;               // c dtau, c dtau^2
+    T tau[kMaxTenor];            // tau_t = dtau t
 };
 
 #ifdef __CUDACC__

@@ -27,180 +27,166 @@
 
 namespace hjm {
 
-template <typename T>
-struct Prec;
-template <>
-struct Prec<double> {
-    static constexpr bool kMixed = false;
-    static constexpr int kThreads = 64;   // FP64: more shared memory per path, fewer paths per CTA
-};
-template <>
-struct Prec<float> {
-    static constexpr bool kMixed = true;
-    static constexpr int kThreads = kCta;
-};
-
-// Shared-memory layout of path_kernel (dynamic), per CTA of kCta threads,
-// column tid private to its thread until the epilogue:
-//   cf_s   [B+1][kCta] T       cash flows of the sampled dates
-//   acc_s  [B+1][kCta] double  FP64 discount sums of the stochastic part per tenor
-//   work_s mixed: [max(NT, B+1)][kCta] float   block-partial staging, then exposures
-//          FP64:  [2(B+2)][kCta] double        curve at block start / end, then exposures
-//   red_s  [2 * kCta/32] double CVA statistics
-__host__ __device__ inline int path_threads(bool mixed) { return mixed ? Prec<float>::kThreads : Prec<double>::kThreads; }
+// Shared-memory layout of the FP64 path kernel (dynamic), per CTA of
+// kFp64Cta threads, column tid private to its thread until the epilogue:
+//   cf_s   [B+1] double   cash flows of the sampled dates
+//   acc_s  [B+1] double   FP64 discount sums of the stochastic part per tenor
+//   work_s [2(B+2)] double  curve at block start / end, then exposures
+//   red_s  [2 * kFp64Cta/32] double  CVA statistics
+constexpr int kFp64Cta = 64;
 
 __host__ __device__ inline size_t path_smem_bytes(int nt, int n_blocks, bool mixed)
 {
-    const size_t kCta = (size_t)path_threads(mixed);
-    const size_t te = mixed ? 4 : 8;
+    (void)nt;
+    (void)mixed;
     const size_t rows = (size_t)n_blocks + 1;
-    size_t b = rows * kCta * te;                       // cf_s
-    b = (b + 7) & ~(size_t)7;
-    b += rows * kCta * 8;                              // acc_s
-    const size_t wrows = mixed ? ((size_t)nt > rows ? (size_t)nt : rows) : 2 * (rows + 1);
+    size_t b = rows * kFp64Cta * 8;  // cf_s
+    b += rows * kFp64Cta * 8;        // acc_s
     b = (b + 127) & ~(size_t)127;
-    b += wrows * kCta * te;                            // work_s
-    b += 2 * (kCta / 32) * 8;                          // red_s
+    b += 2 * (rows + 1) * kFp64Cta * 8;  // work_s
+    b += 2 * (kFp64Cta / 32) * 8;        // red_s
     return b;
 }
 
-// FP64 mode: discount sums by block-sum recovery.  Over one block of Euler
-// steps n = n0 .. n0+stride-1 the states h_n = A h_{n-1} + S phi_n sum to
-//     (I - A) H = S Phi - A (h_end - h_start),   H = sum_n h_n, Phi = sum_n phi_n,
+// Discount sums by block-sum recovery.  Over one block of Euler steps
+// n = n0 .. n0+stride-1 the states h_n = A h_{n-1} + xi_n sum to
+//     (I - A) H = sum_n xi_n - A (h_end - h_start),   H = sum_n h_n,
 // and (I - A) H [t] = c (H[t] - H[t+1]) for t below the last tenor.  So with
 // one tenor accumulated directly (H[B], the last tenor still to be sampled),
-//     H[t] = H[t+1] + (sum_k sv[k][t] Phi_k - (A d)[t]) / c,  d = h_end - h_start,
+//     H[t] = H[t+1] + (Xi[t] - (A d)[t]) / c,  d = h_end - h_start,
 // gives every block sum the discount needs in O(B) FP64 operations per block
 // instead of one FP64 addition per tenor per step (the FP64 pipe is the bound).
 // Exact in exact arithmetic; in FP64 the recovered sums differ from step-by-
 // step accumulation by ~1e-14 relative.
-template <int NT, typename T, bool EXT>
-__global__ void __launch_bounds__(Prec<T>::kThreads, Prec<T>::kMixed ? 3 : 4)
-    path_kernel(const __grid_constant__ PathParams<T> P, const double* __restrict__ ext,
-                double* __restrict__ partials, T* __restrict__ estore)
+//
+// Polynomial volatility (POLY).  When sqrt(dt) sigma_k(T) = sum_d svc[k][d] T^d
+// with degree <= 2, the noise of a step is xi = alpha + beta T + gamma T^2 and
+// the convection operator maps that basis into itself up to one last-tenor
+// term:  A 1 = 1,  A T = T + c dtau 1,  A T^2 = T^2 + 2 c dtau T + c dtau^2 1
+// - 2 c dtau^2 e_L.  Writing h = S 1 + U T + W T^2 + hc, the Euler step becomes
+//     S <- S + c dtau U + c dtau^2 W + alpha,   U <- U + 2 c dtau W + beta,
+//     W <- W + gamma,   hc <- A hc - 2 c dtau^2 W e_L   (old U, W on the right),
+// exact in exact arithmetic: the curve is advanced in full, with 2 operations
+// per tenor (the convection of hc) instead of 5, plus a dozen per step.
+template <int NT, bool EXT, bool POLY>
+__global__ void __launch_bounds__(kFp64Cta, 4)
+    path_kernel_fp64(const __grid_constant__ PathParams<double> P, const double* __restrict__ ext,
+                     double* __restrict__ partials, double* __restrict__ estore)
 {
-    constexpr bool kMixed = Prec<T>::kMixed;
-    constexpr int kCta = Prec<T>::kThreads;  // paths per CTA
+    constexpr int kCta = kFp64Cta;
+    constexpr int L = NT - 1;
     extern __shared__ __align__(128) unsigned char smem[];
     const int tid = threadIdx.x;
     const int B = P.n_blocks;
     const int rows = B + 1;
-    T* cf_s = reinterpret_cast<T*>(smem);
-    size_t off = ((size_t)rows * kCta * sizeof(T) + 7) & ~(size_t)7;
-    double* acc_s = reinterpret_cast<double*>(smem + off);
-    off += (size_t)rows * kCta * 8;
-    off = (off + 127) & ~(size_t)127;
-    T* work_s = reinterpret_cast<T*>(smem + off);
-    const int wrows = kMixed ? (NT > rows ? NT : rows) : 2 * (rows + 1);
-    double* red_s = reinterpret_cast<double*>(smem + off + (size_t)wrows * kCta * sizeof(T));
+    double* cf_s = reinterpret_cast<double*>(smem);
+    double* acc_s = cf_s + (size_t)rows * kCta;
+    size_t off = ((size_t)rows * kCta * 16 + 127) & ~(size_t)127;
+    double* work_s = reinterpret_cast<double*>(smem + off);
+    double* red_s = work_s + (size_t)2 * (rows + 1) * kCta;
 
     const int64_t cta_base = (int64_t)blockIdx.x * kCta;
     const int64_t lp = cta_base + tid;            // path index within this launch
     const bool active = lp < P.n_paths;
     const uint64_t gpath = P.path_offset + (uint64_t)lp;
 
-    // stochastic part of the curve; zero through block 0 (spot hold)
-    T h[NT];
+    // stochastic part of the curve (POLY: its convected remainder hc); zero
+    // through block 0 (spot hold)
+    double h[NT];
 #pragma unroll
-    for (int t = 0; t < NT; ++t) h[t] = T(0);
+    for (int t = 0; t < NT; ++t) h[t] = 0.0;
+    double S = 0.0, U = 0.0, W = 0.0;  // POLY: parallel, tilt and curvature parts
     for (int i = 0; i < rows; ++i) acc_s[i * kCta + tid] = 0.0;
+    double* hs_s = work_s;
+    double* he_s = work_s + (size_t)(rows + 1) * kCta;
+    for (int t = 0; t <= B + 1; ++t) hs_s[t * kCta + tid] = 0.0;
 
-    // mixed: FP32 block partials of the discount sums, folded into acc_s per block
-    T pb[kMixed ? NT : 1];
-#pragma unroll
-    for (int t = 0; t < (kMixed ? NT : 1); ++t) pb[t] = T(0);
-    // FP64: curve at the start / end of the block, tenors 0 .. B+1
-    double* hs_s = reinterpret_cast<double*>(work_s);
-    double* he_s = hs_s + (size_t)(rows + 1) * kCta;
-    if (!kMixed)
-        for (int t = 0; t <= B + 1; ++t) hs_s[t * kCta + tid] = 0.0;
-
+    auto value_at = [&](int i) -> double {
+        double v = select_reg<NT, double>(h, i);
+        if (POLY) v += fma(P.tau[i], fma(P.tau[i], W, U), S);
+        return v;
+    };
     // price date i from the sampled numeraire (x_i, D_i)
     auto sample = [&](int i) {
-        const T hi = select_reg<NT, T>(h, i);
-        const double x = P.psamp[i] + (double)hi;
+        const double x = P.psamp[i] + value_at(i);
         const double a = P.psum[i] + acc_s[i * kCta + tid];
-        T cf;
-        if constexpr (kMixed) {
-            const float D = expf((float)(-a * P.dt));
-            const float mm = (float)P.m;
-            const float L = mm * expm1f((float)x / mm);
-            cf = D * ((float)P.payA[i] * L - (float)P.payB[i]);
-        } else {
-            const double D = exp(-a * P.dt);
-            const double L = P.m * (exp(x / P.m) - 1.0);
-            cf = D * (P.payA[i] * L - P.payB[i]);
-        }
-        cf_s[i * kCta + tid] = cf;
+        const double D = exp(-a * P.dt);
+        const double Lb = P.m * (exp(x / P.m) - 1.0);
+        cf_s[i * kCta + tid] = D * (P.payA[i] * Lb - P.payB[i]);
     };
 
     sample(1);
-    const T c = P.c;
+    const double c = P.c;
     for (int b = 1; b < B; ++b) {
-        double f0 = 0.0, f1 = 0.0, f2 = 0.0, hb = 0.0;  // FP64 mode: block sums of phi_k and of h[B]
+        double f0 = 0.0, f1 = 0.0, f2 = 0.0, hb = 0.0;  // block sums of phi_k and of h[B]
+        double sS = 0.0, sU = 0.0, sW = 0.0;            // POLY: block sums of S, U, W
         for (int s = 0; s < P.stride; ++s) {
             const int n = b * P.stride + s;
-            T phi0, phi1, phi2;
-            draw_phi<T, EXT>(ext, gpath, active ? lp : 0, P.n_paths, n, P.rk0, P.rk1, phi0, phi1, phi2);
-            euler_step<NT, T>(h, P, c, phi0, phi1, phi2);
-            if constexpr (kMixed) {
-                // only the groups of 8 tenors that meet (b, B] (uniform branches)
+            double phi0, phi1, phi2;
+            draw_phi<double, EXT>(ext, gpath, active ? lp : 0, P.n_paths, n, P.rk0, P.rk1, phi0, phi1, phi2);
+            if constexpr (POLY) {
+                const double al = fma(P.svc[2][0], phi2, fma(P.svc[1][0], phi1, P.svc[0][0] * phi0));
+                const double be = fma(P.svc[2][1], phi2, fma(P.svc[1][1], phi1, P.svc[0][1] * phi0));
+                const double ga = fma(P.svc[2][2], phi2, fma(P.svc[1][2], phi1, P.svc[0][2] * phi0));
+                const double src = -2.0 * P.k2 * W;
+                double hn[NT];
 #pragma unroll
-                for (int g = 0; g < NT; g += 8) {
-                    if (g + 7 > b && g <= B) {
-#pragma unroll
-                        for (int t = (g == 0 ? 1 : g); t < g + 8 && t < NT; ++t) pb[t] += h[t];
-                    }
+                for (int t = 0; t < NT; ++t) {
+                    const double d = (t < L) ? (h[t + 1] - h[t]) : (h[t] - h[t - 1]);
+                    hn[t] = fma(c, d, h[t]);
                 }
+                hn[L] += src;
+#pragma unroll
+                for (int t = 0; t < NT; ++t) h[t] = hn[t];
+                const double Sn = fma(P.k2, W, fma(P.k1, U, S)) + al;
+                U = fma(2.0 * P.k1, W, U) + be;
+                W += ga;
+                S = Sn;
+                sS += S;
+                sU += U;
+                sW += W;
             } else {
-                f0 += (double)phi0;
-                f1 += (double)phi1;
-                f2 += (double)phi2;
-                hb += (double)select_reg<NT, T>(h, B);
+                euler_step<NT, double>(h, P, c, phi0, phi1, phi2);
+                f0 += phi0;
+                f1 += phi1;
+                f2 += phi2;
             }
+            hb += select_reg<NT, double>(h, B);
         }
-        if constexpr (kMixed) {
-            // fold the FP32 block partials of the tenors still to be sampled
-            // into the FP64 accumulators
+        // stage the block-end curve, then recover the block sums of tenors (b, B]
 #pragma unroll
-            for (int t = 1; t < NT; ++t) {
-                work_s[t * kCta + tid] = pb[t];
-                pb[t] = T(0);
-            }
-            for (int t = b + 1; t <= B; ++t) acc_s[t * kCta + tid] += (double)work_s[t * kCta + tid];
-        } else {
-            // stage the block-end curve, then recover the block sums of tenors (b, B]
-#pragma unroll
-            for (int t = 0; t < NT; ++t)
-                if (t <= B + 1) he_s[t * kCta + tid] = (double)h[t];
-            double Hn = hb;
-            acc_s[B * kCta + tid] += Hn;
-            double dn = he_s[B * kCta + tid] - hs_s[B * kCta + tid];
-            for (int t = B - 1; t > b; --t) {
-                const double d = he_s[t * kCta + tid] - hs_s[t * kCta + tid];
-                const double xi = fma((double)P.sv[2][t], f2, fma((double)P.sv[1][t], f1, (double)P.sv[0][t] * f0));
-                const double ad = fma((double)c, dn - d, d);
-                Hn = fma(xi - ad, P.inv_c, Hn);
-                acc_s[t * kCta + tid] += Hn;
-                dn = d;
-            }
-            double* tmp = hs_s;
-            hs_s = he_s;
-            he_s = tmp;
+        for (int t = 0; t < NT; ++t)
+            if (t <= B + 1) he_s[t * kCta + tid] = h[t];
+        auto poly_part = [&](int t) -> double {
+            return POLY ? fma(P.tau[t], fma(P.tau[t], sW, sU), sS) : 0.0;
+        };
+        double Hn = hb;
+        acc_s[B * kCta + tid] += Hn + poly_part(B);
+        double dn = he_s[B * kCta + tid] - hs_s[B * kCta + tid];
+        for (int t = B - 1; t > b; --t) {
+            const double d = he_s[t * kCta + tid] - hs_s[t * kCta + tid];
+            const double xi = POLY ? 0.0 : fma(P.sv[2][t], f2, fma(P.sv[1][t], f1, P.sv[0][t] * f0));
+            const double ad = fma(c, dn - d, d);
+            Hn = fma(xi - ad, P.inv_c, Hn);
+            acc_s[t * kCta + tid] += Hn + poly_part(t);
+            dn = d;
         }
+        double* tmp = hs_s;
+        hs_s = he_s;
+        he_s = tmp;
         sample(b + 1);
     }
 
     // exposure profile E_j = max(sum_{i>j} cf_i, 0), FP64 suffix sums, and the
     // path's CVA contribution sum_j cvaw[j] E_j
-    T* e_s = work_s;
+    double* e_s = work_s;
     double v = 0.0, cva_c = 0.0;
-    e_s[B * kCta + tid] = T(0);
+    e_s[B * kCta + tid] = 0.0;
     for (int j = B - 1; j >= 0; --j) {
-        v += (double)cf_s[(j + 1) * kCta + tid];
+        v += cf_s[(j + 1) * kCta + tid];
         double e = (v > 0.0) ? v : 0.0;
         if (!active) e = 0.0;
-        e_s[j * kCta + tid] = (T)e;
+        e_s[j * kCta + tid] = e;
         cva_c = fma(P.cvaw[j], e, cva_c);
     }
     __syncthreads();
@@ -209,11 +195,11 @@ __global__ void __launch_bounds__(Prec<T>::kThreads, Prec<T>::kMixed ? 3 : 4)
     const int warp = tid >> 5, lane = tid & 31;
     const int R = B + 3;
     for (int j = warp; j <= B; j += kCta / 32) {
-        double s = 0.0;
+        double sum = 0.0;
 #pragma unroll
-        for (int q = 0; q < kCta / 32; ++q) s += (double)e_s[j * kCta + lane + 32 * q];
-        s = warp_sum(s);
-        if (lane == 0) partials[(size_t)blockIdx.x * R + j] = s;
+        for (int q = 0; q < kCta / 32; ++q) sum += e_s[j * kCta + lane + 32 * q];
+        sum = warp_sum(sum);
+        if (lane == 0) partials[(size_t)blockIdx.x * R + j] = sum;
     }
     {
         const double s1 = warp_sum(cva_c), s2 = warp_sum(cva_c * cva_c);
@@ -222,10 +208,7 @@ __global__ void __launch_bounds__(Prec<T>::kThreads, Prec<T>::kMixed ? 3 : 4)
             red_s[kCta / 32 + warp] = s2;
         }
     }
-    if (P.store_exposures) {
-        // date rows of this CTA's paths, smem -> HBM with the bulk-copy (TMA) engine
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    }
+    if (P.store_exposures) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
     if (tid == 0) {
         double s1 = 0.0, s2 = 0.0;
@@ -236,11 +219,11 @@ __global__ void __launch_bounds__(Prec<T>::kThreads, Prec<T>::kMixed ? 3 : 4)
         partials[(size_t)blockIdx.x * R + B + 1] = s1;
         partials[(size_t)blockIdx.x * R + B + 2] = s2;
         if (P.store_exposures) {
+            // date rows of this CTA's paths, smem -> HBM with the bulk-copy (TMA) engine
             const int64_t cnt = (P.n_paths - cta_base < kCta) ? (P.n_paths - cta_base) : kCta;
-            constexpr int kVec = 16 / (int)sizeof(T);
-            const uint32_t bytes = (uint32_t)(((cnt + kVec - 1) / kVec) * kVec * sizeof(T));
+            const uint32_t bytes = (uint32_t)(((cnt + 1) / 2) * 2 * sizeof(double));
             for (int j = 0; j <= B; ++j) {
-                T* dst = estore + (size_t)j * (size_t)P.ld + (size_t)cta_base;
+                double* dst = estore + (size_t)j * (size_t)P.ld + (size_t)cta_base;
                 const uint32_t src = (uint32_t)__cvta_generic_to_shared(e_s + (size_t)j * kCta);
                 asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
                              :: "l"(dst), "r"(src), "r"(bytes) : "memory");
@@ -251,7 +234,6 @@ __global__ void __launch_bounds__(Prec<T>::kThreads, Prec<T>::kMixed ? 3 : 4)
     }
 }
 
-// ---------------------------------------------------------------------------
 // Mixed precision with packed FP32x2 arithmetic.  The curve of one path is held
 // as H = ceil(NT/2) float2 pairs, pair p = {h[p], h[p+H]}: the upwind neighbour
 // h[t+1] of every tenor lies in the same component of pair p+1, so each packed
@@ -274,12 +256,11 @@ __global__ void __launch_bounds__(Prec<T>::kThreads, Prec<T>::kMixed ? 3 : 4)
 // Shared memory per thread: acc (B+1) FP64 discount sums, whose slot i holds
 // date i's cash flow once tenor i is sampled; hs (B+2) FP32 curve at the block
 // start, reused for the exposure tile at the end.
-template <int NT, bool EXT>
+template <int NT, bool EXT, bool POLY>
 __global__ void __launch_bounds__(kCta, 4)
     path_kernel_mixed(const __grid_constant__ MixedParams M, const double* __restrict__ ext,
                       double* __restrict__ partials, float* __restrict__ estore)
 {
-    constexpr int H = PairGrid<NT>::H;
     const PathParams<float>& P = M.P;
     extern __shared__ __align__(128) unsigned char smem[];
     const int tid = threadIdx.x;
@@ -294,45 +275,39 @@ __global__ void __launch_bounds__(kCta, 4)
     const bool active = lp < P.n_paths;
     const uint64_t gpath = P.path_offset + (uint64_t)lp;
 
-    float2 h[H];
-#pragma unroll
-    for (int p = 0; p < H; ++p) h[p] = make_float2(0.f, 0.f);
+    MixedPath<NT, POLY> x;
+    x.reset();
     for (int i = 0; i < rows; ++i) acc_s[i * kCta + tid] = 0.0;
     for (int t = 0; t <= B + 1; ++t) hs_s[t * kCta + tid] = 0.f;
 
-    // tenor t of the packed curve (t static after unrolling)
-    auto ht = [&](int t) -> float { return t < H ? h[t].x : h[t - H].y; };
-
     auto sample = [&](int i) {
-        const double x = P.psamp[i] + (double)select_pair<NT>(h, i);
+        const double xv = P.psamp[i] + (double)x.value(P, i);
         const double a = P.psum[i] + acc_s[i * kCta + tid];
         const float D = expf((float)(-a * P.dt));
         const float mm = (float)P.m;
-        const float L = mm * expm1f((float)x / mm);
+        const float L = mm * expm1f((float)xv / mm);
         acc_s[i * kCta + tid] = (double)(D * ((float)P.payA[i] * L - (float)P.payB[i]));  // cash flow of date i
     };
 
     sample(1);
     for (int b = 1; b < B; ++b) {
-        float F0 = 0.f, F1 = 0.f, F2 = 0.f, H1 = 0.f;  // block sums of phi_k and of h[1]
+        BlockSums bs;
+        bs.reset();
         for (int s = 0; s < P.stride; ++s) {
             const int n = b * P.stride + s;
             float phi0, phi1, phi2;
             draw_phi<float, EXT>(ext, gpath, active ? lp : 0, P.n_paths, n, P.rk0, P.rk1, phi0, phi1, phi2);
-            euler_step_pairs<NT>(h, M, phi0, phi1, phi2);
-            F0 += phi0;
-            F1 += phi1;
-            F2 += phi2;
-            H1 += h[1].x;
+            x.step(M, phi0, phi1, phi2);
+            bs.add(x, phi0, phi1, phi2);
         }
-        // recover the block sums of tenors 2 .. B upwards from H[1]; fold (b, B] into FP64
-        recover_sums_up<NT>(h, hs_s, tid, kCta, P, F0, F1, F2, H1, B, [&](int t, float Ht) {
+        // block sums of tenors 2 .. B; fold (b, B] into FP64
+        block_sums_up<NT, POLY>(x, hs_s, tid, kCta, P, bs, B, [&](int t, float Ht) {
             if (t > b) acc_s[t * kCta + tid] += (double)Ht;
         });
-        // the block-end curve is the next block's start (tenors 1 .. B+1)
+        // the block-end curve (POLY: its convected part) is the next block's start
 #pragma unroll
         for (int t = 1; t < NT; ++t)
-            if (t <= B + 1) hs_s[t * kCta + tid] = ht(t);
+            if (t <= B + 1) hs_s[t * kCta + tid] = pair_tenor<NT>(x.h, t);
         sample(b + 1);
     }
 
@@ -407,6 +382,10 @@ void pack_mixed_params(int nt, const PathParams<float>& P, MixedParams& M)
             M.svp[k][p].y = (H + p < nt) ? P.sv[k][H + p] : 0.0f;
         }
     M.cp = make_float2(P.c, P.c);
+    for (int k = 0; k < kFactors; ++k)
+        for (int d = 0; d < 3; ++d) M.svcf[k][d] = (float)P.svc[k][d];
+    M.k1f = (float)P.k1;
+    M.k2f = (float)P.k2;
 }
 
 // ---------------------------------------------------------------------------
@@ -608,43 +587,43 @@ __global__ void widen_exposures_kernel(const T* __restrict__ in, int64_t ld, int
 // ---------------------------------------------------------------------------
 // Host launchers
 // ---------------------------------------------------------------------------
-template <int NT, typename T, bool EXT>
-static cudaError_t launch_path_t(const PathParams<T>& P, const double* ext, double* partials, T* estore,
+template <int NT, bool EXT, bool POLY>
+static cudaError_t launch_fp64_t(const PathParams<double>& P, const double* ext, double* partials, double* estore,
                                  cudaStream_t s)
 {
-    const size_t smem = path_smem_bytes(NT, P.n_blocks, Prec<T>::kMixed);
-    auto k = path_kernel<NT, T, EXT>;
+    const size_t smem = path_smem_bytes(NT, P.n_blocks, false);
+    auto k = path_kernel_fp64<NT, EXT, POLY>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    constexpr int cta = Prec<T>::kThreads;
-    const int64_t grid = (P.n_paths + cta - 1) / cta;
-    k<<<(unsigned)grid, cta, smem, s>>>(P, ext, partials, estore);
+    const int64_t grid = (P.n_paths + kFp64Cta - 1) / kFp64Cta;
+    k<<<(unsigned)grid, kFp64Cta, smem, s>>>(P, ext, partials, estore);
     return cudaGetLastError();
 }
 
-template <typename T>
-static cudaError_t launch_path_nt(int nt, const PathParams<T>& P, const double* ext, double* partials, T* estore,
-                                  cudaStream_t s)
+template <int NT>
+static cudaError_t launch_fp64_nt(const PathParams<double>& P, bool poly, const double* ext, double* partials,
+                                  double* estore, cudaStream_t s)
 {
-    if (nt == 51) return ext ? launch_path_t<51, T, true>(P, ext, partials, estore, s)
-                             : launch_path_t<51, T, false>(P, ext, partials, estore, s);
-    if (nt == 61) return ext ? launch_path_t<61, T, true>(P, ext, partials, estore, s)
-                             : launch_path_t<61, T, false>(P, ext, partials, estore, s);
+    if (ext) return poly ? launch_fp64_t<NT, true, true>(P, ext, partials, estore, s)
+                         : launch_fp64_t<NT, true, false>(P, ext, partials, estore, s);
+    return poly ? launch_fp64_t<NT, false, true>(P, ext, partials, estore, s)
+                : launch_fp64_t<NT, false, false>(P, ext, partials, estore, s);
+}
+
+cudaError_t launch_path_fp64(int nt, const PathParams<double>& P, bool poly, const double* ext, double* partials,
+                             double* estore, cudaStream_t s)
+{
+    if (nt == 51) return launch_fp64_nt<51>(P, poly, ext, partials, estore, s);
+    if (nt == 61) return launch_fp64_nt<61>(P, poly, ext, partials, estore, s);
     return cudaErrorInvalidValue;
 }
 
-cudaError_t launch_path_fp64(int nt, const PathParams<double>& P, const double* ext, double* partials,
-                             double* estore, cudaStream_t s)
-{
-    return launch_path_nt<double>(nt, P, ext, partials, estore, s);
-}
-
-template <int NT, bool EXT>
+template <int NT, bool EXT, bool POLY>
 static cudaError_t launch_mixed_t(const MixedParams& M, const double* ext, double* partials, float* estore,
                                   cudaStream_t s)
 {
     const size_t smem = mixed_smem_bytes(NT, M.P.n_blocks);
-    auto k = path_kernel_mixed<NT, EXT>;
+    auto k = path_kernel_mixed<NT, EXT, POLY>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const int64_t grid = (M.P.n_paths + kCta - 1) / kCta;
@@ -652,13 +631,21 @@ static cudaError_t launch_mixed_t(const MixedParams& M, const double* ext, doubl
     return cudaGetLastError();
 }
 
-cudaError_t launch_path_mixed(int nt, const MixedParams& M, const double* ext, double* partials, float* estore,
-                              cudaStream_t s)
+template <int NT>
+static cudaError_t launch_mixed_nt(const MixedParams& M, bool poly, const double* ext, double* partials,
+                                   float* estore, cudaStream_t s)
 {
-    if (nt == 51) return ext ? launch_mixed_t<51, true>(M, ext, partials, estore, s)
-                             : launch_mixed_t<51, false>(M, ext, partials, estore, s);
-    if (nt == 61) return ext ? launch_mixed_t<61, true>(M, ext, partials, estore, s)
-                             : launch_mixed_t<61, false>(M, ext, partials, estore, s);
+    if (ext) return poly ? launch_mixed_t<NT, true, true>(M, ext, partials, estore, s)
+                         : launch_mixed_t<NT, true, false>(M, ext, partials, estore, s);
+    return poly ? launch_mixed_t<NT, false, true>(M, ext, partials, estore, s)
+                : launch_mixed_t<NT, false, false>(M, ext, partials, estore, s);
+}
+
+cudaError_t launch_path_mixed(int nt, const MixedParams& M, bool poly, const double* ext, double* partials,
+                              float* estore, cudaStream_t s)
+{
+    if (nt == 51) return launch_mixed_nt<51>(M, poly, ext, partials, estore, s);
+    if (nt == 61) return launch_mixed_nt<61>(M, poly, ext, partials, estore, s);
     return cudaErrorInvalidValue;
 }
 
@@ -669,7 +656,7 @@ size_t path_smem(int nt, int n_blocks, bool mixed)
     return mixed ? mixed_smem_bytes(nt, n_blocks) : path_smem_bytes(nt, n_blocks, false);
 }
 
-int path_cta(bool mixed) { return path_threads(mixed); }
+int path_cta(bool mixed) { return mixed ? kCta : kFp64Cta; }
 
 cudaError_t launch_reduce(const double* partials, int64_t n_rows, int R, double* sums, const FinalParams& F,
                           double* result, cudaStream_t s)

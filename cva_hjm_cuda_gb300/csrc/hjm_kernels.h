@@ -37,13 +37,17 @@ struct MixedParams {
     PathParams<float> P;
     float2 svp[kFactors][kMaxTenor / 2];
     float2 cp;  // {c, c}
+    // polynomial volatility in FP32: sqrt(dt) sigma_k(T) = sum_d svcf[k][d] T^d
+    float svcf[kFactors][3];
+    float k1f, k2f;  // c dtau, c dtau^2
 };
 
 
-cudaError_t launch_path_fp64(int nt, const PathParams<double>& P, const double* ext, double* partials,
+// poly: the volatility factors are polynomials of degree <= 2 in T (PathParams::svc)
+cudaError_t launch_path_fp64(int nt, const PathParams<double>& P, bool poly, const double* ext, double* partials,
                              double* estore, cudaStream_t s);
-cudaError_t launch_path_mixed(int nt, const MixedParams& M, const double* ext, double* partials, float* estore,
-                              cudaStream_t s);
+cudaError_t launch_path_mixed(int nt, const MixedParams& M, bool poly, const double* ext, double* partials,
+                              float* estore, cudaStream_t s);
 void pack_mixed_params(int nt, const PathParams<float>& P, MixedParams& M);
 bool path_tenor_supported(int nt);
 size_t path_smem(int nt, int n_blocks, bool mixed);
@@ -72,6 +76,7 @@ struct AdjParams {
 size_t adjoint_smem(int nt, int n_blocks);
 int adjoint_columns(int nt, int n_blocks);
 int adjoint_cta();  // paths per CTA of the adjoint kernel (one partial-sum row each)
-cudaError_t launch_adjoint(int nt, const AdjParams& A, double* partials, float* ck_h, double* ck_a, cudaStream_t s);
+cudaError_t launch_adjoint(int nt, const AdjParams& A, bool poly, double* partials, float* ck_h, double* ck_a,
+                           cudaStream_t s);
 
 }  // namespace hjm

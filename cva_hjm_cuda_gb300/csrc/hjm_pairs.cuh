@@ -98,6 +98,113 @@ __device__ __forceinline__ void recover_sums_up(const float2 (&h)[PairGrid<NT>::
     }
 }
 
+// The convection part of the step, h <- A h + src e_L (polynomial volatility:
+// the noise lives in the scalar parts S, U, W), on the packed curve.
+template <int NT>
+__device__ __forceinline__ void convect_pairs(float2 (&h)[PairGrid<NT>::H], float2 cp, float src)
+{
+    constexpr int H = PairGrid<NT>::H, L = PairGrid<NT>::L;
+    const float2 m1 = make_float2(-1.0f, -1.0f);
+    float2 hn[H];
+#pragma unroll
+    for (int p = 0; p < H; ++p) {
+        const int q = H + p;
+        float2 d;
+        if (p + 1 < H && q < L) {
+            d = __ffma2_rn(m1, h[p], h[p + 1]);
+        } else {
+            d.x = ((p + 1 < H) ? h[p + 1].x : h[0].y) - h[p].x;
+            if (q < L)
+                d.y = h[p + 1].y - h[p].y;
+            else if (q == L)
+                d.y = h[p].y - h[p - 1].y;
+            else
+                d.y = 0.0f;
+        }
+        hn[p] = __ffma2_rn(cp, d, h[p]);
+        if (q == L) hn[p].y += src;
+    }
+#pragma unroll
+    for (int p = 0; p < H; ++p) h[p] = hn[p];
+}
+
+// One path's stochastic curve in mixed precision.  Table volatility: the packed
+// curve h itself.  Polynomial volatility (POLY, degree <= 2): h = S 1 + U T +
+// W T^2 + hc, with the packed hc only convected (see the FP64 kernel for the
+// algebra: A 1 = 1, A T = T + c dtau 1, A T^2 = T^2 + 2 c dtau T + c dtau^2 1
+// - 2 c dtau^2 e_L).
+template <int NT, bool POLY>
+struct MixedPath {
+    static constexpr int H = PairGrid<NT>::H;
+    float2 h[H];
+    float S, U, W;
+
+    __device__ __forceinline__ void reset()
+    {
+#pragma unroll
+        for (int p = 0; p < H; ++p) h[p] = make_float2(0.f, 0.f);
+        S = U = W = 0.f;
+    }
+    __device__ __forceinline__ void step(const MixedParams& M, float phi0, float phi1, float phi2)
+    {
+        if constexpr (POLY) {
+            const float al = fmaf(M.svcf[2][0], phi2, fmaf(M.svcf[1][0], phi1, M.svcf[0][0] * phi0));
+            const float be = fmaf(M.svcf[2][1], phi2, fmaf(M.svcf[1][1], phi1, M.svcf[0][1] * phi0));
+            const float ga = fmaf(M.svcf[2][2], phi2, fmaf(M.svcf[1][2], phi1, M.svcf[0][2] * phi0));
+            convect_pairs<NT>(h, M.cp, -2.0f * M.k2f * W);
+            const float Sn = fmaf(M.k2f, W, fmaf(M.k1f, U, S)) + al;
+            U = fmaf(2.0f * M.k1f, W, U) + be;
+            W += ga;
+            S = Sn;
+        } else {
+            euler_step_pairs<NT>(h, M, phi0, phi1, phi2);
+        }
+    }
+    // tenor i (runtime) of the stochastic curve
+    __device__ __forceinline__ float value(const PathParams<float>& P, int i) const
+    {
+        float v = select_pair<NT>(h, i);
+        if (POLY) v += fmaf(P.tau[i], fmaf(P.tau[i], W, U), S);
+        return v;
+    }
+};
+
+// Running sums over a block (or a partial block) of steps for the recovery.
+struct BlockSums {
+    float F0, F1, F2, H1, sS, sU, sW;
+    __device__ __forceinline__ void reset() { F0 = F1 = F2 = H1 = sS = sU = sW = 0.f; }
+    template <int NT, bool POLY>
+    __device__ __forceinline__ void add(const MixedPath<NT, POLY>& x, float phi0, float phi1, float phi2)
+    {
+        if constexpr (POLY) {
+            sS += x.S;
+            sU += x.U;
+            sW += x.W;
+        } else {
+            F0 += phi0;
+            F1 += phi1;
+            F2 += phi2;
+        }
+        H1 += x.h[1].x;
+    }
+};
+
+// Block sums of tenors 2 .. tmax of the stochastic curve over the steps the
+// sums cover (upward recovery from tenor 1 plus, POLY, the scalar parts);
+// fold(t, sum) is called for t = 2 .. tmax.
+template <int NT, bool POLY, typename Fold>
+__device__ __forceinline__ void block_sums_up(const MixedPath<NT, POLY>& x, const float* hs_s, int tid, int cta,
+                                              const PathParams<float>& P, const BlockSums& bs, int tmax, Fold fold)
+{
+    if constexpr (POLY) {
+        recover_sums_up<NT>(x.h, hs_s, tid, cta, P, 0.f, 0.f, 0.f, bs.H1, tmax, [&](int t, float Ht) {
+            fold(t, Ht + fmaf(P.tau[t], fmaf(P.tau[t], bs.sW, bs.sU), bs.sS));
+        });
+    } else {
+        recover_sums_up<NT>(x.h, hs_s, tid, cta, P, bs.F0, bs.F1, bs.F2, bs.H1, tmax, fold);
+    }
+}
+
 // g <- A^T g on the packed adjoint state (A: the upwind convection of the Euler
 // step).  Per tenor, with L the last tenor:
 //   t = 0:          (1 - c) g[0]

@@ -88,6 +88,15 @@ class HJMEngine:
     def keep_exposures(self, keep: bool = True) -> None:
         self._check(self.lib.hjm_ctx_keep_exposures(self.ctx, 1 if keep else 0))
 
+    def vol_decomposition(self, enable: bool | None = None) -> bool:
+        """Allow (True) or forbid (False) the polynomial volatility decomposition;
+        returns whether the current market runs it."""
+        if enable is not None:
+            self._check(self.lib.hjm_ctx_set_vol_decomposition(self.ctx, 1 if enable else 0))
+        active = C.c_int32(0)
+        self._check(self.lib.hjm_ctx_vol_decomposition(self.ctx, C.byref(active)))
+        return bool(active.value)
+
     def set_market(self, market: Market, drift: bool = True) -> None:
         spot, vol = _f64(market.spot), _f64(market.vol).ravel()
         d = _f64(market.drift) if drift else None

@@ -81,6 +81,18 @@ hjm_status hjm_ctx_set_stream(hjm_ctx* ctx, void* cuda_stream);
  * hjm_get_exposures); they are always kept when a PFE is requested. */
 hjm_status hjm_ctx_keep_exposures(hjm_ctx* ctx, int32_t keep);
 
+/* Polynomial volatility decomposition.  When every volatility factor is a
+ * polynomial of degree <= 2 in the tenor T (given by hjm_set_market_poly, or a
+ * table that hjm_set_market finds to be one to 1e-12 of each row's scale, as
+ * the reference's own table simulation_gpu_testing.cpp:47-63 is), the kernels
+ * carry the stochastic curve as S + U T + W T^2 plus a remainder driven only at
+ * the last tenor, instead of adding the three factor columns to every tenor
+ * each step (simulation_gpu.cu:153-180).  enable = 0 forces the generic
+ * table-driven step; default 1.  hjm_ctx_vol_decomposition reports whether the
+ * current market runs the decomposition. */
+hjm_status hjm_ctx_set_vol_decomposition(hjm_ctx* ctx, int32_t enable);
+hjm_status hjm_ctx_vol_decomposition(hjm_ctx* ctx, int32_t* active);
+
 /* ---- inputs --------------------------------------------------------------- */
 /* Market: spot forward curve, volatility factors, and the drift.  With
  * drift_host == NULL the Musiela no-arbitrage drift is computed in FP64 by the

@@ -1,0 +1,203 @@
+"""GPU parity of the polynomial-volatility path (hjm_set_market_poly).
+
+With every factor a polynomial of degree <= 2 in the tenor T, the kernels
+carry the stochastic curve as S + U T + W T^2 plus a convected remainder that
+is driven only at the last tenor, instead of injecting the three factor
+columns into every tenor each step.  The decomposition is exact algebra, so
+the oracle's table-driven restatement of simulation_cpu.h (volatility table
+sampled from the same polynomials, trapezoid drift) is the reference:
+
+* FP64 EE, exposures, PFE and CVA within 1e-10 relative of the oracle;
+* mixed precision within 1e-4 relative and inside the Monte Carlo error;
+* external normals on the polynomial path reproduce the Philox run;
+* the 30-year (61-tenor) grid, ragged path counts, and the netting set.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle_lib as O
+from cva_hjm_cuda_gb300.market import (DEFAULT_VOL_COEFFS, Market, RunConfig, Swap, nelson_siegel_curve,
+                                       random_netting_set, tenor_grid)
+
+pytestmark = pytest.mark.gpu
+
+FP64_RTOL = 1e-10
+MIXED_RTOL = 1e-4
+
+
+def _assert_rel(actual, desired, rtol, what):
+    actual, desired = np.asarray(actual), np.asarray(desired)
+    scale = np.max(np.abs(desired)) if desired.size else 0.0
+    err = np.abs(actual - desired)
+    bad = err > rtol * np.maximum(np.abs(desired), 1e-300)
+    bad &= err > rtol * scale * 1e-3
+    assert not np.any(bad), f"{what}: max rel err {np.max(err / np.maximum(np.abs(desired), 1e-300)):.3e}"
+
+
+def _poly_market(engine, nt=51, coef=DEFAULT_VOL_COEFFS):
+    mk = Market(n_tenor=nt, vol_coeffs=np.array(coef))
+    engine.set_market_poly(nt, mk.dtau, mk.spot, coef)
+    return mk
+
+
+@pytest.fixture(scope="module")
+def poly_config1(engine):
+    mk = _poly_market(engine)
+    sw = Swap()
+    engine.set_swap(sw)
+    cfg = RunConfig(n_paths=5000, n_steps=1000, dt=0.01, seed=4321)
+    normals = engine.dump_normals(cfg.n_paths, cfg.n_steps, cfg.seed)
+    x = O.exposure_paths(mk, sw, cfg.n_steps, cfg.dt, normals)
+    ee = O.expected_exposure(x)
+    cva, _ = O.cva(ee, 21, mk.dtau, cfg.hazard, cfg.recovery)
+    pfe = O.pfe(x, 21, cfg.pfe_quantile)
+    return mk, sw, cfg, normals, x, ee, cva, pfe
+
+
+def test_poly_fp64_vs_oracle(engine, poly_config1):
+    mk, sw, cfg, normals, xo, ee, cva, pfe = poly_config1
+    _poly_market(engine)
+    engine.set_swap(sw)
+    engine.keep_exposures(True)
+    v = engine.run(cfg, "fp64")
+    x = engine.exposures()
+    engine.keep_exposures(False)
+    _assert_rel(x, xo[:, :21].T, FP64_RTOL, "exposures")
+    _assert_rel(v.ee, ee, FP64_RTOL, "EE")
+    _assert_rel(v.cva, cva, FP64_RTOL, "CVA")
+    _assert_rel(v.pfe[:21], pfe, FP64_RTOL, "PFE")
+
+
+def test_poly_mixed_vs_oracle(engine, poly_config1):
+    mk, sw, cfg, normals, xo, ee, cva, pfe = poly_config1
+    _poly_market(engine)
+    engine.set_swap(sw)
+    v = engine.run(cfg, "mixed")
+    rel = np.abs(v.ee[:20] - ee[:20]) / ee[:20]
+    assert np.max(rel) < MIXED_RTOL, f"per-point EE rel err {rel}"
+    assert abs(v.cva - cva) < MIXED_RTOL * cva
+    assert abs(v.cva - cva) < v.cva_stderr
+    _assert_rel(v.pfe[:20], pfe[:20], MIXED_RTOL, "mixed PFE")
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_poly_external_normals_reproduce_philox(engine, poly_config1, precision):
+    mk, sw, cfg, normals, *_ = poly_config1
+    _poly_market(engine)
+    engine.set_swap(sw)
+    a = engine.run(cfg, precision)
+    b = engine.run_with_normals(normals, cfg.n_steps, cfg.dt, precision)
+    np.testing.assert_array_equal(a.ee, b.ee)
+    assert a.cva == b.cva
+
+
+@pytest.fixture
+def generic_path(engine):
+    """Force the generic table-driven Euler step for the test's duration."""
+    engine.vol_decomposition(False)
+    try:
+        yield
+    finally:
+        engine.vol_decomposition(True)
+
+
+def test_reference_table_is_detected_as_polynomial(engine, golden_10y):
+    from conftest import market_from_golden
+
+    mk, sw = market_from_golden(golden_10y)
+    engine.set_market(mk)
+    assert engine.vol_decomposition()
+    bumped = Market(vol=mk.vol + 1e-6 * np.sin(np.arange(51))[None, :])
+    engine.set_market(bumped)
+    assert not engine.vol_decomposition()
+    engine.vol_decomposition(False)
+    engine.set_market(mk)
+    assert not engine.vol_decomposition()
+    engine.vol_decomposition(True)
+    assert engine.vol_decomposition()
+
+
+def test_generic_path_vs_oracle(engine, poly_config1, generic_path):
+    mk, sw, cfg, normals, xo, ee, cva, pfe = poly_config1
+    engine.set_market(mk)
+    engine.set_swap(sw)
+    assert not engine.vol_decomposition()
+    v = engine.run(cfg, "fp64")
+    _assert_rel(v.ee, ee, FP64_RTOL, "EE")
+    _assert_rel(v.cva, cva, FP64_RTOL, "CVA")
+    _assert_rel(v.pfe[:21], pfe, FP64_RTOL, "PFE")
+    m = engine.run(cfg, "mixed")
+    assert np.max(np.abs(m.ee[:20] - ee[:20]) / ee[:20]) < MIXED_RTOL
+    assert abs(m.cva - cva) < MIXED_RTOL * cva
+
+
+def test_non_polynomial_table_vs_oracle(engine):
+    """A table that is no quadratic runs the generic step, at the same parity."""
+    mk = Market(vol=Market().vol * (1.0 + 0.1 * np.cos(np.arange(51) / 7.0))[None, :])
+    sw = Swap()
+    engine.set_market(mk)
+    engine.set_swap(sw)
+    assert not engine.vol_decomposition()
+    cfg = RunConfig(n_paths=3000, seed=8)
+    normals = engine.dump_normals(cfg.n_paths, cfg.n_steps, cfg.seed)
+    x = O.exposure_paths(mk, sw, cfg.n_steps, cfg.dt, normals)
+    ee = O.expected_exposure(x)
+    cva, _ = O.cva(ee, 21, mk.dtau, cfg.hazard, cfg.recovery)
+    v = engine.run(cfg, "fp64")
+    _assert_rel(v.ee, ee, FP64_RTOL, "EE")
+    _assert_rel(v.cva, cva, FP64_RTOL, "CVA")
+
+
+def test_poly_matches_table_market(engine):
+    """The same market on the generic step and on the decomposition."""
+    cfg = RunConfig(n_paths=30000, seed=99)
+    mk = Market()
+    engine.vol_decomposition(False)
+    try:
+        engine.set_market(mk)
+        engine.set_swap(Swap())
+        t64, tmx = engine.run(cfg, "fp64"), engine.run(cfg, "mixed")
+    finally:
+        engine.vol_decomposition(True)
+    _poly_market(engine)
+    engine.set_swap(Swap())
+    p64, pmx = engine.run(cfg, "fp64"), engine.run(cfg, "mixed")
+    _assert_rel(p64.ee, t64.ee, FP64_RTOL, "fp64 EE poly vs table")
+    _assert_rel(p64.cva, t64.cva, FP64_RTOL, "fp64 CVA poly vs table")
+    _assert_rel(pmx.ee[:20], tmx.ee[:20], MIXED_RTOL, "mixed EE poly vs table")
+    assert abs(pmx.cva - tmx.cva) < MIXED_RTOL * tmx.cva
+
+
+@pytest.mark.parametrize("n_paths", [1, 63, 257])
+def test_poly_30y_ragged_vs_oracle(engine, n_paths):
+    mk = _poly_market(engine, nt=61)
+    sw = Swap(n_tenor=61, n_periods=60)
+    engine.set_swap(sw)
+    cfg = RunConfig(n_paths=n_paths, n_steps=3000, dt=0.01, seed=11)
+    normals = engine.dump_normals(cfg.n_paths, cfg.n_steps, cfg.seed)
+    x = O.exposure_paths(mk, sw, cfg.n_steps, cfg.dt, normals)
+    ee = O.expected_exposure(x)
+    cva, _ = O.cva(ee, 61, mk.dtau, cfg.hazard, cfg.recovery)
+    v = engine.run(cfg, "fp64")
+    _assert_rel(v.ee[:61], ee[:61], FP64_RTOL, "30y EE")
+    _assert_rel(v.cva, cva, FP64_RTOL, "30y CVA")
+    m = engine.run(cfg, "mixed")
+    if n_paths >= 63:
+        assert abs(m.cva - cva) < 1e-3 * cva
+
+
+def test_poly_netting_set_vs_oracle(engine):
+    mk = _poly_market(engine, nt=61)
+    ns = random_netting_set(64)
+    engine.set_netting_set(ns)
+    payA, payB = ns.payoff_vectors(61)
+    cfg = RunConfig(n_paths=2000, n_steps=3000, dt=0.01, seed=3)
+    normals = engine.dump_normals(cfg.n_paths, cfg.n_steps, cfg.seed)
+    x = O.exposure_paths_netting(mk, payA, payB, cfg.n_steps, cfg.dt, normals)
+    ee = O.expected_exposure(x)
+    cva, _ = O.cva(ee, 61, mk.dtau, cfg.hazard, cfg.recovery)
+    v = engine.run(cfg, "fp64")
+    _assert_rel(v.ee[:61], ee[:61], FP64_RTOL, "netting EE")
+    _assert_rel(v.cva, cva, FP64_RTOL, "netting CVA")
