@@ -61,16 +61,29 @@ def env_rank():
             int(os.environ.get("WORLD_SIZE", 1)))
 
 
-def algorithmic_flops_per_path(n_tenor: int, n_steps: int, stride: int) -> int:
-    """Flops the method needs per path: the Euler update of the stochastic curve,
-    4 FMAs + 1 subtraction = 9 flops per tenor per evolved step (the first block
-    holds the curve at spot and does no arithmetic), plus one addition per
-    discount accumulation of a tenor that is still to be sampled.  Pricing,
-    normals and reductions are not counted, so the fraction is a lower bound."""
+def algorithmic_flops_per_path(n_tenor: int, n_steps: int, stride: int, form: str) -> int:
+    """Floating-point operations the path kernel's algorithm needs per path
+    (FMA = 2), counted from its formulas, not measured.
+
+    ``poly`` (volatility factors quadratic in T, the reference's own table):
+    per evolved Euler step the growth-scaled convection of the remainder
+    (NT + 1 FMAs), the noise projection onto the three scalar parts
+    (3 MUL + 6 FMA), their update (4 FMA + 3 ADD), the last-tenor source
+    (1 MUL) and the block sums (3 ADD + 1 FMA): 2 NT + 32 flops.
+    ``table`` (generic volatility table): 4 FMAs per tenor (three factor
+    loadings and the convection; 5 operations at the last tenor), the
+    normals' scaling (3 MUL), the block sums (3 ADD + 1 FMA): 8 NT + 10.
+    Both add, per block, the renormalisation (NT MUL) and the block-sum
+    recovery of the tenors still to be sampled (about 12 flops each).  The
+    first block holds the curve at spot and does no arithmetic.  Normals,
+    pricing and reductions are not counted, so the fraction is a lower bound
+    on the pipe's use."""
     B = n_steps // stride
     evolved = n_steps - stride
-    acc = stride * sum(B - b for b in range(1, B))
-    return evolved * 9 * n_tenor + acc
+    per_step = 2 * n_tenor + 32 if form == "poly" else 8 * n_tenor + 10
+    per_block = n_tenor
+    recovery = 12 * sum(B - b for b in range(1, B))
+    return evolved * per_step + (B - 1) * per_block + recovery
 
 
 class ClockSampler:
@@ -233,6 +246,7 @@ def run_ours(args) -> None:
     else:
         eng.set_market(mk)
     set_product()
+    vol_form_poly = eng.vol_decomposition()
     # weak scaling across ranks: rank r owns paths [r*n, (r+1)*n)
     cfg = RunConfig(n_paths=n_paths, n_steps=n_steps, dt=DT, seed=SEED, path_offset=rank * n_paths)
     flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
@@ -302,7 +316,8 @@ def run_ours(args) -> None:
             dist.destroy_process_group()
         return
 
-    flops = algorithmic_flops_per_path(mk.n_tenor, n_steps, stride) * n_paths * (2 if is_adjoint else 1)
+    form = "poly" if vol_form_poly else "table"
+    flops = algorithmic_flops_per_path(mk.n_tenor, n_steps, stride, form) * n_paths * (2 if is_adjoint else 1)
     extras = {}
     peak_key = "fp64" if prec == "fp64" else "mixed"
     peak = None
@@ -317,14 +332,15 @@ def run_ours(args) -> None:
     traffic = profiled_traffic(f"{prec}-{n_paths}")
     roofline = {"bound": "fp64_pipe" if prec == "fp64" else "fp32_pipe", "achieved": achieved, "peak": peak,
                 "unit": "TFLOP/s", "frac": (achieved / peak) if peak else None, "traffic": traffic,
-                "kernel": ("adjoint_kernel<51,true>" if is_adjoint else
-                           f"path_kernel<{mk.n_tenor},double,false>" if prec == "fp64" else
-                           f"path_kernel_mixed<{mk.n_tenor},false>"),
+                "kernel": (f"adjoint_kernel<{mk.n_tenor},ckpt,{form}>" if is_adjoint else
+                           f"path_kernel_fp64<{mk.n_tenor},philox,{form}>" if prec == "fp64" else
+                           f"path_kernel_mixed<{mk.n_tenor},philox,{form}>"),
                 "algorithmic_flops_per_launch": flops, "avg_launch_ms": path_ms,
                 "peak_source": "measured live by bench.py (FMA microkernel, this GPU)",
                 "hbm_peak_gbs_measured": _measured_hbm()}
 
     if not args.no_extras and prec == "fp64":
+        extras["generic_table_step"] = generic_step_run(eng, mk, sw, args, flush, stride, peak64, peak32)
         extras["mixed"] = mixed_vs_fp64(eng, mk, sw, args, stream, flush, value)
         extras["adjoint"] = adjoint_cost(eng, args, flush)
         extras["netting"] = netting_set_run(eng, args, flush)
@@ -345,7 +361,10 @@ def run_ours(args) -> None:
         "config": {"workload": wl["name"], "n_paths_per_gpu": n_paths, "n_steps": n_steps, "dt": DT,
                    "n_tenor": mk.n_tenor, "factors": 3, "sampled_dates": n_steps // stride,
                    "pfe_quantile": None if is_adjoint else 0.975, "hazard": 0.02,
-                   "recovery": 0.4, "seed": SEED, "parallelism": f"replicas{world}" if world > 1 else "single",
+                   "recovery": 0.4, "seed": SEED,
+                   "vol_form": ("quadratic factors (detected in the volatility table): decomposed step" if vol_form_poly
+                                else "volatility table: generic step"),
+                   "parallelism": f"replicas{world}" if world > 1 else "single",
                    "l2": f"flushed between steps ({FLUSH_BYTES >> 20} MiB device write, inside the timed region)"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(st["d2h_bytes"]), "call": "hjm_set_market + hjm_set_swap + hjm_run"},
@@ -412,6 +431,44 @@ def mixed_vs_fp64(eng, mk, sw, args, stream, flush, fp64_value) -> dict:
         "cva_stderr": mx.cva_stderr,
         "pfe_max_rel_err_vs_fp64": float(np.max(np.abs(mx.pfe[:20] - f64.pfe[:20]) / f64.pfe[:20])),
     }
+
+
+def generic_step_run(eng, mk, sw, args, flush, stride, peak64, peak32) -> dict:
+    """The same valuations with the polynomial decomposition switched off (the
+    generic volatility-table step every market can use)."""
+    import torch
+
+    from cva_hjm_cuda_gb300 import RunConfig
+
+    out = {}
+    eng.vol_decomposition(False)
+    try:
+        eng.set_market(mk)
+        eng.set_swap(sw)
+        for prec, n, peak in (("fp64", WORKLOADS["fp64"]["n_paths"], peak64),
+                              ("mixed", WORKLOADS["mixed"]["n_paths"], peak32)):
+            cfg = RunConfig(n_paths=n, n_steps=N_STEPS, dt=DT, seed=SEED)
+            for _ in range(args.warmup):
+                eng.enqueue(cfg, prec)
+                flush.zero_()
+            torch.cuda.synchronize()
+            for _ in range(args.steps):
+                eng.enqueue(cfg, prec)
+                flush.zero_()
+            torch.cuda.synchronize()
+            hist = eng.timing_history(min(args.steps, 64))
+            kern_ms, step_ms = float(hist[:, 0].mean()), float(hist[:, 3].mean())
+            res = eng.fetch()
+            fl = algorithmic_flops_per_path(mk.n_tenor, N_STEPS, stride, "table") * n
+            out[prec] = {"n_paths": n, "path_steps_per_s": n * N_STEPS / (step_ms * 1e-3), "device_ms_per_step": step_ms,
+                         "path_kernel_ms": kern_ms, "achieved_tflops": fl / (kern_ms * 1e-3) / 1e12,
+                         "frac_of_measured_fma_peak": (fl / (kern_ms * 1e-3) / 1e12 / peak) if peak else None,
+                         "cva": res.cva}
+    finally:
+        eng.vol_decomposition(True)
+        eng.set_market(mk)
+        eng.set_swap(sw)
+    return out
 
 
 def adjoint_cost(eng, args, flush) -> dict:

@@ -167,13 +167,15 @@ __global__ void __launch_bounds__(kAdjCta, 6)
         }
     };
 
-    // checkpoint rows: the NT tenors of the curve (POLY: its convected part),
-    // then S, U, W
-    constexpr int kCkRows = NT + 3;
+    // checkpoint rows: the NT tenors of the scaled curve v (POLY: its convected
+    // part), then S, U, W and the scales g, ig: the recomputation restarts from
+    // the forward pass's own state and repeats its arithmetic
+    constexpr int kCkRows = NT + 5;
     sample(1);
     for (int b = 1; b < B; ++b) {
         BlockSums bs;
         bs.reset();
+        x.begin_block(P, b);
         for (int s = 0; s < stride; ++s) {
             const int n = b * stride + s;
             if (CKPT && ((n - stride) % K) == 0) {
@@ -193,6 +195,8 @@ __global__ void __launch_bounds__(kAdjCta, 6)
                     ck_h[((size_t)ck * kCkRows + NT) * ld + lp] = x.S;
                     ck_h[((size_t)ck * kCkRows + NT + 1) * ld + lp] = x.U;
                     ck_h[((size_t)ck * kCkRows + NT + 2) * ld + lp] = x.W;
+                    ck_h[((size_t)ck * kCkRows + NT + 3) * ld + lp] = x.g;
+                    ck_h[((size_t)ck * kCkRows + NT + 4) * ld + lp] = x.ig;
                     ck_a[(size_t)ck * ld + lp] = acc_s[inext * kCtaA + tid] + part;
                 }
             }
@@ -206,7 +210,7 @@ __global__ void __launch_bounds__(kAdjCta, 6)
         });
 #pragma unroll
         for (int t = 1; t < NT; ++t)
-            if (t <= B + 1) hs_s[t * kCtaA + tid] = pair_tenor<NT>(x.h, t);
+            if (t <= B + 1) hs_s[t * kCtaA + tid] = x.rem(t);
         sample(b + 1);
     }
 
@@ -302,9 +306,11 @@ __global__ void __launch_bounds__(kAdjCta, 6)
             xr.S = active ? ck_h[(base + NT) * ld + lp] : 0.f;
             xr.U = active ? ck_h[(base + NT + 1) * ld + lp] : 0.f;
             xr.W = active ? ck_h[(base + NT + 2) * ld + lp] : 0.f;
+            xr.g = active ? ck_h[(base + NT + 3) * ld + lp] : 1.f;
+            xr.ig = active ? ck_h[(base + NT + 4) * ld + lp] : 1.f;
 #pragma unroll
             for (int t = 1; t < NT; ++t)
-                if (t <= B + 1) hs_s[t * kCtaA + tid] = pair_tenor<NT>(xr.h, t);
+                if (t <= B + 1) hs_s[t * kCtaA + tid] = xr.rem(t);
             const double a0 = active ? ck_a[(size_t)sg * ld + lp] : 0.0;
             BlockSums bs;
             bs.reset();

@@ -394,6 +394,8 @@ static hjm_status check_run(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, doub
     const long st = std::lround(r);
     if (st < 1 || std::fabs(r - (double)st) > 1e-9 * r)
         return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "dtau/dt = %.17g is not an integer number of steps", r);
+    if (st < 2)
+        return fail(ctx, HJM_ERR_UNSUPPORTED, "dt must be at most dtau/2 (the kernels need c = dt/dtau < 1)");
     if (n_steps <= 0 || n_steps % st != 0)
         return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "n_steps %d is not a positive multiple of the block length %ld",
                     n_steps, st);
@@ -469,6 +471,7 @@ static void fill_params(const hjm_ctx* ctx, const RunShape& sh, int64_t n_paths,
             for (int d = 0; d < 3; ++d) P.svc[k][d] = sq * ctx->coef[k * 3 + d];
     P.k1 = (dt / ctx->dtau) * ctx->dtau;
     P.k2 = (dt / ctx->dtau) * ctx->dtau * ctx->dtau;
+    fill_growth_scale(P, dt / ctx->dtau, P.k2, sh.stride, sh.B);
     for (int t = 0; t < nt; ++t) P.tau[t] = (T)(ctx->dtau * t);
     P.c = (T)(dt / ctx->dtau);
     P.dt = dt;
@@ -779,7 +782,7 @@ hjm_status hjm_run_adjoint(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, doubl
     HJM_CUDA(ctx, ctx->sums.ensure(sizeof(double) * kMaxTenor * 4));
     HJM_CUDA(ctx, ctx->result.ensure(sizeof(double) * kResLen));
     if (K > 0) {
-        HJM_CUDA(ctx, ctx->ck_h.ensure(sizeof(float) * (size_t)S * (nt + 3) * (size_t)ld));
+        HJM_CUDA(ctx, ctx->ck_h.ensure(sizeof(float) * (size_t)S * (nt + 5) * (size_t)ld));
         HJM_CUDA(ctx, ctx->ck_a.ensure(sizeof(double) * (size_t)S * (size_t)ld));
     }
     AdjParams A;

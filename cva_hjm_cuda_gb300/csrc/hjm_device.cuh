@@ -5,6 +5,7 @@
 // :1057-1071), the kernel parameter block, and small warp helpers.
 #pragma once
 
+#include <cmath>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -140,7 +141,41 @@ struct PathParams {
     double svc[kFactors][3];
     double k1, k2;               // c dtau, c dtau^2
     T tau[kMaxTenor];            // tau_t = dtau t
+    // Growth-scaled convection.  After n' Euler steps of the stochastic part
+    // the kernels hold v = h (1 + rr)^n' instead of h, rr = c / (1 - c) rounded
+    // to T once.  The upwind step h[t] + c (h[t+1] - h[t]) then reads
+    //   v'[t] = v[t] + rr v[t+1]                     (t < L, one FMA),
+    //   v'[L] = v[L] + rr (2 v[L] - v[L-1])          (backward difference),
+    // plus the noise times (1 + rr)^(n'+1): exactly the reference scheme for
+    // c_eff = rr / (1 + rr) (c to within T's rounding), with every constant
+    // derived from the one rounded rr so that the homogeneous step stays
+    // consistent.  v is never rescaled (its growth is at most e^(number of
+    // tenors)); h = v / (1 + rr)^n' is formed only where it is read.
+    T gblk[kMaxTenor];           // (1 + rr)^-(b-1) stride: the scale at the start of block b
+    T igblk[kMaxTenor];          // its inverse
+    T rr;                        // c / (1 - c)
+    T qm;                        // 1 / (1 + rr): per-step factor of the scale
+    T ip;                        // 1 + rr: per-step factor of the inverse scale
+    T m2k2;                      // -2 c dtau^2: the polynomial form's last-tenor source per unit W
 };
+
+// Host: the growth-scale constants of PathParams from c = dt / dtau, k2 and
+// the block layout.
+template <typename T>
+inline void fill_growth_scale(PathParams<T>& P, double c, double k2, int stride, int n_blocks)
+{
+    const T rr = (T)(c / (1.0 - c));
+    const double base = 1.0 + (double)rr;  // exact in double for T = float
+    for (int b = 0; b < kMaxTenor; ++b) {
+        const double e = (b >= 1 && b <= n_blocks) ? (double)((b - 1) * stride) : 0.0;
+        P.gblk[b] = (T)std::pow(base, -e);
+        P.igblk[b] = (T)std::pow(base, e);
+    }
+    P.rr = rr;
+    P.qm = (T)(1.0 / base);
+    P.ip = (T)base;
+    P.m2k2 = (T)(-2.0 * k2);
+}
 
 #ifdef __CUDACC__
 // The three normals of (path, step): Philox in registers, or read from a
@@ -163,27 +198,6 @@ __device__ __forceinline__ void draw_phi(const double* __restrict__ ext, uint64_
         phi1 = (T)z1;
         phi2 = (T)z2;
     }
-}
-
-// One Musiela Euler step of the stochastic part of the curve
-// (simulation_cpu.h:37-54 with the drift moved into the deterministic part):
-//   h[t] <- h[t] + sum_k sv[k][t] phi_k + c (h[t+1] - h[t])   (backward difference
-// at the last tenor, simulation_cpu.h:96-108); 5 FMA-pipe instructions per
-// tenor with every coefficient read from the constant bank.
-template <int NT, typename T>
-__device__ __forceinline__ void euler_step(T (&h)[NT], const PathParams<T>& P, T c, T phi0, T phi1, T phi2)
-{
-    T hn[NT];
-#pragma unroll
-    for (int t = 0; t < NT; ++t) {
-        T x = fma(P.sv[0][t], phi0, h[t]);
-        x = fma(P.sv[1][t], phi1, x);
-        x = fma(P.sv[2][t], phi2, x);
-        const T d = (t < NT - 1) ? (h[t + 1] - h[t]) : (h[t] - h[t - 1]);
-        hn[t] = fma(c, d, x);
-    }
-#pragma unroll
-    for (int t = 0; t < NT; ++t) h[t] = hn[t];
 }
 
 // Static selection of a register-array element by a runtime index (uniform

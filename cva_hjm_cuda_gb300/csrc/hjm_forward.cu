@@ -66,8 +66,10 @@ __host__ __device__ inline size_t path_smem_bytes(int nt, int n_blocks, bool mix
 // - 2 c dtau^2 e_L.  Writing h = S 1 + U T + W T^2 + hc, the Euler step becomes
 //     S <- S + c dtau U + c dtau^2 W + alpha,   U <- U + 2 c dtau W + beta,
 //     W <- W + gamma,   hc <- A hc - 2 c dtau^2 W e_L   (old U, W on the right),
-// exact in exact arithmetic: the curve is advanced in full, with 2 operations
-// per tenor (the convection of hc) instead of 5, plus a dozen per step.
+// exact in exact arithmetic: the curve is advanced in full, with the
+// convection of hc per tenor instead of 5 operations, plus a dozen per step.
+// With the growth scaling of PathParams (v = h / (1-c)^j) the convection is
+// one FMA per tenor, and the table form four.
 template <int NT, bool EXT, bool POLY>
 __global__ void __launch_bounds__(kFp64Cta, 4)
     path_kernel_fp64(const __grid_constant__ PathParams<double> P, const double* __restrict__ ext,
@@ -101,8 +103,9 @@ __global__ void __launch_bounds__(kFp64Cta, 4)
     double* he_s = work_s + (size_t)(rows + 1) * kCta;
     for (int t = 0; t <= B + 1; ++t) hs_s[t * kCta + tid] = 0.0;
 
+    double g = 1.0;  // the kernel holds v; h = g v
     auto value_at = [&](int i) -> double {
-        double v = select_reg<NT, double>(h, i);
+        double v = g * select_reg<NT, double>(h, i);
         if (POLY) v += fma(P.tau[i], fma(P.tau[i], W, U), S);
         return v;
     };
@@ -116,28 +119,26 @@ __global__ void __launch_bounds__(kFp64Cta, 4)
     };
 
     sample(1);
-    const double c = P.c;
+    const double c = P.c, rr = P.rr;
     for (int b = 1; b < B; ++b) {
         double f0 = 0.0, f1 = 0.0, f2 = 0.0, hb = 0.0;  // block sums of phi_k and of h[B]
         double sS = 0.0, sU = 0.0, sW = 0.0;            // POLY: block sums of S, U, W
+        g = P.gblk[b];
+        double ig = P.igblk[b];
         for (int s = 0; s < P.stride; ++s) {
             const int n = b * P.stride + s;
             double phi0, phi1, phi2;
             draw_phi<double, EXT>(ext, gpath, active ? lp : 0, P.n_paths, n, P.rk0, P.rk1, phi0, phi1, phi2);
+            ig *= P.ip;
+            double hn[NT];
             if constexpr (POLY) {
                 const double al = fma(P.svc[2][0], phi2, fma(P.svc[1][0], phi1, P.svc[0][0] * phi0));
                 const double be = fma(P.svc[2][1], phi2, fma(P.svc[1][1], phi1, P.svc[0][1] * phi0));
                 const double ga = fma(P.svc[2][2], phi2, fma(P.svc[1][2], phi1, P.svc[0][2] * phi0));
-                const double src = -2.0 * P.k2 * W;
-                double hn[NT];
+                const double src = (P.m2k2 * W) * ig;  // -2 c dtau^2 W, scaled
 #pragma unroll
-                for (int t = 0; t < NT; ++t) {
-                    const double d = (t < L) ? (h[t + 1] - h[t]) : (h[t] - h[t - 1]);
-                    hn[t] = fma(c, d, h[t]);
-                }
-                hn[L] += src;
-#pragma unroll
-                for (int t = 0; t < NT; ++t) h[t] = hn[t];
+                for (int t = 0; t < L; ++t) hn[t] = fma(rr, h[t + 1], h[t]);
+                hn[L] = fma(rr, fma(2.0, h[L], -h[L - 1]), h[L]) + src;
                 const double Sn = fma(P.k2, W, fma(P.k1, U, S)) + al;
                 U = fma(2.0 * P.k1, W, U) + be;
                 W += ga;
@@ -146,17 +147,31 @@ __global__ void __launch_bounds__(kFp64Cta, 4)
                 sU += U;
                 sW += W;
             } else {
-                euler_step<NT, double>(h, P, c, phi0, phi1, phi2);
+                const double p0 = phi0 * ig, p1 = phi1 * ig, p2 = phi2 * ig;
+#pragma unroll
+                for (int t = 0; t < L; ++t) {
+                    double x = fma(P.sv[0][t], p0, h[t]);
+                    x = fma(P.sv[1][t], p1, x);
+                    x = fma(P.sv[2][t], p2, x);
+                    hn[t] = fma(rr, h[t + 1], x);
+                }
+                double xl = fma(P.sv[0][L], p0, h[L]);
+                xl = fma(P.sv[1][L], p1, xl);
+                xl = fma(P.sv[2][L], p2, xl);
+                hn[L] = fma(rr, fma(2.0, h[L], -h[L - 1]), xl);
                 f0 += phi0;
                 f1 += phi1;
                 f2 += phi2;
             }
-            hb += select_reg<NT, double>(h, B);
+#pragma unroll
+            for (int t = 0; t < NT; ++t) h[t] = hn[t];
+            g *= P.qm;
+            hb = fma(g, select_reg<NT, double>(h, B), hb);
         }
         // stage the block-end curve, then recover the block sums of tenors (b, B]
 #pragma unroll
         for (int t = 0; t < NT; ++t)
-            if (t <= B + 1) he_s[t * kCta + tid] = h[t];
+            if (t <= B + 1) he_s[t * kCta + tid] = g * h[t];
         auto poly_part = [&](int t) -> double {
             return POLY ? fma(P.tau[t], fma(P.tau[t], sW, sU), sS) : 0.0;
         };
@@ -237,12 +252,11 @@ __global__ void __launch_bounds__(kFp64Cta, 4)
 // Mixed precision with packed FP32x2 arithmetic.  The curve of one path is held
 // as H = ceil(NT/2) float2 pairs, pair p = {h[p], h[p+H]}: the upwind neighbour
 // h[t+1] of every tenor lies in the same component of pair p+1, so each packed
-// FMA (__ffma2_rn) advances two tenors and the Euler step costs half the issue
-// slots of the scalar form.  Only the seam pair (p = H-1, whose .x neighbour is
-// pair 0's .y), the pair holding the last tenor (backward difference) and the
-// padding tenor of an odd grid take scalar fix-ups.  Every element sees exactly
-// the scalar kernel's operations (fma(sv, phi, h) three times, one rounded
-// difference, fma(c, d, x)), so the results are bit-identical to it.
+// FMA (__ffma2_rn) advances two tenors: with the growth scaling of PathParams
+// the polynomial form's step is one packed FMA per pair, the table form's four.
+// Only the seam pair (p = H-1, whose .x neighbour is pair 0's .y), the pair
+// holding the last tenor (backward difference) and the padding tenor of an odd
+// grid take scalar fix-ups.
 // ---------------------------------------------------------------------------
 // Mixed-precision discount sums: FP32 block sums by the same recovery as the
 // FP64 kernel, but anchored at tenor 1 and run upwards,
@@ -293,6 +307,7 @@ __global__ void __launch_bounds__(kCta, 4)
     for (int b = 1; b < B; ++b) {
         BlockSums bs;
         bs.reset();
+        x.begin_block(P, b);
         for (int s = 0; s < P.stride; ++s) {
             const int n = b * P.stride + s;
             float phi0, phi1, phi2;
@@ -307,7 +322,7 @@ __global__ void __launch_bounds__(kCta, 4)
         // the block-end curve (POLY: its convected part) is the next block's start
 #pragma unroll
         for (int t = 1; t < NT; ++t)
-            if (t <= B + 1) hs_s[t * kCta + tid] = pair_tenor<NT>(x.h, t);
+            if (t <= B + 1) hs_s[t * kCta + tid] = x.rem(t);
         sample(b + 1);
     }
 
@@ -382,6 +397,7 @@ void pack_mixed_params(int nt, const PathParams<float>& P, MixedParams& M)
             M.svp[k][p].y = (H + p < nt) ? P.sv[k][H + p] : 0.0f;
         }
     M.cp = make_float2(P.c, P.c);
+    M.rp = make_float2(P.rr, P.rr);
     for (int k = 0; k < kFactors; ++k)
         for (int d = 0; d < 3; ++d) M.svcf[k][d] = (float)P.svc[k][d];
     M.k1f = (float)P.k1;

@@ -20,33 +20,42 @@ struct PairGrid {
     static constexpr int L = NT - 1;        // last tenor
 };
 
+// One growth-scaled Euler step of the packed curve v (table volatility): with
+// the normals already scaled by (1 + rr)^(n'+1) (p0..p2),
+//   v'[t] = v[t] + sum_k sv[k][t] p_k + rr v[t+1],        t < L,
+//   v'[L] = v[L] + sum_k sv[k][L] p_k + rr (2 v[L] - v[L-1]),
+// four packed FMAs per pair of tenors.  The seam pair (p = H-1, whose .x
+// neighbour is pair 0's .y), the pair holding the last tenor and the padding
+// tenor of an odd grid take scalar fix-ups.
 template <int NT>
-__device__ __forceinline__ void euler_step_pairs(float2 (&h)[PairGrid<NT>::H], const MixedParams& M, float phi0,
-                                                 float phi1, float phi2)
+__device__ __forceinline__ void euler_step_pairs(float2 (&h)[PairGrid<NT>::H], const MixedParams& M, float p0,
+                                                 float p1, float p2)
 {
     constexpr int H = PairGrid<NT>::H, L = PairGrid<NT>::L;
-    const float2 f0 = make_float2(phi0, phi0), f1 = make_float2(phi1, phi1), f2 = make_float2(phi2, phi2);
-    const float2 m1 = make_float2(-1.0f, -1.0f);
+    const float2 f0 = make_float2(p0, p0), f1 = make_float2(p1, p1), f2 = make_float2(p2, p2);
+    const float rr = M.P.rr;
     float2 hn[H];
 #pragma unroll
     for (int p = 0; p < H; ++p) {
-        float2 x = __ffma2_rn(M.svp[0][p], f0, h[p]);
-        x = __ffma2_rn(M.svp[1][p], f1, x);
-        x = __ffma2_rn(M.svp[2][p], f2, x);
         const int q = H + p;  // tenor held in .y
-        float2 d;
         if (p + 1 < H && q < L) {
-            d = __ffma2_rn(m1, h[p], h[p + 1]);  // h[t+1] - h[t] for both tenors, one rounding each
+            float2 x = __ffma2_rn(M.svp[0][p], f0, h[p]);
+            x = __ffma2_rn(M.svp[1][p], f1, x);
+            x = __ffma2_rn(M.svp[2][p], f2, x);
+            hn[p] = __ffma2_rn(M.rp, h[p + 1], x);
         } else {
-            d.x = ((p + 1 < H) ? h[p + 1].x : h[0].y) - h[p].x;
-            if (q < L)
-                d.y = h[p + 1].y - h[p].y;
-            else if (q == L)
-                d.y = h[p].y - h[p - 1].y;  // backward difference at the last tenor
-            else
-                d.y = 0.0f;                 // padding tenor of an odd grid: stays zero
+            float x = fmaf(M.svp[2][p].x, p2, fmaf(M.svp[1][p].x, p1, fmaf(M.svp[0][p].x, p0, h[p].x)));
+            hn[p].x = fmaf(rr, (p + 1 < H) ? h[p + 1].x : h[0].y, x);
+            if (q < L) {
+                x = fmaf(M.svp[2][p].y, p2, fmaf(M.svp[1][p].y, p1, fmaf(M.svp[0][p].y, p0, h[p].y)));
+                hn[p].y = fmaf(rr, h[p + 1].y, x);
+            } else if (q == L) {
+                x = fmaf(M.svp[2][p].y, p2, fmaf(M.svp[1][p].y, p1, fmaf(M.svp[0][p].y, p0, h[p].y)));
+                hn[p].y = fmaf(rr, fmaf(2.0f, h[p].y, -h[p - 1].y), x);
+            } else {
+                hn[p].y = 0.0f;  // padding tenor of an odd grid: stays zero
+            }
         }
-        hn[p] = __ffma2_rn(M.cp, d, x);
     }
 #pragma unroll
     for (int p = 0; p < H; ++p) h[p] = hn[p];
@@ -75,21 +84,22 @@ __device__ __forceinline__ float pair_tenor(const float2 (&h)[PairGrid<NT>::H], 
 
 // Block-sum recovery in FP32, upwards from the anchor tenor 1.  Over a run of
 // Euler steps, with Phi_k the sums of the normals, H1 the sum of h[1] and
-// d = h_now - h_start (h_start in hs_s, thread column tid, stride cta),
+// d = h_now - h_start (h_now = gs * v, h_start in hs_s, thread column tid,
+// stride cta),
 //     H[t+1] = H[t] + ((A d)[t] - sum_k sv[k][t] Phi_k) / c,   t = 1 .. tmax-1,
 // and fold(t, H[t]) is called for t = 2 .. tmax (tmax <= NT-1).
 template <int NT, typename Fold>
 __device__ __forceinline__ void recover_sums_up(const float2 (&h)[PairGrid<NT>::H], const float* hs_s, int tid,
-                                                int cta, const PathParams<float>& P, float F0, float F1, float F2,
-                                                float H1, int tmax, Fold fold)
+                                                int cta, const PathParams<float>& P, float gs, float F0, float F1,
+                                                float F2, float H1, int tmax, Fold fold)
 {
     const float c = P.c, inv_c = (float)P.inv_c;
     float Hn = H1;
-    float d = pair_tenor<NT>(h, 1) - hs_s[1 * cta + tid];
+    float d = fmaf(gs, pair_tenor<NT>(h, 1), -hs_s[1 * cta + tid]);
 #pragma unroll
     for (int t = 1; t < NT - 1; ++t) {
         if (t >= tmax) break;
-        const float dn = pair_tenor<NT>(h, t + 1) - hs_s[(t + 1) * cta + tid];
+        const float dn = fmaf(gs, pair_tenor<NT>(h, t + 1), -hs_s[(t + 1) * cta + tid]);
         const float xi = fmaf(P.sv[2][t], F2, fmaf(P.sv[1][t], F1, P.sv[0][t] * F0));
         const float ad = fmaf(c, dn - d, d);
         Hn = fmaf(ad - xi, inv_c, Hn);
@@ -98,31 +108,29 @@ __device__ __forceinline__ void recover_sums_up(const float2 (&h)[PairGrid<NT>::
     }
 }
 
-// The convection part of the step, h <- A h + src e_L (polynomial volatility:
-// the noise lives in the scalar parts S, U, W), on the packed curve.
+// The growth-scaled convection of the packed curve (polynomial volatility:
+// the noise lives in the scalar parts S, U, W), with the last-tenor source
+// src already scaled by (1 + rr)^(n'+1): one packed FMA per pair of tenors.
 template <int NT>
-__device__ __forceinline__ void convect_pairs(float2 (&h)[PairGrid<NT>::H], float2 cp, float src)
+__device__ __forceinline__ void convect_pairs(float2 (&h)[PairGrid<NT>::H], const MixedParams& M, float src)
 {
     constexpr int H = PairGrid<NT>::H, L = PairGrid<NT>::L;
-    const float2 m1 = make_float2(-1.0f, -1.0f);
+    const float rr = M.P.rr;
     float2 hn[H];
 #pragma unroll
     for (int p = 0; p < H; ++p) {
         const int q = H + p;
-        float2 d;
         if (p + 1 < H && q < L) {
-            d = __ffma2_rn(m1, h[p], h[p + 1]);
+            hn[p] = __ffma2_rn(M.rp, h[p + 1], h[p]);
         } else {
-            d.x = ((p + 1 < H) ? h[p + 1].x : h[0].y) - h[p].x;
+            hn[p].x = fmaf(rr, (p + 1 < H) ? h[p + 1].x : h[0].y, h[p].x);
             if (q < L)
-                d.y = h[p + 1].y - h[p].y;
+                hn[p].y = fmaf(rr, h[p + 1].y, h[p].y);
             else if (q == L)
-                d.y = h[p].y - h[p - 1].y;
+                hn[p].y = fmaf(rr, fmaf(2.0f, h[p].y, -h[p - 1].y), h[p].y) + src;
             else
-                d.y = 0.0f;
+                hn[p].y = 0.0f;
         }
-        hn[p] = __ffma2_rn(cp, d, h[p]);
-        if (q == L) hn[p].y += src;
     }
 #pragma unroll
     for (int p = 0; p < H; ++p) h[p] = hn[p];
@@ -136,37 +144,50 @@ __device__ __forceinline__ void convect_pairs(float2 (&h)[PairGrid<NT>::H], floa
 template <int NT, bool POLY>
 struct MixedPath {
     static constexpr int H = PairGrid<NT>::H;
-    float2 h[H];
+    float2 h[H];  // v = h / g (POLY: the convected remainder hc, scaled alike)
     float S, U, W;
+    float g, ig;  // (1 + rr)^-n' and its inverse, n' = steps evolved so far
 
     __device__ __forceinline__ void reset()
     {
 #pragma unroll
         for (int p = 0; p < H; ++p) h[p] = make_float2(0.f, 0.f);
         S = U = W = 0.f;
+        g = ig = 1.f;
+    }
+    // the scales at the start of block b, from the table (no drift across blocks)
+    __device__ __forceinline__ void begin_block(const PathParams<float>& P, int b)
+    {
+        g = P.gblk[b];
+        ig = P.igblk[b];
     }
     __device__ __forceinline__ void step(const MixedParams& M, float phi0, float phi1, float phi2)
     {
+        ig *= M.P.ip;
         if constexpr (POLY) {
             const float al = fmaf(M.svcf[2][0], phi2, fmaf(M.svcf[1][0], phi1, M.svcf[0][0] * phi0));
             const float be = fmaf(M.svcf[2][1], phi2, fmaf(M.svcf[1][1], phi1, M.svcf[0][1] * phi0));
             const float ga = fmaf(M.svcf[2][2], phi2, fmaf(M.svcf[1][2], phi1, M.svcf[0][2] * phi0));
-            convect_pairs<NT>(h, M.cp, -2.0f * M.k2f * W);
+            convect_pairs<NT>(h, M, (M.P.m2k2 * W) * ig);
             const float Sn = fmaf(M.k2f, W, fmaf(M.k1f, U, S)) + al;
             U = fmaf(2.0f * M.k1f, W, U) + be;
             W += ga;
             S = Sn;
         } else {
-            euler_step_pairs<NT>(h, M, phi0, phi1, phi2);
+            euler_step_pairs<NT>(h, M, phi0 * ig, phi1 * ig, phi2 * ig);
         }
+        g *= M.P.qm;
     }
     // tenor i (runtime) of the stochastic curve
     __device__ __forceinline__ float value(const PathParams<float>& P, int i) const
     {
-        float v = select_pair<NT>(h, i);
+        float v = g * select_pair<NT>(h, i);
         if (POLY) v += fmaf(P.tau[i], fmaf(P.tau[i], W, U), S);
         return v;
     }
+    // tenor t (compile-time after unrolling) of the stochastic curve without
+    // the polynomial part
+    __device__ __forceinline__ float rem(int t) const { return g * pair_tenor<NT>(h, t); }
 };
 
 // Running sums over a block (or a partial block) of steps for the recovery.
@@ -185,7 +206,7 @@ struct BlockSums {
             F1 += phi1;
             F2 += phi2;
         }
-        H1 += x.h[1].x;
+        H1 = fmaf(x.g, x.h[1].x, H1);
     }
 };
 
@@ -197,11 +218,11 @@ __device__ __forceinline__ void block_sums_up(const MixedPath<NT, POLY>& x, cons
                                               const PathParams<float>& P, const BlockSums& bs, int tmax, Fold fold)
 {
     if constexpr (POLY) {
-        recover_sums_up<NT>(x.h, hs_s, tid, cta, P, 0.f, 0.f, 0.f, bs.H1, tmax, [&](int t, float Ht) {
+        recover_sums_up<NT>(x.h, hs_s, tid, cta, P, x.g, 0.f, 0.f, 0.f, bs.H1, tmax, [&](int t, float Ht) {
             fold(t, Ht + fmaf(P.tau[t], fmaf(P.tau[t], bs.sW, bs.sU), bs.sS));
         });
     } else {
-        recover_sums_up<NT>(x.h, hs_s, tid, cta, P, bs.F0, bs.F1, bs.F2, bs.H1, tmax, fold);
+        recover_sums_up<NT>(x.h, hs_s, tid, cta, P, x.g, bs.F0, bs.F1, bs.F2, bs.H1, tmax, fold);
     }
 }
 

@@ -153,6 +153,8 @@ static void static_params(int nt, double dtau, const double* spot, const double*
         F.dcvaw[j] = (1.0 - recovery) * (-t0 * e0 + t1 * e1);
     }
     P.c = (T)(dt / dtau);
+    P.k2 = dt * dtau;
+    fill_growth_scale(P, dt / dtau, P.k2, stride, B);
     P.dt = dt;
     P.m = 1.0 / dtau;
     P.key0 = (uint32_t)seed;
@@ -206,6 +208,8 @@ hjm_status hjm_run_static(void* cuda_stream, int32_t n_tenor, double dtau, const
     const long stride = std::lround(r);
     if (stride < 1 || std::fabs(r - (double)stride) > 1e-9 * r)
         return static_fail(HJM_ERR_INVALID_ARGUMENT, "dtau/dt = %.17g is not an integer number of steps", r);
+    if (stride < 2)
+        return static_fail(HJM_ERR_UNSUPPORTED, "dt must be at most dtau/2 (the kernels need c = dt/dtau < 1)");
     if (n_steps <= 0 || n_steps % stride != 0)
         return static_fail(HJM_ERR_INVALID_ARGUMENT, "n_steps %d is not a positive multiple of %ld", n_steps, stride);
     const int B = n_steps / (int)stride;
