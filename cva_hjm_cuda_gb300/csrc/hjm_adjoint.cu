@@ -34,13 +34,15 @@
 // on the host.  The normals are regenerated from their Philox counters.
 //
 // Checkpoint mode (checkpoint_every = K in [1, stride]).  The forward pass
-// keeps only the cash flows; it writes the stochastic curve h and the FP64
-// discount sum of the next tenor to be sampled to HBM before every K-th
-// Euler step.  The reverse sweep walks the segments backwards, reloads the
-// segment's checkpoint, recomputes the segment's states forward (regenerated
-// normals) to rebuild the sampled forward and discount of the date that falls
-// inside it, and then sweeps the segment backwards.  With K = 0 the forward
-// pass keeps the per-date (x_i, D_i) instead and nothing is recomputed.
+// keeps only the cash flows; before every K-th Euler step it writes the
+// path's state (scaled curve, polynomial parts, scales) and the FP64 discount
+// sum of the next tenor to be sampled to HBM.  Because the Jacobian is
+// state-independent, the reverse sweep needs the forward state only at the
+// sampling steps: the seed pass recomputes each date's state from the last
+// checkpoint before it (at most K steps, repeating the forward arithmetic from
+// the stored state) and forms the date's seeds; the sweep then runs backwards
+// over the steps with the regenerated normals.  With K = 0 the forward pass
+// keeps the per-date (x_i, D_i) instead and nothing is recomputed.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -117,8 +119,16 @@ __device__ __forceinline__ void pair_add(float2 (&v)[PairGrid<NT>::H], int i, fl
     }
 }
 
+// Resident CTAs per SM: the reverse sweep holds 2 ceil(NT/2) float2 (adjoint
+// state and discount seeds) besides the normals' state.  Registers are
+// granted per scheduler (16 K each), so 6 CTAs of 2 warps (3 warps per
+// scheduler, 168 registers) is the budget for 51 tenors and 4 CTAs (2 warps
+// per scheduler, 255 registers) keeps 61 tenors free of spills.
+template <int NT>
+constexpr int adj_min_ctas() { return NT > 56 ? 4 : 6; }
+
 template <int NT, bool CKPT, bool POLY>
-__global__ void __launch_bounds__(kAdjCta, 6)
+__global__ void __launch_bounds__(kAdjCta, adj_min_ctas<NT>())
     adjoint_kernel(const __grid_constant__ AdjParams A, double* __restrict__ partials, float* __restrict__ ck_h,
                    double* __restrict__ ck_a)
 {
@@ -172,17 +182,18 @@ __global__ void __launch_bounds__(kAdjCta, 6)
     // the forward pass's own state and repeats its arithmetic
     constexpr int kCkRows = NT + 5;
     sample(1);
+    int ck = 0, ck_next = stride;  // next checkpoint: before step ck_next
     for (int b = 1; b < B; ++b) {
         BlockSums bs;
         bs.reset();
         x.begin_block(P, b);
         for (int s = 0; s < stride; ++s) {
             const int n = b * stride + s;
-            if (CKPT && ((n - stride) % K) == 0) {
+            if (CKPT && n == ck_next) {
                 // checkpoint before step n: the curve, and the discount sum of the
                 // next tenor to be sampled (completed blocks + this block so far,
                 // the latter recovered from the partial sums of the block)
-                const int ck = (n - stride) / K;
+                ck_next += K;
                 const int inext = b + 1;
                 double part = 0.0;
                 if (s > 0)
@@ -199,6 +210,7 @@ __global__ void __launch_bounds__(kAdjCta, 6)
                     ck_h[((size_t)ck * kCkRows + NT + 4) * ld + lp] = x.ig;
                     ck_a[(size_t)ck * ld + lp] = acc_s[inext * kCtaA + tid] + part;
                 }
+                ++ck;
             }
             float phi0, phi1, phi2;
             draw_phi<float, false>(nullptr, gpath, lp, P.n_paths, n, P.rk0, P.rk1, phi0, phi1, phi2);
@@ -270,6 +282,60 @@ __global__ void __launch_bounds__(kAdjCta, 6)
         }
     }
 
+    // ------------------------------------------------- date seeds (checkpoints)
+    // The sweep needs the forward state only where the pricing reads it: the
+    // sampled forward and discount of each date.  Each date's state is
+    // recomputed from the last checkpoint before its sampling step (at most K
+    // steps, inside one block), repeating the forward pass's arithmetic from
+    // its stored state; date 1 is deterministic (h = 0 through block 0).
+    if (CKPT) {
+        for (int i = B; i >= 1; --i) {
+            float xb, ab;
+            if (i == 1) {
+                const float D1 = expf((float)(-P.psum[1] * P.dt));
+                date_seeds(P, 1, P.psamp[1], D1, xs_s[1 * kCtaA + tid], xb, ab);
+            } else {
+                const int ni = i * stride - 1;   // the step that samples date i
+                const int sg = (ni - stride) / K;
+                const int n0 = stride + sg * K;  // its checkpoint
+                MixedPath<NT, POLY> xr;
+                const size_t base = (size_t)sg * kCkRows;
+#pragma unroll
+                for (int p = 0; p < H; ++p) {
+                    xr.h[p].x = active ? ck_h[(base + p) * ld + lp] : 0.f;
+                    xr.h[p].y = (active && p + H < NT) ? ck_h[(base + p + H) * ld + lp] : 0.f;
+                }
+                xr.S = active ? ck_h[(base + NT) * ld + lp] : 0.f;
+                xr.U = active ? ck_h[(base + NT + 1) * ld + lp] : 0.f;
+                xr.W = active ? ck_h[(base + NT + 2) * ld + lp] : 0.f;
+                xr.g = active ? ck_h[(base + NT + 3) * ld + lp] : 1.f;
+                xr.ig = active ? ck_h[(base + NT + 4) * ld + lp] : 1.f;
+#pragma unroll
+                for (int t = 1; t < NT; ++t)
+                    if (t <= B + 1) hs_s[t * kCtaA + tid] = xr.rem(t);
+                const double a0 = active ? ck_a[(size_t)sg * ld + lp] : 0.0;
+                BlockSums bs;
+                bs.reset();
+                for (int n = n0; n <= ni; ++n) {
+                    float phi0, phi1, phi2;
+                    draw_phi<float, false>(nullptr, gpath, lp, P.n_paths, n, P.rk0, P.rk1, phi0, phi1, phi2);
+                    xr.step(M, phi0, phi1, phi2);
+                    bs.add(xr, phi0, phi1, phi2);
+                }
+                double part = 0.0;
+                block_sums_up<NT, POLY>(xr, hs_s, tid, kCtaA, P, bs, i, [&](int t, float Ht) {
+                    if (t == i) part = (double)Ht;
+                });
+                const double xv = P.psamp[i] + (double)xr.value(P, i);
+                const double a = P.psum[i] + a0 + part;
+                const float D = expf((float)(-a * P.dt));
+                date_seeds(P, i, xv, D, xs_s[i * kCtaA + tid], xb, ab);
+            }
+            xs_s[i * kCtaA + tid] = xb;  // the seeds replace cfbar (no longer needed)
+            ds_s[i * kCtaA + tid] = ab;
+        }
+    }
+
     // ---------------------------------------------------------------- reverse
     for (int q = 0; q < 9; ++q) cb_s[q * kCtaA + tid] = 0.0;
     float2 g[H], inj[H];
@@ -278,86 +344,31 @@ __global__ void __launch_bounds__(kAdjCta, 6)
         g[p] = make_float2(0.f, 0.f);
         inj[p] = make_float2(0.f, 0.f);
     }
-    float cbb[9];
-#pragma unroll
-    for (int q = 0; q < 9; ++q) cbb[q] = 0.f;
     // moments of g and of the injected discount seeds
     float M0 = 0.f, M1 = 0.f, M2 = 0.f, I0 = 0.f, I1 = 0.f, I2 = 0.f;
     const float dtau = (float)(1.0 / P.m);
     const float k1 = P.c * dtau, k2 = P.c * dtau * dtau;
 
-    const int E = n_steps - stride;
-    const int S = (E + K - 1) / K;
-    for (int sg = S - 1; sg >= 0; --sg) {
-        const int n0 = stride + sg * K;
-        const int n1 = (n0 + K < n_steps) ? n0 + K : n_steps;
-        int idate = 0;
-        float sx = 0.f, sa = 0.f;
-        if (CKPT) {
-            // recompute the segment from its checkpoint; rebuild the seeds of
-            // the date sampled inside it (at most one, since K <= stride)
-            MixedPath<NT, POLY> xr;
-            const size_t base = (size_t)sg * kCkRows;
-#pragma unroll
-            for (int p = 0; p < H; ++p) {
-                xr.h[p].x = active ? ck_h[(base + p) * ld + lp] : 0.f;
-                xr.h[p].y = (active && p + H < NT) ? ck_h[(base + p + H) * ld + lp] : 0.f;
-            }
-            xr.S = active ? ck_h[(base + NT) * ld + lp] : 0.f;
-            xr.U = active ? ck_h[(base + NT + 1) * ld + lp] : 0.f;
-            xr.W = active ? ck_h[(base + NT + 2) * ld + lp] : 0.f;
-            xr.g = active ? ck_h[(base + NT + 3) * ld + lp] : 1.f;
-            xr.ig = active ? ck_h[(base + NT + 4) * ld + lp] : 1.f;
-#pragma unroll
-            for (int t = 1; t < NT; ++t)
-                if (t <= B + 1) hs_s[t * kCtaA + tid] = xr.rem(t);
-            const double a0 = active ? ck_a[(size_t)sg * ld + lp] : 0.0;
-            BlockSums bs;
-            bs.reset();
-            for (int n = n0; n < n1; ++n) {
-                float phi0, phi1, phi2;
-                draw_phi<float, false>(nullptr, gpath, lp, P.n_paths, n, P.rk0, P.rk1, phi0, phi1, phi2);
-                xr.step(M, phi0, phi1, phi2);
-                bs.add(xr, phi0, phi1, phi2);
-                if ((n + 1) % stride == 0) {
-                    const int i = (n + 1) / stride;
-                    double part = 0.0;
-                    block_sums_up<NT, POLY>(xr, hs_s, tid, kCtaA, P, bs, i, [&](int t, float Ht) {
-                        if (t == i) part = (double)Ht;
-                    });
-                    const double xv = P.psamp[i] + (double)xr.value(P, i);
-                    const double a = P.psum[i] + a0 + part;
-                    const float D = expf((float)(-a * P.dt));
-                    date_seeds(P, i, xv, D, xs_s[i * kCtaA + tid], sx, sa);
-                    xs_s[i * kCtaA + tid] = sx;  // the seeds replace cfbar (no longer needed)
-                    ds_s[i * kCtaA + tid] = sa;
-                    idate = i;
-                }
-            }
+    // block i-1 (steps (i-1) stride .. i stride - 1) ends by sampling date i
+    for (int i = B; i >= 2; --i) {
+        {
+            // date i: its discount seed switches on for all earlier steps, its
+            // forward seed enters at its sampling step
+            const float xb = xs_s[i * kCtaA + tid], ab = ds_s[i * kCtaA + tid];
+            pair_set<NT>(inj, i, ab);
+            pair_add<NT>(g, i, xb);
+            const float ti = dtau * (float)i;
+            I0 += ab;
+            I1 = fmaf(ab, ti, I1);
+            I2 = fmaf(ab, ti * ti, I2);
+            M0 += xb;
+            M1 = fmaf(xb, ti, M1);
+            M2 = fmaf(xb, ti * ti, M2);
         }
-        for (int n = n1 - 1; n >= n0; --n) {
-            if ((n + 1) % stride == 0) {
-                // step n samples date i: its discount seed switches on for all
-                // earlier steps, its forward seed enters here
-                const int i = (n + 1) / stride;
-                float xb, ab;
-                if (CKPT) {
-                    xb = (i == idate) ? sx : 0.f;
-                    ab = (i == idate) ? sa : 0.f;
-                } else {
-                    xb = xs_s[i * kCtaA + tid];
-                    ab = ds_s[i * kCtaA + tid];
-                }
-                pair_set<NT>(inj, i, ab);
-                pair_add<NT>(g, i, xb);
-                const float ti = dtau * (float)i;
-                I0 += ab;
-                I1 = fmaf(ab, ti, I1);
-                I2 = fmaf(ab, ti * ti, I2);
-                M0 += xb;
-                M1 = fmaf(xb, ti, M1);
-                M2 = fmaf(xb, ti * ti, M2);
-            }
+        float cbb[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) cbb[q] = 0.f;
+        for (int n = i * stride - 1; n >= (i - 1) * stride; --n) {
 #pragma unroll
             for (int p = 0; p < H; ++p) g[p] = __fadd2_rn(g[p], inj[p]);
             M0 += I0;
@@ -380,20 +391,9 @@ __global__ void __launch_bounds__(kAdjCta, 6)
             M1 = fmaf(k1, M0, M1);
             adjoint_convection_pairs<NT>(g, M.cp);
         }
-        // fold the segment's FP32 partials
+        // fold the block's FP32 partials
 #pragma unroll
-        for (int q = 0; q < 9; ++q) {
-            cb_s[q * kCtaA + tid] += (double)cbb[q];
-            cbb[q] = 0.f;
-        }
-    }
-    // seeds of date 1 (deterministic: h = 0 through block 0), for the seed means
-    if (CKPT) {
-        const float D1 = expf((float)(-P.psum[1] * P.dt));
-        float xb, ab;
-        date_seeds(P, 1, P.psamp[1], D1, xs_s[1 * kCtaA + tid], xb, ab);
-        xs_s[1 * kCtaA + tid] = xb;
-        ds_s[1 * kCtaA + tid] = ab;
+        for (int q = 0; q < 9; ++q) cb_s[q * kCtaA + tid] += (double)cbb[q];
     }
 
     // ---------------------------------------------------------------- CTA reduction
