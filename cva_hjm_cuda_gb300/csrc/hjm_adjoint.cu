@@ -183,6 +183,9 @@ __global__ void __launch_bounds__(kAdjCta, adj_min_ctas<NT>())
     constexpr int kCkRows = NT + 5;
     sample(1);
     int ck = 0, ck_next = stride;  // next checkpoint: before step ck_next
+    const int n_last = n_steps - 1;
+    float q0, q1, q2;  // normals drawn one step ahead (as in path_kernel_mixed)
+    draw_phi<float, false>(nullptr, gpath, lp, P.n_paths, stride, P.rk0, P.rk1, q0, q1, q2);
     for (int b = 1; b < B; ++b) {
         BlockSums bs;
         bs.reset();
@@ -212,8 +215,8 @@ __global__ void __launch_bounds__(kAdjCta, adj_min_ctas<NT>())
                 }
                 ++ck;
             }
-            float phi0, phi1, phi2;
-            draw_phi<float, false>(nullptr, gpath, lp, P.n_paths, n, P.rk0, P.rk1, phi0, phi1, phi2);
+            const float phi0 = q0, phi1 = q1, phi2 = q2;
+            draw_phi<float, false>(nullptr, gpath, lp, P.n_paths, min(n + 1, n_last), P.rk0, P.rk1, q0, q1, q2);
             x.step(M, phi0, phi1, phi2);
             bs.add(x, phi0, phi1, phi2);
         }
@@ -316,9 +319,11 @@ __global__ void __launch_bounds__(kAdjCta, adj_min_ctas<NT>())
                 const double a0 = active ? ck_a[(size_t)sg * ld + lp] : 0.0;
                 BlockSums bs;
                 bs.reset();
+                float r0, r1, r2;
+                draw_phi<float, false>(nullptr, gpath, lp, P.n_paths, n0, P.rk0, P.rk1, r0, r1, r2);
                 for (int n = n0; n <= ni; ++n) {
-                    float phi0, phi1, phi2;
-                    draw_phi<float, false>(nullptr, gpath, lp, P.n_paths, n, P.rk0, P.rk1, phi0, phi1, phi2);
+                    const float phi0 = r0, phi1 = r1, phi2 = r2;
+                    draw_phi<float, false>(nullptr, gpath, lp, P.n_paths, min(n + 1, ni), P.rk0, P.rk1, r0, r1, r2);
                     xr.step(M, phi0, phi1, phi2);
                     bs.add(xr, phi0, phi1, phi2);
                 }
@@ -349,7 +354,10 @@ __global__ void __launch_bounds__(kAdjCta, adj_min_ctas<NT>())
     const float dtau = (float)(1.0 / P.m);
     const float k1 = P.c * dtau, k2 = P.c * dtau * dtau;
 
-    // block i-1 (steps (i-1) stride .. i stride - 1) ends by sampling date i
+    // block i-1 (steps (i-1) stride .. i stride - 1) ends by sampling date i;
+    // normals drawn one step ahead (descending)
+    float r0, r1, r2;
+    draw_phi<float, false>(nullptr, gpath, lp, P.n_paths, n_steps - 1, P.rk0, P.rk1, r0, r1, r2);
     for (int i = B; i >= 2; --i) {
         {
             // date i: its discount seed switches on for all earlier steps, its
@@ -368,14 +376,14 @@ __global__ void __launch_bounds__(kAdjCta, adj_min_ctas<NT>())
         float cbb[9];
 #pragma unroll
         for (int q = 0; q < 9; ++q) cbb[q] = 0.f;
+        // g holds the adjoint times (1 + rr)^k after k steps of this block
+        float sig = 1.f, gam = 1.f;  // (1 + rr)^k and its inverse
         for (int n = i * stride - 1; n >= (i - 1) * stride; --n) {
-#pragma unroll
-            for (int p = 0; p < H; ++p) g[p] = __fadd2_rn(g[p], inj[p]);
             M0 += I0;
             M1 += I1;
             M2 += I2;
-            float phi0, phi1, phi2;
-            draw_phi<float, false>(nullptr, gpath, lp, P.n_paths, n, P.rk0, P.rk1, phi0, phi1, phi2);
+            const float phi0 = r0, phi1 = r1, phi2 = r2;
+            draw_phi<float, false>(nullptr, gpath, lp, P.n_paths, max(n - 1, stride), P.rk0, P.rk1, r0, r1, r2);
             cbb[0] = fmaf(phi0, M0, cbb[0]);
             cbb[1] = fmaf(phi0, M1, cbb[1]);
             cbb[2] = fmaf(phi0, M2, cbb[2]);
@@ -385,11 +393,20 @@ __global__ void __launch_bounds__(kAdjCta, adj_min_ctas<NT>())
             cbb[6] = fmaf(phi2, M0, cbb[6]);
             cbb[7] = fmaf(phi2, M1, cbb[7]);
             cbb[8] = fmaf(phi2, M2, cbb[8]);
-            // moments of A^T g from those of g and its last tenor, then the sweep itself
-            const float gL = pair_tenor<NT>(g, NT - 1);
+            // the sweep itself (seeds of this step folded in), then the
+            // moments of A^T g from those of g and its last tenor
+            float GL;
+            adjoint_step_pairs<NT>(g, inj, sig, P.rr, GL);
+            const float gL = gam * GL;
             M2 = fmaf(-2.f * k2, gL, fmaf(k2, M0, fmaf(2.f * k1, M1, M2)));
             M1 = fmaf(k1, M0, M1);
-            adjoint_convection_pairs<NT>(g, M.cp);
+            sig *= P.ip;
+            gam *= P.qm;
+        }
+        {
+            const float2 gg = make_float2(gam, gam);
+#pragma unroll
+            for (int p = 0; p < H; ++p) g[p] = __fmul2_rn(g[p], gg);
         }
         // fold the block's FP32 partials
 #pragma unroll

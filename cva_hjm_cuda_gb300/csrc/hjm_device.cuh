@@ -73,22 +73,27 @@ __host__ __device__ __forceinline__ uint4 normals_counter(uint64_t path, uint32_
 
 #ifdef __CUDACC__
 // Three N(0,1) draws for one path-step: Box-Muller on the two uniform pairs
-// a = (word >> 8) * 2^-24 in [0, 1) (exact in FP32); radius from log(1 - a),
-// angle pi * (2a - 1).  FP32 with the SFU intrinsics: the normals are inputs
-// of both precision modes (the FP64 mode promotes them exactly), and the
-// oracle consumes these very values through hjm_dump_normals.
+// a = (word >> 8) * 2^-24 in [0, 1) (exact in FP32); radius sqrt(-2 ln(1 - a)),
+// angle pi (2a - 1).  FP32 with the SFU: 1 - a and the angle are one FMA each
+// on the integer's conversion, the logarithm is log2 times -2 ln 2, and the
+// square root is t * rsqrt(t) (t >= 2^-23 or exactly 0, which the max keeps
+// finite).  The normals are inputs of both precision modes (the FP64 mode
+// promotes them exactly), and the oracle consumes these very values through
+// hjm_dump_normals.
 __device__ __forceinline__ void normals3(uint4 w, float& z0, float& z1, float& z2)
 {
-    const float a0 = (float)(w.x >> 8) * 0x1p-24f;
-    const float a1 = (float)(w.y >> 8) * 0x1p-24f;
-    const float a2 = (float)(w.z >> 8) * 0x1p-24f;
-    const float a3 = (float)(w.w >> 8) * 0x1p-24f;
-    const float pi = 3.14159265358979323846f;
-    const float r0 = sqrtf(-2.0f * __logf(1.0f - a0));
-    const float r1 = sqrtf(-2.0f * __logf(1.0f - a2));
+    const float u0 = (float)(w.x >> 8), u1 = (float)(w.y >> 8);
+    const float u2 = (float)(w.z >> 8), u3 = (float)(w.w >> 8);
+    const float kM2Ln2 = -1.38629436111989061883f;          // -2 ln 2
+    const float kAng = 3.74507028e-07f;                      // 2 pi 2^-24
+    const float kPi = 3.14159265358979323846f;
+    const float t0 = kM2Ln2 * __log2f(fmaf(-0x1p-24f, u0, 1.0f));
+    const float t1 = kM2Ln2 * __log2f(fmaf(-0x1p-24f, u2, 1.0f));
+    const float r0 = t0 * rsqrtf(fmaxf(t0, 1e-30f));
+    const float r1 = t1 * rsqrtf(fmaxf(t1, 1e-30f));
     float s0, c0;
-    __sincosf(pi * (2.0f * a1 - 1.0f), &s0, &c0);
-    const float c1 = __cosf(pi * (2.0f * a3 - 1.0f));
+    __sincosf(fmaf(kAng, u1, -kPi), &s0, &c0);
+    const float c1 = __cosf(fmaf(kAng, u3, -kPi));
     z0 = r0 * c0;
     z1 = r0 * s0;
     z2 = r1 * c1;

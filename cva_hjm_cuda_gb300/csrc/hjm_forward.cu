@@ -304,14 +304,20 @@ __global__ void __launch_bounds__(kCta, 4)
     };
 
     sample(1);
+    // normals drawn one step ahead, so that the generator's dependent chain
+    // overlaps the curve update (the last step redraws itself, unused)
+    const int n_last = B * P.stride - 1;
+    const int64_t lpc = active ? lp : 0;
+    float q0, q1, q2;
+    draw_phi<float, EXT>(ext, gpath, lpc, P.n_paths, P.stride, P.rk0, P.rk1, q0, q1, q2);
     for (int b = 1; b < B; ++b) {
         BlockSums bs;
         bs.reset();
         x.begin_block(P, b);
         for (int s = 0; s < P.stride; ++s) {
             const int n = b * P.stride + s;
-            float phi0, phi1, phi2;
-            draw_phi<float, EXT>(ext, gpath, active ? lp : 0, P.n_paths, n, P.rk0, P.rk1, phi0, phi1, phi2);
+            const float phi0 = q0, phi1 = q1, phi2 = q2;
+            draw_phi<float, EXT>(ext, gpath, lpc, P.n_paths, min(n + 1, n_last), P.rk0, P.rk1, q0, q1, q2);
             x.step(M, phi0, phi1, phi2);
             bs.add(x, phi0, phi1, phi2);
         }
@@ -396,7 +402,6 @@ void pack_mixed_params(int nt, const PathParams<float>& P, MixedParams& M)
             M.svp[k][p].x = P.sv[k][p];
             M.svp[k][p].y = (H + p < nt) ? P.sv[k][H + p] : 0.0f;
         }
-    M.cp = make_float2(P.c, P.c);
     M.rp = make_float2(P.rr, P.rr);
     for (int k = 0; k < kFactors; ++k)
         for (int d = 0; d < 3; ++d) M.svcf[k][d] = (float)P.svc[k][d];

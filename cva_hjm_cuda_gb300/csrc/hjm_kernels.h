@@ -36,7 +36,6 @@ struct SelState {
 struct MixedParams {
     PathParams<float> P;
     float2 svp[kFactors][kMaxTenor / 2];
-    float2 cp;  // {c, c}: the adjoint's convection
     float2 rp;  // {rr, rr}: the growth-scaled upwind coefficient
     // polynomial volatility in FP32: sqrt(dt) sigma_k(T) = sum_d svcf[k][d] T^d
     float svcf[kFactors][3];

@@ -226,40 +226,49 @@ __device__ __forceinline__ void block_sums_up(const MixedPath<NT, POLY>& x, cons
     }
 }
 
-// g <- A^T g on the packed adjoint state (A: the upwind convection of the Euler
-// step).  Per tenor, with L the last tenor:
+// One growth-scaled reverse step on the packed adjoint state.  The adjoint
+// obeys g <- A^T (g + inj) with A^T, per tenor (L the last tenor):
 //   t = 0:          (1 - c) g[0]
-//   1 <= t <= L-2:  g[t] + c (g[t-1] - g[t])
-//   t = L-1:        g[t] + c (g[t-1] - g[t]) - c g[L]
-//   t = L:          g[L] + c (g[L] + g[L-1])
+//   1 <= t <= L-2:  (1 - c) g[t] + c g[t-1]
+//   t = L-1:        (1 - c) g[t] + c (g[t-1] - g[L])
+//   t = L:          (1 + c) g[L] + c g[L-1].
+// Holding gs = g (1 + rr)^k after k steps of a block (rr = c / (1 - c), the
+// forward's constant), the step is gs <- Ahat (gs + sig inj) with sig =
+// (1 + rr)^k and Ahat = A^T / (1 - c):
+//   G[t] + rr G[t-1],  G[L-1] + rr (G[L-2] - G[L]),  G[L] + rr (2 G[L] + G[L-1]),
+// one packed FMA for the seeds and one for the step per pair of tenors.
 template <int NT>
-__device__ __forceinline__ void adjoint_convection_pairs(float2 (&g)[PairGrid<NT>::H], float2 cp)
+__device__ __forceinline__ void adjoint_step_pairs(float2 (&g)[PairGrid<NT>::H], const float2 (&inj)[PairGrid<NT>::H],
+                                                   float sig, float rr, float& G_last)
 {
     constexpr int H = PairGrid<NT>::H, L = PairGrid<NT>::L;
-    const float c = cp.x;
-    const float2 m1 = make_float2(-1.0f, -1.0f);
-    float2 gn[H];
+    const float2 ss = make_float2(sig, sig), rp = make_float2(rr, rr);
+    // streamed in ascending pairs with the previous pair's G in registers; the
+    // two values needed ahead of their pair (tenor H-1 for the seam, tenor L
+    // for row L-1) are formed first
+    const float G_seam = fmaf(inj[H - 1].x, sig, g[H - 1].x);
+    G_last = fmaf(inj[L - H].y, sig, g[L - H].y);
+    float2 Gprev = make_float2(0.f, 0.f);
 #pragma unroll
     for (int p = 0; p < H; ++p) {
         const int q = H + p;
+        const float2 Gp = __ffma2_rn(inj[p], ss, g[p]);
         if (p >= 1 && q < L - 1) {
-            gn[p] = __ffma2_rn(cp, __ffma2_rn(m1, g[p], g[p - 1]), g[p]);
+            g[p] = __ffma2_rn(rp, Gprev, Gp);
         } else {
-            gn[p].x = (p == 0) ? fmaf(-c, g[0].x, g[0].x) : fmaf(c, g[p - 1].x - g[p].x, g[p].x);
-            const float gprev = (p == 0) ? g[H - 1].x : g[p - 1].y;  // tenor q-1
-            if (q < L - 1) {
-                gn[p].y = fmaf(c, gprev - g[p].y, g[p].y);
-            } else if (q == L - 1) {
-                gn[p].y = fmaf(-c, g[p + 1].y, fmaf(c, gprev - g[p].y, g[p].y));
-            } else if (q == L) {
-                gn[p].y = fmaf(c, g[p].y + gprev, g[p].y);
-            } else {
-                gn[p].y = 0.0f;  // padding tenor
-            }
+            g[p].x = (p == 0) ? Gp.x : fmaf(rr, Gprev.x, Gp.x);
+            const float gprev = (p == 0) ? G_seam : Gprev.y;  // tenor q-1
+            if (q < L - 1)
+                g[p].y = fmaf(rr, gprev, Gp.y);
+            else if (q == L - 1)
+                g[p].y = fmaf(rr, gprev - G_last, Gp.y);
+            else if (q == L)
+                g[p].y = fmaf(rr, fmaf(2.0f, Gp.y, gprev), Gp.y);
+            else
+                g[p].y = 0.0f;  // padding tenor
         }
+        Gprev = Gp;
     }
-#pragma unroll
-    for (int p = 0; p < H; ++p) g[p] = gn[p];
 }
 
 }  // namespace hjm
