@@ -65,25 +65,26 @@ def algorithmic_flops_per_path(n_tenor: int, n_steps: int, stride: int, form: st
     """Floating-point operations the path kernel's algorithm needs per path
     (FMA = 2), counted from its formulas, not measured.
 
-    ``poly`` (volatility factors quadratic in T, the reference's own table):
-    per evolved Euler step the growth-scaled convection of the remainder
-    (NT + 1 FMAs), the noise projection onto the three scalar parts
-    (3 MUL + 6 FMA), their update (4 FMA + 3 ADD), the last-tenor source
-    (1 MUL) and the block sums (3 ADD + 1 FMA): 2 NT + 32 flops.
-    ``table`` (generic volatility table): 4 FMAs per tenor (three factor
-    loadings and the convection; 5 operations at the last tenor), the
-    normals' scaling (3 MUL), the block sums (3 ADD + 1 FMA): 8 NT + 10.
-    Both add, per block, the renormalisation (NT MUL) and the block-sum
-    recovery of the tenors still to be sampled (about 12 flops each).  The
-    first block holds the curve at spot and does no arithmetic.  Normals,
-    pricing and reductions are not counted, so the fraction is a lower bound
-    on the pipe's use."""
+    Per evolved Euler step:
+    ``poly_tri`` (factor k a polynomial of degree <= k in T, the reference's
+    own volatility table): the growth-scaled convection of the remainder (NT - 1
+    FMAs, 2 FMAs + 1 ADD at the last tenor), the noise projection onto the
+    three scalar parts (3 MUL + 3 FMA), their update (3 FMA + 3 ADD), the
+    scaled last-tenor source (2 MUL) and the block sums (3 ADD + 1 FMA):
+    2 NT + 28 flops.  ``poly`` (general quadratic factors): 6 more (3 FMA),
+    2 NT + 34.  ``table`` (generic volatility table): 4 FMAs per tenor (three
+    factor loadings and the convection; 5 at the last tenor), the normals'
+    scaling (4 MUL), the block sums (3 ADD + 1 FMA): 8 NT + 11.
+    Per block: the block-sum recovery of the tenors still to be sampled
+    (about 12 flops each).  The first block holds the curve at spot and does
+    no arithmetic.  Normals, pricing and reductions are not counted, and an
+    ADD or MUL issues like an FMA, so the fraction is a lower bound on the
+    FP64 pipe's use (ncu's pipe utilisation is the direct measure)."""
     B = n_steps // stride
     evolved = n_steps - stride
-    per_step = 2 * n_tenor + 32 if form == "poly" else 8 * n_tenor + 10
-    per_block = n_tenor
+    per_step = {"poly_tri": 2 * n_tenor + 28, "poly": 2 * n_tenor + 34, "table": 8 * n_tenor + 11}[form]
     recovery = 12 * sum(B - b for b in range(1, B))
-    return evolved * per_step + (B - 1) * per_block + recovery
+    return evolved * per_step + recovery
 
 
 class ClockSampler:
@@ -246,7 +247,8 @@ def run_ours(args) -> None:
     else:
         eng.set_market(mk)
     set_product()
-    vol_form_poly = eng.vol_decomposition()
+    vol_form = eng.vol_form()
+    vol_form_poly = vol_form != "table"
     # weak scaling across ranks: rank r owns paths [r*n, (r+1)*n)
     cfg = RunConfig(n_paths=n_paths, n_steps=n_steps, dt=DT, seed=SEED, path_offset=rank * n_paths)
     flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
@@ -316,7 +318,7 @@ def run_ours(args) -> None:
             dist.destroy_process_group()
         return
 
-    form = "poly" if vol_form_poly else "table"
+    form = vol_form
     flops = algorithmic_flops_per_path(mk.n_tenor, n_steps, stride, form) * n_paths * (2 if is_adjoint else 1)
     extras = {}
     peak_key = "fp64" if prec == "fp64" else "mixed"

@@ -219,7 +219,9 @@ hjm_status hjm_ctx_vol_decomposition(hjm_ctx* ctx, int32_t* active)
 {
     HJM_CHECK_CTX(ctx);
     if (!active) return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "active must not be null");
-    *active = (ctx->have_market && ctx->poly_path && ctx->allow_poly_path) ? 1 : 0;
+    const bool on = ctx->have_market && ctx->poly_path && ctx->allow_poly_path;
+    const bool tri = ctx->coef[1] == 0.0 && ctx->coef[2] == 0.0 && ctx->coef[5] == 0.0;
+    *active = on ? (tri ? 2 : 1) : 0;
     return HJM_OK;
 }
 
@@ -240,11 +242,15 @@ static bool fit_quadratic_vols(const std::vector<double>& vol, int nt, double dt
         // Lagrange basis l_j(x) = prod (x - x_m) / (x_j - x_m) expanded in 1, x, x^2
         const double d0 = (x0 - x1) * (x0 - x2), d1 = (x1 - x0) * (x1 - x2), d2 = (x2 - x0) * (x2 - x1);
         const double w0 = v[i0] / d0, w1 = v[i1] / d1, w2 = v[i2] / d2;
-        const double c2 = w0 + w1 + w2;
-        const double c1 = -(w0 * (x1 + x2) + w1 * (x0 + x2) + w2 * (x0 + x1));
+        double c2 = w0 + w1 + w2;
+        double c1 = -(w0 * (x1 + x2) + w1 * (x0 + x2) + w2 * (x0 + x1));
         const double c0 = w0 * x1 * x2 + w1 * x0 * x2 + w2 * x0 * x1;
         double scale = 0.0;
         for (int t = 0; t < nt; ++t) scale = std::max(scale, std::fabs(v[t]));
+        // a term below rounding over the whole grid is an exact zero of the
+        // factor (lower-degree factors then take the cheaper projection)
+        if (std::fabs(c1) * x2 <= 1e-14 * scale) c1 = 0.0;
+        if (std::fabs(c2) * x2 * x2 <= 1e-14 * scale) c2 = 0.0;
         for (int t = 0; t < nt; ++t) {
             const double T = dtau * t;
             if (std::fabs(c0 + c1 * T + c2 * T * T - v[t]) > 1e-12 * scale) return false;

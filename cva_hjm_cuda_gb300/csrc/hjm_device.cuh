@@ -183,6 +183,21 @@ inline void fill_growth_scale(PathParams<T>& P, double c, double k2, int stride,
 }
 
 #ifdef __CUDACC__
+// Exact FP32 -> FP64 widening with integer operations: the conversion
+// instruction issues on the FP64 pipe, the bound of the FP64 path kernel, and
+// these bit moves do not.  Exact for zero and normal numbers; the Box-Muller
+// outputs are zero or at least ~1e-12 in magnitude, never subnormal, and a
+// subnormal input would give a signed zero.
+__device__ __forceinline__ double widen_f32(float f)
+{
+    const uint32_t u = __float_as_uint(f);
+    const uint32_t mag = u & 0x7fffffffu;
+    const bool normal = mag >= 0x00800000u;
+    const uint32_t hi = (u & 0x80000000u) | (normal ? (mag >> 3) + 0x38000000u : 0u);
+    const uint32_t lo = normal ? (mag << 29) : 0u;
+    return __hiloint2double((int)hi, (int)lo);
+}
+
 // The three normals of (path, step): Philox in registers, or read from a
 // caller-supplied buffer laid out [step][3][path] (coalesced across threads).
 template <typename T, bool EXT>
@@ -199,9 +214,15 @@ __device__ __forceinline__ void draw_phi(const double* __restrict__ ext, uint64_
         const uint4 w = philox4x32_10_rk(normals_counter(gpath, (uint32_t)n), rk0, rk1);
         float z0, z1, z2;
         normals3(w, z0, z1, z2);
-        phi0 = (T)z0;
-        phi1 = (T)z1;
-        phi2 = (T)z2;
+        if constexpr (sizeof(T) == 8) {
+            phi0 = widen_f32(z0);
+            phi1 = widen_f32(z1);
+            phi2 = widen_f32(z2);
+        } else {
+            phi0 = z0;
+            phi1 = z1;
+            phi2 = z2;
+        }
     }
 }
 

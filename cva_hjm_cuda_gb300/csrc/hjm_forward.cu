@@ -70,13 +70,18 @@ __host__ __device__ inline size_t path_smem_bytes(int nt, int n_blocks, bool mix
 // convection of hc per tenor instead of 5 operations, plus a dozen per step.
 // With the growth scaling of PathParams (v = h / (1-c)^j) the convection is
 // one FMA per tenor, and the table form four.
-template <int NT, bool EXT, bool POLY>
+// FORM: kFormTable (volatility table), kFormPoly (quadratic factors) or
+// kFormPolyTri (factor k of degree <= k, the reference's own table: the noise
+// projection then skips the three zero coefficients).
+template <int NT, bool EXT, int FORM>
 __global__ void __launch_bounds__(kFp64Cta, 4)
     path_kernel_fp64(const __grid_constant__ PathParams<double> P, const double* __restrict__ ext,
                      double* __restrict__ partials, double* __restrict__ estore)
 {
     constexpr int kCta = kFp64Cta;
     constexpr int L = NT - 1;
+    constexpr bool POLY = FORM != kFormTable;
+    constexpr bool TRI = FORM == kFormPolyTri;
     extern __shared__ __align__(128) unsigned char smem[];
     const int tid = threadIdx.x;
     const int B = P.n_blocks;
@@ -121,24 +126,36 @@ __global__ void __launch_bounds__(kFp64Cta, 4)
     sample(1);
     const double c = P.c, rr = P.rr;
     for (int b = 1; b < B; ++b) {
-        double f0 = 0.0, f1 = 0.0, f2 = 0.0, hb = 0.0;  // block sums of phi_k and of h[B]
-        double sS = 0.0, sU = 0.0, sW = 0.0;            // POLY: block sums of S, U, W
-        g = P.gblk[b];
-        double ig = P.igblk[b];
+        double f0 = 0.0, f1 = 0.0, f2 = 0.0;  // block sums of phi_k
+        double sS = 0.0, sU = 0.0, sW = 0.0;  // POLY: block sums of S, U, W
+        // anchor: hb = sum_s h_s[B] = g_end * Tb with Tb <- (1 + rr) Tb + v[B]
+        // (g_s = g_end (1 + rr)^(stride - s)), one FMA per step
+        double Tb = 0.0;
+        double ig = P.igblk[b];          // table form: (1 + rr)^n'
+        double mig = P.m2k2 * P.igblk[b];  // polynomial form: -2 c dtau^2 (1 + rr)^n'
         for (int s = 0; s < P.stride; ++s) {
             const int n = b * P.stride + s;
             double phi0, phi1, phi2;
             draw_phi<double, EXT>(ext, gpath, active ? lp : 0, P.n_paths, n, P.rk0, P.rk1, phi0, phi1, phi2);
-            ig *= P.ip;
-            double hn[NT];
+            // in place, ascending (h[t+1] is still the old value); the last
+            // tenor, which reads h[L-1], first
             if constexpr (POLY) {
-                const double al = fma(P.svc[2][0], phi2, fma(P.svc[1][0], phi1, P.svc[0][0] * phi0));
-                const double be = fma(P.svc[2][1], phi2, fma(P.svc[1][1], phi1, P.svc[0][1] * phi0));
-                const double ga = fma(P.svc[2][2], phi2, fma(P.svc[1][2], phi1, P.svc[0][2] * phi0));
-                const double src = (P.m2k2 * W) * ig;  // -2 c dtau^2 W, scaled
+                double al, be, ga;
+                if constexpr (TRI) {
+                    al = fma(P.svc[2][0], phi2, fma(P.svc[1][0], phi1, P.svc[0][0] * phi0));
+                    be = fma(P.svc[2][1], phi2, P.svc[1][1] * phi1);
+                    ga = P.svc[2][2] * phi2;
+                } else {
+                    al = fma(P.svc[2][0], phi2, fma(P.svc[1][0], phi1, P.svc[0][0] * phi0));
+                    be = fma(P.svc[2][1], phi2, fma(P.svc[1][1], phi1, P.svc[0][1] * phi0));
+                    ga = fma(P.svc[2][2], phi2, fma(P.svc[1][2], phi1, P.svc[0][2] * phi0));
+                }
+                mig *= P.ip;
+                const double src = mig * W;  // -2 c dtau^2 W, scaled
+                const double hl = fma(rr, fma(2.0, h[L], -h[L - 1]), h[L]) + src;
 #pragma unroll
-                for (int t = 0; t < L; ++t) hn[t] = fma(rr, h[t + 1], h[t]);
-                hn[L] = fma(rr, fma(2.0, h[L], -h[L - 1]), h[L]) + src;
+                for (int t = 0; t < L; ++t) h[t] = fma(rr, h[t + 1], h[t]);
+                h[L] = hl;
                 const double Sn = fma(P.k2, W, fma(P.k1, U, S)) + al;
                 U = fma(2.0 * P.k1, W, U) + be;
                 W += ga;
@@ -147,28 +164,28 @@ __global__ void __launch_bounds__(kFp64Cta, 4)
                 sU += U;
                 sW += W;
             } else {
+                ig *= P.ip;
                 const double p0 = phi0 * ig, p1 = phi1 * ig, p2 = phi2 * ig;
+                double xl = fma(P.sv[0][L], p0, h[L]);
+                xl = fma(P.sv[1][L], p1, xl);
+                xl = fma(P.sv[2][L], p2, xl);
+                const double hl = fma(rr, fma(2.0, h[L], -h[L - 1]), xl);
 #pragma unroll
                 for (int t = 0; t < L; ++t) {
                     double x = fma(P.sv[0][t], p0, h[t]);
                     x = fma(P.sv[1][t], p1, x);
                     x = fma(P.sv[2][t], p2, x);
-                    hn[t] = fma(rr, h[t + 1], x);
+                    h[t] = fma(rr, h[t + 1], x);
                 }
-                double xl = fma(P.sv[0][L], p0, h[L]);
-                xl = fma(P.sv[1][L], p1, xl);
-                xl = fma(P.sv[2][L], p2, xl);
-                hn[L] = fma(rr, fma(2.0, h[L], -h[L - 1]), xl);
+                h[L] = hl;
                 f0 += phi0;
                 f1 += phi1;
                 f2 += phi2;
             }
-#pragma unroll
-            for (int t = 0; t < NT; ++t) h[t] = hn[t];
-            g *= P.qm;
-            hb = fma(g, select_reg<NT, double>(h, B), hb);
+            Tb = fma(P.ip, Tb, select_reg<NT, double>(h, B));
         }
-        // stage the block-end curve, then recover the block sums of tenors (b, B]
+        g = P.gblk[b + 1];  // (1 + rr)^-(b stride): the scale at the block end
+        const double hb = g * Tb;
 #pragma unroll
         for (int t = 0; t < NT; ++t)
             if (t <= B + 1) he_s[t * kCta + tid] = g * h[t];
@@ -608,12 +625,12 @@ __global__ void widen_exposures_kernel(const T* __restrict__ in, int64_t ld, int
 // ---------------------------------------------------------------------------
 // Host launchers
 // ---------------------------------------------------------------------------
-template <int NT, bool EXT, bool POLY>
+template <int NT, bool EXT, int FORM>
 static cudaError_t launch_fp64_t(const PathParams<double>& P, const double* ext, double* partials, double* estore,
                                  cudaStream_t s)
 {
     const size_t smem = path_smem_bytes(NT, P.n_blocks, false);
-    auto k = path_kernel_fp64<NT, EXT, POLY>;
+    auto k = path_kernel_fp64<NT, EXT, FORM>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const int64_t grid = (P.n_paths + kFp64Cta - 1) / kFp64Cta;
@@ -625,10 +642,13 @@ template <int NT>
 static cudaError_t launch_fp64_nt(const PathParams<double>& P, bool poly, const double* ext, double* partials,
                                   double* estore, cudaStream_t s)
 {
-    if (ext) return poly ? launch_fp64_t<NT, true, true>(P, ext, partials, estore, s)
-                         : launch_fp64_t<NT, true, false>(P, ext, partials, estore, s);
-    return poly ? launch_fp64_t<NT, false, true>(P, ext, partials, estore, s)
-                : launch_fp64_t<NT, false, false>(P, ext, partials, estore, s);
+    const bool tri = poly && P.svc[0][1] == 0.0 && P.svc[0][2] == 0.0 && P.svc[1][2] == 0.0;
+    if (ext) return tri    ? launch_fp64_t<NT, true, kFormPolyTri>(P, ext, partials, estore, s)
+                    : poly ? launch_fp64_t<NT, true, kFormPoly>(P, ext, partials, estore, s)
+                           : launch_fp64_t<NT, true, kFormTable>(P, ext, partials, estore, s);
+    return tri    ? launch_fp64_t<NT, false, kFormPolyTri>(P, ext, partials, estore, s)
+           : poly ? launch_fp64_t<NT, false, kFormPoly>(P, ext, partials, estore, s)
+                  : launch_fp64_t<NT, false, kFormTable>(P, ext, partials, estore, s);
 }
 
 cudaError_t launch_path_fp64(int nt, const PathParams<double>& P, bool poly, const double* ext, double* partials,

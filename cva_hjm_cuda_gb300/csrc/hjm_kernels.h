@@ -43,6 +43,11 @@ struct MixedParams {
 };
 
 
+// Volatility forms of the FP64 path kernel.
+constexpr int kFormTable = 0;    // volatility table PathParams::sv
+constexpr int kFormPoly = 1;     // factors quadratic in T, PathParams::svc
+constexpr int kFormPolyTri = 2;  // ... with factor k of degree <= k
+
 // poly: the volatility factors are polynomials of degree <= 2 in T (PathParams::svc)
 cudaError_t launch_path_fp64(int nt, const PathParams<double>& P, bool poly, const double* ext, double* partials,
                              double* estore, cudaStream_t s);

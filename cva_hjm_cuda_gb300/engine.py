@@ -93,9 +93,13 @@ class HJMEngine:
         returns whether the current market runs it."""
         if enable is not None:
             self._check(self.lib.hjm_ctx_set_vol_decomposition(self.ctx, 1 if enable else 0))
+        return self.vol_form() != "table"
+
+    def vol_form(self) -> str:
+        """The step the current market runs: "table", "poly" or "poly_tri"."""
         active = C.c_int32(0)
         self._check(self.lib.hjm_ctx_vol_decomposition(self.ctx, C.byref(active)))
-        return bool(active.value)
+        return ("table", "poly", "poly_tri")[active.value]
 
     def set_market(self, market: Market, drift: bool = True) -> None:
         spot, vol = _f64(market.spot), _f64(market.vol).ravel()

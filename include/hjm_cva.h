@@ -88,8 +88,9 @@ hjm_status hjm_ctx_keep_exposures(hjm_ctx* ctx, int32_t keep);
  * carry the stochastic curve as S + U T + W T^2 plus a remainder driven only at
  * the last tenor, instead of adding the three factor columns to every tenor
  * each step (simulation_gpu.cu:153-180).  enable = 0 forces the generic
- * table-driven step; default 1.  hjm_ctx_vol_decomposition reports whether the
- * current market runs the decomposition. */
+ * table-driven step; default 1.  hjm_ctx_vol_decomposition reports what the
+ * current market runs: 0 the table step, 1 the decomposition, 2 the
+ * decomposition with factor k of degree <= k (three zero coefficients). */
 hjm_status hjm_ctx_set_vol_decomposition(hjm_ctx* ctx, int32_t enable);
 hjm_status hjm_ctx_vol_decomposition(hjm_ctx* ctx, int32_t* active);
 

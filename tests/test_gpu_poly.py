@@ -109,6 +109,7 @@ def test_reference_table_is_detected_as_polynomial(engine, golden_10y):
     mk, sw = market_from_golden(golden_10y)
     engine.set_market(mk)
     assert engine.vol_decomposition()
+    assert engine.vol_form() == "poly_tri"  # factor k of degree k, as fitted from the table
     bumped = Market(vol=mk.vol + 1e-6 * np.sin(np.arange(51))[None, :])
     engine.set_market(bumped)
     assert not engine.vol_decomposition()
@@ -201,3 +202,29 @@ def test_poly_netting_set_vs_oracle(engine):
     v = engine.run(cfg, "fp64")
     _assert_rel(v.ee[:61], ee[:61], FP64_RTOL, "netting EE")
     _assert_rel(v.cva, cva, FP64_RTOL, "netting CVA")
+
+
+FULL_COEFFS = np.array([[0.0060, 0.00010, -0.000004],
+                        [-0.0036, 0.00040, 0.000003],
+                        [0.0020, -0.00060, 0.00002]])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_general_quadratic_factors_vs_oracle(engine, precision):
+    """Quadratic factors without the triangular zeros take the full projection."""
+    mk = _poly_market(engine, coef=FULL_COEFFS)
+    assert engine.vol_form() == "poly"
+    sw = Swap()
+    engine.set_swap(sw)
+    cfg = RunConfig(n_paths=4000, seed=21)
+    normals = engine.dump_normals(cfg.n_paths, cfg.n_steps, cfg.seed)
+    x = O.exposure_paths(mk, sw, cfg.n_steps, cfg.dt, normals)
+    ee = O.expected_exposure(x)
+    cva, _ = O.cva(ee, 21, mk.dtau, cfg.hazard, cfg.recovery)
+    v = engine.run(cfg, precision)
+    tol = FP64_RTOL if precision == "fp64" else MIXED_RTOL
+    _assert_rel(v.ee[:20], ee[:20], tol, "EE")
+    _assert_rel(v.cva, cva, tol, "CVA")
+    # the same market as a table is detected as the same (general) form
+    engine.set_market(mk)
+    assert engine.vol_form() == "poly"
