@@ -129,16 +129,14 @@ class ClockSampler:
 
 
 def profiled_traffic(kernel_key: str) -> float | None:
-    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
-    f = ROOT / "profiles" / "path_kernel_ncu.md"
-    if not f.exists():
-        return None
-    for line in f.read_text().splitlines():
-        if line.startswith(f"traffic_bytes_per_launch[{kernel_key}]:"):
-            try:
-                return float(line.split(":", 1)[1].strip().split()[0])
-            except ValueError:
-                return None
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summaries."""
+    for f in sorted((ROOT / "profiles").glob("*.md")):
+        for line in f.read_text().splitlines():
+            if line.startswith(f"traffic_bytes_per_launch[{kernel_key}]:"):
+                try:
+                    return float(line.split(":", 1)[1].strip().split()[0])
+                except ValueError:
+                    return None
     return None
 
 
