@@ -26,7 +26,7 @@ LIB_DIR = PKG / "lib"
 LIB = LIB_DIR / "libhjmcva.so"
 
 CUDA_SOURCES = ["hjm_forward.cu", "hjm_adjoint.cu", "hjm_capi.cu", "hjm_static.cu", "peak_fma.cu"]
-CXX_SOURCES = ["hjm_dropin.cpp"]
+CXX_SOURCES = ["hjm_dropin.cpp", "hjm_calib.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

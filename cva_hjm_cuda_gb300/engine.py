@@ -220,6 +220,37 @@ class HJMEngine:
         return v.value
 
 
+@dataclass
+class Calibration:
+    vol: np.ndarray        # [3][n_tenor] factor volatilities sqrt(lambda_k) e_k
+    eigval: np.ndarray     # [3] annualised eigenvalues, descending
+    vol_coeffs: np.ndarray # [3][3] polynomial fit of factor k, degree min(k, 2)
+    explained: float       # share of the total variance the three factors carry
+
+    def market(self, spot, dtau: float = 0.5, poly: bool = True) -> Market:
+        """A Market on the calibrated factors: the polynomial fit (poly) or the raw table."""
+        spot = np.asarray(spot, dtype=np.float64)
+        if poly:
+            return Market(n_tenor=spot.size, dtau=dtau, spot=spot, vol_coeffs=self.vol_coeffs.copy())
+        return Market(n_tenor=spot.size, dtau=dtau, spot=spot, vol=self.vol.copy())
+
+
+def calibrate_pca(curves, dtau: float = 0.5, obs_per_year: float = 252.0) -> Calibration:
+    """Volatility factors from historical forward curves [n_obs][n_tenor]
+    (hjm_calibrate_pca: principal components of the annualised covariance of
+    the curve changes, then a polynomial fit of each factor)."""
+    curves = _f64(curves)
+    if curves.ndim != 2:
+        raise ValueError("curves must be [n_obs][n_tenor]")
+    n_obs, nt = curves.shape
+    lib = _lib.load()
+    vol, eig, coef, expl = np.zeros(3 * nt), np.zeros(3), np.zeros(9), C.c_double(0.0)
+    st = lib.hjm_calibrate_pca(_dptr(curves), n_obs, nt, dtau, obs_per_year, 3, _dptr(vol), _dptr(eig), _dptr(coef),
+                               C.byref(expl))
+    _lib.check(st)
+    return Calibration(vol.reshape(3, nt), eig, coef.reshape(3, 3), expl.value)
+
+
 def calculate_exposure_gpu(expected_exposure: np.ndarray, notional: float, K: float, expiry: float, dtau: float,
                            accrual, spot_rates, drift, volatilities, scale: float, num_gpus: int, simN: int,
                            dt: float) -> None:

@@ -152,13 +152,35 @@ hjm_status hjm_run_with_normals(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, 
  * matrix of simulation_gpu.cu:1003 / simulation_cpu.h:362, transposed). */
 hjm_status hjm_get_exposures(hjm_ctx* ctx, double* out_host, int64_t capacity);
 
+/* ---- market input step ------------------------------------------------------ */
+/* Volatility factors from historical forward curves (the step before the path:
+ * the reference hard-codes its result, simulation_gpu_testing.cpp:47-63, and
+ * lists the calibration as a to-do, doc/TODO:13).  Principal components of the
+ * covariance of the curve changes, annualised by obs_per_year (252 for daily
+ * curves):
+ *   curves      [n_obs][n_tenor], tenor t at T = dtau t
+ *   vol_out     [n_factor][n_tenor] sqrt(lambda_k) e_k (factor-major, the
+ *               layout hjm_set_market takes); the component of largest
+ *               magnitude of each factor is positive
+ *   eigval_out  [n_factor] lambda_k, descending (may be NULL)
+ *   coef_out    [n_factor * 3] least-squares fit of factor k by a polynomial of
+ *               degree min(k, 2) in T (coefficients of 1, T, T^2; the input of
+ *               hjm_set_market_poly; may be NULL)
+ *   explained_out  share of the total variance the factors carry (may be NULL)
+ * n_factor must be 3.  Host computation in FP64; needs no GPU. */
+hjm_status hjm_calibrate_pca(const double* curves, int32_t n_obs, int32_t n_tenor, double dtau,
+                             double obs_per_year, int32_t n_factor, double* vol_out, double* eigval_out,
+                             double* coef_out, double* explained_out);
+
 /* ---- sensitivities ---------------------------------------------------------- */
 /* Pathwise adjoint of the CVA: dCVA/d(initial forwards) [n_tenor],
  * dCVA/d(drift table) [n_tenor], dCVA/d(polynomial volatility coefficients)
  * [HJM_N_VOL_COEF] (diffusion and trapezoid-drift paths; coefficient (k,d)
  * multiplies T^d in factor k), and dCVA/d(hazard).  Curve states are
- * checkpointed every checkpoint_every steps (0 = none) and recomputed in the
- * reverse sweep.  Requires a market set through hjm_set_market_poly. */
+ * checkpointed every checkpoint_every steps (0 = none: the sampled states are
+ * kept instead) and each date's state is recomputed from the last checkpoint
+ * before it for the reverse sweep.  Requires a market set through
+ * hjm_set_market_poly. */
 hjm_status hjm_set_market_poly(hjm_ctx* ctx, int32_t n_tenor, double dtau, const double* spot_host,
                                const double* vol_coef_host /* [3][3] */);
 hjm_status hjm_run_adjoint(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, double dt, uint64_t seed,
