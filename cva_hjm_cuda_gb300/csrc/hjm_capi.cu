@@ -96,6 +96,20 @@ struct hjm_ctx {
     cudaEvent_t ring[kRing][4] = {};
     int64_t n_enqueued = 0;
     cudaEvent_t* ev = nullptr;  // the quadruple of the current valuation
+
+    // what hjm_write_report writes: the last valuation fetched, or the last
+    // adjoint run (run = the inputs of the call, filled at enqueue time)
+    struct Report {
+        bool valid = false, adjoint = false, pfe = false, external_normals = false;
+        int64_t n_paths = 0;
+        int n_steps = 0, n_dates = 0, precision = 0, vol_form = 0, ckpt = 0, nt = 0;
+        double dt = 0, dtau = 0, hazard = 0, recovery = 0, pfe_q = 0;
+        uint64_t seed = 0, path_offset = 0;
+        std::vector<double> ee, pfe_v, dspot, ddrift;
+        double dcoef[HJM_N_VOL_COEF] = {0};
+        bool have_dcoef = false;
+        double cva = 0, cva_stderr = 0, dhazard = 0;
+    } rep, rep_run;
 };
 
 static hjm_status fail(hjm_ctx* ctx, hjm_status st, const char* fmt, ...)
@@ -208,6 +222,15 @@ hjm_status hjm_ctx_keep_exposures(hjm_ctx* ctx, int32_t keep)
     return HJM_OK;
 }
 
+static bool use_poly_path(const hjm_ctx* ctx) { return ctx->poly_path && ctx->allow_poly_path; }
+
+// 0: table step, 1: quadratic factors, 2: factor k of degree <= k
+static int vol_form_code(const hjm_ctx* ctx)
+{
+    if (!(ctx->have_market && use_poly_path(ctx))) return 0;
+    return (ctx->coef[1] == 0.0 && ctx->coef[2] == 0.0 && ctx->coef[5] == 0.0) ? 2 : 1;
+}
+
 hjm_status hjm_ctx_set_vol_decomposition(hjm_ctx* ctx, int32_t enable)
 {
     HJM_CHECK_CTX(ctx);
@@ -219,9 +242,7 @@ hjm_status hjm_ctx_vol_decomposition(hjm_ctx* ctx, int32_t* active)
 {
     HJM_CHECK_CTX(ctx);
     if (!active) return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "active must not be null");
-    const bool on = ctx->have_market && ctx->poly_path && ctx->allow_poly_path;
-    const bool tri = ctx->coef[1] == 0.0 && ctx->coef[2] == 0.0 && ctx->coef[5] == 0.0;
-    *active = on ? (tri ? 2 : 1) : 0;
+    *active = vol_form_code(ctx);
     return HJM_OK;
 }
 
@@ -447,7 +468,6 @@ static void deterministic_curve(const hjm_ctx* ctx, int stride, int B, double dt
     }
 }
 
-static bool use_poly_path(const hjm_ctx* ctx) { return ctx->poly_path && ctx->allow_poly_path; }
 
 template <typename T>
 static void fill_params(const hjm_ctx* ctx, const RunShape& sh, int64_t n_paths, double dt, uint64_t seed,
@@ -559,6 +579,25 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
         ctx->stat_launches += 2 + 2 * (mixed ? 4 : 8);  // init, 8-bit digit passes (histogram + scan), write
     }
     HJM_CUDA(ctx, cudaEventRecord(ctx->ev[3], s));
+    {
+        hjm_ctx::Report& r = ctx->rep_run;
+        r = hjm_ctx::Report();
+        r.n_paths = n_paths;
+        r.n_steps = n_steps;
+        r.n_dates = n_dates;
+        r.nt = ctx->nt;
+        r.precision = precision;
+        r.vol_form = vol_form_code(ctx);
+        r.dt = dt;
+        r.dtau = ctx->dtau;
+        r.hazard = hazard;
+        r.recovery = recovery;
+        r.pfe_q = pfe_q;
+        r.pfe = want_pfe;
+        r.seed = seed;
+        r.path_offset = path_offset;
+        r.external_normals = ext_dev != nullptr;
+    }
     ctx->last_n_paths = n_paths;
     ctx->last_n_dates = n_dates;
     ctx->last_mixed = mixed;
@@ -596,6 +635,14 @@ hjm_status hjm_fetch_results(hjm_ctx* ctx, double* ee_out, double* pfe_out, doub
         cva_out[HJM_CVA_STDERR] = res[kResCVAStderr];
         cva_out[HJM_CVA_DHAZARD] = res[kResDCVADHazard];
     }
+    hjm_ctx::Report& r = ctx->rep;
+    r = ctx->rep_run;
+    r.valid = true;
+    r.ee.assign(res + kResEE, res + kResEE + ctx->nt);
+    if (ctx->last_pfe) r.pfe_v.assign(res + kResPFE, res + kResPFE + ctx->nt);
+    r.cva = res[kResCVA];
+    r.cva_stderr = res[kResCVAStderr];
+    r.dhazard = res[kResDCVADHazard];
     return HJM_OK;
 }
 
@@ -853,11 +900,33 @@ hjm_status hjm_run_adjoint(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, doubl
         qn[L] = q[L] + c * (q[L] + q[L - 1]);
         q.swap(qn);
     }
+    hjm_ctx::Report& r = ctx->rep;
+    r = hjm_ctx::Report();
+    r.valid = r.adjoint = true;
+    r.n_paths = n_paths;
+    r.n_steps = n_steps;
+    r.n_dates = B + 1;
+    r.nt = nt;
+    r.precision = HJM_PRECISION_MIXED;
+    r.vol_form = vol_form_code(ctx);
+    r.ckpt = K;
+    r.dt = dt;
+    r.dtau = ctx->dtau;
+    r.hazard = hazard_rate;
+    r.recovery = recovery;
+    r.seed = seed;
+    r.path_offset = path_offset;
+    r.cva = res[kResCVA];
+    r.cva_stderr = res[kResCVAStderr];
+    r.dhazard = res[kResDCVADHazard];
+    r.dspot.resize(nt);
+    for (int t = 0; t < nt; ++t) r.dspot[t] = q[t] + (double)(sh.stride - 1) * inj[t];
+    r.ddrift = dmu;
     if (dcva_dspot_out)
-        for (int t = 0; t < nt; ++t) dcva_dspot_out[t] = q[t] + (double)(sh.stride - 1) * inj[t];
+        for (int t = 0; t < nt; ++t) dcva_dspot_out[t] = r.dspot[t];
     if (dcva_ddrift_out)
         for (int t = 0; t < nt; ++t) dcva_ddrift_out[t] = dmu[t];
-    if (dcva_dvolcoef_out) {
+    if (ctx->have_poly) {
         // diffusion part, then the trapezoid drift's dependence on the coefficients:
         // mu_i = sum_k sigma_k(tau_i) I_k(i), I_k(i) = sum_{j<=i} (sigma_k(tau_j)+sigma_k(tau_{j-1}))/2 dtau
         // d mu_i / d c_{k,d} = tau_i^d I_k(i) + sigma_k(tau_i) J_d(i),  J_d(i) = sum_{j<=i} (tau_j^d+tau_{j-1}^d)/2 dtau
@@ -876,10 +945,85 @@ hjm_status hjm_run_adjoint(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, doubl
                     }
                     v += dmu[i] * (std::pow(ti, d) * I + sig[i] * J);
                 }
-                dcva_dvolcoef_out[k * 3 + d] = v;
+                r.dcoef[k * 3 + d] = v;
+                if (dcva_dvolcoef_out) dcva_dvolcoef_out[k * 3 + d] = v;
             }
         }
+        r.have_dcoef = true;
     }
+    return HJM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// report
+// ---------------------------------------------------------------------------
+static void put_array(FILE* f, const char* name, const std::vector<double>& v, bool comma = true)
+{
+    std::fprintf(f, "  \"%s\": [", name);
+    for (size_t i = 0; i < v.size(); ++i) std::fprintf(f, "%s%.17g", i ? ", " : "", v[i]);
+    std::fprintf(f, "]%s\n", comma ? "," : "");
+}
+
+hjm_status hjm_write_report(hjm_ctx* ctx, const char* path, int32_t format)
+{
+    HJM_CHECK_CTX(ctx);
+    const hjm_ctx::Report& r = ctx->rep;
+    if (!r.valid) return fail(ctx, HJM_ERR_NOT_CONFIGURED, "no valuation fetched and no adjoint run yet");
+    if (!path) return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "path must not be null");
+    if (format != HJM_REPORT_JSON && format != HJM_REPORT_CSV)
+        return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "unknown report format %d", format);
+    FILE* f = std::fopen(path, "w");
+    if (!f) return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "cannot open %s for writing", path);
+    static const char* kForms[] = {"table", "poly", "poly_tri"};
+    std::vector<double> dates(r.nt);
+    for (int j = 0; j < r.nt; ++j) dates[j] = r.dtau * j;
+    const char* prec = r.precision == HJM_PRECISION_FP64 ? "fp64" : "mixed";
+    if (format == HJM_REPORT_JSON) {
+        std::fprintf(f, "{\n  \"engine\": \"%s\",\n", hjm_version());
+        std::fprintf(f, "  \"kind\": \"%s\",\n", r.adjoint ? "adjoint" : "valuation");
+        std::fprintf(f,
+                     "  \"run\": {\"n_paths\": %lld, \"n_steps\": %d, \"dt\": %.17g, \"dtau\": %.17g, "
+                     "\"n_tenor\": %d, \"sampled_dates\": %d, \"seed\": %llu, \"path_offset\": %llu, "
+                     "\"precision\": \"%s\", \"vol_form\": \"%s\", \"hazard\": %.17g, \"recovery\": %.17g, "
+                     "\"pfe_quantile\": %.17g, \"checkpoint_every\": %d, \"external_normals\": %s},\n",
+                     (long long)r.n_paths, r.n_steps, r.dt, r.dtau, r.nt, r.n_dates - 1, (unsigned long long)r.seed,
+                     (unsigned long long)r.path_offset, prec, kForms[r.vol_form], r.hazard, r.recovery,
+                     r.pfe ? r.pfe_q : 0.0, r.ckpt, r.external_normals ? "true" : "false");
+        std::fprintf(f, "  \"cva\": %.17g,\n  \"cva_stderr\": %.17g,\n  \"dcva_dhazard\": %.17g,\n", r.cva,
+                     r.cva_stderr, r.dhazard);
+        put_array(f, "dates", dates);
+        if (r.adjoint) {
+            put_array(f, "dcva_dspot", r.dspot);
+            std::vector<double> dc(r.dcoef, r.dcoef + HJM_N_VOL_COEF);
+            put_array(f, "dcva_dvolcoef", dc, true);
+            put_array(f, "dcva_ddrift", r.ddrift, false);
+        } else {
+            put_array(f, "ee", r.ee, r.pfe);
+            if (r.pfe) put_array(f, "pfe", r.pfe_v, false);
+        }
+        std::fprintf(f, "}\n");
+    } else {
+        std::fprintf(f, "# %s %s\n", hjm_version(), r.adjoint ? "adjoint" : "valuation");
+        std::fprintf(f, "key,value\n");
+        std::fprintf(f, "n_paths,%lld\nn_steps,%d\ndt,%.17g\ndtau,%.17g\nseed,%llu\nprecision,%s\nvol_form,%s\n",
+                     (long long)r.n_paths, r.n_steps, r.dt, r.dtau, (unsigned long long)r.seed, prec,
+                     kForms[r.vol_form]);
+        std::fprintf(f, "hazard,%.17g\nrecovery,%.17g\ncva,%.17g\ncva_stderr,%.17g\ndcva_dhazard,%.17g\n", r.hazard,
+                     r.recovery, r.cva, r.cva_stderr, r.dhazard);
+        if (r.adjoint) {
+            for (int q = 0; q < HJM_N_VOL_COEF; ++q)
+                std::fprintf(f, "dcva_dvolcoef_%d%d,%.17g\n", q / 3, q % 3, r.dcoef[q]);
+            std::fprintf(f, "tenor,t,dcva_dspot,dcva_ddrift\n");
+            for (int j = 0; j < r.nt; ++j)
+                std::fprintf(f, "%d,%.17g,%.17g,%.17g\n", j, dates[j], r.dspot[j], r.ddrift[j]);
+        } else {
+            std::fprintf(f, "date,t,ee,pfe\n");
+            for (int j = 0; j < r.nt; ++j)
+                std::fprintf(f, "%d,%.17g,%.17g,%.17g\n", j, dates[j], r.ee[j], r.pfe ? r.pfe_v[j] : 0.0);
+        }
+    }
+    const bool ok = std::fclose(f) == 0;
+    if (!ok) return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "writing %s failed", path);
     return HJM_OK;
 }
 

@@ -88,6 +88,11 @@ class HJMEngine:
     def keep_exposures(self, keep: bool = True) -> None:
         self._check(self.lib.hjm_ctx_keep_exposures(self.ctx, 1 if keep else 0))
 
+    def write_report(self, path, fmt: str = "json") -> None:
+        """The last valuation (or adjoint run) with its inputs, as JSON or CSV."""
+        code = {"json": 0, "csv": 1}[fmt]
+        self._check(self.lib.hjm_write_report(self.ctx, str(path).encode(), code))
+
     def vol_decomposition(self, enable: bool | None = None) -> bool:
         """Allow (True) or forbid (False) the polynomial volatility decomposition;
         returns whether the current market runs it."""

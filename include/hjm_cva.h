@@ -152,6 +152,17 @@ hjm_status hjm_run_with_normals(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, 
  * matrix of simulation_gpu.cu:1003 / simulation_cpu.h:362, transposed). */
 hjm_status hjm_get_exposures(hjm_ctx* ctx, double* out_host, int64_t capacity);
 
+/* ---- report ----------------------------------------------------------------- */
+/* The results of the last valuation fetched (hjm_run, hjm_fetch_results,
+ * hjm_run_with_normals) or of the last hjm_run_adjoint, with the run's inputs,
+ * written to a file: JSON (one object: run, cva, cva_stderr, dcva_dhazard,
+ * dates, ee and pfe, or the sensitivities) or CSV (key,value lines, then one
+ * row per tenor).  Numbers round-trip (17 significant digits).  The reference
+ * prints its 51 EE values on stdout (simulation_gpu_testing.cpp:248-252). */
+#define HJM_REPORT_JSON 0
+#define HJM_REPORT_CSV 1
+hjm_status hjm_write_report(hjm_ctx* ctx, const char* path, int32_t format);
+
 /* ---- market input step ------------------------------------------------------ */
 /* Volatility factors from historical forward curves (the step before the path:
  * the reference hard-codes its result, simulation_gpu_testing.cpp:47-63, and
