@@ -65,26 +65,33 @@ def algorithmic_flops_per_path(n_tenor: int, n_steps: int, stride: int, form: st
     """Floating-point operations the path kernel's algorithm needs per path
     (FMA = 2), counted from its formulas, not measured.
 
-    Per evolved Euler step:
+    During block b (the steps that end by sampling date b+1) only tenors
+    b+1 .. L are ever read again (the upwind step carries information from
+    high to low tenors), so the needed convection covers those.  Per evolved
+    Euler step of block b:
     ``poly_tri`` (factor k a polynomial of degree <= k in T, the reference's
-    own volatility table): the growth-scaled convection of the remainder (NT - 1
-    FMAs, 2 FMAs + 1 ADD at the last tenor), the noise projection onto the
-    three scalar parts (3 MUL + 3 FMA), their update (3 FMA + 3 ADD), the
-    scaled last-tenor source (2 MUL) and the block sums (3 ADD + 1 FMA):
-    2 NT + 28 flops.  ``poly`` (general quadratic factors): 6 more (3 FMA),
-    2 NT + 34.  ``table`` (generic volatility table): 4 FMAs per tenor (three
-    factor loadings and the convection; 5 at the last tenor), the normals'
-    scaling (4 MUL), the block sums (3 ADD + 1 FMA): 8 NT + 11.
+    own volatility table): the growth-scaled convection of the remainder
+    (L - 1 - b FMAs, 2 FMAs + 1 ADD at the last tenor), the noise projection
+    onto the three scalar parts (3 MUL + 3 FMA), their update (3 FMA + 3 ADD),
+    the scaled last-tenor source (2 MUL) and the block sums (3 ADD + 1 FMA):
+    2 (NT - b) + 26 flops.  ``poly`` (general quadratic factors): 6 more.
+    ``table`` (generic volatility table): 4 FMAs per live tenor (three factor
+    loadings and the convection; 5 at the last tenor), the normals' scaling
+    (4 MUL), the block sums (3 ADD + 1 FMA): 8 (NT - b) + 3.
     Per block: the block-sum recovery of the tenors still to be sampled
     (about 12 flops each).  The first block holds the curve at spot and does
     no arithmetic.  Normals, pricing and reductions are not counted, and an
     ADD or MUL issues like an FMA, so the fraction is a lower bound on the
     FP64 pipe's use (ncu's pipe utilisation is the direct measure)."""
     B = n_steps // stride
-    evolved = n_steps - stride
-    per_step = {"poly_tri": 2 * n_tenor + 28, "poly": 2 * n_tenor + 34, "table": 8 * n_tenor + 11}[form]
+
+    def per_step(b: int) -> int:
+        return {"poly_tri": 2 * (n_tenor - b) + 26, "poly": 2 * (n_tenor - b) + 32,
+                "table": 8 * (n_tenor - b) + 3}[form]
+
+    steps = sum(stride * per_step(b) for b in range(1, B))
     recovery = 12 * sum(B - b for b in range(1, B))
-    return evolved * per_step + recovery
+    return steps + recovery
 
 
 class ClockSampler:

@@ -82,6 +82,8 @@ __global__ void __launch_bounds__(kFp64Cta, 4)
     constexpr int L = NT - 1;
     constexpr bool POLY = FORM != kFormTable;
     constexpr bool TRI = FORM == kFormPolyTri;
+    constexpr int kGroup = 8;                      // dead-tenor skipping granularity
+    constexpr int kGroups = (L + kGroup - 1) / kGroup;
     extern __shared__ __align__(128) unsigned char smem[];
     const int tid = threadIdx.x;
     const int B = P.n_blocks;
@@ -132,6 +134,10 @@ __global__ void __launch_bounds__(kFp64Cta, 4)
         // (g_s = g_end (1 + rr)^(stride - s)), one FMA per step
         double Tb = 0.0;
         double ig = P.igblk[b];          // table form: (1 + rr)^n'
+        // tenors <= b are never read again (date b was sampled; the upwind step
+        // carries information from high to low tenors only): their groups of
+        // kGroup tenors are skipped, which changes no output bit
+        const int live = b + 1;
         double mig = P.m2k2 * P.igblk[b];  // polynomial form: -2 c dtau^2 (1 + rr)^n'
         for (int s = 0; s < P.stride; ++s) {
             const int n = b * P.stride + s;
@@ -154,7 +160,15 @@ __global__ void __launch_bounds__(kFp64Cta, 4)
                 const double src = mig * W;  // -2 c dtau^2 W, scaled
                 const double hl = fma(rr, fma(2.0, h[L], -h[L - 1]), h[L]) + src;
 #pragma unroll
-                for (int t = 0; t < L; ++t) h[t] = fma(rr, h[t + 1], h[t]);
+                for (int g = 0; g < kGroups; ++g) {
+                    if (kGroup * g + kGroup > live) {  // uniform: skip groups of dead tenors
+#pragma unroll
+                        for (int j = 0; j < kGroup; ++j) {
+                            const int t = kGroup * g + j;
+                            if (t < L) h[t] = fma(rr, h[t + 1], h[t]);
+                        }
+                    }
+                }
                 h[L] = hl;
                 const double Sn = fma(P.k2, W, fma(P.k1, U, S)) + al;
                 U = fma(2.0 * P.k1, W, U) + be;
@@ -171,11 +185,19 @@ __global__ void __launch_bounds__(kFp64Cta, 4)
                 xl = fma(P.sv[2][L], p2, xl);
                 const double hl = fma(rr, fma(2.0, h[L], -h[L - 1]), xl);
 #pragma unroll
-                for (int t = 0; t < L; ++t) {
-                    double x = fma(P.sv[0][t], p0, h[t]);
-                    x = fma(P.sv[1][t], p1, x);
-                    x = fma(P.sv[2][t], p2, x);
-                    h[t] = fma(rr, h[t + 1], x);
+                for (int g = 0; g < kGroups; ++g) {
+                    if (kGroup * g + kGroup > live) {
+#pragma unroll
+                        for (int j = 0; j < kGroup; ++j) {
+                            const int t = kGroup * g + j;
+                            if (t < L) {
+                                double x = fma(P.sv[0][t], p0, h[t]);
+                                x = fma(P.sv[1][t], p1, x);
+                                x = fma(P.sv[2][t], p2, x);
+                                h[t] = fma(rr, h[t + 1], x);
+                            }
+                        }
+                    }
                 }
                 h[L] = hl;
                 f0 += phi0;
