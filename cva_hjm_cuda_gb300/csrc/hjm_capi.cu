@@ -67,6 +67,7 @@ struct hjm_ctx {
     bool have_poly = false;       // coefficients given by hjm_set_market_poly (sensitivities)
     bool poly_path = false;       // the kernels run the polynomial decomposition (coef)
     bool allow_poly_path = true;  // hjm_ctx_set_vol_decomposition
+    int scheme = HJM_SCHEME_EULER;  // hjm_ctx_set_scheme
     int nt = 0;
     double dtau = 0.5;
     std::vector<double> spot, vol, drift;
@@ -102,7 +103,7 @@ struct hjm_ctx {
     struct Report {
         bool valid = false, adjoint = false, pfe = false, external_normals = false;
         int64_t n_paths = 0;
-        int n_steps = 0, n_dates = 0, precision = 0, vol_form = 0, ckpt = 0, nt = 0;
+        int n_steps = 0, n_dates = 0, precision = 0, vol_form = 0, ckpt = 0, nt = 0, scheme = 0;
         double dt = 0, dtau = 0, hazard = 0, recovery = 0, pfe_q = 0;
         uint64_t seed = 0, path_offset = 0;
         std::vector<double> ee, pfe_v, dspot, ddrift;
@@ -229,6 +230,15 @@ static int vol_form_code(const hjm_ctx* ctx)
 {
     if (!(ctx->have_market && use_poly_path(ctx))) return 0;
     return (ctx->coef[1] == 0.0 && ctx->coef[2] == 0.0 && ctx->coef[5] == 0.0) ? 2 : 1;
+}
+
+hjm_status hjm_ctx_set_scheme(hjm_ctx* ctx, int32_t scheme)
+{
+    HJM_CHECK_CTX(ctx);
+    if (scheme != HJM_SCHEME_EULER && scheme != HJM_SCHEME_PREDICTOR_CORRECTOR)
+        return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "unknown time scheme %d", scheme);
+    ctx->scheme = scheme;
+    return HJM_OK;
 }
 
 hjm_status hjm_ctx_set_vol_decomposition(hjm_ctx* ctx, int32_t enable)
@@ -401,6 +411,10 @@ struct RunShape {
     int stride = 0, B = 0;
 };
 
+// Largest growth exponent of the growth-scaled FP32 curve: the scaled noise,
+// |phi| <= 5.8 times e^growth, stays below 1e36 (FP32 overflows at 3.4e38).
+constexpr double kMaxGrowthFp32 = 80.0;
+
 static hjm_status check_run(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, double dt, int32_t precision,
                             double hazard, double recovery, double pfe_q, RunShape& sh)
 {
@@ -431,8 +445,19 @@ static hjm_status check_run(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, doub
         return fail(ctx, HJM_ERR_INVALID_ARGUMENT,
                     "%d sampled dates need %d tenors; the grid has %d (n_steps * dt must not exceed the last tenor)",
                     B, B + 1, ctx->nt);
-    const size_t smem = path_smem(ctx->nt, B, precision == HJM_PRECISION_MIXED);
+    const size_t smem = ctx->scheme == HJM_SCHEME_PREDICTOR_CORRECTOR
+                            ? pc_smem(ctx->nt, B, precision == HJM_PRECISION_MIXED)
+                            : path_smem(ctx->nt, B, precision == HJM_PRECISION_MIXED);
     if (smem > 227 * 1024) return fail(ctx, HJM_ERR_UNSUPPORTED, "shared memory %zu B exceeds 227 KB", smem);
+    // the growth-scaled curve grows by (1 + rr)^n_steps, rr = c / (1 - c); in
+    // FP32 the scaled noise must stay far from overflow
+    const double cc = dt / ctx->dtau;
+    const double growth = (double)n_steps * std::log1p(cc / (1.0 - cc));
+    if (precision == HJM_PRECISION_MIXED && growth > kMaxGrowthFp32)
+        return fail(ctx, HJM_ERR_UNSUPPORTED,
+                    "mixed precision: %d steps at dt/dtau = %.6g grow the scaled curve by e^%.1f (limit e^%.0f); "
+                    "use FP64 or a smaller dt",
+                    n_steps, cc, growth, kMaxGrowthFp32);
     sh.stride = (int)st;
     sh.B = B;
     return HJM_OK;
@@ -444,7 +469,12 @@ static hjm_status check_run(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, doub
 static void deterministic_curve(const hjm_ctx* ctx, int stride, int B, double dt, double* psamp, double* psum)
 {
     const int nt = ctx->nt;
-    std::vector<double> p(ctx->spot), pn(nt), acc(nt, 0.0);
+    std::vector<double> p(ctx->spot), pn(nt), acc(nt, 0.0), ps(nt);
+    // drift term a(f)[t] = mu[t] + dF/dtau (forward difference, backward at the last tenor)
+    auto drift_term = [&](const std::vector<double>& f, int t) {
+        const double dF = (t == nt - 1) ? f[t] - f[t - 1] : f[t + 1] - f[t];
+        return ctx->drift[t] + dF / ctx->dtau;
+    };
     for (int i = 0; i < kMaxTenor; ++i) psamp[i] = psum[i] = 0.0;
     for (int s = 0; s < stride; ++s)
         for (int t = 0; t < nt; ++t) acc[t] += p[t];
@@ -452,11 +482,16 @@ static void deterministic_curve(const hjm_ctx* ctx, int stride, int B, double dt
     psum[1] = acc[1];
     for (int b = 1; b < B; ++b) {
         for (int s = 0; s < stride; ++s) {
-            for (int t = 0; t < nt; ++t) {
-                const double dF = (t == nt - 1) ? p[t] - p[t - 1] : p[t + 1] - p[t];
-                double dfbar = ctx->drift[t] * dt;
-                dfbar += (dF / ctx->dtau) * dt;
-                pn[t] = p[t] + dfbar;
+            if (ctx->scheme == HJM_SCHEME_PREDICTOR_CORRECTOR) {
+                for (int t = 0; t < nt; ++t) ps[t] = p[t] + drift_term(p, t) * dt;
+                for (int t = 0; t < nt; ++t) pn[t] = p[t] + 0.5 * (drift_term(p, t) + drift_term(ps, t)) * dt;
+            } else {
+                for (int t = 0; t < nt; ++t) {
+                    const double dF = (t == nt - 1) ? p[t] - p[t - 1] : p[t + 1] - p[t];
+                    double dfbar = ctx->drift[t] * dt;
+                    dfbar += (dF / ctx->dtau) * dt;
+                    pn[t] = p[t] + dfbar;
+                }
             }
             for (int t = 0; t < nt; ++t) {
                 p[t] = pn[t];
@@ -516,6 +551,43 @@ static void fill_params(const hjm_ctx* ctx, const RunShape& sh, int64_t n_paths,
     F.n_blocks = sh.B;
 }
 
+// Predictor-corrector parameters from the Euler ones: loadings N sqrt(dt)
+// sigma (N = I + c Dl / 2), the stencil r1 = a1/a0, r2 = a2/a0 rounded once,
+// growth scales and effective coefficients derived from them.
+template <typename T>
+static void fill_pc(const hjm_ctx* ctx, const RunShape& sh, double dt, const PathParams<T>& P, PcParams<T>& Q)
+{
+    std::memset(&Q, 0, sizeof(Q));
+    Q.P = P;
+    const int nt = ctx->nt;
+    const double c = dt / ctx->dtau, sq = std::sqrt(dt);
+    for (int k = 0; k < kFactors; ++k) {
+        const double* sig = ctx->vol.data() + (size_t)k * nt;
+        for (int t = 0; t < nt; ++t) {
+            const double d = (t == nt - 1) ? sig[t] - sig[t - 1] : sig[t + 1] - sig[t];
+            Q.P.sv[k][t] = (T)(sq * (sig[t] + 0.5 * c * d));
+        }
+    }
+    const double a0 = 1.0 - c + 0.5 * c * c, a1 = c - c * c, a2 = 0.5 * c * c;
+    const T r1 = (T)(a1 / a0), r2 = (T)(a2 / a0);
+    const double base = 1.0 + (double)r1 + (double)r2;
+    for (int b = 0; b < kMaxTenor; ++b) {
+        const double e = (b >= 1 && b <= sh.B) ? (double)((b - 1) * sh.stride) : 0.0;
+        Q.P.gblk[b] = (T)std::pow(base, -e);
+        Q.P.igblk[b] = (T)std::pow(base, e);
+    }
+    Q.P.ip = (T)base;
+    Q.r1 = r1;
+    Q.r2 = r2;
+    const double ce = ((double)r1 + 2.0 * (double)r2) / base;
+    Q.a0e = (T)(1.0 / base);
+    Q.a1e = (T)((double)r1 / base);
+    Q.a2e = (T)((double)r2 / base);
+    Q.ce = (T)ce;
+    Q.inv_1ma0 = (T)(base / ((double)r1 + (double)r2));
+    Q.inv_ce = (T)(1.0 / ce);
+}
+
 static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, double dt, uint64_t seed,
                                uint64_t path_offset, int32_t precision, double hazard, double recovery, double pfe_q,
                                const double* ext_dev)
@@ -529,7 +601,8 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
     const bool store = want_pfe || ctx->keep_exposures;
     const int n_dates = sh.B + 1;
     const int R = sh.B + 3;
-    const int cta = path_cta(mixed);
+    const bool pc = ctx->scheme == HJM_SCHEME_PREDICTOR_CORRECTOR;
+    const int cta = pc ? pc_cta() : path_cta(mixed);
     const int64_t n_ctas = (n_paths + cta - 1) / cta;
     const int64_t ld = (n_paths + 3) / 4 * 4;
     const size_t esize = mixed ? 4 : 8;
@@ -553,7 +626,23 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
     ctx->stat_h2d = (mixed ? sizeof(MixedParams) : sizeof(PathParams<double>)) + sizeof(FinalParams);
     ctx->stat_d2h = 0;
     HJM_CUDA(ctx, cudaEventRecord(ctx->ev[0], s));
-    if (mixed) {
+    if (pc && mixed) {
+        PathParams<float> P;
+        fill_params<float>(ctx, sh, n_paths, dt, seed, path_offset, hazard, recovery, ld, store, P, F);
+        PcParams<float> Q;
+        fill_pc<float>(ctx, sh, dt, P, Q);
+        ctx->stat_h2d = sizeof(Q) + sizeof(FinalParams);
+        HJM_CUDA(ctx, launch_path_pc(ctx->nt, Q, ext_dev, (double*)ctx->partials.p,
+                                     store ? (float*)ctx->estore.p : nullptr, s));
+    } else if (pc) {
+        PathParams<double> P;
+        fill_params<double>(ctx, sh, n_paths, dt, seed, path_offset, hazard, recovery, ld, store, P, F);
+        PcParams<double> Q;
+        fill_pc<double>(ctx, sh, dt, P, Q);
+        ctx->stat_h2d = sizeof(Q) + sizeof(FinalParams);
+        HJM_CUDA(ctx, launch_path_pc(ctx->nt, Q, ext_dev, (double*)ctx->partials.p,
+                                     store ? (double*)ctx->estore.p : nullptr, s));
+    } else if (mixed) {
         PathParams<float> P;
         fill_params<float>(ctx, sh, n_paths, dt, seed, path_offset, hazard, recovery, ld, store, P, F);
         MixedParams M;
@@ -597,6 +686,7 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
         r.seed = seed;
         r.path_offset = path_offset;
         r.external_normals = ext_dev != nullptr;
+        r.scheme = ctx->scheme;
     }
     ctx->last_n_paths = n_paths;
     ctx->last_n_dates = n_dates;
@@ -815,6 +905,8 @@ hjm_status hjm_run_adjoint(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, doubl
     RunShape sh;
     hjm_status st = check_run(ctx, n_paths, n_steps, dt, HJM_PRECISION_MIXED, hazard_rate, recovery, 0.0, sh);
     if (st != HJM_OK) return st;
+    if (ctx->scheme != HJM_SCHEME_EULER)
+        return fail(ctx, HJM_ERR_UNSUPPORTED, "the adjoint is built for the Euler scheme");
     if (checkpoint_every < 0 || checkpoint_every > sh.stride)
         return fail(ctx, HJM_ERR_UNSUPPORTED, "checkpoint_every %d: must be 0 (none) or in [1, %d] (the block length)",
                     checkpoint_every, sh.stride);
@@ -985,10 +1077,12 @@ hjm_status hjm_write_report(hjm_ctx* ctx, const char* path, int32_t format)
                      "  \"run\": {\"n_paths\": %lld, \"n_steps\": %d, \"dt\": %.17g, \"dtau\": %.17g, "
                      "\"n_tenor\": %d, \"sampled_dates\": %d, \"seed\": %llu, \"path_offset\": %llu, "
                      "\"precision\": \"%s\", \"vol_form\": \"%s\", \"hazard\": %.17g, \"recovery\": %.17g, "
-                     "\"pfe_quantile\": %.17g, \"checkpoint_every\": %d, \"external_normals\": %s},\n",
+                     "\"pfe_quantile\": %.17g, \"checkpoint_every\": %d, \"external_normals\": %s, "
+                     "\"scheme\": \"%s\"},\n",
                      (long long)r.n_paths, r.n_steps, r.dt, r.dtau, r.nt, r.n_dates - 1, (unsigned long long)r.seed,
                      (unsigned long long)r.path_offset, prec, kForms[r.vol_form], r.hazard, r.recovery,
-                     r.pfe ? r.pfe_q : 0.0, r.ckpt, r.external_normals ? "true" : "false");
+                     r.pfe ? r.pfe_q : 0.0, r.ckpt, r.external_normals ? "true" : "false",
+                     r.scheme == HJM_SCHEME_PREDICTOR_CORRECTOR ? "predictor_corrector" : "euler");
         std::fprintf(f, "  \"cva\": %.17g,\n  \"cva_stderr\": %.17g,\n  \"dcva_dhazard\": %.17g,\n", r.cva,
                      r.cva_stderr, r.dhazard);
         put_array(f, "dates", dates);
@@ -1005,9 +1099,11 @@ hjm_status hjm_write_report(hjm_ctx* ctx, const char* path, int32_t format)
     } else {
         std::fprintf(f, "# %s %s\n", hjm_version(), r.adjoint ? "adjoint" : "valuation");
         std::fprintf(f, "key,value\n");
-        std::fprintf(f, "n_paths,%lld\nn_steps,%d\ndt,%.17g\ndtau,%.17g\nseed,%llu\nprecision,%s\nvol_form,%s\n",
+        std::fprintf(f,
+                     "n_paths,%lld\nn_steps,%d\ndt,%.17g\ndtau,%.17g\nseed,%llu\nprecision,%s\nvol_form,%s\n"
+                     "scheme,%s\n",
                      (long long)r.n_paths, r.n_steps, r.dt, r.dtau, (unsigned long long)r.seed, prec,
-                     kForms[r.vol_form]);
+                     kForms[r.vol_form], r.scheme == HJM_SCHEME_PREDICTOR_CORRECTOR ? "predictor_corrector" : "euler");
         std::fprintf(f, "hazard,%.17g\nrecovery,%.17g\ncva,%.17g\ncva_stderr,%.17g\ndcva_dhazard,%.17g\n", r.hazard,
                      r.recovery, r.cva, r.cva_stderr, r.dhazard);
         if (r.adjoint) {

@@ -71,6 +71,23 @@ cudaError_t launch_widen_exposures(const void* in, bool fp64, int64_t ld, int64_
                                    cudaStream_t s);
 cudaError_t measure_fma_peak(bool fp64, cudaStream_t s, int n_sms, double* tflops);
 
+// Predictor-corrector kernel parameters: the path parameters (loadings
+// N sqrt(dt) sigma, the PC deterministic curve, growth scales with base =
+// 1 + r1 + r2) plus the stencil and the effective recovery coefficients.
+template <typename T>
+struct PcParams {
+    PathParams<T> P;
+    T r1, r2;              // a1 / a0, a2 / a0 (rounded once)
+    T a0e, a1e, a2e, ce;   // effective scheme: 1/base, r1/base, r2/base, (r1 + 2 r2)/base
+    T inv_1ma0, inv_ce;    // 1 / (1 - a0e), 1 / ce
+};
+cudaError_t launch_path_pc(int nt, const PcParams<double>& Q, const double* ext, double* partials, double* estore,
+                           cudaStream_t s);
+cudaError_t launch_path_pc(int nt, const PcParams<float>& Q, const double* ext, double* partials, float* estore,
+                           cudaStream_t s);
+size_t pc_smem(int nt, int n_blocks, bool mixed);
+int pc_cta();
+
 // Adjoint kernel parameters: the mixed-precision path parameters plus the
 // checkpoint layout.
 struct AdjParams {

@@ -210,6 +210,9 @@ hjm_status hjm_run_static(void* cuda_stream, int32_t n_tenor, double dtau, const
         return static_fail(HJM_ERR_INVALID_ARGUMENT, "dtau/dt = %.17g is not an integer number of steps", r);
     if (stride < 2)
         return static_fail(HJM_ERR_UNSUPPORTED, "dt must be at most dtau/2 (the kernels need c = dt/dtau < 1)");
+    if (precision == HJM_PRECISION_MIXED && (double)n_steps * std::log1p(1.0 / ((double)stride - 1.0)) > 80.0)
+        return static_fail(HJM_ERR_UNSUPPORTED,
+                           "mixed precision: the growth-scaled curve would exceed e^80; use FP64 or a smaller dt");
     if (n_steps <= 0 || n_steps % stride != 0)
         return static_fail(HJM_ERR_INVALID_ARGUMENT, "n_steps %d is not a positive multiple of %ld", n_steps, stride);
     const int B = n_steps / (int)stride;

@@ -88,6 +88,11 @@ class HJMEngine:
     def keep_exposures(self, keep: bool = True) -> None:
         self._check(self.lib.hjm_ctx_keep_exposures(self.ctx, 1 if keep else 0))
 
+    def set_scheme(self, scheme: str = "euler") -> None:
+        """Time scheme of the Musiela SDE: "euler" (the reference's) or
+        "predictor_corrector"."""
+        self._check(self.lib.hjm_ctx_set_scheme(self.ctx, {"euler": 0, "predictor_corrector": 1}[scheme]))
+
     def write_report(self, path, fmt: str = "json") -> None:
         """The last valuation (or adjoint run) with its inputs, as JSON or CSV."""
         code = {"json": 0, "csv": 1}[fmt]

@@ -81,6 +81,16 @@ hjm_status hjm_ctx_set_stream(hjm_ctx* ctx, void* cuda_stream);
  * hjm_get_exposures); they are always kept when a PFE is requested. */
 hjm_status hjm_ctx_keep_exposures(hjm_ctx* ctx, int32_t keep);
 
+/* Time scheme of the Musiela SDE.  HJM_SCHEME_EULER (default) is the
+ * reference's Euler step (simulation_cpu.h:37-54); HJM_SCHEME_PREDICTOR_CORRECTOR
+ * (the reference's doc/TODO:3) averages the drift term mu + dF/dtau at the
+ * curve and at its Euler prediction: f' = f + (a(f) + a(f*)) dt / 2 + xi.
+ * Valuations (both precisions, table volatility step) support both; the
+ * adjoint and hjm_run_static the Euler step only. */
+#define HJM_SCHEME_EULER 0
+#define HJM_SCHEME_PREDICTOR_CORRECTOR 1
+hjm_status hjm_ctx_set_scheme(hjm_ctx* ctx, int32_t scheme);
+
 /* Polynomial volatility decomposition.  When every volatility factor is a
  * polynomial of degree <= 2 in the tenor T (given by hjm_set_market_poly, or a
  * table that hjm_set_market finds to be one to 1e-12 of each row's scale, as

@@ -130,6 +130,11 @@ typedef struct {
      * D_i * (payA[i] * L_i - payB[i]), payA = sum of signed notional x accrual,
      * payB = the same times each swap's fixed rate; NULL = the single swap */
     const double *payA, *payB;
+    /* time scheme (new, not in the reference; its doc/TODO:3 lists it):
+     * 0 = the reference's Euler step, 1 = predictor-corrector (Heun) on the
+     * drift term a(f) = mu + dF/dtau: f* = Euler step, then
+     * f' = f + (a(f) + a(f*)) dt / 2 + sqrt(dt) sum_k sigma_k phi_k */
+    int scheme;
 } oracle_model;
 
 /* One path: simulation_cpu.h:188-262 called from the block loop at :413-436,
@@ -149,10 +154,23 @@ static void simulate_path(const oracle_model* M, const double* normals_path,
     for (int path = 0; path < M->n_steps; path += M->stride) {      /* :413 */
         for (int s = 0; s < M->stride; ++s) {                        /* :203 */
             const double* phi = normals_path + (size_t)(path + s) * 3; /* :205-207 */
+            double fs[ORACLE_MAX_TENOR];
+            if (path != 0 && M->scheme == 1)                         /* predictor: the Euler step */
+                for (int t = 0; t < nt; ++t)
+                    fs[t] = musiela_sde(M->drift[t], M->vol[t], M->vol[nt + t], M->vol[2 * nt + t],
+                                        phi[0], phi[1], phi[2], dfau(t, nt, f), f[t], M->dtau, M->dt);
             for (int t = 0; t < nt; ++t) {                           /* :210 */
                 double rate;
                 if (path == 0) {
                     rate = M->spot[t];                               /* :212-213 */
+                } else if (M->scheme == 1) {
+                    /* corrector: the average of the drift terms at f and f* */
+                    const double a0 = M->drift[t] + dfau(t, nt, f) / M->dtau;
+                    const double a1 = M->drift[t] + dfau(t, nt, fs) / M->dtau;
+                    double vol_sum = M->vol[t] * phi[0];
+                    vol_sum += M->vol[nt + t] * phi[1];
+                    vol_sum += M->vol[2 * nt + t] * phi[2];
+                    rate = f[t] + 0.5 * (a0 + a1) * M->dt + vol_sum * sqrt(M->dt);
                 } else {
                     double dF = dfau(t, nt, f);
                     rate = musiela_sde(M->drift[t], M->vol[t], M->vol[nt + t], M->vol[2 * nt + t],
@@ -200,6 +218,7 @@ static int model_init(oracle_model* M, int n_tenor, double dtau, double dt, int 
     M->spot = spot; M->vol = vol; M->drift = drift; M->accrual = accrual;
     M->notional = notional; M->strike = strike; M->sign = sign;
     M->payA = NULL; M->payB = NULL;
+    M->scheme = 0;
     return 0;
 }
 
@@ -213,6 +232,23 @@ int oracle_exposure_paths(int n_tenor, double dtau, double dt, int n_steps,
     oracle_model M;
     int rc = model_init(&M, n_tenor, dtau, dt, n_steps, spot, vol, drift, accrual, notional, strike, sign);
     if (rc) return rc;
+    double cf[ORACLE_MAX_TENOR];
+    for (int p = 0; p < n_paths; ++p)
+        simulate_path(&M, normals + (size_t)p * n_steps * 3, exposures + (size_t)p * n_tenor, cf);
+    return 0;
+}
+
+/* The same with a time scheme: 0 = Euler (the reference), 1 = predictor-corrector. */
+int oracle_exposure_paths_scheme(int scheme, int n_tenor, double dtau, double dt, int n_steps,
+                                 const double* spot, const double* vol, const double* drift,
+                                 const double* accrual, double notional, double strike, double sign,
+                                 int n_paths, const double* normals, double* exposures)
+{
+    oracle_model M;
+    int rc = model_init(&M, n_tenor, dtau, dt, n_steps, spot, vol, drift, accrual, notional, strike, sign);
+    if (rc) return rc;
+    if (scheme != 0 && scheme != 1) return -4;
+    M.scheme = scheme;
     double cf[ORACLE_MAX_TENOR];
     for (int p = 0; p < n_paths; ++p)
         simulate_path(&M, normals + (size_t)p * n_steps * 3, exposures + (size_t)p * n_tenor, cf);

@@ -44,6 +44,11 @@ def oracle() -> C.CDLL:
             C.c_int, C.c_double, C.c_double, C.c_int, _dp, _dp, _dp, _dp,
             C.c_double, C.c_double, C.c_double, C.c_int, _dp, _dp,
         ]
+        lib.oracle_exposure_paths_scheme.restype = C.c_int
+        lib.oracle_exposure_paths_scheme.argtypes = [
+            C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, _dp, _dp, _dp, _dp,
+            C.c_double, C.c_double, C.c_double, C.c_int, _dp, _dp,
+        ]
         lib.oracle_exposure_paths_netting.restype = C.c_int
         lib.oracle_exposure_paths_netting.argtypes = [
             C.c_int, C.c_double, C.c_double, C.c_int, _dp, _dp, _dp, _dp, _dp, C.c_int, _dp, _dp,
@@ -113,6 +118,20 @@ def exposure_paths(market, swap, n_steps: int, dt: float, normals: np.ndarray) -
     )
     if rc != 0:
         raise ValueError(f"oracle_exposure_paths rejected its arguments (rc={rc})")
+    return out
+
+
+def exposure_paths_pc(market, swap, n_steps: int, dt: float, normals: np.ndarray) -> np.ndarray:
+    """Per-path exposures under the predictor-corrector scheme."""
+    normals = np.ascontiguousarray(normals, dtype=np.float64)
+    n_paths = normals.shape[0]
+    out = np.zeros((n_paths, market.n_tenor), dtype=np.float64)
+    rc = oracle().oracle_exposure_paths_scheme(
+        1, market.n_tenor, market.dtau, dt, n_steps, market.spot, market.vol.ravel(), market.drift,
+        swap.accrual, swap.notional, swap.strike, swap.sign, n_paths, normals.ravel(), out.ravel(),
+    )
+    if rc != 0:
+        raise ValueError(f"oracle_exposure_paths_scheme rejected its arguments (rc={rc})")
     return out
 
 

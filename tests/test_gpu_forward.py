@@ -239,3 +239,28 @@ def test_fma_peaks_are_measured(engine):
     fp64 = engine.fma_peak_tflops("fp64")
     fp32 = engine.fma_peak_tflops("mixed")
     assert fp64 > 0.1 and fp32 > 10.0 and fp32 > fp64
+
+
+def test_coarsest_time_step(engine):
+    """dt = dtau/2 (c = 0.5, the largest the growth-scaled step takes): FP64
+    and mixed match the oracle; on 61 tenors with 60 dates the FP32 scaled
+    curve would grow by e^83, so mixed precision is refused while FP64 runs."""
+    mk, sw = Market(), Swap()
+    _setup(engine, mk, sw)
+    cfg = RunConfig(n_paths=2000, n_steps=40, dt=0.25, seed=5)
+    normals = engine.dump_normals(cfg.n_paths, cfg.n_steps, cfg.seed)
+    x, ee, cva, *_ = _oracle_all(mk, sw, cfg.n_steps, cfg.dt, normals, 21)
+    v = engine.run(cfg, "fp64")
+    _assert_rel(v.ee, ee, FP64_RTOL, "EE c=0.5")
+    m = engine.run(cfg, "mixed")
+    _assert_rel(m.ee[:20], ee[:20], MIXED_RTOL, "mixed EE c=0.5")
+
+    mk61, sw61 = Market(n_tenor=61), Swap(n_tenor=61, n_periods=60)
+    _setup(engine, mk61, sw61)
+    long = RunConfig(n_paths=500, n_steps=120, dt=0.25, seed=6)
+    with pytest.raises(_lib.HJMError) as ei:
+        engine.run(long, "mixed")
+    assert ei.value.status == 2
+    normals = engine.dump_normals(long.n_paths, long.n_steps, long.seed)
+    x, ee, *_ = _oracle_all(mk61, sw61, long.n_steps, long.dt, normals, 61)
+    _assert_rel(engine.run(long, "fp64").ee[:61], ee[:61], FP64_RTOL, "EE 61 tenors c=0.5")
