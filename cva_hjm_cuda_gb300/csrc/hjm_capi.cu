@@ -1047,6 +1047,112 @@ hjm_status hjm_run_adjoint(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, doubl
 }
 
 // ---------------------------------------------------------------------------
+// multi-level Monte Carlo
+// ---------------------------------------------------------------------------
+hjm_status hjm_run_mlmc(hjm_ctx* ctx, int32_t n_levels, const int64_t* n_paths, int32_t n_steps, double dt,
+                        uint64_t seed, double hazard_rate, double recovery, double* ee_out, double* cva_out,
+                        double* level_out)
+{
+    HJM_CHECK_CTX(ctx);
+    if (n_levels < 1 || n_levels > HJM_MLMC_MAX_LEVELS || !n_paths)
+        return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "n_levels must be in [1, %d] with n_paths per level",
+                    HJM_MLMC_MAX_LEVELS);
+    if (ctx->scheme != HJM_SCHEME_EULER)
+        return fail(ctx, HJM_ERR_UNSUPPORTED, "multi-level Monte Carlo is built for the Euler scheme");
+    for (int l = 0; l < n_levels; ++l)
+        if (n_paths[l] <= 0 || n_paths[l] > ((int64_t)1 << 31))
+            return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "level %d: n_paths %lld outside [1, 2^31]", l,
+                        (long long)n_paths[l]);
+    // validate every level's grid (dt / 2^l, n_steps 2^l) before launching anything
+    std::vector<RunShape> shapes(n_levels);
+    for (int l = 0; l < n_levels; ++l) {
+        hjm_status st = check_run(ctx, n_paths[l], n_steps << l, dt / (double)(1 << l), HJM_PRECISION_MIXED,
+                                  hazard_rate, recovery, 0.0, shapes[l]);
+        if (st != HJM_OK) return st;
+        if (l >= 1 && mlmc_smem(shapes[l].B) > 227 * 1024)
+            return fail(ctx, HJM_ERR_UNSUPPORTED, "level %d: shared memory exceeds 227 KB", l);
+    }
+    const int nt = ctx->nt;
+    std::vector<double> ee(nt, 0.0), lev(4 * (size_t)n_levels, 0.0);
+    double cva = 0.0, var = 0.0, dhaz = 0.0;
+    // level 0: the plain mixed-precision valuation on the coarsest grid
+    {
+        double e0[kMaxTenor], c0[HJM_CVA_OUT_LEN];
+        hjm_status st = enqueue_impl(ctx, n_paths[0], n_steps, dt, seed, 0, HJM_PRECISION_MIXED, hazard_rate,
+                                     recovery, 0.0, nullptr);
+        if (st != HJM_OK) return st;
+        st = hjm_fetch_results(ctx, e0, nullptr, c0);
+        if (st != HJM_OK) return st;
+        float ms = 0.f;
+        HJM_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[2]));
+        for (int j = 0; j < nt; ++j) ee[j] += e0[j];
+        cva += c0[HJM_CVA_VALUE];
+        var += c0[HJM_CVA_STDERR] * c0[HJM_CVA_STDERR];
+        dhaz += c0[HJM_CVA_DHAZARD];
+        lev[0] = c0[HJM_CVA_VALUE];
+        lev[1] = c0[HJM_CVA_STDERR];
+        lev[2] = ms;
+        lev[3] = (double)n_paths[0];
+    }
+    // levels >= 1: the coupled kernel; normals of level l from path index + l 2^40
+    cudaStream_t s = ctx->stream;
+    for (int l = 1; l < n_levels; ++l) {
+        const RunShape& shf = shapes[l];
+        const RunShape& shc = shapes[l - 1];
+        const double dtf = dt / (double)(1 << l), dtc = dt / (double)(1 << (l - 1));
+        const uint64_t offset = (uint64_t)l << 40;
+        const int R = shf.B + 3;
+        const int64_t n_ctas = (n_paths[l] + mlmc_cta() - 1) / mlmc_cta();
+        HJM_CUDA(ctx, ctx->partials.ensure(sizeof(double) * (size_t)n_ctas * R));
+        HJM_CUDA(ctx, ctx->sums.ensure(sizeof(double) * kMaxTenor * 4));
+        HJM_CUDA(ctx, ctx->result.ensure(sizeof(double) * kResLen));
+        MlmcParams Q;
+        FinalParams F, Fc;
+        {
+            PathParams<float> P;
+            fill_params<float>(ctx, shf, n_paths[l], dtf, seed, offset, hazard_rate, recovery, 0, false, P, F);
+            pack_mixed_params(nt, P, Q.fine);
+            fill_params<float>(ctx, shc, n_paths[l], dtc, seed, offset, hazard_rate, recovery, 0, false, P, Fc);
+            pack_mixed_params(nt, P, Q.coarse);
+        }
+        ctx->ev = ctx->ring[ctx->n_enqueued % hjm_ctx::kRing];
+        ctx->n_enqueued++;
+        HJM_CUDA(ctx, cudaMemsetAsync(ctx->result.p, 0, sizeof(double) * kResLen, s));
+        HJM_CUDA(ctx, cudaEventRecord(ctx->ev[0], s));
+        HJM_CUDA(ctx, launch_mlmc_level(nt, Q, use_poly_path(ctx), (double*)ctx->partials.p, s));
+        HJM_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
+        HJM_CUDA(ctx, launch_reduce((const double*)ctx->partials.p, n_ctas, R, (double*)ctx->sums.p, F,
+                                    (double*)ctx->result.p, s));
+        HJM_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
+        HJM_CUDA(ctx, cudaEventRecord(ctx->ev[3], s));
+        double res[kResLen];
+        HJM_CUDA(ctx, cudaMemcpyAsync(res, ctx->result.p, sizeof(res), cudaMemcpyDeviceToHost, s));
+        HJM_CUDA(ctx, cudaStreamSynchronize(s));
+        float ms = 0.f;
+        HJM_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[2]));
+        for (int j = 0; j < nt; ++j) ee[j] += res[kResEE + j];
+        cva += res[kResCVA];
+        var += res[kResCVAStderr] * res[kResCVAStderr];
+        dhaz += res[kResDCVADHazard];
+        lev[4 * l + 0] = res[kResCVA];
+        lev[4 * l + 1] = res[kResCVAStderr];
+        lev[4 * l + 2] = ms;
+        lev[4 * l + 3] = (double)n_paths[l];
+    }
+    ctx->have_result = false;  // the result buffers hold the last level, not a valuation
+    if (ee_out)
+        for (int j = 0; j < nt; ++j) ee_out[j] = ee[j];
+    if (cva_out) {
+        cva_out[HJM_CVA_VALUE] = cva;
+        cva_out[HJM_CVA_STDERR] = std::sqrt(var);
+        cva_out[HJM_CVA_DHAZARD] = dhaz;
+    }
+    if (level_out)
+        for (size_t q = 0; q < lev.size(); ++q) level_out[q] = lev[q];
+    return HJM_OK;
+}
+
+// ---------------------------------------------------------------------------
 // report
 // ---------------------------------------------------------------------------
 static void put_array(FILE* f, const char* name, const std::vector<double>& v, bool comma = true)

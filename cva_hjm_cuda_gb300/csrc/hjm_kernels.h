@@ -88,6 +88,16 @@ cudaError_t launch_path_pc(int nt, const PcParams<float>& Q, const double* ext, 
 size_t pc_smem(int nt, int n_blocks, bool mixed);
 int pc_cta();
 
+// Multi-level Monte Carlo: the coupled level kernel's two parameter blocks
+// (the fine grid, and the coarse grid with half the steps per block).
+struct MlmcParams {
+    MixedParams fine;
+    MixedParams coarse;
+};
+cudaError_t launch_mlmc_level(int nt, const MlmcParams& Q, bool poly, double* partials, cudaStream_t s);
+size_t mlmc_smem(int n_blocks);
+int mlmc_cta();
+
 // Adjoint kernel parameters: the mixed-precision path parameters plus the
 // checkpoint layout.
 struct AdjParams {

@@ -88,6 +88,21 @@ class HJMEngine:
     def keep_exposures(self, keep: bool = True) -> None:
         self._check(self.lib.hjm_ctx_keep_exposures(self.ctx, 1 if keep else 0))
 
+    def run_mlmc(self, n_paths_per_level, n_steps: int = 1000, dt: float = 0.01, seed: int = 1234,
+                 hazard: float = 0.02, recovery: float = 0.4) -> dict:
+        """Multi-level Monte Carlo EE / CVA: level l uses dt / 2^l on
+        n_paths_per_level[l] paths (hjm_run_mlmc).  Returns the summed EE, CVA
+        and standard error, and per level the CVA difference, its standard
+        error, the device ms and the path count."""
+        n = np.ascontiguousarray(n_paths_per_level, dtype=np.int64)
+        nt = self.n_tenor
+        ee, cva, lev = np.zeros(nt), np.zeros(3), np.zeros(4 * n.size)
+        self._check(self.lib.hjm_run_mlmc(self.ctx, n.size, n.ctypes.data_as(C.POINTER(C.c_int64)), n_steps, dt,
+                                          seed, hazard, recovery, _dptr(ee), _dptr(cva), _dptr(lev)))
+        lev = lev.reshape(n.size, 4)
+        return {"ee": ee, "cva": cva[0], "cva_stderr": cva[1], "dcva_dhazard": cva[2],
+                "levels": [{"cva_diff": r[0], "stderr": r[1], "ms": r[2], "n_paths": int(r[3])} for r in lev]}
+
     def set_scheme(self, scheme: str = "euler") -> None:
         """Time scheme of the Musiela SDE: "euler" (the reference's) or
         "predictor_corrector"."""
@@ -243,6 +258,18 @@ class Calibration:
         if poly:
             return Market(n_tenor=spot.size, dtau=dtau, spot=spot, vol_coeffs=self.vol_coeffs.copy())
         return Market(n_tenor=spot.size, dtau=dtau, spot=spot, vol=self.vol.copy())
+
+
+def mlmc_allocation(level_var, level_cost, target_stderr: float) -> np.ndarray:
+    """Paths per level minimising the cost for a target standard error
+    (Giles 2008): N_l = ceil(sqrt(V_l / C_l) * sum_k sqrt(V_k C_k) / eps^2),
+    with V_l the per-path variance and C_l the per-path cost of level l."""
+    v = np.asarray(level_var, dtype=np.float64)
+    c = np.asarray(level_cost, dtype=np.float64)
+    if np.any(v < 0) or np.any(c <= 0) or target_stderr <= 0:
+        raise ValueError("variances >= 0, costs > 0 and a positive target are required")
+    n = np.sqrt(v / c) * np.sum(np.sqrt(v * c)) / target_stderr**2
+    return np.maximum(np.ceil(n), 1).astype(np.int64)
 
 
 def calibrate_pca(curves, dtau: float = 0.5, obs_per_year: float = 252.0) -> Calibration:

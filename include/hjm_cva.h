@@ -162,6 +162,22 @@ hjm_status hjm_run_with_normals(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, 
  * matrix of simulation_gpu.cu:1003 / simulation_cpu.h:362, transposed). */
 hjm_status hjm_get_exposures(hjm_ctx* ctx, double* out_host, int64_t capacity);
 
+/* ---- multi-level Monte Carlo --------------------------------------------------- */
+/* EE and CVA by multi-level Monte Carlo (the reference's doc/TODO:15): level l
+ * runs the Euler scheme with dt / 2^l and n_steps 2^l; level 0 is the plain
+ * mixed-precision valuation on n_paths[0] paths, level l >= 1 estimates
+ * E[P_l - P_{l-1}] on n_paths[l] paths whose fine and coarse curves share the
+ * Brownian increments (coarse normal = (phi_a + phi_b) / sqrt 2).  The outputs
+ * sum the levels: ee_out [n_tenor], cva_out [HJM_CVA_OUT_LEN] (the standard
+ * error combines the levels' independent errors); level_out [n_levels][4] =
+ * {CVA difference of the level, its standard error, device ms, paths}, the
+ * inputs of the usual path allocation N_l ~ sqrt(V_l / C_l).  Mixed
+ * precision, Euler scheme; normals of level l come from path index + l 2^40. */
+#define HJM_MLMC_MAX_LEVELS 6
+hjm_status hjm_run_mlmc(hjm_ctx* ctx, int32_t n_levels, const int64_t* n_paths, int32_t n_steps, double dt,
+                        uint64_t seed, double hazard_rate, double recovery, double* ee_out, double* cva_out,
+                        double* level_out);
+
 /* ---- report ----------------------------------------------------------------- */
 /* The results of the last valuation fetched (hjm_run, hjm_fetch_results,
  * hjm_run_with_normals) or of the last hjm_run_adjoint, with the run's inputs,
