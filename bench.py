@@ -349,6 +349,7 @@ def run_ours(args) -> None:
     if not args.no_extras and prec == "fp64":
         extras["generic_table_step"] = generic_step_run(eng, mk, sw, args, flush, stride, peak64, peak32)
         extras["predictor_corrector"] = predictor_corrector_run(eng, mk, sw, args, flush)
+        extras["mlmc"] = mlmc_run(eng, mk, sw)
         extras["mixed"] = mixed_vs_fp64(eng, mk, sw, args, stream, flush, value)
         extras["adjoint"] = adjoint_cost(eng, args, flush)
         extras["netting"] = netting_set_run(eng, args, flush)
@@ -514,6 +515,38 @@ def predictor_corrector_run(eng, mk, sw, args, flush) -> dict:
     finally:
         eng.set_scheme("euler")
     return out
+
+
+def mlmc_run(eng, mk, sw) -> dict:
+    """Multi-level Monte Carlo against a plain valuation on the finest grid
+    (dt = 0.00625, 1,600 steps for the 10y swap; levels dt = 0.1 / 2^l, l =
+    0..4), both in mixed precision at the same CVA standard error: a pilot
+    run gives each level's per-path variance and cost, the Giles allocation
+    the paths per level."""
+    import numpy as np
+
+    from cva_hjm_cuda_gb300 import RunConfig
+    from cva_hjm_cuda_gb300.engine import mlmc_allocation
+
+    eng.set_market(mk)
+    eng.set_swap(sw)
+    n_plain = WORKLOADS["fp64"]["n_paths"]
+    fine = RunConfig(n_paths=n_plain, n_steps=1600, dt=0.00625, seed=SEED)
+    eng.run(fine, "mixed", pfe=False)  # warm-up
+    plain = eng.run(fine, "mixed", pfe=False)
+    plain_ms = float(eng.timing_history(1)[0, 3])
+    levels = 5
+    pilot = eng.run_mlmc([65536] * levels, n_steps=100, dt=0.1, seed=SEED + 1)
+    var = [lv["stderr"] ** 2 * lv["n_paths"] for lv in pilot["levels"]]
+    cost = [lv["ms"] / lv["n_paths"] for lv in pilot["levels"]]
+    n = mlmc_allocation(var, cost, plain.cva_stderr)
+    m = eng.run_mlmc(list(n), n_steps=100, dt=0.1, seed=SEED + 2)
+    ms = sum(lv["ms"] for lv in m["levels"])
+    return {"finest_dt": 0.00625, "levels": levels, "plain_paths": n_plain, "plain_ms": plain_ms,
+            "plain_cva": plain.cva, "plain_stderr": plain.cva_stderr, "mlmc_paths_per_level": [int(x) for x in n],
+            "mlmc_ms": ms, "mlmc_cva": m["cva"], "mlmc_stderr": m["cva_stderr"],
+            "speedup_at_equal_stderr": plain_ms / ms,
+            "level_var_per_path": [float(v) for v in var], "level_cost_ms_per_path": [float(c) for c in cost]}
 
 
 def adjoint_cost(eng, args, flush) -> dict:

@@ -260,16 +260,17 @@ class Calibration:
         return Market(n_tenor=spot.size, dtau=dtau, spot=spot, vol=self.vol.copy())
 
 
-def mlmc_allocation(level_var, level_cost, target_stderr: float) -> np.ndarray:
+def mlmc_allocation(level_var, level_cost, target_stderr: float, min_paths: int = 1024) -> np.ndarray:
     """Paths per level minimising the cost for a target standard error
     (Giles 2008): N_l = ceil(sqrt(V_l / C_l) * sum_k sqrt(V_k C_k) / eps^2),
-    with V_l the per-path variance and C_l the per-path cost of level l."""
+    with V_l the per-path variance and C_l the per-path cost of level l; at
+    least min_paths per level so that every level's variance is estimated."""
     v = np.asarray(level_var, dtype=np.float64)
     c = np.asarray(level_cost, dtype=np.float64)
     if np.any(v < 0) or np.any(c <= 0) or target_stderr <= 0:
         raise ValueError("variances >= 0, costs > 0 and a positive target are required")
     n = np.sqrt(v / c) * np.sum(np.sqrt(v * c)) / target_stderr**2
-    return np.maximum(np.ceil(n), 1).astype(np.int64)
+    return np.maximum(np.ceil(n), min_paths).astype(np.int64)
 
 
 def calibrate_pca(curves, dtau: float = 0.5, obs_per_year: float = 252.0) -> Calibration:

@@ -68,8 +68,9 @@ def test_estimator_matches_finest_grid_and_reduces_variance(engine):
 
 
 def test_allocation_and_errors(engine):
-    n = mlmc_allocation([1.0, 0.01, 0.0025], [1.0, 3.0, 6.0], 0.01)
+    n = mlmc_allocation([1.0, 0.01, 0.0025], [1.0, 3.0, 6.0], 0.01, min_paths=1)
     assert n[0] > n[1] > n[2] >= 1
+    assert np.all(mlmc_allocation([1.0, 1e-9], [1.0, 3.0], 0.01) >= 1024)
     # cost-weighted optimum: the estimator variance meets the target
     assert np.sum(np.array([1.0, 0.01, 0.0025]) / n) <= 0.01**2 * 1.0001
     engine.set_market(Market())
