@@ -71,10 +71,11 @@ def algorithmic_flops_per_path(n_tenor: int, n_steps: int, stride: int, form: st
     Euler step of block b:
     ``poly_tri`` (factor k a polynomial of degree <= k in T, the reference's
     own volatility table): the growth-scaled convection of the remainder
-    (L - 1 - b FMAs, 2 FMAs + 1 ADD at the last tenor), the noise projection
-    onto the three scalar parts (3 MUL + 3 FMA), their update (3 FMA + 3 ADD),
-    the scaled last-tenor source (2 MUL) and the block sums (3 ADD + 1 FMA):
-    2 (NT - b) + 26 flops.  ``poly`` (general quadratic factors): 6 more.
+    (L - 1 - b FMAs, 3 FMAs at the last tenor with its source), the scaled
+    source coefficient (1 MUL), the updates of the three scalar parts with the
+    noise projection folded in (9 FMA), the block sums (3 ADD) and the anchor
+    (1 FMA): 2 (NT - b) + 26 flops.  ``poly`` (general quadratic factors): 3
+    more FMAs, 2 (NT - b) + 32.
     ``table`` (generic volatility table): 4 FMAs per live tenor (three factor
     loadings and the convection; 5 at the last tenor), the normals' scaling
     (4 MUL), the block sums (3 ADD + 1 FMA): 8 (NT - b) + 3.

@@ -146,34 +146,33 @@ __global__ void __launch_bounds__(kFp64Cta, 4)
             // in place, ascending (h[t+1] is still the old value); the last
             // tenor, which reads h[L-1], first
             if constexpr (POLY) {
-                double al, be, ga;
-                if constexpr (TRI) {
-                    al = fma(P.svc[2][0], phi2, fma(P.svc[1][0], phi1, P.svc[0][0] * phi0));
-                    be = fma(P.svc[2][1], phi2, P.svc[1][1] * phi1);
-                    ga = P.svc[2][2] * phi2;
-                } else {
-                    al = fma(P.svc[2][0], phi2, fma(P.svc[1][0], phi1, P.svc[0][0] * phi0));
-                    be = fma(P.svc[2][1], phi2, fma(P.svc[1][1], phi1, P.svc[0][1] * phi0));
-                    ga = fma(P.svc[2][2], phi2, fma(P.svc[1][2], phi1, P.svc[0][2] * phi0));
-                }
+                // the noise projection folded into the updates of S, U, W:
+                // S' = S + c dtau U + c dtau^2 W + sum_k svc[k][0] phi_k, etc.
+                // (old U, W on the right; factor k of degree <= k drops 3 terms)
                 mig *= P.ip;
-                const double src = mig * W;  // -2 c dtau^2 W, scaled
-                const double hl = fma(rr, fma(2.0, h[L], -h[L - 1]), h[L]) + src;
+                const double hl = fma(mig, W, fma(rr, fma(2.0, h[L], -h[L - 1]), h[L]));  // + scaled source
 #pragma unroll
-                for (int g = 0; g < kGroups; ++g) {
-                    if (kGroup * g + kGroup > live) {  // uniform: skip groups of dead tenors
+                for (int gi = 0; gi < kGroups; ++gi) {
+                    if (kGroup * gi + kGroup > live) {  // uniform: skip groups of dead tenors
 #pragma unroll
                         for (int j = 0; j < kGroup; ++j) {
-                            const int t = kGroup * g + j;
+                            const int t = kGroup * gi + j;
                             if (t < L) h[t] = fma(rr, h[t + 1], h[t]);
                         }
                     }
                 }
                 h[L] = hl;
-                const double Sn = fma(P.k2, W, fma(P.k1, U, S)) + al;
-                U = fma(2.0 * P.k1, W, U) + be;
-                W += ga;
+                double Sn = fma(P.svc[0][0], phi0, fma(P.k2, W, fma(P.k1, U, S)));
+                Sn = fma(P.svc[2][0], phi2, fma(P.svc[1][0], phi1, Sn));
+                double Un = fma(P.svc[2][1], phi2, fma(P.svc[1][1], phi1, fma(2.0 * P.k1, W, U)));
+                double Wn = fma(P.svc[2][2], phi2, W);
+                if constexpr (!TRI) {
+                    Un = fma(P.svc[0][1], phi0, Un);
+                    Wn = fma(P.svc[1][2], phi1, fma(P.svc[0][2], phi0, Wn));
+                }
                 S = Sn;
+                U = Un;
+                W = Wn;
                 sS += S;
                 sU += U;
                 sW += W;
@@ -185,11 +184,11 @@ __global__ void __launch_bounds__(kFp64Cta, 4)
                 xl = fma(P.sv[2][L], p2, xl);
                 const double hl = fma(rr, fma(2.0, h[L], -h[L - 1]), xl);
 #pragma unroll
-                for (int g = 0; g < kGroups; ++g) {
-                    if (kGroup * g + kGroup > live) {
+                for (int gi = 0; gi < kGroups; ++gi) {
+                    if (kGroup * gi + kGroup > live) {
 #pragma unroll
                         for (int j = 0; j < kGroup; ++j) {
-                            const int t = kGroup * g + j;
+                            const int t = kGroup * gi + j;
                             if (t < L) {
                                 double x = fma(P.sv[0][t], p0, h[t]);
                                 x = fma(P.sv[1][t], p1, x);

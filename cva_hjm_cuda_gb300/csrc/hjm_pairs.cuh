@@ -146,7 +146,8 @@ struct MixedPath {
     static constexpr int H = PairGrid<NT>::H;
     float2 h[H];  // v = h / g (POLY: the convected remainder hc, scaled alike)
     float S, U, W;
-    float g, ig;  // (1 + rr)^-n' and its inverse, n' = steps evolved so far
+    float g;      // (1 + rr)^-n', n' = steps evolved so far
+    float ig;     // (1 + rr)^n' (POLY: times -2 c dtau^2, the source per unit W)
 
     __device__ __forceinline__ void reset()
     {
@@ -159,20 +160,22 @@ struct MixedPath {
     __device__ __forceinline__ void begin_block(const PathParams<float>& P, int b)
     {
         g = P.gblk[b];
-        ig = P.igblk[b];
+        ig = POLY ? P.m2k2 * P.igblk[b] : P.igblk[b];
     }
     __device__ __forceinline__ void step(const MixedParams& M, float phi0, float phi1, float phi2)
     {
         ig *= M.P.ip;
         if constexpr (POLY) {
-            const float al = fmaf(M.svcf[2][0], phi2, fmaf(M.svcf[1][0], phi1, M.svcf[0][0] * phi0));
-            const float be = fmaf(M.svcf[2][1], phi2, fmaf(M.svcf[1][1], phi1, M.svcf[0][1] * phi0));
-            const float ga = fmaf(M.svcf[2][2], phi2, fmaf(M.svcf[1][2], phi1, M.svcf[0][2] * phi0));
-            convect_pairs<NT>(h, M, (M.P.m2k2 * W) * ig);
-            const float Sn = fmaf(M.k2f, W, fmaf(M.k1f, U, S)) + al;
-            U = fmaf(2.0f * M.k1f, W, U) + be;
-            W += ga;
+            convect_pairs<NT>(h, M, ig * W);
+            // the noise projection folded into the updates (old U, W on the right)
+            float Sn = fmaf(M.svcf[0][0], phi0, fmaf(M.k2f, W, fmaf(M.k1f, U, S)));
+            Sn = fmaf(M.svcf[2][0], phi2, fmaf(M.svcf[1][0], phi1, Sn));
+            float Un = fmaf(M.svcf[1][1], phi1, fmaf(M.svcf[0][1], phi0, fmaf(2.0f * M.k1f, W, U)));
+            Un = fmaf(M.svcf[2][1], phi2, Un);
+            const float Wn = fmaf(M.svcf[2][2], phi2, fmaf(M.svcf[1][2], phi1, fmaf(M.svcf[0][2], phi0, W)));
             S = Sn;
+            U = Un;
+            W = Wn;
         } else {
             euler_step_pairs<NT>(h, M, phi0 * ig, phi1 * ig, phi2 * ig);
         }
