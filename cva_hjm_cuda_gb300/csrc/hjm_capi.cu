@@ -107,6 +107,7 @@ struct hjm_ctx {
         double dt = 0, dtau = 0, hazard = 0, recovery = 0, pfe_q = 0;
         uint64_t seed = 0, path_offset = 0;
         std::vector<double> ee, pfe_v, dspot, ddrift;
+        std::vector<double> levels;  // multi-level MC: [level][4] as hjm_run_mlmc's level_out
         double dcoef[HJM_N_VOL_COEF] = {0};
         bool have_dcoef = false;
         double cva = 0, cva_stderr = 0, dhazard = 0;
@@ -1140,6 +1141,30 @@ hjm_status hjm_run_mlmc(hjm_ctx* ctx, int32_t n_levels, const int64_t* n_paths, 
         lev[4 * l + 3] = (double)n_paths[l];
     }
     ctx->have_result = false;  // the result buffers hold the last level, not a valuation
+    {
+        // the report describes the estimate: the finest grid, all levels' paths
+        hjm_ctx::Report& r = ctx->rep;
+        r = hjm_ctx::Report();
+        r.valid = true;
+        int64_t total = 0;
+        for (int l = 0; l < n_levels; ++l) total += n_paths[l];
+        r.n_paths = total;
+        r.n_steps = n_steps << (n_levels - 1);
+        r.dt = dt / (double)(1 << (n_levels - 1));
+        r.n_dates = shapes[0].B + 1;
+        r.nt = nt;
+        r.precision = HJM_PRECISION_MIXED;
+        r.vol_form = vol_form_code(ctx);
+        r.dtau = ctx->dtau;
+        r.hazard = hazard_rate;
+        r.recovery = recovery;
+        r.seed = seed;
+        r.ee = ee;
+        r.cva = cva;
+        r.cva_stderr = std::sqrt(var);
+        r.dhazard = dhaz;
+        r.levels = lev;
+    }
     if (ee_out)
         for (int j = 0; j < nt; ++j) ee_out[j] = ee[j];
     if (cva_out) {
@@ -1178,7 +1203,15 @@ hjm_status hjm_write_report(hjm_ctx* ctx, const char* path, int32_t format)
     const char* prec = r.precision == HJM_PRECISION_FP64 ? "fp64" : "mixed";
     if (format == HJM_REPORT_JSON) {
         std::fprintf(f, "{\n  \"engine\": \"%s\",\n", hjm_version());
-        std::fprintf(f, "  \"kind\": \"%s\",\n", r.adjoint ? "adjoint" : "valuation");
+        std::fprintf(f, "  \"kind\": \"%s\",\n", r.adjoint ? "adjoint" : r.levels.empty() ? "valuation" : "mlmc");
+        if (!r.levels.empty()) {
+            std::fprintf(f, "  \"levels\": [");
+            for (size_t l = 0; l < r.levels.size() / 4; ++l)
+                std::fprintf(f, "%s{\"cva_diff\": %.17g, \"stderr\": %.17g, \"ms\": %.17g, \"n_paths\": %.0f}",
+                             l ? ", " : "", r.levels[4 * l], r.levels[4 * l + 1], r.levels[4 * l + 2],
+                             r.levels[4 * l + 3]);
+            std::fprintf(f, "],\n");
+        }
         std::fprintf(f,
                      "  \"run\": {\"n_paths\": %lld, \"n_steps\": %d, \"dt\": %.17g, \"dtau\": %.17g, "
                      "\"n_tenor\": %d, \"sampled_dates\": %d, \"seed\": %llu, \"path_offset\": %llu, "
@@ -1203,7 +1236,11 @@ hjm_status hjm_write_report(hjm_ctx* ctx, const char* path, int32_t format)
         }
         std::fprintf(f, "}\n");
     } else {
-        std::fprintf(f, "# %s %s\n", hjm_version(), r.adjoint ? "adjoint" : "valuation");
+        std::fprintf(f, "# %s %s\n", hjm_version(),
+                     r.adjoint ? "adjoint" : r.levels.empty() ? "valuation" : "mlmc");
+        for (size_t l = 0; l < r.levels.size() / 4; ++l)
+            std::fprintf(f, "# level %zu: cva_diff %.17g stderr %.17g ms %.17g n_paths %.0f\n", l, r.levels[4 * l],
+                         r.levels[4 * l + 1], r.levels[4 * l + 2], r.levels[4 * l + 3]);
         std::fprintf(f, "key,value\n");
         std::fprintf(f,
                      "n_paths,%lld\nn_steps,%d\ndt,%.17g\ndtau,%.17g\nseed,%llu\nprecision,%s\nvol_form,%s\n"

@@ -180,7 +180,8 @@ hjm_status hjm_run_mlmc(hjm_ctx* ctx, int32_t n_levels, const int64_t* n_paths, 
 
 /* ---- report ----------------------------------------------------------------- */
 /* The results of the last valuation fetched (hjm_run, hjm_fetch_results,
- * hjm_run_with_normals) or of the last hjm_run_adjoint, with the run's inputs,
+ * hjm_run_with_normals), of the last hjm_run_adjoint or of the last
+ * hjm_run_mlmc (kind "mlmc", with its levels), with the run's inputs,
  * written to a file: JSON (one object: run, cva, cva_stderr, dcva_dhazard,
  * dates, ee and pfe, or the sensitivities) or CSV (key,value lines, then one
  * row per tenor).  Numbers round-trip (17 significant digits).  The reference

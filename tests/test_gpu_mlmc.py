@@ -81,3 +81,16 @@ def test_allocation_and_errors(engine):
         engine.run_mlmc([100, 0], n_steps=500, dt=0.02)
     with pytest.raises(_lib.HJMError):  # dt / 2^l must keep an integer number of steps per block
         engine.run_mlmc([100, 100], n_steps=40, dt=0.25 * 1.5)
+
+
+def test_mlmc_report(engine, tmp_path):
+    import json
+
+    engine.set_market(Market())
+    engine.set_swap(Swap())
+    m = engine.run_mlmc([8192, 2048], n_steps=500, dt=0.02, seed=3)
+    engine.write_report(tmp_path / "m.json")
+    r = json.loads((tmp_path / "m.json").read_text())
+    assert r["kind"] == "mlmc" and len(r["levels"]) == 2
+    assert r["cva"] == m["cva"] and r["run"]["n_steps"] == 1000 and r["run"]["n_paths"] == 8192 + 2048
+    np.testing.assert_array_equal(r["ee"], m["ee"])
