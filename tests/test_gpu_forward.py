@@ -264,3 +264,34 @@ def test_coarsest_time_step(engine):
     normals = engine.dump_normals(long.n_paths, long.n_steps, long.seed)
     x, ee, *_ = _oracle_all(mk61, sw61, long.n_steps, long.dt, normals, 61)
     _assert_rel(engine.run(long, "fp64").ee[:61], ee[:61], FP64_RTOL, "EE 61 tenors c=0.5")
+
+
+@pytest.mark.parametrize("n_steps", [50, 100])
+def test_one_and_two_dates_every_mode(engine, n_steps):
+    """The shortest runs: one block (date 1 only, no evolution) and two
+    blocks, through FP64, mixed, predictor-corrector, the adjoint and the
+    multi-level estimator."""
+    from cva_hjm_cuda_gb300.market import DEFAULT_VOL_COEFFS
+
+    mk, sw = Market(), Swap(n_periods=2)
+    _setup(engine, mk, sw)
+    cfg = RunConfig(n_paths=777, n_steps=n_steps, dt=0.01, seed=2)
+    normals = engine.dump_normals(cfg.n_paths, cfg.n_steps, cfg.seed)
+    n_dates = n_steps // 50 + 1
+    x, ee, cva, *_ = _oracle_all(mk, sw, cfg.n_steps, cfg.dt, normals, n_dates)
+    _assert_rel(engine.run(cfg, "fp64").ee[:n_dates], ee[:n_dates], FP64_RTOL, "fp64")
+    _assert_rel(engine.run(cfg, "mixed").ee[:n_dates], ee[:n_dates], MIXED_RTOL, "mixed")
+    engine.set_scheme("predictor_corrector")
+    try:
+        xp = O.exposure_paths_pc(mk, sw, cfg.n_steps, cfg.dt, normals)
+        _assert_rel(engine.run(cfg, "fp64").ee[:n_dates], O.expected_exposure(xp)[:n_dates], FP64_RTOL, "pc")
+    finally:
+        engine.set_scheme("euler")
+    engine.set_market_poly(51, 0.5, mk.spot, DEFAULT_VOL_COEFFS)
+    engine.set_swap(sw)
+    v = engine.run(cfg, "mixed", pfe=False)
+    for k in (0, 32):
+        s = engine.run_adjoint(cfg, checkpoint_every=k)
+        assert s.cva == v.cva and np.all(np.isfinite(s.dcva_dspot))
+    m = engine.run_mlmc([777, 512], n_steps=n_steps // 2, dt=0.02, seed=2)
+    assert np.isfinite(m["cva"]) and m["levels"][1]["n_paths"] == 512
