@@ -80,6 +80,23 @@ __host__ __device__ __forceinline__ uint4 normals_counter(uint64_t path, uint32_
 // finite).  The normals are inputs of both precision modes (the FP64 mode
 // promotes them exactly), and the oracle consumes these very values through
 // hjm_dump_normals.
+// The SFU's approximate log2 and reciprocal square root with subnormals
+// flushed: the operands here are never subnormal (1 - a >= 2^-24, t >= 1e-30),
+// so the results equal those of the non-flushing forms without their
+// subnormal checks.
+__device__ __forceinline__ float lg2_ftz(float x)
+{
+    float y;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rsqrt_ftz(float x)
+{
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 __device__ __forceinline__ void normals3(uint4 w, float& z0, float& z1, float& z2)
 {
     const float u0 = (float)(w.x >> 8), u1 = (float)(w.y >> 8);
@@ -87,10 +104,10 @@ __device__ __forceinline__ void normals3(uint4 w, float& z0, float& z1, float& z
     const float kM2Ln2 = -1.38629436111989061883f;          // -2 ln 2
     const float kAng = 3.74507028e-07f;                      // 2 pi 2^-24
     const float kPi = 3.14159265358979323846f;
-    const float t0 = kM2Ln2 * __log2f(fmaf(-0x1p-24f, u0, 1.0f));
-    const float t1 = kM2Ln2 * __log2f(fmaf(-0x1p-24f, u2, 1.0f));
-    const float r0 = t0 * rsqrtf(fmaxf(t0, 1e-30f));
-    const float r1 = t1 * rsqrtf(fmaxf(t1, 1e-30f));
+    const float t0 = kM2Ln2 * lg2_ftz(fmaf(-0x1p-24f, u0, 1.0f));
+    const float t1 = kM2Ln2 * lg2_ftz(fmaf(-0x1p-24f, u2, 1.0f));
+    const float r0 = t0 * rsqrt_ftz(fmaxf(t0, 1e-30f));
+    const float r1 = t1 * rsqrt_ftz(fmaxf(t1, 1e-30f));
     float s0, c0;
     __sincosf(fmaf(kAng, u1, -kPi), &s0, &c0);
     const float c1 = __cosf(fmaf(kAng, u3, -kPi));
