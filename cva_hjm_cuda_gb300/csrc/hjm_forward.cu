@@ -352,6 +352,7 @@ __global__ void __launch_bounds__(kCta, 4)
         BlockSums bs;
         bs.reset();
         x.begin_block(P, b);
+#pragma unroll(POLY ? 2 : 1)  // ping-pong the normals drawn ahead instead of copying them
         for (int s = 0; s < P.stride; ++s) {
             const int n = b * P.stride + s;
             const float phi0 = q0, phi1 = q1, phi2 = q2;
