@@ -34,15 +34,16 @@
 // on the host.  The normals are regenerated from their Philox counters.
 //
 // Checkpoint mode (checkpoint_every = K in [1, stride]).  The forward pass
-// keeps only the cash flows; before every K-th Euler step it writes the
-// path's state (scaled curve, polynomial parts, scales) and the FP64 discount
-// sum of the next tenor to be sampled to HBM.  Because the Jacobian is
-// state-independent, the reverse sweep needs the forward state only at the
-// sampling steps: the seed pass recomputes each date's state from the last
-// checkpoint before it (at most K steps, repeating the forward arithmetic from
-// the stored state) and forms the date's seeds; the sweep then runs backwards
-// over the steps with the regenerated normals.  With K = 0 the forward pass
-// keeps the per-date (x_i, D_i) instead and nothing is recomputed.
+// keeps only the cash flows; before every K-th Euler step whose segment holds
+// a date's sampling step it writes the path's state (scaled curve, polynomial
+// parts, scales) and the FP64 discount sum of the next tenor to be sampled to
+// HBM.  Because the Jacobian is state-independent, the reverse sweep needs the
+// forward state only at the sampling steps: the seed pass recomputes each
+// date's state from the last checkpoint before it (at most K steps, repeating
+// the forward arithmetic from the stored state) and forms the date's seeds;
+// the sweep then runs backwards over the steps with the regenerated normals.
+// With K = 0 the forward pass keeps the per-date (x_i, D_i) instead and
+// nothing is recomputed.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -198,12 +199,15 @@ __global__ void __launch_bounds__(kAdjCta, adj_min_ctas<NT>())
                 // the latter recovered from the partial sums of the block)
                 ck_next += K;
                 const int inext = b + 1;
+                // only a segment that holds a date's sampling step (the block's
+                // last step) is ever restarted by the seed pass
+                const bool needed = (b + 1) * stride - 1 < n + K;
                 double part = 0.0;
-                if (s > 0)
+                if (needed && s > 0)
                     block_sums_up<NT, POLY>(x, hs_s, tid, kCtaA, P, bs, inext, [&](int t, float Ht) {
                         if (t == inext) part = (double)Ht;
                     });
-                if (active) {
+                if (needed && active) {
 #pragma unroll
                     for (int t = 0; t < NT; ++t) ck_h[((size_t)ck * kCkRows + t) * ld + lp] = pair_tenor<NT>(x.h, t);
                     ck_h[((size_t)ck * kCkRows + NT) * ld + lp] = x.S;
