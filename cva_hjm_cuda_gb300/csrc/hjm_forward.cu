@@ -153,7 +153,12 @@ __global__ void __launch_bounds__(kFp64Cta, 4)
                 const double hl = fma(mig, W, fma(rr, fma(2.0, h[L], -h[L - 1]), h[L]));  // + scaled source
 #pragma unroll
                 for (int gi = 0; gi < kGroups; ++gi) {
-                    if (kGroup * gi + kGroup > live) {  // uniform: skip groups of dead tenors
+                    // uniform: skip groups of dead tenors, and (polynomial form)
+                    // the exact zeros below the remainder's front: driven only
+                    // at the last tenor from zero, after k steps it is nonzero
+                    // on tenors >= L - k only
+                    const int front = L - 1 - ((b - 1) * P.stride + s);
+                    if (kGroup * gi + kGroup > (live > front ? live : front)) {
 #pragma unroll
                         for (int j = 0; j < kGroup; ++j) {
                             const int t = kGroup * gi + j;
