@@ -67,7 +67,9 @@ def algorithmic_flops_per_path(n_tenor: int, n_steps: int, stride: int, form: st
 
     During block b (the steps that end by sampling date b+1) only tenors
     b+1 .. L are ever read again (the upwind step carries information from
-    high to low tenors), so the needed convection covers those.  Per evolved
+    high to low tenors), so the needed convection covers those; in the
+    polynomial forms the remainder is also exactly zero below its front
+    during the first block.  Per evolved
     Euler step of block b:
     ``poly_tri`` (factor k a polynomial of degree <= k in T, the reference's
     own volatility table): the growth-scaled convection of the remainder
@@ -85,12 +87,16 @@ def algorithmic_flops_per_path(n_tenor: int, n_steps: int, stride: int, form: st
     ADD or MUL issues like an FMA, so the fraction is a lower bound on the
     FP64 pipe's use (ncu's pipe utilisation is the direct measure)."""
     B = n_steps // stride
+    L = n_tenor - 1
 
-    def per_step(b: int) -> int:
-        return {"poly_tri": 2 * (n_tenor - b) + 26, "poly": 2 * (n_tenor - b) + 32,
-                "table": 8 * (n_tenor - b) + 3}[form]
+    def per_step(b: int, k: int) -> int:
+        # polynomial forms: the remainder is still zero below tenor L - 1 - k
+        # after k evolved steps
+        lo = b if form == "table" else max(b, L - 2 - k)
+        return {"poly_tri": 2 * (n_tenor - lo) + 26, "poly": 2 * (n_tenor - lo) + 32,
+                "table": 8 * (n_tenor - lo) + 3}[form]
 
-    steps = sum(stride * per_step(b) for b in range(1, B))
+    steps = sum(per_step(b, (b - 1) * stride + s) for b in range(1, B) for s in range(stride))
     recovery = 12 * sum(B - b for b in range(1, B))
     return steps + recovery
 
