@@ -295,3 +295,20 @@ def test_one_and_two_dates_every_mode(engine, n_steps):
         assert s.cva == v.cva and np.all(np.isfinite(s.dcva_dspot))
     m = engine.run_mlmc([777, 512], n_steps=n_steps // 2, dt=0.02, seed=2)
     assert np.isfinite(m["cva"]) and m["levels"][1]["n_paths"] == 512
+
+
+@pytest.mark.slow
+def test_large_run_equals_its_halves(engine):
+    """33,554,432 paths (2^25) in mixed precision with PFE: a 2.8 GB exposure
+    store and 524,288 CTAs.  The full run's EE and CVA equal the path-weighted
+    mean of its two halves run separately through path_offset (the same
+    normals), up to the reduction's rounding."""
+    _setup(engine, Market(), Swap())
+    n = 1 << 25
+    full = engine.run(RunConfig(n_paths=n, seed=9), "mixed")
+    a = engine.run(RunConfig(n_paths=n // 2, seed=9), "mixed", pfe=False)
+    b = engine.run(RunConfig(n_paths=n // 2, seed=9, path_offset=n // 2), "mixed", pfe=False)
+    np.testing.assert_allclose(full.ee, 0.5 * (a.ee + b.ee), rtol=1e-12, atol=1e-12 * np.max(full.ee))
+    assert full.cva == pytest.approx(0.5 * (a.cva + b.cva), rel=1e-12)
+    assert np.all(np.diff(full.pfe[:20]) < 0.5 * full.pfe[0])  # finite and ordered like a quantile profile
+    assert np.all(full.pfe[:20] >= full.ee[:20])
