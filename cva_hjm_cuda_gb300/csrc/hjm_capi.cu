@@ -587,6 +587,22 @@ static void fill_pc(const hjm_ctx* ctx, const RunShape& sh, double dt, const Pat
     Q.ce = (T)ce;
     Q.inv_1ma0 = (T)(base / ((double)r1 + (double)r2));
     Q.inv_ce = (T)(1.0 / ce);
+    // polynomial form: N xi = (alpha + c dtau beta / 2 + c dtau^2 gamma / 2) + (beta + c dtau gamma) T
+    // + gamma T^2 - c dtau^2 gamma e_L;  A2 T^2 = T^2 + 2 c dtau T + (c + c^2) dtau^2
+    // - c^2 dtau^2 e_{L-1} - (2c + c^2) dtau^2 e_L
+    const double dtau = ctx->dtau;
+    for (int k = 0; k < kFactors; ++k) {
+        const double c0 = sq * ctx->coef[3 * k], c1 = sq * ctx->coef[3 * k + 1], c2 = sq * ctx->coef[3 * k + 2];
+        Q.aS[k] = (T)(c0 + 0.5 * c * dtau * c1 + 0.5 * c * dtau * dtau * c2);
+        Q.aU[k] = (T)(c1 + c * dtau * c2);
+        Q.aW[k] = (T)c2;
+    }
+    Q.k1 = (T)(c * dtau);
+    Q.k2p = (T)((c + c * c) * dtau * dtau);
+    Q.k1x2 = (T)(2.0 * c * dtau);
+    Q.wL1 = (T)(-c * c * dtau * dtau);
+    Q.wL = (T)(-(2.0 * c + c * c) * dtau * dtau);
+    Q.gL = (T)(-c * dtau * dtau);
 }
 
 static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, double dt, uint64_t seed,
@@ -633,7 +649,7 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
         PcParams<float> Q;
         fill_pc<float>(ctx, sh, dt, P, Q);
         ctx->stat_h2d = sizeof(Q) + sizeof(FinalParams);
-        HJM_CUDA(ctx, launch_path_pc(ctx->nt, Q, ext_dev, (double*)ctx->partials.p,
+        HJM_CUDA(ctx, launch_path_pc(ctx->nt, Q, use_poly_path(ctx), ext_dev, (double*)ctx->partials.p,
                                      store ? (float*)ctx->estore.p : nullptr, s));
     } else if (pc) {
         PathParams<double> P;
@@ -641,7 +657,7 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
         PcParams<double> Q;
         fill_pc<double>(ctx, sh, dt, P, Q);
         ctx->stat_h2d = sizeof(Q) + sizeof(FinalParams);
-        HJM_CUDA(ctx, launch_path_pc(ctx->nt, Q, ext_dev, (double*)ctx->partials.p,
+        HJM_CUDA(ctx, launch_path_pc(ctx->nt, Q, use_poly_path(ctx), ext_dev, (double*)ctx->partials.p,
                                      store ? (double*)ctx->estore.p : nullptr, s));
     } else if (mixed) {
         PathParams<float> P;

@@ -80,11 +80,17 @@ struct PcParams {
     T r1, r2;              // a1 / a0, a2 / a0 (rounded once)
     T a0e, a1e, a2e, ce;   // effective scheme: 1/base, r1/base, r2/base, (r1 + 2 r2)/base
     T inv_1ma0, inv_ce;    // 1 / (1 - a0e), 1 / ce
+    // polynomial form (factors of degree <= 2, PathParams::svc): h = S + U T +
+    // W T^2 + remainder, with the noise N xi projected onto S, U, W and
+    // last-tenor sources for the remainder
+    T aS[kFactors], aU[kFactors], aW[kFactors];  // noise loadings of S, U, W
+    T k1, k2p, k1x2;       // c dtau, (c + c^2) dtau^2, 2 c dtau
+    T wL1, wL, gL;         // sources: -c^2 dtau^2 W at L-1; -(2c + c^2) dtau^2 W - c dtau^2 gamma at L
 };
-cudaError_t launch_path_pc(int nt, const PcParams<double>& Q, const double* ext, double* partials, double* estore,
-                           cudaStream_t s);
-cudaError_t launch_path_pc(int nt, const PcParams<float>& Q, const double* ext, double* partials, float* estore,
-                           cudaStream_t s);
+cudaError_t launch_path_pc(int nt, const PcParams<double>& Q, bool poly, const double* ext, double* partials,
+                           double* estore, cudaStream_t s);
+cudaError_t launch_path_pc(int nt, const PcParams<float>& Q, bool poly, const double* ext, double* partials,
+                           float* estore, cudaStream_t s);
 size_t pc_smem(int nt, int n_blocks, bool mixed);
 int pc_cta();
 

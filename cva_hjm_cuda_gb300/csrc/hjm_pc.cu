@@ -63,7 +63,7 @@ __host__ __device__ inline size_t pc_smem_bytes(int nt, int n_blocks, size_t tsi
     return b + 2 * (kPcCta / 32) * 8;
 }
 
-template <int NT, typename T, bool EXT>
+template <int NT, typename T, bool EXT, bool POLY>
 __global__ void __launch_bounds__(kPcCta, 4)
     path_kernel_pc(const __grid_constant__ PcParams<T> Q, const double* __restrict__ ext,
                    double* __restrict__ partials, T* __restrict__ estore)
@@ -93,8 +93,10 @@ __global__ void __launch_bounds__(kPcCta, 4)
     for (int t = 0; t < NT; ++t) hs_s[t * kPcCta + tid] = T(0);
 
     T g = T(1);
+    T S = T(0), U = T(0), W = T(0);  // POLY: the polynomial parts
+    auto poly_at = [&](T s_, T u_, T w_, int t) -> T { return POLY ? fma(P.tau[t], fma(P.tau[t], w_, u_), s_) : T(0); };
     auto sample = [&](int i) {
-        const double x = P.psamp[i] + (double)(g * select_reg<NT, T>(v, i));
+        const double x = P.psamp[i] + (double)(g * select_reg<NT, T>(v, i) + poly_at(S, U, W, i));
         const double a = P.psum[i] + acc_s[i * kPcCta + tid];
         const T D = exp_t<T>((T)(-a * P.dt));
         const T mm = (T)P.m;
@@ -106,6 +108,7 @@ __global__ void __launch_bounds__(kPcCta, 4)
     const T r1 = Q.r1, r2 = Q.r2;
     for (int b = 1; b < B; ++b) {
         T F0 = T(0), F1 = T(0), F2 = T(0), Tb = T(0);  // block sums of phi_k; anchor sum of v[L]
+        T sS = T(0), sU = T(0), sW = T(0), XL1 = T(0), XL = T(0);  // POLY: sums of S, U, W and the sources
         T ig = P.igblk[b];
         const int live = b + 1;  // tenors <= b are never read again
         for (int s = 0; s < P.stride; ++s) {
@@ -118,8 +121,32 @@ __global__ void __launch_bounds__(kPcCta, 4)
             // the two Euler rows first (they read v[L-1], v[L]), then the
             // interior ascending in place (v[t+1], v[t+2] still old)
             const T eL = fma(T(2), v[L], -v[L - 1]);
-            const T vL1 = fma(r2, eL, fma(r1, v[L], v[L - 1])) + noise(L - 1);
-            const T vL = fma(r2, fma(T(3), v[L], T(-2) * v[L - 1]), fma(r1, eL, v[L])) + noise(L);
+            T vL1 = fma(r2, eL, fma(r1, v[L], v[L - 1]));
+            T vL = fma(r2, fma(T(3), v[L], T(-2) * v[L - 1]), fma(r1, eL, v[L]));
+            if constexpr (POLY) {
+                // the remainder's sources (old W), then S, U, W (old values on the right)
+                const T gam = fma(Q.aW[2], phi2, fma(Q.aW[1], phi1, Q.aW[0] * phi0));
+                const T sL1 = Q.wL1 * W, sL = fma(Q.gL, gam, Q.wL * W);
+                vL1 = fma(sL1, ig, vL1);
+                vL = fma(sL, ig, vL);
+                XL1 += sL1;
+                XL += sL;
+                T Sn = fma(Q.aS[0], phi0, fma(Q.k2p, W, fma(Q.k1, U, S)));
+                Sn = fma(Q.aS[2], phi2, fma(Q.aS[1], phi1, Sn));
+                const T Un = fma(Q.aU[2], phi2, fma(Q.aU[1], phi1, fma(Q.aU[0], phi0, fma(Q.k1x2, W, U))));
+                S = Sn;
+                U = Un;
+                W += gam;
+                sS += S;
+                sU += U;
+                sW += W;
+            } else {
+                vL1 += noise(L - 1);
+                vL += noise(L);
+                F0 += phi0;
+                F1 += phi1;
+                F2 += phi2;
+            }
 #pragma unroll
             for (int gi = 0; gi < kGroups; ++gi) {
                 if (kGroup * gi + kGroup > live) {
@@ -127,9 +154,12 @@ __global__ void __launch_bounds__(kPcCta, 4)
                     for (int j = 0; j < kGroup; ++j) {
                         const int t = kGroup * gi + j;
                         if (t <= L - 2) {
-                            T x = fma(P.sv[0][t], p0, v[t]);
-                            x = fma(P.sv[1][t], p1, x);
-                            x = fma(P.sv[2][t], p2, x);
+                            T x = v[t];
+                            if constexpr (!POLY) {
+                                x = fma(P.sv[0][t], p0, x);
+                                x = fma(P.sv[1][t], p1, x);
+                                x = fma(P.sv[2][t], p2, x);
+                            }
                             x = fma(r1, v[t + 1], x);
                             v[t] = fma(r2, v[t + 2], x);
                         }
@@ -138,21 +168,21 @@ __global__ void __launch_bounds__(kPcCta, 4)
             }
             v[L - 1] = vL1;
             v[L] = vL;
-            F0 += phi0;
-            F1 += phi1;
-            F2 += phi2;
             Tb = fma(P.ip, Tb, v[L]);
         }
         g = P.gblk[b + 1];  // base^-(b stride): the scale at the block end
         // block sums of tenors b+1 .. L, downward from the anchor H[L] = g Tb
         {
-            auto X = [&](int t) -> T { return fma(P.sv[2][t], F2, fma(P.sv[1][t], F1, P.sv[0][t] * F0)); };
+            auto X = [&](int t) -> T {
+                if constexpr (POLY) return t == L - 1 ? XL1 : (t == L ? XL : T(0));
+                return fma(P.sv[2][t], F2, fma(P.sv[1][t], F1, P.sv[0][t] * F0));
+            };
             const T dL = fma(g, v[L], -hs_s[L * kPcCta + tid]);
             const T dL1 = fma(g, v[L - 1], -hs_s[(L - 1) * kPcCta + tid]);
             const T HL = g * Tb;
             const T HL1 = fma(X(L - 1) - fma(Q.ce, dL - dL1, dL1), Q.inv_ce, HL);
-            if (L <= B) acc_s[L * kPcCta + tid] += (double)HL;
-            if (L - 1 <= B && L - 1 > b) acc_s[(L - 1) * kPcCta + tid] += (double)HL1;
+            if (L <= B) acc_s[L * kPcCta + tid] += (double)(HL + poly_at(sS, sU, sW, L));
+            if (L - 1 <= B && L - 1 > b) acc_s[(L - 1) * kPcCta + tid] += (double)(HL1 + poly_at(sS, sU, sW, L - 1));
             T H1 = HL1, H2 = HL, d1 = dL1, d2 = dL;
 #pragma unroll
             for (int t = L - 2; t >= 1; --t) {
@@ -160,7 +190,7 @@ __global__ void __launch_bounds__(kPcCta, 4)
                 const T d = fma(g, v[t], -hs_s[t * kPcCta + tid]);
                 const T a2d = fma(Q.a2e, d2, fma(Q.a1e, d1, Q.a0e * d));
                 const T Ht = (X(t) - a2d + fma(Q.a1e, H1, Q.a2e * H2)) * Q.inv_1ma0;
-                if (t <= B) acc_s[t * kPcCta + tid] += (double)Ht;
+                if (t <= B) acc_s[t * kPcCta + tid] += (double)(Ht + poly_at(sS, sU, sW, t));
                 H2 = H1;
                 H1 = Ht;
                 d2 = d1;
@@ -229,11 +259,11 @@ __global__ void __launch_bounds__(kPcCta, 4)
     }
 }
 
-template <int NT, typename T, bool EXT>
+template <int NT, typename T, bool EXT, bool POLY>
 static cudaError_t launch_pc_t(const PcParams<T>& Q, const double* ext, double* partials, T* estore, cudaStream_t s)
 {
     const size_t smem = pc_smem_bytes(NT, Q.P.n_blocks, sizeof(T));
-    auto k = path_kernel_pc<NT, T, EXT>;
+    auto k = path_kernel_pc<NT, T, EXT, POLY>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const int64_t grid = (Q.P.n_paths + kPcCta - 1) / kPcCta;
@@ -241,27 +271,35 @@ static cudaError_t launch_pc_t(const PcParams<T>& Q, const double* ext, double* 
     return cudaGetLastError();
 }
 
-template <typename T>
-static cudaError_t launch_pc_any(int nt, const PcParams<T>& Q, const double* ext, double* partials, T* estore,
-                                 cudaStream_t s)
+template <int NT, typename T>
+static cudaError_t launch_pc_nt(const PcParams<T>& Q, bool poly, const double* ext, double* partials, T* estore,
+                                cudaStream_t s)
 {
-    if (nt == 51) return ext ? launch_pc_t<51, T, true>(Q, ext, partials, estore, s)
-                             : launch_pc_t<51, T, false>(Q, ext, partials, estore, s);
-    if (nt == 61) return ext ? launch_pc_t<61, T, true>(Q, ext, partials, estore, s)
-                             : launch_pc_t<61, T, false>(Q, ext, partials, estore, s);
+    if (ext) return poly ? launch_pc_t<NT, T, true, true>(Q, ext, partials, estore, s)
+                         : launch_pc_t<NT, T, true, false>(Q, ext, partials, estore, s);
+    return poly ? launch_pc_t<NT, T, false, true>(Q, ext, partials, estore, s)
+                : launch_pc_t<NT, T, false, false>(Q, ext, partials, estore, s);
+}
+
+template <typename T>
+static cudaError_t launch_pc_any(int nt, const PcParams<T>& Q, bool poly, const double* ext, double* partials,
+                                 T* estore, cudaStream_t s)
+{
+    if (nt == 51) return launch_pc_nt<51, T>(Q, poly, ext, partials, estore, s);
+    if (nt == 61) return launch_pc_nt<61, T>(Q, poly, ext, partials, estore, s);
     return cudaErrorInvalidValue;
 }
 
-cudaError_t launch_path_pc(int nt, const PcParams<double>& Q, const double* ext, double* partials, double* estore,
-                           cudaStream_t s)
+cudaError_t launch_path_pc(int nt, const PcParams<double>& Q, bool poly, const double* ext, double* partials,
+                           double* estore, cudaStream_t s)
 {
-    return launch_pc_any<double>(nt, Q, ext, partials, estore, s);
+    return launch_pc_any<double>(nt, Q, poly, ext, partials, estore, s);
 }
 
-cudaError_t launch_path_pc(int nt, const PcParams<float>& Q, const double* ext, double* partials, float* estore,
-                           cudaStream_t s)
+cudaError_t launch_path_pc(int nt, const PcParams<float>& Q, bool poly, const double* ext, double* partials,
+                           float* estore, cudaStream_t s)
 {
-    return launch_pc_any<float>(nt, Q, ext, partials, estore, s);
+    return launch_pc_any<float>(nt, Q, poly, ext, partials, estore, s);
 }
 
 size_t pc_smem(int nt, int n_blocks, bool mixed) { return pc_smem_bytes(nt, n_blocks, mixed ? 4 : 8); }

@@ -85,8 +85,9 @@ hjm_status hjm_ctx_keep_exposures(hjm_ctx* ctx, int32_t keep);
  * reference's Euler step (simulation_cpu.h:37-54); HJM_SCHEME_PREDICTOR_CORRECTOR
  * (the reference's doc/TODO:3) averages the drift term mu + dF/dtau at the
  * curve and at its Euler prediction: f' = f + (a(f) + a(f*)) dt / 2 + xi.
- * Valuations (both precisions, table volatility step) support both; the
- * adjoint and hjm_run_static the Euler step only. */
+ * Valuations (both precisions, the table and the decomposed volatility step)
+ * support both; the adjoint, hjm_run_mlmc and hjm_run_static the Euler step
+ * only. */
 #define HJM_SCHEME_EULER 0
 #define HJM_SCHEME_PREDICTOR_CORRECTOR 1
 hjm_status hjm_ctx_set_scheme(hjm_ctx* ctx, int32_t scheme);

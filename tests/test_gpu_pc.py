@@ -1,5 +1,6 @@
 """GPU parity of the predictor-corrector time scheme (hjm_ctx_set_scheme)
-against the oracle's restatement of the same scheme on the device's normals.
+against the oracle's restatement of the same scheme on the device's normals,
+on the decomposed step (quadratic factors) and on the generic table step.
 
 FP64 EE, PFE, CVA and per-path exposures within 1e-10 relative; mixed
 precision within 1e-4 and inside the Monte Carlo error; the scheme differs
@@ -106,3 +107,32 @@ def test_pc_adjoint_is_refused(pc):
         pc.run_adjoint(RunConfig(n_paths=1000))
     assert ei.value.status == 2
     assert pc.lib.hjm_ctx_set_scheme(pc.ctx, 7) == 1  # unknown scheme: HJM_ERR_INVALID_ARGUMENT
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_pc_generic_table_step_vs_oracle(pc, case, precision):
+    """The same scheme on the generic table step (the decomposition off)."""
+    mk, sw, cfg, normals, x, ee, cva = case
+    pc.vol_decomposition(False)
+    try:
+        pc.set_market(mk)
+        pc.set_swap(sw)
+        v = pc.run(cfg, precision)
+    finally:
+        pc.vol_decomposition(True)
+    tol = FP64_RTOL if precision == "fp64" else MIXED_RTOL
+    _assert_rel(v.ee[:20], ee[:20], tol, "EE (table step)")
+    _assert_rel(v.cva, cva, tol, "CVA (table step)")
+
+
+def test_pc_general_quadratic_factors(pc):
+    coef = np.array([[0.0060, 0.00010, -0.000004], [-0.0036, 0.00040, 0.000003], [0.0020, -0.00060, 0.00002]])
+    mk = Market(vol_coeffs=coef)
+    pc.set_market_poly(51, 0.5, mk.spot, coef)
+    sw = Swap()
+    pc.set_swap(sw)
+    assert pc.vol_form() == "poly"
+    cfg = RunConfig(n_paths=3000, seed=12)
+    normals = pc.dump_normals(cfg.n_paths, cfg.n_steps, cfg.seed)
+    ee = O.expected_exposure(O.exposure_paths_pc(mk, sw, cfg.n_steps, cfg.dt, normals))
+    _assert_rel(pc.run(cfg, "fp64").ee[:20], ee[:20], FP64_RTOL, "EE (general quadratic)")
