@@ -61,7 +61,8 @@ def env_rank():
             int(os.environ.get("WORLD_SIZE", 1)))
 
 
-def algorithmic_flops_per_path(n_tenor: int, n_steps: int, stride: int, form: str) -> int:
+def algorithmic_flops_per_path(n_tenor: int, n_steps: int, stride: int, form: str,
+                               remainder: str = "convect") -> int:
     """Floating-point operations the path kernel's algorithm needs per path
     (FMA = 2), counted from its formulas, not measured.
 
@@ -85,9 +86,21 @@ def algorithmic_flops_per_path(n_tenor: int, n_steps: int, stride: int, form: st
     (about 12 flops each).  The first block holds the curve at spot and does
     no arithmetic.  Normals, pricing and reductions are not counted, and an
     ADD or MUL issues like an FMA, so the fraction is a lower bound on the
-    FP64 pipe's use (ncu's pipe utilisation is the direct measure)."""
+    FP64 pipe's use (ncu's pipe utilisation is the direct measure).
+
+    ``remainder="response"`` (polynomial forms, FP64, at most 24 dates): the
+    remainder is carried as impulse-response sums at the sampled tenors, two
+    FMAs per date still to be sampled whose response is not yet an exact zero
+    (its lag must reach the date's tenor), plus the scalar parts (9 FMA, or 12
+    for general quadratic factors) and their running sums (3 ADD); no block
+    recovery."""
     B = n_steps // stride
     L = n_tenor - 1
+    if remainder == "response" and form != "table":
+        per = 21 if form == "poly_tri" else 27
+        live = sum(1 for b in range(1, B) for s in range(stride) for j in range(b + 1, B + 1)
+                   if s + 1 + L + b * stride <= j * (stride + 1))
+        return per * (B - 1) * stride + 4 * live
 
     def per_step(b: int, k: int) -> int:
         # polynomial forms: the remainder is still zero below tenor L - 1 - k
@@ -331,7 +344,9 @@ def run_ours(args) -> None:
         return
 
     form = vol_form
-    flops = algorithmic_flops_per_path(mk.n_tenor, n_steps, stride, form) * n_paths * (2 if is_adjoint else 1)
+    remainder = "convect" if (is_adjoint or prec != "fp64") else eng.remainder_form()
+    flops = (algorithmic_flops_per_path(mk.n_tenor, n_steps, stride, form, remainder) * n_paths
+             * (2 if is_adjoint else 1))
     extras = {}
     peak_key = "fp64" if prec == "fp64" else "mixed"
     peak = None
@@ -347,6 +362,8 @@ def run_ours(args) -> None:
     roofline = {"bound": "fp64_pipe" if prec == "fp64" else "fp32_pipe", "achieved": achieved, "peak": peak,
                 "unit": "TFLOP/s", "frac": (achieved / peak) if peak else None, "traffic": traffic,
                 "kernel": (f"adjoint_kernel<{mk.n_tenor},ckpt,{form}>" if is_adjoint else
+                           f"path_kernel_fp64_resp<{mk.n_tenor},philox,{form}>"
+                           if prec == "fp64" and remainder == "response" else
                            f"path_kernel_fp64<{mk.n_tenor},philox,{form}>" if prec == "fp64" else
                            f"path_kernel_mixed<{mk.n_tenor},philox,{form}>"),
                 "algorithmic_flops_per_launch": flops, "avg_launch_ms": path_ms,
@@ -380,6 +397,7 @@ def run_ours(args) -> None:
                    "recovery": 0.4, "seed": SEED,
                    "vol_form": ("quadratic factors (detected in the volatility table): decomposed step" if vol_form_poly
                                 else "volatility table: generic step"),
+                   "remainder": remainder,
                    "parallelism": f"replicas{world}" if world > 1 else "single",
                    "l2": f"flushed between steps ({FLUSH_BYTES >> 20} MiB device write, inside the timed region)"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),

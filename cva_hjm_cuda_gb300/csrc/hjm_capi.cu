@@ -68,6 +68,7 @@ struct hjm_ctx {
     bool poly_path = false;       // the kernels run the polynomial decomposition (coef)
     bool allow_poly_path = true;  // hjm_ctx_set_vol_decomposition
     int scheme = HJM_SCHEME_EULER;  // hjm_ctx_set_scheme
+    int remainder = HJM_REMAINDER_AUTO;  // hjm_ctx_set_remainder_form
     int nt = 0;
     double dtau = 0.5;
     std::vector<double> spot, vol, drift;
@@ -80,7 +81,15 @@ struct hjm_ctx {
     bool keep_exposures = false;
 
     // device buffers
-    DevBuf partials, sums, result, estore, sel, hist, ext, ext_raw, wide, scratch, ck_h, ck_a;
+    DevBuf partials, sums, result, estore, sel, hist, ext, ext_raw, wide, scratch, ck_h, ck_a, resp;
+    // the response table in resp holds the run shape of resp_key; resp_used
+    // is recorded after the last kernel that reads it
+    struct RespKey {
+        bool valid = false;
+        int nt = 0, stride = 0, B = 0;
+        double c = 0, kappa = 0;
+    } resp_key;
+    cudaEvent_t resp_used = nullptr;
 
     // last valuation
     bool have_result = false;
@@ -104,6 +113,7 @@ struct hjm_ctx {
         bool valid = false, adjoint = false, pfe = false, external_normals = false;
         int64_t n_paths = 0;
         int n_steps = 0, n_dates = 0, precision = 0, vol_form = 0, ckpt = 0, nt = 0, scheme = 0;
+        int remainder = 0;  // 0 none (table step), 1 convected, 2 impulse responses
         double dt = 0, dtau = 0, hazard = 0, recovery = 0, pfe_q = 0;
         uint64_t seed = 0, path_offset = 0;
         std::vector<double> ee, pfe_v, dspot, ddrift;
@@ -200,8 +210,9 @@ hjm_status hjm_ctx_destroy(hjm_ctx* ctx)
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     for (DevBuf* b : {&ctx->partials, &ctx->sums, &ctx->result, &ctx->estore, &ctx->sel, &ctx->hist, &ctx->ext,
-                      &ctx->ext_raw, &ctx->wide, &ctx->scratch, &ctx->ck_h, &ctx->ck_a})
+                      &ctx->ext_raw, &ctx->wide, &ctx->scratch, &ctx->ck_h, &ctx->ck_a, &ctx->resp})
         b->release();
+    if (ctx->resp_used) cudaEventDestroy(ctx->resp_used);
     for (auto& q : ctx->ring)
         for (auto& ev : q)
             if (ev) cudaEventDestroy(ev);
@@ -239,6 +250,23 @@ hjm_status hjm_ctx_set_scheme(hjm_ctx* ctx, int32_t scheme)
     if (scheme != HJM_SCHEME_EULER && scheme != HJM_SCHEME_PREDICTOR_CORRECTOR)
         return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "unknown time scheme %d", scheme);
     ctx->scheme = scheme;
+    return HJM_OK;
+}
+
+hjm_status hjm_ctx_set_remainder_form(hjm_ctx* ctx, int32_t form)
+{
+    HJM_CHECK_CTX(ctx);
+    if (form != HJM_REMAINDER_AUTO && form != HJM_REMAINDER_CONVECT && form != HJM_REMAINDER_RESPONSE)
+        return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "unknown remainder form %d", form);
+    ctx->remainder = form;
+    return HJM_OK;
+}
+
+hjm_status hjm_ctx_remainder_form(hjm_ctx* ctx, int32_t* form)
+{
+    HJM_CHECK_CTX(ctx);
+    if (!form) return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "form must not be null");
+    *form = ctx->rep_run.remainder;
     return HJM_OK;
 }
 
@@ -605,6 +633,49 @@ static void fill_pc(const hjm_ctx* ctx, const RunShape& sh, double dt, const Pat
     Q.gL = (T)(-c * dtau * dtau);
 }
 
+// FP64 Euler valuation with the decomposition: the remainder in impulse
+// responses (two FMAs per date still to be sampled and ~12 FP64 operations per
+// step) when that is cheaper than its convection (one FMA per live tenor and
+// ~17 per step), summed over the evolved blocks.
+static bool use_response_form(const hjm_ctx* ctx, const RunShape& sh)
+{
+    if (!use_poly_path(ctx) || ctx->scheme != HJM_SCHEME_EULER || sh.B > response_max_dates()) return false;
+    if (ctx->remainder != HJM_REMAINDER_AUTO) return ctx->remainder == HJM_REMAINDER_RESPONSE;
+    long conv = 0, resp = 0;
+    for (int b = 1; b < sh.B; ++b) {
+        conv += (ctx->nt - 1 - b) + 17;
+        resp += 2 * (sh.B - b) + 12;
+    }
+    return resp < conv;
+}
+
+// The response table of the run shape, on the stream: recomputed only when the
+// shape changed, after the kernels of earlier valuations that read it.
+static hjm_status ensure_response_table(hjm_ctx* ctx, const RunShape& sh, const PathParams<double>& P,
+                                        cudaStream_t s)
+{
+    const double kappa = -2.0 * P.k2;
+    hjm_ctx::RespKey& k = ctx->resp_key;
+    if (!ctx->resp_used) HJM_CUDA(ctx, cudaEventCreateWithFlags(&ctx->resp_used, cudaEventDisableTiming));
+    if (k.valid && k.nt == ctx->nt && k.stride == sh.stride && k.B == sh.B && k.c == P.c && k.kappa == kappa)
+        return HJM_OK;
+    k.valid = false;
+    const size_t bytes = sizeof(double2) * response_table_elems(sh.stride, sh.B);
+    if (bytes > ctx->resp.bytes)
+        HJM_CUDA(ctx, ctx->resp.ensure(bytes));  // cudaFree waits for the device
+    else
+        HJM_CUDA(ctx, cudaStreamWaitEvent(s, ctx->resp_used, 0));
+    HJM_CUDA(ctx, launch_response_table(ctx->nt, P.c, kappa, sh.stride, sh.B, (double2*)ctx->resp.p, s));
+    ctx->stat_launches += 1;
+    k.nt = ctx->nt;
+    k.stride = sh.stride;
+    k.B = sh.B;
+    k.c = P.c;
+    k.kappa = kappa;
+    k.valid = true;
+    return HJM_OK;
+}
+
 static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, double dt, uint64_t seed,
                                uint64_t path_offset, int32_t precision, double hazard, double recovery, double pfe_q,
                                const double* ext_dev)
@@ -614,6 +685,10 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
     if (st != HJM_OK) return st;
     HJM_CUDA(ctx, cudaSetDevice(ctx->device));
     const bool mixed = precision == HJM_PRECISION_MIXED;
+    if (!mixed && ctx->remainder == HJM_REMAINDER_RESPONSE && use_poly_path(ctx) &&
+        ctx->scheme == HJM_SCHEME_EULER && sh.B > response_max_dates())
+        return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "the response form holds at most %d dates (run has %d)",
+                    response_max_dates(), sh.B);
     const bool want_pfe = pfe_q > 0.0;
     const bool store = want_pfe || ctx->keep_exposures;
     const int n_dates = sh.B + 1;
@@ -643,6 +718,7 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
     ctx->stat_h2d = (mixed ? sizeof(MixedParams) : sizeof(PathParams<double>)) + sizeof(FinalParams);
     ctx->stat_d2h = 0;
     HJM_CUDA(ctx, cudaEventRecord(ctx->ev[0], s));
+    bool resp = false;
     if (pc && mixed) {
         PathParams<float> P;
         fill_params<float>(ctx, sh, n_paths, dt, seed, path_offset, hazard, recovery, ld, store, P, F);
@@ -669,8 +745,15 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
     } else {
         PathParams<double> P;
         fill_params<double>(ctx, sh, n_paths, dt, seed, path_offset, hazard, recovery, ld, store, P, F);
-        HJM_CUDA(ctx, launch_path_fp64(ctx->nt, P, use_poly_path(ctx), ext_dev, (double*)ctx->partials.p,
-                                       store ? (double*)ctx->estore.p : nullptr, s));
+        resp = use_response_form(ctx, sh);
+        if (resp) {
+            st = ensure_response_table(ctx, sh, P, s);
+            if (st != HJM_OK) return st;
+        }
+        HJM_CUDA(ctx, launch_path_fp64(ctx->nt, P, use_poly_path(ctx), resp ? (const double2*)ctx->resp.p : nullptr,
+                                       ext_dev, (double*)ctx->partials.p, store ? (double*)ctx->estore.p : nullptr,
+                                       s));
+        if (resp) HJM_CUDA(ctx, cudaEventRecord(ctx->resp_used, s));
     }
     HJM_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
     HJM_CUDA(ctx, launch_reduce((const double*)ctx->partials.p, n_ctas, R, (double*)ctx->sums.p, F,
@@ -704,6 +787,7 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
         r.path_offset = path_offset;
         r.external_normals = ext_dev != nullptr;
         r.scheme = ctx->scheme;
+        r.remainder = resp ? 2 : use_poly_path(ctx) ? 1 : 0;
     }
     ctx->last_n_paths = n_paths;
     ctx->last_n_dates = n_dates;
@@ -1018,6 +1102,7 @@ hjm_status hjm_run_adjoint(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, doubl
     r.nt = nt;
     r.precision = HJM_PRECISION_MIXED;
     r.vol_form = vol_form_code(ctx);
+    r.remainder = use_poly_path(ctx) ? 1 : 0;
     r.ckpt = K;
     r.dt = dt;
     r.dtau = ctx->dtau;
@@ -1171,6 +1256,7 @@ hjm_status hjm_run_mlmc(hjm_ctx* ctx, int32_t n_levels, const int64_t* n_paths, 
         r.nt = nt;
         r.precision = HJM_PRECISION_MIXED;
         r.vol_form = vol_form_code(ctx);
+        r.remainder = use_poly_path(ctx) ? 1 : 0;
         r.dtau = ctx->dtau;
         r.hazard = hazard_rate;
         r.recovery = recovery;
@@ -1214,6 +1300,7 @@ hjm_status hjm_write_report(hjm_ctx* ctx, const char* path, int32_t format)
     FILE* f = std::fopen(path, "w");
     if (!f) return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "cannot open %s for writing", path);
     static const char* kForms[] = {"table", "poly", "poly_tri"};
+    static const char* kRemainders[] = {"none", "convect", "response"};
     std::vector<double> dates(r.nt);
     for (int j = 0; j < r.nt; ++j) dates[j] = r.dtau * j;
     const char* prec = r.precision == HJM_PRECISION_FP64 ? "fp64" : "mixed";
@@ -1233,11 +1320,12 @@ hjm_status hjm_write_report(hjm_ctx* ctx, const char* path, int32_t format)
                      "\"n_tenor\": %d, \"sampled_dates\": %d, \"seed\": %llu, \"path_offset\": %llu, "
                      "\"precision\": \"%s\", \"vol_form\": \"%s\", \"hazard\": %.17g, \"recovery\": %.17g, "
                      "\"pfe_quantile\": %.17g, \"checkpoint_every\": %d, \"external_normals\": %s, "
-                     "\"scheme\": \"%s\"},\n",
+                     "\"scheme\": \"%s\", \"remainder\": \"%s\"},\n",
                      (long long)r.n_paths, r.n_steps, r.dt, r.dtau, r.nt, r.n_dates - 1, (unsigned long long)r.seed,
                      (unsigned long long)r.path_offset, prec, kForms[r.vol_form], r.hazard, r.recovery,
                      r.pfe ? r.pfe_q : 0.0, r.ckpt, r.external_normals ? "true" : "false",
-                     r.scheme == HJM_SCHEME_PREDICTOR_CORRECTOR ? "predictor_corrector" : "euler");
+                     r.scheme == HJM_SCHEME_PREDICTOR_CORRECTOR ? "predictor_corrector" : "euler",
+                     kRemainders[r.remainder]);
         std::fprintf(f, "  \"cva\": %.17g,\n  \"cva_stderr\": %.17g,\n  \"dcva_dhazard\": %.17g,\n", r.cva,
                      r.cva_stderr, r.dhazard);
         put_array(f, "dates", dates);
@@ -1260,9 +1348,10 @@ hjm_status hjm_write_report(hjm_ctx* ctx, const char* path, int32_t format)
         std::fprintf(f, "key,value\n");
         std::fprintf(f,
                      "n_paths,%lld\nn_steps,%d\ndt,%.17g\ndtau,%.17g\nseed,%llu\nprecision,%s\nvol_form,%s\n"
-                     "scheme,%s\n",
+                     "scheme,%s\nremainder,%s\n",
                      (long long)r.n_paths, r.n_steps, r.dt, r.dtau, (unsigned long long)r.seed, prec,
-                     kForms[r.vol_form], r.scheme == HJM_SCHEME_PREDICTOR_CORRECTOR ? "predictor_corrector" : "euler");
+                     kForms[r.vol_form], r.scheme == HJM_SCHEME_PREDICTOR_CORRECTOR ? "predictor_corrector" : "euler",
+                     kRemainders[r.remainder]);
         std::fprintf(f, "hazard,%.17g\nrecovery,%.17g\ncva,%.17g\ncva_stderr,%.17g\ndcva_dhazard,%.17g\n", r.hazard,
                      r.recovery, r.cva, r.cva_stderr, r.dhazard);
         if (r.adjoint) {

@@ -48,6 +48,73 @@ __host__ __device__ inline size_t path_smem_bytes(int nt, int n_blocks, bool mix
     return b;
 }
 
+// Epilogue of the FP64 path kernels: the exposure profile E_j = max(sum_{i>j}
+// cf_i, 0) by FP64 suffix sums, the path's CVA contribution sum_j cvaw[j] E_j,
+// the CTA's partial sums (dates 0..B, then sum c and sum c^2) and, if asked,
+// the exposure rows of the CTA's paths to HBM.  cf_s rows 1..B hold the cash
+// flows, column tid private to its thread; e_s (B+1 rows) may alias cf_s one
+// row up: row j of e_s is written after row j+1 of cf_s, the one aliased, is read.
+template <int kCta>
+__device__ __forceinline__ void fp64_epilogue(const PathParams<double>& P, const double* cf_s, double* e_s,
+                                              double* red_s, double* __restrict__ partials,
+                                              double* __restrict__ estore, int64_t cta_base, bool active)
+{
+    const int tid = threadIdx.x;
+    const int B = P.n_blocks;
+    double v = 0.0, cva_c = 0.0;
+    e_s[B * kCta + tid] = 0.0;
+    for (int j = B - 1; j >= 0; --j) {
+        v += cf_s[(j + 1) * kCta + tid];
+        double e = (v > 0.0) ? v : 0.0;
+        if (!active) e = 0.0;
+        e_s[j * kCta + tid] = e;
+        cva_c = fma(P.cvaw[j], e, cva_c);
+    }
+    __syncthreads();
+
+    // CTA partial sums: dates 0..B, then sum c and sum c^2
+    const int warp = tid >> 5, lane = tid & 31;
+    const int R = B + 3;
+    for (int j = warp; j <= B; j += kCta / 32) {
+        double sum = 0.0;
+#pragma unroll
+        for (int q = 0; q < kCta / 32; ++q) sum += e_s[j * kCta + lane + 32 * q];
+        sum = warp_sum(sum);
+        if (lane == 0) partials[(size_t)blockIdx.x * R + j] = sum;
+    }
+    {
+        const double s1 = warp_sum(cva_c), s2 = warp_sum(cva_c * cva_c);
+        if (lane == 0) {
+            red_s[warp] = s1;
+            red_s[kCta / 32 + warp] = s2;
+        }
+    }
+    if (P.store_exposures) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+        double s1 = 0.0, s2 = 0.0;
+        for (int w = 0; w < kCta / 32; ++w) {
+            s1 += red_s[w];
+            s2 += red_s[kCta / 32 + w];
+        }
+        partials[(size_t)blockIdx.x * R + B + 1] = s1;
+        partials[(size_t)blockIdx.x * R + B + 2] = s2;
+        if (P.store_exposures) {
+            // date rows of this CTA's paths, smem -> HBM with the bulk-copy (TMA) engine
+            const int64_t cnt = (P.n_paths - cta_base < kCta) ? (P.n_paths - cta_base) : kCta;
+            const uint32_t bytes = (uint32_t)(((cnt + 1) / 2) * 2 * sizeof(double));
+            for (int j = 0; j <= B; ++j) {
+                double* dst = estore + (size_t)j * (size_t)P.ld + (size_t)cta_base;
+                const uint32_t src = (uint32_t)__cvta_generic_to_shared(e_s + (size_t)j * kCta);
+                asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
+                             :: "l"(dst), "r"(src), "r"(bytes) : "memory");
+            }
+            asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+            asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+        }
+    }
+}
+
 // Discount sums by block-sum recovery.  Over one block of Euler steps
 // n = n0 .. n0+stride-1 the states h_n = A h_{n-1} + xi_n sum to
 //     (I - A) H = sum_n xi_n - A (h_end - h_start),   H = sum_n h_n,
@@ -235,60 +302,167 @@ __global__ void __launch_bounds__(kFp64Cta, 4)
         sample(b + 1);
     }
 
-    // exposure profile E_j = max(sum_{i>j} cf_i, 0), FP64 suffix sums, and the
-    // path's CVA contribution sum_j cvaw[j] E_j
-    double* e_s = work_s;
-    double v = 0.0, cva_c = 0.0;
-    e_s[B * kCta + tid] = 0.0;
-    for (int j = B - 1; j >= 0; --j) {
-        v += cf_s[(j + 1) * kCta + tid];
-        double e = (v > 0.0) ? v : 0.0;
-        if (!active) e = 0.0;
-        e_s[j * kCta + tid] = e;
-        cva_c = fma(P.cvaw[j], e, cva_c);
-    }
-    __syncthreads();
+    fp64_epilogue<kCta>(P, cf_s, work_s, red_s, partials, estore, cta_base, active);
+}
 
-    // CTA partial sums: dates 0..B, then sum c and sum c^2
-    const int warp = tid >> 5, lane = tid & 31;
-    const int R = B + 3;
-    for (int j = warp; j <= B; j += kCta / 32) {
-        double sum = 0.0;
+// Response form of the FP64 path (polynomial volatility, at most kRespDates
+// sampled dates).  The remainder hc of the polynomial decomposition starts at
+// zero, is driven only at the last tenor, by kappa W_{n-1} at step n (kappa =
+// -2 c dtau^2, W before the step's update), and is otherwise convected by A.
+// So after step K its value at tenor j and its running sum are
+//     hc_K[j]               = sum_{n<=K} G_j(K - n)  kappa W_{n-1},  G_j(m) = (A^m e_L)[j],
+//     sum_{K'<=K} hc_K'[j]  = sum_{n<=K} CG_j(K - n) kappa W_{n-1},  CG_j(m) = sum_{r<=m} G_j(r),
+// exact in exact arithmetic.  The pricing reads hc only at tenor j at date
+// j's sampling step K_j = j stride - 1 (its value and, for the discount, its
+// running sum), so the kernel keeps those two numbers per date still to be
+// sampled and adds one term to each per step: 2 (B - b) FMAs in block b, in
+// place of the convection of every live tenor and the block-end discount
+// recovery.  G_j(m) vanishes for m < L - j (the remainder's support reaches
+// one tenor further down per step), so a date takes no term while its lag is
+// that short.
+//
+// The accumulators of date j sit in slot r = B - j.  At step s of block b the
+// dates with a nonzero term are j = b + q for q_min <= q <= B - b, q_min the
+// least q with lag q stride - 1 - s >= L - b - q: slots 0 .. n_act - 1, a
+// prefix.  A switch on n_act enters a fall-through chain of the terms at slot
+// n_act - 1 (Duff's device): the skipped terms issue nothing, where a
+// predicated loop would still issue their FMAs to the FP64 pipe.  The impulse
+// responses come from response_table_kernel.
+constexpr int kRespDates = 24;                // dates the response form holds (slots 0 .. 22)
+constexpr int kRespSlots = kRespDates - 1;    // dates 2 .. B (date 1 is priced at spot)
+constexpr int kRespRow = 24;                  // response-table row: one double2 per slot, padded
+
+__host__ __device__ inline size_t resp_smem_bytes(int n_blocks)
+{
+    // cf_s [B+2][kCta] (the epilogue's exposures alias it one row up), red_s
+    return ((size_t)n_blocks + 2) * kFp64Cta * 8 + 2 * (kFp64Cta / 32) * 8;
+}
+
+template <int NT, bool EXT, bool TRI>
+__global__ void __launch_bounds__(kFp64Cta, 6)
+    path_kernel_fp64_resp(const __grid_constant__ PathParams<double> P, const double2* __restrict__ resp,
+                          const double* __restrict__ ext, double* __restrict__ partials,
+                          double* __restrict__ estore)
+{
+    constexpr int kCta = kFp64Cta;
+    constexpr int L = NT - 1;
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int tid = threadIdx.x;
+    const int B = P.n_blocks;
+    double* cf_s = reinterpret_cast<double*>(smem);
+    double* red_s = cf_s + (size_t)(B + 2) * kCta;
+
+    const int64_t cta_base = (int64_t)blockIdx.x * kCta;
+    const int64_t lp = cta_base + tid;  // path index within this launch
+    const bool active = lp < P.n_paths;
+    const uint64_t gpath = P.path_offset + (uint64_t)lp;
+
+    // remainder at tenor j and its running sum, slot B - j, for the dates j
+    // not yet sampled
+    double a[kRespSlots], ai[kRespSlots];
 #pragma unroll
-        for (int q = 0; q < kCta / 32; ++q) sum += e_s[j * kCta + lane + 32 * q];
-        sum = warp_sum(sum);
-        if (lane == 0) partials[(size_t)blockIdx.x * R + j] = sum;
-    }
-    {
-        const double s1 = warp_sum(cva_c), s2 = warp_sum(cva_c * cva_c);
-        if (lane == 0) {
-            red_s[warp] = s1;
-            red_s[kCta / 32 + warp] = s2;
-        }
-    }
-    if (P.store_exposures) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    __syncthreads();
-    if (tid == 0) {
-        double s1 = 0.0, s2 = 0.0;
-        for (int w = 0; w < kCta / 32; ++w) {
-            s1 += red_s[w];
-            s2 += red_s[kCta / 32 + w];
-        }
-        partials[(size_t)blockIdx.x * R + B + 1] = s1;
-        partials[(size_t)blockIdx.x * R + B + 2] = s2;
-        if (P.store_exposures) {
-            // date rows of this CTA's paths, smem -> HBM with the bulk-copy (TMA) engine
-            const int64_t cnt = (P.n_paths - cta_base < kCta) ? (P.n_paths - cta_base) : kCta;
-            const uint32_t bytes = (uint32_t)(((cnt + 1) / 2) * 2 * sizeof(double));
-            for (int j = 0; j <= B; ++j) {
-                double* dst = estore + (size_t)j * (size_t)P.ld + (size_t)cta_base;
-                const uint32_t src = (uint32_t)__cvta_generic_to_shared(e_s + (size_t)j * kCta);
-                asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
-                             :: "l"(dst), "r"(src), "r"(bytes) : "memory");
+    for (int r = 0; r < kRespSlots; ++r) a[r] = ai[r] = 0.0;
+    double S = 0.0, U = 0.0, W = 0.0;     // parallel, tilt and curvature parts
+    double sS = 0.0, sU = 0.0, sW = 0.0;  // their running sums over the evolved steps
+
+    // price date i from the sampled numeraire (x_i, D_i)
+    auto sample = [&](int i) {
+        const double tau = P.tau[i];
+        const double hc = i >= 2 ? select_reg<kRespSlots, double>(a, B - i) : 0.0;
+        const double hcs = i >= 2 ? select_reg<kRespSlots, double>(ai, B - i) : 0.0;
+        const double x = P.psamp[i] + (fma(tau, fma(tau, W, U), S) + hc);
+        const double acc = fma(tau, fma(tau, sW, sU), sS) + hcs;
+        const double D = exp(-(P.psum[i] + acc) * P.dt);
+        const double Lb = P.m * (exp(x / P.m) - 1.0);
+        cf_s[i * kCta + tid] = D * (P.payA[i] * Lb - P.payB[i]);
+    };
+
+    sample(1);
+    const int st1 = P.stride + 1;
+    for (int b = 1; b < B; ++b) {
+        const double2* row = resp + (size_t)b * P.stride * kRespRow;
+        const int nlive = B - b;
+        for (int s = 0; s < P.stride; ++s) {
+            const int n = b * P.stride + s;
+            double phi0, phi1, phi2;
+            draw_phi<double, EXT>(ext, gpath, active ? lp : 0, P.n_paths, n, P.rk0, P.rk1, phi0, phi1, phi2);
+            // q_min = ceil((s + 1 + L - b) / (stride + 1)) >= 1 (uniform)
+            const int q_min = (s + 1 + L - b + P.stride) / st1;
+            const int n_act = nlive - q_min + 1;
+            const double2* rr = row + (size_t)s * kRespRow;
+#define HJM_RESP_TERM(R)                    \
+    case R + 1: {                           \
+        const double2 k = __ldg(rr + R);    \
+        a[R] = fma(k.x, W, a[R]);           \
+        ai[R] = fma(k.y, W, ai[R]);         \
+    }                                       \
+        [[fallthrough]];
+            switch (n_act) {
+                HJM_RESP_TERM(22) HJM_RESP_TERM(21) HJM_RESP_TERM(20) HJM_RESP_TERM(19) HJM_RESP_TERM(18)
+                HJM_RESP_TERM(17) HJM_RESP_TERM(16) HJM_RESP_TERM(15) HJM_RESP_TERM(14) HJM_RESP_TERM(13)
+                HJM_RESP_TERM(12) HJM_RESP_TERM(11) HJM_RESP_TERM(10) HJM_RESP_TERM(9) HJM_RESP_TERM(8)
+                HJM_RESP_TERM(7) HJM_RESP_TERM(6) HJM_RESP_TERM(5) HJM_RESP_TERM(4) HJM_RESP_TERM(3)
+                HJM_RESP_TERM(2) HJM_RESP_TERM(1) HJM_RESP_TERM(0)
+                default:
+                    break;
             }
-            asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-            asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+#undef HJM_RESP_TERM
+            // S' = S + c dtau U + c dtau^2 W + sum_k svc[k][0] phi_k, etc. (old
+            // U, W on the right; factor k of degree <= k drops 3 terms)
+            double Sn = fma(P.svc[0][0], phi0, fma(P.k2, W, fma(P.k1, U, S)));
+            Sn = fma(P.svc[2][0], phi2, fma(P.svc[1][0], phi1, Sn));
+            double Un = fma(P.svc[2][1], phi2, fma(P.svc[1][1], phi1, fma(2.0 * P.k1, W, U)));
+            double Wn = fma(P.svc[2][2], phi2, W);
+            if constexpr (!TRI) {
+                Un = fma(P.svc[0][1], phi0, Un);
+                Wn = fma(P.svc[1][2], phi1, fma(P.svc[0][2], phi0, Wn));
+            }
+            S = Sn;
+            U = Un;
+            W = Wn;
+            sS += S;
+            sU += U;
+            sW += W;
         }
+        sample(b + 1);
+    }
+    fp64_epilogue<kCta>(P, cf_s, cf_s + kCta, red_s, partials, estore, cta_base, active);
+}
+
+// Impulse responses of the convection at the sampled tenors, for the response
+// form: entry (row b stride + s, column r = B - j) of resp holds kappa
+// (G_j(lag), CG_j(lag)), lag = (j - b) stride - 1 - s the distance from step
+// s of block b to date j's sampling step, for 1 <= b < j <= B <= kRespDates;
+// G_j(m) = (A^m e_L)[j] by m applications of the upwind step (backward
+// difference at the last tenor, simulation_cpu.h:96-108) and CG_j(m) =
+// sum_{r<=m} G_j(r).  Every lag m in [0, (j-1) stride - 1] of date j maps to
+// exactly one entry (q = j - b = m / stride + 1, s = q stride - 1 - m).  One
+// CTA of kMaxTenor threads, thread t holding tenor t.
+__global__ void __launch_bounds__(kMaxTenor)
+    response_table_kernel(int nt, double c, double kappa, int stride, int B, double2* __restrict__ resp)
+{
+    __shared__ double v_s[kMaxTenor];
+    const int t = threadIdx.x;
+    const int L = nt - 1;
+    double v = (t == L) ? 1.0 : 0.0;
+    double cum = 0.0;
+    const int M = (B - 1) * stride - 1;  // the longest lag read
+    for (int m = 0; m <= M; ++m) {
+        cum += v;
+        if (t >= 2 && t <= B) {
+            const int q = m / stride + 1;
+            const int b = t - q;
+            if (b >= 1)
+                resp[((size_t)b * stride + (size_t)(q * stride - 1 - m)) * kRespRow + (B - t)] =
+                    make_double2(kappa * v, kappa * cum);
+        }
+        v_s[t] = v;
+        __syncthreads();
+        if (t < L)
+            v += c * (v_s[t + 1] - v);
+        else if (t == L)
+            v += c * (v - v_s[L - 1]);
+        __syncthreads();
     }
 }
 
@@ -665,11 +839,31 @@ static cudaError_t launch_fp64_t(const PathParams<double>& P, const double* ext,
     return cudaGetLastError();
 }
 
+template <int NT, bool EXT, bool TRI>
+static cudaError_t launch_fp64_resp_t(const PathParams<double>& P, const double2* resp, const double* ext,
+                                      double* partials, double* estore, cudaStream_t s)
+{
+    const size_t smem = resp_smem_bytes(P.n_blocks);
+    auto k = path_kernel_fp64_resp<NT, EXT, TRI>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const int64_t grid = (P.n_paths + kFp64Cta - 1) / kFp64Cta;
+    k<<<(unsigned)grid, kFp64Cta, smem, s>>>(P, resp, ext, partials, estore);
+    return cudaGetLastError();
+}
+
 template <int NT>
-static cudaError_t launch_fp64_nt(const PathParams<double>& P, bool poly, const double* ext, double* partials,
-                                  double* estore, cudaStream_t s)
+static cudaError_t launch_fp64_nt(const PathParams<double>& P, bool poly, const double2* resp, const double* ext,
+                                  double* partials, double* estore, cudaStream_t s)
 {
     const bool tri = poly && P.svc[0][1] == 0.0 && P.svc[0][2] == 0.0 && P.svc[1][2] == 0.0;
+    if (resp) {
+        if (!poly || P.n_blocks > kRespDates) return cudaErrorInvalidValue;
+        if (ext) return tri ? launch_fp64_resp_t<NT, true, true>(P, resp, ext, partials, estore, s)
+                            : launch_fp64_resp_t<NT, true, false>(P, resp, ext, partials, estore, s);
+        return tri ? launch_fp64_resp_t<NT, false, true>(P, resp, ext, partials, estore, s)
+                   : launch_fp64_resp_t<NT, false, false>(P, resp, ext, partials, estore, s);
+    }
     if (ext) return tri    ? launch_fp64_t<NT, true, kFormPolyTri>(P, ext, partials, estore, s)
                     : poly ? launch_fp64_t<NT, true, kFormPoly>(P, ext, partials, estore, s)
                            : launch_fp64_t<NT, true, kFormTable>(P, ext, partials, estore, s);
@@ -678,12 +872,24 @@ static cudaError_t launch_fp64_nt(const PathParams<double>& P, bool poly, const 
                   : launch_fp64_t<NT, false, kFormTable>(P, ext, partials, estore, s);
 }
 
-cudaError_t launch_path_fp64(int nt, const PathParams<double>& P, bool poly, const double* ext, double* partials,
-                             double* estore, cudaStream_t s)
+cudaError_t launch_path_fp64(int nt, const PathParams<double>& P, bool poly, const double2* resp, const double* ext,
+                             double* partials, double* estore, cudaStream_t s)
 {
-    if (nt == 51) return launch_fp64_nt<51>(P, poly, ext, partials, estore, s);
-    if (nt == 61) return launch_fp64_nt<61>(P, poly, ext, partials, estore, s);
+    if (nt == 51) return launch_fp64_nt<51>(P, poly, resp, ext, partials, estore, s);
+    if (nt == 61) return launch_fp64_nt<61>(P, poly, resp, ext, partials, estore, s);
     return cudaErrorInvalidValue;
+}
+
+int response_max_dates() { return kRespDates; }
+
+size_t response_table_elems(int stride, int n_blocks) { return (size_t)n_blocks * stride * kRespRow; }
+
+cudaError_t launch_response_table(int nt, double c, double kappa, int stride, int n_blocks, double2* resp,
+                                  cudaStream_t s)
+{
+    if (nt < 2 || nt > kMaxTenor || n_blocks > kRespDates || n_blocks >= nt || stride < 1) return cudaErrorInvalidValue;
+    response_table_kernel<<<1, kMaxTenor, 0, s>>>(nt, c, kappa, stride, n_blocks, resp);
+    return cudaGetLastError();
 }
 
 template <int NT, bool EXT, bool POLY>

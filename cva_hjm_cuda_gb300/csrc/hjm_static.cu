@@ -267,7 +267,7 @@ hjm_status hjm_run_static(void* cuda_stream, int32_t n_tenor, double dtau, const
         PathParams<double> P;
         static_params<double>(n_tenor, dtau, spot_host, vol_host, drift, payA, payB, (int)stride, B, n_paths, dt,
                               seed, path_offset, hazard_rate, recovery, P, F);
-        STATIC_CUDA(launch_path_fp64(n_tenor, P, false, nullptr, partials, nullptr, s));
+        STATIC_CUDA(launch_path_fp64(n_tenor, P, false, nullptr, nullptr, partials, nullptr, s));
     }
     STATIC_CUDA(launch_reduce(partials, n_ctas, R, sums, F, result, s));
     double res[kResLen];

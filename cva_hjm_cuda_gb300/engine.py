@@ -108,6 +108,19 @@ class HJMEngine:
         "predictor_corrector"."""
         self._check(self.lib.hjm_ctx_set_scheme(self.ctx, {"euler": 0, "predictor_corrector": 1}[scheme]))
 
+    def set_remainder_form(self, form: str = "auto") -> None:
+        """FP64 form of the decomposition's remainder: "convect" (over the live
+        tenors every step), "response" (impulse responses at the sampled tenors,
+        at most 24 dates) or "auto" (the cheaper one for the run)."""
+        self._check(self.lib.hjm_ctx_set_remainder_form(self.ctx, {"auto": 0, "convect": 1, "response": 2}[form]))
+
+    def remainder_form(self) -> str:
+        """The remainder form of the last valuation enqueued: "none" (table
+        step), "convect" or "response"."""
+        form = C.c_int32(0)
+        self._check(self.lib.hjm_ctx_remainder_form(self.ctx, C.byref(form)))
+        return ("none", "convect", "response")[form.value]
+
     def write_report(self, path, fmt: str = "json") -> None:
         """The last valuation (or adjoint run) with its inputs, as JSON or CSV."""
         code = {"json": 0, "csv": 1}[fmt]

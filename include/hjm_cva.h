@@ -105,6 +105,26 @@ hjm_status hjm_ctx_set_scheme(hjm_ctx* ctx, int32_t scheme);
 hjm_status hjm_ctx_set_vol_decomposition(hjm_ctx* ctx, int32_t enable);
 hjm_status hjm_ctx_vol_decomposition(hjm_ctx* ctx, int32_t* active);
 
+/* FP64 form of the decomposition's remainder.  The remainder is driven only at
+ * the last tenor and priced only at each date's own tenor, so an FP64 Euler
+ * valuation either convects it over the live tenors every step
+ * (HJM_REMAINDER_CONVECT) or carries, for each date still to be sampled, its
+ * value and running sum as sums of impulse responses of the convection
+ * (HJM_REMAINDER_RESPONSE: two FMAs per such date per step, at most
+ * HJM_RESPONSE_MAX_DATES dates, a run with more fails with
+ * HJM_ERR_INVALID_ARGUMENT).  HJM_REMAINDER_AUTO (default) takes the form with
+ * fewer FP64 operations for the run.  The forms agree to rounding; mixed
+ * precision, the predictor-corrector scheme and the table step do not use
+ * this setting.  The report names the form a valuation ran ("remainder"). */
+#define HJM_REMAINDER_AUTO 0
+#define HJM_REMAINDER_CONVECT 1
+#define HJM_REMAINDER_RESPONSE 2
+#define HJM_RESPONSE_MAX_DATES 24
+hjm_status hjm_ctx_set_remainder_form(hjm_ctx* ctx, int32_t form);
+/* The remainder form of the last valuation enqueued: 0 none (the table step),
+ * HJM_REMAINDER_CONVECT or HJM_REMAINDER_RESPONSE. */
+hjm_status hjm_ctx_remainder_form(hjm_ctx* ctx, int32_t* form);
+
 /* ---- inputs --------------------------------------------------------------- */
 /* Market: spot forward curve, volatility factors, and the drift.  With
  * drift_host == NULL the Musiela no-arbitrage drift is computed in FP64 by the

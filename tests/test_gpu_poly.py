@@ -228,3 +228,100 @@ def test_general_quadratic_factors_vs_oracle(engine, precision):
     # the same market as a table is detected as the same (general) form
     engine.set_market(mk)
     assert engine.vol_form() == "poly"
+
+
+# ---------------------------------------------------------------------------
+# FP64 remainder forms: convected over the live tenors, or impulse responses
+# at the sampled tenors (at most 24 dates)
+# ---------------------------------------------------------------------------
+@pytest.fixture
+def remainder_form(engine):
+    yield engine.set_remainder_form
+    engine.set_remainder_form("auto")
+
+
+def _oracle_run(engine, mk, sw, cfg):
+    normals = engine.dump_normals(cfg.n_paths, cfg.n_steps, cfg.seed)
+    x = O.exposure_paths(mk, sw, cfg.n_steps, cfg.dt, normals)
+    ee = O.expected_exposure(x)
+    nd = cfg.n_steps // int(round(mk.dtau / cfg.dt))
+    cva, _ = O.cva(ee, nd + 1, mk.dtau, cfg.hazard, cfg.recovery)
+    return x, ee, cva, O.pfe(x, nd + 1, cfg.pfe_quantile)
+
+
+@pytest.mark.parametrize("nt,coef", [(51, DEFAULT_VOL_COEFFS), (51, FULL_COEFFS), (61, DEFAULT_VOL_COEFFS)],
+                         ids=["51-tri", "51-general", "61-tri"])
+def test_remainder_forms_agree_and_match_oracle(engine, remainder_form, nt, coef):
+    mk = _poly_market(engine, nt=nt, coef=coef)
+    sw = Swap(n_tenor=nt)
+    engine.set_swap(sw)
+    cfg = RunConfig(n_paths=3000, seed=77)
+    out = {}
+    engine.keep_exposures(True)
+    try:
+        for form in ("convect", "response"):
+            remainder_form(form)
+            v = engine.run(cfg, "fp64")
+            assert engine.remainder_form() == form
+            out[form] = (v, engine.exposures())
+    finally:
+        engine.keep_exposures(False)
+    (vc, xc), (vr, xr) = out["convect"], out["response"]
+    _assert_rel(xr, xc, 1e-12, "exposures response vs convect")
+    _assert_rel(vr.ee, vc.ee, 1e-12, "EE response vs convect")
+    _assert_rel(vr.cva, vc.cva, 1e-12, "CVA response vs convect")
+    x, ee, cva, pfe = _oracle_run(engine, mk, sw, cfg)
+    _assert_rel(xr, x[:, :21].T, FP64_RTOL, "exposures vs oracle")
+    _assert_rel(vr.ee, ee, FP64_RTOL, "EE vs oracle")
+    _assert_rel(vr.cva, cva, FP64_RTOL, "CVA vs oracle")
+    _assert_rel(vr.pfe[:21], pfe, FP64_RTOL, "PFE vs oracle")
+
+
+@pytest.mark.parametrize("n_paths,n_steps,dt", [(1, 1000, 0.01), (63, 500, 0.02), (257, 1200, 0.01),
+                                                (100, 250, 0.01), (64, 1000, 0.005), (100, 50, 0.05)],
+                         ids=["1-path", "stride25", "24-dates", "5-dates", "stride100", "stride10-all-zero"])
+def test_response_form_shapes_vs_oracle(engine, remainder_form, n_paths, n_steps, dt):
+    """Ragged path counts, strides 10 to 100, 5 to 24 dates (the form's maximum);
+    with stride 10 the remainder never reaches a sampled tenor (all responses zero)."""
+    mk = _poly_market(engine)
+    stride = int(round(mk.dtau / dt))
+    sw = Swap(n_periods=max(n_steps // stride, 1))
+    engine.set_swap(sw)
+    remainder_form("response")
+    cfg = RunConfig(n_paths=n_paths, n_steps=n_steps, dt=dt, seed=5)
+    v = engine.run(cfg, "fp64")
+    assert engine.remainder_form() == "response"
+    x, ee, cva, pfe = _oracle_run(engine, mk, sw, cfg)
+    nd = n_steps // stride
+    _assert_rel(v.ee[:nd + 1], ee[:nd + 1], FP64_RTOL, "EE")
+    _assert_rel(v.cva, cva, FP64_RTOL, "CVA")
+
+
+def test_remainder_form_choice_and_limits(engine, remainder_form, tmp_path):
+    import json
+
+    from cva_hjm_cuda_gb300 import _lib
+
+    _poly_market(engine)
+    engine.set_swap(Swap())
+    engine.run(RunConfig(n_paths=256), "fp64")
+    assert engine.remainder_form() == "response"  # 20 dates on 51 tenors: the cheaper form
+    engine.write_report(tmp_path / "r.json")
+    assert json.loads((tmp_path / "r.json").read_text())["run"]["remainder"] == "response"
+    engine.run(RunConfig(n_paths=256), "mixed")
+    assert engine.remainder_form() == "convect"  # mixed precision always convects
+    _poly_market(engine, nt=61)
+    engine.set_swap(Swap(n_tenor=61, n_periods=60))
+    cfg30 = RunConfig(n_paths=256, n_steps=3000)
+    engine.run(cfg30, "fp64")
+    assert engine.remainder_form() == "convect"  # 60 dates
+    remainder_form("response")
+    with pytest.raises(_lib.HJMError) as ei:
+        engine.run(cfg30, "fp64")
+    assert "24 dates" in str(ei.value)
+    engine.set_market(Market(vol=Market().vol * (1.0 + 0.1 * np.cos(np.arange(51) / 7.0))[None, :]))
+    engine.set_swap(Swap())
+    engine.run(RunConfig(n_paths=256), "fp64")
+    assert engine.remainder_form() == "none"  # table step: no remainder
+    with pytest.raises(_lib.HJMError):
+        _lib.check(engine.lib.hjm_ctx_set_remainder_form(engine.ctx, 7), engine.ctx)
