@@ -660,12 +660,12 @@ static hjm_status ensure_response_table(hjm_ctx* ctx, const RunShape& sh, const 
     if (k.valid && k.nt == ctx->nt && k.stride == sh.stride && k.B == sh.B && k.c == P.c && k.kappa == kappa)
         return HJM_OK;
     k.valid = false;
-    const size_t bytes = sizeof(double2) * response_table_elems(sh.stride, sh.B);
+    const size_t bytes = sizeof(float4) * response_table_elems(sh.stride, sh.B);
     if (bytes > ctx->resp.bytes)
         HJM_CUDA(ctx, ctx->resp.ensure(bytes));  // cudaFree waits for the device
     else
         HJM_CUDA(ctx, cudaStreamWaitEvent(s, ctx->resp_used, 0));
-    HJM_CUDA(ctx, launch_response_table(ctx->nt, P.c, kappa, sh.stride, sh.B, (double2*)ctx->resp.p, s));
+    HJM_CUDA(ctx, launch_response_table(ctx->nt, P.c, kappa, sh.stride, sh.B, (float4*)ctx->resp.p, s));
     ctx->stat_launches += 1;
     k.nt = ctx->nt;
     k.stride = sh.stride;
@@ -750,7 +750,7 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
             st = ensure_response_table(ctx, sh, P, s);
             if (st != HJM_OK) return st;
         }
-        HJM_CUDA(ctx, launch_path_fp64(ctx->nt, P, use_poly_path(ctx), resp ? (const double2*)ctx->resp.p : nullptr,
+        HJM_CUDA(ctx, launch_path_fp64(ctx->nt, P, use_poly_path(ctx), resp ? (const float4*)ctx->resp.p : nullptr,
                                        ext_dev, (double*)ctx->partials.p, store ? (double*)ctx->estore.p : nullptr,
                                        s));
         if (resp) HJM_CUDA(ctx, cudaEventRecord(ctx->resp_used, s));

@@ -321,6 +321,19 @@ __global__ void __launch_bounds__(kFp64Cta, 4)
 // one tenor further down per step), so a date takes no term while its lag is
 // that short.
 //
+// Both sums are carried in double-FP32 arithmetic on the FP32 pipe (76 times
+// the FP64 pipe's rate on GB300): the table holds each coefficient as a pair
+// of floats hi + lo (48 significant bits), W is split by truncation into
+// W_hi + W_lo (integer operations and one exact FP64 subtraction), the
+// product's leading term is made exact by an FMA and the accumulation by
+// Knuth's two-sum, packed {value, running sum} in FP32x2 instructions.  The
+// relative error of a date's sum stays below ~1e-13 of its magnitude, and the
+// remainder at a sampled tenor is small: |hc| <= 7e-5 for 24 dates, the most
+// this form takes, against a curve of ~0.03 (the far tail of the transport
+// from the last tenor; below 1e-6 for the 10y swap on 51 tenors), so its
+// rounding stays within an ulp of the FP64 curve.  Per step the FP64 pipe
+// does only the polynomial parts.
+//
 // The accumulators of date j sit in slot r = B - j.  At step s of block b the
 // dates with a nonzero term are j = b + q for q_min <= q <= B - b, q_min the
 // least q with lag q stride - 1 - s >= L - b - q: slots 0 .. n_act - 1, a
@@ -330,7 +343,55 @@ __global__ void __launch_bounds__(kFp64Cta, 4)
 // responses come from response_table_kernel.
 constexpr int kRespDates = 24;                // dates the response form holds (slots 0 .. 22)
 constexpr int kRespSlots = kRespDates - 1;    // dates 2 .. B (date 1 is priced at spot)
-constexpr int kRespRow = 24;                  // response-table row: one double2 per slot, padded
+constexpr int kRespRow = 24;                  // response-table row: one float4 per slot, padded
+
+// A double as hi + lo + O(2^-47 |d|), hi and lo FP32, by truncation of the
+// significand with integer operations (conversion instructions issue on the
+// FP64 pipe); hi_d is hi as a double.  Magnitudes below the FP32 normal range
+// (2^-126) become zero, magnitudes above it saturate.
+__device__ __forceinline__ float trunc_f32(double d, double& as_double)
+{
+    const unsigned long long u = (unsigned long long)__double_as_longlong(d);
+    const uint32_t top = (uint32_t)(u >> 32);
+    int e = (int)((top >> 20) & 0x7ffu) - 1023 + 127;
+    const uint32_t sign = top & 0x80000000u;
+    if (e <= 0) {
+        as_double = 0.0;
+        return __uint_as_float(sign);
+    }
+    uint32_t m = (uint32_t)(u >> 29) & 0x7fffffu;
+    if (e > 254) {
+        e = 254;
+        m = 0x7fffffu;
+    }
+    as_double = __longlong_as_double((long long)(u & ~((1ull << 29) - 1)));
+    return __uint_as_float(sign | ((uint32_t)e << 23) | m);
+}
+
+__device__ __forceinline__ void split_f64(double d, float& hi, float& lo)
+{
+    double hi_d, unused;
+    hi = trunc_f32(d, hi_d);
+    lo = trunc_f32(d - hi_d, unused);  // exact subtraction: the truncated bits
+}
+
+// (A, Al) += (kh + kl) (wh + wl) in double-FP32, both lanes: the product's
+// leading term exact by FMA, the cross terms in FP32, kl wl (2^-48) dropped;
+// Knuth's two-sum keeps A + Al exact up to the FP32 rounding of Al.
+__device__ __forceinline__ void df_acc(float2& A, float2& Al, float2 kh, float2 kl, float2 wh, float2 wl)
+{
+    const float2 m1 = make_float2(-1.0f, -1.0f);
+    const float2 p = __fmul2_rn(kh, wh);
+    float2 e = __ffma2_rn(kh, wh, __fmul2_rn(p, m1));
+    e = __ffma2_rn(kh, wl, e);
+    e = __ffma2_rn(kl, wh, e);
+    const float2 sum = __fadd2_rn(A, p);
+    const float2 bp = __ffma2_rn(A, m1, sum);   // sum - A
+    const float2 ap = __ffma2_rn(bp, m1, sum);  // sum - bp
+    const float2 err = __fadd2_rn(__ffma2_rn(ap, m1, A), __ffma2_rn(bp, m1, p));
+    Al = __fadd2_rn(Al, __fadd2_rn(err, e));
+    A = sum;
+}
 
 __host__ __device__ inline size_t resp_smem_bytes(int n_blocks)
 {
@@ -340,7 +401,7 @@ __host__ __device__ inline size_t resp_smem_bytes(int n_blocks)
 
 template <int NT, bool EXT, bool TRI>
 __global__ void __launch_bounds__(kFp64Cta, 6)
-    path_kernel_fp64_resp(const __grid_constant__ PathParams<double> P, const double2* __restrict__ resp,
+    path_kernel_fp64_resp(const __grid_constant__ PathParams<double> P, const float4* __restrict__ resp,
                           const double* __restrict__ ext, double* __restrict__ partials,
                           double* __restrict__ estore)
 {
@@ -357,19 +418,23 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
     const bool active = lp < P.n_paths;
     const uint64_t gpath = P.path_offset + (uint64_t)lp;
 
-    // remainder at tenor j and its running sum, slot B - j, for the dates j
-    // not yet sampled
-    double a[kRespSlots], ai[kRespSlots];
+    // {remainder at tenor j, its running sum} as hi + lo pairs, slot B - j,
+    // for the dates j not yet sampled
+    float2 A[kRespSlots], Al[kRespSlots];
 #pragma unroll
-    for (int r = 0; r < kRespSlots; ++r) a[r] = ai[r] = 0.0;
+    for (int r = 0; r < kRespSlots; ++r) A[r] = Al[r] = make_float2(0.0f, 0.0f);
     double S = 0.0, U = 0.0, W = 0.0;     // parallel, tilt and curvature parts
     double sS = 0.0, sU = 0.0, sW = 0.0;  // their running sums over the evolved steps
 
     // price date i from the sampled numeraire (x_i, D_i)
     auto sample = [&](int i) {
         const double tau = P.tau[i];
-        const double hc = i >= 2 ? select_reg<kRespSlots, double>(a, B - i) : 0.0;
-        const double hcs = i >= 2 ? select_reg<kRespSlots, double>(ai, B - i) : 0.0;
+        double hc = 0.0, hcs = 0.0;
+        if (i >= 2) {
+            const float2 h = select_reg<kRespSlots, float2>(A, B - i), l = select_reg<kRespSlots, float2>(Al, B - i);
+            hc = widen_f32(h.x) + widen_f32(l.x);
+            hcs = widen_f32(h.y) + widen_f32(l.y);
+        }
         const double x = P.psamp[i] + (fma(tau, fma(tau, W, U), S) + hc);
         const double acc = fma(tau, fma(tau, sW, sU), sS) + hcs;
         const double D = exp(-(P.psum[i] + acc) * P.dt);
@@ -380,7 +445,7 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
     sample(1);
     const int st1 = P.stride + 1;
     for (int b = 1; b < B; ++b) {
-        const double2* row = resp + (size_t)b * P.stride * kRespRow;
+        const float4* row = resp + (size_t)b * P.stride * kRespRow;
         const int nlive = B - b;
         for (int s = 0; s < P.stride; ++s) {
             const int n = b * P.stride + s;
@@ -389,13 +454,15 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
             // q_min = ceil((s + 1 + L - b) / (stride + 1)) >= 1 (uniform)
             const int q_min = (s + 1 + L - b + P.stride) / st1;
             const int n_act = nlive - q_min + 1;
-            const double2* rr = row + (size_t)s * kRespRow;
-#define HJM_RESP_TERM(R)                    \
-    case R + 1: {                           \
-        const double2 k = __ldg(rr + R);    \
-        a[R] = fma(k.x, W, a[R]);           \
-        ai[R] = fma(k.y, W, ai[R]);         \
-    }                                       \
+            const float4* rr = row + (size_t)s * kRespRow;
+            float wh, wl;
+            split_f64(W, wh, wl);
+            const float2 wh2 = make_float2(wh, wh), wl2 = make_float2(wl, wl);
+#define HJM_RESP_TERM(R)                                                                          \
+    case R + 1: {                                                                                 \
+        const float4 k = __ldg(rr + R);                                                           \
+        df_acc(A[R], Al[R], make_float2(k.x, k.y), make_float2(k.z, k.w), wh2, wl2);              \
+    }                                                                                             \
         [[fallthrough]];
             switch (n_act) {
                 HJM_RESP_TERM(22) HJM_RESP_TERM(21) HJM_RESP_TERM(20) HJM_RESP_TERM(19) HJM_RESP_TERM(18)
@@ -431,7 +498,7 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
 
 // Impulse responses of the convection at the sampled tenors, for the response
 // form: entry (row b stride + s, column r = B - j) of resp holds kappa
-// (G_j(lag), CG_j(lag)), lag = (j - b) stride - 1 - s the distance from step
+// G_j(lag) and kappa CG_j(lag) as FP32 pairs {G hi, CG hi, G lo, CG lo}, lag = (j - b) stride - 1 - s the distance from step
 // s of block b to date j's sampling step, for 1 <= b < j <= B <= kRespDates;
 // G_j(m) = (A^m e_L)[j] by m applications of the upwind step (backward
 // difference at the last tenor, simulation_cpu.h:96-108) and CG_j(m) =
@@ -439,7 +506,7 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
 // exactly one entry (q = j - b = m / stride + 1, s = q stride - 1 - m).  One
 // CTA of kMaxTenor threads, thread t holding tenor t.
 __global__ void __launch_bounds__(kMaxTenor)
-    response_table_kernel(int nt, double c, double kappa, int stride, int B, double2* __restrict__ resp)
+    response_table_kernel(int nt, double c, double kappa, int stride, int B, float4* __restrict__ resp)
 {
     __shared__ double v_s[kMaxTenor];
     const int t = threadIdx.x;
@@ -452,9 +519,12 @@ __global__ void __launch_bounds__(kMaxTenor)
         if (t >= 2 && t <= B) {
             const int q = m / stride + 1;
             const int b = t - q;
-            if (b >= 1)
+            if (b >= 1) {
+                const double g = kappa * v, cg = kappa * cum;
+                const float gh = __double2float_rn(g), cgh = __double2float_rn(cg);
                 resp[((size_t)b * stride + (size_t)(q * stride - 1 - m)) * kRespRow + (B - t)] =
-                    make_double2(kappa * v, kappa * cum);
+                    make_float4(gh, cgh, __double2float_rn(g - (double)gh), __double2float_rn(cg - (double)cgh));
+            }
         }
         v_s[t] = v;
         __syncthreads();
@@ -840,7 +910,7 @@ static cudaError_t launch_fp64_t(const PathParams<double>& P, const double* ext,
 }
 
 template <int NT, bool EXT, bool TRI>
-static cudaError_t launch_fp64_resp_t(const PathParams<double>& P, const double2* resp, const double* ext,
+static cudaError_t launch_fp64_resp_t(const PathParams<double>& P, const float4* resp, const double* ext,
                                       double* partials, double* estore, cudaStream_t s)
 {
     const size_t smem = resp_smem_bytes(P.n_blocks);
@@ -853,7 +923,7 @@ static cudaError_t launch_fp64_resp_t(const PathParams<double>& P, const double2
 }
 
 template <int NT>
-static cudaError_t launch_fp64_nt(const PathParams<double>& P, bool poly, const double2* resp, const double* ext,
+static cudaError_t launch_fp64_nt(const PathParams<double>& P, bool poly, const float4* resp, const double* ext,
                                   double* partials, double* estore, cudaStream_t s)
 {
     const bool tri = poly && P.svc[0][1] == 0.0 && P.svc[0][2] == 0.0 && P.svc[1][2] == 0.0;
@@ -872,7 +942,7 @@ static cudaError_t launch_fp64_nt(const PathParams<double>& P, bool poly, const 
                   : launch_fp64_t<NT, false, kFormTable>(P, ext, partials, estore, s);
 }
 
-cudaError_t launch_path_fp64(int nt, const PathParams<double>& P, bool poly, const double2* resp, const double* ext,
+cudaError_t launch_path_fp64(int nt, const PathParams<double>& P, bool poly, const float4* resp, const double* ext,
                              double* partials, double* estore, cudaStream_t s)
 {
     if (nt == 51) return launch_fp64_nt<51>(P, poly, resp, ext, partials, estore, s);
@@ -884,7 +954,7 @@ int response_max_dates() { return kRespDates; }
 
 size_t response_table_elems(int stride, int n_blocks) { return (size_t)n_blocks * stride * kRespRow; }
 
-cudaError_t launch_response_table(int nt, double c, double kappa, int stride, int n_blocks, double2* resp,
+cudaError_t launch_response_table(int nt, double c, double kappa, int stride, int n_blocks, float4* resp,
                                   cudaStream_t s)
 {
     if (nt < 2 || nt > kMaxTenor || n_blocks > kRespDates || n_blocks >= nt || stride < 1) return cudaErrorInvalidValue;

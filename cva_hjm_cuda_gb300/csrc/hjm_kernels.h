@@ -51,11 +51,11 @@ constexpr int kFormPolyTri = 2;  // ... with factor k of degree <= k
 // poly: the volatility factors are polynomials of degree <= 2 in T (PathParams::svc);
 // resp: the response table of the polynomial form's remainder (the response
 // form, at most response_max_dates() dates), or null for the convected form
-cudaError_t launch_path_fp64(int nt, const PathParams<double>& P, bool poly, const double2* resp, const double* ext,
+cudaError_t launch_path_fp64(int nt, const PathParams<double>& P, bool poly, const float4* resp, const double* ext,
                              double* partials, double* estore, cudaStream_t s);
 int response_max_dates();
-size_t response_table_elems(int stride, int n_blocks);  // double2 entries of the table
-cudaError_t launch_response_table(int nt, double c, double kappa, int stride, int n_blocks, double2* resp,
+size_t response_table_elems(int stride, int n_blocks);  // float4 entries of the table
+cudaError_t launch_response_table(int nt, double c, double kappa, int stride, int n_blocks, float4* resp,
                                   cudaStream_t s);
 cudaError_t launch_path_mixed(int nt, const MixedParams& M, bool poly, const double* ext, double* partials,
                               float* estore, cudaStream_t s);
