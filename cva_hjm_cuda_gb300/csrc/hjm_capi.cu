@@ -665,6 +665,7 @@ static hjm_status ensure_response_table(hjm_ctx* ctx, const RunShape& sh, const 
         HJM_CUDA(ctx, ctx->resp.ensure(bytes));  // cudaFree waits for the device
     else
         HJM_CUDA(ctx, cudaStreamWaitEvent(s, ctx->resp_used, 0));
+    HJM_CUDA(ctx, cudaMemsetAsync(ctx->resp.p, 0, bytes, s));  // entries the kernel reads as exact zeros
     HJM_CUDA(ctx, launch_response_table(ctx->nt, P.c, kappa, sh.stride, sh.B, (float4*)ctx->resp.p, s));
     ctx->stat_launches += 1;
     k.nt = ctx->nt;

@@ -337,13 +337,16 @@ __global__ void __launch_bounds__(kFp64Cta, 4)
 // The accumulators of date j sit in slot r = B - j.  At step s of block b the
 // dates with a nonzero term are j = b + q for q_min <= q <= B - b, q_min the
 // least q with lag q stride - 1 - s >= L - b - q: slots 0 .. n_act - 1, a
-// prefix.  A switch on n_act enters a fall-through chain of the terms at slot
-// n_act - 1 (Duff's device): the skipped terms issue nothing, where a
-// predicated loop would still issue their FMAs to the FP64 pipe.  The impulse
-// responses come from response_table_kernel.
-constexpr int kRespDates = 24;                // dates the response form holds (slots 0 .. 22)
-constexpr int kRespSlots = kRespDates - 1;    // dates 2 .. B (date 1 is priced at spot)
-constexpr int kRespRow = 24;                  // response-table row: one float4 per slot, padded
+// prefix.  A switch on the number of groups of four slots covering it enters
+// a fall-through chain of groups (Duff's device): the skipped groups issue
+// nothing (a predicated loop would issue them all), and the four terms of a
+// group form one basic block, their loads in flight together and their FP32
+// chains interleaved.  The table is zero outside the live nonzero entries, so
+// the slots a group adds beyond n_act add exact zeros (dead or not yet
+// reached dates).  The impulse responses come from response_table_kernel.
+constexpr int kRespDates = 24;   // dates the response form holds (slots 0 .. 22 for dates 2 .. B)
+constexpr int kRespSlots = 24;   // accumulator slots, a multiple of the group of 4 (slot 23 stays zero)
+constexpr int kRespRow = 24;     // response-table row: one float4 per slot
 
 // A double as hi + lo + O(2^-47 |d|), hi and lo FP32, by truncation of the
 // significand with integer operations (conversion instructions issue on the
@@ -458,22 +461,21 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
             float wh, wl;
             split_f64(W, wh, wl);
             const float2 wh2 = make_float2(wh, wh), wl2 = make_float2(wl, wl);
-#define HJM_RESP_TERM(R)                                                                          \
-    case R + 1: {                                                                                 \
-        const float4 k = __ldg(rr + R);                                                           \
-        df_acc(A[R], Al[R], make_float2(k.x, k.y), make_float2(k.z, k.w), wh2, wl2);              \
+#define HJM_RESP_GROUP(G)                                                                         \
+    case G + 1: {                                                                                 \
+        float4 k[4];                                                                              \
+        _Pragma("unroll") for (int u = 0; u < 4; ++u) k[u] = __ldg(rr + 4 * G + u);              \
+        _Pragma("unroll") for (int u = 0; u < 4; ++u)                                            \
+            df_acc(A[4 * G + u], Al[4 * G + u], make_float2(k[u].x, k[u].y), make_float2(k[u].z, k[u].w), wh2, wl2); \
     }                                                                                             \
         [[fallthrough]];
-            switch (n_act) {
-                HJM_RESP_TERM(22) HJM_RESP_TERM(21) HJM_RESP_TERM(20) HJM_RESP_TERM(19) HJM_RESP_TERM(18)
-                HJM_RESP_TERM(17) HJM_RESP_TERM(16) HJM_RESP_TERM(15) HJM_RESP_TERM(14) HJM_RESP_TERM(13)
-                HJM_RESP_TERM(12) HJM_RESP_TERM(11) HJM_RESP_TERM(10) HJM_RESP_TERM(9) HJM_RESP_TERM(8)
-                HJM_RESP_TERM(7) HJM_RESP_TERM(6) HJM_RESP_TERM(5) HJM_RESP_TERM(4) HJM_RESP_TERM(3)
-                HJM_RESP_TERM(2) HJM_RESP_TERM(1) HJM_RESP_TERM(0)
+            switch ((n_act + 3) >> 2) {
+                HJM_RESP_GROUP(5) HJM_RESP_GROUP(4) HJM_RESP_GROUP(3) HJM_RESP_GROUP(2) HJM_RESP_GROUP(1)
+                HJM_RESP_GROUP(0)
                 default:
                     break;
             }
-#undef HJM_RESP_TERM
+#undef HJM_RESP_GROUP
             // S' = S + c dtau U + c dtau^2 W + sum_k svc[k][0] phi_k, etc. (old
             // U, W on the right; factor k of degree <= k drops 3 terms)
             double Sn = fma(P.svc[0][0], phi0, fma(P.k2, W, fma(P.k1, U, S)));
