@@ -323,11 +323,11 @@ __global__ void __launch_bounds__(kFp64Cta, 4)
 //
 // Both sums are carried in double-FP32 arithmetic on the FP32 pipe (76 times
 // the FP64 pipe's rate on GB300): the table holds each coefficient as a pair
-// of floats hi + lo (48 significant bits), W is split by truncation into
-// W_hi + W_lo (integer operations and one exact FP64 subtraction), the
-// product's leading term is made exact by an FMA and the accumulation by
-// Knuth's two-sum, packed {value, running sum} in FP32x2 instructions.  The
-// relative error of a date's sum stays below ~1e-13 of its magnitude, and the
+// of floats hi + lo (48 significant bits), W is split into W_hi + W_lo with
+// integer operations, the product's leading term is made exact by an FMA and
+// the accumulation by Knuth's two-sum, packed {value, running sum} in FP32x2
+// instructions.  The relative error of a date's sum stays below ~1e-12 of its
+// magnitude (checked against FP64 sums of the same terms), and the
 // remainder at a sampled tenor is small: |hc| <= 7e-5 for 24 dates, the most
 // this form takes, against a curve of ~0.03 (the far tail of the transport
 // from the last tenor; below 1e-6 for the 10y swap on 51 tenors), so its
@@ -348,34 +348,32 @@ constexpr int kRespDates = 24;   // dates the response form holds (slots 0 .. 22
 constexpr int kRespSlots = 24;   // accumulator slots, a multiple of the group of 4 (slot 23 stays zero)
 constexpr int kRespRow = 24;     // response-table row: one float4 per slot
 
-// A double as hi + lo + O(2^-47 |d|), hi and lo FP32, by truncation of the
-// significand with integer operations (conversion instructions issue on the
-// FP64 pipe); hi_d is hi as a double.  Magnitudes below the FP32 normal range
-// (2^-126) become zero, magnitudes above it saturate.
-__device__ __forceinline__ float trunc_f32(double d, double& as_double)
+// A double as hi + lo + O(2^-47 |d|), hi and lo FP32, with integer
+// operations only (conversion and arithmetic instructions on doubles issue on
+// the FP64 pipe): hi is d with its significand truncated to 24 bits, lo the
+// remaining 29 bits, converted (rounded to 24 bits) and scaled by 2^(E - 52).
+// |d| below 2^-126 gives zeros, lo below the FP32 normal range is dropped
+// (|d| < 2^-74: then hi alone, within 2^-24), |d| above 2^128 saturates.
+__device__ __forceinline__ void split_f64(double d, float& hi, float& lo)
 {
     const unsigned long long u = (unsigned long long)__double_as_longlong(d);
     const uint32_t top = (uint32_t)(u >> 32);
-    int e = (int)((top >> 20) & 0x7ffu) - 1023 + 127;
     const uint32_t sign = top & 0x80000000u;
-    if (e <= 0) {
-        as_double = 0.0;
-        return __uint_as_float(sign);
+    const int e = (int)((top >> 20) & 0x7ffu);  // biased FP64 exponent
+    const int eh = e - 1023 + 127;               // biased FP32 exponent of hi
+    if (eh <= 0) {
+        hi = lo = __uint_as_float(sign);
+        return;
     }
-    uint32_t m = (uint32_t)(u >> 29) & 0x7fffffu;
-    if (e > 254) {
-        e = 254;
-        m = 0x7fffffu;
+    if (eh > 254) {
+        hi = __uint_as_float(sign | 0x7f7fffffu);
+        lo = __uint_as_float(sign);
+        return;
     }
-    as_double = __longlong_as_double((long long)(u & ~((1ull << 29) - 1)));
-    return __uint_as_float(sign | ((uint32_t)e << 23) | m);
-}
-
-__device__ __forceinline__ void split_f64(double d, float& hi, float& lo)
-{
-    double hi_d, unused;
-    hi = trunc_f32(d, hi_d);
-    lo = trunc_f32(d - hi_d, unused);  // exact subtraction: the truncated bits
+    hi = __uint_as_float(sign | ((uint32_t)eh << 23) | ((uint32_t)(u >> 29) & 0x7fffffu));
+    const uint32_t r = (uint32_t)u & 0x1fffffffu;  // the truncated bits, in units of 2^(E - 52)
+    const float scale = (eh > 52) ? __uint_as_float((uint32_t)(eh - 52) << 23) : 0.0f;
+    lo = __uint_as_float(sign | __float_as_uint((float)r * scale));
 }
 
 // (A, Al) += (kh + kl) (wh + wl) in double-FP32, both lanes: the product's
@@ -427,7 +425,10 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
 #pragma unroll
     for (int r = 0; r < kRespSlots; ++r) A[r] = Al[r] = make_float2(0.0f, 0.0f);
     double S = 0.0, U = 0.0, W = 0.0;     // parallel, tilt and curvature parts
-    double sS = 0.0, sU = 0.0, sW = 0.0;  // their running sums over the evolved steps
+    // their running sums over the evolved steps before the current one (one
+    // step behind, so that no instruction of a step waits for the FP64 update
+    // it has just issued; sampling adds the current values, in the same order)
+    double sS = 0.0, sU = 0.0, sW = 0.0;
 
     // price date i from the sampled numeraire (x_i, D_i)
     auto sample = [&](int i) {
@@ -439,7 +440,7 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
             hcs = widen_f32(h.y) + widen_f32(l.y);
         }
         const double x = P.psamp[i] + (fma(tau, fma(tau, W, U), S) + hc);
-        const double acc = fma(tau, fma(tau, sW, sU), sS) + hcs;
+        const double acc = fma(tau, fma(tau, sW + W, sU + U), sS + S) + hcs;
         const double D = exp(-(P.psum[i] + acc) * P.dt);
         const double Lb = P.m * (exp(x / P.m) - 1.0);
         cf_s[i * kCta + tid] = D * (P.payA[i] * Lb - P.payB[i]);
@@ -476,12 +477,15 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
                     break;
             }
 #undef HJM_RESP_GROUP
+            sS += S;
+            sU += U;
+            sW += W;
             // S' = S + c dtau U + c dtau^2 W + sum_k svc[k][0] phi_k, etc. (old
             // U, W on the right; factor k of degree <= k drops 3 terms)
+            double Wn = fma(P.svc[2][2], phi2, W);
             double Sn = fma(P.svc[0][0], phi0, fma(P.k2, W, fma(P.k1, U, S)));
             Sn = fma(P.svc[2][0], phi2, fma(P.svc[1][0], phi1, Sn));
             double Un = fma(P.svc[2][1], phi2, fma(P.svc[1][1], phi1, fma(2.0 * P.k1, W, U)));
-            double Wn = fma(P.svc[2][2], phi2, W);
             if constexpr (!TRI) {
                 Un = fma(P.svc[0][1], phi0, Un);
                 Wn = fma(P.svc[1][2], phi1, fma(P.svc[0][2], phi0, Wn));
@@ -489,9 +493,6 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
             S = Sn;
             U = Un;
             W = Wn;
-            sS += S;
-            sU += U;
-            sW += W;
         }
         sample(b + 1);
     }
