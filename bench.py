@@ -89,18 +89,14 @@ def algorithmic_flops_per_path(n_tenor: int, n_steps: int, stride: int, form: st
     FP64 pipe's use (ncu's pipe utilisation is the direct measure).
 
     ``remainder="response"`` (polynomial forms, FP64, at most 24 dates): the
-    remainder is carried as impulse-response sums at the sampled tenors, two
-    FMAs per date still to be sampled whose response is not yet an exact zero
-    (its lag must reach the date's tenor), plus the scalar parts (9 FMA, or 12
-    for general quadratic factors) and their running sums (3 ADD); no block
-    recovery."""
+    FP64 pipe does the scalar parts (9 FMA, or 12 for general quadratic
+    factors) and their running sums (3 ADD) per evolved step; the remainder's
+    impulse-response sums run in double-FP32 on the FP32 pipe
+    (``response_fp32_flops_per_path``); no block recovery."""
     B = n_steps // stride
     L = n_tenor - 1
     if remainder == "response" and form != "table":
-        per = 21 if form == "poly_tri" else 27
-        live = sum(1 for b in range(1, B) for s in range(stride) for j in range(b + 1, B + 1)
-                   if s + 1 + L + b * stride <= j * (stride + 1))
-        return per * (B - 1) * stride + 4 * live
+        return (21 if form == "poly_tri" else 27) * (B - 1) * stride
 
     def per_step(b: int, k: int) -> int:
         # polynomial forms: the remainder is still zero below tenor L - 1 - k
@@ -112,6 +108,23 @@ def algorithmic_flops_per_path(n_tenor: int, n_steps: int, stride: int, form: st
     steps = sum(per_step(b, (b - 1) * stride + s) for b in range(1, B) for s in range(stride))
     recovery = 12 * sum(B - b for b in range(1, B))
     return steps + recovery
+
+
+def response_fp32_flops_per_path(n_tenor: int, n_steps: int, stride: int) -> int:
+    """FP32 flops of the response form's double-FP32 terms per path: at each
+    evolved step the date slots in groups of four covering the dates whose
+    response is not yet an exact zero, each slot one packed {value, running
+    sum} update of 2 FMUL2 + 7 FFMA2 + 4 FADD2 = 40 flops (product with its
+    exact leading term, Knuth two-sum, low-part update)."""
+    B = n_steps // stride
+    L = n_tenor - 1
+    slots = 0
+    for b in range(1, B):
+        for s in range(stride):
+            q_min = (s + 1 + L - b + stride) // (stride + 1)
+            n_act = B - b - q_min + 1
+            slots += 4 * ((n_act + 3) // 4) if n_act > 0 else 0
+    return 40 * slots
 
 
 class ClockSampler:
@@ -359,6 +372,14 @@ def run_ours(args) -> None:
                                                     "8 CTAs x 256 threads per SM, best of 3 (2 flops per FMA)"}
     achieved = flops / (path_ms * 1e-3) / 1e12
     traffic = profiled_traffic(f"{prec}-{n_paths}")
+    if remainder == "response":
+        f32 = response_fp32_flops_per_path(mk.n_tenor, n_steps, stride) * n_paths
+        a32 = f32 / (path_ms * 1e-3) / 1e12
+        p32 = extras.get("measured_fma_peak_tflops", {}).get("fp32")
+        fp32_side = {"pipe": "fp32 (double-FP32 response sums)", "algorithmic_flops_per_launch": f32,
+                     "achieved": a32, "peak": p32, "frac": (a32 / p32) if p32 else None}
+    else:
+        fp32_side = None
     roofline = {"bound": "fp64_pipe" if prec == "fp64" else "fp32_pipe", "achieved": achieved, "peak": peak,
                 "unit": "TFLOP/s", "frac": (achieved / peak) if peak else None, "traffic": traffic,
                 "kernel": (f"adjoint_kernel<{mk.n_tenor},ckpt,{form}>" if is_adjoint else
@@ -369,6 +390,8 @@ def run_ours(args) -> None:
                 "algorithmic_flops_per_launch": flops, "avg_launch_ms": path_ms,
                 "peak_source": "measured live by bench.py (FMA microkernel, this GPU)",
                 "hbm_peak_gbs_measured": _measured_hbm()}
+    if fp32_side:
+        roofline["fp32_side"] = fp32_side
 
     if not args.no_extras and prec == "fp64":
         extras["generic_table_step"] = generic_step_run(eng, mk, sw, args, flush, stride, peak64, peak32)

@@ -353,7 +353,7 @@ constexpr int kRespRow = 24;     // response-table row: one float4 per slot
 // the FP64 pipe): hi is d with its significand truncated to 24 bits, lo the
 // remaining 29 bits, converted (rounded to 24 bits) and scaled by 2^(E - 52).
 // |d| below 2^-126 gives zeros, lo below the FP32 normal range is dropped
-// (|d| < 2^-74: then hi alone, within 2^-24), |d| above 2^128 saturates.
+// (|d| < 2^-74: then hi alone, within 2^-23), |d| above 2^128 saturates.
 __device__ __forceinline__ void split_f64(double d, float& hi, float& lo)
 {
     const unsigned long long u = (unsigned long long)__double_as_longlong(d);

@@ -249,13 +249,18 @@ def _oracle_run(engine, mk, sw, cfg):
     return x, ee, cva, O.pfe(x, nd + 1, cfg.pfe_quantile)
 
 
-@pytest.mark.parametrize("nt,coef", [(51, DEFAULT_VOL_COEFFS), (51, FULL_COEFFS), (61, DEFAULT_VOL_COEFFS)],
-                         ids=["51-tri", "51-general", "61-tri"])
-def test_remainder_forms_agree_and_match_oracle(engine, remainder_form, nt, coef):
+@pytest.mark.parametrize("nt,coef,n_steps", [(51, DEFAULT_VOL_COEFFS, 1000), (51, FULL_COEFFS, 1000),
+                                             (61, DEFAULT_VOL_COEFFS, 1000), (51, DEFAULT_VOL_COEFFS, 1200)],
+                         ids=["51-tri", "51-general", "61-tri", "51-tri-24-dates"])
+def test_remainder_forms_agree_and_match_oracle(engine, remainder_form, nt, coef, n_steps):
+    """The response form (double-FP32 sums) against the convected FP64
+    remainder on the same paths, 24 dates being the most the form takes (the
+    remainder at the last date nearest the transport front, largest)."""
     mk = _poly_market(engine, nt=nt, coef=coef)
-    sw = Swap(n_tenor=nt)
+    nd = n_steps // 50
+    sw = Swap(n_tenor=nt, n_periods=nd)
     engine.set_swap(sw)
-    cfg = RunConfig(n_paths=3000, seed=77)
+    cfg = RunConfig(n_paths=3000, n_steps=n_steps, seed=77)
     out = {}
     engine.keep_exposures(True)
     try:
@@ -271,10 +276,10 @@ def test_remainder_forms_agree_and_match_oracle(engine, remainder_form, nt, coef
     _assert_rel(vr.ee, vc.ee, 1e-12, "EE response vs convect")
     _assert_rel(vr.cva, vc.cva, 1e-12, "CVA response vs convect")
     x, ee, cva, pfe = _oracle_run(engine, mk, sw, cfg)
-    _assert_rel(xr, x[:, :21].T, FP64_RTOL, "exposures vs oracle")
+    _assert_rel(xr, x[:, :nd + 1].T, FP64_RTOL, "exposures vs oracle")
     _assert_rel(vr.ee, ee, FP64_RTOL, "EE vs oracle")
     _assert_rel(vr.cva, cva, FP64_RTOL, "CVA vs oracle")
-    _assert_rel(vr.pfe[:21], pfe, FP64_RTOL, "PFE vs oracle")
+    _assert_rel(vr.pfe[:nd + 1], pfe, FP64_RTOL, "PFE vs oracle")
 
 
 @pytest.mark.parametrize("n_paths,n_steps,dt", [(1, 1000, 0.01), (63, 500, 0.02), (257, 1200, 0.01),

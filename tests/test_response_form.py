@@ -1,0 +1,204 @@
+"""CPU checks of the FP64 response form's algorithm (no GPU).
+
+The response form carries the remainder hc of the polynomial decomposition,
+driven by kappa W at the last tenor and convected upwind, as impulse-response
+sums at the sampled tenors: for date j, hc at its sampling step and the
+running sum of hc, both sum_n coef(lag) W_{n-1}.  Restated here in numpy, as
+response_table_kernel and path_kernel_fp64_resp compute them:
+
+* the table: entry (row b*stride + s, slot B - j) holds kappa G_j(lag) and
+  kappa CG_j(lag), lag = (j - b) stride - 1 - s, every lag of every date in
+  exactly one entry;
+* the active prefix: at step s of block b the slots 0 .. n_act - 1 with
+  q_min = ceil((s + 1 + L - b) / (stride + 1)) cover every nonzero entry;
+* the sums equal the direct recursion hc <- A hc + kappa W e_L to rounding;
+* the double-FP32 arithmetic (truncation split of W, exact leading product,
+  two-sum) stays within ~1e-12 of the FP64 sums, and the split within 2^-47.
+"""
+from __future__ import annotations
+
+import struct
+
+import numpy as np
+import pytest
+
+ROW = 24  # table row width (slots)
+
+
+def response_table(nt, stride, B, c, dtau):
+    L = nt - 1
+    kappa = -2.0 * c * dtau * dtau
+    tab = np.zeros((B * stride * ROW, 2))
+    written = np.zeros(B * stride * ROW, dtype=int)
+    v = np.zeros(nt)
+    v[L] = 1.0
+    cum = np.zeros(nt)
+    for m in range((B - 1) * stride):
+        cum = cum + v
+        for t in range(2, B + 1):
+            q = m // stride + 1
+            b = t - q
+            if b >= 1:
+                idx = (b * stride + (q * stride - 1 - m)) * ROW + (B - t)
+                tab[idx] = (kappa * v[t], kappa * cum[t])
+                written[idx] += 1
+        vn = v.copy()
+        vn[:L] = v[:L] + c * (v[1:] - v[:L])
+        vn[L] = v[L] + c * (v[L] - v[L - 1])
+        v = vn
+    return tab, written, kappa
+
+
+def n_active(s, b, B, L, stride):
+    q_min = (s + 1 + L - b + stride) // (stride + 1)
+    return B - b - q_min + 1
+
+
+SHAPES = [(51, 50, 20, 0.02), (61, 50, 20, 0.02), (51, 25, 24, 0.04), (51, 100, 10, 0.01), (51, 10, 5, 0.1)]
+
+
+@pytest.mark.parametrize("nt,stride,B,c", SHAPES)
+def test_table_covers_every_lag_once_and_prefix_holds_the_nonzeros(nt, stride, B, c):
+    tab, written, _ = response_table(nt, stride, B, c, 0.5)
+    L = nt - 1
+    assert written.max() <= 1
+    for b in range(1, B):
+        for s in range(stride):
+            n_act = n_active(s, b, B, L, stride)
+            assert n_act <= 23
+            for r in range(ROW):
+                idx = (b * stride + s) * ROW + r
+                live = r < B - b  # date j = B - r > b
+                assert written[idx] == (1 if live and B - r >= 2 else 0)
+                if r >= max(n_act, 0):
+                    assert tab[idx, 0] == 0.0 and tab[idx, 1] == 0.0, (b, s, r)
+
+
+def _direct_and_response(nt, stride, B, c, dtau, W, df=False):
+    tab, _, kappa = response_table(nt, stride, B, c, dtau)
+    L = nt - 1
+    acc = np.zeros((ROW, 2))
+    dfa = [[DF(), DF()] for _ in range(ROW)]
+    hc = np.zeros(nt)
+    hsum = np.zeros(nt)
+    got, want = {}, {}
+    w = 0.0
+    for b in range(1, B):
+        for s in range(stride):
+            n = b * stride + s
+            n_act = n_active(s, b, B, L, stride)
+            wh, wl = split_f64(w)
+            for r in range(max(n_act, 0)):
+                k = tab[(b * stride + s) * ROW + r]
+                acc[r] += k * w
+                if df:
+                    for q in range(2):
+                        dfa[r][q].add(k[q], wh, wl)
+            hn = hc.copy()
+            hn[:L] = hc[:L] + c * (hc[1:] - hc[:L])
+            hn[L] = hc[L] + c * (hc[L] - hc[L - 1]) + kappa * w
+            hc = hn
+            hsum += hc
+            w = W[n]
+        j = b + 1
+        r = B - j
+        want[j] = (hc[j], hsum[j])
+        got[j] = tuple(dfa[r][q].value() for q in range(2)) if df else (acc[r, 0], acc[r, 1])
+    return got, want
+
+
+def _rel(a, b):
+    return abs(a - b) / abs(b) if b != 0.0 else abs(a)
+
+
+@pytest.mark.parametrize("nt,stride,B,c", SHAPES[:4])
+def test_response_sums_equal_the_convected_remainder(nt, stride, B, c):
+    rng = np.random.default_rng(7)
+    W = np.cumsum(rng.normal(size=B * stride)) * 1e-5
+    got, want = _direct_and_response(nt, stride, B, c, 0.5, W)
+    for j in got:
+        for q in range(2):
+            assert _rel(got[j][q], want[j][q]) < 1e-12, (j, q, got[j][q], want[j][q])
+
+
+# --- double-FP32 arithmetic, as the kernel's split_f64 / df_acc -------------
+_f32 = np.float32
+
+
+def _bits_f32(u):
+    return struct.unpack("<f", struct.pack("<I", u))[0]
+
+
+def split_f64(d):
+    u = struct.unpack("<Q", struct.pack("<d", float(d)))[0]
+    top = u >> 32
+    sign = top & 0x80000000
+    eh = ((top >> 20) & 0x7FF) - 1023 + 127
+    if eh <= 0:
+        return _f32(_bits_f32(sign)), _f32(_bits_f32(sign))
+    if eh > 254:
+        return _f32(_bits_f32(sign | 0x7F7FFFFF)), _f32(_bits_f32(sign))
+    hi = _f32(_bits_f32(sign | (eh << 23) | ((u >> 29) & 0x7FFFFF)))
+    r = u & 0x1FFFFFFF
+    scale = _f32(_bits_f32((eh - 52) << 23)) if eh > 52 else _f32(0.0)
+    lo_abs = _f32(_f32(r) * scale)
+    lo = _f32(_bits_f32(sign | struct.unpack("<I", struct.pack("<f", lo_abs))[0]))
+    return hi, lo
+
+
+def _fma32(a, b, c):
+    # float32 a*b is exact in float64; one float64 rounding before the float32 one
+    return _f32(np.float64(a) * np.float64(b) + np.float64(c))
+
+
+class DF:
+    """One lane of the kernel's (A, Al) accumulator."""
+
+    def __init__(self):
+        self.A = _f32(0.0)
+        self.Al = _f32(0.0)
+
+    def add(self, k, wh, wl):
+        kh = _f32(k)
+        kl = _f32(k - np.float64(kh))
+        p = _f32(kh * wh)
+        e = _fma32(kh, wh, -p)
+        e = _fma32(kh, wl, e)
+        e = _fma32(kl, wh, e)
+        s = _f32(self.A + p)
+        bp = _f32(s - self.A)
+        ap = _f32(s - bp)
+        err = _f32(_f32(self.A - ap) + _f32(p - bp))
+        self.Al = _f32(self.Al + _f32(err + e))
+        self.A = s
+
+    def value(self):
+        return np.float64(self.A) + np.float64(self.Al)
+
+
+def test_split_is_within_2_pow_47():
+    rng = np.random.default_rng(0)
+    d = rng.normal(size=4000) * 10.0 ** rng.uniform(-20, 3, size=4000)
+    for x in d:
+        hi, lo = split_f64(x)
+        assert abs(np.float64(hi) + np.float64(lo) - x) <= 2.0**-47 * abs(x)
+        assert abs(np.float64(hi)) <= abs(x)
+    assert split_f64(0.0) == (0.0, 0.0)
+    hi, lo = split_f64(1e-30)  # below 2^-74: the low part is dropped, hi truncated
+    assert lo == 0.0 and abs(np.float64(hi) - 1e-30) <= 2.0**-23 * 1e-30
+
+
+@pytest.mark.parametrize("nt,stride,B,c", [(51, 50, 24, 0.02), (51, 25, 24, 0.04), (51, 50, 20, 0.02)])
+def test_double_fp32_sums_track_fp64_sums(nt, stride, B, c):
+    """The most dates the form takes (24, the remainder nearest the transport
+    front), with a curvature random walk five times the reference market's.
+    Terms whose coefficient lies below FP32's range (under ~1e-38: the far
+    tail of the transport at early dates) come out as zero; the absolute
+    floor 1e-30 is far below the curve's FP64 ulp (~3e-18)."""
+    rng = np.random.default_rng(1)
+    W = np.cumsum(rng.normal(size=B * stride)) * np.sqrt(c * 0.5) * 2e-5 * 5
+    got, want = _direct_and_response(nt, stride, B, c, 0.5, W, df=True)
+    for j in got:
+        for q in range(2):
+            assert abs(got[j][q] - want[j][q]) <= 2e-12 * abs(want[j][q]) + 1e-30, (j, q, got[j][q], want[j][q])
+    assert abs(want[B][0]) > 1e-7  # the last date's remainder is well inside FP32's range
