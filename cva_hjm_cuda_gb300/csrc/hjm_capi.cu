@@ -650,14 +650,15 @@ static bool use_response_form(const hjm_ctx* ctx, const RunShape& sh)
 }
 
 // The response table of the run shape, on the stream: recomputed only when the
-// shape changed, after the kernels of earlier valuations that read it.
-static hjm_status ensure_response_table(hjm_ctx* ctx, const RunShape& sh, const PathParams<double>& P,
-                                        cudaStream_t s)
+// shape changed, after the kernels of earlier valuations that read it.  c and
+// kappa = -2 c dtau^2 as fill_params forms them.
+static hjm_status ensure_response_table(hjm_ctx* ctx, const RunShape& sh, double dt, cudaStream_t s)
 {
-    const double kappa = -2.0 * P.k2;
+    const double c = dt / ctx->dtau;
+    const double kappa = -2.0 * ((dt / ctx->dtau) * ctx->dtau * ctx->dtau);
     hjm_ctx::RespKey& k = ctx->resp_key;
     if (!ctx->resp_used) HJM_CUDA(ctx, cudaEventCreateWithFlags(&ctx->resp_used, cudaEventDisableTiming));
-    if (k.valid && k.nt == ctx->nt && k.stride == sh.stride && k.B == sh.B && k.c == P.c && k.kappa == kappa)
+    if (k.valid && k.nt == ctx->nt && k.stride == sh.stride && k.B == sh.B && k.c == c && k.kappa == kappa)
         return HJM_OK;
     k.valid = false;
     const size_t bytes = sizeof(float4) * response_table_elems(sh.stride, sh.B);
@@ -666,12 +667,12 @@ static hjm_status ensure_response_table(hjm_ctx* ctx, const RunShape& sh, const 
     else
         HJM_CUDA(ctx, cudaStreamWaitEvent(s, ctx->resp_used, 0));
     HJM_CUDA(ctx, cudaMemsetAsync(ctx->resp.p, 0, bytes, s));  // entries the kernel reads as exact zeros
-    HJM_CUDA(ctx, launch_response_table(ctx->nt, P.c, kappa, sh.stride, sh.B, (float4*)ctx->resp.p, s));
+    HJM_CUDA(ctx, launch_response_table(ctx->nt, c, kappa, sh.stride, sh.B, (float4*)ctx->resp.p, s));
     ctx->stat_launches += 1;
     k.nt = ctx->nt;
     k.stride = sh.stride;
     k.B = sh.B;
-    k.c = P.c;
+    k.c = c;
     k.kappa = kappa;
     k.valid = true;
     return HJM_OK;
@@ -748,7 +749,7 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
         fill_params<double>(ctx, sh, n_paths, dt, seed, path_offset, hazard, recovery, ld, store, P, F);
         resp = use_response_form(ctx, sh);
         if (resp) {
-            st = ensure_response_table(ctx, sh, P, s);
+            st = ensure_response_table(ctx, sh, dt, s);
             if (st != HJM_OK) return st;
         }
         HJM_CUDA(ctx, launch_path_fp64(ctx->nt, P, use_poly_path(ctx), resp ? (const float4*)ctx->resp.p : nullptr,

@@ -24,6 +24,7 @@
 #include "hjm_device.cuh"
 #include "hjm_kernels.h"
 #include "hjm_pairs.cuh"
+#include "hjm_resp.cuh"
 
 namespace hjm {
 
@@ -305,95 +306,8 @@ __global__ void __launch_bounds__(kFp64Cta, 4)
     fp64_epilogue<kCta>(P, cf_s, work_s, red_s, partials, estore, cta_base, active);
 }
 
-// Response form of the FP64 path (polynomial volatility, at most kRespDates
-// sampled dates).  The remainder hc of the polynomial decomposition starts at
-// zero, is driven only at the last tenor, by kappa W_{n-1} at step n (kappa =
-// -2 c dtau^2, W before the step's update), and is otherwise convected by A.
-// So after step K its value at tenor j and its running sum are
-//     hc_K[j]               = sum_{n<=K} G_j(K - n)  kappa W_{n-1},  G_j(m) = (A^m e_L)[j],
-//     sum_{K'<=K} hc_K'[j]  = sum_{n<=K} CG_j(K - n) kappa W_{n-1},  CG_j(m) = sum_{r<=m} G_j(r),
-// exact in exact arithmetic.  The pricing reads hc only at tenor j at date
-// j's sampling step K_j = j stride - 1 (its value and, for the discount, its
-// running sum), so the kernel keeps those two numbers per date still to be
-// sampled and adds one term to each per step: 2 (B - b) FMAs in block b, in
-// place of the convection of every live tenor and the block-end discount
-// recovery.  G_j(m) vanishes for m < L - j (the remainder's support reaches
-// one tenor further down per step), so a date takes no term while its lag is
-// that short.
-//
-// Both sums are carried in double-FP32 arithmetic on the FP32 pipe (76 times
-// the FP64 pipe's rate on GB300): the table holds each coefficient as a pair
-// of floats hi + lo (48 significant bits), W is split into W_hi + W_lo with
-// integer operations, the product's leading term is made exact by an FMA and
-// the accumulation by Knuth's two-sum, packed {value, running sum} in FP32x2
-// instructions.  The relative error of a date's sum stays below ~1e-12 of its
-// magnitude (checked against FP64 sums of the same terms), and the
-// remainder at a sampled tenor is small: |hc| <= 7e-5 for 24 dates, the most
-// this form takes, against a curve of ~0.03 (the far tail of the transport
-// from the last tenor; below 1e-6 for the 10y swap on 51 tenors), so its
-// rounding stays within an ulp of the FP64 curve.  Per step the FP64 pipe
-// does only the polynomial parts.
-//
-// The accumulators of date j sit in slot r = B - j.  At step s of block b the
-// dates with a nonzero term are j = b + q for q_min <= q <= B - b, q_min the
-// least q with lag q stride - 1 - s >= L - b - q: slots 0 .. n_act - 1, a
-// prefix.  A switch on the number of groups of four slots covering it enters
-// a fall-through chain of groups (Duff's device): the skipped groups issue
-// nothing (a predicated loop would issue them all), and the four terms of a
-// group form one basic block, their loads in flight together and their FP32
-// chains interleaved.  The table is zero outside the live nonzero entries, so
-// the slots a group adds beyond n_act add exact zeros (dead or not yet
-// reached dates).  The impulse responses come from response_table_kernel.
-constexpr int kRespDates = 24;   // dates the response form holds (slots 0 .. 22 for dates 2 .. B)
-constexpr int kRespSlots = 24;   // accumulator slots, a multiple of the group of 4 (slot 23 stays zero)
-constexpr int kRespRow = 24;     // response-table row: one float4 per slot
-
-// A double as hi + lo + O(2^-47 |d|), hi and lo FP32, with integer
-// operations only (conversion and arithmetic instructions on doubles issue on
-// the FP64 pipe): hi is d with its significand truncated to 24 bits, lo the
-// remaining 29 bits, converted (rounded to 24 bits) and scaled by 2^(E - 52).
-// |d| below 2^-126 gives zeros, lo below the FP32 normal range is dropped
-// (|d| < 2^-74: then hi alone, within 2^-23), |d| above 2^128 saturates.
-__device__ __forceinline__ void split_f64(double d, float& hi, float& lo)
-{
-    const unsigned long long u = (unsigned long long)__double_as_longlong(d);
-    const uint32_t top = (uint32_t)(u >> 32);
-    const uint32_t sign = top & 0x80000000u;
-    const int e = (int)((top >> 20) & 0x7ffu);  // biased FP64 exponent
-    const int eh = e - 1023 + 127;               // biased FP32 exponent of hi
-    if (eh <= 0) {
-        hi = lo = __uint_as_float(sign);
-        return;
-    }
-    if (eh > 254) {
-        hi = __uint_as_float(sign | 0x7f7fffffu);
-        lo = __uint_as_float(sign);
-        return;
-    }
-    hi = __uint_as_float(sign | ((uint32_t)eh << 23) | ((uint32_t)(u >> 29) & 0x7fffffu));
-    const uint32_t r = (uint32_t)u & 0x1fffffffu;  // the truncated bits, in units of 2^(E - 52)
-    const float scale = (eh > 52) ? __uint_as_float((uint32_t)(eh - 52) << 23) : 0.0f;
-    lo = __uint_as_float(sign | __float_as_uint((float)r * scale));
-}
-
-// (A, Al) += (kh + kl) (wh + wl) in double-FP32, both lanes: the product's
-// leading term exact by FMA, the cross terms in FP32, kl wl (2^-48) dropped;
-// Knuth's two-sum keeps A + Al exact up to the FP32 rounding of Al.
-__device__ __forceinline__ void df_acc(float2& A, float2& Al, float2 kh, float2 kl, float2 wh, float2 wl)
-{
-    const float2 m1 = make_float2(-1.0f, -1.0f);
-    const float2 p = __fmul2_rn(kh, wh);
-    float2 e = __ffma2_rn(kh, wh, __fmul2_rn(p, m1));
-    e = __ffma2_rn(kh, wl, e);
-    e = __ffma2_rn(kl, wh, e);
-    const float2 sum = __fadd2_rn(A, p);
-    const float2 bp = __ffma2_rn(A, m1, sum);   // sum - A
-    const float2 ap = __ffma2_rn(bp, m1, sum);  // sum - bp
-    const float2 err = __fadd2_rn(__ffma2_rn(ap, m1, A), __ffma2_rn(bp, m1, p));
-    Al = __fadd2_rn(Al, __fadd2_rn(err, e));
-    A = sum;
-}
-
+// The FP64 response form (hjm_resp.cuh): the polynomial parts S, U, W in FP64,
+// the remainder as double-FP32 impulse-response sums per date slot.
 __host__ __device__ inline size_t resp_smem_bytes(int n_blocks)
 {
     // cf_s [B+2][kCta] (the epilogue's exposures alias it one row up), red_s
@@ -447,36 +361,27 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
     };
 
     sample(1);
-    const int st1 = P.stride + 1;
     for (int b = 1; b < B; ++b) {
         const float4* row = resp + (size_t)b * P.stride * kRespRow;
-        const int nlive = B - b;
         for (int s = 0; s < P.stride; ++s) {
             const int n = b * P.stride + s;
             double phi0, phi1, phi2;
             draw_phi<double, EXT>(ext, gpath, active ? lp : 0, P.n_paths, n, P.rk0, P.rk1, phi0, phi1, phi2);
-            // q_min = ceil((s + 1 + L - b) / (stride + 1)) >= 1 (uniform)
-            const int q_min = (s + 1 + L - b + P.stride) / st1;
-            const int n_act = nlive - q_min + 1;
+            const int n_act = resp_n_act(s, b, B, L, P.stride);  // uniform
             const float4* rr = row + (size_t)s * kRespRow;
             float wh, wl;
             split_f64(W, wh, wl);
             const float2 wh2 = make_float2(wh, wh), wl2 = make_float2(wl, wl);
-#define HJM_RESP_GROUP(G)                                                                         \
-    case G + 1: {                                                                                 \
-        float4 k[4];                                                                              \
-        _Pragma("unroll") for (int u = 0; u < 4; ++u) k[u] = __ldg(rr + 4 * G + u);              \
-        _Pragma("unroll") for (int u = 0; u < 4; ++u)                                            \
-            df_acc(A[4 * G + u], Al[4 * G + u], make_float2(k[u].x, k[u].y), make_float2(k[u].z, k[u].w), wh2, wl2); \
-    }                                                                                             \
-        [[fallthrough]];
-            switch ((n_act + 3) >> 2) {
-                HJM_RESP_GROUP(5) HJM_RESP_GROUP(4) HJM_RESP_GROUP(3) HJM_RESP_GROUP(2) HJM_RESP_GROUP(1)
-                HJM_RESP_GROUP(0)
-                default:
-                    break;
-            }
-#undef HJM_RESP_GROUP
+            resp_groups(n_act, [&](auto gc) {
+                constexpr int G = decltype(gc)::value;
+                float4 k[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) k[u] = __ldg(rr + 4 * G + u);
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    df_acc(A[4 * G + u], Al[4 * G + u], make_float2(k[u].x, k[u].y), make_float2(k[u].z, k[u].w),
+                           wh2, wl2);
+            });
             sS += S;
             sU += U;
             sW += W;
@@ -536,6 +441,67 @@ __global__ void __launch_bounds__(kMaxTenor)
         else if (t == L)
             v += c * (v - v_s[L - 1]);
         __syncthreads();
+    }
+}
+
+// Epilogue of the mixed-precision path kernels (as fp64_epilogue, exposures
+// and their store in FP32): acc_s rows 1..B hold the cash flows (FP64), e_s
+// B+1 FP32 rows (free for this use).
+__device__ __forceinline__ void mixed_epilogue(const PathParams<float>& P, const double* acc_s, float* e_s,
+                                               double* red_s, double* __restrict__ partials,
+                                               float* __restrict__ estore, int64_t cta_base, bool active)
+{
+    const int tid = threadIdx.x;
+    const int B = P.n_blocks;
+    double v = 0.0, cva_c = 0.0;
+    e_s[B * kCta + tid] = 0.f;
+    for (int j = B - 1; j >= 0; --j) {
+        v += acc_s[(j + 1) * kCta + tid];
+        double e = (v > 0.0) ? v : 0.0;
+        if (!active) e = 0.0;
+        e_s[j * kCta + tid] = (float)e;
+        cva_c = fma(P.cvaw[j], e, cva_c);
+    }
+    __syncthreads();
+
+    const int warp = tid >> 5, lane = tid & 31;
+    const int R = B + 3;
+    for (int j = warp; j <= B; j += kCta / 32) {
+        double sum = 0.0;
+#pragma unroll
+        for (int q = 0; q < kCta / 32; ++q) sum += (double)e_s[j * kCta + lane + 32 * q];
+        sum = warp_sum(sum);
+        if (lane == 0) partials[(size_t)blockIdx.x * R + j] = sum;
+    }
+    {
+        const double s1 = warp_sum(cva_c), s2 = warp_sum(cva_c * cva_c);
+        if (lane == 0) {
+            red_s[warp] = s1;
+            red_s[kCta / 32 + warp] = s2;
+        }
+    }
+    if (P.store_exposures) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+        double s1 = 0.0, s2 = 0.0;
+        for (int w = 0; w < kCta / 32; ++w) {
+            s1 += red_s[w];
+            s2 += red_s[kCta / 32 + w];
+        }
+        partials[(size_t)blockIdx.x * R + B + 1] = s1;
+        partials[(size_t)blockIdx.x * R + B + 2] = s2;
+        if (P.store_exposures) {
+            const int64_t cnt = (P.n_paths - cta_base < kCta) ? (P.n_paths - cta_base) : kCta;
+            const uint32_t bytes = (uint32_t)(((cnt + 3) / 4) * 4 * sizeof(float));
+            for (int j = 0; j <= B; ++j) {
+                float* dst = estore + (size_t)j * (size_t)P.ld + (size_t)cta_base;
+                const uint32_t src = (uint32_t)__cvta_generic_to_shared(e_s + (size_t)j * kCta);
+                asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
+                             :: "l"(dst), "r"(src), "r"(bytes) : "memory");
+            }
+            asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+            asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+        }
     }
 }
 
@@ -623,57 +589,7 @@ __global__ void __launch_bounds__(kCta, 4)
         sample(b + 1);
     }
 
-    float* e_s = hs_s;  // [B+1][kCta] exposures
-    double v = 0.0, cva_c = 0.0;
-    e_s[B * kCta + tid] = 0.f;
-    for (int j = B - 1; j >= 0; --j) {
-        v += acc_s[(j + 1) * kCta + tid];
-        double e = (v > 0.0) ? v : 0.0;
-        if (!active) e = 0.0;
-        e_s[j * kCta + tid] = (float)e;
-        cva_c = fma(P.cvaw[j], e, cva_c);
-    }
-    __syncthreads();
-
-    const int warp = tid >> 5, lane = tid & 31;
-    const int R = B + 3;
-    for (int j = warp; j <= B; j += kCta / 32) {
-        double sum = 0.0;
-#pragma unroll
-        for (int q = 0; q < kCta / 32; ++q) sum += (double)e_s[j * kCta + lane + 32 * q];
-        sum = warp_sum(sum);
-        if (lane == 0) partials[(size_t)blockIdx.x * R + j] = sum;
-    }
-    {
-        const double s1 = warp_sum(cva_c), s2 = warp_sum(cva_c * cva_c);
-        if (lane == 0) {
-            red_s[warp] = s1;
-            red_s[kCta / 32 + warp] = s2;
-        }
-    }
-    if (P.store_exposures) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    __syncthreads();
-    if (tid == 0) {
-        double s1 = 0.0, s2 = 0.0;
-        for (int w = 0; w < kCta / 32; ++w) {
-            s1 += red_s[w];
-            s2 += red_s[kCta / 32 + w];
-        }
-        partials[(size_t)blockIdx.x * R + B + 1] = s1;
-        partials[(size_t)blockIdx.x * R + B + 2] = s2;
-        if (P.store_exposures) {
-            const int64_t cnt = (P.n_paths - cta_base < kCta) ? (P.n_paths - cta_base) : kCta;
-            const uint32_t bytes = (uint32_t)(((cnt + 3) / 4) * 4 * sizeof(float));
-            for (int j = 0; j <= B; ++j) {
-                float* dst = estore + (size_t)j * (size_t)P.ld + (size_t)cta_base;
-                const uint32_t src = (uint32_t)__cvta_generic_to_shared(e_s + (size_t)j * kCta);
-                asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
-                             :: "l"(dst), "r"(src), "r"(bytes) : "memory");
-            }
-            asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-            asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
-        }
-    }
+    mixed_epilogue(P, acc_s, hs_s, red_s, partials, estore, cta_base, active);
 }
 
 __host__ __device__ inline size_t mixed_smem_bytes(int nt, int n_blocks)

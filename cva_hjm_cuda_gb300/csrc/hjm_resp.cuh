@@ -1,0 +1,147 @@
+// hjm_resp.cuh -- the response form of the polynomial decomposition's remainder.
+//
+// The impulse-response table layout, the active prefix of date slots per
+// step, the fall-through dispatch over groups of four slots and the
+// double-FP32 helpers of the FP64 response form (path_kernel_fp64_resp in
+// hjm_forward.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <type_traits>
+
+#include "hjm_kernels.h"
+
+namespace hjm {
+
+// Response form (polynomial volatility, at most kRespDates sampled dates).  The remainder hc of the polynomial decomposition starts at
+// zero, is driven only at the last tenor, by kappa W_{n-1} at step n (kappa =
+// -2 c dtau^2, W before the step's update), and is otherwise convected by A.
+// So after step K its value at tenor j and its running sum are
+//     hc_K[j]               = sum_{n<=K} G_j(K - n)  kappa W_{n-1},  G_j(m) = (A^m e_L)[j],
+//     sum_{K'<=K} hc_K'[j]  = sum_{n<=K} CG_j(K - n) kappa W_{n-1},  CG_j(m) = sum_{r<=m} G_j(r),
+// exact in exact arithmetic.  The pricing reads hc only at tenor j at date
+// j's sampling step K_j = j stride - 1 (its value and, for the discount, its
+// running sum), so the kernel keeps those two numbers per date still to be
+// sampled and adds one term to each per step: 2 (B - b) FMAs in block b, in
+// place of the convection of every live tenor and the block-end discount
+// recovery.  G_j(m) vanishes for m < L - j (the remainder's support reaches
+// one tenor further down per step), so a date takes no term while its lag is
+// that short.
+//
+// Both sums are carried in double-FP32 arithmetic on the FP32 pipe (76 times
+// the FP64 pipe's rate on GB300): the table holds each coefficient as a pair
+// of floats hi + lo (48 significant bits), W is split into W_hi + W_lo with
+// integer operations, the product's leading term is made exact by an FMA and
+// the accumulation by Knuth's two-sum, packed {value, running sum} in FP32x2
+// instructions.  The relative error of a date's sum stays below ~1e-12 of its
+// magnitude (checked against FP64 sums of the same terms), and the
+// remainder at a sampled tenor is small: |hc| <= 7e-5 for 24 dates, the most
+// this form takes, against a curve of ~0.03 (the far tail of the transport
+// from the last tenor; below 1e-6 for the 10y swap on 51 tenors), so its
+// rounding stays within an ulp of the FP64 curve.  Per step the FP64 pipe
+// does only the polynomial parts.
+//
+// The accumulators of date j sit in slot r = B - j.  At step s of block b the
+// dates with a nonzero term are j = b + q for q_min <= q <= B - b, q_min the
+// least q with lag q stride - 1 - s >= L - b - q: slots 0 .. n_act - 1, a
+// prefix.  A switch on the number of groups of four slots covering it enters
+// a fall-through chain of groups (Duff's device): the skipped groups issue
+// nothing (a predicated loop would issue them all), and the four terms of a
+// group form one basic block, their loads in flight together and their FP32
+// chains interleaved.  The table is zero outside the live nonzero entries, so
+// the slots a group adds beyond n_act add exact zeros (dead or not yet
+// reached dates).  The impulse responses come from response_table_kernel.
+constexpr int kRespDates = 24;   // dates the response form holds (slots 0 .. 22 for dates 2 .. B)
+constexpr int kRespSlots = 24;   // accumulator slots, a multiple of the group of 4 (slot 23 stays zero)
+constexpr int kRespRow = 24;     // response-table row: one float4 per slot
+
+// A double as hi + lo + O(2^-47 |d|), hi and lo FP32, with integer
+// operations only (conversion and arithmetic instructions on doubles issue on
+// the FP64 pipe): hi is d with its significand truncated to 24 bits, lo the
+// remaining 29 bits, converted (rounded to 24 bits) and scaled by 2^(E - 52).
+// |d| below 2^-126 gives zeros, lo below the FP32 normal range is dropped
+// (|d| < 2^-74: then hi alone, within 2^-23), |d| above 2^128 saturates.
+__device__ __forceinline__ void split_f64(double d, float& hi, float& lo)
+{
+    const unsigned long long u = (unsigned long long)__double_as_longlong(d);
+    const uint32_t top = (uint32_t)(u >> 32);
+    const uint32_t sign = top & 0x80000000u;
+    const int e = (int)((top >> 20) & 0x7ffu);  // biased FP64 exponent
+    const int eh = e - 1023 + 127;               // biased FP32 exponent of hi
+    if (eh <= 0) {
+        hi = lo = __uint_as_float(sign);
+        return;
+    }
+    if (eh > 254) {
+        hi = __uint_as_float(sign | 0x7f7fffffu);
+        lo = __uint_as_float(sign);
+        return;
+    }
+    hi = __uint_as_float(sign | ((uint32_t)eh << 23) | ((uint32_t)(u >> 29) & 0x7fffffu));
+    const uint32_t r = (uint32_t)u & 0x1fffffffu;  // the truncated bits, in units of 2^(E - 52)
+    const float scale = (eh > 52) ? __uint_as_float((uint32_t)(eh - 52) << 23) : 0.0f;
+    lo = __uint_as_float(sign | __float_as_uint((float)r * scale));
+}
+
+// (A, Al) += (kh + kl) (wh + wl) in double-FP32, both lanes: the product's
+// leading term exact by FMA, the cross terms in FP32, kl wl (2^-48) dropped;
+// Knuth's two-sum keeps A + Al exact up to the FP32 rounding of Al.
+__device__ __forceinline__ void df_acc(float2& A, float2& Al, float2 kh, float2 kl, float2 wh, float2 wl)
+{
+    const float2 m1 = make_float2(-1.0f, -1.0f);
+    const float2 p = __fmul2_rn(kh, wh);
+    float2 e = __ffma2_rn(kh, wh, __fmul2_rn(p, m1));
+    e = __ffma2_rn(kh, wl, e);
+    e = __ffma2_rn(kl, wh, e);
+    const float2 sum = __fadd2_rn(A, p);
+    const float2 bp = __ffma2_rn(A, m1, sum);   // sum - A
+    const float2 ap = __ffma2_rn(bp, m1, sum);  // sum - bp
+    const float2 err = __fadd2_rn(__ffma2_rn(ap, m1, A), __ffma2_rn(bp, m1, p));
+    Al = __fadd2_rn(Al, __fadd2_rn(err, e));
+    A = sum;
+}
+
+// Slots with a nonzero term at step s of block b: q_min = ceil((s + 1 + L - b)
+// / (stride + 1)) is the nearest date whose lag reaches its tenor, and the
+// slots 0 .. n_act - 1 hold the dates b + q_min .. B (n_act <= 0: none).
+__device__ __forceinline__ int resp_n_act(int s, int b, int B, int L, int stride)
+{
+    const int q_min = (s + 1 + L - b + stride) / (stride + 1);
+    return B - b - q_min + 1;
+}
+
+// fn(std::integral_constant<int, G>) for the groups G = ceil(n_act/4) - 1 .. 0
+// of four slots each, by a switch that enters a fall-through chain (Duff's
+// device): no instruction of a skipped group issues, and each group is one
+// basic block (its loads in flight together, its chains interleaved).
+template <typename Fn>
+__device__ __forceinline__ void resp_groups(int n_act, Fn&& fn)
+{
+    static_assert(kRespSlots == 24, "six groups of four slots");
+    switch ((n_act + 3) >> 2) {
+        case 6:
+            fn(std::integral_constant<int, 5>{});
+            [[fallthrough]];
+        case 5:
+            fn(std::integral_constant<int, 4>{});
+            [[fallthrough]];
+        case 4:
+            fn(std::integral_constant<int, 3>{});
+            [[fallthrough]];
+        case 3:
+            fn(std::integral_constant<int, 2>{});
+            [[fallthrough]];
+        case 2:
+            fn(std::integral_constant<int, 1>{});
+            [[fallthrough]];
+        case 1:
+            fn(std::integral_constant<int, 0>{});
+            [[fallthrough]];
+        default:
+            break;
+    }
+}
+
+}  // namespace hjm

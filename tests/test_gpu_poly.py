@@ -314,7 +314,7 @@ def test_remainder_form_choice_and_limits(engine, remainder_form, tmp_path):
     engine.write_report(tmp_path / "r.json")
     assert json.loads((tmp_path / "r.json").read_text())["run"]["remainder"] == "response"
     engine.run(RunConfig(n_paths=256), "mixed")
-    assert engine.remainder_form() == "convect"  # mixed precision always convects
+    assert engine.remainder_form() == "convect"  # mixed precision convects (the FP32 pairs cost less)
     _poly_market(engine, nt=61)
     engine.set_swap(Swap(n_tenor=61, n_periods=60))
     cfg30 = RunConfig(n_paths=256, n_steps=3000)
