@@ -86,8 +86,8 @@ struct hjm_ctx {
     // is recorded after the last kernel that reads it
     struct RespKey {
         bool valid = false;
-        int nt = 0, stride = 0, B = 0;
-        double c = 0, kappa = 0;
+        int nt = 0, stride = 0, B = 0, scheme = 0;
+        double c = 0, dtau = 0;
     } resp_key;
     cudaEvent_t resp_used = nullptr;
 
@@ -633,32 +633,47 @@ static void fill_pc(const hjm_ctx* ctx, const RunShape& sh, double dt, const Pat
     Q.gL = (T)(-c * dtau * dtau);
 }
 
-// FP64 Euler valuation with the decomposition: the remainder in impulse
-// responses (two FMAs per date still to be sampled and ~12 FP64 operations per
-// step) when that is cheaper than its convection (one FMA per live tenor and
-// ~17 per step), summed over the evolved blocks.
+// FP64 valuation with the decomposition (Euler or predictor-corrector): the
+// remainder in impulse responses (its terms on the FP32 pipe, ~12 FP64
+// operations per step for the polynomial parts) when that is cheaper than its
+// convection (one FMA per live tenor and ~17 per step for Euler, two and ~20
+// for the predictor-corrector), summed over the evolved blocks; the response
+// terms count as two FMAs per date still to be sampled.
 static bool use_response_form(const hjm_ctx* ctx, const RunShape& sh)
 {
-    if (!use_poly_path(ctx) || ctx->scheme != HJM_SCHEME_EULER || sh.B > response_max_dates()) return false;
+    if (!use_poly_path(ctx) || sh.B > response_max_dates()) return false;
     if (ctx->remainder != HJM_REMAINDER_AUTO) return ctx->remainder == HJM_REMAINDER_RESPONSE;
+    const bool pc = ctx->scheme == HJM_SCHEME_PREDICTOR_CORRECTOR;
     long conv = 0, resp = 0;
     for (int b = 1; b < sh.B; ++b) {
-        conv += (ctx->nt - 1 - b) + 17;
+        conv += pc ? 2 * (ctx->nt - 1 - b) + 20 : (ctx->nt - 1 - b) + 17;
         resp += 2 * (sh.B - b) + 12;
     }
     return resp < conv;
 }
 
-// The response table of the run shape, on the stream: recomputed only when the
-// shape changed, after the kernels of earlier valuations that read it.  c and
-// kappa = -2 c dtau^2 as fill_params forms them.
+// The response table of the run shape and scheme, on the stream: recomputed
+// only when they changed, after the kernels of earlier valuations that read
+// it.  Euler: the source -2 c dtau^2 W at the last tenor (fill_params' k2);
+// predictor-corrector: the sources of fill_pc (wL1 at L-1; wL, gL at L).
 static hjm_status ensure_response_table(hjm_ctx* ctx, const RunShape& sh, double dt, cudaStream_t s)
 {
-    const double c = dt / ctx->dtau;
-    const double kappa = -2.0 * ((dt / ctx->dtau) * ctx->dtau * ctx->dtau);
+    const double dtau = ctx->dtau;
+    const double c = dt / dtau;
+    const bool pc = ctx->scheme == HJM_SCHEME_PREDICTOR_CORRECTOR;
+    double w0 = 0.0, w1, w2 = 0.0;
+    if (pc) {
+        const double wL1 = -c * c * dtau * dtau, wL = -(2.0 * c + c * c) * dtau * dtau, gL = -c * dtau * dtau;
+        w0 = wL1;
+        w1 = wL - gL;
+        w2 = gL;
+    } else {
+        w1 = -2.0 * ((dt / dtau) * dtau * dtau);
+    }
     hjm_ctx::RespKey& k = ctx->resp_key;
     if (!ctx->resp_used) HJM_CUDA(ctx, cudaEventCreateWithFlags(&ctx->resp_used, cudaEventDisableTiming));
-    if (k.valid && k.nt == ctx->nt && k.stride == sh.stride && k.B == sh.B && k.c == c && k.kappa == kappa)
+    if (k.valid && k.nt == ctx->nt && k.stride == sh.stride && k.B == sh.B && k.c == c && k.dtau == dtau &&
+        k.scheme == ctx->scheme)
         return HJM_OK;
     k.valid = false;
     const size_t bytes = sizeof(float4) * response_table_elems(sh.stride, sh.B);
@@ -667,13 +682,14 @@ static hjm_status ensure_response_table(hjm_ctx* ctx, const RunShape& sh, double
     else
         HJM_CUDA(ctx, cudaStreamWaitEvent(s, ctx->resp_used, 0));
     HJM_CUDA(ctx, cudaMemsetAsync(ctx->resp.p, 0, bytes, s));  // entries the kernel reads as exact zeros
-    HJM_CUDA(ctx, launch_response_table(ctx->nt, c, kappa, sh.stride, sh.B, (float4*)ctx->resp.p, s));
+    HJM_CUDA(ctx, launch_response_table(ctx->nt, c, sh.stride, sh.B, pc, w0, w1, w2, (float4*)ctx->resp.p, s));
     ctx->stat_launches += 1;
     k.nt = ctx->nt;
     k.stride = sh.stride;
     k.B = sh.B;
     k.c = c;
-    k.kappa = kappa;
+    k.dtau = dtau;
+    k.scheme = ctx->scheme;
     k.valid = true;
     return HJM_OK;
 }
@@ -687,8 +703,7 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
     if (st != HJM_OK) return st;
     HJM_CUDA(ctx, cudaSetDevice(ctx->device));
     const bool mixed = precision == HJM_PRECISION_MIXED;
-    if (!mixed && ctx->remainder == HJM_REMAINDER_RESPONSE && use_poly_path(ctx) &&
-        ctx->scheme == HJM_SCHEME_EULER && sh.B > response_max_dates())
+    if (!mixed && ctx->remainder == HJM_REMAINDER_RESPONSE && use_poly_path(ctx) && sh.B > response_max_dates())
         return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "the response form holds at most %d dates (run has %d)",
                     response_max_dates(), sh.B);
     const bool want_pfe = pfe_q > 0.0;
@@ -735,8 +750,15 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
         PcParams<double> Q;
         fill_pc<double>(ctx, sh, dt, P, Q);
         ctx->stat_h2d = sizeof(Q) + sizeof(FinalParams);
-        HJM_CUDA(ctx, launch_path_pc(ctx->nt, Q, use_poly_path(ctx), ext_dev, (double*)ctx->partials.p,
-                                     store ? (double*)ctx->estore.p : nullptr, s));
+        resp = use_response_form(ctx, sh);
+        if (resp) {
+            st = ensure_response_table(ctx, sh, dt, s);
+            if (st != HJM_OK) return st;
+        }
+        HJM_CUDA(ctx, launch_path_pc(ctx->nt, Q, use_poly_path(ctx), resp ? (const float4*)ctx->resp.p : nullptr,
+                                     ext_dev, (double*)ctx->partials.p, store ? (double*)ctx->estore.p : nullptr,
+                                     s));
+        if (resp) HJM_CUDA(ctx, cudaEventRecord(ctx->resp_used, s));
     } else if (mixed) {
         PathParams<float> P;
         fill_params<float>(ctx, sh, n_paths, dt, seed, path_offset, hazard, recovery, ld, store, P, F);

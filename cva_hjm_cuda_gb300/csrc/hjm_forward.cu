@@ -25,6 +25,7 @@
 #include "hjm_kernels.h"
 #include "hjm_pairs.cuh"
 #include "hjm_resp.cuh"
+#include "hjm_epilogue.cuh"
 
 namespace hjm {
 
@@ -47,73 +48,6 @@ __host__ __device__ inline size_t path_smem_bytes(int nt, int n_blocks, bool mix
     b += 2 * (rows + 1) * kFp64Cta * 8;  // work_s
     b += 2 * (kFp64Cta / 32) * 8;        // red_s
     return b;
-}
-
-// Epilogue of the FP64 path kernels: the exposure profile E_j = max(sum_{i>j}
-// cf_i, 0) by FP64 suffix sums, the path's CVA contribution sum_j cvaw[j] E_j,
-// the CTA's partial sums (dates 0..B, then sum c and sum c^2) and, if asked,
-// the exposure rows of the CTA's paths to HBM.  cf_s rows 1..B hold the cash
-// flows, column tid private to its thread; e_s (B+1 rows) may alias cf_s one
-// row up: row j of e_s is written after row j+1 of cf_s, the one aliased, is read.
-template <int kCta>
-__device__ __forceinline__ void fp64_epilogue(const PathParams<double>& P, const double* cf_s, double* e_s,
-                                              double* red_s, double* __restrict__ partials,
-                                              double* __restrict__ estore, int64_t cta_base, bool active)
-{
-    const int tid = threadIdx.x;
-    const int B = P.n_blocks;
-    double v = 0.0, cva_c = 0.0;
-    e_s[B * kCta + tid] = 0.0;
-    for (int j = B - 1; j >= 0; --j) {
-        v += cf_s[(j + 1) * kCta + tid];
-        double e = (v > 0.0) ? v : 0.0;
-        if (!active) e = 0.0;
-        e_s[j * kCta + tid] = e;
-        cva_c = fma(P.cvaw[j], e, cva_c);
-    }
-    __syncthreads();
-
-    // CTA partial sums: dates 0..B, then sum c and sum c^2
-    const int warp = tid >> 5, lane = tid & 31;
-    const int R = B + 3;
-    for (int j = warp; j <= B; j += kCta / 32) {
-        double sum = 0.0;
-#pragma unroll
-        for (int q = 0; q < kCta / 32; ++q) sum += e_s[j * kCta + lane + 32 * q];
-        sum = warp_sum(sum);
-        if (lane == 0) partials[(size_t)blockIdx.x * R + j] = sum;
-    }
-    {
-        const double s1 = warp_sum(cva_c), s2 = warp_sum(cva_c * cva_c);
-        if (lane == 0) {
-            red_s[warp] = s1;
-            red_s[kCta / 32 + warp] = s2;
-        }
-    }
-    if (P.store_exposures) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    __syncthreads();
-    if (tid == 0) {
-        double s1 = 0.0, s2 = 0.0;
-        for (int w = 0; w < kCta / 32; ++w) {
-            s1 += red_s[w];
-            s2 += red_s[kCta / 32 + w];
-        }
-        partials[(size_t)blockIdx.x * R + B + 1] = s1;
-        partials[(size_t)blockIdx.x * R + B + 2] = s2;
-        if (P.store_exposures) {
-            // date rows of this CTA's paths, smem -> HBM with the bulk-copy (TMA) engine
-            const int64_t cnt = (P.n_paths - cta_base < kCta) ? (P.n_paths - cta_base) : kCta;
-            const uint32_t bytes = (uint32_t)(((cnt + 1) / 2) * 2 * sizeof(double));
-            for (int j = 0; j <= B; ++j) {
-                double* dst = estore + (size_t)j * (size_t)P.ld + (size_t)cta_base;
-                const uint32_t src = (uint32_t)__cvta_generic_to_shared(e_s + (size_t)j * kCta);
-                asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
-                             :: "l"(dst), "r"(src), "r"(bytes) : "memory");
-            }
-            asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-            asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
-        }
-    }
 }
 
 // Discount sums by block-sum recovery.  Over one block of Euler steps
@@ -405,41 +339,79 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
 }
 
 // Impulse responses of the convection at the sampled tenors, for the response
-// form: entry (row b stride + s, column r = B - j) of resp holds kappa
-// G_j(lag) and kappa CG_j(lag) as FP32 pairs {G hi, CG hi, G lo, CG lo}, lag = (j - b) stride - 1 - s the distance from step
-// s of block b to date j's sampling step, for 1 <= b < j <= B <= kRespDates;
-// G_j(m) = (A^m e_L)[j] by m applications of the upwind step (backward
-// difference at the last tenor, simulation_cpu.h:96-108) and CG_j(m) =
-// sum_{r<=m} G_j(r).  Every lag m in [0, (j-1) stride - 1] of date j maps to
-// exactly one entry (q = j - b = m / stride + 1, s = q stride - 1 - m).  One
-// CTA of kMaxTenor threads, thread t holding tenor t.
+// form: entry (row b stride + s, column r = B - j) of resp holds, as FP32 pairs
+// {coef hi, sum hi, coef lo, sum lo}, the coefficient of the old W at step s of
+// block b in date j's remainder and in its running sum, at lag l = (j - b)
+// stride - 1 - s (the distance to date j's sampling step), for 1 <= b < j <=
+// B <= kRespDates.  Every lag l in [0, (j-1) stride - 1] of date j maps to
+// exactly one entry (q = j - b = l / stride + 1, s = q stride - 1 - l); the
+// rest of the table stays zero.  One CTA of kMaxTenor threads, thread t
+// holding tenor t of the responses.
+//  * Euler (pc = 0): coef = kappa G_j(l), G_j(m) = (A^m e_L)[j] by m
+//    applications of the upwind step (backward difference at the last tenor,
+//    simulation_cpu.h:96-108), sum = kappa CG_j(l), CG_j(m) = sum_{r<=m} G_j(r);
+//    kappa = w1.
+//  * predictor-corrector (pc = 1): the remainder is driven at L-1 by w0' W_old
+//    and at L by wL W_old + gL gamma, gamma = W_new - W_old; grouping the terms
+//    by W, the coefficient of the old W at lag l is H1(l) + H2(l+1) with
+//    H1 = w0 G1 + w1 G2 (w0 = wL1, w1 = wL - gL) and H2 = w2 G2 (w2 = gL), G1,
+//    G2 the responses of A2 (three-point stencil a0, a1, a2; Euler rows at
+//    L-1, L) to e_{L-1}, e_L, and the sum likewise with the running sums.
 __global__ void __launch_bounds__(kMaxTenor)
-    response_table_kernel(int nt, double c, double kappa, int stride, int B, float4* __restrict__ resp)
+    response_table_kernel(int nt, double c, int stride, int B, int pc, double w0, double w1, double w2,
+                          float4* __restrict__ resp)
 {
-    __shared__ double v_s[kMaxTenor];
+    __shared__ double v_s[kMaxTenor], u_s[kMaxTenor];
     const int t = threadIdx.x;
     const int L = nt - 1;
-    double v = (t == L) ? 1.0 : 0.0;
-    double cum = 0.0;
     const int M = (B - 1) * stride - 1;  // the longest lag read
-    for (int m = 0; m <= M; ++m) {
-        cum += v;
-        if (t >= 2 && t <= B) {
-            const int q = m / stride + 1;
-            const int b = t - q;
-            if (b >= 1) {
-                const double g = kappa * v, cg = kappa * cum;
-                const float gh = __double2float_rn(g), cgh = __double2float_rn(cg);
-                resp[((size_t)b * stride + (size_t)(q * stride - 1 - m)) * kRespRow + (B - t)] =
-                    make_float4(gh, cgh, __double2float_rn(g - (double)gh), __double2float_rn(cg - (double)cgh));
-            }
+    auto put = [&](int l, double coef, double sum) {
+        if (t < 2 || t > B) return;
+        const int q = l / stride + 1;
+        const int b = t - q;
+        if (b < 1) return;
+        const float ch = __double2float_rn(coef), sh = __double2float_rn(sum);
+        resp[((size_t)b * stride + (size_t)(q * stride - 1 - l)) * kRespRow + (B - t)] =
+            make_float4(ch, sh, __double2float_rn(coef - (double)ch), __double2float_rn(sum - (double)sh));
+    };
+    if (!pc) {
+        double v = (t == L) ? 1.0 : 0.0;
+        double cum = 0.0;
+        for (int m = 0; m <= M; ++m) {
+            cum += v;
+            put(m, w1 * v, w1 * cum);
+            v_s[t] = v;
+            __syncthreads();
+            if (t < L)
+                v += c * (v_s[t + 1] - v);
+            else if (t == L)
+                v += c * (v - v_s[L - 1]);
+            __syncthreads();
         }
-        v_s[t] = v;
+        return;
+    }
+    const double a0 = 1.0 - c + 0.5 * c * c, a1 = c - c * c, a2 = 0.5 * c * c;
+    double g1 = (t == L - 1) ? 1.0 : 0.0, g2 = (t == L) ? 1.0 : 0.0;
+    double cg1 = 0.0, cg2 = 0.0, h1p = 0.0, ch1p = 0.0;  // H1, CH1 at the previous lag
+    for (int m = 0; m <= M + 1; ++m) {
+        cg1 += g1;
+        cg2 += g2;
+        if (m >= 1) put(m - 1, h1p + w2 * g2, ch1p + w2 * cg2);
+        h1p = w0 * g1 + w1 * g2;
+        ch1p = w0 * cg1 + w1 * cg2;
+        v_s[t] = g1;
+        u_s[t] = g2;
         __syncthreads();
-        if (t < L)
-            v += c * (v_s[t + 1] - v);
-        else if (t == L)
-            v += c * (v - v_s[L - 1]);
+        if (t < L - 1) {
+            g1 = a0 * g1 + a1 * v_s[t + 1] + a2 * v_s[t + 2];
+            g2 = a0 * g2 + a1 * u_s[t + 1] + a2 * u_s[t + 2];
+        } else if (t == L - 1) {
+            g1 += c * (v_s[L] - g1);
+            g2 += c * (u_s[L] - g2);
+        } else if (t == L) {
+            g1 += c * (g1 - v_s[L - 1]);
+            g2 += c * (g2 - u_s[L - 1]);
+        }
         __syncthreads();
     }
 }
@@ -873,11 +845,11 @@ int response_max_dates() { return kRespDates; }
 
 size_t response_table_elems(int stride, int n_blocks) { return (size_t)n_blocks * stride * kRespRow; }
 
-cudaError_t launch_response_table(int nt, double c, double kappa, int stride, int n_blocks, float4* resp,
-                                  cudaStream_t s)
+cudaError_t launch_response_table(int nt, double c, int stride, int n_blocks, bool pc, double w0, double w1,
+                                  double w2, float4* resp, cudaStream_t s)
 {
-    if (nt < 2 || nt > kMaxTenor || n_blocks > kRespDates || n_blocks >= nt || stride < 1) return cudaErrorInvalidValue;
-    response_table_kernel<<<1, kMaxTenor, 0, s>>>(nt, c, kappa, stride, n_blocks, resp);
+    if (nt < 3 || nt > kMaxTenor || n_blocks > kRespDates || n_blocks >= nt || stride < 1) return cudaErrorInvalidValue;
+    response_table_kernel<<<1, kMaxTenor, 0, s>>>(nt, c, stride, n_blocks, pc ? 1 : 0, w0, w1, w2, resp);
     return cudaGetLastError();
 }
 

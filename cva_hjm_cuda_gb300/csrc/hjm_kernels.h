@@ -55,8 +55,10 @@ cudaError_t launch_path_fp64(int nt, const PathParams<double>& P, bool poly, con
                              double* partials, double* estore, cudaStream_t s);
 int response_max_dates();
 size_t response_table_elems(int stride, int n_blocks);  // float4 entries of the table
-cudaError_t launch_response_table(int nt, double c, double kappa, int stride, int n_blocks, float4* resp,
-                                  cudaStream_t s);
+// Euler: w1 = kappa = -2 c dtau^2 (w0, w2 unused); predictor-corrector: w0 =
+// wL1, w1 = wL - gL, w2 = gL (PcParams)
+cudaError_t launch_response_table(int nt, double c, int stride, int n_blocks, bool pc, double w0, double w1,
+                                  double w2, float4* resp, cudaStream_t s);
 cudaError_t launch_path_mixed(int nt, const MixedParams& M, bool poly, const double* ext, double* partials,
                               float* estore, cudaStream_t s);
 void pack_mixed_params(int nt, const PathParams<float>& P, MixedParams& M);
@@ -93,8 +95,10 @@ struct PcParams {
     T k1, k2p, k1x2;       // c dtau, (c + c^2) dtau^2, 2 c dtau
     T wL1, wL, gL;         // sources: -c^2 dtau^2 W at L-1; -(2c + c^2) dtau^2 W - c dtau^2 gamma at L
 };
-cudaError_t launch_path_pc(int nt, const PcParams<double>& Q, bool poly, const double* ext, double* partials,
-                           double* estore, cudaStream_t s);
+// resp (FP64 only): the predictor-corrector response table (the response
+// form, polynomial volatility, at most response_max_dates() dates) or null
+cudaError_t launch_path_pc(int nt, const PcParams<double>& Q, bool poly, const float4* resp, const double* ext,
+                           double* partials, double* estore, cudaStream_t s);
 cudaError_t launch_path_pc(int nt, const PcParams<float>& Q, bool poly, const double* ext, double* partials,
                            float* estore, cudaStream_t s);
 size_t pc_smem(int nt, int n_blocks, bool mixed);

@@ -32,7 +32,9 @@
 #include <cstring>
 
 #include "hjm_device.cuh"
+#include "hjm_epilogue.cuh"
 #include "hjm_kernels.h"
+#include "hjm_resp.cuh"
 
 namespace hjm {
 
@@ -259,6 +261,117 @@ __global__ void __launch_bounds__(kPcCta, 4)
     }
 }
 
+// Response form of the FP64 predictor-corrector path (polynomial volatility,
+// at most kRespDates dates), as path_kernel_fp64_resp in hjm_forward.cu: the
+// polynomial parts in FP64 with the N-projected loadings,
+//     S' = S + c dtau U + (c + c^2) dtau^2 W + aS.phi,  U' = U + 2 c dtau W + aU.phi,
+//     W' = W + aW.phi   (old values on the right),
+// and the remainder, driven at L-1 and L by W and by the step's curvature
+// noise, as double-FP32 sums of the predictor-corrector response table (the
+// coefficient of the old W per date slot and lag; response_table_kernel with
+// pc = 1) over the active prefix of slots.  TRI: factor k of degree <= k
+// (aU[0] = aW[0] = aW[1] = 0).
+template <int NT, bool EXT, bool TRI>
+__global__ void __launch_bounds__(kPcCta, 6)
+    path_kernel_pc_resp(const __grid_constant__ PcParams<double> Q, const float4* __restrict__ resp,
+                        const double* __restrict__ ext, double* __restrict__ partials, double* __restrict__ estore)
+{
+    constexpr int L = NT - 1;
+    const PathParams<double>& P = Q.P;
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int tid = threadIdx.x;
+    const int B = P.n_blocks;
+    double* cf_s = reinterpret_cast<double*>(smem);  // [B+2][kPcCta]; exposures alias it one row up
+    double* red_s = cf_s + (size_t)(B + 2) * kPcCta;
+
+    const int64_t cta_base = (int64_t)blockIdx.x * kPcCta;
+    const int64_t lp = cta_base + tid;
+    const bool active = lp < P.n_paths;
+    const uint64_t gpath = P.path_offset + (uint64_t)lp;
+
+    float2 A[kRespSlots], Al[kRespSlots];  // {remainder at tenor j, its running sum}, slot B - j, hi + lo
+#pragma unroll
+    for (int r = 0; r < kRespSlots; ++r) A[r] = Al[r] = make_float2(0.0f, 0.0f);
+    double S = 0.0, U = 0.0, W = 0.0;
+    double sS = 0.0, sU = 0.0, sW = 0.0;  // running sums before the current step (sampling adds it)
+
+    auto sample = [&](int i) {
+        const double tau = P.tau[i];
+        const float2 h = select_reg<kRespSlots, float2>(A, B - i), l = select_reg<kRespSlots, float2>(Al, B - i);
+        const double hc = widen_f32(h.x) + widen_f32(l.x), hcs = widen_f32(h.y) + widen_f32(l.y);
+        const double x = P.psamp[i] + (fma(tau, fma(tau, W, U), S) + hc);
+        const double acc = fma(tau, fma(tau, sW + W, sU + U), sS + S) + hcs;
+        const double D = exp(-(P.psum[i] + acc) * P.dt);
+        const double Lb = P.m * (exp(x / P.m) - 1.0);
+        cf_s[i * kPcCta + tid] = D * (P.payA[i] * Lb - P.payB[i]);
+    };
+
+    sample(1);
+    for (int b = 1; b < B; ++b) {
+        const float4* row = resp + (size_t)b * P.stride * kRespRow;
+        for (int s = 0; s < P.stride; ++s) {
+            const int n = b * P.stride + s;
+            double phi0, phi1, phi2;
+            draw_phi<double, EXT>(ext, gpath, active ? lp : 0, P.n_paths, n, P.rk0, P.rk1, phi0, phi1, phi2);
+            const int n_act = resp_n_act<true>(s, b, B, L, P.stride);  // uniform
+            const float4* rr = row + (size_t)s * kRespRow;
+            float wh, wl;
+            split_f64(W, wh, wl);
+            const float2 wh2 = make_float2(wh, wh), wl2 = make_float2(wl, wl);
+            resp_groups(n_act, [&](auto gc) {
+                constexpr int G = decltype(gc)::value;
+                float4 k[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) k[u] = __ldg(rr + 4 * G + u);
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    df_acc(A[4 * G + u], Al[4 * G + u], make_float2(k[u].x, k[u].y), make_float2(k[u].z, k[u].w),
+                           wh2, wl2);
+            });
+            sS += S;
+            sU += U;
+            sW += W;
+            double Wn = fma(Q.aW[2], phi2, W);
+            double Sn = fma(Q.aS[0], phi0, fma(Q.k2p, W, fma(Q.k1, U, S)));
+            Sn = fma(Q.aS[2], phi2, fma(Q.aS[1], phi1, Sn));
+            double Un = fma(Q.aU[2], phi2, fma(Q.aU[1], phi1, fma(Q.k1x2, W, U)));
+            if constexpr (!TRI) {
+                Un = fma(Q.aU[0], phi0, Un);
+                Wn = fma(Q.aW[1], phi1, fma(Q.aW[0], phi0, Wn));
+            }
+            S = Sn;
+            U = Un;
+            W = Wn;
+        }
+        sample(b + 1);
+    }
+    fp64_epilogue<kPcCta>(P, cf_s, cf_s + kPcCta, red_s, partials, estore, cta_base, active);
+}
+
+template <int NT, bool EXT, bool TRI>
+static cudaError_t launch_pc_resp_t(const PcParams<double>& Q, const float4* resp, const double* ext,
+                                    double* partials, double* estore, cudaStream_t s)
+{
+    const size_t smem = ((size_t)Q.P.n_blocks + 2) * kPcCta * 8 + 2 * (kPcCta / 32) * 8;
+    auto k = path_kernel_pc_resp<NT, EXT, TRI>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const int64_t grid = (Q.P.n_paths + kPcCta - 1) / kPcCta;
+    k<<<(unsigned)grid, kPcCta, smem, s>>>(Q, resp, ext, partials, estore);
+    return cudaGetLastError();
+}
+
+template <int NT>
+static cudaError_t launch_pc_resp_nt(const PcParams<double>& Q, const float4* resp, const double* ext,
+                                     double* partials, double* estore, cudaStream_t s)
+{
+    const bool tri = Q.aU[0] == 0.0 && Q.aW[0] == 0.0 && Q.aW[1] == 0.0;
+    if (ext) return tri ? launch_pc_resp_t<NT, true, true>(Q, resp, ext, partials, estore, s)
+                        : launch_pc_resp_t<NT, true, false>(Q, resp, ext, partials, estore, s);
+    return tri ? launch_pc_resp_t<NT, false, true>(Q, resp, ext, partials, estore, s)
+               : launch_pc_resp_t<NT, false, false>(Q, resp, ext, partials, estore, s);
+}
+
 template <int NT, typename T, bool EXT, bool POLY>
 static cudaError_t launch_pc_t(const PcParams<T>& Q, const double* ext, double* partials, T* estore, cudaStream_t s)
 {
@@ -290,9 +403,15 @@ static cudaError_t launch_pc_any(int nt, const PcParams<T>& Q, bool poly, const 
     return cudaErrorInvalidValue;
 }
 
-cudaError_t launch_path_pc(int nt, const PcParams<double>& Q, bool poly, const double* ext, double* partials,
-                           double* estore, cudaStream_t s)
+cudaError_t launch_path_pc(int nt, const PcParams<double>& Q, bool poly, const float4* resp, const double* ext,
+                           double* partials, double* estore, cudaStream_t s)
 {
+    if (resp) {
+        if (!poly || Q.P.n_blocks > kRespDates) return cudaErrorInvalidValue;
+        if (nt == 51) return launch_pc_resp_nt<51>(Q, resp, ext, partials, estore, s);
+        if (nt == 61) return launch_pc_resp_nt<61>(Q, resp, ext, partials, estore, s);
+        return cudaErrorInvalidValue;
+    }
     return launch_pc_any<double>(nt, Q, poly, ext, partials, estore, s);
 }
 

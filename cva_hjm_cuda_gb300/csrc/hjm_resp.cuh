@@ -103,12 +103,20 @@ __device__ __forceinline__ void df_acc(float2& A, float2& Al, float2 kh, float2 
     A = sum;
 }
 
-// Slots with a nonzero term at step s of block b: q_min = ceil((s + 1 + L - b)
-// / (stride + 1)) is the nearest date whose lag reaches its tenor, and the
-// slots 0 .. n_act - 1 hold the dates b + q_min .. B (n_act <= 0: none).
+// Slots with a nonzero term at step s of block b: q_min is the nearest date
+// whose lag l = q stride - 1 - s reaches its tenor, and the slots 0 .. n_act -
+// 1 hold the dates b + q_min .. B (n_act <= 0: none).  Euler (one tenor per
+// step from L): l >= L - j, q_min = ceil((L - b + 1 + s) / (stride + 1)).
+// Predictor-corrector (the two-point stencil reaches two tenors per step, and
+// its coefficient at lag l includes the response of the next step to the
+// curvature noise): 2 l >= L - 2 - j, q_min = ceil((L - b + 2 s) / (2 stride + 1)).
+template <bool PC = false>
 __device__ __forceinline__ int resp_n_act(int s, int b, int B, int L, int stride)
 {
-    const int q_min = (s + 1 + L - b + stride) / (stride + 1);
+    const int num = PC ? L - b + 2 * s : L - b + 1 + s;
+    const int den = PC ? 2 * stride + 1 : stride + 1;
+    const int q = (num + den - 1) / den;
+    const int q_min = q > 1 ? q : 1;
     return B - b - q_min + 1;
 }
 

@@ -106,16 +106,17 @@ hjm_status hjm_ctx_set_vol_decomposition(hjm_ctx* ctx, int32_t enable);
 hjm_status hjm_ctx_vol_decomposition(hjm_ctx* ctx, int32_t* active);
 
 /* FP64 form of the decomposition's remainder.  The remainder is driven only at
- * the last tenor and priced only at each date's own tenor, so an FP64 Euler
- * valuation either convects it over the live tenors every step
- * (HJM_REMAINDER_CONVECT) or carries, for each date still to be sampled, its
- * value and running sum as sums of impulse responses of the convection
- * (HJM_REMAINDER_RESPONSE: two FMAs per such date per step, at most
+ * the last tenor (the last two for the predictor-corrector) and priced only at
+ * each date's own tenor, so an FP64 valuation either convects it over the
+ * live tenors every step (HJM_REMAINDER_CONVECT) or carries, for each date
+ * still to be sampled, its value and running sum as sums of impulse responses
+ * of the convection (HJM_REMAINDER_RESPONSE: one double-FP32 term per such
+ * date per step, on the FP32 pipe, at most
  * HJM_RESPONSE_MAX_DATES dates, a run with more fails with
  * HJM_ERR_INVALID_ARGUMENT).  HJM_REMAINDER_AUTO (default) takes the form with
- * fewer FP64 operations for the run.  The forms agree to rounding; mixed
- * precision, the predictor-corrector scheme and the table step do not use
- * this setting.  The report names the form a valuation ran ("remainder"). */
+ * fewer FP64 operations for the run.  Both time schemes; the forms agree to
+ * rounding; mixed precision and the table step do not use this setting.  The
+ * report names the form a valuation ran ("remainder"). */
 #define HJM_REMAINDER_AUTO 0
 #define HJM_REMAINDER_CONVECT 1
 #define HJM_REMAINDER_RESPONSE 2

@@ -136,3 +136,65 @@ def test_pc_general_quadratic_factors(pc):
     normals = pc.dump_normals(cfg.n_paths, cfg.n_steps, cfg.seed)
     ee = O.expected_exposure(O.exposure_paths_pc(mk, sw, cfg.n_steps, cfg.dt, normals))
     _assert_rel(pc.run(cfg, "fp64").ee[:20], ee[:20], FP64_RTOL, "EE (general quadratic)")
+
+
+@pytest.mark.parametrize("general", [False, True], ids=["tri", "general-quadratic"])
+def test_pc_response_form_vs_convected_and_oracle(pc, case, general):
+    """The predictor-corrector's remainder as double-FP32 response sums (the
+    default for the 10y swap) against its FP64 convection on the same paths
+    (1e-11) and against the oracle (1e-10); the external-normals path takes the
+    same form."""
+    mk, sw, cfg, normals, x, ee, cva = case
+    if general:
+        coef = np.array([[0.0060, 0.00010, -0.000004], [-0.0036, 0.00040, 0.000003], [0.0020, -0.00060, 0.00002]])
+        mk = Market(vol_coeffs=coef)
+        pc.set_market_poly(51, 0.5, mk.spot, coef)
+        x = O.exposure_paths_pc(mk, sw, cfg.n_steps, cfg.dt, normals)
+        ee = O.expected_exposure(x)
+        cva, _ = O.cva(ee, 21, mk.dtau, cfg.hazard, cfg.recovery)
+    else:
+        pc.set_market(mk)
+    pc.set_swap(sw)
+    out = {}
+    pc.keep_exposures(True)
+    try:
+        for form in ("convect", "response"):
+            pc.set_remainder_form(form)
+            out[form] = (pc.run(cfg, "fp64"), pc.exposures())
+            assert pc.remainder_form() == form
+        pc.set_remainder_form("auto")
+        ext = pc.run_with_normals(normals, cfg.n_steps, cfg.dt, "fp64")
+        assert pc.remainder_form() == "response"
+    finally:
+        pc.keep_exposures(False)
+        pc.set_remainder_form("auto")
+    (vc, xc), (vr, xr) = out["convect"], out["response"]
+    # both forms sit ~3e-12 (relative) from the oracle on exposures, ~4e-15 of
+    # the largest exposure in absolute terms: agreement to 1e-11
+    _assert_rel(xr, xc, 1e-11, "exposures response vs convect")
+    _assert_rel(vr.ee, vc.ee, 1e-11, "EE response vs convect")
+    _assert_rel(xr, x[:, :21].T, FP64_RTOL, "exposures vs oracle")
+    _assert_rel(vr.ee, ee, FP64_RTOL, "EE vs oracle")
+    _assert_rel(vr.cva, cva, FP64_RTOL, "CVA vs oracle")
+    np.testing.assert_array_equal(ext.ee, vr.ee)
+
+
+@pytest.mark.parametrize("n_paths,n_steps,dt", [(1, 1000, 0.01), (257, 1200, 0.01), (63, 500, 0.02)],
+                         ids=["1-path", "24-dates", "stride25"])
+def test_pc_response_form_shapes_vs_oracle(pc, n_paths, n_steps, dt):
+    mk = Market()
+    pc.set_market(mk)
+    stride = int(round(mk.dtau / dt))
+    sw = Swap(n_periods=n_steps // stride)
+    pc.set_swap(sw)
+    pc.set_remainder_form("response")
+    try:
+        cfg = RunConfig(n_paths=n_paths, n_steps=n_steps, dt=dt, seed=6)
+        v = pc.run(cfg, "fp64")
+        assert pc.remainder_form() == "response"
+    finally:
+        pc.set_remainder_form("auto")
+    normals = pc.dump_normals(cfg.n_paths, cfg.n_steps, cfg.seed)
+    ee = O.expected_exposure(O.exposure_paths_pc(mk, sw, cfg.n_steps, cfg.dt, normals))
+    nd = n_steps // stride
+    _assert_rel(v.ee[:nd + 1], ee[:nd + 1], FP64_RTOL, "EE")

@@ -202,3 +202,100 @@ def test_double_fp32_sums_track_fp64_sums(nt, stride, B, c):
         for q in range(2):
             assert abs(got[j][q] - want[j][q]) <= 2e-12 * abs(want[j][q]) + 1e-30, (j, q, got[j][q], want[j][q])
     assert abs(want[B][0]) > 1e-7  # the last date's remainder is well inside FP32's range
+
+
+# --- predictor-corrector -----------------------------------------------------
+def pc_step(v, c):
+    """A2: three-point stencil a0, a1, a2 below L-1; Euler rows at L-1, L."""
+    L = v.size - 1
+    a0, a1, a2 = 1 - c + c * c / 2, c - c * c, c * c / 2
+    vn = v.copy()
+    vn[:L - 1] = a0 * v[:L - 1] + a1 * v[1:L] + a2 * v[2:L + 1]
+    vn[L - 1] = v[L - 1] + c * (v[L] - v[L - 1])
+    vn[L] = v[L] + c * (v[L] - v[L - 1])
+    return vn
+
+
+def pc_sources(c, dtau):
+    return -c * c * dtau * dtau, -(2 * c + c * c) * dtau * dtau, -c * dtau * dtau  # wL1, wL, gL
+
+
+def response_table_pc(nt, stride, B, c, dtau):
+    """As response_table_kernel with pc = 1: the coefficient of the old W at
+    lag l is H1(l) + H2(l+1), H1 = wL1 G1 + (wL - gL) G2, H2 = gL G2."""
+    L = nt - 1
+    wL1, wL, gL = pc_sources(c, dtau)
+    w0, w1, w2 = wL1, wL - gL, gL
+    tab = np.zeros((B * stride * ROW, 2))
+    written = np.zeros(B * stride * ROW, dtype=int)
+    g1 = np.zeros(nt)
+    g1[L - 1] = 1.0
+    g2 = np.zeros(nt)
+    g2[L] = 1.0
+    cg1, cg2 = np.zeros(nt), np.zeros(nt)
+    h1p, ch1p = np.zeros(nt), np.zeros(nt)
+    for m in range((B - 1) * stride + 1):
+        cg1, cg2 = cg1 + g1, cg2 + g2
+        if m >= 1:
+            l = m - 1
+            for t in range(2, B + 1):
+                q = l // stride + 1
+                b = t - q
+                if b >= 1:
+                    idx = (b * stride + (q * stride - 1 - l)) * ROW + (B - t)
+                    tab[idx] = (h1p[t] + w2 * g2[t], ch1p[t] + w2 * cg2[t])
+                    written[idx] += 1
+        h1p, ch1p = w0 * g1 + w1 * g2, w0 * cg1 + w1 * cg2
+        g1, g2 = pc_step(g1, c), pc_step(g2, c)
+    return tab, written
+
+
+def n_active_pc(s, b, B, L, stride):
+    q_min = max(1, -(-(L - b + 2 * s) // (2 * stride + 1)))
+    return B - b - q_min + 1
+
+
+@pytest.mark.parametrize("nt,stride,B,c", SHAPES)
+def test_pc_table_covers_every_lag_once_and_prefix_holds_the_nonzeros(nt, stride, B, c):
+    tab, written = response_table_pc(nt, stride, B, c, 0.5)
+    L = nt - 1
+    assert written.max() <= 1
+    for b in range(1, B):
+        for s in range(stride):
+            n_act = n_active_pc(s, b, B, L, stride)
+            for r in range(ROW):
+                idx = (b * stride + s) * ROW + r
+                live = r < B - b
+                assert written[idx] == (1 if live and B - r >= 2 else 0)
+                if r >= max(n_act, 0):
+                    assert tab[idx, 0] == 0.0 and tab[idx, 1] == 0.0, (b, s, r)
+
+
+@pytest.mark.parametrize("nt,stride,B,c", SHAPES[:4])
+def test_pc_response_sums_equal_the_convected_remainder(nt, stride, B, c):
+    """The remainder of the predictor-corrector's polynomial form, driven at
+    L-1 by wL1 W and at L by wL W + gL gamma (gamma the step's curvature noise,
+    W the curvature before the step), against the response sums of the old W."""
+    dtau = 0.5
+    tab, _ = response_table_pc(nt, stride, B, c, dtau)
+    wL1, wL, gL = pc_sources(c, dtau)
+    L = nt - 1
+    rng = np.random.default_rng(3)
+    acc = np.zeros((ROW, 2))
+    hc, hsum = np.zeros(nt), np.zeros(nt)
+    W = 0.0
+    for b in range(1, B):
+        for s in range(stride):
+            n_act = n_active_pc(s, b, B, L, stride)
+            for r in range(max(n_act, 0)):
+                acc[r] += tab[(b * stride + s) * ROW + r] * W
+            gam = rng.normal() * 1e-5
+            hn = pc_step(hc, c)
+            hn[L - 1] += wL1 * W
+            hn[L] += wL * W + gL * gam
+            hc = hn
+            hsum += hc
+            W += gam
+        j = b + 1
+        for got, want in ((acc[B - j, 0], hc[j]), (acc[B - j, 1], hsum[j])):
+            assert abs(got - want) <= 1e-12 * abs(want) + 1e-300, (j, got, want)
