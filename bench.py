@@ -394,6 +394,8 @@ def run_ours(args) -> None:
         roofline["fp32_side"] = fp32_side
 
     if not args.no_extras and prec == "fp64":
+        if remainder == "response":
+            extras["fp64_convected_form"] = convected_form_run(eng, mk, sw, args, flush, stride, peak64, res)
         extras["generic_table_step"] = generic_step_run(eng, mk, sw, args, flush, stride, peak64, peak32)
         extras["predictor_corrector"] = predictor_corrector_run(eng, mk, sw, args, flush)
         extras["mlmc"] = mlmc_run(eng, mk, sw)
@@ -421,6 +423,9 @@ def run_ours(args) -> None:
                    "vol_form": ("quadratic factors (detected in the volatility table): decomposed step" if vol_form_poly
                                 else "volatility table: generic step"),
                    "remainder": remainder,
+                   "arithmetic": ("FP64 curve, pricing, discounting and reductions; the remainder's response sums "
+                                  "(<= 7e-5 of the curve) in double-FP32 (46-bit), see fp64_convected_form for the "
+                                  "all-FP64 form" if remainder == "response" and prec == "fp64" else None),
                    "parallelism": f"replicas{world}" if world > 1 else "single",
                    "l2": f"flushed between steps ({FLUSH_BYTES >> 20} MiB device write, inside the timed region)"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
@@ -526,6 +531,42 @@ def generic_step_run(eng, mk, sw, args, flush, stride, peak64, peak32) -> dict:
         eng.set_market(mk)
         eng.set_swap(sw)
     return out
+
+
+def convected_form_run(eng, mk, sw, args, flush, stride, peak64, res_resp) -> dict:
+    """The headline valuation with the decomposition's remainder convected in
+    FP64 over the live tenors (every operation of the curve in FP64), against
+    the response form's run on the same paths."""
+    import numpy as np
+    import torch
+
+    from cva_hjm_cuda_gb300 import RunConfig
+
+    n = WORKLOADS["fp64"]["n_paths"]
+    cfg = RunConfig(n_paths=n, n_steps=N_STEPS, dt=DT, seed=SEED)
+    eng.set_remainder_form("convect")
+    try:
+        for _ in range(args.warmup):
+            eng.enqueue(cfg, "fp64")
+            flush.zero_()
+        torch.cuda.synchronize()
+        for _ in range(args.steps):
+            eng.enqueue(cfg, "fp64")
+            flush.zero_()
+        torch.cuda.synchronize()
+        hist = eng.timing_history(min(args.steps, 64))
+        kern_ms, step_ms = float(hist[:, 0].mean()), float(hist[:, 3].mean())
+        res = eng.fetch()
+        assert eng.remainder_form() == "convect"
+    finally:
+        eng.set_remainder_form("auto")
+    fl = algorithmic_flops_per_path(mk.n_tenor, N_STEPS, stride, eng.vol_form()) * n
+    return {"n_paths": n, "path_steps_per_s": n * N_STEPS / (step_ms * 1e-3), "device_ms_per_step": step_ms,
+            "path_kernel_ms": kern_ms, "achieved_tflops": fl / (kern_ms * 1e-3) / 1e12,
+            "frac_of_measured_fma_peak": (fl / (kern_ms * 1e-3) / 1e12 / peak64) if peak64 else None,
+            "cva": res.cva, "response_form_cva": res_resp.cva,
+            "ee_max_rel_diff_vs_response_form": float(np.max(np.abs(res.ee[1:20] - res_resp.ee[1:20])
+                                                             / np.abs(res_resp.ee[1:20])))}
 
 
 def predictor_corrector_run(eng, mk, sw, args, flush) -> dict:
