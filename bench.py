@@ -88,15 +88,21 @@ def algorithmic_flops_per_path(n_tenor: int, n_steps: int, stride: int, form: st
     ADD or MUL issues like an FMA, so the fraction is a lower bound on the
     FP64 pipe's use (ncu's pipe utilisation is the direct measure).
 
-    ``remainder="response"`` (polynomial forms, FP64, at most 24 dates): the
+    ``remainder="response"`` (FP64, at most 24 dates): polynomial forms, the
     FP64 pipe does the scalar parts (9 FMA, or 12 for general quadratic
-    factors) and their running sums (3 ADD) per evolved step; the remainder's
+    factors) and their running sums (3 ADD) per evolved step, the remainder's
     impulse-response sums run in double-FP32 on the FP32 pipe
-    (``response_fp32_flops_per_path``); no block recovery."""
+    (``response_fp32_flops_per_path``); ``table``, six FP64 FMAs per date still
+    to be sampled per step (the three factors' responses, value and running
+    sum); no block recovery."""
     B = n_steps // stride
     L = n_tenor - 1
     if remainder == "response" and form != "table":
         return (21 if form == "poly_tri" else 27) * (B - 1) * stride
+    if remainder == "response":
+        # volatility table in the response form: per step and date still to be
+        # sampled, three FMAs for the value and three for the running sum
+        return 12 * stride * sum(B - b for b in range(1, B))
 
     def per_step(b: int, k: int) -> int:
         # polynomial forms: the remainder is still zero below tenor L - 1 - k
@@ -521,8 +527,10 @@ def generic_step_run(eng, mk, sw, args, flush, stride, peak64, peak32) -> dict:
             hist = eng.timing_history(min(args.steps, 64))
             kern_ms, step_ms = float(hist[:, 0].mean()), float(hist[:, 3].mean())
             res = eng.fetch()
-            fl = algorithmic_flops_per_path(mk.n_tenor, N_STEPS, stride, "table") * n
-            out[prec] = {"n_paths": n, "path_steps_per_s": n * N_STEPS / (step_ms * 1e-3), "device_ms_per_step": step_ms,
+            form = eng.remainder_form() if prec == "fp64" else "convect"
+            fl = algorithmic_flops_per_path(mk.n_tenor, N_STEPS, stride, "table", form) * n
+            out[prec] = {"n_paths": n, "remainder": form,
+                         "path_steps_per_s": n * N_STEPS / (step_ms * 1e-3), "device_ms_per_step": step_ms,
                          "path_kernel_ms": kern_ms, "achieved_tflops": fl / (kern_ms * 1e-3) / 1e12,
                          "frac_of_measured_fma_peak": (fl / (kern_ms * 1e-3) / 1e12 / peak) if peak else None,
                          "cva": res.cva}

@@ -81,7 +81,7 @@ struct hjm_ctx {
     bool keep_exposures = false;
 
     // device buffers
-    DevBuf partials, sums, result, estore, sel, hist, ext, ext_raw, wide, scratch, ck_h, ck_a, resp;
+    DevBuf partials, sums, result, estore, sel, hist, ext, ext_raw, wide, scratch, ck_h, ck_a, resp, vresp;
     // the response table in resp holds the run shape of resp_key; resp_used
     // is recorded after the last kernel that reads it
     struct RespKey {
@@ -89,6 +89,12 @@ struct hjm_ctx {
         int nt = 0, stride = 0, B = 0, scheme = 0;
         double c = 0, dtau = 0;
     } resp_key;
+    struct VrespKey {  // the volatility-table response table in vresp
+        bool valid = false;
+        int nt = 0, stride = 0, B = 0, scheme = 0;
+        double c = 0;
+        std::vector<double> sv;
+    } vresp_key;
     cudaEvent_t resp_used = nullptr;
 
     // last valuation
@@ -113,7 +119,7 @@ struct hjm_ctx {
         bool valid = false, adjoint = false, pfe = false, external_normals = false;
         int64_t n_paths = 0;
         int n_steps = 0, n_dates = 0, precision = 0, vol_form = 0, ckpt = 0, nt = 0, scheme = 0;
-        int remainder = 0;  // 0 none (table step), 1 convected, 2 impulse responses
+        int remainder = 0;  // 1 convected, 2 impulse responses (0: not a valuation)
         double dt = 0, dtau = 0, hazard = 0, recovery = 0, pfe_q = 0;
         uint64_t seed = 0, path_offset = 0;
         std::vector<double> ee, pfe_v, dspot, ddrift;
@@ -210,7 +216,7 @@ hjm_status hjm_ctx_destroy(hjm_ctx* ctx)
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     for (DevBuf* b : {&ctx->partials, &ctx->sums, &ctx->result, &ctx->estore, &ctx->sel, &ctx->hist, &ctx->ext,
-                      &ctx->ext_raw, &ctx->wide, &ctx->scratch, &ctx->ck_h, &ctx->ck_a, &ctx->resp})
+                      &ctx->ext_raw, &ctx->wide, &ctx->scratch, &ctx->ck_h, &ctx->ck_a, &ctx->resp, &ctx->vresp})
         b->release();
     if (ctx->resp_used) cudaEventDestroy(ctx->resp_used);
     for (auto& q : ctx->ring)
@@ -639,17 +645,64 @@ static void fill_pc(const hjm_ctx* ctx, const RunShape& sh, double dt, const Pat
 // convection (one FMA per live tenor and ~17 per step for Euler, two and ~20
 // for the predictor-corrector), summed over the evolved blocks; the response
 // terms count as two FMAs per date still to be sampled.
+//
+// Volatility-table step (no decomposition): the whole stochastic curve in
+// impulse responses, six FP64 FMAs per date still to be sampled per step,
+// against four FMAs per live tenor (five for the predictor-corrector) and ~10
+// per step.
 static bool use_response_form(const hjm_ctx* ctx, const RunShape& sh)
 {
-    if (!use_poly_path(ctx) || sh.B > response_max_dates()) return false;
+    if (sh.B > response_max_dates()) return false;
     if (ctx->remainder != HJM_REMAINDER_AUTO) return ctx->remainder == HJM_REMAINDER_RESPONSE;
     const bool pc = ctx->scheme == HJM_SCHEME_PREDICTOR_CORRECTOR;
+    const bool poly = use_poly_path(ctx);
     long conv = 0, resp = 0;
     for (int b = 1; b < sh.B; ++b) {
-        conv += pc ? 2 * (ctx->nt - 1 - b) + 20 : (ctx->nt - 1 - b) + 17;
-        resp += 2 * (sh.B - b) + 12;
+        const int live = ctx->nt - 1 - b;
+        if (poly) {
+            conv += pc ? 2 * live + 20 : live + 17;
+            resp += 2 * (sh.B - b) + 12;
+        } else {
+            conv += pc ? 5 * live + 12 : 4 * live + 10;
+            resp += 6 * (sh.B - b);
+        }
     }
     return resp < conv;
+}
+
+// The volatility-table response table of the run shape, scheme and loadings
+// sv [kFactors][kMaxTenor] (the path parameters'), as ensure_response_table.
+static hjm_status ensure_vol_response_table(hjm_ctx* ctx, const RunShape& sh, double dt, const double* sv,
+                                            cudaStream_t s)
+{
+    const double c = dt / ctx->dtau;
+    const int nt = ctx->nt;
+    std::vector<double> key((size_t)kFactors * nt);
+    for (int k = 0; k < kFactors; ++k)
+        for (int t = 0; t < nt; ++t) key[(size_t)k * nt + t] = sv[k * kMaxTenor + t];
+    hjm_ctx::VrespKey& k = ctx->vresp_key;
+    if (!ctx->resp_used) HJM_CUDA(ctx, cudaEventCreateWithFlags(&ctx->resp_used, cudaEventDisableTiming));
+    if (k.valid && k.nt == nt && k.stride == sh.stride && k.B == sh.B && k.c == c && k.scheme == ctx->scheme &&
+        k.sv == key)
+        return HJM_OK;
+    k.valid = false;
+    const size_t bytes = sizeof(double2) * response_table_vol_elems(sh.stride, sh.B);
+    if (bytes > ctx->vresp.bytes)
+        HJM_CUDA(ctx, ctx->vresp.ensure(bytes));  // cudaFree waits for the device
+    else
+        HJM_CUDA(ctx, cudaStreamWaitEvent(s, ctx->resp_used, 0));
+    HJM_CUDA(ctx, cudaMemsetAsync(ctx->vresp.p, 0, bytes, s));  // entries the kernel reads as exact zeros
+    HJM_CUDA(ctx, launch_response_table_vol(nt, c, sh.stride, sh.B, ctx->scheme == HJM_SCHEME_PREDICTOR_CORRECTOR, sv,
+                                            (double2*)ctx->vresp.p, s));
+    ctx->stat_launches += 1;
+    k.nt = nt;
+    k.stride = sh.stride;
+    k.B = sh.B;
+    k.c = c;
+    k.scheme = ctx->scheme;
+    k.sv = key;
+    k.valid = true;
+    return HJM_OK;
 }
 
 // The response table of the run shape and scheme, on the stream: recomputed
@@ -703,7 +756,7 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
     if (st != HJM_OK) return st;
     HJM_CUDA(ctx, cudaSetDevice(ctx->device));
     const bool mixed = precision == HJM_PRECISION_MIXED;
-    if (!mixed && ctx->remainder == HJM_REMAINDER_RESPONSE && use_poly_path(ctx) && sh.B > response_max_dates())
+    if (!mixed && ctx->remainder == HJM_REMAINDER_RESPONSE && sh.B > response_max_dates())
         return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "the response form holds at most %d dates (run has %d)",
                     response_max_dates(), sh.B);
     const bool want_pfe = pfe_q > 0.0;
@@ -751,13 +804,21 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
         fill_pc<double>(ctx, sh, dt, P, Q);
         ctx->stat_h2d = sizeof(Q) + sizeof(FinalParams);
         resp = use_response_form(ctx, sh);
-        if (resp) {
-            st = ensure_response_table(ctx, sh, dt, s);
+        if (resp && !use_poly_path(ctx)) {
+            st = ensure_vol_response_table(ctx, sh, dt, &Q.P.sv[0][0], s);
             if (st != HJM_OK) return st;
+            HJM_CUDA(ctx, launch_path_fp64_vresp(ctx->nt, Q.P, (const double2*)ctx->vresp.p, ext_dev,
+                                                 (double*)ctx->partials.p, store ? (double*)ctx->estore.p : nullptr,
+                                                 s));
+        } else {
+            if (resp) {
+                st = ensure_response_table(ctx, sh, dt, s);
+                if (st != HJM_OK) return st;
+            }
+            HJM_CUDA(ctx, launch_path_pc(ctx->nt, Q, use_poly_path(ctx), resp ? (const float4*)ctx->resp.p : nullptr,
+                                         ext_dev, (double*)ctx->partials.p,
+                                         store ? (double*)ctx->estore.p : nullptr, s));
         }
-        HJM_CUDA(ctx, launch_path_pc(ctx->nt, Q, use_poly_path(ctx), resp ? (const float4*)ctx->resp.p : nullptr,
-                                     ext_dev, (double*)ctx->partials.p, store ? (double*)ctx->estore.p : nullptr,
-                                     s));
         if (resp) HJM_CUDA(ctx, cudaEventRecord(ctx->resp_used, s));
     } else if (mixed) {
         PathParams<float> P;
@@ -770,13 +831,21 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
         PathParams<double> P;
         fill_params<double>(ctx, sh, n_paths, dt, seed, path_offset, hazard, recovery, ld, store, P, F);
         resp = use_response_form(ctx, sh);
-        if (resp) {
-            st = ensure_response_table(ctx, sh, dt, s);
+        if (resp && !use_poly_path(ctx)) {
+            st = ensure_vol_response_table(ctx, sh, dt, &P.sv[0][0], s);
             if (st != HJM_OK) return st;
+            HJM_CUDA(ctx, launch_path_fp64_vresp(ctx->nt, P, (const double2*)ctx->vresp.p, ext_dev,
+                                                 (double*)ctx->partials.p, store ? (double*)ctx->estore.p : nullptr,
+                                                 s));
+        } else {
+            if (resp) {
+                st = ensure_response_table(ctx, sh, dt, s);
+                if (st != HJM_OK) return st;
+            }
+            HJM_CUDA(ctx, launch_path_fp64(ctx->nt, P, use_poly_path(ctx),
+                                           resp ? (const float4*)ctx->resp.p : nullptr, ext_dev,
+                                           (double*)ctx->partials.p, store ? (double*)ctx->estore.p : nullptr, s));
         }
-        HJM_CUDA(ctx, launch_path_fp64(ctx->nt, P, use_poly_path(ctx), resp ? (const float4*)ctx->resp.p : nullptr,
-                                       ext_dev, (double*)ctx->partials.p, store ? (double*)ctx->estore.p : nullptr,
-                                       s));
         if (resp) HJM_CUDA(ctx, cudaEventRecord(ctx->resp_used, s));
     }
     HJM_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
@@ -811,7 +880,7 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
         r.path_offset = path_offset;
         r.external_normals = ext_dev != nullptr;
         r.scheme = ctx->scheme;
-        r.remainder = resp ? 2 : use_poly_path(ctx) ? 1 : 0;
+        r.remainder = resp ? 2 : 1;
     }
     ctx->last_n_paths = n_paths;
     ctx->last_n_dates = n_dates;
@@ -1126,7 +1195,7 @@ hjm_status hjm_run_adjoint(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, doubl
     r.nt = nt;
     r.precision = HJM_PRECISION_MIXED;
     r.vol_form = vol_form_code(ctx);
-    r.remainder = use_poly_path(ctx) ? 1 : 0;
+    r.remainder = 1;
     r.ckpt = K;
     r.dt = dt;
     r.dtau = ctx->dtau;
@@ -1280,7 +1349,7 @@ hjm_status hjm_run_mlmc(hjm_ctx* ctx, int32_t n_levels, const int64_t* n_paths, 
         r.nt = nt;
         r.precision = HJM_PRECISION_MIXED;
         r.vol_form = vol_form_code(ctx);
-        r.remainder = use_poly_path(ctx) ? 1 : 0;
+        r.remainder = 1;
         r.dtau = ctx->dtau;
         r.hazard = hazard_rate;
         r.recovery = recovery;

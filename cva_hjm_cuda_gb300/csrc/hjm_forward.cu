@@ -477,6 +477,136 @@ __device__ __forceinline__ void mixed_epilogue(const PathParams<float>& P, const
     }
 }
 
+// Response form of the volatility-table step (FP64, any factor shapes, at most
+// kRespDates dates, both time schemes).  Without a polynomial part the whole
+// stochastic curve is driven by the injected noise: h_n = A h_{n-1} + S phi_n
+// (A the upwind step, or the predictor-corrector's A2 with the loadings S
+// N-projected), so at date j's tenor after step K
+//     h_K[j] = sum_{n<=K} sum_k phi_{n,k} R_jk(K - n),   R_jk(l) = (A^l S_k)[j],
+// and its running sum likewise with CR_jk(l) = sum_{r<=l} R_jk(r).  Per step
+// and date still to be sampled: six FP64 FMAs (three factors, value and sum)
+// on coefficients read from the table (response_table_vol_kernel), in place of
+// four FMAs per live tenor and the block-end recovery.  FP64 throughout: here
+// the response sums are the curve's whole stochastic part, so no double-FP32
+// shortcut keeps FP64 accuracy.  Entry (row b stride + s, slot B - j) holds
+// three double2 {R_jk, CR_jk} at lag (j - b) stride - 1 - s.
+template <int NT, bool EXT>
+__global__ void __launch_bounds__(kFp64Cta, 6)
+    path_kernel_fp64_vresp(const __grid_constant__ PathParams<double> P, const double2* __restrict__ vresp,
+                           const double* __restrict__ ext, double* __restrict__ partials,
+                           double* __restrict__ estore)
+{
+    constexpr int kCta = kFp64Cta;
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int tid = threadIdx.x;
+    const int B = P.n_blocks;
+    double* cf_s = reinterpret_cast<double*>(smem);
+    double* red_s = cf_s + (size_t)(B + 2) * kCta;
+
+    const int64_t cta_base = (int64_t)blockIdx.x * kCta;
+    const int64_t lp = cta_base + tid;
+    const bool active = lp < P.n_paths;
+    const uint64_t gpath = P.path_offset + (uint64_t)lp;
+
+    double a[kRespSlots], ai[kRespSlots];  // h at tenor j and its running sum, slot B - j
+#pragma unroll
+    for (int r = 0; r < kRespSlots; ++r) a[r] = ai[r] = 0.0;
+
+    auto sample = [&](int i) {
+        const double h = i >= 2 ? select_reg<kRespSlots, double>(a, B - i) : 0.0;
+        const double hs = i >= 2 ? select_reg<kRespSlots, double>(ai, B - i) : 0.0;
+        const double x = P.psamp[i] + h;
+        const double D = exp(-(P.psum[i] + hs) * P.dt);
+        const double Lb = P.m * (exp(x / P.m) - 1.0);
+        cf_s[i * kCta + tid] = D * (P.payA[i] * Lb - P.payB[i]);
+    };
+
+    sample(1);
+    for (int b = 1; b < B; ++b) {
+        const double2* row = vresp + (size_t)b * P.stride * kRespRow * 3;
+        const int n_act = B - b;  // every date still to be sampled (the factors reach every tenor)
+        for (int s = 0; s < P.stride; ++s) {
+            const int n = b * P.stride + s;
+            double phi0, phi1, phi2;
+            draw_phi<double, EXT>(ext, gpath, active ? lp : 0, P.n_paths, n, P.rk0, P.rk1, phi0, phi1, phi2);
+            const double2* rr = row + (size_t)s * kRespRow * 3;
+            resp_groups(n_act, [&](auto gc) {
+                constexpr int G = decltype(gc)::value;
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const double2* e = rr + (4 * G + u) * 3;
+                    const double2 k0 = __ldg(e), k1 = __ldg(e + 1), k2 = __ldg(e + 2);
+                    a[4 * G + u] = fma(k2.x, phi2, fma(k1.x, phi1, fma(k0.x, phi0, a[4 * G + u])));
+                    ai[4 * G + u] = fma(k2.y, phi2, fma(k1.y, phi1, fma(k0.y, phi0, ai[4 * G + u])));
+                }
+            });
+        }
+        sample(b + 1);
+    }
+    fp64_epilogue<kCta>(P, cf_s, cf_s + kCta, red_s, partials, estore, cta_base, active);
+}
+
+// Loadings of the three factors on the tenor grid (sqrt(dt) sigma_k, the
+// predictor-corrector's N-projected ones), by value.
+struct VolLoadings {
+    double sv[kFactors][kMaxTenor];
+};
+
+// The table of path_kernel_fp64_vresp: R_jk(m) = (A^m S_k)[j] by m applications
+// of the upwind step (Euler: backward difference at L, simulation_cpu.h:96-108)
+// or of A2 (predictor-corrector: three-point stencil, Euler rows at L-1, L),
+// and their running sums; the lag -> entry map of response_table_kernel.  One
+// CTA of kMaxTenor threads, thread t holding tenor t of the three responses.
+__global__ void __launch_bounds__(kMaxTenor)
+    response_table_vol_kernel(int nt, double c, int stride, int B, int pc, const __grid_constant__ VolLoadings S,
+                              double2* __restrict__ vresp)
+{
+    __shared__ double v_s[kFactors][kMaxTenor];
+    const int t = threadIdx.x;
+    const int L = nt - 1;
+    const int M = (B - 1) * stride - 1;
+    const double a0 = 1.0 - c + 0.5 * c * c, a1 = c - c * c, a2 = 0.5 * c * c;
+    double v[kFactors], cum[kFactors];
+#pragma unroll
+    for (int k = 0; k < kFactors; ++k) {
+        v[k] = t < nt ? S.sv[k][t] : 0.0;
+        cum[k] = 0.0;
+    }
+    for (int m = 0; m <= M; ++m) {
+#pragma unroll
+        for (int k = 0; k < kFactors; ++k) cum[k] += v[k];
+        if (t >= 2 && t <= B) {
+            const int q = m / stride + 1;
+            const int b = t - q;
+            if (b >= 1) {
+                double2* e = vresp + (((size_t)b * stride + (size_t)(q * stride - 1 - m)) * kRespRow + (B - t)) * 3;
+#pragma unroll
+                for (int k = 0; k < kFactors; ++k) e[k] = make_double2(v[k], cum[k]);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < kFactors; ++k) v_s[k][t] = v[k];
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kFactors; ++k) {
+            if (!pc) {
+                if (t < L)
+                    v[k] += c * (v_s[k][t + 1] - v[k]);
+                else if (t == L)
+                    v[k] += c * (v[k] - v_s[k][L - 1]);
+            } else {
+                if (t < L - 1)
+                    v[k] = a0 * v[k] + a1 * v_s[k][t + 1] + a2 * v_s[k][t + 2];
+                else if (t == L - 1)
+                    v[k] += c * (v_s[k][L] - v[k]);
+                else if (t == L)
+                    v[k] += c * (v[k] - v_s[k][L - 1]);
+            }
+        }
+        __syncthreads();
+    }
+}
+
 // Mixed precision with packed FP32x2 arithmetic.  The curve of one path is held
 // as H = ceil(NT/2) float2 pairs, pair p = {h[p], h[p+H]}: the upwind neighbour
 // h[t+1] of every tenor lies in the same component of pair p+1, so each packed
@@ -839,6 +969,44 @@ cudaError_t launch_path_fp64(int nt, const PathParams<double>& P, bool poly, con
     if (nt == 51) return launch_fp64_nt<51>(P, poly, resp, ext, partials, estore, s);
     if (nt == 61) return launch_fp64_nt<61>(P, poly, resp, ext, partials, estore, s);
     return cudaErrorInvalidValue;
+}
+
+template <int NT, bool EXT>
+static cudaError_t launch_fp64_vresp_t(const PathParams<double>& P, const double2* vresp, const double* ext,
+                                       double* partials, double* estore, cudaStream_t s)
+{
+    const size_t smem = resp_smem_bytes(P.n_blocks);
+    auto k = path_kernel_fp64_vresp<NT, EXT>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const int64_t grid = (P.n_paths + kFp64Cta - 1) / kFp64Cta;
+    k<<<(unsigned)grid, kFp64Cta, smem, s>>>(P, vresp, ext, partials, estore);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_path_fp64_vresp(int nt, const PathParams<double>& P, const double2* vresp, const double* ext,
+                                   double* partials, double* estore, cudaStream_t s)
+{
+    if (!vresp || P.n_blocks > kRespDates) return cudaErrorInvalidValue;
+    if (nt == 51) return ext ? launch_fp64_vresp_t<51, true>(P, vresp, ext, partials, estore, s)
+                             : launch_fp64_vresp_t<51, false>(P, vresp, ext, partials, estore, s);
+    if (nt == 61) return ext ? launch_fp64_vresp_t<61, true>(P, vresp, ext, partials, estore, s)
+                             : launch_fp64_vresp_t<61, false>(P, vresp, ext, partials, estore, s);
+    return cudaErrorInvalidValue;
+}
+
+size_t response_table_vol_elems(int stride, int n_blocks) { return (size_t)n_blocks * stride * kRespRow * 3; }
+
+cudaError_t launch_response_table_vol(int nt, double c, int stride, int n_blocks, bool pc, const double* sv,
+                                      double2* vresp, cudaStream_t s)
+{
+    if (nt < 3 || nt > kMaxTenor || n_blocks > kRespDates || n_blocks >= nt || stride < 1) return cudaErrorInvalidValue;
+    VolLoadings S;
+    std::memset(&S, 0, sizeof(S));
+    for (int k = 0; k < kFactors; ++k)
+        for (int t = 0; t < nt; ++t) S.sv[k][t] = sv[k * kMaxTenor + t];
+    response_table_vol_kernel<<<1, kMaxTenor, 0, s>>>(nt, c, stride, n_blocks, pc ? 1 : 0, S, vresp);
+    return cudaGetLastError();
 }
 
 int response_max_dates() { return kRespDates; }

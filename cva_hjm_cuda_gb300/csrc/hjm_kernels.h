@@ -54,6 +54,14 @@ constexpr int kFormPolyTri = 2;  // ... with factor k of degree <= k
 cudaError_t launch_path_fp64(int nt, const PathParams<double>& P, bool poly, const float4* resp, const double* ext,
                              double* partials, double* estore, cudaStream_t s);
 int response_max_dates();
+// The response form of the volatility-table step (FP64, either scheme: the
+// table carries the scheme): vresp from launch_response_table_vol with the
+// kernel's loadings sv [kFactors][kMaxTenor] (PathParams::sv)
+cudaError_t launch_path_fp64_vresp(int nt, const PathParams<double>& P, const double2* vresp, const double* ext,
+                                   double* partials, double* estore, cudaStream_t s);
+size_t response_table_vol_elems(int stride, int n_blocks);  // double2 entries
+cudaError_t launch_response_table_vol(int nt, double c, int stride, int n_blocks, bool pc, const double* sv,
+                                      double2* vresp, cudaStream_t s);
 size_t response_table_elems(int stride, int n_blocks);  // float4 entries of the table
 // Euler: w1 = kappa = -2 c dtau^2 (w0, w2 unused); predictor-corrector: w0 =
 // wL1, w1 = wL - gL, w2 = gL (PcParams)

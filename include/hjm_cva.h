@@ -105,25 +105,29 @@ hjm_status hjm_ctx_set_scheme(hjm_ctx* ctx, int32_t scheme);
 hjm_status hjm_ctx_set_vol_decomposition(hjm_ctx* ctx, int32_t enable);
 hjm_status hjm_ctx_vol_decomposition(hjm_ctx* ctx, int32_t* active);
 
-/* FP64 form of the decomposition's remainder.  The remainder is driven only at
- * the last tenor (the last two for the predictor-corrector) and priced only at
- * each date's own tenor, so an FP64 valuation either convects it over the
- * live tenors every step (HJM_REMAINDER_CONVECT) or carries, for each date
- * still to be sampled, its value and running sum as sums of impulse responses
- * of the convection (HJM_REMAINDER_RESPONSE: one double-FP32 term per such
- * date per step, on the FP32 pipe, at most
- * HJM_RESPONSE_MAX_DATES dates, a run with more fails with
- * HJM_ERR_INVALID_ARGUMENT).  HJM_REMAINDER_AUTO (default) takes the form with
- * fewer FP64 operations for the run.  Both time schemes; the forms agree to
- * rounding; mixed precision and the table step do not use this setting.  The
- * report names the form a valuation ran ("remainder"). */
+/* FP64 transport form.  The pricing reads the stochastic curve only at each
+ * date's own tenor.  With the polynomial decomposition the remainder, driven
+ * only at the last tenor (the last two for the predictor-corrector), is either
+ * convected over the live tenors every step (HJM_REMAINDER_CONVECT) or carried,
+ * for each date still to be sampled, as its value and running sum in impulse
+ * responses of the convection (HJM_REMAINDER_RESPONSE: one double-FP32 term
+ * per such date per step, on the FP32 pipe; the remainder is ~1e-5 of the
+ * curve).  With a volatility table of any shape (no decomposition) the whole
+ * stochastic curve is either convected with the noise injected at every tenor,
+ * or carried in the response form as sums of the three factors' impulse
+ * responses (six FP64 FMAs per date per step).  The response form holds at
+ * most HJM_RESPONSE_MAX_DATES dates (a run with more fails with
+ * HJM_ERR_INVALID_ARGUMENT when it is forced).  HJM_REMAINDER_AUTO (default)
+ * takes the form with fewer FP64 operations for the run.  Both time schemes;
+ * the forms agree to rounding; mixed precision always convects.  The report
+ * names the form a valuation ran ("remainder"). */
 #define HJM_REMAINDER_AUTO 0
 #define HJM_REMAINDER_CONVECT 1
 #define HJM_REMAINDER_RESPONSE 2
 #define HJM_RESPONSE_MAX_DATES 24
 hjm_status hjm_ctx_set_remainder_form(hjm_ctx* ctx, int32_t form);
-/* The remainder form of the last valuation enqueued: 0 none (the table step),
- * HJM_REMAINDER_CONVECT or HJM_REMAINDER_RESPONSE. */
+/* The transport form of the last valuation enqueued: HJM_REMAINDER_CONVECT or
+ * HJM_REMAINDER_RESPONSE. */
 hjm_status hjm_ctx_remainder_form(hjm_ctx* ctx, int32_t* form);
 
 /* ---- inputs --------------------------------------------------------------- */

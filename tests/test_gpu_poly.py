@@ -326,7 +326,78 @@ def test_remainder_form_choice_and_limits(engine, remainder_form, tmp_path):
     assert "24 dates" in str(ei.value)
     engine.set_market(Market(vol=Market().vol * (1.0 + 0.1 * np.cos(np.arange(51) / 7.0))[None, :]))
     engine.set_swap(Swap())
+    remainder_form("auto")
     engine.run(RunConfig(n_paths=256), "fp64")
-    assert engine.remainder_form() == "none"  # table step: no remainder
+    assert engine.remainder_form() == "response"  # table step: the factors' responses
+    remainder_form("convect")
+    engine.run(RunConfig(n_paths=256), "fp64")
+    assert engine.remainder_form() == "convect"
     with pytest.raises(_lib.HJMError):
         _lib.check(engine.lib.hjm_ctx_set_remainder_form(engine.ctx, 7), engine.ctx)
+
+
+# ---------------------------------------------------------------------------
+# the volatility-table step (a table of any shape) in the response form: the
+# whole stochastic curve as FP64 sums of the three factors' impulse responses
+# ---------------------------------------------------------------------------
+def _bumpy_market(nt=51):
+    mk = Market(n_tenor=nt)
+    return Market(n_tenor=nt, vol=mk.vol * (1.0 + 0.1 * np.cos(np.arange(nt) / 7.0))[None, :])
+
+
+@pytest.mark.parametrize("scheme", ["euler", "predictor_corrector"])
+@pytest.mark.parametrize("nt", [51, 61])
+def test_table_step_response_vs_convected_and_oracle(engine, remainder_form, scheme, nt):
+    mk = _bumpy_market(nt)
+    sw = Swap(n_tenor=nt)
+    engine.set_scheme(scheme)
+    try:
+        engine.set_market(mk)
+        engine.set_swap(sw)
+        assert engine.vol_form() == "table"
+        cfg = RunConfig(n_paths=2500, seed=31)
+        out = {}
+        engine.keep_exposures(True)
+        for form in ("convect", "response"):
+            remainder_form(form)
+            out[form] = (engine.run(cfg, "fp64"), engine.exposures())
+            assert engine.remainder_form() == form
+        remainder_form("auto")
+        normals = engine.dump_normals(cfg.n_paths, cfg.n_steps, cfg.seed)
+        ext = engine.run_with_normals(normals, cfg.n_steps, cfg.dt, "fp64")
+        assert engine.remainder_form() == "response"
+    finally:
+        engine.keep_exposures(False)
+        engine.set_scheme("euler")
+    (vc, xc), (vr, xr) = out["convect"], out["response"]
+    _assert_rel(xr, xc, 1e-11, "exposures response vs convect")
+    paths = O.exposure_paths_pc if scheme == "predictor_corrector" else O.exposure_paths
+    x = paths(mk, sw, cfg.n_steps, cfg.dt, normals)
+    ee = O.expected_exposure(x)
+    cva, _ = O.cva(ee, 21, mk.dtau, cfg.hazard, cfg.recovery)
+    _assert_rel(xr, x[:, :21].T, FP64_RTOL, "exposures vs oracle")
+    _assert_rel(vr.ee[:21], ee[:21], FP64_RTOL, "EE vs oracle")
+    _assert_rel(vr.cva, cva, FP64_RTOL, "CVA vs oracle")
+    _assert_rel(vr.pfe[:21], O.pfe(x, 21, cfg.pfe_quantile), FP64_RTOL, "PFE vs oracle")
+    np.testing.assert_array_equal(ext.ee, vr.ee)
+
+
+@pytest.mark.parametrize("n_paths,n_steps,dt", [(1, 1000, 0.01), (257, 1200, 0.01), (63, 500, 0.02)],
+                         ids=["1-path", "24-dates", "stride25"])
+def test_table_step_response_shapes_vs_oracle(engine, remainder_form, n_paths, n_steps, dt):
+    mk = _bumpy_market()
+    engine.set_market(mk)
+    stride = int(round(mk.dtau / dt))
+    sw = Swap(n_periods=n_steps // stride)
+    engine.set_swap(sw)
+    remainder_form("response")
+    cfg = RunConfig(n_paths=n_paths, n_steps=n_steps, dt=dt, seed=8)
+    v = engine.run(cfg, "fp64")
+    assert engine.remainder_form() == "response"
+    normals = engine.dump_normals(cfg.n_paths, cfg.n_steps, cfg.seed)
+    x = O.exposure_paths(mk, sw, cfg.n_steps, cfg.dt, normals)
+    ee = O.expected_exposure(x)
+    nd = n_steps // stride
+    cva, _ = O.cva(ee, nd + 1, mk.dtau, cfg.hazard, cfg.recovery)
+    _assert_rel(v.ee[:nd + 1], ee[:nd + 1], FP64_RTOL, "EE")
+    _assert_rel(v.cva, cva, FP64_RTOL, "CVA")

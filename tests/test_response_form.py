@@ -299,3 +299,48 @@ def test_pc_response_sums_equal_the_convected_remainder(nt, stride, B, c):
         j = b + 1
         for got, want in ((acc[B - j, 0], hc[j]), (acc[B - j, 1], hsum[j])):
             assert abs(got - want) <= 1e-12 * abs(want) + 1e-300, (j, got, want)
+
+
+# --- volatility-table step: the whole stochastic curve in factor responses ---
+def euler_step(v, c):
+    L = v.size - 1
+    vn = v.copy()
+    vn[:L] = v[:L] + c * (v[1:] - v[:L])
+    vn[L] = v[L] + c * (v[L] - v[L - 1])
+    return vn
+
+
+@pytest.mark.parametrize("scheme", ["euler", "pc"])
+@pytest.mark.parametrize("nt,stride,B,c", SHAPES[:4])
+def test_vol_table_response_sums_equal_the_direct_recursion(scheme, nt, stride, B, c):
+    """As response_table_vol_kernel and path_kernel_fp64_vresp: entry (step,
+    slot B - j, factor k) = (R_jk, CR_jk) at lag l, R_jk(l) = (A^l S_k)[j]; the
+    sums over steps of R phi equal h <- A h + S phi at the dates."""
+    step = pc_step if scheme == "pc" else euler_step
+    L = nt - 1
+    rng = np.random.default_rng(11)
+    S = rng.uniform(0.001, 0.01, size=(3, nt)) * np.sqrt(c * 0.5)
+    tab = np.zeros((B * stride * ROW, 3, 2))
+    v = S.copy()
+    cum = np.zeros_like(S)
+    for m in range((B - 1) * stride):
+        cum = cum + v
+        for t in range(2, B + 1):
+            q = m // stride + 1
+            b = t - q
+            if b >= 1:
+                tab[(b * stride + (q * stride - 1 - m)) * ROW + (B - t)] = np.stack([v[:, t], cum[:, t]], axis=1)
+        v = np.stack([step(v[k], c) for k in range(3)])
+    acc = np.zeros((ROW, 2))
+    h, hsum = np.zeros(nt), np.zeros(nt)
+    for b in range(1, B):
+        for s in range(stride):
+            phi = rng.normal(size=3)
+            for r in range(B - b):
+                e = tab[(b * stride + s) * ROW + r]
+                acc[r] += e.T @ phi
+            h = step(h, c) + S.T @ phi
+            hsum += h
+        j = b + 1
+        for got, want in ((acc[B - j, 0], h[j]), (acc[B - j, 1], hsum[j])):
+            assert abs(got - want) <= 1e-12 * abs(want) + 1e-300, (j, got, want)
