@@ -401,3 +401,45 @@ def test_table_step_response_shapes_vs_oracle(engine, remainder_form, n_paths, n
     cva, _ = O.cva(ee, nd + 1, mk.dtau, cfg.hazard, cfg.recovery)
     _assert_rel(v.ee[:nd + 1], ee[:nd + 1], FP64_RTOL, "EE")
     _assert_rel(v.cva, cva, FP64_RTOL, "CVA")
+
+
+def test_response_tables_follow_shape_market_and_scheme(engine):
+    """The context caches the response tables per run shape, scheme and (table
+    step) loadings: alternating them on one context gives bit for bit what a
+    fresh context gives for each case."""
+    from cva_hjm_cuda_gb300 import HJMEngine
+
+    cases = [
+        ("poly", "euler", RunConfig(n_paths=700, seed=2)),
+        ("table", "euler", RunConfig(n_paths=700, seed=2)),
+        ("poly", "euler", RunConfig(n_paths=700, n_steps=500, dt=0.02, seed=2)),
+        ("table2", "predictor_corrector", RunConfig(n_paths=700, seed=2)),
+        ("table", "predictor_corrector", RunConfig(n_paths=700, seed=2)),
+        ("poly", "predictor_corrector", RunConfig(n_paths=700, n_steps=1200, seed=2)),
+        ("poly", "euler", RunConfig(n_paths=700, seed=2)),
+    ]
+
+    def setup(eng, market, scheme, cfg):
+        eng.set_scheme(scheme)
+        if market == "poly":
+            eng.set_market(Market())
+        else:
+            bump = 0.1 if market == "table" else -0.07
+            eng.set_market(Market(vol=Market().vol * (1.0 + bump * np.cos(np.arange(51) / 7.0))[None, :]))
+        stride = int(round(0.5 / cfg.dt))
+        eng.set_swap(Swap(n_periods=cfg.n_steps // stride))
+
+    got = []
+    try:
+        for market, scheme, cfg in cases:
+            setup(engine, market, scheme, cfg)
+            got.append(engine.run(cfg, "fp64"))
+            assert engine.remainder_form() == "response"
+    finally:
+        engine.set_scheme("euler")
+    for (market, scheme, cfg), g in zip(cases, got):
+        with HJMEngine(0) as fresh:
+            setup(fresh, market, scheme, cfg)
+            f = fresh.run(cfg, "fp64")
+        np.testing.assert_array_equal(g.ee, f.ee)
+        assert g.cva == f.cva
