@@ -395,7 +395,12 @@ def run_ours(args) -> None:
                            f"path_kernel_mixed<{mk.n_tenor},philox,{form}>"),
                 "algorithmic_flops_per_launch": flops, "avg_launch_ms": path_ms,
                 "peak_source": "measured live by bench.py (FMA microkernel, this GPU)",
-                "hbm_peak_gbs_measured": _measured_hbm()}
+                "hbm_peak_gbs_measured": _measured_hbm(),
+                # the reference's Euler step, 11 flops per tenor per path-step,
+                # at this run's rate (the kernel runs an exact reformulation
+                # with far fewer operations; not a roofline of this kernel)
+                "reference_equivalent_tflops": 11 * mk.n_tenor * world * n_paths * n_steps * args.steps
+                / elapsed / 1e12 if not is_adjoint else None}
     if fp32_side:
         roofline["fp32_side"] = fp32_side
 
