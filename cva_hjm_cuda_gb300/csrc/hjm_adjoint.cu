@@ -51,6 +51,7 @@
 #include "hjm_device.cuh"
 #include "hjm_kernels.h"
 #include "hjm_pairs.cuh"
+#include "hjm_pc.cuh"
 
 namespace hjm {
 
@@ -440,6 +441,262 @@ __global__ void __launch_bounds__(kAdjCta, adj_min_ctas<NT>())
         for (int w = 0; w < kCtaA / 32; ++w) sum += wred[w * R + col];
         partials[(size_t)blockIdx.x * R + col] = sum;
     }
+}
+
+// ---------------------------------------------------------------------------
+// Predictor-corrector adjoint (mixed precision; the sampled states are kept,
+// checkpoint_every = 0).  The forward pass is the valuation's (PcPath: FP32
+// curve with the effective scheme a0e, a1e, a2e and Euler rows with ce at
+// L-1, L; FP64 discount sums), so the CVA equals the predictor-corrector
+// valuation's bit for bit.  The reverse sweep carries the per-tenor adjoint
+// through the transpose of that scheme,
+//     (A2^T v)[t] = a0e v[t] + a1e v[t-1] + a2e v[t-2]                 (t <= L-2),
+//     (A2^T v)[L-1] = a1e v[L-2] + a2e v[L-3] + (1 - ce) v[L-1] - ce v[L],
+//     (A2^T v)[L]   = a2e v[L-2] + ce v[L-1] + (1 + ce) v[L],
+// and the moments M_d = sum_t g[t] tau_t^d through A2's action on the
+// polynomial basis (the forward's decomposition constants):
+//     M1' = M1 + c dtau M0,  M2' = M2 + 2 c dtau M1 + (c + c^2) dtau^2 M0 + wL1 g[L-1] + wL g[L].
+// The noise enters through the N-projected loadings alpha = aS.phi (S), beta
+// = aU.phi (U), gamma = aW.phi (W, and gL gamma at the last tenor), so per
+// step the coefficient columns gather phi_k (M0, M1, M2 + gL g[L]); the host
+// chains them to the coefficients (aS, aU, aW are linear in them) and runs
+// the FP64 adjoint of the deterministic curve p' = A2 p + N mu dt.
+struct PcAdjLayout {
+    size_t acc, hs, xs, ds, cb, red, total;
+};
+
+__host__ __device__ inline PcAdjLayout pc_adj_layout(int nt, int B, int R)
+{
+    PcAdjLayout L;
+    const size_t rows = (size_t)B + 1;
+    const size_t hs_rows = (size_t)(nt > B + 1 ? nt : B + 1);
+    L.acc = 0;
+    L.hs = align128(rows * 8 * kPcCta);
+    L.xs = align128(L.hs + hs_rows * kPcCta * 4);
+    L.ds = align128(L.xs + rows * kPcCta * 4);
+    L.cb = align128(L.ds + rows * kPcCta * 4);
+    L.red = align128(L.cb + (size_t)9 * kPcCta * 8);
+    L.total = align128(L.red + (size_t)(kPcCta / 32) * R * 8);
+    return L;
+}
+
+template <int NT, bool POLY>
+__global__ void __launch_bounds__(kPcCta, 4)
+    adjoint_kernel_pc(const __grid_constant__ PcParams<float> Q, double* __restrict__ partials)
+{
+    constexpr int L = NT - 1;
+    constexpr int kC = kPcCta;
+    const PathParams<float>& P = Q.P;
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int tid = threadIdx.x;
+    const int B = P.n_blocks;
+    const int R = 3 * B + 12;
+    const PcAdjLayout Ly = pc_adj_layout(NT, B, R);
+    double* acc_s = reinterpret_cast<double*>(smem + Ly.acc);
+    float* hs_s = reinterpret_cast<float*>(smem + Ly.hs);
+    float* xs_s = reinterpret_cast<float*>(smem + Ly.xs);
+    float* ds_s = reinterpret_cast<float*>(smem + Ly.ds);
+    double* cb_s = reinterpret_cast<double*>(smem + Ly.cb);
+    double* red_s = reinterpret_cast<double*>(smem + Ly.red);
+
+    const int64_t lp = (int64_t)blockIdx.x * kC + tid;
+    const bool active = lp < P.n_paths;
+    const uint64_t gpath = P.path_offset + (uint64_t)lp;
+    const int stride = P.stride;
+    const int n_steps = B * stride;
+
+    // ---------------------------------------------------------------- forward
+    PcPath<NT, float, POLY> x;
+    x.reset();
+    for (int i = 0; i <= B; ++i) acc_s[i * kC + tid] = 0.0;
+    for (int t = 0; t < NT; ++t) hs_s[t * kC + tid] = 0.f;
+    auto sample = [&](int i) {
+        const double xv = P.psamp[i] + (double)x.value(P, i);
+        const double a = P.psum[i] + acc_s[i * kC + tid];
+        const float D = exp_t<float>((float)(-a * P.dt));
+        const float mm = (float)P.m;
+        const float Lb = mm * expm1_t<float>((float)xv / mm);
+        acc_s[i * kC + tid] = (double)(D * ((float)P.payA[i] * Lb - (float)P.payB[i]));
+        xs_s[i * kC + tid] = (float)xv;
+        ds_s[i * kC + tid] = D;
+    };
+    sample(1);
+    for (int b = 1; b < B; ++b) {
+        x.begin_block(P, b);
+        for (int s = 0; s < stride; ++s) {
+            float phi0, phi1, phi2;
+            draw_phi<float, false>(nullptr, gpath, active ? lp : 0, P.n_paths, b * stride + s, P.rk0, P.rk1, phi0,
+                                   phi1, phi2);
+            x.step(Q, phi0, phi1, phi2);
+        }
+        x.end_block(Q, b, B, hs_s, acc_s, tid);
+        sample(b + 1);
+    }
+
+    // exposures, the path's CVA contribution, the CTA's EE and CVA partial sums
+    float* e_s = hs_s;
+    double vsum = 0.0, cva_c = 0.0;
+    e_s[B * kC + tid] = 0.f;
+    for (int j = B - 1; j >= 0; --j) {
+        vsum += acc_s[(j + 1) * kC + tid];
+        double e = (vsum > 0.0) ? vsum : 0.0;
+        if (!active) e = 0.0;
+        e_s[j * kC + tid] = (float)e;
+        cva_c = fma(P.cvaw[j], e, cva_c);
+    }
+    __syncthreads();
+    const int warp = tid >> 5, lane = tid & 31;
+    for (int j = warp; j <= B; j += kC / 32) {
+        double sum = 0.0;
+#pragma unroll
+        for (int q = 0; q < kC / 32; ++q) sum += (double)e_s[j * kC + lane + 32 * q];
+        sum = warp_sum(sum);
+        if (lane == 0) partials[(size_t)blockIdx.x * R + j] = sum;
+    }
+    {
+        const double s1 = warp_sum(cva_c), s2 = warp_sum(cva_c * cva_c);
+        if (lane == 0) {
+            red_s[warp] = s1;
+            red_s[kC / 32 + warp] = s2;
+        }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        double s1 = 0.0, s2 = 0.0;
+        for (int w = 0; w < kC / 32; ++w) {
+            s1 += red_s[w];
+            s2 += red_s[kC / 32 + w];
+        }
+        partials[(size_t)blockIdx.x * R + B + 1] = s1;
+        partials[(size_t)blockIdx.x * R + B + 2] = s2;
+    }
+    // per-date seeds from cfbar_i = sum_{j<i} w_j [E_j > 0]
+    {
+        float cfbar = 0.f;
+        for (int i = 1; i <= B; ++i) {
+            if (e_s[(i - 1) * kC + tid] > 0.f) cfbar += (float)P.cvaw[i - 1];
+            if (!active) cfbar = 0.f;
+            float xbar, abar;
+            date_seeds(P, i, (double)xs_s[i * kC + tid], ds_s[i * kC + tid], cfbar, xbar, abar);
+            xs_s[i * kC + tid] = xbar;
+            ds_s[i * kC + tid] = abar;
+        }
+    }
+
+    // ---------------------------------------------------------------- reverse
+    for (int q = 0; q < 9; ++q) cb_s[q * kC + tid] = 0.0;
+    float gv[NT], inj[NT];
+#pragma unroll
+    for (int t = 0; t < NT; ++t) gv[t] = inj[t] = 0.f;
+    float M0 = 0.f, M1 = 0.f, M2 = 0.f, I0 = 0.f, I1 = 0.f, I2 = 0.f;
+    const float dtau = (float)(1.0 / P.m);
+    const float a0 = Q.a0e, a1 = Q.a1e, a2 = Q.a2e, ce = Q.ce;
+    float r0, r1, r2;  // normals drawn one step ahead (descending)
+    draw_phi<float, false>(nullptr, gpath, active ? lp : 0, P.n_paths, n_steps - 1, P.rk0, P.rk1, r0, r1, r2);
+    for (int i = B; i >= 2; --i) {
+        {
+            const float xb = xs_s[i * kC + tid], ab = ds_s[i * kC + tid];
+#pragma unroll
+            for (int t = 0; t < NT; ++t) {
+                if (t == i) {
+                    inj[t] = ab;
+                    gv[t] += xb;
+                }
+            }
+            const float ti = dtau * (float)i;
+            I0 += ab;
+            I1 = fmaf(ab, ti, I1);
+            I2 = fmaf(ab, ti * ti, I2);
+            M0 += xb;
+            M1 = fmaf(xb, ti, M1);
+            M2 = fmaf(xb, ti * ti, M2);
+        }
+        float cbb[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) cbb[q] = 0.f;
+        for (int n = i * stride - 1; n >= (i - 1) * stride; --n) {
+            M0 += I0;
+            M1 += I1;
+            M2 += I2;
+            const float phi0 = r0, phi1 = r1, phi2 = r2;
+            draw_phi<float, false>(nullptr, gpath, active ? lp : 0, P.n_paths, max(n - 1, stride), P.rk0, P.rk1, r0,
+                                   r1, r2);
+            // v = g + inj: the adjoint of the state after step n; then g <- A2^T v,
+            // descending in place (v[t-1], v[t-2] still unchanged)
+#pragma unroll
+            for (int t = 0; t < NT; ++t) gv[t] += inj[t];
+            const float vL = gv[L], vL1 = gv[L - 1];
+            if constexpr (POLY) {
+                const float M2g = fmaf(Q.gL, vL, M2);
+                cbb[0] = fmaf(phi0, M0, cbb[0]);
+                cbb[1] = fmaf(phi0, M1, cbb[1]);
+                cbb[2] = fmaf(phi0, M2g, cbb[2]);
+                cbb[3] = fmaf(phi1, M0, cbb[3]);
+                cbb[4] = fmaf(phi1, M1, cbb[4]);
+                cbb[5] = fmaf(phi1, M2g, cbb[5]);
+                cbb[6] = fmaf(phi2, M0, cbb[6]);
+                cbb[7] = fmaf(phi2, M1, cbb[7]);
+                cbb[8] = fmaf(phi2, M2g, cbb[8]);
+            }
+            gv[L] = fmaf(a2, gv[L - 2], fmaf(ce, vL1, (1.f + ce) * vL));
+            gv[L - 1] = fmaf(a1, gv[L - 2], fmaf(a2, gv[L - 3], fmaf(1.f - ce, vL1, -ce * vL)));
+#pragma unroll
+            for (int t = L - 2; t >= 0; --t) {
+                float y = a0 * gv[t];
+                if (t >= 1) y = fmaf(a1, gv[t - 1], y);
+                if (t >= 2) y = fmaf(a2, gv[t - 2], y);
+                gv[t] = y;
+            }
+            M2 = fmaf(Q.wL, vL, fmaf(Q.wL1, vL1, fmaf(Q.k2p, M0, fmaf(Q.k1x2, M1, M2))));
+            M1 = fmaf(Q.k1, M0, M1);
+        }
+#pragma unroll
+        for (int q = 0; q < 9; ++q) cb_s[q * kC + tid] += (double)cbb[q];
+    }
+
+    // ---------------------------------------------------------------- CTA reduction
+    const int cx = B + 3, ca = 2 * B + 3, cc = 3 * B + 3;
+    double* wred = red_s;
+    __syncthreads();
+    for (int i = 1; i <= B; ++i) {
+        const double sx_ = warp_sum(active ? (double)xs_s[i * kC + tid] : 0.0);
+        const double sa_ = warp_sum(active ? (double)ds_s[i * kC + tid] : 0.0);
+        if (lane == 0) {
+            wred[warp * R + cx + i - 1] = sx_;
+            wred[warp * R + ca + i - 1] = sa_;
+        }
+    }
+    for (int q = 0; q < 9; ++q) {
+        const double sum = warp_sum(active ? cb_s[q * kC + tid] : 0.0);
+        if (lane == 0) wred[warp * R + cc + q] = sum;
+    }
+    __syncthreads();
+    for (int col = cx + tid; col < R; col += kC) {
+        double sum = 0.0;
+        for (int w = 0; w < kC / 32; ++w) sum += wred[w * R + col];
+        partials[(size_t)blockIdx.x * R + col] = sum;
+    }
+}
+
+size_t adjoint_pc_smem(int nt, int n_blocks) { return pc_adj_layout(nt, n_blocks, 3 * n_blocks + 12).total; }
+
+template <int NT, bool POLY>
+static cudaError_t launch_adj_pc_t(const PcParams<float>& Q, double* partials, cudaStream_t s)
+{
+    const size_t smem = adjoint_pc_smem(NT, Q.P.n_blocks);
+    auto k = adjoint_kernel_pc<NT, POLY>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const int64_t grid = (Q.P.n_paths + kPcCta - 1) / kPcCta;
+    k<<<(unsigned)grid, kPcCta, smem, s>>>(Q, partials);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adjoint_pc(int nt, const PcParams<float>& Q, bool poly, double* partials, cudaStream_t s)
+{
+    if (nt == 51) return poly ? launch_adj_pc_t<51, true>(Q, partials, s) : launch_adj_pc_t<51, false>(Q, partials, s);
+    if (nt == 61) return poly ? launch_adj_pc_t<61, true>(Q, partials, s) : launch_adj_pc_t<61, false>(Q, partials, s);
+    return cudaErrorInvalidValue;
 }
 
 size_t adjoint_smem(int nt, int n_blocks) { return adj_layout(nt, n_blocks, 3 * n_blocks + 12).total; }

@@ -1099,8 +1099,10 @@ hjm_status hjm_run_adjoint(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, doubl
     RunShape sh;
     hjm_status st = check_run(ctx, n_paths, n_steps, dt, HJM_PRECISION_MIXED, hazard_rate, recovery, 0.0, sh);
     if (st != HJM_OK) return st;
-    if (ctx->scheme != HJM_SCHEME_EULER)
-        return fail(ctx, HJM_ERR_UNSUPPORTED, "the adjoint is built for the Euler scheme");
+    const bool pc = ctx->scheme == HJM_SCHEME_PREDICTOR_CORRECTOR;
+    if (pc && checkpoint_every != 0)
+        return fail(ctx, HJM_ERR_UNSUPPORTED,
+                    "the predictor-corrector adjoint keeps the sampled states: checkpoint_every must be 0");
     if (checkpoint_every < 0 || checkpoint_every > sh.stride)
         return fail(ctx, HJM_ERR_UNSUPPORTED, "checkpoint_every %d: must be 0 (none) or in [1, %d] (the block length)",
                     checkpoint_every, sh.stride);
@@ -1109,7 +1111,7 @@ hjm_status hjm_run_adjoint(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, doubl
                     "volatility-coefficient sensitivities need a polynomial market (hjm_set_market_poly)");
     const int nt = ctx->nt, B = sh.B;
     const int R = adjoint_columns(nt, B);
-    const size_t smem = adjoint_smem(nt, B);
+    const size_t smem = pc ? adjoint_pc_smem(nt, B) : adjoint_smem(nt, B);
     if (smem > 227 * 1024) return fail(ctx, HJM_ERR_UNSUPPORTED, "adjoint shared memory %zu B exceeds 227 KB", smem);
     HJM_CUDA(ctx, cudaSetDevice(ctx->device));
     const int64_t n_ctas = (n_paths + adjoint_cta() - 1) / adjoint_cta();
@@ -1125,12 +1127,16 @@ hjm_status hjm_run_adjoint(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, doubl
         HJM_CUDA(ctx, ctx->ck_a.ensure(sizeof(double) * (size_t)S * (size_t)ld));
     }
     AdjParams A;
+    PcParams<float> Qp;
     FinalParams F;
     std::memset(&A, 0, sizeof(A));
     {
         PathParams<float> P;
         fill_params<float>(ctx, sh, n_paths, dt, seed, path_offset, hazard_rate, recovery, 0, false, P, F);
-        pack_mixed_params(nt, P, A.M);
+        if (pc)
+            fill_pc<float>(ctx, sh, dt, P, Qp);
+        else
+            pack_mixed_params(nt, P, A.M);
     }
     A.ckpt_every = K;
     A.ck_ld = ld;
@@ -1139,15 +1145,18 @@ hjm_status hjm_run_adjoint(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, doubl
     ctx->n_enqueued++;
     HJM_CUDA(ctx, cudaMemsetAsync(ctx->result.p, 0, sizeof(double) * kResLen, s));
     HJM_CUDA(ctx, cudaEventRecord(ctx->ev[0], s));
-    HJM_CUDA(ctx, launch_adjoint(nt, A, use_poly_path(ctx), (double*)ctx->partials.p, K > 0 ? (float*)ctx->ck_h.p : nullptr,
-                                 K > 0 ? (double*)ctx->ck_a.p : nullptr, s));
+    if (pc)
+        HJM_CUDA(ctx, launch_adjoint_pc(nt, Qp, use_poly_path(ctx), (double*)ctx->partials.p, s));
+    else
+        HJM_CUDA(ctx, launch_adjoint(nt, A, use_poly_path(ctx), (double*)ctx->partials.p,
+                                     K > 0 ? (float*)ctx->ck_h.p : nullptr, K > 0 ? (double*)ctx->ck_a.p : nullptr, s));
     HJM_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
     HJM_CUDA(ctx, launch_reduce((const double*)ctx->partials.p, n_ctas, R, (double*)ctx->sums.p, F,
                                 (double*)ctx->result.p, s));
     HJM_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
     HJM_CUDA(ctx, cudaEventRecord(ctx->ev[3], s));
     ctx->stat_launches = 3;
-    ctx->stat_h2d = sizeof(AdjParams) + sizeof(FinalParams);
+    ctx->stat_h2d = (pc ? sizeof(PcParams<float>) : sizeof(AdjParams)) + sizeof(FinalParams);
     std::vector<double> res(kResLen), sums(R);
     HJM_CUDA(ctx, cudaMemcpyAsync(res.data(), ctx->result.p, sizeof(double) * kResLen, cudaMemcpyDeviceToHost, s));
     HJM_CUDA(ctx, cudaMemcpyAsync(sums.data(), ctx->sums.p, sizeof(double) * R, cudaMemcpyDeviceToHost, s));
@@ -1163,12 +1172,15 @@ hjm_status hjm_run_adjoint(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, doubl
     // dCVA/dspot and dCVA/dmu: the path means of the per-date seeds through the
     // FP64 adjoint of the deterministic curve (p_n = spot for the first block,
     // p_n = A p_{n-1} + dt mu after; date i reads p_{n_i}[i] and sum_{n<=n_i} p_n[i]).
+    // Predictor-corrector: p_n = A2 p_{n-1} + dt N mu with A2 = I + dt D + dt^2
+    // D^2 / 2 and N = I + dt D / 2 (D the forward difference / dtau, backward
+    // at the last tenor), so q <- A2^T q and dmu += dt N^T q.
     std::vector<double> xbar(B + 1, 0.0), abar(B + 1, 0.0);
     for (int i = 1; i <= B; ++i) {
         xbar[i] = sums[B + 3 + i - 1] * inv_n;
         abar[i] = sums[2 * B + 3 + i - 1] * inv_n;
     }
-    std::vector<double> q(nt, 0.0), qn(nt), dmu(nt, 0.0), inj(nt, 0.0);
+    std::vector<double> q(nt, 0.0), qn(nt), d2(nt), dmu(nt, 0.0), inj(nt, 0.0);
     const double c = dt / ctx->dtau;
     const int L = nt - 1;
     for (int n = n_steps - 1; n >= sh.stride - 1; --n) {
@@ -1179,6 +1191,25 @@ hjm_status hjm_run_adjoint(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, doubl
         }
         for (int t = 0; t < nt; ++t) q[t] += inj[t];
         if (n < sh.stride) break;  // q = adjoint of p_{stride-1} = spot
+        if (pc) {
+            auto DT = [&](const std::vector<double>& y, std::vector<double>& out) {
+                for (int t = 0; t < nt; ++t) out[t] = 0.0;
+                for (int r = 0; r < L; ++r) {
+                    out[r] -= y[r];
+                    out[r + 1] += y[r];
+                }
+                out[L - 1] -= y[L];
+                out[L] += y[L];
+                for (int t = 0; t < nt; ++t) out[t] /= ctx->dtau;
+            };
+            DT(q, qn);
+            DT(qn, d2);
+            for (int t = 0; t < nt; ++t) {
+                dmu[t] += dt * (q[t] + 0.5 * dt * qn[t]);
+                q[t] += dt * qn[t] + 0.5 * dt * dt * d2[t];
+            }
+            continue;
+        }
         for (int t = 0; t < nt; ++t) dmu[t] += dt * q[t];
         qn[0] = (1.0 - c) * q[0];
         for (int t = 1; t <= L - 2; ++t) qn[t] = q[t] + c * (q[t - 1] - q[t]);
@@ -1196,6 +1227,7 @@ hjm_status hjm_run_adjoint(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, doubl
     r.precision = HJM_PRECISION_MIXED;
     r.vol_form = vol_form_code(ctx);
     r.remainder = 1;
+    r.scheme = ctx->scheme;
     r.ckpt = K;
     r.dt = dt;
     r.dtau = ctx->dtau;
@@ -1220,8 +1252,17 @@ hjm_status hjm_run_adjoint(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, doubl
         const double sq = std::sqrt(dt);
         for (int k = 0; k < HJM_N_FACTOR; ++k) {
             const double* sig = ctx->vol.data() + (size_t)k * nt;
+            // diffusion: Euler, the columns are dCVA/d(sqrt(dt) c_{k,d}); the
+            // predictor-corrector, dCVA/d(aS_k, aU_k, aW_k) of the N-projected
+            // loadings aS = sqrt(dt) (c0 + c dtau c1 / 2 + c dtau^2 c2 / 2),
+            // aU = sqrt(dt) (c1 + c dtau c2), aW = sqrt(dt) c2
+            const double X0 = sums[3 * B + 3 + k * 3] * inv_n, X1 = sums[3 * B + 3 + k * 3 + 1] * inv_n,
+                         X2 = sums[3 * B + 3 + k * 3 + 2] * inv_n;
+            const double cd = c * ctx->dtau;
+            const double diff[3] = {pc ? X0 : X0, pc ? 0.5 * cd * X0 + X1 : X1,
+                                    pc ? 0.5 * cd * ctx->dtau * X0 + cd * X1 + X2 : X2};
             for (int d = 0; d < 3; ++d) {
-                double v = sq * sums[3 * B + 3 + k * 3 + d] * inv_n;
+                double v = sq * diff[d];
                 double I = 0.0, J = 0.0;
                 for (int i = 0; i < nt; ++i) {
                     const double ti = ctx->dtau * i;

@@ -134,5 +134,9 @@ int adjoint_columns(int nt, int n_blocks);
 int adjoint_cta();  // paths per CTA of the adjoint kernel (one partial-sum row each)
 cudaError_t launch_adjoint(int nt, const AdjParams& A, bool poly, double* partials, float* ck_h, double* ck_a,
                            cudaStream_t s);
+// the predictor-corrector adjoint (sampled states kept; same partial-sum columns
+// as launch_adjoint, the coefficient columns gather phi_k (M0, M1, M2 + gL g[L]))
+size_t adjoint_pc_smem(int nt, int n_blocks);
+cudaError_t launch_adjoint_pc(int nt, const PcParams<float>& Q, bool poly, double* partials, cudaStream_t s);
 
 }  // namespace hjm

@@ -34,24 +34,10 @@
 #include "hjm_device.cuh"
 #include "hjm_epilogue.cuh"
 #include "hjm_kernels.h"
+#include "hjm_pc.cuh"
 #include "hjm_resp.cuh"
 
 namespace hjm {
-
-constexpr int kPcCta = 64;
-
-template <typename T>
-__device__ __forceinline__ T exp_t(T x);
-template <>
-__device__ __forceinline__ double exp_t<double>(double x) { return exp(x); }
-template <>
-__device__ __forceinline__ float exp_t<float>(float x) { return expf(x); }
-template <typename T>
-__device__ __forceinline__ T expm1_t(T x);
-template <>
-__device__ __forceinline__ double expm1_t<double>(double x) { return exp(x) - 1.0; }
-template <>
-__device__ __forceinline__ float expm1_t<float>(float x) { return expm1f(x); }
 
 // Shared memory per thread (columns of kPcCta): acc (B+1) FP64, slot i the
 // discount sum of tenor i until date i is sampled, then its cash flow; hs
@@ -70,9 +56,6 @@ __global__ void __launch_bounds__(kPcCta, 4)
     path_kernel_pc(const __grid_constant__ PcParams<T> Q, const double* __restrict__ ext,
                    double* __restrict__ partials, T* __restrict__ estore)
 {
-    constexpr int L = NT - 1;
-    constexpr int kGroup = 8;
-    constexpr int kGroups = (L - 1 + kGroup - 1) / kGroup;  // tenors 0 .. L-2
     const PathParams<T>& P = Q.P;
     extern __shared__ __align__(128) unsigned char smem[];
     const int tid = threadIdx.x;
@@ -88,119 +71,30 @@ __global__ void __launch_bounds__(kPcCta, 4)
     const bool active = lp < P.n_paths;
     const uint64_t gpath = P.path_offset + (uint64_t)lp;
 
-    T v[NT];
-#pragma unroll
-    for (int t = 0; t < NT; ++t) v[t] = T(0);
+    PcPath<NT, T, POLY> x;
+    x.reset();
     for (int i = 0; i <= B; ++i) acc_s[i * kPcCta + tid] = 0.0;
     for (int t = 0; t < NT; ++t) hs_s[t * kPcCta + tid] = T(0);
 
-    T g = T(1);
-    T S = T(0), U = T(0), W = T(0);  // POLY: the polynomial parts
-    auto poly_at = [&](T s_, T u_, T w_, int t) -> T { return POLY ? fma(P.tau[t], fma(P.tau[t], w_, u_), s_) : T(0); };
     auto sample = [&](int i) {
-        const double x = P.psamp[i] + (double)(g * select_reg<NT, T>(v, i) + poly_at(S, U, W, i));
+        const double xv = P.psamp[i] + (double)x.value(P, i);
         const double a = P.psum[i] + acc_s[i * kPcCta + tid];
         const T D = exp_t<T>((T)(-a * P.dt));
         const T mm = (T)P.m;
-        const T Lb = mm * expm1_t<T>((T)x / mm);
+        const T Lb = mm * expm1_t<T>((T)xv / mm);
         acc_s[i * kPcCta + tid] = (double)(D * ((T)P.payA[i] * Lb - (T)P.payB[i]));
     };
 
     sample(1);
-    const T r1 = Q.r1, r2 = Q.r2;
     for (int b = 1; b < B; ++b) {
-        T F0 = T(0), F1 = T(0), F2 = T(0), Tb = T(0);  // block sums of phi_k; anchor sum of v[L]
-        T sS = T(0), sU = T(0), sW = T(0), XL1 = T(0), XL = T(0);  // POLY: sums of S, U, W and the sources
-        T ig = P.igblk[b];
-        const int live = b + 1;  // tenors <= b are never read again
+        x.begin_block(P, b);
         for (int s = 0; s < P.stride; ++s) {
             const int n = b * P.stride + s;
             T phi0, phi1, phi2;
             draw_phi<T, EXT>(ext, gpath, active ? lp : 0, P.n_paths, n, P.rk0, P.rk1, phi0, phi1, phi2);
-            ig *= P.ip;
-            const T p0 = phi0 * ig, p1 = phi1 * ig, p2 = phi2 * ig;
-            auto noise = [&](int t) -> T { return fma(P.sv[2][t], p2, fma(P.sv[1][t], p1, P.sv[0][t] * p0)); };
-            // the two Euler rows first (they read v[L-1], v[L]), then the
-            // interior ascending in place (v[t+1], v[t+2] still old)
-            const T eL = fma(T(2), v[L], -v[L - 1]);
-            T vL1 = fma(r2, eL, fma(r1, v[L], v[L - 1]));
-            T vL = fma(r2, fma(T(3), v[L], T(-2) * v[L - 1]), fma(r1, eL, v[L]));
-            if constexpr (POLY) {
-                // the remainder's sources (old W), then S, U, W (old values on the right)
-                const T gam = fma(Q.aW[2], phi2, fma(Q.aW[1], phi1, Q.aW[0] * phi0));
-                const T sL1 = Q.wL1 * W, sL = fma(Q.gL, gam, Q.wL * W);
-                vL1 = fma(sL1, ig, vL1);
-                vL = fma(sL, ig, vL);
-                XL1 += sL1;
-                XL += sL;
-                T Sn = fma(Q.aS[0], phi0, fma(Q.k2p, W, fma(Q.k1, U, S)));
-                Sn = fma(Q.aS[2], phi2, fma(Q.aS[1], phi1, Sn));
-                const T Un = fma(Q.aU[2], phi2, fma(Q.aU[1], phi1, fma(Q.aU[0], phi0, fma(Q.k1x2, W, U))));
-                S = Sn;
-                U = Un;
-                W += gam;
-                sS += S;
-                sU += U;
-                sW += W;
-            } else {
-                vL1 += noise(L - 1);
-                vL += noise(L);
-                F0 += phi0;
-                F1 += phi1;
-                F2 += phi2;
-            }
-#pragma unroll
-            for (int gi = 0; gi < kGroups; ++gi) {
-                if (kGroup * gi + kGroup > live) {
-#pragma unroll
-                    for (int j = 0; j < kGroup; ++j) {
-                        const int t = kGroup * gi + j;
-                        if (t <= L - 2) {
-                            T x = v[t];
-                            if constexpr (!POLY) {
-                                x = fma(P.sv[0][t], p0, x);
-                                x = fma(P.sv[1][t], p1, x);
-                                x = fma(P.sv[2][t], p2, x);
-                            }
-                            x = fma(r1, v[t + 1], x);
-                            v[t] = fma(r2, v[t + 2], x);
-                        }
-                    }
-                }
-            }
-            v[L - 1] = vL1;
-            v[L] = vL;
-            Tb = fma(P.ip, Tb, v[L]);
+            x.step(Q, phi0, phi1, phi2);
         }
-        g = P.gblk[b + 1];  // base^-(b stride): the scale at the block end
-        // block sums of tenors b+1 .. L, downward from the anchor H[L] = g Tb
-        {
-            auto X = [&](int t) -> T {
-                if constexpr (POLY) return t == L - 1 ? XL1 : (t == L ? XL : T(0));
-                return fma(P.sv[2][t], F2, fma(P.sv[1][t], F1, P.sv[0][t] * F0));
-            };
-            const T dL = fma(g, v[L], -hs_s[L * kPcCta + tid]);
-            const T dL1 = fma(g, v[L - 1], -hs_s[(L - 1) * kPcCta + tid]);
-            const T HL = g * Tb;
-            const T HL1 = fma(X(L - 1) - fma(Q.ce, dL - dL1, dL1), Q.inv_ce, HL);
-            if (L <= B) acc_s[L * kPcCta + tid] += (double)(HL + poly_at(sS, sU, sW, L));
-            if (L - 1 <= B && L - 1 > b) acc_s[(L - 1) * kPcCta + tid] += (double)(HL1 + poly_at(sS, sU, sW, L - 1));
-            T H1 = HL1, H2 = HL, d1 = dL1, d2 = dL;
-#pragma unroll
-            for (int t = L - 2; t >= 1; --t) {
-                if (t <= b) break;
-                const T d = fma(g, v[t], -hs_s[t * kPcCta + tid]);
-                const T a2d = fma(Q.a2e, d2, fma(Q.a1e, d1, Q.a0e * d));
-                const T Ht = (X(t) - a2d + fma(Q.a1e, H1, Q.a2e * H2)) * Q.inv_1ma0;
-                if (t <= B) acc_s[t * kPcCta + tid] += (double)(Ht + poly_at(sS, sU, sW, t));
-                H2 = H1;
-                H1 = Ht;
-                d2 = d1;
-                d1 = d;
-            }
-        }
-#pragma unroll
-        for (int t = 0; t < NT; ++t) hs_s[t * kPcCta + tid] = g * v[t];
+        x.end_block(Q, b, B, hs_s, acc_s, tid);
         sample(b + 1);
     }
 

@@ -86,8 +86,8 @@ hjm_status hjm_ctx_keep_exposures(hjm_ctx* ctx, int32_t keep);
  * (the reference's doc/TODO:3) averages the drift term mu + dF/dtau at the
  * curve and at its Euler prediction: f' = f + (a(f) + a(f*)) dt / 2 + xi.
  * Valuations (both precisions, the table and the decomposed volatility step)
- * support both; the adjoint, hjm_run_mlmc and hjm_run_static the Euler step
- * only. */
+ * and hjm_run_adjoint (with checkpoint_every = 0 for the predictor-corrector)
+ * support both; hjm_run_mlmc and hjm_run_static the Euler step only. */
 #define HJM_SCHEME_EULER 0
 #define HJM_SCHEME_PREDICTOR_CORRECTOR 1
 hjm_status hjm_ctx_set_scheme(hjm_ctx* ctx, int32_t scheme);
@@ -243,8 +243,9 @@ hjm_status hjm_calibrate_pca(const double* curves, int32_t n_obs, int32_t n_teno
  * multiplies T^d in factor k), and dCVA/d(hazard).  Curve states are
  * checkpointed every checkpoint_every steps (0 = none: the sampled states are
  * kept instead) and each date's state is recomputed from the last checkpoint
- * before it for the reverse sweep.  Requires a market set through
- * hjm_set_market_poly. */
+ * before it for the reverse sweep; the predictor-corrector scheme keeps the
+ * sampled states (checkpoint_every must be 0).  The coefficient sensitivities
+ * require a market set through hjm_set_market_poly. */
 hjm_status hjm_set_market_poly(hjm_ctx* ctx, int32_t n_tenor, double dtau, const double* spot_host,
                                const double* vol_coef_host /* [3][3] */);
 hjm_status hjm_run_adjoint(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, double dt, uint64_t seed,

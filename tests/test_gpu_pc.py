@@ -99,14 +99,71 @@ def test_pc_external_normals_and_61_tenors(pc, precision):
     _assert_rel(a.ee[:61], ee[:61], tol, "61-tenor EE")
 
 
-def test_pc_adjoint_is_refused(pc):
+def test_pc_adjoint_cva_equals_pc_mixed_valuation(pc):
+    """The predictor-corrector adjoint runs the mixed-precision valuation's
+    forward pass (the shared path state), so CVA, its standard error and
+    dCVA/dhazard are the valuation's bit for bit; it keeps the sampled states
+    (checkpoint_every = 0 only)."""
     mk = Market()
     pc.set_market_poly(51, 0.5, mk.spot, DEFAULT_VOL_COEFFS)
     pc.set_swap(Swap())
+    cfg = RunConfig(n_paths=40000, seed=77)
+    v = pc.run(cfg, "mixed", pfe=False)
+    a = pc.run_adjoint(cfg, checkpoint_every=0)
+    assert a.cva == v.cva
+    assert a.cva_stderr == v.cva_stderr
+    assert a.dcva_dhazard == v.dcva_dhazard
     with pytest.raises(_lib.HJMError) as ei:
-        pc.run_adjoint(RunConfig(n_paths=1000))
+        pc.run_adjoint(cfg, checkpoint_every=32)
     assert ei.value.status == 2
     assert pc.lib.hjm_ctx_set_scheme(pc.ctx, 7) == 1  # unknown scheme: HJM_ERR_INVALID_ARGUMENT
+
+
+def test_pc_adjoint_matches_fp64_finite_differences(pc):
+    """dCVA/d(initial forwards), d(volatility coefficients) and d(hazard) of the
+    predictor-corrector adjoint against central differences of the FP64
+    predictor-corrector valuation on the same paths, within 2e-3 (the bumps of
+    the Euler adjoint's test: 1e-5 on forwards and hazard, 1e-8 25^-d on the
+    coefficient of T^d)."""
+    from cva_hjm_cuda_gb300.market import nelson_siegel_curve, tenor_grid
+
+    cfg = RunConfig(n_paths=100000, seed=2024)
+    spot = nelson_siegel_curve(tenor_grid(51, 0.5))
+    coef = np.array(DEFAULT_VOL_COEFFS, dtype=float)
+
+    def val(sp, cf, hz=0.02):
+        pc.set_market_poly(51, 0.5, sp, cf)
+        pc.set_swap(Swap())
+        c = RunConfig(n_paths=cfg.n_paths, n_steps=cfg.n_steps, dt=cfg.dt, seed=cfg.seed, hazard=hz)
+        return pc.run(c, "fp64", pfe=False).cva
+
+    pc.set_market_poly(51, 0.5, spot, coef)
+    pc.set_swap(Swap())
+    sens = pc.run_adjoint(cfg, checkpoint_every=0)
+
+    def close(g, fd, group_max):
+        return abs(g - fd) <= 2e-3 * max(abs(fd), 0.01 * group_max)
+
+    scale_s = np.max(np.abs(sens.dcva_dspot))
+    for t in (0, 1, 5, 10, 19, 20, 30, 50):
+        h = 1e-5
+        up, dn = spot.copy(), spot.copy()
+        up[t] += h
+        dn[t] -= h
+        fd = (val(up, coef) - val(dn, coef)) / (2 * h)
+        assert close(sens.dcva_dspot[t], fd, scale_s), (t, sens.dcva_dspot[t], fd)
+    w = np.array([25.0 ** (q % 3) for q in range(9)])
+    gc = sens.dcva_dvolcoef.ravel()
+    scale_c = np.max(np.abs(gc / w))
+    for q in range(9):
+        h = 1e-8 / w[q]
+        up, dn = coef.copy(), coef.copy()
+        up.flat[q] += h
+        dn.flat[q] -= h
+        fd = (val(spot, up) - val(spot, dn)) / (2 * h)
+        assert close(gc[q] / w[q], fd / w[q], scale_c), (q, gc[q], fd)
+    fd = (val(spot, coef, 0.02 + 1e-5) - val(spot, coef, 0.02 - 1e-5)) / 2e-5
+    assert abs(sens.dcva_dhazard - fd) <= 1e-6 * abs(fd)
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
