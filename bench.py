@@ -614,8 +614,31 @@ def predictor_corrector_run(eng, mk, sw, args, flush) -> dict:
                          "device_ms_per_step": step_ms, "path_kernel_ms": float(hist[:, 0].mean()),
                          "cva": res.cva, "cva_euler": eu.cva,
                          "ee_max_rel_diff_vs_euler": float(np.max(np.abs(res.ee[:20] - eu.ee[:20]) / eu.ee[:20]))}
+        # the adjoint under the scheme (mixed precision, the sampled states kept)
+        # against one mixed-precision valuation of the same paths
+        n = WORKLOADS["adjoint"]["n_paths"]
+        cfg = RunConfig(n_paths=n, n_steps=N_STEPS, dt=DT, seed=SEED)
+        eng.set_market_poly(mk.n_tenor, mk.dtau, mk.spot, mk.vol_coeffs)
+        eng.set_swap(sw)
+        for _ in range(args.warmup):
+            eng.run_adjoint(cfg, checkpoint_every=0)
+        adj_ms = []
+        for _ in range(args.steps):
+            eng.run_adjoint(cfg, checkpoint_every=0)
+            adj_ms.append(float(eng.timing_history(1)[0, 0]))
+        for _ in range(args.warmup):
+            eng.enqueue(cfg, "mixed", pfe=False)
+        torch.cuda.synchronize()
+        for _ in range(args.steps):
+            eng.enqueue(cfg, "mixed", pfe=False)
+        torch.cuda.synchronize()
+        val_ms = float(eng.timing_history(min(args.steps, 64))[:, 0].mean())
+        out["adjoint"] = {"n_paths": n, "checkpoint_every": 0, "adjoint_ms": float(np.mean(adj_ms)),
+                          "one_cva_valuation_ms": val_ms, "adjoint_cost_in_valuations": float(np.mean(adj_ms)) / val_ms}
     finally:
         eng.set_scheme("euler")
+        eng.set_market(mk)
+        eng.set_swap(sw)
     return out
 
 
