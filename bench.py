@@ -286,6 +286,8 @@ def run_ours(args) -> None:
         set_product = lambda: eng.set_netting_set(netting)  # noqa: E731
     else:
         set_product = lambda: eng.set_swap(sw)  # noqa: E731
+    if args.table_step:
+        eng.vol_decomposition(False)  # the volatility-table step (profiling)
     if is_adjoint:
         eng.set_market_poly(mk.n_tenor, mk.dtau, mk.spot, mk.vol_coeffs)
     else:
@@ -377,8 +379,8 @@ def run_ours(args) -> None:
                                              "how": "hjm_measure_fma_peak: 8 independent FMA chains per thread, "
                                                     "8 CTAs x 256 threads per SM, best of 3 (2 flops per FMA)"}
     achieved = flops / (path_ms * 1e-3) / 1e12
-    traffic = profiled_traffic(f"{prec}-{n_paths}")
-    if remainder == "response":
+    traffic = profiled_traffic(f"{prec}-table-{n_paths}" if args.table_step else f"{prec}-{n_paths}")
+    if remainder == "response" and form != "table":
         f32 = response_fp32_flops_per_path(mk.n_tenor, n_steps, stride) * n_paths
         a32 = f32 / (path_ms * 1e-3) / 1e12
         p32 = extras.get("measured_fma_peak_tflops", {}).get("fp32")
@@ -389,6 +391,8 @@ def run_ours(args) -> None:
     roofline = {"bound": "fp64_pipe" if prec == "fp64" else "fp32_pipe", "achieved": achieved, "peak": peak,
                 "unit": "TFLOP/s", "frac": (achieved / peak) if peak else None, "traffic": traffic,
                 "kernel": (f"adjoint_kernel<{mk.n_tenor},ckpt,{form}>" if is_adjoint else
+                           f"path_kernel_fp64_vresp<{mk.n_tenor},philox>"
+                           if prec == "fp64" and remainder == "response" and form == "table" else
                            f"path_kernel_fp64_resp<{mk.n_tenor},philox,{form}>"
                            if prec == "fp64" and remainder == "response" else
                            f"path_kernel_fp64<{mk.n_tenor},philox,{form}>" if prec == "fp64" else
@@ -768,6 +772,8 @@ def main() -> None:
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="fp64")
     ap.add_argument("--paths", type=int, default=0, help="override the workload's path count (profiling only)")
     ap.add_argument("--no-extras", action="store_true", help="only the headline workload")
+    ap.add_argument("--table-step", action="store_true",
+                    help="run the workload on the volatility-table step (no decomposition; profiling only)")
     args = ap.parse_args()
     if args.warmup < 3:
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
