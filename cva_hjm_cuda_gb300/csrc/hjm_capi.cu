@@ -1293,8 +1293,7 @@ hjm_status hjm_run_mlmc(hjm_ctx* ctx, int32_t n_levels, const int64_t* n_paths, 
     if (n_levels < 1 || n_levels > HJM_MLMC_MAX_LEVELS || !n_paths)
         return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "n_levels must be in [1, %d] with n_paths per level",
                     HJM_MLMC_MAX_LEVELS);
-    if (ctx->scheme != HJM_SCHEME_EULER)
-        return fail(ctx, HJM_ERR_UNSUPPORTED, "multi-level Monte Carlo is built for the Euler scheme");
+    const bool pc = ctx->scheme == HJM_SCHEME_PREDICTOR_CORRECTOR;
     for (int l = 0; l < n_levels; ++l)
         if (n_paths[l] <= 0 || n_paths[l] > ((int64_t)1 << 31))
             return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "level %d: n_paths %lld outside [1, 2^31]", l,
@@ -1305,7 +1304,7 @@ hjm_status hjm_run_mlmc(hjm_ctx* ctx, int32_t n_levels, const int64_t* n_paths, 
         hjm_status st = check_run(ctx, n_paths[l], n_steps << l, dt / (double)(1 << l), HJM_PRECISION_MIXED,
                                   hazard_rate, recovery, 0.0, shapes[l]);
         if (st != HJM_OK) return st;
-        if (l >= 1 && mlmc_smem(shapes[l].B) > 227 * 1024)
+        if (l >= 1 && (pc ? mlmc_pc_smem(ctx->nt, shapes[l].B) : mlmc_smem(shapes[l].B)) > 227 * 1024)
             return fail(ctx, HJM_ERR_UNSUPPORTED, "level %d: shared memory exceeds 227 KB", l);
     }
     const int nt = ctx->nt;
@@ -1343,19 +1342,29 @@ hjm_status hjm_run_mlmc(hjm_ctx* ctx, int32_t n_levels, const int64_t* n_paths, 
         HJM_CUDA(ctx, ctx->sums.ensure(sizeof(double) * kMaxTenor * 4));
         HJM_CUDA(ctx, ctx->result.ensure(sizeof(double) * kResLen));
         MlmcParams Q;
+        MlmcPcParams Qp;
         FinalParams F, Fc;
         {
             PathParams<float> P;
             fill_params<float>(ctx, shf, n_paths[l], dtf, seed, offset, hazard_rate, recovery, 0, false, P, F);
-            pack_mixed_params(nt, P, Q.fine);
+            if (pc)
+                fill_pc<float>(ctx, shf, dtf, P, Qp.fine);
+            else
+                pack_mixed_params(nt, P, Q.fine);
             fill_params<float>(ctx, shc, n_paths[l], dtc, seed, offset, hazard_rate, recovery, 0, false, P, Fc);
-            pack_mixed_params(nt, P, Q.coarse);
+            if (pc)
+                fill_pc<float>(ctx, shc, dtc, P, Qp.coarse);
+            else
+                pack_mixed_params(nt, P, Q.coarse);
         }
         ctx->ev = ctx->ring[ctx->n_enqueued % hjm_ctx::kRing];
         ctx->n_enqueued++;
         HJM_CUDA(ctx, cudaMemsetAsync(ctx->result.p, 0, sizeof(double) * kResLen, s));
         HJM_CUDA(ctx, cudaEventRecord(ctx->ev[0], s));
-        HJM_CUDA(ctx, launch_mlmc_level(nt, Q, use_poly_path(ctx), (double*)ctx->partials.p, s));
+        if (pc)
+            HJM_CUDA(ctx, launch_mlmc_level_pc(nt, Qp, use_poly_path(ctx), (double*)ctx->partials.p, s));
+        else
+            HJM_CUDA(ctx, launch_mlmc_level(nt, Q, use_poly_path(ctx), (double*)ctx->partials.p, s));
         HJM_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
         HJM_CUDA(ctx, launch_reduce((const double*)ctx->partials.p, n_ctas, R, (double*)ctx->sums.p, F,
                                     (double*)ctx->result.p, s));
@@ -1391,6 +1400,7 @@ hjm_status hjm_run_mlmc(hjm_ctx* ctx, int32_t n_levels, const int64_t* n_paths, 
         r.precision = HJM_PRECISION_MIXED;
         r.vol_form = vol_form_code(ctx);
         r.remainder = 1;
+        r.scheme = ctx->scheme;
         r.dtau = ctx->dtau;
         r.hazard = hazard_rate;
         r.recovery = recovery;

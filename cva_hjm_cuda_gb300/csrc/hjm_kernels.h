@@ -119,6 +119,13 @@ struct MlmcParams {
     MixedParams coarse;
 };
 cudaError_t launch_mlmc_level(int nt, const MlmcParams& Q, bool poly, double* partials, cudaStream_t s);
+// ... and the predictor-corrector's (fine and coarse PcParams)
+struct MlmcPcParams {
+    PcParams<float> fine;
+    PcParams<float> coarse;
+};
+cudaError_t launch_mlmc_level_pc(int nt, const MlmcPcParams& Q, bool poly, double* partials, cudaStream_t s);
+size_t mlmc_pc_smem(int nt, int n_blocks);
 size_t mlmc_smem(int n_blocks);
 int mlmc_cta();
 

@@ -85,9 +85,9 @@ hjm_status hjm_ctx_keep_exposures(hjm_ctx* ctx, int32_t keep);
  * reference's Euler step (simulation_cpu.h:37-54); HJM_SCHEME_PREDICTOR_CORRECTOR
  * (the reference's doc/TODO:3) averages the drift term mu + dF/dtau at the
  * curve and at its Euler prediction: f' = f + (a(f) + a(f*)) dt / 2 + xi.
- * Valuations (both precisions, the table and the decomposed volatility step)
- * and hjm_run_adjoint (with checkpoint_every = 0 for the predictor-corrector)
- * support both; hjm_run_mlmc and hjm_run_static the Euler step only. */
+ * Valuations (both precisions, the table and the decomposed volatility step),
+ * hjm_run_adjoint (with checkpoint_every = 0 for the predictor-corrector) and
+ * hjm_run_mlmc support both; hjm_run_static the Euler step only. */
 #define HJM_SCHEME_EULER 0
 #define HJM_SCHEME_PREDICTOR_CORRECTOR 1
 hjm_status hjm_ctx_set_scheme(hjm_ctx* ctx, int32_t scheme);
@@ -190,7 +190,7 @@ hjm_status hjm_get_exposures(hjm_ctx* ctx, double* out_host, int64_t capacity);
 
 /* ---- multi-level Monte Carlo --------------------------------------------------- */
 /* EE and CVA by multi-level Monte Carlo (the reference's doc/TODO:15): level l
- * runs the Euler scheme with dt / 2^l and n_steps 2^l; level 0 is the plain
+ * runs the context's time scheme with dt / 2^l and n_steps 2^l; level 0 is the plain
  * mixed-precision valuation on n_paths[0] paths, level l >= 1 estimates
  * E[P_l - P_{l-1}] on n_paths[l] paths whose fine and coarse curves share the
  * Brownian increments (coarse normal = (phi_a + phi_b) / sqrt 2).  The outputs
@@ -198,7 +198,8 @@ hjm_status hjm_get_exposures(hjm_ctx* ctx, double* out_host, int64_t capacity);
  * error combines the levels' independent errors); level_out [n_levels][4] =
  * {CVA difference of the level, its standard error, device ms, paths}, the
  * inputs of the usual path allocation N_l ~ sqrt(V_l / C_l).  Mixed
- * precision, Euler scheme; normals of level l come from path index + l 2^40. */
+ * precision, Euler or predictor-corrector; normals of level l come from path
+ * index + l 2^40. */
 #define HJM_MLMC_MAX_LEVELS 6
 hjm_status hjm_run_mlmc(hjm_ctx* ctx, int32_t n_levels, const int64_t* n_paths, int32_t n_steps, double dt,
                         uint64_t seed, double hazard_rate, double recovery, double* ee_out, double* cva_out,

@@ -94,3 +94,51 @@ def test_mlmc_report(engine, tmp_path):
     assert r["kind"] == "mlmc" and len(r["levels"]) == 2
     assert r["cva"] == m["cva"] and r["run"]["n_steps"] == 1000 and r["run"]["n_paths"] == 8192 + 2048
     np.testing.assert_array_equal(r["ee"], m["ee"])
+
+
+@pytest.fixture
+def pc_engine(engine):
+    engine.set_scheme("predictor_corrector")
+    try:
+        yield engine
+    finally:
+        engine.set_scheme("euler")
+
+
+def test_pc_level_correction_vs_oracle(pc_engine):
+    """The predictor-corrector's coupled level kernel against the oracle's
+    predictor-corrector on the same fine normals and their coarse sums."""
+    eng = pc_engine
+    mk, sw = Market(), Swap()
+    eng.set_market(mk)
+    eng.set_swap(sw)
+    n0, n1, steps0, dt0 = 4096, 3000, 500, 0.02
+    base = eng.run_mlmc([n0], n_steps=steps0, dt=dt0, seed=21)
+    two = eng.run_mlmc([n0, n1], n_steps=steps0, dt=dt0, seed=21)
+    diff = two["ee"] - base["ee"]
+    fine = eng.dump_normals(n1, 2 * steps0, seed=21, path_offset=1 << 40)
+    coarse = _coarse_normals(fine)
+    xf = O.exposure_paths_pc(mk, sw, 2 * steps0, dt0 / 2, fine)
+    xc = O.exposure_paths_pc(mk, sw, steps0, dt0, coarse)
+    ee_d = O.expected_exposure(xf - xc)
+    scale = np.max(np.abs(base["ee"]))
+    assert np.max(np.abs(diff[:21] - ee_d[:21])) < 1e-6 * scale
+    d = O.cva_paths(xf, 21, mk.dtau, 0.02, 0.4) - O.cva_paths(xc, 21, mk.dtau, 0.02, 0.4)
+    lev1 = two["levels"][1]
+    assert abs(lev1["cva_diff"] - d.mean()) < 1e-6 * base["cva"]
+    assert lev1["stderr"] == pytest.approx(d.std(ddof=1) / np.sqrt(n1), rel=1e-3)
+    # level 0 is the predictor-corrector valuation itself
+    plain = eng.run(RunConfig(n_paths=n0, n_steps=steps0, dt=dt0, seed=21), "mixed", pfe=False)
+    assert two["levels"][0]["cva_diff"] == plain.cva
+
+
+def test_pc_estimator_matches_finest_grid(pc_engine):
+    eng = pc_engine
+    eng.set_market(Market())
+    eng.set_swap(Swap())
+    m = eng.run_mlmc([400_000, 100_000, 50_000], n_steps=500, dt=0.02, seed=5)
+    plain = eng.run(RunConfig(n_paths=400_000, n_steps=2000, dt=0.005, seed=77), "mixed", pfe=False)
+    tol = 4.0 * np.hypot(m["cva_stderr"], plain.cva_stderr)
+    assert abs(m["cva"] - plain.cva) < tol, (m["cva"], plain.cva, tol)
+    v = [lv["stderr"] ** 2 * lv["n_paths"] for lv in m["levels"]]
+    assert v[1] < 0.05 * v[0] and v[2] < 0.05 * v[0], v
