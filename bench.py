@@ -421,9 +421,14 @@ def run_ours(args) -> None:
         cb = cpu_oracle_sample(target_s=3.0, n_threads=os.cpu_count() or 1)
         n_cpu = cb["n_paths"]
         t_cpu = cb["run"](n_cpu)
+        # the reference's own CPU path is single-threaded: the same port on one thread
+        cb1 = cpu_oracle_sample(target_s=1.5, n_threads=1)
+        t1 = cb1["run"](cb1["n_paths"])
         cpu_baseline = {"value": n_cpu * N_STEPS / t_cpu, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
                         "sample": f"first {n_cpu} paths x {N_STEPS} steps, FP64, oracle port, all host threads",
-                        "cpu": cpu_model()}
+                        "cpu": cpu_model(),
+                        "single_thread": {"value": cb1["n_paths"] * N_STEPS / t1, "unit": UNIT, "cores": 1,
+                                          "sample": f"first {cb1['n_paths']} paths x {N_STEPS} steps"}}
     else:
         cpu_baseline = None
 
