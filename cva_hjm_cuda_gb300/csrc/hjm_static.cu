@@ -18,6 +18,13 @@
 // cudaGetSymbolAddress, with that device current, and passes it to the same
 // path and reduction kernels that hjm_run launches.
 //
+// FP64 runs take the volatility-table step in its response form (the whole
+// stochastic curve as FP64 sums of the three factors' impulse responses, three
+// times the convected step's speed) when its table fits a second static array
+// (4 MB: with 20 dates up to ~180 steps per date, 3,640 steps in all at 24
+// dates); the table is recomputed on the device at every call.  Larger runs,
+// and mixed precision, take the convected step.
+//
 // Limits: at most HJM_STATIC_MAX_PATHS paths per call; EE and CVA only (the
 // per-path exposure store a PFE needs would not fit a modest static buffer).
 // Every call shares the array: calls that overlap on the GPU (two streams, two
@@ -51,10 +58,12 @@ constexpr size_t kPartialsDoubles = (size_t)kStaticCtas * kStaticCols;
 constexpr size_t kSumsOffset = kPartialsDoubles;        // 2 * kMaxTenor doubles
 constexpr size_t kResultOffset = kSumsOffset + 2 * kMaxTenor;
 constexpr size_t kScratchDoubles = kResultOffset + kResLen;
+constexpr size_t kStaticRespEntries = (size_t)1 << 18;  // double2: 4 MB of response table
 constexpr int kMaxDevices = 64;
 
 std::mutex g_static_mu;
 double* g_static_ptr[kMaxDevices] = {};
+double2* g_static_resp_ptr[kMaxDevices] = {};
 
 hjm_status static_fail(hjm_status st, const char* fmt, ...)
 {
@@ -72,6 +81,8 @@ hjm_status static_fail(hjm_status st, const char* fmt, ...)
 // The scratch: 8.4 MB of FP64 per device (HJM_STATIC_MAX_PATHS / 64 CTA rows
 // of 64 partial sums, plus column sums and the result block).
 static __device__ __align__(256) double g_hjm_static_scratch[kScratchDoubles];
+// ... and 4 MB for the FP64 response table.
+static __device__ __align__(256) double2 g_hjm_static_resp[kStaticRespEntries];
 
 #define STATIC_CUDA(call)                                                                          \
     do {                                                                                           \
@@ -80,10 +91,10 @@ static __device__ __align__(256) double g_hjm_static_scratch[kScratchDoubles];
             return static_fail(HJM_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));      \
     } while (0)
 
-// Device address of the scratch array on the current device, looked up once
-// per device (the first call on a device does this; make that first call
+// Device addresses of the two static arrays on the current device, looked up
+// once per device (the first call on a device does this; make that first call
 // before any stream capture).
-static hjm_status static_scratch(double** out)
+static hjm_status static_scratch(double** out, double2** resp_out)
 {
     int dev = 0;
     STATIC_CUDA(cudaGetDevice(&dev));
@@ -91,13 +102,17 @@ static hjm_status static_scratch(double** out)
     std::lock_guard<std::mutex> lock(g_static_mu);
     if (!g_static_ptr[dev]) {
         void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_hjm_static_scratch);
-        if (e != cudaSuccess || p == nullptr)
+        void* q = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_hjm_static_scratch);
+        if (e == cudaSuccess) e = cudaGetSymbolAddress(&q, g_hjm_static_resp);
+        if (e != cudaSuccess || p == nullptr || q == nullptr)
             return static_fail(HJM_ERR_CUDA, "cudaGetSymbolAddress(scratch) on device %d failed: %s", dev,
                                cudaGetErrorString(e));
+        g_static_resp_ptr[dev] = static_cast<double2*>(q);
         g_static_ptr[dev] = static_cast<double*>(p);
     }
     *out = g_static_ptr[dev];
+    *resp_out = g_static_resp_ptr[dev];
     return HJM_OK;
 }
 
@@ -247,7 +262,8 @@ hjm_status hjm_run_static(void* cuda_stream, int32_t n_tenor, double dtau, const
     }
 
     double* scratch = nullptr;
-    hjm_status st = static_scratch(&scratch);
+    double2* resp_table = nullptr;
+    hjm_status st = static_scratch(&scratch, &resp_table);
     if (st != HJM_OK) return st;
     double* partials = scratch;
     double* sums = scratch + kSumsOffset;
@@ -267,7 +283,15 @@ hjm_status hjm_run_static(void* cuda_stream, int32_t n_tenor, double dtau, const
         PathParams<double> P;
         static_params<double>(n_tenor, dtau, spot_host, vol_host, drift, payA, payB, (int)stride, B, n_paths, dt,
                               seed, path_offset, hazard_rate, recovery, P, F);
-        STATIC_CUDA(launch_path_fp64(n_tenor, P, false, nullptr, nullptr, partials, nullptr, s));
+        const size_t entries = response_table_vol_elems((int)stride, B);
+        if (B >= 2 && B <= response_max_dates() && entries <= kStaticRespEntries) {
+            // the response form: its table (zero outside the live entries) into the static array
+            STATIC_CUDA(cudaMemsetAsync(resp_table, 0, sizeof(double2) * entries, s));
+            STATIC_CUDA(launch_response_table_vol(n_tenor, dt / dtau, (int)stride, B, false, &P.sv[0][0], resp_table, s));
+            STATIC_CUDA(launch_path_fp64_vresp(n_tenor, P, resp_table, nullptr, partials, nullptr, s));
+        } else {
+            STATIC_CUDA(launch_path_fp64(n_tenor, P, false, nullptr, nullptr, partials, nullptr, s));
+        }
     }
     STATIC_CUDA(launch_reduce(partials, n_ctas, R, sums, F, result, s));
     double res[kResLen];

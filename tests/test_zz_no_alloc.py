@@ -72,6 +72,32 @@ def test_static_entry_matches_hjm_run_twice(precision, rtol):
 
 
 @pytest.mark.skipif(not _have_gpu(), reason="no CUDA device")
+@pytest.mark.parametrize("case", ["bumpy-table", "table-beyond-static"])
+def test_static_fp64_response_and_fallback_match_hjm_run(case):
+    """FP64 static runs take the volatility-table step's response form when its
+    table fits the static array (any table shape), the convected step when it
+    does not (here 250 steps per date); both equal hjm_run within 1e-10."""
+    from cva_hjm_cuda_gb300.engine import HJMEngine
+
+    lib = _lib.load()
+    if case == "bumpy-table":
+        mk = Market(vol=Market().vol * (1.0 + 0.1 * np.cos(np.arange(51) / 7.0))[None, :])
+        cfg = RunConfig(n_paths=20_000, seed=8)
+    else:
+        mk = Market()
+        cfg = RunConfig(n_paths=20_000, n_steps=5000, dt=0.002, seed=8)
+    sw = Swap()
+    with HJMEngine(0) as eng:
+        eng.set_market(mk)
+        eng.set_swap(sw)
+        ref = eng.run(cfg, "fp64", pfe=False)
+    st, ee, cva = _run_static(lib, mk, sw, cfg, "fp64")
+    assert st == 0, lib.hjm_last_error(None)
+    np.testing.assert_allclose(ee, ref.ee, rtol=FP64_RTOL, atol=0)
+    assert abs(cva[0] - ref.cva) <= FP64_RTOL * abs(ref.cva)
+
+
+@pytest.mark.skipif(not _have_gpu(), reason="no CUDA device")
 def test_static_entry_rejects_oversize_runs():
     lib = _lib.load()
     mk, sw = Market(), Swap()
