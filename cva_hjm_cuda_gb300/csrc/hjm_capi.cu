@@ -298,13 +298,18 @@ hjm_status hjm_ctx_vol_decomposition(hjm_ctx* ctx, int32_t* active)
 // T = dtau t?  The quadratic through the rows' values at t = 0, mid, last
 // (Lagrange form) must reproduce every entry to 1e-12 of the row's largest
 // magnitude; its monomial coefficients go to coef[k * 3 + d].
-static bool fit_quadratic_vols(const std::vector<double>& vol, int nt, double dtau, double* coef)
+namespace hjm {
+// The quadratic fit of a volatility table (factor-major [3][nt]) that decides
+// the decomposition: true with coef [3][3] when every factor is a polynomial of
+// degree <= 2 to 1e-12 of its scale.  Internal to the library (hjm_run_static
+// uses it too).
+__attribute__((visibility("hidden"))) bool fit_quadratic_vols(const double* vol, int nt, double dtau, double* coef)
 {
     if (nt < 3) return false;
     const int i0 = 0, i1 = (nt - 1) / 2, i2 = nt - 1;
     const double x0 = dtau * i0, x1 = dtau * i1, x2 = dtau * i2;
     for (int k = 0; k < HJM_N_FACTOR; ++k) {
-        const double* v = vol.data() + (size_t)k * nt;
+        const double* v = vol + (size_t)k * nt;
         // Lagrange basis l_j(x) = prod (x - x_m) / (x_j - x_m) expanded in 1, x, x^2
         const double d0 = (x0 - x1) * (x0 - x2), d1 = (x1 - x0) * (x1 - x2), d2 = (x2 - x0) * (x2 - x1);
         const double w0 = v[i0] / d0, w1 = v[i1] / d1, w2 = v[i2] / d2;
@@ -327,6 +332,7 @@ static bool fit_quadratic_vols(const std::vector<double>& vol, int nt, double dt
     }
     return true;
 }
+}  // namespace hjm
 
 static void trapezoid_drift(const std::vector<double>& vol, int nt, double dtau, std::vector<double>& drift)
 {
@@ -366,7 +372,7 @@ hjm_status hjm_set_market(hjm_ctx* ctx, int32_t n_tenor, double dtau, const doub
         trapezoid_drift(ctx->vol, n_tenor, dtau, ctx->drift);
     ctx->have_market = true;
     ctx->have_poly = false;
-    ctx->poly_path = fit_quadratic_vols(ctx->vol, n_tenor, dtau, ctx->coef);
+    ctx->poly_path = fit_quadratic_vols(ctx->vol.data(), n_tenor, dtau, ctx->coef);
     if (ctx->have_product && (int)ctx->payA.size() != n_tenor) ctx->have_product = false;
     return HJM_OK;
 }

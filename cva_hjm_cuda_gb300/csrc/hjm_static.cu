@@ -18,12 +18,13 @@
 // cudaGetSymbolAddress, with that device current, and passes it to the same
 // path and reduction kernels that hjm_run launches.
 //
-// FP64 runs take the volatility-table step in its response form (the whole
-// stochastic curve as FP64 sums of the three factors' impulse responses, three
-// times the convected step's speed) when its table fits a second static array
-// (4 MB: with 20 dates up to ~180 steps per date, 3,640 steps in all at 24
-// dates); the table is recomputed on the device at every call.  Larger runs,
-// and mixed precision, take the convected step.
+// FP64 runs take a response form when its table fits a second static array
+// (4 MB; recomputed on the device at every call), as hjm_run does: with a
+// volatility table whose factors are quadratics (the reference's), the
+// polynomial decomposition's remainder in double-FP32 impulse-response sums
+// (12x the convected table step), else the whole stochastic curve as FP64 sums
+// of the three factors' responses (3x; with 20 dates up to ~180 steps per
+// date).  Larger runs, and mixed precision, take the convected table step.
 //
 // Limits: at most HJM_STATIC_MAX_PATHS paths per call; EE and CVA only (the
 // per-path exposure store a PFE needs would not fit a modest static buffer).
@@ -47,6 +48,7 @@ using namespace hjm;
 
 namespace hjm {
 void set_thread_error(const char* msg);  // hjm_capi.cu: the message hjm_last_error(NULL) returns
+bool fit_quadratic_vols(const double* vol, int nt, double dtau, double* coef);  // hjm_capi.cu
 }
 
 namespace {
@@ -81,8 +83,10 @@ hjm_status static_fail(hjm_status st, const char* fmt, ...)
 // The scratch: 8.4 MB of FP64 per device (HJM_STATIC_MAX_PATHS / 64 CTA rows
 // of 64 partial sums, plus column sums and the result block).
 static __device__ __align__(256) double g_hjm_static_scratch[kScratchDoubles];
-// ... and 4 MB for the FP64 response table.
+// ... and 4 MB for the FP64 response table (double2 entries of the
+// volatility-table form, or float4 entries of the polynomial form).
 static __device__ __align__(256) double2 g_hjm_static_resp[kStaticRespEntries];
+static_assert(sizeof(float4) == sizeof(double2), "both response tables use 16-byte entries");
 
 #define STATIC_CUDA(call)                                                                          \
     do {                                                                                           \
@@ -283,8 +287,23 @@ hjm_status hjm_run_static(void* cuda_stream, int32_t n_tenor, double dtau, const
         PathParams<double> P;
         static_params<double>(n_tenor, dtau, spot_host, vol_host, drift, payA, payB, (int)stride, B, n_paths, dt,
                               seed, path_offset, hazard_rate, recovery, P, F);
+        double coef[HJM_N_VOL_COEF];
+        const bool poly = fit_quadratic_vols(vol_host, n_tenor, dtau, coef);
         const size_t entries = response_table_vol_elems((int)stride, B);
-        if (B >= 2 && B <= response_max_dates() && entries <= kStaticRespEntries) {
+        if (poly && B >= 2 && B <= response_max_dates() && response_table_elems((int)stride, B) <= kStaticRespEntries) {
+            // the decomposition: S, U, W in FP64, the remainder's table (FP32
+            // pairs, 16 bytes per entry like the double2 array) in the static array
+            const double sq = std::sqrt(dt), c = dt / dtau;
+            for (int k = 0; k < kFactors; ++k)
+                for (int d = 0; d < 3; ++d) P.svc[k][d] = sq * coef[k * 3 + d];
+            P.k1 = c * dtau;
+            P.k2 = c * dtau * dtau;
+            for (int t = 0; t < n_tenor; ++t) P.tau[t] = dtau * t;
+            float4* table = reinterpret_cast<float4*>(resp_table);
+            STATIC_CUDA(cudaMemsetAsync(table, 0, sizeof(float4) * response_table_elems((int)stride, B), s));
+            STATIC_CUDA(launch_response_table(n_tenor, c, (int)stride, B, false, 0.0, -2.0 * P.k2, 0.0, table, s));
+            STATIC_CUDA(launch_path_fp64(n_tenor, P, true, table, nullptr, partials, nullptr, s));
+        } else if (B >= 2 && B <= response_max_dates() && entries <= kStaticRespEntries) {
             // the response form: its table (zero outside the live entries) into the static array
             STATIC_CUDA(cudaMemsetAsync(resp_table, 0, sizeof(double2) * entries, s));
             STATIC_CUDA(launch_response_table_vol(n_tenor, dt / dtau, (int)stride, B, false, &P.sv[0][0], resp_table, s));

@@ -74,9 +74,10 @@ def test_static_entry_matches_hjm_run_twice(precision, rtol):
 @pytest.mark.skipif(not _have_gpu(), reason="no CUDA device")
 @pytest.mark.parametrize("case", ["bumpy-table", "table-beyond-static"])
 def test_static_fp64_response_and_fallback_match_hjm_run(case):
-    """FP64 static runs take the volatility-table step's response form when its
-    table fits the static array (any table shape), the convected step when it
-    does not (here 250 steps per date); both equal hjm_run within 1e-10."""
+    """FP64 static runs take a response form when its table fits the static
+    array: the polynomial one for quadratic factors (the test above), the
+    volatility-table one for any other table (bumpy-table), the convected step
+    when neither fits (1,000 steps per date); all equal hjm_run within 1e-10."""
     from cva_hjm_cuda_gb300.engine import HJMEngine
 
     lib = _lib.load()
@@ -85,7 +86,7 @@ def test_static_fp64_response_and_fallback_match_hjm_run(case):
         cfg = RunConfig(n_paths=20_000, seed=8)
     else:
         mk = Market()
-        cfg = RunConfig(n_paths=20_000, n_steps=5000, dt=0.002, seed=8)
+        cfg = RunConfig(n_paths=20_000, n_steps=20000, dt=0.0005, seed=8)
     sw = Swap()
     with HJMEngine(0) as eng:
         eng.set_market(mk)
