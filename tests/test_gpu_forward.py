@@ -31,7 +31,7 @@ def _assert_rel(actual, desired, rtol, what):
     scale = np.max(np.abs(desired)) if desired.size else 0.0
     err = np.abs(actual - desired)
     bad = err > rtol * np.maximum(np.abs(desired), 1e-300)
-    # exact zeros must stay exact; tiny values are judged against the profile's scale
+    # exact zeros must stay exact; tiny values are compared against the profile's scale
     bad &= err > rtol * scale * 1e-3
     assert not np.any(bad), f"{what}: max rel err {np.max(err / np.maximum(np.abs(desired), 1e-300)):.3e}"
 
