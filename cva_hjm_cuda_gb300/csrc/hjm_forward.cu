@@ -272,13 +272,16 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
     float2 A[kRespSlots], Al[kRespSlots];
 #pragma unroll
     for (int r = 0; r < kRespSlots; ++r) A[r] = Al[r] = make_float2(0.0f, 0.0f);
-    double S = 0.0, U = 0.0, W = 0.0;     // parallel, tilt and curvature parts
-    // their running sums over the evolved steps before the current one (one
-    // step behind, so that no instruction of a step waits for the FP64 update
-    // it has just issued; sampling adds the current values, in the same order)
-    double sS = 0.0, sU = 0.0, sW = 0.0;
+    // the parallel, tilt and curvature parts in the moving frame, {y_c, v_c}
+    // as hi + lo pairs (c = S, U, W)
+    float2 Y[3], Yl[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) Y[c] = Yl[c] = make_float2(0.0f, 0.0f);
+    const float4* coef = resp + (size_t)B * P.stride * kRespRow;
+    const double k1 = P.k1, k2 = P.k2, k1s = P.k1 * P.k1;
 
-    // price date i from the sampled numeraire (x_i, D_i)
+    // price date i from the sampled numeraire (x_i, D_i); the parts after
+    // E = (i - 1) stride evolved steps: x_E = M^E y, Z_E = Q(E) y - v
     auto sample = [&](int i) {
         const double tau = P.tau[i];
         double hc = 0.0, hcs = 0.0;
@@ -287,8 +290,23 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
             hc = widen_f32(h.x) + widen_f32(l.x);
             hcs = widen_f32(h.y) + widen_f32(l.y);
         }
+        double y[3], v[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            df_norm(Y[c], Yl[c]);
+            y[c] = widen_f32(Y[c].x) + widen_f32(Yl[c].x);
+            v[c] = widen_f32(Y[c].y) + widen_f32(Yl[c].y);
+        }
+        const double E = (double)((i - 1) * P.stride), e1 = 0.5 * E * (E + 1.0);
+        const double W = y[2];
+        const double U = fma(2.0 * E * k1, y[2], y[1]);
+        const double S = fma(E * k1, y[1], fma(E * fma(E - 1.0, k1s, k2), y[2], y[0]));
+        const double ZW = fma(E, y[2], -v[2]);
+        const double ZU = fma(E, y[1], fma(2.0 * e1 * k1, y[2], -v[1]));
+        const double ZS =
+            fma(E, y[0], fma(e1 * k1, y[1], fma(fma(e1, k2, (E + 1.0) * E * (E - 1.0) / 3.0 * k1s), y[2], -v[0])));
         const double x = P.psamp[i] + (fma(tau, fma(tau, W, U), S) + hc);
-        const double acc = fma(tau, fma(tau, sW + W, sU + U), sS + S) + hcs;
+        const double acc = fma(tau, fma(tau, ZW, ZU), ZS) + hcs;
         const double D = exp(-(P.psum[i] + acc) * P.dt);
         const double Lb = P.m * (exp(x / P.m) - 1.0);
         cf_s[i * kCta + tid] = D * (P.payA[i] * Lb - P.payB[i]);
@@ -299,13 +317,20 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
         const float4* row = resp + (size_t)b * P.stride * kRespRow;
         for (int s = 0; s < P.stride; ++s) {
             const int n = b * P.stride + s;
-            double phi0, phi1, phi2;
-            draw_phi<double, EXT>(ext, gpath, active ? lp : 0, P.n_paths, n, P.rk0, P.rk1, phi0, phi1, phi2);
+            float ph[3], pl[3];  // the normals as hi + lo (lo = 0 for the generator's FP32 draws)
+            if constexpr (EXT) {
+                double d0, d1, d2;
+                draw_phi<double, true>(ext, gpath, active ? lp : 0, P.n_paths, n, P.rk0, P.rk1, d0, d1, d2);
+                split_f64(d0, ph[0], pl[0]);
+                split_f64(d1, ph[1], pl[1]);
+                split_f64(d2, ph[2], pl[2]);
+            } else {
+                draw_phi<float, false>(ext, gpath, lp, P.n_paths, n, P.rk0, P.rk1, ph[0], ph[1], ph[2]);
+            }
             const int n_act = resp_n_act(s, b, B, L, P.stride);  // uniform
             const float4* rr = row + (size_t)s * kRespRow;
-            float wh, wl;
-            split_f64(W, wh, wl);
-            const float2 wh2 = make_float2(wh, wh), wl2 = make_float2(wl, wl);
+            // the remainder's source: W before this step's update
+            const float2 wh2 = make_float2(Y[2].x, Y[2].x), wl2 = make_float2(Yl[2].x, Yl[2].x);
             resp_groups(n_act, [&](auto gc) {
                 constexpr int G = decltype(gc)::value;
                 float4 k[4];
@@ -316,22 +341,22 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
                     df_acc(A[4 * G + u], Al[4 * G + u], make_float2(k[u].x, k[u].y), make_float2(k[u].z, k[u].w),
                            wh2, wl2);
             });
-            sS += S;
-            sU += U;
-            sW += W;
-            // S' = S + c dtau U + c dtau^2 W + sum_k svc[k][0] phi_k, etc. (old
-            // U, W on the right; factor k of degree <= k drops 3 terms)
-            double Wn = fma(P.svc[2][2], phi2, W);
-            double Sn = fma(P.svc[0][0], phi0, fma(P.k2, W, fma(P.k1, U, S)));
-            Sn = fma(P.svc[2][0], phi2, fma(P.svc[1][0], phi1, Sn));
-            double Un = fma(P.svc[2][1], phi2, fma(P.svc[1][1], phi1, fma(2.0 * P.k1, W, U)));
-            if constexpr (!TRI) {
-                Un = fma(P.svc[0][1], phi0, Un);
-                Wn = fma(P.svc[1][2], phi1, fma(P.svc[0][2], phi0, Wn));
+            // y += C(m) phi, v += G(m) phi (factor k of degree <= k loads parts c <= k only)
+            const float4* cr = coef + (size_t)n * kStateRow;
+            float4 q[kStateRow];
+#pragma unroll
+            for (int t = 0; t < kStateRow; ++t)
+                if (!TRI || t / 3 <= t % 3) q[t] = __ldg(cr + t);
+#pragma unroll
+            for (int t = 0; t < kStateRow; ++t) {
+                const int c = t / 3, k = t % 3;
+                if (TRI && c > k) continue;
+                const float2 kh = make_float2(q[t].x, q[t].y), kl = make_float2(q[t].z, q[t].w);
+                if constexpr (EXT)
+                    df_acc(Y[c], Yl[c], kh, kl, make_float2(ph[k], ph[k]), make_float2(pl[k], pl[k]));
+                else
+                    df_acc_w(Y[c], Yl[c], kh, kl, make_float2(ph[k], ph[k]));
             }
-            S = Sn;
-            U = Un;
-            W = Wn;
         }
         sample(b + 1);
     }
@@ -414,6 +439,37 @@ __global__ void __launch_bounds__(kMaxTenor)
         }
         __syncthreads();
     }
+}
+
+// The moving-frame coefficients of the Euler response form's parts (the
+// frame, M^-k and Q(a) are stated with kStateRow): row n = b stride + s of
+// the evolved steps (b >= 1, m = n - stride), entry 3 c + k = {C hi, G hi,
+// C lo, G lo} of C(m) = M^-(m+1) B and G(m) = Q(m) C(m), B[c][k] = svc[k][c];
+// FP64, each split into the nearest float and the float nearest the rest.
+struct StateCoefArgs {
+    double k1, k2;
+    double svc[kFactors][3];
+};
+
+__global__ void state_coef_kernel(StateCoefArgs a, int stride, int B, float4* __restrict__ coef)
+{
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t rows = (int64_t)(B - 1) * stride;
+    if (idx >= rows * kStateRow) return;
+    const int64_t m = idx / kStateRow;
+    const int c = (int)(idx % kStateRow) / 3, k = (int)(idx % kStateRow) % 3;
+    const double kk = (double)(m + 1), q = (double)m, k1 = a.k1, k2 = a.k2;
+    const double minv[3][3] = {{1.0, -kk * k1, -kk * k2 + kk * (kk + 1.0) * k1 * k1}, {0.0, 1.0, -2.0 * kk * k1},
+                               {0.0, 0.0, 1.0}};
+    const double h = 0.5 * q * (q + 1.0);
+    const double Q[3][3] = {{q, h * k1, h * k2 + (q + 1.0) * q * (q - 1.0) / 3.0 * k1 * k1}, {0.0, q, 2.0 * h * k1},
+                            {0.0, 0.0, q}};
+    double C[3];  // column k of C(m)
+    for (int r = 0; r < 3; ++r) C[r] = minv[r][0] * a.svc[k][0] + minv[r][1] * a.svc[k][1] + minv[r][2] * a.svc[k][2];
+    const double cv = C[c], gv = Q[c][0] * C[0] + Q[c][1] * C[1] + Q[c][2] * C[2];
+    const float ch = __double2float_rn(cv), gh = __double2float_rn(gv);
+    coef[(size_t)(stride + m) * kStateRow + 3 * c + k] =
+        make_float4(ch, gh, __double2float_rn(cv - (double)ch), __double2float_rn(gv - (double)gh));
 }
 
 // Epilogue of the mixed-precision path kernels (as fp64_epilogue, exposures
@@ -1011,7 +1067,25 @@ cudaError_t launch_response_table_vol(int nt, double c, int stride, int n_blocks
 
 int response_max_dates() { return kRespDates; }
 
-size_t response_table_elems(int stride, int n_blocks) { return (size_t)n_blocks * stride * kRespRow; }
+size_t response_table_elems(int stride, int n_blocks)
+{
+    return (size_t)n_blocks * stride * (kRespRow + kStateRow);
+}
+
+cudaError_t launch_state_coefs(const PathParams<double>& P, float4* resp, cudaStream_t s)
+{
+    if (P.n_blocks < 2 || P.n_blocks > kRespDates || P.stride < 1) return cudaErrorInvalidValue;
+    StateCoefArgs a;
+    a.k1 = P.k1;
+    a.k2 = P.k2;
+    for (int k = 0; k < kFactors; ++k)
+        for (int d = 0; d < 3; ++d) a.svc[k][d] = P.svc[k][d];
+    const int64_t total = (int64_t)(P.n_blocks - 1) * P.stride * kStateRow;
+    const int threads = 256;
+    state_coef_kernel<<<(unsigned)((total + threads - 1) / threads), threads, 0, s>>>(
+        a, P.stride, P.n_blocks, resp + (size_t)P.n_blocks * P.stride * kRespRow);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_response_table(int nt, double c, int stride, int n_blocks, bool pc, double w0, double w1,
                                   double w2, float4* resp, cudaStream_t s)

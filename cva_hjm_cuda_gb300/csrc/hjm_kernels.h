@@ -50,7 +50,8 @@ constexpr int kFormPolyTri = 2;  // ... with factor k of degree <= k
 
 // poly: the volatility factors are polynomials of degree <= 2 in T (PathParams::svc);
 // resp: the response table of the polynomial form's remainder (the response
-// form, at most response_max_dates() dates), or null for the convected form
+// form, at most response_max_dates() dates) followed by the moving-frame
+// coefficients of its parts (launch_state_coefs), or null for the convected form
 cudaError_t launch_path_fp64(int nt, const PathParams<double>& P, bool poly, const float4* resp, const double* ext,
                              double* partials, double* estore, cudaStream_t s);
 int response_max_dates();
@@ -62,11 +63,15 @@ cudaError_t launch_path_fp64_vresp(int nt, const PathParams<double>& P, const do
 size_t response_table_vol_elems(int stride, int n_blocks);  // double2 entries
 cudaError_t launch_response_table_vol(int nt, double c, int stride, int n_blocks, bool pc, const double* sv,
                                       double2* vresp, cudaStream_t s);
-size_t response_table_elems(int stride, int n_blocks);  // float4 entries of the table
+size_t response_table_elems(int stride, int n_blocks);  // float4 entries: responses, then coefficients
 // Euler: w1 = kappa = -2 c dtau^2 (w0, w2 unused); predictor-corrector: w0 =
 // wL1, w1 = wL - gL, w2 = gL (PcParams)
 cudaError_t launch_response_table(int nt, double c, int stride, int n_blocks, bool pc, double w0, double w1,
                                   double w2, float4* resp, cudaStream_t s);
+// The Euler response form's moving-frame coefficients of S, U, W from P.k1,
+// P.k2, P.svc, P.stride and P.n_blocks, into the rows after the response
+// table in resp (whose size response_table_elems counts)
+cudaError_t launch_state_coefs(const PathParams<double>& P, float4* resp, cudaStream_t s);
 cudaError_t launch_path_mixed(int nt, const MixedParams& M, bool poly, const double* ext, double* partials,
                               float* estore, cudaStream_t s);
 void pack_mixed_params(int nt, const PathParams<float>& P, MixedParams& M);

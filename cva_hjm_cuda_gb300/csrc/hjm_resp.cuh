@@ -103,6 +103,60 @@ __device__ __forceinline__ void df_acc(float2& A, float2& Al, float2 kh, float2 
     A = sum;
 }
 
+// (A, Al) += (kh + kl) w for w exact in FP32 (a normal draw): df_acc
+// without the w_lo term.
+__device__ __forceinline__ void df_acc_w(float2& A, float2& Al, float2 kh, float2 kl, float2 w)
+{
+    const float2 m1 = make_float2(-1.0f, -1.0f);
+    const float2 p = __fmul2_rn(kh, w);
+    float2 e = __ffma2_rn(kh, w, __fmul2_rn(p, m1));
+    e = __ffma2_rn(kl, w, e);
+    const float2 sum = __fadd2_rn(A, p);
+    const float2 bp = __ffma2_rn(A, m1, sum);
+    const float2 ap = __ffma2_rn(bp, m1, sum);
+    const float2 err = __fadd2_rn(__ffma2_rn(ap, m1, A), __ffma2_rn(bp, m1, p));
+    Al = __fadd2_rn(Al, __fadd2_rn(err, e));
+    A = sum;
+}
+
+// (A, Al) renormalised: A = fl(A + Al) and Al the exact rest (Knuth's two-sum).
+__device__ __forceinline__ void df_norm(float2& A, float2& Al)
+{
+    const float2 m1 = make_float2(-1.0f, -1.0f);
+    const float2 sum = __fadd2_rn(A, Al);
+    const float2 bp = __ffma2_rn(A, m1, sum);
+    const float2 ap = __ffma2_rn(bp, m1, sum);
+    Al = __fadd2_rn(__ffma2_rn(ap, m1, A), __ffma2_rn(bp, m1, Al));
+    A = sum;
+}
+
+// Polynomial parts in a moving frame (FP64 response form, Euler).  The Euler
+// step maps the parts x = (S, U, W) of h's quadratic to M x + B phi with
+// M = I + N, N = [[0, k1, k2], [0, 0, 2 k1], [0, 0, 0]] (the upwind
+// difference of a quadratic, which the scheme takes exactly) and B[c][k] =
+// svc[k][c].  M is unipotent (N^3 = 0), so y_e = M^-e x_e moves by the noise
+// alone,
+//     y_{m+1} = y_m + C(m) phi_m,                 C(m) = M^-(m+1) B,
+// and the running sum of the parts over the evolved steps is
+//     Z_E = sum_{e=1..E} x_e = Q(E) y_E - v_E,    Q(a) = sum_{e=1..a} M^e,
+//     v_E = sum_{m<E} G(m) phi_m,                  G(m) = Q(m) C(m),
+// with M^E, M^-k and Q(a) polynomials of degree <= 3 in E, k, a:
+//     M^E   = [[1, E k1, E k2 + E(E-1) k1^2], [0, 1, 2 E k1], [0, 0, 1]],
+//     M^-k  = [[1, -k k1, -k k2 + k(k+1) k1^2], [0, 1, -2 k k1], [0, 0, 1]],
+//     Q(a)  = [[a, a(a+1)/2 k1, a(a+1)/2 k2 + (a+1)a(a-1)/3 k1^2],
+//              [0, a, a(a+1) k1], [0, 0, a]].
+// Per step the kernel adds C(m) phi to y and G(m) phi to v (6 terms for
+// factors of degree <= k, 9 in general), packed {y, v} per part in
+// double-FP32 on the FP32 pipe, and forms x_E = M^E y and Z_E in FP64 only at
+// the sampling dates.  W = y_W in every frame, so the remainder's source reads
+// its accumulator directly.  Row n (= b stride + s, m = n - stride) of the
+// coefficient table holds kStateRow float4 {C hi, G hi, C lo, G lo}, entry
+// 3 c + k for part c and factor k (state_coef_kernel), after the response
+// rows.  The rounding of x and Z: ~2e-13 of the magnitude of their terms
+// (2^-48 per double-FP32 operation over ~3,000 additions), the FP64 recursion
+// ~1e-14.
+constexpr int kStateRow = 9;
+
 // Slots with a nonzero term at step s of block b: q_min is the nearest date
 // whose lag l = q stride - 1 - s reaches its tenor, and the slots 0 .. n_act -
 // 1 hold the dates b + q_min .. B (n_act <= 0: none).  Euler (one tenor per

@@ -291,8 +291,9 @@ hjm_status hjm_run_static(void* cuda_stream, int32_t n_tenor, double dtau, const
         const bool poly = fit_quadratic_vols(vol_host, n_tenor, dtau, coef);
         const size_t entries = response_table_vol_elems((int)stride, B);
         if (poly && B >= 2 && B <= response_max_dates() && response_table_elems((int)stride, B) <= kStaticRespEntries) {
-            // the decomposition: S, U, W in FP64, the remainder's table (FP32
-            // pairs, 16 bytes per entry like the double2 array) in the static array
+            // the decomposition: the remainder's table and the coefficients of
+            // S, U, W (FP32 pairs, 16 bytes per entry like the double2 array)
+            // in the static array
             const double sq = std::sqrt(dt), c = dt / dtau;
             for (int k = 0; k < kFactors; ++k)
                 for (int d = 0; d < 3; ++d) P.svc[k][d] = sq * coef[k * 3 + d];
@@ -302,6 +303,7 @@ hjm_status hjm_run_static(void* cuda_stream, int32_t n_tenor, double dtau, const
             float4* table = reinterpret_cast<float4*>(resp_table);
             STATIC_CUDA(cudaMemsetAsync(table, 0, sizeof(float4) * response_table_elems((int)stride, B), s));
             STATIC_CUDA(launch_response_table(n_tenor, c, (int)stride, B, false, 0.0, -2.0 * P.k2, 0.0, table, s));
+            STATIC_CUDA(launch_state_coefs(P, table, s));
             STATIC_CUDA(launch_path_fp64(n_tenor, P, true, table, nullptr, partials, nullptr, s));
         } else if (B >= 2 && B <= response_max_dates() && entries <= kStaticRespEntries) {
             // the response form: its table (zero outside the live entries) into the static array
