@@ -117,24 +117,52 @@ def algorithmic_flops_per_path(n_tenor: int, n_steps: int, stride: int, form: st
     return steps + recovery
 
 
+def response_active_prefix(n_tenor: int, n_steps: int, stride: int, dtau: float = 0.5):
+    """Per row b stride + s of the Euler response table, the active prefix the
+    kernel reads (response_active_kernel): the slots up to the last whose
+    coefficient kappa G_j(lag) or running-sum coefficient kappa CG_j(lag), in
+    FP32, is nonzero and at least 2^-70 of its slot's largest; lag = (j - b)
+    stride - 1 - s for date j = B - slot, G_j(m) = (A^m e_L)[j] by m upwind
+    steps with c = 1 / stride."""
+    import numpy as np
+
+    B, L = n_steps // stride, n_tenor - 1
+    c = 1.0 / stride
+    kappa = -2.0 * c * dtau * dtau
+    rows = B * stride
+    tab = np.zeros((rows, 24, 2))
+    v = np.zeros(n_tenor)
+    v[L] = 1.0
+    cum = np.zeros(n_tenor)
+    for m in range((B - 1) * stride):
+        cum += v
+        q = m // stride + 1
+        for j in range(max(2, q + 1), B + 1):
+            tab[(j - q) * stride + (q * stride - 1 - m), B - j] = (kappa * v[j], kappa * cum[j])
+        vn = v.copy()
+        vn[:L] = v[:L] + c * (v[1:] - v[:L])
+        vn[L] = v[L] + c * (v[L] - v[L - 1])
+        v = vn
+    t32 = tab.astype(np.float32)
+    a = np.abs(t32)
+    thr = (a.max(axis=0) * np.float32(2.0 ** -70)).astype(np.float32)
+    sig = ((t32 != 0) & (a >= thr)).any(axis=2)
+    return np.where(sig.any(axis=1), 24 - np.argmax(sig[:, ::-1], axis=1), 0)
+
+
 def response_fp32_flops_per_path(n_tenor: int, n_steps: int, stride: int, form: str = "poly_tri") -> int:
     """FP32 flops of the Euler response form's double-FP32 terms per path.
-    At each evolved step: the date slots in groups of four covering the dates
-    whose response is not yet an exact zero, each slot one packed {value,
-    running sum} update of 2 FMUL2 + 7 FFMA2 + 4 FADD2 = 40 flops (product with
+    At each evolved step: the date slots in groups of four covering the row's
+    active prefix (``response_active_prefix``), each slot one packed {value,
+    running sum} update of 1 FMUL2 + 8 FFMA2 + 3 FADD2 = 40 flops (product with
     its exact leading term, Knuth two-sum, low-part update); and the parts'
     moving-frame terms, 6 (``poly_tri``) or 9 (``poly``) packed {y, v} updates
-    with an exact FP32 normal, 2 FMUL2 + 6 FFMA2 + 4 FADD2 = 36 flops each.
+    with an exact FP32 normal, 1 FMUL2 + 7 FFMA2 + 3 FADD2 = 36 flops each.
     At each sampled date the parts' renormalisation, 3 x (2 FADD2 + 4 FFMA2)
     = 60 flops."""
     B = n_steps // stride
-    L = n_tenor - 1
-    slots = 0
-    for b in range(1, B):
-        for s in range(stride):
-            q_min = (s + 1 + L - b + stride) // (stride + 1)
-            n_act = B - b - q_min + 1
-            slots += 4 * ((n_act + 3) // 4) if n_act > 0 else 0
+    pre = response_active_prefix(n_tenor, n_steps, stride)[stride:]
+    slots = int((4 * ((pre + 3) // 4)).sum())
     terms = 6 if form == "poly_tri" else 9
     return 40 * slots + 36 * terms * (B - 1) * stride + 60 * B
 

@@ -746,7 +746,8 @@ static hjm_status ensure_response_table(hjm_ctx* ctx, const RunShape& sh, double
         HJM_CUDA(ctx, cudaStreamWaitEvent(s, ctx->resp_used, 0));
     HJM_CUDA(ctx, cudaMemsetAsync(ctx->resp.p, 0, bytes, s));  // entries the kernel reads as exact zeros
     HJM_CUDA(ctx, launch_response_table(ctx->nt, c, sh.stride, sh.B, pc, w0, w1, w2, (float4*)ctx->resp.p, s));
-    ctx->stat_launches += 1;
+    HJM_CUDA(ctx, launch_response_active(sh.stride, sh.B, (float4*)ctx->resp.p, s));
+    ctx->stat_launches += 2;
     if (P) {
         HJM_CUDA(ctx, launch_state_coefs(*P, (float4*)ctx->resp.p, s));
         ctx->stat_launches += 1;

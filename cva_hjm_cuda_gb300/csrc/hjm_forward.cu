@@ -278,6 +278,7 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
 #pragma unroll
     for (int c = 0; c < 3; ++c) Y[c] = Yl[c] = make_float2(0.0f, 0.0f);
     const float4* coef = resp + (size_t)B * P.stride * kRespRow;
+    const int* nact = reinterpret_cast<const int*>(coef + (size_t)B * P.stride * kStateRow);
     const double k1 = P.k1, k2 = P.k2, k1s = P.k1 * P.k1;
 
     // price date i from the sampled numeraire (x_i, D_i); the parts after
@@ -327,10 +328,11 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
             } else {
                 draw_phi<float, false>(ext, gpath, lp, P.n_paths, n, P.rk0, P.rk1, ph[0], ph[1], ph[2]);
             }
-            const int n_act = resp_n_act(s, b, B, L, P.stride);  // uniform
+            const int n_act = __ldg(nact + n);  // uniform: the row's active prefix
             const float4* rr = row + (size_t)s * kRespRow;
             // the remainder's source: W before this step's update
             const float2 wh2 = make_float2(Y[2].x, Y[2].x), wl2 = make_float2(Yl[2].x, Yl[2].x);
+            const float2 nwh2 = make_float2(-Y[2].x, -Y[2].x);
             resp_groups(n_act, [&](auto gc) {
                 constexpr int G = decltype(gc)::value;
                 float4 k[4];
@@ -339,7 +341,7 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
 #pragma unroll
                 for (int u = 0; u < 4; ++u)
                     df_acc(A[4 * G + u], Al[4 * G + u], make_float2(k[u].x, k[u].y), make_float2(k[u].z, k[u].w),
-                           wh2, wl2);
+                           wh2, wl2, nwh2);
             });
             // y += C(m) phi, v += G(m) phi (factor k of degree <= k loads parts c <= k only)
             const float4* cr = coef + (size_t)n * kStateRow;
@@ -353,9 +355,10 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
                 if (TRI && c > k) continue;
                 const float2 kh = make_float2(q[t].x, q[t].y), kl = make_float2(q[t].z, q[t].w);
                 if constexpr (EXT)
-                    df_acc(Y[c], Yl[c], kh, kl, make_float2(ph[k], ph[k]), make_float2(pl[k], pl[k]));
+                    df_acc(Y[c], Yl[c], kh, kl, make_float2(ph[k], ph[k]), make_float2(pl[k], pl[k]),
+                           make_float2(-ph[k], -ph[k]));
                 else
-                    df_acc_w(Y[c], Yl[c], kh, kl, make_float2(ph[k], ph[k]));
+                    df_acc_w(Y[c], Yl[c], kh, kl, make_float2(ph[k], ph[k]), make_float2(-ph[k], -ph[k]));
             }
         }
         sample(b + 1);
@@ -438,6 +441,40 @@ __global__ void __launch_bounds__(kMaxTenor)
             g2 += c * (g2 - u_s[L - 1]);
         }
         __syncthreads();
+    }
+}
+
+// Per row of the response table (rows * kRespRow entries), the active
+// prefix n_act[row]: the slots up to the last one whose coefficient or
+// running-sum coefficient reaches 2^-70 of the largest of its slot over all
+// rows (slot r is one date, so the largest is that date's largest response).
+// The slots after it hold only terms near the transport front, where the
+// response is vanishingly small (at most ~1e3 terms, each below 2^-70 of the
+// date's largest coefficient, times W); the kernels skip them.  Zero slots
+// never count.  n_act[rows] = 0 (read ahead by the kernels).  One CTA.
+__global__ void __launch_bounds__(1024) response_active_kernel(int rows, const float4* __restrict__ resp,
+                                                               int* __restrict__ n_act)
+{
+    __shared__ unsigned int mc[kRespRow], ms[kRespRow];
+    if (threadIdx.x < kRespRow) mc[threadIdx.x] = ms[threadIdx.x] = 0u;
+    __syncthreads();
+    const int64_t total = (int64_t)rows * kRespRow;
+    for (int64_t i = threadIdx.x; i < total; i += blockDim.x) {
+        const float4 e = resp[i];
+        const int r = (int)(i % kRespRow);
+        atomicMax(&mc[r], __float_as_uint(fabsf(e.x)));  // non-negative floats order as their bits
+        atomicMax(&ms[r], __float_as_uint(fabsf(e.y)));
+    }
+    __syncthreads();
+    for (int row = threadIdx.x; row <= rows; row += blockDim.x) {
+        int n = 0;
+        if (row < rows)
+            for (int r = 0; r < kRespRow; ++r) {
+                const float4 e = resp[(size_t)row * kRespRow + r];
+                const float tc = __uint_as_float(mc[r]) * 0x1p-70f, ts = __uint_as_float(ms[r]) * 0x1p-70f;
+                if ((e.x != 0.0f && fabsf(e.x) >= tc) || (e.y != 0.0f && fabsf(e.y) >= ts)) n = r + 1;
+            }
+        n_act[row] = n;
     }
 }
 
@@ -1069,7 +1106,17 @@ int response_max_dates() { return kRespDates; }
 
 size_t response_table_elems(int stride, int n_blocks)
 {
-    return (size_t)n_blocks * stride * (kRespRow + kStateRow);
+    const size_t rows = (size_t)n_blocks * stride;
+    return rows * (kRespRow + kStateRow) + (rows + 4) / 4;  // + the active counts (and one more), 4 ints per entry
+}
+
+cudaError_t launch_response_active(int stride, int n_blocks, float4* resp, cudaStream_t s)
+{
+    if (n_blocks < 1 || n_blocks > kRespDates || stride < 1) return cudaErrorInvalidValue;
+    const int rows = n_blocks * stride;
+    response_active_kernel<<<1, 1024, 0, s>>>(rows, resp,
+                                             reinterpret_cast<int*>(resp + (size_t)rows * (kRespRow + kStateRow)));
+    return cudaGetLastError();
 }
 
 cudaError_t launch_state_coefs(const PathParams<double>& P, float4* resp, cudaStream_t s)

@@ -63,11 +63,14 @@ cudaError_t launch_path_fp64_vresp(int nt, const PathParams<double>& P, const do
 size_t response_table_vol_elems(int stride, int n_blocks);  // double2 entries
 cudaError_t launch_response_table_vol(int nt, double c, int stride, int n_blocks, bool pc, const double* sv,
                                       double2* vresp, cudaStream_t s);
-size_t response_table_elems(int stride, int n_blocks);  // float4 entries: responses, then coefficients
+size_t response_table_elems(int stride, int n_blocks);  // float4 entries: responses, coefficients, prefixes
 // Euler: w1 = kappa = -2 c dtau^2 (w0, w2 unused); predictor-corrector: w0 =
 // wL1, w1 = wL - gL, w2 = gL (PcParams)
 cudaError_t launch_response_table(int nt, double c, int stride, int n_blocks, bool pc, double w0, double w1,
                                   double w2, float4* resp, cudaStream_t s);
+// The active prefix of each row of the response table in resp (after the
+// table and the coefficient rows), from the table's values
+cudaError_t launch_response_active(int stride, int n_blocks, float4* resp, cudaStream_t s);
 // The Euler response form's moving-frame coefficients of S, U, W from P.k1,
 // P.k2, P.svc, P.stride and P.n_blocks, into the rows after the response
 // table in resp (whose size response_table_elems counts)

@@ -188,6 +188,8 @@ __global__ void __launch_bounds__(kPcCta, 6)
     for (int r = 0; r < kRespSlots; ++r) A[r] = Al[r] = make_float2(0.0f, 0.0f);
     double S = 0.0, U = 0.0, W = 0.0;
     double sS = 0.0, sU = 0.0, sW = 0.0;  // running sums before the current step (sampling adds it)
+    // the active prefix of each row, after the table's response and coefficient rows
+    const int* nact = reinterpret_cast<const int*>(resp + (size_t)B * P.stride * (kRespRow + kStateRow));
 
     auto sample = [&](int i) {
         const double tau = P.tau[i];
@@ -207,11 +209,11 @@ __global__ void __launch_bounds__(kPcCta, 6)
             const int n = b * P.stride + s;
             double phi0, phi1, phi2;
             draw_phi<double, EXT>(ext, gpath, active ? lp : 0, P.n_paths, n, P.rk0, P.rk1, phi0, phi1, phi2);
-            const int n_act = resp_n_act<true>(s, b, B, L, P.stride);  // uniform
+            const int n_act = __ldg(nact + n);  // uniform: the row's active prefix
             const float4* rr = row + (size_t)s * kRespRow;
             float wh, wl;
             split_f64(W, wh, wl);
-            const float2 wh2 = make_float2(wh, wh), wl2 = make_float2(wl, wl);
+            const float2 wh2 = make_float2(wh, wh), wl2 = make_float2(wl, wl), nwh2 = make_float2(-wh, -wh);
             resp_groups(n_act, [&](auto gc) {
                 constexpr int G = decltype(gc)::value;
                 float4 k[4];
@@ -220,7 +222,7 @@ __global__ void __launch_bounds__(kPcCta, 6)
 #pragma unroll
                 for (int u = 0; u < 4; ++u)
                     df_acc(A[4 * G + u], Al[4 * G + u], make_float2(k[u].x, k[u].y), make_float2(k[u].z, k[u].w),
-                           wh2, wl2);
+                           wh2, wl2, nwh2);
             });
             sS += S;
             sU += U;

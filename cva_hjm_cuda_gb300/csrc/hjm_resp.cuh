@@ -32,16 +32,16 @@ namespace hjm {
 //
 // Both sums are carried in double-FP32 arithmetic on the FP32 pipe (76 times
 // the FP64 pipe's rate on GB300): the table holds each coefficient as a pair
-// of floats hi + lo (48 significant bits), W is split into W_hi + W_lo with
-// integer operations, the product's leading term is made exact by an FMA and
-// the accumulation by Knuth's two-sum, packed {value, running sum} in FP32x2
-// instructions.  The relative error of a date's sum stays below ~1e-12 of its
-// magnitude (checked against FP64 sums of the same terms), and the
-// remainder at a sampled tenor is small: |hc| <= 7e-5 for 24 dates, the most
-// this form takes, against a curve of ~0.03 (the far tail of the transport
-// from the last tenor; below 1e-6 for the 10y swap on 51 tenors), so its
-// rounding stays within an ulp of the FP64 curve.  Per step the FP64 pipe
-// does only the polynomial parts.
+// of floats hi + lo (48 significant bits), W comes as W_hi + W_lo (the Euler
+// kernel's own double-FP32 accumulator of W; the predictor-corrector kernel
+// splits its FP64 W with integer operations), the product's leading term is
+// made exact by an FMA and the accumulation by Knuth's two-sum, packed
+// {value, running sum} in FP32x2 instructions.  The relative error of a
+// date's sum stays below ~1e-12 of its magnitude (checked against FP64 sums
+// of the same terms), and the remainder at a sampled tenor is small: |hc| <=
+// 7e-5 for 24 dates, the most this form takes, against a curve of ~0.03 (the
+// far tail of the transport from the last tenor; below 1e-6 for the 10y swap
+// on 51 tenors), so its rounding stays within an ulp of the FP64 curve.
 //
 // The accumulators of date j sit in slot r = B - j.  At step s of block b the
 // dates with a nonzero term are j = b + q for q_min <= q <= B - b, q_min the
@@ -87,34 +87,39 @@ __device__ __forceinline__ void split_f64(double d, float& hi, float& lo)
 
 // (A, Al) += (kh + kl) (wh + wl) in double-FP32, both lanes: the product's
 // leading term exact by FMA, the cross terms in FP32, kl wl (2^-48) dropped;
-// Knuth's two-sum keeps A + Al exact up to the FP32 rounding of Al.
-__device__ __forceinline__ void df_acc(float2& A, float2& Al, float2 kh, float2 kl, float2 wh, float2 wl)
+// Knuth's two-sum keeps A + Al exact up to the FP32 rounding of Al.  nwh =
+// -wh (formed once per step by the caller): the product is taken negated,
+// pn = -fl(kh wh), so that the exact error kh wh - fl(kh wh) is one FMA with
+// pn as the addend and no instruction negates a product; every rounding is
+// that of the plain formulation (negation is exact).
+__device__ __forceinline__ void df_acc(float2& A, float2& Al, float2 kh, float2 kl, float2 wh, float2 wl, float2 nwh)
 {
     const float2 m1 = make_float2(-1.0f, -1.0f);
-    const float2 p = __fmul2_rn(kh, wh);
-    float2 e = __ffma2_rn(kh, wh, __fmul2_rn(p, m1));
+    const float2 pn = __fmul2_rn(kh, nwh);
+    float2 e = __ffma2_rn(kh, wh, pn);
     e = __ffma2_rn(kh, wl, e);
     e = __ffma2_rn(kl, wh, e);
-    const float2 sum = __fadd2_rn(A, p);
+    const float2 sum = __ffma2_rn(pn, m1, A);   // A + p
     const float2 bp = __ffma2_rn(A, m1, sum);   // sum - A
     const float2 ap = __ffma2_rn(bp, m1, sum);  // sum - bp
-    const float2 err = __fadd2_rn(__ffma2_rn(ap, m1, A), __ffma2_rn(bp, m1, p));
+    // (A - ap) + (p - bp), with p - bp = -(pn + bp)
+    const float2 err = __ffma2_rn(__fadd2_rn(pn, bp), m1, __ffma2_rn(ap, m1, A));
     Al = __fadd2_rn(Al, __fadd2_rn(err, e));
     A = sum;
 }
 
-// (A, Al) += (kh + kl) w for w exact in FP32 (a normal draw): df_acc
-// without the w_lo term.
-__device__ __forceinline__ void df_acc_w(float2& A, float2& Al, float2 kh, float2 kl, float2 w)
+// (A, Al) += (kh + kl) w for w exact in FP32 (a normal draw), nw = -w:
+// df_acc without the w_lo term.
+__device__ __forceinline__ void df_acc_w(float2& A, float2& Al, float2 kh, float2 kl, float2 w, float2 nw)
 {
     const float2 m1 = make_float2(-1.0f, -1.0f);
-    const float2 p = __fmul2_rn(kh, w);
-    float2 e = __ffma2_rn(kh, w, __fmul2_rn(p, m1));
+    const float2 pn = __fmul2_rn(kh, nw);
+    float2 e = __ffma2_rn(kh, w, pn);
     e = __ffma2_rn(kl, w, e);
-    const float2 sum = __fadd2_rn(A, p);
+    const float2 sum = __ffma2_rn(pn, m1, A);
     const float2 bp = __ffma2_rn(A, m1, sum);
     const float2 ap = __ffma2_rn(bp, m1, sum);
-    const float2 err = __fadd2_rn(__ffma2_rn(ap, m1, A), __ffma2_rn(bp, m1, p));
+    const float2 err = __ffma2_rn(__fadd2_rn(pn, bp), m1, __ffma2_rn(ap, m1, A));
     Al = __fadd2_rn(Al, __fadd2_rn(err, e));
     A = sum;
 }

@@ -2,7 +2,15 @@
 numerators): each form's count restated from its kernel's formulas."""
 from __future__ import annotations
 
+import sys
+from pathlib import Path
+
+import numpy as np
+
 import bench
+
+sys.path.insert(0, str(Path(__file__).parent))
+import test_response_form as R  # noqa: E402
 
 
 def test_response_forms_count_the_kernels_operations():
@@ -28,3 +36,10 @@ def test_convected_forms_exceed_the_response_forms():
         conv = bench.algorithmic_flops_per_path(51, 1000, 50, form)
         resp = bench.algorithmic_flops_per_path(51, 1000, 50, form, "response")
         assert resp < conv, form
+
+
+def test_response_slots_follow_the_kernels_value_prefix():
+    for nt, n_steps, stride in ((51, 1000, 50), (61, 1000, 50), (51, 600, 25)):
+        B = n_steps // stride
+        tab, _, _ = R.response_table(nt, stride, B, 1.0 / stride, 0.5)
+        np.testing.assert_array_equal(bench.response_active_prefix(nt, n_steps, stride), R.active_prefix(tab, B, stride))

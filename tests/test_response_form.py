@@ -74,8 +74,46 @@ def test_table_covers_every_lag_once_and_prefix_holds_the_nonzeros(nt, stride, B
                     assert tab[idx, 0] == 0.0 and tab[idx, 1] == 0.0, (b, s, r)
 
 
-def _direct_and_response(nt, stride, B, c, dtau, W, df=False):
+@pytest.mark.parametrize("nt,stride,B,c", SHAPES)
+def test_value_prefix_drops_only_vanishing_terms(nt, stride, B, c):
+    """The kernels' prefix from the table's values never exceeds the
+    closed-form one, and the terms it drops (near the transport front) add up,
+    over all its rows (at most 2,400 here), to less than rows x 2^-70 of the
+    date's largest coefficient per unit |W|: below 2^-58, far under the
+    double-FP32 sums' own 2^-48 rounding."""
+    tab, _, _ = response_table(nt, stride, B, c, 0.5)
+    L = nt - 1
+    pre = active_prefix(tab, B, stride)
+    T = tab.reshape(B * stride, ROW, 2)
+    dropped = np.zeros((ROW, 2))
+    for b in range(1, B):
+        for s in range(stride):
+            n = b * stride + s
+            assert pre[n] <= max(n_active(s, b, B, L, stride), 0)
+            # (entries that are zero in FP32 are zeros of the kernels' table anyway)
+            tail = T[n, pre[n]:]
+            dropped[pre[n]:] += np.where(tail.astype(np.float32) != 0, np.abs(tail), 0.0)
+    big = np.abs(T).max(axis=0)
+    assert np.all(dropped <= B * stride * 2.0 ** -70 * big + 1e-300)
+    if (nt, stride, B) == (51, 50, 20):
+        assert pre[stride:].mean() < 0.9 * np.mean([max(n_active(s, b, B, L, stride), 0)
+                                                    for b in range(1, B) for s in range(stride)])
+
+
+def active_prefix(tab, B, stride):
+    """As response_active_kernel: per row, the slots up to the last whose
+    coefficient or running-sum coefficient (FP32 hi part) is nonzero and at
+    least 2^-70 of its slot's largest over all rows."""
+    T = tab.reshape(B * stride, ROW, 2).astype(np.float32)
+    a = np.abs(T)
+    thr = (a.max(axis=0) * np.float32(2.0 ** -70)).astype(np.float32)
+    sig = ((T != 0) & (a >= thr)).any(axis=2)
+    return np.where(sig.any(axis=1), ROW - np.argmax(sig[:, ::-1], axis=1), 0)
+
+
+def _direct_and_response(nt, stride, B, c, dtau, W, df=False, cutoff=False):
     tab, _, kappa = response_table(nt, stride, B, c, dtau)
+    prefix = active_prefix(tab, B, stride) if cutoff else None
     L = nt - 1
     acc = np.zeros((ROW, 2))
     dfa = [[DF(), DF()] for _ in range(ROW)]
@@ -86,7 +124,7 @@ def _direct_and_response(nt, stride, B, c, dtau, W, df=False):
     for b in range(1, B):
         for s in range(stride):
             n = b * stride + s
-            n_act = n_active(s, b, B, L, stride)
+            n_act = prefix[n] if cutoff else n_active(s, b, B, L, stride)
             wh, wl = split_f64(w)
             for r in range(max(n_act, 0)):
                 k = tab[(b * stride + s) * ROW + r]
@@ -111,14 +149,20 @@ def _rel(a, b):
     return abs(a - b) / abs(b) if b != 0.0 else abs(a)
 
 
+@pytest.mark.parametrize("cutoff", [False, True], ids=["closed-form-prefix", "value-prefix"])
 @pytest.mark.parametrize("nt,stride,B,c", SHAPES[:4])
-def test_response_sums_equal_the_convected_remainder(nt, stride, B, c):
+def test_response_sums_equal_the_convected_remainder(nt, stride, B, c, cutoff):
     rng = np.random.default_rng(7)
     W = np.cumsum(rng.normal(size=B * stride)) * 1e-5
-    got, want = _direct_and_response(nt, stride, B, c, 0.5, W)
+    got, want = _direct_and_response(nt, stride, B, c, 0.5, W, cutoff=cutoff)
+    big = np.abs(response_table(nt, stride, B, c, 0.5)[0].reshape(B * stride, ROW, 2)).max(axis=0)
     for j in got:
         for q in range(2):
-            assert _rel(got[j][q], want[j][q]) < 1e-12, (j, q, got[j][q], want[j][q])
+            # the value prefix drops terms below rows x 2^-70 of the date's largest
+            # per unit |W|, and coefficients below FP32's range (the table's
+            # FP32 pairs hold them as zeros; 1e-30 is far below the curve's ulp)
+            floor = B * stride * 2.0 ** -70 * big[B - j, q] * np.max(np.abs(W)) + 1e-30 if cutoff else 0.0
+            assert abs(got[j][q] - want[j][q]) <= 1e-12 * abs(want[j][q]) + floor, (j, q, got[j][q], want[j][q])
 
 
 # --- double-FP32 arithmetic, as the kernel's split_f64 / df_acc -------------
