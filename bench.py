@@ -90,16 +90,17 @@ def algorithmic_flops_per_path(n_tenor: int, n_steps: int, stride: int, form: st
 
     ``remainder="response"`` (FP64, at most 24 dates): polynomial forms, the
     FP64 pipe forms the parts and their running sums from the moving-frame
-    sums only at the sampled dates (56 flops per date: widening the six sums,
-    x = M^E y, Z = Q(E) y - v and the two quadratics at the date's tenor); the
-    per-step work runs in double-FP32 on the FP32 pipe
+    sums only at the sampled dates (41 flops per date: widening the six sums
+    (6), x = M^a y (6), Z += Q(a) y - v (15), the two quadratics at the date's
+    tenor (11) and the re-anchoring's rests (3)); the per-step work runs in
+    double-FP32 on the FP32 pipe
     (``response_fp32_flops_per_path``); ``table``, six FP64 FMAs per date still
     to be sampled per step (the three factors' responses, value and running
     sum); no block recovery."""
     B = n_steps // stride
     L = n_tenor - 1
     if remainder == "response" and form != "table":
-        return 56 * B
+        return 41 * B
     if remainder == "response":
         # volatility table in the response form: per step and date still to be
         # sampled, three FMAs for the value and three for the running sum
@@ -157,14 +158,13 @@ def response_fp32_flops_per_path(n_tenor: int, n_steps: int, stride: int, form: 
     running sum} update of 1 FMUL2 + 8 FFMA2 + 3 FADD2 = 40 flops (product with
     its exact leading term, Knuth two-sum, low-part update); and the parts'
     moving-frame terms, 6 (``poly_tri``) or 9 (``poly``) packed {y, v} updates
-    with an exact FP32 normal, 1 FMUL2 + 7 FFMA2 + 3 FADD2 = 36 flops each.
-    At each sampled date the parts' renormalisation, 3 x (2 FADD2 + 4 FFMA2)
-    = 60 flops."""
+    with an exact FP32 normal, 1 FMUL2 + 7 FFMA2 + 3 FADD2 = 36 flops each,
+    and their renormalisation, 3 x (1 FADD2 + 2 FFMA2) = 30 flops."""
     B = n_steps // stride
     pre = response_active_prefix(n_tenor, n_steps, stride)[stride:]
     slots = int((4 * ((pre + 3) // 4)).sum())
     terms = 6 if form == "poly_tri" else 9
-    return 40 * slots + 36 * terms * (B - 1) * stride + 60 * B
+    return 40 * slots + (36 * terms + 30) * (B - 1) * stride
 
 
 class ClockSampler:

@@ -248,6 +248,12 @@ __host__ __device__ inline size_t resp_smem_bytes(int n_blocks)
     return ((size_t)n_blocks + 2) * kFp64Cta * 8 + 2 * (kFp64Cta / 32) * 8;
 }
 
+// the Euler response kernel: and the running sums of the parts [3][kCta]
+__host__ __device__ inline size_t resp_smem_bytes_parts(int n_blocks)
+{
+    return resp_smem_bytes(n_blocks) + 3 * kFp64Cta * 8;
+}
+
 template <int NT, bool EXT, bool TRI>
 __global__ void __launch_bounds__(kFp64Cta, 6)
     path_kernel_fp64_resp(const __grid_constant__ PathParams<double> P, const float4* __restrict__ resp,
@@ -272,40 +278,55 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
     float2 A[kRespSlots], Al[kRespSlots];
 #pragma unroll
     for (int r = 0; r < kRespSlots; ++r) A[r] = Al[r] = make_float2(0.0f, 0.0f);
-    // the parallel, tilt and curvature parts in the moving frame, {y_c, v_c}
-    // as hi + lo pairs (c = S, U, W)
+    // the parallel, tilt and curvature parts in the block's moving frame,
+    // {y_c, v_c} as hi + lo pairs (c = S, U, W), anchored at the block's start
     float2 Y[3], Yl[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) Y[c] = Yl[c] = make_float2(0.0f, 0.0f);
-    const float4* coef = resp + (size_t)B * P.stride * kRespRow;
-    const int* nact = reinterpret_cast<const int*>(coef + (size_t)B * P.stride * kStateRow);
-    const double k1 = P.k1, k2 = P.k2, k1s = P.k1 * P.k1;
+    const float4* coef = resp + resp_coef_offset(P.stride, B);
+    const int* nact = reinterpret_cast<const int*>(resp + resp_nact_offset(P.stride, B));
+    // the running sums Z of the parts over the evolved steps, FP64, between blocks
+    double* z_s = red_s + 2 * (kCta / 32);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) z_s[c * kCta + tid] = 0.0;
+    // M^a and Q(a) for a block of a = stride steps (uniform)
+    const double a = (double)P.stride, k1 = P.k1, k2 = P.k2, k1s = P.k1 * P.k1, ha = 0.5 * a * (a + 1.0);
+    const double m01 = a * k1, m02 = a * fma(a - 1.0, k1s, k2), m12 = 2.0 * a * k1;
+    const double q01 = ha * k1, q02 = fma(ha, k2, (a + 1.0) * a * (a - 1.0) / 3.0 * k1s), q12 = 2.0 * ha * k1;
 
-    // price date i from the sampled numeraire (x_i, D_i); the parts after
-    // E = (i - 1) stride evolved steps: x_E = M^E y, Z_E = Q(E) y - v
+    // price date i from the sampled numeraire (x_i, D_i); for i >= 2 the
+    // block just ended: x = M^a y, Z += Q(a) y - v, then y re-anchored on x
     auto sample = [&](int i) {
         const double tau = P.tau[i];
         double hc = 0.0, hcs = 0.0;
+        double S = 0.0, U = 0.0, W = 0.0, ZS = 0.0, ZU = 0.0, ZW = 0.0;
         if (i >= 2) {
             const float2 h = select_reg<kRespSlots, float2>(A, B - i), l = select_reg<kRespSlots, float2>(Al, B - i);
             hc = widen_f32(h.x) + widen_f32(l.x);
             hcs = widen_f32(h.y) + widen_f32(l.y);
-        }
-        double y[3], v[3];
+            double y[3], v[3];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            df_norm(Y[c], Yl[c]);
-            y[c] = widen_f32(Y[c].x) + widen_f32(Yl[c].x);
-            v[c] = widen_f32(Y[c].y) + widen_f32(Yl[c].y);
+            for (int c = 0; c < 3; ++c) {
+                y[c] = widen_f32(Y[c].x) + widen_f32(Yl[c].x);
+                v[c] = widen_f32(Y[c].y) + widen_f32(Yl[c].y);
+            }
+            W = y[2];
+            U = fma(m12, y[2], y[1]);
+            S = fma(m01, y[1], fma(m02, y[2], y[0]));
+            ZW = z_s[2 * kCta + tid] + fma(a, y[2], -v[2]);
+            ZU = z_s[kCta + tid] + fma(a, y[1], fma(q12, y[2], -v[1]));
+            ZS = z_s[tid] + fma(a, y[0], fma(q01, y[1], fma(q02, y[2], -v[0])));
+            z_s[tid] = ZS;
+            z_s[kCta + tid] = ZU;
+            z_s[2 * kCta + tid] = ZW;
+            const double x3[3] = {S, U, W};
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float xh = __double2float_rn(x3[c]);
+                Y[c] = make_float2(xh, 0.0f);
+                Yl[c] = make_float2(__double2float_rn(x3[c] - (double)xh), 0.0f);
+            }
         }
-        const double E = (double)((i - 1) * P.stride), e1 = 0.5 * E * (E + 1.0);
-        const double W = y[2];
-        const double U = fma(2.0 * E * k1, y[2], y[1]);
-        const double S = fma(E * k1, y[1], fma(E * fma(E - 1.0, k1s, k2), y[2], y[0]));
-        const double ZW = fma(E, y[2], -v[2]);
-        const double ZU = fma(E, y[1], fma(2.0 * e1 * k1, y[2], -v[1]));
-        const double ZS =
-            fma(E, y[0], fma(e1 * k1, y[1], fma(fma(e1, k2, (E + 1.0) * E * (E - 1.0) / 3.0 * k1s), y[2], -v[0])));
         const double x = P.psamp[i] + (fma(tau, fma(tau, W, U), S) + hc);
         const double acc = fma(tau, fma(tau, ZW, ZU), ZS) + hcs;
         const double D = exp(-(P.psum[i] + acc) * P.dt);
@@ -343,8 +364,8 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
                     df_acc(A[4 * G + u], Al[4 * G + u], make_float2(k[u].x, k[u].y), make_float2(k[u].z, k[u].w),
                            wh2, wl2, nwh2);
             });
-            // y += C(m) phi, v += G(m) phi (factor k of degree <= k loads parts c <= k only)
-            const float4* cr = coef + (size_t)n * kStateRow;
+            // y += C(s) phi, v += G(s) phi (factor k of degree <= k loads parts c <= k only)
+            const float4* cr = coef + (size_t)s * kStateRow;
             float4 q[kStateRow];
 #pragma unroll
             for (int t = 0; t < kStateRow; ++t)
@@ -359,6 +380,7 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
                            make_float2(-ph[k], -ph[k]));
                 else
                     df_acc_w(Y[c], Yl[c], kh, kl, make_float2(ph[k], ph[k]), make_float2(-ph[k], -ph[k]));
+                if (k == 2) df_renorm(Y[c], Yl[c]);  // the part's last term of the step
             }
         }
         sample(b + 1);
@@ -479,20 +501,19 @@ __global__ void __launch_bounds__(1024) response_active_kernel(int rows, const f
 }
 
 // The moving-frame coefficients of the Euler response form's parts (the
-// frame, M^-k and Q(a) are stated with kStateRow): row n = b stride + s of
-// the evolved steps (b >= 1, m = n - stride), entry 3 c + k = {C hi, G hi,
-// C lo, G lo} of C(m) = M^-(m+1) B and G(m) = Q(m) C(m), B[c][k] = svc[k][c];
-// FP64, each split into the nearest float and the float nearest the rest.
+// frame, M^-k and Q(a) are stated with kStateRow): row s < stride (the step
+// within a block), entry 3 c + k = {C hi, G hi, C lo, G lo} of C(s) =
+// M^-(s+1) B and G(s) = Q(s) C(s), B[c][k] = svc[k][c]; FP64, each split into
+// the nearest float and the float nearest the rest.
 struct StateCoefArgs {
     double k1, k2;
     double svc[kFactors][3];
 };
 
-__global__ void state_coef_kernel(StateCoefArgs a, int stride, int B, float4* __restrict__ coef)
+__global__ void state_coef_kernel(StateCoefArgs a, int stride, float4* __restrict__ coef)
 {
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t rows = (int64_t)(B - 1) * stride;
-    if (idx >= rows * kStateRow) return;
+    if (idx >= (int64_t)stride * kStateRow) return;
     const int64_t m = idx / kStateRow;
     const int c = (int)(idx % kStateRow) / 3, k = (int)(idx % kStateRow) % 3;
     const double kk = (double)(m + 1), q = (double)m, k1 = a.k1, k2 = a.k2;
@@ -505,7 +526,7 @@ __global__ void state_coef_kernel(StateCoefArgs a, int stride, int B, float4* __
     for (int r = 0; r < 3; ++r) C[r] = minv[r][0] * a.svc[k][0] + minv[r][1] * a.svc[k][1] + minv[r][2] * a.svc[k][2];
     const double cv = C[c], gv = Q[c][0] * C[0] + Q[c][1] * C[1] + Q[c][2] * C[2];
     const float ch = __double2float_rn(cv), gh = __double2float_rn(gv);
-    coef[(size_t)(stride + m) * kStateRow + 3 * c + k] =
+    coef[(size_t)m * kStateRow + 3 * c + k] =
         make_float4(ch, gh, __double2float_rn(cv - (double)ch), __double2float_rn(gv - (double)gh));
 }
 
@@ -1027,7 +1048,7 @@ template <int NT, bool EXT, bool TRI>
 static cudaError_t launch_fp64_resp_t(const PathParams<double>& P, const float4* resp, const double* ext,
                                       double* partials, double* estore, cudaStream_t s)
 {
-    const size_t smem = resp_smem_bytes(P.n_blocks);
+    const size_t smem = resp_smem_bytes_parts(P.n_blocks);
     auto k = path_kernel_fp64_resp<NT, EXT, TRI>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -1107,15 +1128,14 @@ int response_max_dates() { return kRespDates; }
 size_t response_table_elems(int stride, int n_blocks)
 {
     const size_t rows = (size_t)n_blocks * stride;
-    return rows * (kRespRow + kStateRow) + (rows + 4) / 4;  // + the active counts (and one more), 4 ints per entry
+    return resp_nact_offset(stride, n_blocks) + (rows + 4) / 4;  // the active counts (and one more), 4 ints per entry
 }
 
 cudaError_t launch_response_active(int stride, int n_blocks, float4* resp, cudaStream_t s)
 {
     if (n_blocks < 1 || n_blocks > kRespDates || stride < 1) return cudaErrorInvalidValue;
-    const int rows = n_blocks * stride;
-    response_active_kernel<<<1, 1024, 0, s>>>(rows, resp,
-                                             reinterpret_cast<int*>(resp + (size_t)rows * (kRespRow + kStateRow)));
+    response_active_kernel<<<1, 1024, 0, s>>>(n_blocks * stride, resp,
+                                             reinterpret_cast<int*>(resp + resp_nact_offset(stride, n_blocks)));
     return cudaGetLastError();
 }
 
@@ -1127,10 +1147,10 @@ cudaError_t launch_state_coefs(const PathParams<double>& P, float4* resp, cudaSt
     a.k2 = P.k2;
     for (int k = 0; k < kFactors; ++k)
         for (int d = 0; d < 3; ++d) a.svc[k][d] = P.svc[k][d];
-    const int64_t total = (int64_t)(P.n_blocks - 1) * P.stride * kStateRow;
+    const int64_t total = (int64_t)P.stride * kStateRow;
     const int threads = 256;
     state_coef_kernel<<<(unsigned)((total + threads - 1) / threads), threads, 0, s>>>(
-        a, P.stride, P.n_blocks, resp + (size_t)P.n_blocks * P.stride * kRespRow);
+        a, P.stride, resp + resp_coef_offset(P.stride, P.n_blocks));
     return cudaGetLastError();
 }
 

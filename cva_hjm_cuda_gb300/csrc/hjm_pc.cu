@@ -189,7 +189,7 @@ __global__ void __launch_bounds__(kPcCta, 6)
     double S = 0.0, U = 0.0, W = 0.0;
     double sS = 0.0, sU = 0.0, sW = 0.0;  // running sums before the current step (sampling adds it)
     // the active prefix of each row, after the table's response and coefficient rows
-    const int* nact = reinterpret_cast<const int*>(resp + (size_t)B * P.stride * (kRespRow + kStateRow));
+    const int* nact = reinterpret_cast<const int*>(resp + resp_nact_offset(P.stride, B));
 
     auto sample = [&](int i) {
         const double tau = P.tau[i];

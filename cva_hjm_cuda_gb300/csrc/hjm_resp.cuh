@@ -124,14 +124,16 @@ __device__ __forceinline__ void df_acc_w(float2& A, float2& Al, float2 kh, float
     A = sum;
 }
 
-// (A, Al) renormalised: A = fl(A + Al) and Al the exact rest (Knuth's two-sum).
-__device__ __forceinline__ void df_norm(float2& A, float2& Al)
+// (A, Al) renormalised: A = fl(A + Al) and Al the rest (Dekker's fast
+// two-sum, exact when |A| >= |Al| or A = 0, which the accumulators keep: Al
+// only gathers rounding errors of A).  Done after every step's terms, it
+// keeps |Al| <= ulp(A) / 2, so that the FP32 rounding of the low parts stays
+// at 2^-48 of A per addition instead of growing with the number of terms.
+__device__ __forceinline__ void df_renorm(float2& A, float2& Al)
 {
     const float2 m1 = make_float2(-1.0f, -1.0f);
     const float2 sum = __fadd2_rn(A, Al);
-    const float2 bp = __ffma2_rn(A, m1, sum);
-    const float2 ap = __ffma2_rn(bp, m1, sum);
-    Al = __fadd2_rn(__ffma2_rn(ap, m1, A), __ffma2_rn(bp, m1, Al));
+    Al = __ffma2_rn(__ffma2_rn(A, m1, sum), m1, Al);  // Al - (sum - A)
     A = sum;
 }
 
@@ -139,28 +141,41 @@ __device__ __forceinline__ void df_norm(float2& A, float2& Al)
 // step maps the parts x = (S, U, W) of h's quadratic to M x + B phi with
 // M = I + N, N = [[0, k1, k2], [0, 0, 2 k1], [0, 0, 0]] (the upwind
 // difference of a quadratic, which the scheme takes exactly) and B[c][k] =
-// svc[k][c].  M is unipotent (N^3 = 0), so y_e = M^-e x_e moves by the noise
+// svc[k][c].  M is unipotent (N^3 = 0), so within a block, anchored at its
+// first step (y_0 = x at the block's start), y_s = M^-s x moves by the noise
 // alone,
-//     y_{m+1} = y_m + C(m) phi_m,                 C(m) = M^-(m+1) B,
-// and the running sum of the parts over the evolved steps is
-//     Z_E = sum_{e=1..E} x_e = Q(E) y_E - v_E,    Q(a) = sum_{e=1..a} M^e,
-//     v_E = sum_{m<E} G(m) phi_m,                  G(m) = Q(m) C(m),
-// with M^E, M^-k and Q(a) polynomials of degree <= 3 in E, k, a:
-//     M^E   = [[1, E k1, E k2 + E(E-1) k1^2], [0, 1, 2 E k1], [0, 0, 1]],
+//     y_{s+1} = y_s + C(s) phi_s,                  C(s) = M^-(s+1) B,
+// and at the block's end (s = stride)
+//     x_end = M^stride y_stride,
+//     sum_{s'=1..stride} x_s' = Q(stride) y_stride - v,   v = sum_s G(s) phi_s,
+// with Q(a) = sum_{e=1..a} M^e, G(s) = Q(s) C(s), and M^a, M^-k and Q(a)
+// polynomials of degree <= 3 in a, k:
+//     M^a   = [[1, a k1, a k2 + a(a-1) k1^2], [0, 1, 2 a k1], [0, 0, 1]],
 //     M^-k  = [[1, -k k1, -k k2 + k(k+1) k1^2], [0, 1, -2 k k1], [0, 0, 1]],
 //     Q(a)  = [[a, a(a+1)/2 k1, a(a+1)/2 k2 + (a+1)a(a-1)/3 k1^2],
 //              [0, a, a(a+1) k1], [0, 0, a]].
-// Per step the kernel adds C(m) phi to y and G(m) phi to v (6 terms for
+// Per step the kernel adds C(s) phi to y and G(s) phi to v (6 terms for
 // factors of degree <= k, 9 in general), packed {y, v} per part in
-// double-FP32 on the FP32 pipe, and forms x_E = M^E y and Z_E in FP64 only at
-// the sampling dates.  W = y_W in every frame, so the remainder's source reads
-// its accumulator directly.  Row n (= b stride + s, m = n - stride) of the
+// double-FP32 on the FP32 pipe; at each block's end (a sampling date) it
+// widens them, forms x_end and adds the block's sum to the running sums Z in
+// FP64, and re-anchors y on x_end (rounded to FP32 pairs) with v = 0; the
+// pairs are renormalised after every step (df_renorm).  The
+// coefficients are the same in every block: row s (< stride) of the
 // coefficient table holds kStateRow float4 {C hi, G hi, C lo, G lo}, entry
-// 3 c + k for part c and factor k (state_coef_kernel), after the response
-// rows.  The rounding of x and Z: ~2e-13 of the magnitude of their terms
-// (2^-48 per double-FP32 operation over ~3,000 additions), the FP64 recursion
-// ~1e-14.
+// 3 c + k for part c and factor k (state_coef_kernel).  W = y_W in every
+// frame, so the remainder's source reads its accumulator directly.  The
+// rounding: 2^-48 of the accumulator per double-FP32 addition over one
+// block's ~150 additions (~5e-14 of the parts' terms), the rest FP64.
 constexpr int kStateRow = 9;
+
+// Offsets (in float4) within the Euler or predictor-corrector response
+// table buffer: the response rows [B stride][kRespRow], the coefficient rows
+// [stride][kStateRow], the active prefixes [B stride + 1] (int).
+__host__ __device__ inline size_t resp_coef_offset(int stride, int B) { return (size_t)B * stride * kRespRow; }
+__host__ __device__ inline size_t resp_nact_offset(int stride, int B)
+{
+    return (size_t)B * stride * kRespRow + (size_t)stride * kStateRow;
+}
 
 // Slots with a nonzero term at step s of block b: q_min is the nearest date
 // whose lag l = q stride - 1 - s reaches its tenor, and the slots 0 .. n_act -

@@ -17,14 +17,15 @@ def test_response_forms_count_the_kernels_operations():
     nt, n_steps, stride = 51, 1000, 50
     B = n_steps // stride
     # polynomial response form: the FP64 pipe forms the parts at the B dates only
-    assert bench.algorithmic_flops_per_path(nt, n_steps, stride, "poly_tri", "response") == 56 * B
-    assert bench.algorithmic_flops_per_path(nt, n_steps, stride, "poly", "response") == 56 * B
+    assert bench.algorithmic_flops_per_path(nt, n_steps, stride, "poly_tri", "response") == 41 * B
+    assert bench.algorithmic_flops_per_path(nt, n_steps, stride, "poly", "response") == 41 * B
     # volatility table in the response form: six FMAs per date still to be sampled per step
     live = sum(B - b for b in range(1, B)) * stride
     assert bench.algorithmic_flops_per_path(nt, n_steps, stride, "table", "response") == 12 * live
     # the double-FP32 side: 40 flops per slot (slots in groups of four over the
-    # active prefix), 36 per moving-frame term (6 or 9 per step), 60 per date
-    parts_tri = 36 * 6 * (B - 1) * stride + 60 * B
+    # active prefix), 36 per moving-frame term (6 or 9 per step), 30 per step
+    # for the renormalisation
+    parts_tri = (36 * 6 + 30) * (B - 1) * stride
     f32 = bench.response_fp32_flops_per_path(nt, n_steps, stride) - parts_tri
     assert f32 % 160 == 0 and 0 < f32 <= 40 * 24 * (B - 1) * stride
     assert (bench.response_fp32_flops_per_path(nt, n_steps, stride, "poly")

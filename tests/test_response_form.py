@@ -395,12 +395,12 @@ SVC_TRI = np.sqrt(0.01) * np.array([[0.0064, 0.0, 0.0], [-0.0036, 0.0004, 0.0], 
 SVC_GEN = SVC_TRI + np.sqrt(0.01) * np.array([[0.0, 1e-4, 2e-6], [0.0, 0.0, -3e-6], [0.0, 0.0, 0.0]])
 
 
-def state_coefs(stride, B, k1, k2, svc):
-    """As state_coef_kernel: row n = b stride + s (m = n - stride) holds
-    C(m) = M^-(m+1) B and G(m) = Q(m) C(m), B[c][k] = svc[k][c]."""
+def state_coefs(stride, k1, k2, svc):
+    """As state_coef_kernel: row s < stride (the step within a block) holds
+    C(s) = M^-(s+1) B and G(s) = Q(s) C(s), B[c][k] = svc[k][c]."""
     Bm = np.asarray(svc, dtype=np.float64).T
     rows = {}
-    for m in range((B - 1) * stride):
+    for m in range(stride):
         kk, q = m + 1.0, float(m)
         minv = np.array([[1.0, -kk * k1, -kk * k2 + kk * (kk + 1.0) * k1 * k1], [0.0, 1.0, -2.0 * kk * k1],
                          [0.0, 0.0, 1.0]])
@@ -408,17 +408,18 @@ def state_coefs(stride, B, k1, k2, svc):
         Q = np.array([[q, h * k1, h * k2 + (q + 1.0) * q * (q - 1.0) / 3.0 * k1 * k1], [0.0, q, 2.0 * h * k1],
                       [0.0, 0.0, q]])
         C = minv @ Bm
-        rows[stride + m] = (C, Q @ C)
+        rows[m] = (C, Q @ C)
     return rows
 
 
-def parts_at_date(y, v, E, k1, k2):
-    """As the kernel's sampling: x_E = M^E y and Z_E = Q(E) y - v."""
-    e1 = 0.5 * E * (E + 1.0)
-    x = (y[0] + E * k1 * y[1] + E * (k2 + (E - 1.0) * k1 * k1) * y[2], y[1] + 2.0 * E * k1 * y[2], y[2])
-    z = (E * y[0] + e1 * k1 * y[1] + (e1 * k2 + (E + 1.0) * E * (E - 1.0) / 3.0 * k1 * k1) * y[2] - v[0],
-         E * y[1] + 2.0 * e1 * k1 * y[2] - v[1], E * y[2] - v[2])
-    return x, z
+def block_end(y, v, z, a, k1, k2):
+    """As the kernel's sampling after a block of a steps: x = M^a y and
+    Z + Q(a) y - v."""
+    ha = 0.5 * a * (a + 1.0)
+    x = (y[0] + a * k1 * y[1] + a * (k2 + (a - 1.0) * k1 * k1) * y[2], y[1] + 2.0 * a * k1 * y[2], y[2])
+    zn = (z[0] + (a * y[0] + ha * k1 * y[1] + (ha * k2 + (a + 1.0) * a * (a - 1.0) / 3.0 * k1 * k1) * y[2] - v[0]),
+          z[1] + (a * y[1] + 2.0 * ha * k1 * y[2] - v[1]), z[2] + (a * y[2] - v[2]))
+    return np.array(x), np.array(zn)
 
 
 class DFW(DF):
@@ -436,53 +437,54 @@ class DFW(DF):
         self.Al = _f32(self.Al + _f32(err + e))
         self.A = s
 
-    def norm(self):
-        """As df_norm."""
+    def renorm(self):
+        """As df_renorm (fast two-sum)."""
         s = _f32(self.A + self.Al)
-        bp = _f32(s - self.A)
-        ap = _f32(s - bp)
-        self.Al = _f32(_f32(self.A - ap) + _f32(self.Al - bp))
+        self.Al = _f32(self.Al - _f32(s - self.A))
         self.A = s
 
 
 def _moving_frame_errors(svc, stride, B, dt, dtau, seed, df):
-    """The parts and their running sums at the dates from the moving frame
-    (FP64 or the kernel's double-FP32) against the FP64 recursion
-    x <- M x + B phi; errors relative to the sum of the magnitudes of the
-    terms of S + U tau + W tau^2 at the date's tenor."""
+    """The parts and their running sums at the dates from the block-anchored
+    moving frame (FP64 or the kernel's double-FP32) against the FP64
+    recursion x <- M x + B phi; errors relative to the sum of the magnitudes
+    of the terms of S + U tau + W tau^2 at the date's tenor."""
     c = dt / dtau
     k1, k2 = c * dtau, c * dtau * dtau
-    rows = state_coefs(stride, B, k1, k2, svc)
+    rows = state_coefs(stride, k1, k2, svc)
     rng = np.random.default_rng(seed)
     phi = rng.normal(size=(B * stride, 3)).astype(np.float32)
     x = np.zeros(3)
     zsum = np.zeros(3)  # sum of the evolved parts
-    y, v = np.zeros(3), np.zeros(3)
-    acc = [[DFW(), DFW()] for _ in range(3)]
+    xm, zm = np.zeros(3), np.zeros(3)  # the kernel's FP64 values between blocks
     errs = []
     for b in range(1, B):
+        y, v = xm.copy(), np.zeros(3)
+        acc = [[DFW(), DFW()] for _ in range(3)]
+        for cc in range(3):  # the re-anchored accumulators: x rounded to an FP32 pair
+            acc[cc][0].A = _f32(xm[cc])
+            acc[cc][0].Al = _f32(xm[cc] - np.float64(acc[cc][0].A))
         for s in range(stride):
             n = b * stride + s
             p = phi[n].astype(np.float64)
             x = np.array([x[0] + k1 * x[1] + k2 * x[2], x[1] + 2.0 * k1 * x[2], x[2]]) + np.asarray(svc).T @ p
             zsum += x
-            C, G = rows[n]
+            C, G = rows[s]
             if df:
                 for cc in range(3):
                     for k in range(3):
                         if C[cc][k] != 0.0:
                             acc[cc][0].add_exact(C[cc][k], phi[n][k])
                             acc[cc][1].add_exact(G[cc][k], phi[n][k])
+                    acc[cc][0].renorm()
+                    acc[cc][1].renorm()
             else:
                 y += C @ p
                 v += G @ p
         if df:
-            for cc in range(3):
-                for q in range(2):
-                    acc[cc][q].norm()
             y = np.array([acc[cc][0].value() for cc in range(3)])
             v = np.array([acc[cc][1].value() for cc in range(3)])
-        xm, zm = parts_at_date(y, v, float(b * stride), k1, k2)
+        xm, zm = block_end(y, v, zm, float(stride), k1, k2)
         tau = dtau * (b + 1)
         for got, want in ((xm, x), (zm, zsum)):
             g = got[0] + tau * (got[1] + tau * got[2])
@@ -493,9 +495,9 @@ def _moving_frame_errors(svc, stride, B, dt, dtau, seed, df):
 
 @pytest.mark.parametrize("svc", [SVC_TRI, SVC_GEN], ids=["degree<=k", "general"])
 def test_moving_frame_parts_equal_the_fp64_recursion(svc):
-    """In FP64 the moving frame's closed forms (M^E, M^-k, Q(a)) reproduce
-    the step recursion and its running sums to FP64 rounding: 1,000 steps of
-    50 per block, 21 dates, dt = 0.01."""
+    """In FP64 the block-anchored moving frame's closed forms (M^a, M^-k,
+    Q(a)) reproduce the step recursion and its running sums to FP64 rounding:
+    1,000 steps of 50 per block, 21 dates, dt = 0.01."""
     assert _moving_frame_errors(svc, 50, 21, 0.01, 0.5, 3, df=False) < 1e-13
 
 
@@ -503,6 +505,8 @@ def test_moving_frame_parts_equal_the_fp64_recursion(svc):
                                                                                     "general"])
 def test_double_fp32_moving_frame_tracks_the_fp64_recursion(svc, seed):
     """The kernel's arithmetic: coefficients as FP32 pairs, exact FP32 normals,
-    df_acc_w terms packed {y, v}, df_norm at each date: within ~1e-12 of the
-    magnitude of the terms (2^-48 per operation over ~3,000 additions)."""
-    assert _moving_frame_errors(svc, 50, 21, 0.01, 0.5, seed, df=True) < 2e-12
+    df_acc_w terms packed {y, v}, df_renorm after each part's terms of a step,
+    the anchor rounded to an FP32 pair: within ~1e-13 of the magnitude of the
+    terms (2^-48 of the accumulator per addition over a block's ~150
+    additions; FP64 across blocks)."""
+    assert _moving_frame_errors(svc, 50, 21, 0.01, 0.5, seed, df=True) < 3e-13
