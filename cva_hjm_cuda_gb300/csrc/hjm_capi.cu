@@ -84,11 +84,11 @@ struct hjm_ctx {
     DevBuf partials, sums, result, estore, sel, hist, ext, ext_raw, wide, scratch, ck_h, ck_a, resp, vresp;
     // the response table in resp holds the run shape of resp_key; resp_used
     // is recorded after the last kernel that reads it
-    struct RespKey {  // the response table in resp (and, Euler, the parts' coefficients)
+    struct RespKey {  // the response table in resp, with the parts' frame coefficients
         bool valid = false;
         int nt = 0, stride = 0, B = 0, scheme = 0;
         double c = 0, dtau = 0;
-        double svc[kFactors][3] = {};
+        PartsFrame frame = {};
     } resp_key;
     struct VrespKey {  // the volatility-table response table in vresp
         bool valid = false;
@@ -714,10 +714,10 @@ static hjm_status ensure_vol_response_table(hjm_ctx* ctx, const RunShape& sh, do
 
 // The response table of the run shape and scheme, on the stream: recomputed
 // only when they changed, after the kernels of earlier valuations that read
-// it.  Euler: the source -2 c dtau^2 W at the last tenor (fill_params' k2),
-// and the moving-frame coefficients of the parts from P (k1, k2, svc);
-// predictor-corrector (P null): the sources of fill_pc (wL1 at L-1; wL, gL at L).
-static hjm_status ensure_response_table(hjm_ctx* ctx, const RunShape& sh, double dt, const PathParams<double>* P,
+// it.  Euler: the source -2 c dtau^2 W at the last tenor (fill_params' k2);
+// predictor-corrector: the sources of fill_pc (wL1 at L-1; wL, gL at L);
+// then the moving-frame coefficients of the scheme's parts step f.
+static hjm_status ensure_response_table(hjm_ctx* ctx, const RunShape& sh, double dt, const PartsFrame& f,
                                         cudaStream_t s)
 {
     const double dtau = ctx->dtau;
@@ -734,9 +734,8 @@ static hjm_status ensure_response_table(hjm_ctx* ctx, const RunShape& sh, double
     }
     hjm_ctx::RespKey& k = ctx->resp_key;
     if (!ctx->resp_used) HJM_CUDA(ctx, cudaEventCreateWithFlags(&ctx->resp_used, cudaEventDisableTiming));
-    const bool same_svc = !P || std::memcmp(k.svc, P->svc, sizeof(k.svc)) == 0;
     if (k.valid && k.nt == ctx->nt && k.stride == sh.stride && k.B == sh.B && k.c == c && k.dtau == dtau &&
-        k.scheme == ctx->scheme && same_svc)
+        k.scheme == ctx->scheme && std::memcmp(&k.frame, &f, sizeof(f)) == 0)
         return HJM_OK;
     k.valid = false;
     const size_t bytes = sizeof(float4) * response_table_elems(sh.stride, sh.B);
@@ -747,12 +746,9 @@ static hjm_status ensure_response_table(hjm_ctx* ctx, const RunShape& sh, double
     HJM_CUDA(ctx, cudaMemsetAsync(ctx->resp.p, 0, bytes, s));  // entries the kernel reads as exact zeros
     HJM_CUDA(ctx, launch_response_table(ctx->nt, c, sh.stride, sh.B, pc, w0, w1, w2, (float4*)ctx->resp.p, s));
     HJM_CUDA(ctx, launch_response_active(sh.stride, sh.B, (float4*)ctx->resp.p, s));
-    ctx->stat_launches += 2;
-    if (P) {
-        HJM_CUDA(ctx, launch_state_coefs(*P, (float4*)ctx->resp.p, s));
-        ctx->stat_launches += 1;
-        std::memcpy(k.svc, P->svc, sizeof(k.svc));
-    }
+    HJM_CUDA(ctx, launch_state_coefs(f, sh.stride, sh.B, (float4*)ctx->resp.p, s));
+    ctx->stat_launches += 3;
+    std::memcpy(&k.frame, &f, sizeof(f));
     k.nt = ctx->nt;
     k.stride = sh.stride;
     k.B = sh.B;
@@ -828,7 +824,7 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
                                                  s));
         } else {
             if (resp) {
-                st = ensure_response_table(ctx, sh, dt, nullptr, s);
+                st = ensure_response_table(ctx, sh, dt, pc_parts_frame(Q), s);
                 if (st != HJM_OK) return st;
             }
             HJM_CUDA(ctx, launch_path_pc(ctx->nt, Q, use_poly_path(ctx), resp ? (const float4*)ctx->resp.p : nullptr,
@@ -855,7 +851,7 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
                                                  s));
         } else {
             if (resp) {
-                st = ensure_response_table(ctx, sh, dt, &P, s);
+                st = ensure_response_table(ctx, sh, dt, euler_parts_frame(P), s);
                 if (st != HJM_OK) return st;
             }
             HJM_CUDA(ctx, launch_path_fp64(ctx->nt, P, use_poly_path(ctx),

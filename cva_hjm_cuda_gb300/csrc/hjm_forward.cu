@@ -289,10 +289,7 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
     double* z_s = red_s + 2 * (kCta / 32);
 #pragma unroll
     for (int c = 0; c < 3; ++c) z_s[c * kCta + tid] = 0.0;
-    // M^a and Q(a) for a block of a = stride steps (uniform)
-    const double a = (double)P.stride, k1 = P.k1, k2 = P.k2, k1s = P.k1 * P.k1, ha = 0.5 * a * (a + 1.0);
-    const double m01 = a * k1, m02 = a * fma(a - 1.0, k1s, k2), m12 = 2.0 * a * k1;
-    const double q01 = ha * k1, q02 = fma(ha, k2, (a + 1.0) * a * (a - 1.0) / 3.0 * k1s), q12 = 2.0 * ha * k1;
+    const BlockFrame F(P.k1, P.k2, 2.0 * P.k1, (double)P.stride);  // the Euler step on a quadratic
 
     // price date i from the sampled numeraire (x_i, D_i); for i >= 2 the
     // block just ended: x = M^a y, Z += Q(a) y - v, then y re-anchored on x
@@ -304,28 +301,7 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
             const float2 h = select_reg<kRespSlots, float2>(A, B - i), l = select_reg<kRespSlots, float2>(Al, B - i);
             hc = widen_f32(h.x) + widen_f32(l.x);
             hcs = widen_f32(h.y) + widen_f32(l.y);
-            double y[3], v[3];
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                y[c] = widen_f32(Y[c].x) + widen_f32(Yl[c].x);
-                v[c] = widen_f32(Y[c].y) + widen_f32(Yl[c].y);
-            }
-            W = y[2];
-            U = fma(m12, y[2], y[1]);
-            S = fma(m01, y[1], fma(m02, y[2], y[0]));
-            ZW = z_s[2 * kCta + tid] + fma(a, y[2], -v[2]);
-            ZU = z_s[kCta + tid] + fma(a, y[1], fma(q12, y[2], -v[1]));
-            ZS = z_s[tid] + fma(a, y[0], fma(q01, y[1], fma(q02, y[2], -v[0])));
-            z_s[tid] = ZS;
-            z_s[kCta + tid] = ZU;
-            z_s[2 * kCta + tid] = ZW;
-            const double x3[3] = {S, U, W};
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                const float xh = __double2float_rn(x3[c]);
-                Y[c] = make_float2(xh, 0.0f);
-                Yl[c] = make_float2(__double2float_rn(x3[c] - (double)xh), 0.0f);
-            }
+            frame_block_end(Y, Yl, F, z_s + tid, kCta, S, U, W, ZS, ZU, ZW);
         }
         const double x = P.psamp[i] + (fma(tau, fma(tau, W, U), S) + hc);
         const double acc = fma(tau, fma(tau, ZW, ZU), ZS) + hcs;
@@ -365,23 +341,7 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
                            wh2, wl2, nwh2);
             });
             // y += C(s) phi, v += G(s) phi (factor k of degree <= k loads parts c <= k only)
-            const float4* cr = coef + (size_t)s * kStateRow;
-            float4 q[kStateRow];
-#pragma unroll
-            for (int t = 0; t < kStateRow; ++t)
-                if (!TRI || t / 3 <= t % 3) q[t] = __ldg(cr + t);
-#pragma unroll
-            for (int t = 0; t < kStateRow; ++t) {
-                const int c = t / 3, k = t % 3;
-                if (TRI && c > k) continue;
-                const float2 kh = make_float2(q[t].x, q[t].y), kl = make_float2(q[t].z, q[t].w);
-                if constexpr (EXT)
-                    df_acc(Y[c], Yl[c], kh, kl, make_float2(ph[k], ph[k]), make_float2(pl[k], pl[k]),
-                           make_float2(-ph[k], -ph[k]));
-                else
-                    df_acc_w(Y[c], Yl[c], kh, kl, make_float2(ph[k], ph[k]), make_float2(-ph[k], -ph[k]));
-                if (k == 2) df_renorm(Y[c], Yl[c]);  // the part's last term of the step
-            }
+            frame_step<EXT, TRI>(Y, Yl, coef + (size_t)s * kStateRow, ph, pl);
         }
         sample(b + 1);
     }
@@ -500,30 +460,27 @@ __global__ void __launch_bounds__(1024) response_active_kernel(int rows, const f
     }
 }
 
-// The moving-frame coefficients of the Euler response form's parts (the
-// frame, M^-k and Q(a) are stated with kStateRow): row s < stride (the step
-// within a block), entry 3 c + k = {C hi, G hi, C lo, G lo} of C(s) =
-// M^-(s+1) B and G(s) = Q(s) C(s), B[c][k] = svc[k][c]; FP64, each split into
-// the nearest float and the float nearest the rest.
-struct StateCoefArgs {
-    double k1, k2;
-    double svc[kFactors][3];
-};
-
-__global__ void state_coef_kernel(StateCoefArgs a, int stride, float4* __restrict__ coef)
+// The moving-frame coefficients of the response forms' parts (the frame,
+// M^-k and Q(a) are stated with kStateRow): row s < stride (the step within a
+// block), entry 3 c + k = {C hi, G hi, C lo, G lo} of C(s) = M^-(s+1) B and
+// G(s) = Q(s) C(s); FP64, each split into the nearest float and the float
+// nearest the rest.
+__global__ void state_coef_kernel(PartsFrame f, int stride, float4* __restrict__ coef)
 {
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (int64_t)stride * kStateRow) return;
     const int64_t m = idx / kStateRow;
     const int c = (int)(idx % kStateRow) / 3, k = (int)(idx % kStateRow) % 3;
-    const double kk = (double)(m + 1), q = (double)m, k1 = a.k1, k2 = a.k2;
-    const double minv[3][3] = {{1.0, -kk * k1, -kk * k2 + kk * (kk + 1.0) * k1 * k1}, {0.0, 1.0, -2.0 * kk * k1},
+    const double kk = (double)(m + 1), q = (double)m, nn = f.n01 * f.n12;
+    const double minv[3][3] = {{1.0, -kk * f.n01, -kk * f.n02 + 0.5 * kk * (kk + 1.0) * nn},
+                               {0.0, 1.0, -kk * f.n12},
                                {0.0, 0.0, 1.0}};
     const double h = 0.5 * q * (q + 1.0);
-    const double Q[3][3] = {{q, h * k1, h * k2 + (q + 1.0) * q * (q - 1.0) / 3.0 * k1 * k1}, {0.0, q, 2.0 * h * k1},
+    const double Q[3][3] = {{q, h * f.n01, h * f.n02 + (q + 1.0) * q * (q - 1.0) / 6.0 * nn},
+                            {0.0, q, h * f.n12},
                             {0.0, 0.0, q}};
     double C[3];  // column k of C(m)
-    for (int r = 0; r < 3; ++r) C[r] = minv[r][0] * a.svc[k][0] + minv[r][1] * a.svc[k][1] + minv[r][2] * a.svc[k][2];
+    for (int r = 0; r < 3; ++r) C[r] = minv[r][0] * f.bm[0][k] + minv[r][1] * f.bm[1][k] + minv[r][2] * f.bm[2][k];
     const double cv = C[c], gv = Q[c][0] * C[0] + Q[c][1] * C[1] + Q[c][2] * C[2];
     const float ch = __double2float_rn(cv), gh = __double2float_rn(gv);
     coef[(size_t)m * kStateRow + 3 * c + k] =
@@ -1139,18 +1096,13 @@ cudaError_t launch_response_active(int stride, int n_blocks, float4* resp, cudaS
     return cudaGetLastError();
 }
 
-cudaError_t launch_state_coefs(const PathParams<double>& P, float4* resp, cudaStream_t s)
+cudaError_t launch_state_coefs(const PartsFrame& f, int stride, int n_blocks, float4* resp, cudaStream_t s)
 {
-    if (P.n_blocks < 2 || P.n_blocks > kRespDates || P.stride < 1) return cudaErrorInvalidValue;
-    StateCoefArgs a;
-    a.k1 = P.k1;
-    a.k2 = P.k2;
-    for (int k = 0; k < kFactors; ++k)
-        for (int d = 0; d < 3; ++d) a.svc[k][d] = P.svc[k][d];
-    const int64_t total = (int64_t)P.stride * kStateRow;
+    if (n_blocks < 2 || n_blocks > kRespDates || stride < 1) return cudaErrorInvalidValue;
+    const int64_t total = (int64_t)stride * kStateRow;
     const int threads = 256;
     state_coef_kernel<<<(unsigned)((total + threads - 1) / threads), threads, 0, s>>>(
-        a, P.stride, resp + resp_coef_offset(P.stride, P.n_blocks));
+        f, stride, resp + resp_coef_offset(stride, n_blocks));
     return cudaGetLastError();
 }
 

@@ -71,10 +71,17 @@ cudaError_t launch_response_table(int nt, double c, int stride, int n_blocks, bo
 // The active prefix of each row of the response table in resp (after the
 // table and the coefficient rows), from the table's values
 cudaError_t launch_response_active(int stride, int n_blocks, float4* resp, cudaStream_t s);
-// The Euler response form's moving-frame coefficients of S, U, W from P.k1,
-// P.k2, P.svc, P.stride and P.n_blocks, into the rows after the response
+// The moving frame of the response forms' polynomial parts: the step
+// x <- M x + B phi on x = (S, U, W), M = I + N with N's entries n01 (S from
+// U), n02 (S from W), n12 (U from W), and bm[c][k] = B, the loading of part c
+// on factor k.
+struct PartsFrame {
+    double n01, n02, n12;
+    double bm[3][3];
+};
+// Its coefficients (one block's rows), into the rows after the response
 // table in resp (whose size response_table_elems counts)
-cudaError_t launch_state_coefs(const PathParams<double>& P, float4* resp, cudaStream_t s);
+cudaError_t launch_state_coefs(const PartsFrame& f, int stride, int n_blocks, float4* resp, cudaStream_t s);
 cudaError_t launch_path_mixed(int nt, const MixedParams& M, bool poly, const double* ext, double* partials,
                               float* estore, cudaStream_t s);
 void pack_mixed_params(int nt, const PathParams<float>& P, MixedParams& M);
@@ -111,6 +118,31 @@ struct PcParams {
     T k1, k2p, k1x2;       // c dtau, (c + c^2) dtau^2, 2 c dtau
     T wL1, wL, gL;         // sources: -c^2 dtau^2 W at L-1; -(2c + c^2) dtau^2 W - c dtau^2 gamma at L
 };
+
+// The frames of the two schemes' polynomial steps on (S, U, W)
+inline PartsFrame euler_parts_frame(const PathParams<double>& P)
+{
+    PartsFrame f{};
+    f.n01 = P.k1;
+    f.n02 = P.k2;
+    f.n12 = 2.0 * P.k1;
+    for (int k = 0; k < kFactors; ++k)
+        for (int c = 0; c < 3; ++c) f.bm[c][k] = P.svc[k][c];
+    return f;
+}
+inline PartsFrame pc_parts_frame(const PcParams<double>& Q)
+{
+    PartsFrame f{};
+    f.n01 = Q.k1;
+    f.n02 = Q.k2p;
+    f.n12 = Q.k1x2;
+    for (int k = 0; k < kFactors; ++k) {
+        f.bm[0][k] = Q.aS[k];
+        f.bm[1][k] = Q.aU[k];
+        f.bm[2][k] = Q.aW[k];
+    }
+    return f;
+}
 // resp (FP64 only): the predictor-corrector response table (the response
 // form, polynomial volatility, at most response_max_dates() dates) or null
 cudaError_t launch_path_pc(int nt, const PcParams<double>& Q, bool poly, const float4* resp, const double* ext,

@@ -157,10 +157,11 @@ __global__ void __launch_bounds__(kPcCta, 4)
 
 // Response form of the FP64 predictor-corrector path (polynomial volatility,
 // at most kRespDates dates), as path_kernel_fp64_resp in hjm_forward.cu: the
-// polynomial parts in FP64 with the N-projected loadings,
+// polynomial parts, whose step with the N-projected loadings is
 //     S' = S + c dtau U + (c + c^2) dtau^2 W + aS.phi,  U' = U + 2 c dtau W + aU.phi,
 //     W' = W + aW.phi   (old values on the right),
-// and the remainder, driven at L-1 and L by W and by the step's curvature
+// as double-FP32 sums in the block's moving frame of that step (frame_step,
+// frame_block_end in hjm_resp.cuh), and the remainder, driven at L-1 and L by W and by the step's curvature
 // noise, as double-FP32 sums of the predictor-corrector response table (the
 // coefficient of the old W per date slot and lag; response_table_kernel with
 // pc = 1) over the active prefix of slots.  TRI: factor k of degree <= k
@@ -186,8 +187,16 @@ __global__ void __launch_bounds__(kPcCta, 6)
     float2 A[kRespSlots], Al[kRespSlots];  // {remainder at tenor j, its running sum}, slot B - j, hi + lo
 #pragma unroll
     for (int r = 0; r < kRespSlots; ++r) A[r] = Al[r] = make_float2(0.0f, 0.0f);
-    double S = 0.0, U = 0.0, W = 0.0;
-    double sS = 0.0, sU = 0.0, sW = 0.0;  // running sums before the current step (sampling adds it)
+    // the parts S, U, W in the block's moving frame, {y_c, v_c} as hi + lo
+    // pairs, and their FP64 running sums between blocks (shared memory)
+    float2 Y[3], Yl[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) Y[c] = Yl[c] = make_float2(0.0f, 0.0f);
+    double* z_s = red_s + 2 * (kPcCta / 32);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) z_s[c * kPcCta + tid] = 0.0;
+    const BlockFrame F(Q.k1, Q.k2p, Q.k1x2, (double)P.stride);  // the two-stage step on a quadratic
+    const float4* coef = resp + resp_coef_offset(P.stride, B);
     // the active prefix of each row, after the table's response and coefficient rows
     const int* nact = reinterpret_cast<const int*>(resp + resp_nact_offset(P.stride, B));
 
@@ -195,8 +204,10 @@ __global__ void __launch_bounds__(kPcCta, 6)
         const double tau = P.tau[i];
         const float2 h = select_reg<kRespSlots, float2>(A, B - i), l = select_reg<kRespSlots, float2>(Al, B - i);
         const double hc = widen_f32(h.x) + widen_f32(l.x), hcs = widen_f32(h.y) + widen_f32(l.y);
+        double S = 0.0, U = 0.0, W = 0.0, ZS = 0.0, ZU = 0.0, ZW = 0.0;
+        if (i >= 2) frame_block_end(Y, Yl, F, z_s + tid, kPcCta, S, U, W, ZS, ZU, ZW);
         const double x = P.psamp[i] + (fma(tau, fma(tau, W, U), S) + hc);
-        const double acc = fma(tau, fma(tau, sW + W, sU + U), sS + S) + hcs;
+        const double acc = fma(tau, fma(tau, ZW, ZU), ZS) + hcs;
         const double D = exp(-(P.psum[i] + acc) * P.dt);
         const double Lb = P.m * (exp(x / P.m) - 1.0);
         cf_s[i * kPcCta + tid] = D * (P.payA[i] * Lb - P.payB[i]);
@@ -207,13 +218,21 @@ __global__ void __launch_bounds__(kPcCta, 6)
         const float4* row = resp + (size_t)b * P.stride * kRespRow;
         for (int s = 0; s < P.stride; ++s) {
             const int n = b * P.stride + s;
-            double phi0, phi1, phi2;
-            draw_phi<double, EXT>(ext, gpath, active ? lp : 0, P.n_paths, n, P.rk0, P.rk1, phi0, phi1, phi2);
+            float ph[3], pl[3];  // the normals as hi + lo (lo = 0 for the generator's FP32 draws)
+            if constexpr (EXT) {
+                double d0, d1, d2;
+                draw_phi<double, true>(ext, gpath, active ? lp : 0, P.n_paths, n, P.rk0, P.rk1, d0, d1, d2);
+                split_f64(d0, ph[0], pl[0]);
+                split_f64(d1, ph[1], pl[1]);
+                split_f64(d2, ph[2], pl[2]);
+            } else {
+                draw_phi<float, false>(ext, gpath, lp, P.n_paths, n, P.rk0, P.rk1, ph[0], ph[1], ph[2]);
+            }
             const int n_act = __ldg(nact + n);  // uniform: the row's active prefix
             const float4* rr = row + (size_t)s * kRespRow;
-            float wh, wl;
-            split_f64(W, wh, wl);
-            const float2 wh2 = make_float2(wh, wh), wl2 = make_float2(wl, wl), nwh2 = make_float2(-wh, -wh);
+            // the remainder's sources read W before this step's update
+            const float2 wh2 = make_float2(Y[2].x, Y[2].x), wl2 = make_float2(Yl[2].x, Yl[2].x);
+            const float2 nwh2 = make_float2(-Y[2].x, -Y[2].x);
             resp_groups(n_act, [&](auto gc) {
                 constexpr int G = decltype(gc)::value;
                 float4 k[4];
@@ -224,20 +243,7 @@ __global__ void __launch_bounds__(kPcCta, 6)
                     df_acc(A[4 * G + u], Al[4 * G + u], make_float2(k[u].x, k[u].y), make_float2(k[u].z, k[u].w),
                            wh2, wl2, nwh2);
             });
-            sS += S;
-            sU += U;
-            sW += W;
-            double Wn = fma(Q.aW[2], phi2, W);
-            double Sn = fma(Q.aS[0], phi0, fma(Q.k2p, W, fma(Q.k1, U, S)));
-            Sn = fma(Q.aS[2], phi2, fma(Q.aS[1], phi1, Sn));
-            double Un = fma(Q.aU[2], phi2, fma(Q.aU[1], phi1, fma(Q.k1x2, W, U)));
-            if constexpr (!TRI) {
-                Un = fma(Q.aU[0], phi0, Un);
-                Wn = fma(Q.aW[1], phi1, fma(Q.aW[0], phi0, Wn));
-            }
-            S = Sn;
-            U = Un;
-            W = Wn;
+            frame_step<EXT, TRI>(Y, Yl, coef + (size_t)s * kStateRow, ph, pl);
         }
         sample(b + 1);
     }
@@ -248,7 +254,8 @@ template <int NT, bool EXT, bool TRI>
 static cudaError_t launch_pc_resp_t(const PcParams<double>& Q, const float4* resp, const double* ext,
                                     double* partials, double* estore, cudaStream_t s)
 {
-    const size_t smem = ((size_t)Q.P.n_blocks + 2) * kPcCta * 8 + 2 * (kPcCta / 32) * 8;
+    // cf_s [B+2][kCta], red_s, the parts' running sums [3][kCta]
+    const size_t smem = ((size_t)Q.P.n_blocks + 2) * kPcCta * 8 + 2 * (kPcCta / 32) * 8 + 3 * kPcCta * 8;
     auto k = path_kernel_pc_resp<NT, EXT, TRI>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

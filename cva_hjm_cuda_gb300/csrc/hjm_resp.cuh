@@ -137,36 +137,108 @@ __device__ __forceinline__ void df_renorm(float2& A, float2& Al)
     A = sum;
 }
 
-// Polynomial parts in a moving frame (FP64 response form, Euler).  The Euler
-// step maps the parts x = (S, U, W) of h's quadratic to M x + B phi with
-// M = I + N, N = [[0, k1, k2], [0, 0, 2 k1], [0, 0, 0]] (the upwind
-// difference of a quadratic, which the scheme takes exactly) and B[c][k] =
-// svc[k][c].  M is unipotent (N^3 = 0), so within a block, anchored at its
-// first step (y_0 = x at the block's start), y_s = M^-s x moves by the noise
-// alone,
+// Polynomial parts in a moving frame (the FP64 response forms of both
+// schemes).  A step maps the parts x = (S, U, W) of h's quadratic to
+// M x + B phi with M = I + N, N = [[0, n01, n02], [0, 0, n12], [0, 0, 0]] (the
+// scheme's difference operator on a quadratic, which it takes exactly:
+// Euler n01 = c dtau, n02 = c dtau^2, n12 = 2 c dtau; predictor-corrector
+// n01 = c dtau, n02 = (c + c^2) dtau^2, n12 = 2 c dtau) and B[c][k] the
+// loading of part c on factor k.  M is unipotent (N^3 = 0), so within a
+// block, anchored at its first step (y_0 = x at the block's start), y_s =
+// M^-s x moves by the noise alone,
 //     y_{s+1} = y_s + C(s) phi_s,                  C(s) = M^-(s+1) B,
-// and at the block's end (s = stride)
-//     x_end = M^stride y_stride,
-//     sum_{s'=1..stride} x_s' = Q(stride) y_stride - v,   v = sum_s G(s) phi_s,
-// with Q(a) = sum_{e=1..a} M^e, G(s) = Q(s) C(s), and M^a, M^-k and Q(a)
-// polynomials of degree <= 3 in a, k:
-//     M^a   = [[1, a k1, a k2 + a(a-1) k1^2], [0, 1, 2 a k1], [0, 0, 1]],
-//     M^-k  = [[1, -k k1, -k k2 + k(k+1) k1^2], [0, 1, -2 k k1], [0, 0, 1]],
-//     Q(a)  = [[a, a(a+1)/2 k1, a(a+1)/2 k2 + (a+1)a(a-1)/3 k1^2],
-//              [0, a, a(a+1) k1], [0, 0, a]].
-// Per step the kernel adds C(s) phi to y and G(s) phi to v (6 terms for
+// and at the block's end (s = a = stride)
+//     x_end = M^a y_a,
+//     sum_{s'=1..a} x_s' = Q(a) y_a - v,            v = sum_s G(s) phi_s,
+// with Q(a) = sum_{e=1..a} M^e, G(s) = Q(s) C(s), and (N^2 has the one entry
+// n01 n12 at (S, W))
+//     M^a   = I + a N + a(a-1)/2 N^2,
+//     M^-k  = I - k N + k(k+1)/2 N^2,
+//     Q(a)  = a I + a(a+1)/2 N + (a+1)a(a-1)/6 N^2.
+// Per step the kernels add C(s) phi to y and G(s) phi to v (6 terms for
 // factors of degree <= k, 9 in general), packed {y, v} per part in
-// double-FP32 on the FP32 pipe; at each block's end (a sampling date) it
-// widens them, forms x_end and adds the block's sum to the running sums Z in
-// FP64, and re-anchors y on x_end (rounded to FP32 pairs) with v = 0; the
-// pairs are renormalised after every step (df_renorm).  The
-// coefficients are the same in every block: row s (< stride) of the
-// coefficient table holds kStateRow float4 {C hi, G hi, C lo, G lo}, entry
-// 3 c + k for part c and factor k (state_coef_kernel).  W = y_W in every
-// frame, so the remainder's source reads its accumulator directly.  The
-// rounding: 2^-48 of the accumulator per double-FP32 addition over one
-// block's ~150 additions (~5e-14 of the parts' terms), the rest FP64.
+// double-FP32 on the FP32 pipe, and renormalise the pairs (df_renorm); at
+// each block's end (a sampling date) they widen them, form x_end, add the
+// block's sum to the running sums Z in FP64, and re-anchor y on x_end
+// (rounded to FP32 pairs) with v = 0 (frame_block_end).  The coefficients
+// are the same in every block: row s (< stride) of the coefficient table
+// holds kStateRow float4 {C hi, G hi, C lo, G lo}, entry 3 c + k for part c
+// and factor k (state_coef_kernel).  W = y_W in every frame, so the
+// remainder's source reads its accumulator directly.  The rounding: 2^-48 of
+// the accumulator per double-FP32 addition over one block's ~150 additions
+// (~5e-14 of the parts' terms), the rest FP64.
 constexpr int kStateRow = 9;
+
+// M^a and Q(a) of a block of a steps (uniform across the CTA).
+struct BlockFrame {
+    double a, m01, m02, m12, q01, q02, q12;
+    __device__ BlockFrame(double n01, double n02, double n12, double steps)
+    {
+        a = steps;
+        const double ha = 0.5 * a * (a + 1.0), nn = n01 * n12;
+        m01 = a * n01;
+        m02 = fma(0.5 * a * (a - 1.0), nn, a * n02);
+        m12 = a * n12;
+        q01 = ha * n01;
+        q02 = fma((a + 1.0) * a * (a - 1.0) / 6.0, nn, ha * n02);
+        q12 = ha * n12;
+    }
+};
+
+// One step of the parts: y += C(s) phi, v += G(s) phi from the coefficient
+// row cr, then the pairs renormalised.  ph, pl: the normals as hi + lo (pl
+// unused for FP32 draws, EXT = false).
+template <bool EXT, bool TRI>
+__device__ __forceinline__ void frame_step(float2 (&Y)[3], float2 (&Yl)[3], const float4* __restrict__ cr,
+                                           const float (&ph)[3], const float (&pl)[3])
+{
+    float4 q[kStateRow];
+#pragma unroll
+    for (int t = 0; t < kStateRow; ++t)
+        if (!TRI || t / 3 <= t % 3) q[t] = __ldg(cr + t);
+#pragma unroll
+    for (int t = 0; t < kStateRow; ++t) {
+        const int c = t / 3, k = t % 3;
+        if (TRI && c > k) continue;
+        const float2 kh = make_float2(q[t].x, q[t].y), kl = make_float2(q[t].z, q[t].w);
+        if constexpr (EXT)
+            df_acc(Y[c], Yl[c], kh, kl, make_float2(ph[k], ph[k]), make_float2(pl[k], pl[k]),
+                   make_float2(-ph[k], -ph[k]));
+        else
+            df_acc_w(Y[c], Yl[c], kh, kl, make_float2(ph[k], ph[k]), make_float2(-ph[k], -ph[k]));
+        if (k == 2) df_renorm(Y[c], Yl[c]);  // the part's last term of the step
+    }
+}
+
+// The end of a block: x = M^a y (S, U, W out), Z += Q(a) y - v (z[c *
+// stride_z] in shared memory, out as ZS, ZU, ZW), then y re-anchored on x.
+__device__ __forceinline__ void frame_block_end(float2 (&Y)[3], float2 (&Yl)[3], const BlockFrame& F, double* z,
+                                                int stride_z, double& S, double& U, double& W, double& ZS,
+                                                double& ZU, double& ZW)
+{
+    double y[3], v[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        y[c] = (double)Y[c].x + (double)Yl[c].x;
+        v[c] = (double)Y[c].y + (double)Yl[c].y;
+    }
+    W = y[2];
+    U = fma(F.m12, y[2], y[1]);
+    S = fma(F.m01, y[1], fma(F.m02, y[2], y[0]));
+    ZW = z[2 * stride_z] + fma(F.a, y[2], -v[2]);
+    ZU = z[stride_z] + fma(F.a, y[1], fma(F.q12, y[2], -v[1]));
+    ZS = z[0] + fma(F.a, y[0], fma(F.q01, y[1], fma(F.q02, y[2], -v[0])));
+    z[0] = ZS;
+    z[stride_z] = ZU;
+    z[2 * stride_z] = ZW;
+    const double x3[3] = {S, U, W};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float xh = __double2float_rn(x3[c]);
+        Y[c] = make_float2(xh, 0.0f);
+        Yl[c] = make_float2(__double2float_rn(x3[c] - (double)xh), 0.0f);
+    }
+}
 
 // Offsets (in float4) within the Euler or predictor-corrector response
 // table buffer: the response rows [B stride][kRespRow], the coefficient rows

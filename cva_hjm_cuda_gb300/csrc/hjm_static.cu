@@ -304,7 +304,7 @@ hjm_status hjm_run_static(void* cuda_stream, int32_t n_tenor, double dtau, const
             STATIC_CUDA(cudaMemsetAsync(table, 0, sizeof(float4) * response_table_elems((int)stride, B), s));
             STATIC_CUDA(launch_response_table(n_tenor, c, (int)stride, B, false, 0.0, -2.0 * P.k2, 0.0, table, s));
             STATIC_CUDA(launch_response_active((int)stride, B, table, s));
-            STATIC_CUDA(launch_state_coefs(P, table, s));
+            STATIC_CUDA(launch_state_coefs(euler_parts_frame(P), (int)stride, B, table, s));
             STATIC_CUDA(launch_path_fp64(n_tenor, P, true, table, nullptr, partials, nullptr, s));
         } else if (B >= 2 && B <= response_max_dates() && entries <= kStaticRespEntries) {
             // the response form: its table (zero outside the live entries) into the static array
