@@ -254,7 +254,9 @@ __host__ __device__ inline size_t resp_smem_bytes_parts(int n_blocks)
     return resp_smem_bytes(n_blocks) + 3 * kFp64Cta * 8;
 }
 
-template <int NT, bool EXT, bool TRI>
+// SC: the frame's coefficient rows staged in shared memory (stride at most
+// kFrameSmemRows), else read through L1.
+template <int NT, bool EXT, bool TRI, bool SC>
 __global__ void __launch_bounds__(kFp64Cta, 6)
     path_kernel_fp64_resp(const __grid_constant__ PathParams<double> P, const float4* __restrict__ resp,
                           const double* __restrict__ ext, double* __restrict__ partials,
@@ -283,7 +285,14 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
     float2 Y[3], Yl[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) Y[c] = Yl[c] = make_float2(0.0f, 0.0f);
+    // the frame's coefficient rows (one block's), staged in shared memory for SC
     const float4* coef = resp + resp_coef_offset(P.stride, B);
+    if constexpr (SC) {
+        float4* c_s = reinterpret_cast<float4*>(red_s + 2 * (kCta / 32) + 3 * kCta);
+        for (int i = tid; i < P.stride * kStateRow; i += kCta) c_s[i] = coef[i];
+        __syncthreads();
+        coef = c_s;
+    }
     const int* nact = reinterpret_cast<const int*>(resp + resp_nact_offset(P.stride, B));
     // the running sums Z of the parts over the evolved steps, FP64, between blocks
     double* z_s = red_s + 2 * (kCta / 32);
@@ -341,7 +350,7 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
                            wh2, wl2, nwh2);
             });
             // y += C(s) phi, v += G(s) phi (factor k of degree <= k loads parts c <= k only)
-            frame_step<EXT, TRI>(Y, Yl, coef + (size_t)s * kStateRow, ph, pl);
+            frame_step<EXT, TRI, SC>(Y, Yl, coef + (size_t)s * kStateRow, ph, pl);
         }
         sample(b + 1);
     }
@@ -1005,8 +1014,9 @@ template <int NT, bool EXT, bool TRI>
 static cudaError_t launch_fp64_resp_t(const PathParams<double>& P, const float4* resp, const double* ext,
                                       double* partials, double* estore, cudaStream_t s)
 {
-    const size_t smem = resp_smem_bytes_parts(P.n_blocks);
-    auto k = path_kernel_fp64_resp<NT, EXT, TRI>;
+    const bool sc = P.stride <= kFrameSmemRows;
+    const size_t smem = resp_smem_bytes_parts(P.n_blocks) + (sc ? (size_t)P.stride * kStateRow * 16 : 0);
+    auto k = sc ? path_kernel_fp64_resp<NT, EXT, TRI, true> : path_kernel_fp64_resp<NT, EXT, TRI, false>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const int64_t grid = (P.n_paths + kFp64Cta - 1) / kFp64Cta;

@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(kPcCta, 4)
 // coefficient of the old W per date slot and lag; response_table_kernel with
 // pc = 1) over the active prefix of slots.  TRI: factor k of degree <= k
 // (aU[0] = aW[0] = aW[1] = 0).
-template <int NT, bool EXT, bool TRI>
+template <int NT, bool EXT, bool TRI, bool SC>
 __global__ void __launch_bounds__(kPcCta, 6)
     path_kernel_pc_resp(const __grid_constant__ PcParams<double> Q, const float4* __restrict__ resp,
                         const double* __restrict__ ext, double* __restrict__ partials, double* __restrict__ estore)
@@ -196,7 +196,14 @@ __global__ void __launch_bounds__(kPcCta, 6)
 #pragma unroll
     for (int c = 0; c < 3; ++c) z_s[c * kPcCta + tid] = 0.0;
     const BlockFrame F(Q.k1, Q.k2p, Q.k1x2, (double)P.stride);  // the two-stage step on a quadratic
+    // the frame's coefficient rows (one block's), staged in shared memory for SC
     const float4* coef = resp + resp_coef_offset(P.stride, B);
+    if constexpr (SC) {
+        float4* c_s = reinterpret_cast<float4*>(z_s + 3 * kPcCta);
+        for (int i = tid; i < P.stride * kStateRow; i += kPcCta) c_s[i] = coef[i];
+        __syncthreads();
+        coef = c_s;
+    }
     // the active prefix of each row, after the table's response and coefficient rows
     const int* nact = reinterpret_cast<const int*>(resp + resp_nact_offset(P.stride, B));
 
@@ -243,7 +250,7 @@ __global__ void __launch_bounds__(kPcCta, 6)
                     df_acc(A[4 * G + u], Al[4 * G + u], make_float2(k[u].x, k[u].y), make_float2(k[u].z, k[u].w),
                            wh2, wl2, nwh2);
             });
-            frame_step<EXT, TRI>(Y, Yl, coef + (size_t)s * kStateRow, ph, pl);
+            frame_step<EXT, TRI, SC>(Y, Yl, coef + (size_t)s * kStateRow, ph, pl);
         }
         sample(b + 1);
     }
@@ -254,9 +261,11 @@ template <int NT, bool EXT, bool TRI>
 static cudaError_t launch_pc_resp_t(const PcParams<double>& Q, const float4* resp, const double* ext,
                                     double* partials, double* estore, cudaStream_t s)
 {
-    // cf_s [B+2][kCta], red_s, the parts' running sums [3][kCta]
-    const size_t smem = ((size_t)Q.P.n_blocks + 2) * kPcCta * 8 + 2 * (kPcCta / 32) * 8 + 3 * kPcCta * 8;
-    auto k = path_kernel_pc_resp<NT, EXT, TRI>;
+    // cf_s [B+2][kCta], red_s, the parts' running sums [3][kCta], the frame's coefficients
+    const bool sc = Q.P.stride <= kFrameSmemRows;
+    const size_t smem = ((size_t)Q.P.n_blocks + 2) * kPcCta * 8 + 2 * (kPcCta / 32) * 8 + 3 * kPcCta * 8 +
+                        (sc ? (size_t)Q.P.stride * kStateRow * 16 : 0);
+    auto k = sc ? path_kernel_pc_resp<NT, EXT, TRI, true> : path_kernel_pc_resp<NT, EXT, TRI, false>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const int64_t grid = (Q.P.n_paths + kPcCta - 1) / kPcCta;

@@ -168,6 +168,7 @@ __device__ __forceinline__ void df_renorm(float2& A, float2& Al)
 // the accumulator per double-FP32 addition over one block's ~150 additions
 // (~5e-14 of the parts' terms), the rest FP64.
 constexpr int kStateRow = 9;
+constexpr int kFrameSmemRows = 112;  // rows staged in shared memory (15.75 KB per CTA at most)
 
 // M^a and Q(a) of a block of a steps (uniform across the CTA).
 struct BlockFrame {
@@ -186,16 +187,22 @@ struct BlockFrame {
 };
 
 // One step of the parts: y += C(s) phi, v += G(s) phi from the coefficient
-// row cr, then the pairs renormalised.  ph, pl: the normals as hi + lo (pl
-// unused for FP32 draws, EXT = false).
-template <bool EXT, bool TRI>
+// row cr (in shared memory for SHARED, else read through L1), then the pairs
+// renormalised.  ph, pl: the normals as hi + lo (pl unused for FP32 draws,
+// EXT = false).
+template <bool EXT, bool TRI, bool SHARED = false>
 __device__ __forceinline__ void frame_step(float2 (&Y)[3], float2 (&Yl)[3], const float4* __restrict__ cr,
                                            const float (&ph)[3], const float (&pl)[3])
 {
     float4 q[kStateRow];
 #pragma unroll
     for (int t = 0; t < kStateRow; ++t)
-        if (!TRI || t / 3 <= t % 3) q[t] = __ldg(cr + t);
+        if (!TRI || t / 3 <= t % 3) {
+            if constexpr (SHARED)
+                q[t] = cr[t];
+            else
+                q[t] = __ldg(cr + t);
+        }
 #pragma unroll
     for (int t = 0; t < kStateRow; ++t) {
         const int c = t / 3, k = t % 3;

@@ -238,8 +238,9 @@ def test_pc_response_form_vs_convected_and_oracle(pc, case, general):
     np.testing.assert_array_equal(ext.ee, vr.ee)
 
 
-@pytest.mark.parametrize("n_paths,n_steps,dt", [(1, 1000, 0.01), (257, 1200, 0.01), (63, 500, 0.02)],
-                         ids=["1-path", "24-dates", "stride25"])
+@pytest.mark.parametrize("n_paths,n_steps,dt", [(1, 1000, 0.01), (257, 1200, 0.01), (63, 500, 0.02),
+                                                (65, 1000, 0.004)],
+                         ids=["1-path", "24-dates", "stride25", "stride125-coefficients-via-L1"])
 def test_pc_response_form_shapes_vs_oracle(pc, n_paths, n_steps, dt):
     mk = Market()
     pc.set_market(mk)

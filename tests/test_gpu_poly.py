@@ -292,11 +292,15 @@ def test_remainder_forms_agree_and_match_oracle(engine, remainder_form, nt, coef
 
 
 @pytest.mark.parametrize("n_paths,n_steps,dt", [(1, 1000, 0.01), (63, 500, 0.02), (257, 1200, 0.01),
-                                                (100, 250, 0.01), (64, 1000, 0.005), (100, 50, 0.05)],
-                         ids=["1-path", "stride25", "24-dates", "5-dates", "stride100", "stride10-all-zero"])
+                                                (100, 250, 0.01), (64, 1000, 0.005), (100, 50, 0.05),
+                                                (65, 1000, 0.004)],
+                         ids=["1-path", "stride25", "24-dates", "5-dates", "stride100", "stride10-all-zero",
+                              "stride125-coefficients-via-L1"])
 def test_response_form_shapes_vs_oracle(engine, remainder_form, n_paths, n_steps, dt):
-    """Ragged path counts, strides 10 to 100, 5 to 24 dates (the form's maximum);
-    with stride 10 the remainder never reaches a sampled tenor (all responses zero)."""
+    """Ragged path counts, strides 10 to 125, 5 to 24 dates (the form's maximum);
+    with stride 10 the remainder never reaches a sampled tenor (all responses
+    zero); beyond 112 steps per block the frame's coefficients are read
+    through L1 instead of shared memory."""
     mk = _poly_market(engine)
     stride = int(round(mk.dtau / dt))
     sw = Swap(n_periods=max(n_steps // stride, 1))
