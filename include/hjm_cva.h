@@ -112,7 +112,8 @@ hjm_status hjm_ctx_vol_decomposition(hjm_ctx* ctx, int32_t* active);
  * for each date still to be sampled, as its value and running sum in impulse
  * responses of the convection (HJM_REMAINDER_RESPONSE: one double-FP32 term
  * per such date per step, on the FP32 pipe; the remainder is ~1e-5 of the
- * curve).  With a volatility table of any shape (no decomposition) the whole
+ * curve; the polynomial parts S, U, W then advance as double-FP32 sums in a
+ * moving frame, with FP64 only at the sampled dates).  With a volatility table of any shape (no decomposition) the whole
  * stochastic curve is either convected with the noise injected at every tenor,
  * or carried in the response form as sums of the three factors' impulse
  * responses (six FP64 FMAs per date per step).  The response form holds at
