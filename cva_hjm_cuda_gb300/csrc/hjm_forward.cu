@@ -240,8 +240,9 @@ __global__ void __launch_bounds__(kFp64Cta, 4)
     fp64_epilogue<kCta>(P, cf_s, work_s, red_s, partials, estore, cta_base, active);
 }
 
-// The FP64 response form (hjm_resp.cuh): the polynomial parts S, U, W in FP64,
-// the remainder as double-FP32 impulse-response sums per date slot.
+// The FP64 response form (hjm_resp.cuh): the polynomial parts S, U, W as
+// double-FP32 sums in a moving frame anchored at each block, the remainder as
+// double-FP32 impulse-response sums per date slot, FP64 at the sampled dates.
 __host__ __device__ inline size_t resp_smem_bytes(int n_blocks)
 {
     // cf_s [B+2][kCta] (the epilogue's exposures alias it one row up), red_s
@@ -249,6 +250,7 @@ __host__ __device__ inline size_t resp_smem_bytes(int n_blocks)
 }
 
 // the Euler response kernel: and the running sums of the parts [3][kCta]
+// (the frame's coefficient rows follow when staged)
 __host__ __device__ inline size_t resp_smem_bytes_parts(int n_blocks)
 {
     return resp_smem_bytes(n_blocks) + 3 * kFp64Cta * 8;
