@@ -45,14 +45,19 @@ namespace hjm {
 //
 // The accumulators of date j sit in slot r = B - j.  At step s of block b the
 // dates with a nonzero term are j = b + q for q_min <= q <= B - b, q_min the
-// least q with lag q stride - 1 - s >= L - b - q: slots 0 .. n_act - 1, a
-// prefix.  A switch on the number of groups of four slots covering it enters
-// a fall-through chain of groups (Duff's device): the skipped groups issue
-// nothing (a predicated loop would issue them all), and the four terms of a
-// group form one basic block, their loads in flight together and their FP32
-// chains interleaved.  The table is zero outside the live nonzero entries, so
-// the slots a group adds beyond n_act add exact zeros (dead or not yet
-// reached dates).  The impulse responses come from response_table_kernel.
+// least q whose lag q stride - 1 - s reaches the date's tenor (Euler: one
+// tenor per step from L, lag >= L - j; predictor-corrector: the stencil
+// reaches two tenors per step, 2 lag >= L - 2 - j): slots 0 .. n_act - 1, a
+// prefix.  The kernels read each row's prefix from the table
+// (response_active_kernel), which also drops the trailing slots whose terms
+// are vanishingly small.  A switch on the number of groups of four slots
+// covering it enters a fall-through chain of groups (Duff's device): the
+// skipped groups issue nothing (a predicated loop would issue them all), and
+// the four terms of a group form one basic block, their loads in flight
+// together and their FP32 chains interleaved.  The table is zero outside the
+// live nonzero entries, so the slots a group adds beyond n_act add exact
+// zeros (dead or not yet reached dates).  The impulse responses come from
+// response_table_kernel.
 constexpr int kRespDates = 24;   // dates the response form holds (slots 0 .. 22 for dates 2 .. B)
 constexpr int kRespSlots = 24;   // accumulator slots, a multiple of the group of 4 (slot 23 stays zero)
 constexpr int kRespRow = 24;     // response-table row: one float4 per slot
@@ -254,23 +259,6 @@ __host__ __device__ inline size_t resp_coef_offset(int stride, int B) { return (
 __host__ __device__ inline size_t resp_nact_offset(int stride, int B)
 {
     return (size_t)B * stride * kRespRow + (size_t)stride * kStateRow;
-}
-
-// Slots with a nonzero term at step s of block b: q_min is the nearest date
-// whose lag l = q stride - 1 - s reaches its tenor, and the slots 0 .. n_act -
-// 1 hold the dates b + q_min .. B (n_act <= 0: none).  Euler (one tenor per
-// step from L): l >= L - j, q_min = ceil((L - b + 1 + s) / (stride + 1)).
-// Predictor-corrector (the two-point stencil reaches two tenors per step, and
-// its coefficient at lag l includes the response of the next step to the
-// curvature noise): 2 l >= L - 2 - j, q_min = ceil((L - b + 2 s) / (2 stride + 1)).
-template <bool PC = false>
-__device__ __forceinline__ int resp_n_act(int s, int b, int B, int L, int stride)
-{
-    const int num = PC ? L - b + 2 * s : L - b + 1 + s;
-    const int den = PC ? 2 * stride + 1 : stride + 1;
-    const int q = (num + den - 1) / den;
-    const int q_min = q > 1 ? q : 1;
-    return B - b - q_min + 1;
 }
 
 // fn(std::integral_constant<int, G>) for the groups G = ceil(n_act/4) - 1 .. 0
