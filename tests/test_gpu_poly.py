@@ -417,12 +417,15 @@ def test_table_step_response_shapes_vs_oracle(engine, remainder_form, n_paths, n
 
 
 def test_response_tables_follow_shape_market_and_scheme(engine):
-    """The context caches the response tables per run shape, scheme and (table
-    step) loadings: alternating them on one context gives bit for bit what a
-    fresh context gives for each case."""
+    """The context caches the response tables per run shape, scheme, factor
+    loadings (the parts' frame coefficients) and (table step) volatility
+    table: alternating them on one context gives bit for bit what a fresh
+    context gives for each case."""
     from cva_hjm_cuda_gb300 import HJMEngine
 
     cases = [
+        ("poly", "euler", RunConfig(n_paths=700, seed=2)),
+        ("poly-scaled", "euler", RunConfig(n_paths=700, seed=2)),
         ("poly", "euler", RunConfig(n_paths=700, seed=2)),
         ("table", "euler", RunConfig(n_paths=700, seed=2)),
         ("poly", "euler", RunConfig(n_paths=700, n_steps=500, dt=0.02, seed=2)),
@@ -436,6 +439,9 @@ def test_response_tables_follow_shape_market_and_scheme(engine):
         eng.set_scheme(scheme)
         if market == "poly":
             eng.set_market(Market())
+        elif market == "poly-scaled":
+            mk = Market()
+            eng.set_market_poly(51, mk.dtau, mk.spot, DEFAULT_VOL_COEFFS * 1.3)
         else:
             bump = 0.1 if market == "table" else -0.07
             eng.set_market(Market(vol=Market().vol * (1.0 + bump * np.cos(np.arange(51) / 7.0))[None, :]))
