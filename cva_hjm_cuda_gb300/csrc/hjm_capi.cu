@@ -579,6 +579,7 @@ static void fill_params(const hjm_ctx* ctx, const RunShape& sh, int64_t n_paths,
     P.c = (T)(dt / ctx->dtau);
     P.dt = dt;
     P.m = 1.0 / ctx->dtau;
+    P.inv_m = ctx->dtau;
     P.key0 = (uint32_t)seed;
     P.key1 = (uint32_t)(seed >> 32);
     philox_round_keys(P.key0, P.key1, P.rk0, P.rk1);

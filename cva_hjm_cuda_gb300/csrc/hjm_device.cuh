@@ -179,6 +179,7 @@ struct PathParams {
     T qm;                        // 1 / (1 + rr): per-step factor of the scale
     T ip;                        // 1 + rr: per-step factor of the inverse scale
     T m2k2;                      // -2 c dtau^2: the polynomial form's last-tenor source per unit W
+    double inv_m;                // dtau = 1 / m: the LIBOR's exponent x / m as a product
 };
 
 // Host: the growth-scale constants of PathParams from c = dt / dtau, k2 and

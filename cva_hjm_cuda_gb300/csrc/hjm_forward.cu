@@ -123,7 +123,7 @@ __global__ void __launch_bounds__(kFp64Cta, 4)
         const double x = P.psamp[i] + value_at(i);
         const double a = P.psum[i] + acc_s[i * kCta + tid];
         const double D = exp(-a * P.dt);
-        const double Lb = P.m * (exp(x / P.m) - 1.0);
+        const double Lb = P.m * (exp(x * P.inv_m) - 1.0);
         cf_s[i * kCta + tid] = D * (P.payA[i] * Lb - P.payB[i]);
     };
 
@@ -317,7 +317,7 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
         const double x = P.psamp[i] + (fma(tau, fma(tau, W, U), S) + hc);
         const double acc = fma(tau, fma(tau, ZW, ZU), ZS) + hcs;
         const double D = exp(-(P.psum[i] + acc) * P.dt);
-        const double Lb = P.m * (exp(x / P.m) - 1.0);
+        const double Lb = P.m * (exp(x * P.inv_m) - 1.0);
         cf_s[i * kCta + tid] = D * (P.payA[i] * Lb - P.payB[i]);
     };
 
@@ -599,7 +599,7 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
         const double hs = i >= 2 ? select_reg<kRespSlots, double>(ai, B - i) : 0.0;
         const double x = P.psamp[i] + h;
         const double D = exp(-(P.psum[i] + hs) * P.dt);
-        const double Lb = P.m * (exp(x / P.m) - 1.0);
+        const double Lb = P.m * (exp(x * P.inv_m) - 1.0);
         cf_s[i * kCta + tid] = D * (P.payA[i] * Lb - P.payB[i]);
     };
 

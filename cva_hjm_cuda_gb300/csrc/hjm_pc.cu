@@ -216,7 +216,7 @@ __global__ void __launch_bounds__(kPcCta, 6)
         const double x = P.psamp[i] + (fma(tau, fma(tau, W, U), S) + hc);
         const double acc = fma(tau, fma(tau, ZW, ZU), ZS) + hcs;
         const double D = exp(-(P.psum[i] + acc) * P.dt);
-        const double Lb = P.m * (exp(x / P.m) - 1.0);
+        const double Lb = P.m * (exp(x * P.inv_m) - 1.0);
         cf_s[i * kPcCta + tid] = D * (P.payA[i] * Lb - P.payB[i]);
     };
 

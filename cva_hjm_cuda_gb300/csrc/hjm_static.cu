@@ -176,6 +176,7 @@ static void static_params(int nt, double dtau, const double* spot, const double*
     fill_growth_scale(P, dt / dtau, P.k2, stride, B);
     P.dt = dt;
     P.m = 1.0 / dtau;
+    P.inv_m = dtau;
     P.key0 = (uint32_t)seed;
     P.key1 = (uint32_t)(seed >> 32);
     philox_round_keys(P.key0, P.key1, P.rk0, P.rk1);
