@@ -90,6 +90,9 @@ __device__ __forceinline__ void split_f64(double d, float& hi, float& lo)
     lo = __uint_as_float(sign | __float_as_uint((float)r * scale));
 }
 
+// -v in both lanes (folded into the consumer's operand)
+__device__ __forceinline__ float2 neg2(float2 v) { return make_float2(-v.x, -v.y); }
+
 // (A, Al) += (kh + kl) (wh + wl) in double-FP32, both lanes: the product's
 // leading term exact by FMA, the cross terms in FP32, kl wl (2^-48) dropped;
 // Knuth's two-sum keeps A + Al exact up to the FP32 rounding of Al.  nwh =
@@ -99,16 +102,15 @@ __device__ __forceinline__ void split_f64(double d, float& hi, float& lo)
 // that of the plain formulation (negation is exact).
 __device__ __forceinline__ void df_acc(float2& A, float2& Al, float2 kh, float2 kl, float2 wh, float2 wl, float2 nwh)
 {
-    const float2 m1 = make_float2(-1.0f, -1.0f);
     const float2 pn = __fmul2_rn(kh, nwh);
     float2 e = __ffma2_rn(kh, wh, pn);
     e = __ffma2_rn(kh, wl, e);
     e = __ffma2_rn(kl, wh, e);
-    const float2 sum = __ffma2_rn(pn, m1, A);   // A + p
-    const float2 bp = __ffma2_rn(A, m1, sum);   // sum - A
-    const float2 ap = __ffma2_rn(bp, m1, sum);  // sum - bp
+    const float2 sum = __fadd2_rn(A, neg2(pn));   // A + p
+    const float2 bp = __fadd2_rn(sum, neg2(A));   // sum - A
+    const float2 ap = __fadd2_rn(sum, neg2(bp));  // sum - bp
     // (A - ap) + (p - bp), with p - bp = -(pn + bp)
-    const float2 err = __ffma2_rn(__fadd2_rn(pn, bp), m1, __ffma2_rn(ap, m1, A));
+    const float2 err = __fadd2_rn(__fadd2_rn(A, neg2(ap)), neg2(__fadd2_rn(pn, bp)));
     Al = __fadd2_rn(Al, __fadd2_rn(err, e));
     A = sum;
 }
@@ -117,14 +119,13 @@ __device__ __forceinline__ void df_acc(float2& A, float2& Al, float2 kh, float2 
 // df_acc without the w_lo term.
 __device__ __forceinline__ void df_acc_w(float2& A, float2& Al, float2 kh, float2 kl, float2 w, float2 nw)
 {
-    const float2 m1 = make_float2(-1.0f, -1.0f);
     const float2 pn = __fmul2_rn(kh, nw);
     float2 e = __ffma2_rn(kh, w, pn);
     e = __ffma2_rn(kl, w, e);
-    const float2 sum = __ffma2_rn(pn, m1, A);
-    const float2 bp = __ffma2_rn(A, m1, sum);
-    const float2 ap = __ffma2_rn(bp, m1, sum);
-    const float2 err = __ffma2_rn(__fadd2_rn(pn, bp), m1, __ffma2_rn(ap, m1, A));
+    const float2 sum = __fadd2_rn(A, neg2(pn));
+    const float2 bp = __fadd2_rn(sum, neg2(A));
+    const float2 ap = __fadd2_rn(sum, neg2(bp));
+    const float2 err = __fadd2_rn(__fadd2_rn(A, neg2(ap)), neg2(__fadd2_rn(pn, bp)));
     Al = __fadd2_rn(Al, __fadd2_rn(err, e));
     A = sum;
 }
@@ -136,9 +137,8 @@ __device__ __forceinline__ void df_acc_w(float2& A, float2& Al, float2 kh, float
 // at 2^-48 of A per addition instead of growing with the number of terms.
 __device__ __forceinline__ void df_renorm(float2& A, float2& Al)
 {
-    const float2 m1 = make_float2(-1.0f, -1.0f);
     const float2 sum = __fadd2_rn(A, Al);
-    Al = __ffma2_rn(__ffma2_rn(A, m1, sum), m1, Al);  // Al - (sum - A)
+    Al = __fadd2_rn(Al, neg2(__fadd2_rn(sum, neg2(A))));  // Al - (sum - A)
     A = sum;
 }
 
