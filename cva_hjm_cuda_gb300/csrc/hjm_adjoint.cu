@@ -206,7 +206,7 @@ __global__ void __launch_bounds__(kAdjCta, adj_min_ctas<NT>())
                 double part = 0.0;
                 if (needed && s > 0)
                     block_sums_up<NT, POLY>(x, hs_s, tid, kCtaA, P, bs, inext, [&](int t, float Ht) {
-                        if (t == inext) part = (double)Ht;
+                        if (t == inext) part = as_f64(Ht);
                     });
                 if (needed && active) {
 #pragma unroll
@@ -226,7 +226,7 @@ __global__ void __launch_bounds__(kAdjCta, adj_min_ctas<NT>())
             bs.add(x, phi0, phi1, phi2);
         }
         block_sums_up<NT, POLY>(x, hs_s, tid, kCtaA, P, bs, B, [&](int t, float Ht) {
-            if (t > b) acc_s[t * kCtaA + tid] += (double)Ht;
+            if (t > b) acc_s[t * kCtaA + tid] += as_f64(Ht);
         });
 #pragma unroll
         for (int t = 1; t < NT; ++t)
@@ -334,7 +334,7 @@ __global__ void __launch_bounds__(kAdjCta, adj_min_ctas<NT>())
                 }
                 double part = 0.0;
                 block_sums_up<NT, POLY>(xr, hs_s, tid, kCtaA, P, bs, i, [&](int t, float Ht) {
-                    if (t == i) part = (double)Ht;
+                    if (t == i) part = as_f64(Ht);
                 });
                 const double xv = P.psamp[i] + (double)xr.value(P, i);
                 const double a = P.psum[i] + a0 + part;

@@ -216,6 +216,11 @@ __device__ __forceinline__ double widen_f32(float f)
     return __hiloint2double((int)hi, (int)lo);
 }
 
+// A float or double as a double, the float by widen_f32 (for the FP64 folds of
+// FP32 block sums: no FP64-pipe conversion per fold)
+__device__ __forceinline__ double as_f64(float f) { return widen_f32(f); }
+__device__ __forceinline__ double as_f64(double d) { return d; }
+
 // The three normals of (path, step): Philox in registers, or read from a
 // caller-supplied buffer laid out [step][3][path] (coalesced across threads).
 template <typename T, bool EXT>

@@ -764,7 +764,7 @@ __global__ void __launch_bounds__(kCta, 4)
         }
         // block sums of tenors 2 .. B; fold (b, B] into FP64
         block_sums_up<NT, POLY>(x, hs_s, tid, kCta, P, bs, B, [&](int t, float Ht) {
-            if (t > b) acc_s[t * kCta + tid] += (double)Ht;
+            if (t > b) acc_s[t * kCta + tid] += as_f64(Ht);
         });
         // the block-end curve (POLY: its convected part) is the next block's start
 #pragma unroll

@@ -104,10 +104,10 @@ __global__ void __launch_bounds__(kMlCta, mlmc_min_ctas<POLY>())
             bc.add(xc, c0, c1, c2);
         }
         block_sums_up<NT, POLY>(xf, hsF, tid, kMlCta, PF, bf, B, [&](int t, float Ht) {
-            if (t > b) accF[t * kMlCta + tid] += (double)Ht;
+            if (t > b) accF[t * kMlCta + tid] += as_f64(Ht);
         });
         block_sums_up<NT, POLY>(xc, hsC, tid, kMlCta, PC, bc, B, [&](int t, float Ht) {
-            if (t > b) accC[t * kMlCta + tid] += (double)Ht;
+            if (t > b) accC[t * kMlCta + tid] += as_f64(Ht);
         });
 #pragma unroll
         for (int t = 1; t < NT; ++t)

@@ -142,8 +142,8 @@ struct PcPath {
         const T dL1 = fma(g, v[L - 1], -hs_s[(L - 1) * kPcCta + tid]);
         const T HL = g * Tb;
         const T HL1 = fma(X(L - 1) - fma(Q.ce, dL - dL1, dL1), Q.inv_ce, HL);
-        if (L <= B) acc_s[L * kPcCta + tid] += (double)(HL + poly_at(P, sS, sU, sW, L));
-        if (L - 1 <= B && L - 1 > b) acc_s[(L - 1) * kPcCta + tid] += (double)(HL1 + poly_at(P, sS, sU, sW, L - 1));
+        if (L <= B) acc_s[L * kPcCta + tid] += as_f64(HL + poly_at(P, sS, sU, sW, L));
+        if (L - 1 <= B && L - 1 > b) acc_s[(L - 1) * kPcCta + tid] += as_f64(HL1 + poly_at(P, sS, sU, sW, L - 1));
         T H1 = HL1, H2 = HL, d1 = dL1, d2 = dL;
 #pragma unroll
         for (int t = L - 2; t >= 1; --t) {
@@ -151,7 +151,7 @@ struct PcPath {
             const T d = fma(g, v[t], -hs_s[t * kPcCta + tid]);
             const T a2d = fma(Q.a2e, d2, fma(Q.a1e, d1, Q.a0e * d));
             const T Ht = (X(t) - a2d + fma(Q.a1e, H1, Q.a2e * H2)) * Q.inv_1ma0;
-            if (t <= B) acc_s[t * kPcCta + tid] += (double)(Ht + poly_at(P, sS, sU, sW, t));
+            if (t <= B) acc_s[t * kPcCta + tid] += as_f64(Ht + poly_at(P, sS, sU, sW, t));
             H2 = H1;
             H1 = Ht;
             d2 = d1;
