@@ -152,19 +152,22 @@ def response_active_prefix(n_tenor: int, n_steps: int, stride: int, dtau: float 
 
 
 def response_fp32_flops_per_path(n_tenor: int, n_steps: int, stride: int, form: str = "poly_tri") -> int:
-    """FP32 flops of the Euler response form's double-FP32 terms per path.
-    At each evolved step: the date slots in groups of four covering the row's
-    active prefix (``response_active_prefix``), each slot one packed {value,
-    running sum} update of 1 FMUL2 + 8 FFMA2 + 3 FADD2 = 40 flops (product with
-    its exact leading term, Knuth two-sum, low-part update); and the parts'
-    moving-frame terms, 6 (``poly_tri``) or 9 (``poly``) packed {y, v} updates
-    with an exact FP32 normal, 1 FMUL2 + 7 FFMA2 + 3 FADD2 = 36 flops each,
-    and their renormalisation, 3 x (1 FADD2 + 2 FFMA2) = 30 flops."""
+    """FP32 flops of the Euler response form's double-FP32 terms per path
+    (a multiply or an add 1 flop, an FMA 2; packed instructions count both
+    lanes).  At each evolved step: the date slots in groups of four covering
+    the row's active prefix (``response_active_prefix``), each slot one packed
+    {value, running sum} update of 1 FMUL2 + 3 FFMA2 + 8 FADD2 = 30 flops
+    (product with its exact leading term, Knuth two-sum, low-part update); and
+    the parts' moving-frame terms, 6 (``poly_tri``) or 9 (``poly``) packed
+    {y, v} updates with an exact FP32 normal, 1 FMUL2 + 2 FFMA2 + 8 FADD2 = 26
+    flops each, and their renormalisation, 3 x 3 FADD2 = 18 flops.  An add
+    occupies the FMA pipe as an FMA does, so the pipe is busier than this
+    count's fraction of the FMA peak."""
     B = n_steps // stride
     pre = response_active_prefix(n_tenor, n_steps, stride)[stride:]
     slots = int((4 * ((pre + 3) // 4)).sum())
     terms = 6 if form == "poly_tri" else 9
-    return 40 * slots + (36 * terms + 30) * (B - 1) * stride
+    return 30 * slots + (26 * terms + 18) * (B - 1) * stride
 
 
 class ClockSampler:

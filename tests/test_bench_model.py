@@ -22,14 +22,14 @@ def test_response_forms_count_the_kernels_operations():
     # volatility table in the response form: six FMAs per date still to be sampled per step
     live = sum(B - b for b in range(1, B)) * stride
     assert bench.algorithmic_flops_per_path(nt, n_steps, stride, "table", "response") == 12 * live
-    # the double-FP32 side: 40 flops per slot (slots in groups of four over the
-    # active prefix), 36 per moving-frame term (6 or 9 per step), 30 per step
+    # the double-FP32 side: 30 flops per slot (slots in groups of four over the
+    # active prefix), 26 per moving-frame term (6 or 9 per step), 18 per step
     # for the renormalisation
-    parts_tri = (36 * 6 + 30) * (B - 1) * stride
+    parts_tri = (26 * 6 + 18) * (B - 1) * stride
     f32 = bench.response_fp32_flops_per_path(nt, n_steps, stride) - parts_tri
-    assert f32 % 160 == 0 and 0 < f32 <= 40 * 24 * (B - 1) * stride
+    assert f32 % 120 == 0 and 0 < f32 <= 30 * 24 * (B - 1) * stride
     assert (bench.response_fp32_flops_per_path(nt, n_steps, stride, "poly")
-            - bench.response_fp32_flops_per_path(nt, n_steps, stride, "poly_tri")) == 36 * 3 * (B - 1) * stride
+            - bench.response_fp32_flops_per_path(nt, n_steps, stride, "poly_tri")) == 26 * 3 * (B - 1) * stride
 
 
 def test_convected_forms_exceed_the_response_forms():
