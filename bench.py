@@ -211,16 +211,22 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def profiled_traffic(kernel_key: str) -> float | None:
-    """DRAM bytes per launch of the dominant kernel from the committed ncu summaries."""
+def profiled_value(name: str, kernel_key: str) -> float | None:
+    """A figure of the dominant kernel from the committed ncu summaries (a line
+    ``name[kernel_key]: value``)."""
     for f in sorted((ROOT / "profiles").glob("*.md")):
         for line in f.read_text().splitlines():
-            if line.startswith(f"traffic_bytes_per_launch[{kernel_key}]:"):
+            if line.startswith(f"{name}[{kernel_key}]:"):
                 try:
                     return float(line.split(":", 1)[1].strip().split()[0])
                 except ValueError:
                     return None
     return None
+
+
+def profiled_traffic(kernel_key: str) -> float | None:
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summaries."""
+    return profiled_value("traffic_bytes_per_launch", kernel_key)
 
 
 def cpu_oracle_sample(target_s: float, n_threads: int) -> dict:
@@ -428,6 +434,9 @@ def run_ours(args) -> None:
         achieved = flops / (path_ms * 1e-3) / 1e12
         peak = extras.get("measured_fma_peak_tflops", {}).get("fp32")
         bound = "fp32_pipe (double-FP32)"
+        # the FMA pipe's busy fraction from the committed ncu capture: the
+        # double-FP32 terms are mostly adds, which occupy it as FMAs do
+        fma_busy = profiled_value("fma_pipe_cycles_active", f"{prec}-{n_paths}")
     roofline = {"bound": bound, "achieved": achieved, "peak": peak,
                 "unit": "TFLOP/s", "frac": (achieved / peak) if peak else None, "traffic": traffic,
                 "kernel": (f"adjoint_kernel<{mk.n_tenor},ckpt,{form}>" if is_adjoint else
@@ -447,6 +456,7 @@ def run_ours(args) -> None:
                 / elapsed / 1e12 if not is_adjoint else None}
     if side:
         roofline["fp64_side"] = side
+        roofline["fma_pipe_cycles_active_ncu"] = fma_busy
 
     if not args.no_extras and prec == "fp64":
         if remainder == "response":
