@@ -265,7 +265,6 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
                           double* __restrict__ estore)
 {
     constexpr int kCta = kFp64Cta;
-    constexpr int L = NT - 1;
     extern __shared__ __align__(128) unsigned char smem[];
     const int tid = threadIdx.x;
     const int B = P.n_blocks;

@@ -171,7 +171,6 @@ __global__ void __launch_bounds__(kPcCta, 6)
     path_kernel_pc_resp(const __grid_constant__ PcParams<double> Q, const float4* __restrict__ resp,
                         const double* __restrict__ ext, double* __restrict__ partials, double* __restrict__ estore)
 {
-    constexpr int L = NT - 1;
     const PathParams<double>& P = Q.P;
     extern __shared__ __align__(128) unsigned char smem[];
     const int tid = threadIdx.x;
