@@ -238,14 +238,14 @@ def test_pc_response_form_vs_convected_and_oracle(pc, case, general):
     np.testing.assert_array_equal(ext.ee, vr.ee)
 
 
-@pytest.mark.parametrize("n_paths,n_steps,dt", [(1, 1000, 0.01), (257, 1200, 0.01), (63, 500, 0.02),
-                                                (65, 1000, 0.004)],
-                         ids=["1-path", "24-dates", "stride25", "stride125-coefficients-via-L1"])
-def test_pc_response_form_shapes_vs_oracle(pc, n_paths, n_steps, dt):
-    mk = Market()
+@pytest.mark.parametrize("nt,n_paths,n_steps,dt", [(51, 1, 1000, 0.01), (51, 257, 1200, 0.01), (51, 63, 500, 0.02),
+                                                   (51, 65, 1000, 0.004), (61, 257, 1000, 0.01)],
+                         ids=["1-path", "24-dates", "stride25", "stride125-coefficients-via-L1", "61-tenors"])
+def test_pc_response_form_shapes_vs_oracle(pc, nt, n_paths, n_steps, dt):
+    mk = Market(n_tenor=nt)
     pc.set_market(mk)
     stride = int(round(mk.dtau / dt))
-    sw = Swap(n_periods=n_steps // stride)
+    sw = Swap(n_tenor=nt, n_periods=n_steps // stride)
     pc.set_swap(sw)
     pc.set_remainder_form("response")
     try:
