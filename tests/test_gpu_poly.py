@@ -462,3 +462,30 @@ def test_response_tables_follow_shape_market_and_scheme(engine):
             f = fresh.run(cfg, "fp64")
         np.testing.assert_array_equal(g.ee, f.ee)
         assert g.cva == f.cva
+
+
+@pytest.mark.parametrize("coef", [DEFAULT_VOL_COEFFS, FULL_COEFFS], ids=["degree<=k", "general"])
+def test_response_form_on_double_normals_vs_oracle(engine, remainder_form, coef):
+    """External FP64 normals that FP32 cannot hold (the response form splits
+    each into hi + lo and carries both through the parts' double-FP32 terms),
+    triangular and general quadratic factors: per-path exposures, EE and CVA
+    against the oracle on the same draws."""
+    mk = _poly_market(engine, coef=coef)
+    sw = Swap()
+    engine.set_swap(sw)
+    remainder_form("response")
+    n_paths, n_steps, dt = 300, 1000, 0.01
+    normals = np.random.default_rng(31).standard_normal((n_paths, n_steps, 3))
+    engine.keep_exposures(True)
+    try:
+        v = engine.run_with_normals(normals, n_steps, dt, "fp64")
+        assert engine.remainder_form() == "response"
+        x = engine.exposures()
+    finally:
+        engine.keep_exposures(False)
+    xo = O.exposure_paths(mk, sw, n_steps, dt, normals)
+    ee = O.expected_exposure(xo)
+    cva, _ = O.cva(ee, 21, mk.dtau, 0.02, 0.4)
+    _assert_rel(x, xo[:, :21].T, FP64_RTOL, "exposures")
+    _assert_rel(v.ee[:21], ee[:21], FP64_RTOL, "EE")
+    _assert_rel(v.cva, cva, FP64_RTOL, "CVA")
