@@ -500,7 +500,8 @@ __global__ void state_coef_kernel(PartsFrame f, int stride, float4* __restrict__
 // Epilogue of the mixed-precision path kernels (as fp64_epilogue, exposures
 // and their store in FP32): acc_s rows 1..B hold the cash flows (FP64), e_s
 // B+1 FP32 rows (free for this use).
-__device__ __forceinline__ void mixed_epilogue(const PathParams<float>& P, const double* acc_s, float* e_s,
+template <typename CF>
+__device__ __forceinline__ void mixed_epilogue(const PathParams<float>& P, const CF* acc_s, float* e_s,
                                                double* red_s, double* __restrict__ partials,
                                                float* __restrict__ estore, int64_t cta_base, bool active)
 {
@@ -509,7 +510,7 @@ __device__ __forceinline__ void mixed_epilogue(const PathParams<float>& P, const
     double v = 0.0, cva_c = 0.0;
     e_s[B * kCta + tid] = 0.f;
     for (int j = B - 1; j >= 0; --j) {
-        v += acc_s[(j + 1) * kCta + tid];
+        v += as_f64(acc_s[(j + 1) * kCta + tid]);
         double e = (v > 0.0) ? v : 0.0;
         if (!active) e = 0.0;
         e_s[j * kCta + tid] = (float)e;
@@ -709,19 +710,29 @@ __global__ void __launch_bounds__(kMaxTenor)
 // Shared memory per thread: acc (B+1) FP64 discount sums, whose slot i holds
 // date i's cash flow once tenor i is sampled; hs (B+2) FP32 curve at the block
 // start, reused for the exposure tile at the end.
-template <int NT, bool EXT, bool POLY>
+// CMP (polynomial factors, many dates): acc holds FP32 instead, the sums of the
+// convected remainder only (its block sums in FP32, as folded into FP64
+// otherwise; the remainder is a small fraction of the curve), and the FP64
+// running sums of the scalar parts S, U, W stay in registers, so that the
+// shared memory of a CTA (the occupancy limit with 60 dates) shrinks by a third.
+template <int NT, bool EXT, bool POLY, bool CMP>
 __global__ void __launch_bounds__(kCta, 4)
     path_kernel_mixed(const __grid_constant__ MixedParams M, const double* __restrict__ ext,
                       double* __restrict__ partials, float* __restrict__ estore)
 {
+    static_assert(!CMP || POLY, "the compact sums need the polynomial parts");
+    using Acc = typename std::conditional<CMP, float, double>::type;
     const PathParams<float>& P = M.P;
     extern __shared__ __align__(128) unsigned char smem[];
     const int tid = threadIdx.x;
     const int B = P.n_blocks;
     const int rows = B + 1;
-    double* acc_s = reinterpret_cast<double*>(smem);                       // [B+1][kCta]
-    float* hs_s = reinterpret_cast<float*>(smem + (size_t)rows * kCta * 8);  // [B+2][kCta]
-    double* red_s = reinterpret_cast<double*>(smem + (size_t)rows * kCta * 8 + (size_t)(rows + 1) * kCta * 4);
+    constexpr size_t ka = sizeof(Acc);
+    Acc* acc_s = reinterpret_cast<Acc*>(smem);                                // [B+1][kCta]
+    float* hs_s = reinterpret_cast<float*>(smem + (size_t)rows * kCta * ka);  // [B+2][kCta]
+    double* red_s = reinterpret_cast<double*>(
+        smem + (((size_t)rows * kCta * ka + (size_t)(rows + 1) * kCta * 4 + 7) & ~(size_t)7));
+    double zS = 0.0, zU = 0.0, zW = 0.0;  // CMP: FP64 running sums of the parts over the evolved steps
 
     const int64_t cta_base = (int64_t)blockIdx.x * kCta;
     const int64_t lp = cta_base + tid;
@@ -730,16 +741,21 @@ __global__ void __launch_bounds__(kCta, 4)
 
     MixedPath<NT, POLY> x;
     x.reset();
-    for (int i = 0; i < rows; ++i) acc_s[i * kCta + tid] = 0.0;
+    for (int i = 0; i < rows; ++i) acc_s[i * kCta + tid] = Acc(0);
     for (int t = 0; t <= B + 1; ++t) hs_s[t * kCta + tid] = 0.f;
 
     auto sample = [&](int i) {
         const double xv = P.psamp[i] + (double)x.value(P, i);
-        const double a = P.psum[i] + acc_s[i * kCta + tid];
+        double a = P.psum[i] + as_f64(acc_s[i * kCta + tid]);
+        if constexpr (CMP) {
+            const double ti = (double)P.tau[i];
+            a += fma(ti, fma(ti, zW, zU), zS);
+        }
         const float D = expf((float)(-a * P.dt));
         const float mm = (float)P.m;
         const float L = mm * expm1f((float)xv / mm);
-        acc_s[i * kCta + tid] = (double)(D * ((float)P.payA[i] * L - (float)P.payB[i]));  // cash flow of date i
+        const float cf = D * ((float)P.payA[i] * L - (float)P.payB[i]);
+        acc_s[i * kCta + tid] = (Acc)cf;  // cash flow of date i
     };
 
     sample(1);
@@ -761,10 +777,20 @@ __global__ void __launch_bounds__(kCta, 4)
             x.step(M, phi0, phi1, phi2);
             bs.add(x, phi0, phi1, phi2);
         }
-        // block sums of tenors 2 .. B; fold (b, B] into FP64
-        block_sums_up<NT, POLY>(x, hs_s, tid, kCta, P, bs, B, [&](int t, float Ht) {
-            if (t > b) acc_s[t * kCta + tid] += as_f64(Ht);
-        });
+        // block sums of tenors 2 .. B; fold (b, B] into FP64 (CMP: the
+        // remainder's in FP32, the parts' into their FP64 running sums)
+        if constexpr (CMP) {
+            recover_sums_up<NT>(x.h, hs_s, tid, kCta, P, x.g, 0.f, 0.f, 0.f, bs.H1, B, [&](int t, float Ht) {
+                if (t > b) acc_s[t * kCta + tid] += Ht;
+            });
+            zS += as_f64(bs.sS);
+            zU += as_f64(bs.sU);
+            zW += as_f64(bs.sW);
+        } else {
+            block_sums_up<NT, POLY>(x, hs_s, tid, kCta, P, bs, B, [&](int t, float Ht) {
+                if (t > b) acc_s[t * kCta + tid] += as_f64(Ht);
+            });
+        }
         // the block-end curve (POLY: its convected part) is the next block's start
 #pragma unroll
         for (int t = 1; t < NT; ++t)
@@ -775,11 +801,19 @@ __global__ void __launch_bounds__(kCta, 4)
     mixed_epilogue(P, acc_s, hs_s, red_s, partials, estore, cta_base, active);
 }
 
-__host__ __device__ inline size_t mixed_smem_bytes(int nt, int n_blocks)
+__host__ __device__ inline size_t mixed_smem_bytes(int nt, int n_blocks, bool cmp = false)
 {
     (void)nt;
     const size_t rows = (size_t)n_blocks + 1;
-    return rows * kCta * 8 + (rows + 1) * kCta * 4 + 2 * (kCta / 32) * 8;
+    const size_t head = rows * kCta * (cmp ? 4 : 8) + (rows + 1) * kCta * 4;
+    return ((head + 7) & ~(size_t)7) + 2 * (kCta / 32) * 8;
+}
+
+// The compact sums when the FP64 ones would hold a CTA's shared memory above a
+// quarter of the SM's (fewer than the 4 CTAs the registers allow)
+inline bool mixed_compact(int nt, int n_blocks, bool poly)
+{
+    return poly && mixed_smem_bytes(nt, n_blocks, false) > (size_t)228 * 1024 / 4;
 }
 
 void pack_mixed_params(int nt, const PathParams<float>& P, MixedParams& M)
@@ -1129,8 +1163,9 @@ template <int NT, bool EXT, bool POLY>
 static cudaError_t launch_mixed_t(const MixedParams& M, const double* ext, double* partials, float* estore,
                                   cudaStream_t s)
 {
-    const size_t smem = mixed_smem_bytes(NT, M.P.n_blocks);
-    auto k = path_kernel_mixed<NT, EXT, POLY>;
+    const bool cmp = mixed_compact(NT, M.P.n_blocks, POLY);
+    const size_t smem = mixed_smem_bytes(NT, M.P.n_blocks, cmp);
+    auto k = cmp ? path_kernel_mixed<NT, EXT, POLY, POLY> : path_kernel_mixed<NT, EXT, POLY, false>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const int64_t grid = (M.P.n_paths + kCta - 1) / kCta;
@@ -1160,7 +1195,7 @@ bool path_tenor_supported(int nt) { return nt == 51 || nt == 61; }
 
 size_t path_smem(int nt, int n_blocks, bool mixed)
 {
-    return mixed ? mixed_smem_bytes(nt, n_blocks) : path_smem_bytes(nt, n_blocks, false);
+    return mixed ? mixed_smem_bytes(nt, n_blocks) : path_smem_bytes(nt, n_blocks, false);  // the larger form
 }
 
 int path_cta(bool mixed) { return mixed ? kCta : kFp64Cta; }

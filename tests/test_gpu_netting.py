@@ -79,7 +79,10 @@ def test_netting_adjoint_vs_fp64_finite_differences(engine):
     engine.set_netting_set(ns)
     sens = engine.run_adjoint(cfg, checkpoint_every=32)
     v = engine.run(cfg, "mixed", pfe=False)
-    assert sens.cva == v.cva
+    # with 60 dates the valuation keeps the remainder's discount sums in FP32
+    # beside FP64 sums of the scalar parts (its compact shared memory), the
+    # adjoint's forward pass FP64 sums per tenor: the CVAs agree to rounding
+    assert abs(sens.cva - v.cva) <= 1e-9 * abs(v.cva)
     gmax = np.max(np.abs(sens.dcva_dspot))
     for t in (2, 10, 30, 45, 60):
         h = 1e-5
