@@ -65,22 +65,32 @@ constexpr int kAdjCta = 64;  // paths per CTA of the adjoint kernel
 //   ds_s   (B+1) f32   K = 0: D_i then abar_i;   K > 0: abar_i
 //   cb_s   9 f64       diffusion coefficient adjoints
 //   red_s  (kAdjCta/32) * R f64   CTA reduction
+// With checkpoints (K > 0) xs_s and ds_s are first written after the
+// exposures have consumed the cash flows (a barrier between), so they take
+// acc_s's place: a third less shared memory per CTA, which sets the
+// occupancy when there are many dates.
 struct AdjLayout {
     size_t acc, hs, xs, ds, cb, red, total;
 };
 
 __host__ __device__ inline size_t align128(size_t x) { return (x + 127) & ~(size_t)127; }
 
-__host__ __device__ inline AdjLayout adj_layout(int nt, int B, int R)
+__host__ __device__ inline AdjLayout adj_layout(int nt, int B, int R, bool ckpt = false)
 {
     AdjLayout L;
     (void)nt;
     const size_t rows = (size_t)B + 1;
     L.acc = 0;
     L.hs = align128(rows * 8 * kAdjCta);
-    L.xs = align128(L.hs + (rows + 1) * kAdjCta * 4);
-    L.ds = align128(L.xs + rows * kAdjCta * 4);
-    L.cb = align128(L.ds + rows * kAdjCta * 4);
+    if (ckpt) {
+        L.xs = L.acc;
+        L.ds = L.acc + rows * kAdjCta * 4;
+        L.cb = align128(L.hs + (rows + 1) * kAdjCta * 4);
+    } else {
+        L.xs = align128(L.hs + (rows + 1) * kAdjCta * 4);
+        L.ds = align128(L.xs + rows * kAdjCta * 4);
+        L.cb = align128(L.ds + rows * kAdjCta * 4);
+    }
     L.red = align128(L.cb + (size_t)9 * kAdjCta * 8);
     L.total = align128(L.red + (size_t)(kAdjCta / 32) * R * 8);
     return L;
@@ -143,7 +153,7 @@ __global__ void __launch_bounds__(kAdjCta, adj_min_ctas<NT>())
     const int B = P.n_blocks;
     const int rows = B + 1;
     const int R = 3 * B + 12;
-    const AdjLayout Ly = adj_layout(NT, B, R);
+    const AdjLayout Ly = adj_layout(NT, B, R, CKPT);
     double* acc_s = reinterpret_cast<double*>(smem + Ly.acc);
     float* hs_s = reinterpret_cast<float*>(smem + Ly.hs);
     float* xs_s = reinterpret_cast<float*>(smem + Ly.xs);
@@ -712,7 +722,7 @@ int adjoint_cta() { return kAdjCta; }
 template <int NT, bool CKPT, bool POLY>
 static cudaError_t launch_adj_t(const AdjParams& A, double* partials, float* ck_h, double* ck_a, cudaStream_t s)
 {
-    const size_t smem = adjoint_smem(NT, A.M.P.n_blocks);
+    const size_t smem = adj_layout(NT, A.M.P.n_blocks, 3 * A.M.P.n_blocks + 12, CKPT).total;
     auto k = adjoint_kernel<NT, CKPT, POLY>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
