@@ -401,6 +401,27 @@ def run_ours(args) -> None:
     st = eng.stats()
     h2d = st["h2d_bytes"] + 8 * (mk.spot.size + mk.vol.size + mk.drift.size + sw.accrual.size)
     e2e_value = world * n_paths * n_steps * args.steps / sum(e2e_times)
+    # The warm calls above reuse the context's buffers and its cached response
+    # table (hjm_set_market with unchanged inputs keeps it).  One cold call: a
+    # new context, so its buffers are allocated and the table is built inside
+    # the timed call.
+    t0 = time.perf_counter()
+    with HJMEngine(local_rank) as cold:
+        cold.set_stream(stream.cuda_stream)
+        if is_adjoint:
+            cold.set_market_poly(mk.n_tenor, mk.dtau, mk.spot, mk.vol_coeffs)
+        else:
+            cold.set_market(mk)
+        if args.workload == "netting":
+            cold.set_netting_set(netting)
+        else:
+            cold.set_swap(sw)
+        if is_adjoint:
+            cold.run_adjoint(cfg, checkpoint_every=32)
+        else:
+            cold.run(cfg, prec)
+        cold_s = time.perf_counter() - t0
+    torch.cuda.synchronize()
 
     if rank != 0:
         if dist:
@@ -464,9 +485,9 @@ def run_ours(args) -> None:
         extras["generic_table_step"] = generic_step_run(eng, mk, sw, args, flush, stride, peak64, peak32)
         extras["predictor_corrector"] = predictor_corrector_run(eng, mk, sw, args, flush)
         extras["mlmc"] = mlmc_run(eng, mk, sw)
-        extras["mixed"] = mixed_vs_fp64(eng, mk, sw, args, stream, flush, value)
+        extras["mixed"] = mixed_vs_fp64(eng, mk, sw, args, stream, flush, value, peak32)
         extras["adjoint"] = adjoint_cost(eng, args, flush)
-        extras["netting"] = netting_set_run(eng, args, flush)
+        extras["netting"] = netting_set_run(eng, args, flush, peak32)
     if not args.no_extras:
         cb = cpu_oracle_sample(target_s=3.0, n_threads=os.cpu_count() or 1)
         n_cpu = cb["n_paths"]
@@ -501,10 +522,19 @@ def run_ours(args) -> None:
                                    if form != "table" else
                                    "FP64 (the factors' impulse responses, value and running sum, per date)")
                                   if remainder == "response" and prec == "fp64" else None),
+                   "path_step": ("one Euler step of one path's whole tenor curve, the reference's unit; the "
+                                 "response form computes the same values by exact algebra without evolving every "
+                                 "tenor (fp64_convected_form times the curve-evolving FP64 kernel on the same "
+                                 "paths)"),
                    "parallelism": f"replicas{world}" if world > 1 else "single",
                    "l2": f"flushed between steps ({FLUSH_BYTES >> 20} MiB device write, inside the timed region)"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(st["d2h_bytes"]), "call": "hjm_set_market + hjm_set_swap + hjm_run"},
+                "d2h_bytes_per_step": int(st["d2h_bytes"]), "call": "hjm_set_market + hjm_set_swap + hjm_run",
+                "plan": "warm: the context's buffers and response table (a plan cached per run shape and "
+                        "market) are reused across calls",
+                "cold_call": {"value": world * n_paths * n_steps / cold_s, "unit": UNIT, "ms": 1e3 * cold_s,
+                              "what": "one call on a new context: device buffers allocated and the response "
+                                      "table built inside the timed call"}},
         "gpu_launches": launches,
         "roofline": roofline,
         "cpu_baseline": cpu_baseline,
@@ -521,6 +551,19 @@ def run_ours(args) -> None:
         dist.destroy_process_group()
 
 
+def fp32_roofline(kernel: str, flops_per_launch: float, launch_ms: float, peak32: float | None,
+                  traffic_key: str) -> dict:
+    """The roofline block of an FP32-pipe kernel (mixed precision): algorithmic
+    flops per launch (``algorithmic_flops_per_path``) over the average launch
+    time, against the measured FP32 FMA peak; DRAM traffic per launch from the
+    committed ncu summary."""
+    achieved = flops_per_launch / (launch_ms * 1e-3) / 1e12
+    return {"bound": "fp32_pipe", "achieved": achieved, "peak": peak32, "unit": "TFLOP/s",
+            "frac": (achieved / peak32) if peak32 else None, "traffic": profiled_traffic(traffic_key),
+            "kernel": kernel, "algorithmic_flops_per_launch": flops_per_launch, "avg_launch_ms": launch_ms,
+            "peak_source": "measured live by bench.py (FMA microkernel, this GPU)"}
+
+
 def _measured_hbm():
     f = ROOT / "MEASURED_PEAKS.json"
     try:
@@ -529,7 +572,7 @@ def _measured_hbm():
         return None
 
 
-def mixed_vs_fp64(eng, mk, sw, args, stream, flush, fp64_value) -> dict:
+def mixed_vs_fp64(eng, mk, sw, args, stream, flush, fp64_value, peak32=None) -> dict:
     """Mixed precision at 4,194,304 paths: throughput, and its error against the
     FP64 valuation of the same paths (identical normals)."""
     import numpy as np
@@ -557,9 +600,15 @@ def mixed_vs_fp64(eng, mk, sw, args, stream, flush, fp64_value) -> dict:
     f64_ms = float(eng.timing_history(1)[0, 0])
     rel = np.abs(mx.ee[:20] - f64.ee[:20]) / f64.ee[:20]
     value = n * N_STEPS * args.steps / el
+    stride = int(round(mk.dtau / DT))
+    kern_ms = float(hist[:, 0].mean())
+    form = eng.vol_form()
+    flops = algorithmic_flops_per_path(mk.n_tenor, N_STEPS, stride, form, "convect") * n
     return {
         "value": value, "unit": UNIT, "n_paths": n, "ms_per_step": 1e3 * el / args.steps,
-        "path_kernel_ms": float(hist[:, 0].mean()),
+        "path_kernel_ms": kern_ms,
+        "roofline": fp32_roofline(f"path_kernel_mixed<{mk.n_tenor},philox,{form}>", flops, kern_ms, peak32,
+                                  f"mixed-{n}"),
         "speedup_vs_fp64_path_steps_per_s": value / fp64_value,
         "fp64_same_paths_path_kernel_ms": f64_ms,
         "ee_rel_err_vs_fp64_per_date": [float(x) for x in rel],
@@ -785,7 +834,7 @@ def adjoint_cost(eng, args, flush) -> dict:
     return out
 
 
-def netting_set_run(eng, args, flush) -> dict:
+def netting_set_run(eng, args, flush, peak32=None) -> dict:
     """Config 5: 64 payer/receiver swaps (maturities 1-30y) on a 61-tenor curve,
     3,000 steps, 2,097,152 paths, mixed precision: the netted EE/PFE/CVA
     valuation and the adjoint, each one fused launch (plus reductions)."""
@@ -816,9 +865,14 @@ def netting_set_run(eng, args, flush) -> dict:
         sens = eng.run_adjoint(cfg, checkpoint_every=32)
         ms.append(float(eng.timing_history(1)[0, 3]))
     adj_ms = statistics.median(ms)
+    kern_ms = float(np.median(hist[:, 0]))
+    flops = algorithmic_flops_per_path(61, steps, 50, "poly_tri", "convect") * n
     return {"n_paths": n, "n_steps": steps, "n_tenor": 61, "n_swaps": len(ns), "dates": steps // 50,
             "valuation_ms": val_ms, "path_steps_per_s": n * steps / (val_ms * 1e-3),
-            "path_kernel_ms": float(np.median(hist[:, 0])), "cva": v.cva, "cva_stderr": v.cva_stderr,
+            "path_kernel_ms": kern_ms,
+            "roofline": fp32_roofline("path_kernel_mixed<61,philox,poly_tri,compact>", flops, kern_ms, peak32,
+                                      f"mixed-{n}"),
+            "cva": v.cva, "cva_stderr": v.cva_stderr,
             "adjoint_ms_checkpoint_32": adj_ms, "adjoint_cost_in_valuations": adj_ms / val_ms,
             "adjoint_cva": sens.cva}
 

@@ -29,7 +29,7 @@ N_VOL_COEF = 9
 # every symbol include/hjm_cva.h and include/hjm_dropin.h declare (C linkage)
 EXPORTED = [
     "hjm_version", "hjm_last_error", "hjm_ctx_create", "hjm_ctx_destroy", "hjm_ctx_set_stream",
-    "hjm_ctx_keep_exposures", "hjm_ctx_set_vol_decomposition", "hjm_ctx_set_scheme", "hjm_ctx_vol_decomposition",
+    "hjm_ctx_keep_exposures", "hjm_ctx_set_memory_limit", "hjm_ctx_memory_in_use", "hjm_ctx_set_vol_decomposition", "hjm_ctx_set_scheme", "hjm_ctx_vol_decomposition",
     "hjm_ctx_set_remainder_form", "hjm_ctx_remainder_form", "hjm_set_market", "hjm_set_swap", "hjm_set_netting_set", "hjm_run",
     "hjm_enqueue", "hjm_fetch_results", "hjm_run_with_normals", "hjm_get_exposures", "hjm_set_market_poly", "hjm_calibrate_pca", "hjm_write_report", "hjm_run_mlmc",
     "hjm_run_adjoint", "hjm_dump_normals", "hjm_philox_words", "hjm_last_timings", "hjm_timing_history", "hjm_last_stats", "hjm_measure_fma_peak",
@@ -54,6 +54,8 @@ def _declare(lib: C.CDLL) -> None:
         "hjm_ctx_destroy": (st, [_vp]),
         "hjm_ctx_set_stream": (st, [_vp, _vp]),
         "hjm_ctx_keep_exposures": (st, [_vp, C.c_int32]),
+        "hjm_ctx_set_memory_limit": (st, [_vp, C.c_int64]),
+        "hjm_ctx_memory_in_use": (st, [_vp, C.POINTER(C.c_int64)]),
         "hjm_ctx_set_vol_decomposition": (st, [_vp, C.c_int32]),
         "hjm_ctx_set_scheme": (st, [_vp, C.c_int32]),
         "hjm_ctx_set_remainder_form": (st, [_vp, C.c_int32]),

@@ -709,7 +709,7 @@ cudaError_t launch_adjoint_pc(int nt, const PcParams<float>& Q, bool poly, doubl
     return cudaErrorInvalidValue;
 }
 
-size_t adjoint_smem(int nt, int n_blocks) { return adj_layout(nt, n_blocks, 3 * n_blocks + 12).total; }
+size_t adjoint_smem(int nt, int n_blocks, bool ckpt) { return adj_layout(nt, n_blocks, 3 * n_blocks + 12, ckpt).total; }
 
 int adjoint_columns(int nt, int n_blocks)
 {
@@ -722,7 +722,7 @@ int adjoint_cta() { return kAdjCta; }
 template <int NT, bool CKPT, bool POLY>
 static cudaError_t launch_adj_t(const AdjParams& A, double* partials, float* ck_h, double* ck_a, cudaStream_t s)
 {
-    const size_t smem = adj_layout(NT, A.M.P.n_blocks, 3 * A.M.P.n_blocks + 12, CKPT).total;
+    const size_t smem = adjoint_smem(NT, A.M.P.n_blocks, CKPT);
     auto k = adjoint_kernel<NT, CKPT, POLY>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -26,22 +27,38 @@ namespace {
 
 thread_local std::string g_thread_error;
 
+// Device bytes a context's buffers hold, and the cap a caller may set on them
+// (hjm_ctx_set_memory_limit; 0 = none).
+struct MemBudget {
+    size_t limit = 0;
+    size_t used = 0;
+};
+
 struct DevBuf {
     void* p = nullptr;
     size_t bytes = 0;
+    MemBudget* budget = nullptr;
+    // Grow to at least need bytes (contents not kept).  A growth past the
+    // budget's cap fails as an allocation failure would, before anything is
+    // freed, so the buffer and the context stay as they were.
     cudaError_t ensure(size_t need)
     {
         if (need <= bytes) return cudaSuccess;
-        if (p) cudaFree(p);
-        p = nullptr;
-        bytes = 0;
+        if (budget && budget->limit && budget->used - bytes + need > budget->limit) return cudaErrorMemoryAllocation;
+        release();
         cudaError_t e = cudaMalloc(&p, need);
-        if (e == cudaSuccess) bytes = need;
+        if (e == cudaSuccess) {
+            bytes = need;
+            if (budget) budget->used += need;
+        } else {
+            p = nullptr;
+        }
         return e;
     }
     void release()
     {
         if (p) cudaFree(p);
+        if (budget) budget->used -= bytes;
         p = nullptr;
         bytes = 0;
     }
@@ -82,6 +99,16 @@ struct hjm_ctx {
 
     // device buffers
     DevBuf partials, sums, result, estore, sel, hist, ext, ext_raw, wide, scratch, ck_h, ck_a, resp, vresp;
+    MemBudget budget;
+    hjm_ctx()
+    {
+        for (DevBuf* b : buffers()) b->budget = &budget;
+    }
+    std::array<DevBuf*, 14> buffers()
+    {
+        return {&partials, &sums, &result, &estore, &sel, &hist, &ext, &ext_raw, &wide, &scratch, &ck_h, &ck_a,
+                &resp, &vresp};
+    }
     // the response table in resp holds the run shape of resp_key; resp_used
     // is recorded after the last kernel that reads it
     struct RespKey {  // the response table in resp, with the parts' frame coefficients
@@ -216,9 +243,7 @@ hjm_status hjm_ctx_destroy(hjm_ctx* ctx)
     if (!ctx) return HJM_OK;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
-    for (DevBuf* b : {&ctx->partials, &ctx->sums, &ctx->result, &ctx->estore, &ctx->sel, &ctx->hist, &ctx->ext,
-                      &ctx->ext_raw, &ctx->wide, &ctx->scratch, &ctx->ck_h, &ctx->ck_a, &ctx->resp, &ctx->vresp})
-        b->release();
+    for (DevBuf* b : ctx->buffers()) b->release();
     if (ctx->resp_used) cudaEventDestroy(ctx->resp_used);
     for (auto& q : ctx->ring)
         for (auto& ev : q)
@@ -232,6 +257,22 @@ hjm_status hjm_ctx_set_stream(hjm_ctx* ctx, void* cuda_stream)
 {
     HJM_CHECK_CTX(ctx);
     ctx->stream = cuda_stream ? (cudaStream_t)cuda_stream : ctx->own_stream;
+    return HJM_OK;
+}
+
+hjm_status hjm_ctx_set_memory_limit(hjm_ctx* ctx, int64_t bytes)
+{
+    HJM_CHECK_CTX(ctx);
+    if (bytes < 0) return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "memory limit %lld < 0", (long long)bytes);
+    ctx->budget.limit = (size_t)bytes;
+    return HJM_OK;
+}
+
+hjm_status hjm_ctx_memory_in_use(hjm_ctx* ctx, int64_t* bytes)
+{
+    HJM_CHECK_CTX(ctx);
+    if (!bytes) return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "bytes is null");
+    *bytes = (int64_t)ctx->budget.used;
     return HJM_OK;
 }
 
@@ -1124,7 +1165,7 @@ hjm_status hjm_run_adjoint(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, doubl
                     "volatility-coefficient sensitivities need a polynomial market (hjm_set_market_poly)");
     const int nt = ctx->nt, B = sh.B;
     const int R = adjoint_columns(nt, B);
-    const size_t smem = pc ? adjoint_pc_smem(nt, B) : adjoint_smem(nt, B);
+    const size_t smem = pc ? adjoint_pc_smem(nt, B) : adjoint_smem(nt, B, checkpoint_every > 0);
     if (smem > 227 * 1024) return fail(ctx, HJM_ERR_UNSUPPORTED, "adjoint shared memory %zu B exceeds 227 KB", smem);
     HJM_CUDA(ctx, cudaSetDevice(ctx->device));
     const int64_t n_ctas = (n_paths + adjoint_cta() - 1) / adjoint_cta();

@@ -45,11 +45,22 @@ void run_dropin(real* expected_exposure, const InterestRateSwap<real>& payOff, c
         mu[t] = drift[t];
     }
     for (int t = 0; t < 3 * kTimepoints; ++t) vol[t] = volatilities[t];
-    const double ddt = (double)dt;
-    // pathN = expiry / dt (simulation_gpu.cu:959), rounded when within 1e-9 of an integer
+    // Step counts are ratios of the caller's reals, rounded to the nearest
+    // integer when within the reals' rounding of one (relative 1e-9 for
+    // double, 1e-6 for float: 0.5f / 0.01f is 50.0000011 in double).  A float
+    // dt is then taken as dtau / stride exactly, the step the caller meant
+    // (the reference's float path computes (int)(dtau/dt) = 50 in float).
+    const double tol = sizeof(real) == sizeof(float) ? 1e-6 : 1e-9;
+    double ddt = (double)dt;
+    if (sizeof(real) == sizeof(float) && ddt > 0.0) {
+        const double r = (double)payOff.dtau / ddt;
+        const long rs = std::lround(r);
+        if (rs >= 1 && std::fabs(r - (double)rs) <= tol * r) ddt = (double)payOff.dtau / (double)rs;
+    }
+    // pathN = expiry / dt (simulation_gpu.cu:959)
     const double ratio = (double)payOff.expiry / ddt;
     const long rn = std::lround(ratio);
-    const int n_steps = (std::fabs(ratio - (double)rn) <= 1e-9 * ratio) ? (int)rn : (int)ratio;
+    const int n_steps = (std::fabs(ratio - (double)rn) <= tol * ratio) ? (int)rn : (int)ratio;
 
     std::lock_guard<std::mutex> lock(g_mu);
     hjm_status st = HJM_OK;

@@ -73,7 +73,7 @@ __host__ __device__ inline size_t path_smem_bytes(int nt, int n_blocks, bool mix
 // With the growth scaling of PathParams (v = h / (1-c)^j) the convection is
 // one FMA per tenor, and the table form four.
 // FORM: kFormTable (volatility table), kFormPoly (quadratic factors) or
-// kFormPolyTri (factor k of degree <= k, the reference's own table: the noise
+// kFormPolyTri (factor k of degree <= k, as the synthetic workloads' factors: the noise
 // projection then skips the three zero coefficients).
 template <int NT, bool EXT, int FORM>
 __global__ void __launch_bounds__(kFp64Cta, 4)

@@ -176,7 +176,7 @@ struct AdjParams {
     int ckpt_every;                // 0: no checkpoints; else K in [1, stride]
     int64_t ck_ld;                 // row stride of the checkpoint arrays
 };
-size_t adjoint_smem(int nt, int n_blocks);
+size_t adjoint_smem(int nt, int n_blocks, bool ckpt);  // ckpt: the checkpoint mode's layout
 int adjoint_columns(int nt, int n_blocks);
 int adjoint_cta();  // paths per CTA of the adjoint kernel (one partial-sum row each)
 cudaError_t launch_adjoint(int nt, const AdjParams& A, bool poly, double* partials, float* ck_h, double* ck_a,

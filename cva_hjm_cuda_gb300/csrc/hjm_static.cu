@@ -18,13 +18,17 @@
 // cudaGetSymbolAddress, with that device current, and passes it to the same
 // path and reduction kernels that hjm_run launches.
 //
-// FP64 runs take a response form when its table fits a second static array
-// (4 MB; recomputed on the device at every call), as hjm_run does: with a
-// volatility table whose factors are quadratics (the reference's), the
-// polynomial decomposition's remainder in double-FP32 impulse-response sums
-// (12x the convected table step), else the whole stochastic curve as FP64 sums
-// of the three factors' responses (3x; with 20 dates up to ~180 steps per
-// date).  Larger runs, and mixed precision, take the convected table step.
+// A volatility table whose factors are quadratics in T (the synthetic
+// factors of the configured workloads) runs the polynomial decomposition in
+// both precisions, as hjm_run does.  FP64 runs take a response form whenever
+// its table fits a second static array (4 MB; recomputed on the device at
+// every call; hjm_run weighs the response form against convection by the
+// run's operation counts, which favour it for these shapes anyway): with
+// quadratic factors the decomposition's remainder in double-FP32
+// impulse-response sums (12x the convected table step), else the whole
+// stochastic curve as FP64 sums of the three factors' responses (3x; with 20
+// dates up to ~180 steps per date).  Larger FP64 runs take the convected step
+// (decomposed or table), mixed precision always the convected pairs.
 //
 // Limits: at most HJM_STATIC_MAX_PATHS paths per call; EE and CVA only (the
 // per-path exposure store a PFE needs would not fit a modest static buffer).
@@ -172,8 +176,11 @@ static void static_params(int nt, double dtau, const double* spot, const double*
         F.dcvaw[j] = (1.0 - recovery) * (-t0 * e0 + t1 * e1);
     }
     P.c = (T)(dt / dtau);
-    P.k2 = dt * dtau;
+    // c dtau and c dtau^2 rounded as hjm_run forms them (fill_params)
+    P.k1 = (dt / dtau) * dtau;
+    P.k2 = (dt / dtau) * dtau * dtau;
     fill_growth_scale(P, dt / dtau, P.k2, stride, B);
+    for (int t = 0; t < nt; ++t) P.tau[t] = (T)(dtau * t);
     P.dt = dt;
     P.m = 1.0 / dtau;
     P.inv_m = dtau;
@@ -277,30 +284,34 @@ hjm_status hjm_run_static(void* cuda_stream, int32_t n_tenor, double dtau, const
 
     STATIC_CUDA(cudaMemsetAsync(result, 0, sizeof(double) * kResLen, s));
     FinalParams F;
+    // quadratic factors: the polynomial decomposition's coefficients
+    // sqrt(dt) c_{k,d}, as hjm_run's fill_params
+    double coef[HJM_N_VOL_COEF];
+    const bool poly = fit_quadratic_vols(vol_host, n_tenor, dtau, coef);
+    const double sq = std::sqrt(dt);
     if (precision == HJM_PRECISION_MIXED) {
         PathParams<float> P;
         static_params<float>(n_tenor, dtau, spot_host, vol_host, drift, payA, payB, (int)stride, B, n_paths, dt, seed,
                              path_offset, hazard_rate, recovery, P, F);
+        if (poly)
+            for (int k = 0; k < kFactors; ++k)
+                for (int d = 0; d < 3; ++d) P.svc[k][d] = sq * coef[k * 3 + d];
         MixedParams M;
         pack_mixed_params(n_tenor, P, M);
-        STATIC_CUDA(launch_path_mixed(n_tenor, M, false, nullptr, partials, nullptr, s));
+        STATIC_CUDA(launch_path_mixed(n_tenor, M, poly, nullptr, partials, nullptr, s));
     } else {
         PathParams<double> P;
         static_params<double>(n_tenor, dtau, spot_host, vol_host, drift, payA, payB, (int)stride, B, n_paths, dt,
                               seed, path_offset, hazard_rate, recovery, P, F);
-        double coef[HJM_N_VOL_COEF];
-        const bool poly = fit_quadratic_vols(vol_host, n_tenor, dtau, coef);
+        if (poly)
+            for (int k = 0; k < kFactors; ++k)
+                for (int d = 0; d < 3; ++d) P.svc[k][d] = sq * coef[k * 3 + d];
         const size_t entries = response_table_vol_elems((int)stride, B);
         if (poly && B >= 2 && B <= response_max_dates() && response_table_elems((int)stride, B) <= kStaticRespEntries) {
             // the decomposition: the remainder's table and the coefficients of
             // S, U, W (FP32 pairs, 16 bytes per entry like the double2 array)
             // in the static array
-            const double sq = std::sqrt(dt), c = dt / dtau;
-            for (int k = 0; k < kFactors; ++k)
-                for (int d = 0; d < 3; ++d) P.svc[k][d] = sq * coef[k * 3 + d];
-            P.k1 = c * dtau;
-            P.k2 = c * dtau * dtau;
-            for (int t = 0; t < n_tenor; ++t) P.tau[t] = dtau * t;
+            const double c = dt / dtau;
             float4* table = reinterpret_cast<float4*>(resp_table);
             STATIC_CUDA(cudaMemsetAsync(table, 0, sizeof(float4) * response_table_elems((int)stride, B), s));
             STATIC_CUDA(launch_response_table(n_tenor, c, (int)stride, B, false, 0.0, -2.0 * P.k2, 0.0, table, s));
@@ -313,7 +324,7 @@ hjm_status hjm_run_static(void* cuda_stream, int32_t n_tenor, double dtau, const
             STATIC_CUDA(launch_response_table_vol(n_tenor, dt / dtau, (int)stride, B, false, &P.sv[0][0], resp_table, s));
             STATIC_CUDA(launch_path_fp64_vresp(n_tenor, P, resp_table, nullptr, partials, nullptr, s));
         } else {
-            STATIC_CUDA(launch_path_fp64(n_tenor, P, false, nullptr, nullptr, partials, nullptr, s));
+            STATIC_CUDA(launch_path_fp64(n_tenor, P, poly, nullptr, nullptr, partials, nullptr, s));
         }
     }
     STATIC_CUDA(launch_reduce(partials, n_ctas, R, sums, F, result, s));

@@ -88,6 +88,16 @@ class HJMEngine:
     def keep_exposures(self, keep: bool = True) -> None:
         self._check(self.lib.hjm_ctx_keep_exposures(self.ctx, 1 if keep else 0))
 
+    def set_memory_limit(self, n_bytes: int) -> None:
+        """Cap the device memory of this engine's buffers (0: no cap); a call that
+        would grow past it raises HJMError with status HJM_ERR_OUT_OF_MEMORY (4)."""
+        self._check(self.lib.hjm_ctx_set_memory_limit(self.ctx, int(n_bytes)))
+
+    def memory_in_use(self) -> int:
+        v = C.c_int64(0)
+        self._check(self.lib.hjm_ctx_memory_in_use(self.ctx, C.byref(v)))
+        return v.value
+
     def run_mlmc(self, n_paths_per_level, n_steps: int = 1000, dt: float = 0.01, seed: int = 1234,
                  hazard: float = 0.02, recovery: float = 0.4) -> dict:
         """Multi-level Monte Carlo EE / CVA: level l uses dt / 2^l on

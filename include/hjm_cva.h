@@ -77,6 +77,16 @@ hjm_status hjm_ctx_destroy(hjm_ctx* ctx);
  * (NULL restores the context's stream). */
 hjm_status hjm_ctx_set_stream(hjm_ctx* ctx, void* cuda_stream);
 
+/* Cap on the device memory the context's buffers may hold, in bytes (0, the
+ * default: no cap).  A call whose buffers would grow past it fails with
+ * HJM_ERR_OUT_OF_MEMORY before anything is allocated or freed, exactly as a
+ * failed cudaMalloc is reported; the context stays usable (a later call that
+ * fits, or one after the cap is raised, runs normally).  Buffers already held
+ * are kept when the cap is lowered.  hjm_ctx_memory_in_use reports the bytes
+ * held now. */
+hjm_status hjm_ctx_set_memory_limit(hjm_ctx* ctx, int64_t bytes);
+hjm_status hjm_ctx_memory_in_use(hjm_ctx* ctx, int64_t* bytes);
+
 /* Keep the per-path exposures of every valuation on the device (for
  * hjm_get_exposures); they are always kept when a PFE is requested. */
 hjm_status hjm_ctx_keep_exposures(hjm_ctx* ctx, int32_t keep);
@@ -95,7 +105,7 @@ hjm_status hjm_ctx_set_scheme(hjm_ctx* ctx, int32_t scheme);
 /* Polynomial volatility decomposition.  When every volatility factor is a
  * polynomial of degree <= 2 in the tenor T (given by hjm_set_market_poly, or a
  * table that hjm_set_market finds to be one to 1e-12 of each row's scale, as
- * the reference's own table simulation_gpu_testing.cpp:47-63 is), the kernels
+ * the configured workloads' synthetic factors are), the kernels
  * carry the stochastic curve as S + U T + W T^2 plus a remainder driven only at
  * the last tenor, instead of adding the three factor columns to every tenor
  * each step (simulation_gpu.cu:153-180).  enable = 0 forces the generic
@@ -262,10 +272,12 @@ hjm_status hjm_run_adjoint(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, doubl
  * the device-wide synchronisation a cudaMalloc/cudaFree may cause.  No
  * context: all inputs are host arrays (as for hjm_set_market / hjm_set_swap /
  * hjm_run), the work is enqueued on cuda_stream (NULL = the legacy default
- * stream) and the call returns when ee_out [n_tenor] and cva_out
- * [HJM_CVA_OUT_LEN] hold the results.  Its scratch is a fixed 8.4 MB static
- * device array that each GPU loading the library keeps until exit; it calls
- * no cudaMalloc, cudaFree or allocating library routine.  Limits: at most
+ * stream) and the call is synchronous: it waits for cuda_stream and returns
+ * when ee_out [n_tenor] and cva_out [HJM_CVA_OUT_LEN] hold the results.  Its
+ * device memory is two fixed static arrays that each GPU loading the library
+ * keeps until exit: 8.4 MB of scratch and 4 MB for the FP64 response table,
+ * about 12.4 MB in all; it calls no cudaMalloc, cudaFree or allocating
+ * library routine.  Limits: at most
  * HJM_STATIC_MAX_PATHS paths per call (larger runs fail with
  * HJM_ERR_INVALID_ARGUMENT), EE and CVA only (no PFE).  The first call on a
  * device looks up the scratch address (cudaGetSymbolAddress): make that first

@@ -37,6 +37,13 @@ def golden_25y():
     return load_golden("ref_driver_25y.json")
 
 
+@pytest.fixture(scope="session")
+def golden_own():
+    """The reference driver's own workload (its curve, PCA volatility table,
+    drift table, irregular accruals; N = 10, K = 6.7%, 25y; 5,000 paths)."""
+    return load_golden("ref_driver_own_market.json")
+
+
 def market_from_golden(g: dict):
     from cva_hjm_cuda_gb300.market import Market, Swap
 

@@ -20,13 +20,14 @@ ROOT = Path(__file__).resolve().parents[1]
 ORACLE_DIR = ROOT / "oracle"
 ORACLE_SO = ORACLE_DIR / "_build" / "libhjm_oracle.so"
 REF_SO = ORACLE_DIR / "_ref" / "libhjm_ref.so"
-REFERENCE_TREE = Path("/root/reference")
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 
 
 def build_oracle(with_ref: bool = False) -> None:
-    targets = ["oracle"] + (["ref"] if with_ref and REFERENCE_TREE.exists() else [])
+    """Build the oracle and, with with_ref, the reference's own CPU path where
+    its source tree is present (the Makefile's REF, from HJM_REFERENCE_DIR)."""
+    targets = ["oracle"] + (["ref-if-present"] if with_ref else [])
     subprocess.run(["make", "-s", "-C", str(ORACLE_DIR), *targets], check=True)
 
 
@@ -82,15 +83,21 @@ _ref = None
 
 
 def ref_available() -> bool:
-    return REF_SO.exists() or REFERENCE_TREE.exists()
+    """Whether the reference's CPU path is built (or can be: its tree is present)."""
+    if not REF_SO.exists():
+        try:
+            build_oracle(with_ref=True)
+        except (OSError, subprocess.CalledProcessError):
+            return False
+    return REF_SO.exists()
 
 
 def ref() -> C.CDLL:
     """The reference's own CPU path (only where the reference tree is present)."""
     global _ref
     if _ref is None:
-        if not REF_SO.exists():
-            build_oracle(with_ref=True)
+        if not ref_available():
+            raise OSError("the reference's CPU path is not built and its source tree is absent")
         lib = C.CDLL(str(REF_SO))
         lib.ref_exposure_paths.restype = C.c_int
         lib.ref_exposure_paths.argtypes = [C.c_int, _dp, _dp, _dp, _dp, C.c_double, C.c_double, C.c_int, _dp, _dp, _dp]

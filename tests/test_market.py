@@ -1,16 +1,12 @@
 """Host-side inputs: the synthetic market, the trapezoid drift, quantile ranks."""
 from __future__ import annotations
 
-import re
-from pathlib import Path
-
 import numpy as np
 import pytest
 
 import oracle_lib as O
+from conftest import load_golden
 from cva_hjm_cuda_gb300.market import Market, Swap, nelson_siegel_curve, poly_vols, quantile_rank, trapezoid_drift
-
-REF_DRIVER = Path("/root/reference/simulation_gpu_testing.cpp")
 
 
 def test_market_shapes_and_forms():
@@ -31,19 +27,13 @@ def test_drift_matches_oracle_trapezoid():
     np.testing.assert_allclose(trapezoid_drift(mk.vol, 0.5), O.trapezoid_drift(mk.vol, 0.5), rtol=1e-14, atol=1e-20)
 
 
-def _parse_array(src: str, name: str) -> np.ndarray:
-    m = re.search(r"real\s+" + name + r"\[\d+\]\s*=\s*\{(.*?)\};", src, re.S)
-    return np.array([float(x) for x in m.group(1).replace("\n", " ").split(",") if x.strip()])
-
-
-@pytest.mark.skipif(not REF_DRIVER.exists(), reason="reference tree not present")
 def test_trapezoid_drift_reproduces_reference_drift_table():
     """The reference passes a pre-computed drift (simulation_gpu_testing.cpp:66-71) for its
-    PCA volatility table (:47-63); the trapezoid rule reproduces it to the table's
-    printed precision (7 decimals)."""
-    src = REF_DRIVER.read_text()
-    vol = _parse_array(src, "volatilities").reshape(3, 51)
-    drift = _parse_array(src, "drifts")
+    PCA volatility table (:47-63), both stored verbatim in the driver's golden fixture; the
+    trapezoid rule reproduces it to the table's printed precision (7 decimals)."""
+    g = load_golden("ref_driver_own_market.json")
+    vol = np.array(g["vol"]).reshape(3, 51)
+    drift = np.array(g["drift"])
     mine = trapezoid_drift(vol, 0.5)
     assert np.max(np.abs(mine - drift)) < 2e-7
 

@@ -24,6 +24,21 @@ def test_oracle_matches_reference_driver_25y(golden_25y):
     np.testing.assert_allclose(ee, ref, rtol=1e-13, atol=0)
 
 
+def test_oracle_matches_reference_driver_own_market(golden_own):
+    """The reference driver's own run (simulation_gpu_testing.cpp -cpu -scenarios 5000): its BoE
+    curve, cubic PCA volatility table, hard-coded drift table, irregular accruals, N = 10,
+    K = 6.7%, 25y; EE from the unmodified calculateExposureCPU<double>."""
+    g = golden_own
+    mk, sw = market_from_golden(g)
+    normals = _curand_normals(g)
+    x = O.exposure_paths(mk, sw, g["n_steps"], g["dt"], normals)
+    np.testing.assert_array_equal(x[:16], np.array(g["exposures_first_paths"]))
+    ee, ref = O.expected_exposure(x), np.array(g["ee"])
+    np.testing.assert_allclose(ee, ref, rtol=1e-13, atol=0)
+    assert abs(ref[0] - 0.122920) < 5e-7  # the driver's printed first EE value
+    assert ref[50] == 0.0 and np.all(ref[:50] > 0.0)  # the 25y swap's last date has no cash flow left
+
+
 def test_oracle_matches_reference_blocks_10y(golden_10y):
     """The reference's per-path functions over a 10y swap (zeroed numeraires)."""
     g = golden_10y

@@ -99,6 +99,50 @@ def test_static_fp64_response_and_fallback_match_hjm_run(case):
 
 
 @pytest.mark.skipif(not _have_gpu(), reason="no CUDA device")
+@pytest.mark.parametrize("precision,rtol", [("fp64", FP64_RTOL), ("mixed", MIXED_RTOL)])
+def test_static_entry_matches_oracle(precision, rtol):
+    """hjm_run_static against the oracle directly (5,000 paths of the 10y swap), on the
+    device's own normals: its parity does not rest on hjm_run."""
+    import oracle_lib as O
+    from cva_hjm_cuda_gb300.engine import HJMEngine
+
+    lib = _lib.load()
+    mk, sw = Market(), Swap()
+    cfg = RunConfig(n_paths=5000, n_steps=1000, dt=0.01, seed=1234, path_offset=3)
+    with HJMEngine(0) as eng:
+        normals = eng.dump_normals(cfg.n_paths, cfg.n_steps, cfg.seed, cfg.path_offset)
+    x = O.exposure_paths(mk, sw, cfg.n_steps, cfg.dt, normals)
+    ee = O.expected_exposure(x)
+    cva, dcva = O.cva(ee, 21, mk.dtau, cfg.hazard, cfg.recovery)
+    st, ee_s, cva_s = _run_static(lib, mk, sw, cfg, precision)
+    assert st == 0, lib.hjm_last_error(None)
+    np.testing.assert_allclose(ee_s[:20], ee[:20], rtol=rtol, atol=0)
+    assert np.all(ee_s[20:] == 0.0)
+    assert abs(cva_s[0] - cva) <= rtol * cva
+    assert abs(cva_s[2] - dcva) <= rtol * abs(dcva)
+
+
+@pytest.mark.skipif(not _have_gpu(), reason="no CUDA device")
+def test_static_mixed_runs_the_decomposition_like_hjm_run():
+    """With quadratic factors the static mixed run takes the polynomial decomposition, as
+    hjm_run does, and gives hjm_run's results to rounding."""
+    from cva_hjm_cuda_gb300.engine import HJMEngine
+
+    lib = _lib.load()
+    mk, sw = Market(), Swap()
+    cfg = RunConfig(n_paths=30_000, seed=99)
+    with HJMEngine(0) as eng:
+        eng.set_market(mk)
+        eng.set_swap(sw)
+        assert eng.vol_decomposition() > 0
+        ref = eng.run(cfg, "mixed", pfe=False)
+    st, ee, cva = _run_static(lib, mk, sw, cfg, "mixed")
+    assert st == 0, lib.hjm_last_error(None)
+    np.testing.assert_allclose(ee, ref.ee, rtol=1e-12, atol=0)
+    assert abs(cva[0] - ref.cva) <= 1e-12 * ref.cva
+
+
+@pytest.mark.skipif(not _have_gpu(), reason="no CUDA device")
 def test_static_entry_rejects_oversize_runs():
     lib = _lib.load()
     mk, sw = Market(), Swap()
