@@ -483,6 +483,9 @@ def run_ours(args) -> None:
         if remainder == "response":
             extras["fp64_convected_form"] = convected_form_run(eng, mk, sw, args, flush, stride, peak64, res)
         extras["generic_table_step"] = generic_step_run(eng, mk, sw, args, flush, stride, peak64, peak32)
+        extras["reference_table"] = reference_table_run(eng, args, flush)
+        eng.set_market(mk)
+        eng.set_swap(sw)
         extras["predictor_corrector"] = predictor_corrector_run(eng, mk, sw, args, flush)
         extras["mlmc"] = mlmc_run(eng, mk, sw)
         extras["mixed"] = mixed_vs_fp64(eng, mk, sw, args, stream, flush, value, peak32)
@@ -570,6 +573,55 @@ def _measured_hbm():
         return json.loads(f.read_text()).get("hbm_gbs")
     except (OSError, ValueError):
         return None
+
+
+def reference_table_run(eng, args, flush) -> dict:
+    """The reference driver's own volatility table (simulation_gpu_testing.cpp:47-63,
+    cubic factors to its 9-decimal rounding, read from the committed golden fixture)
+    in FP64 on 1,048,576 paths: the 10y payer swap of the headline (20 dates, one
+    window) and the driver's own 25y swap (N = 10, K = 6.7%, its accruals and
+    spot curve; 50 dates, three windows), each in the cubic response form and in
+    the convected table step on the same paths."""
+    import numpy as np
+    import torch
+
+    from cva_hjm_cuda_gb300 import RunConfig
+    from cva_hjm_cuda_gb300.market import Market, Swap
+
+    g = json.loads((ROOT / "tests" / "golden" / "ref_driver_own_market.json").read_text())
+    vol = np.array(g["vol"]).reshape(3, 51)
+    own = Market(n_tenor=51, dtau=0.5, spot=np.array(g["spot"]), vol=vol, drift=np.array(g["drift"]))
+    drv = Swap(notional=g["notional"], strike=g["strike"], n_tenor=51, dtau=0.5, accrual=np.array(g["accrual"]))
+    n = WORKLOADS["fp64"]["n_paths"]
+    out = {}
+    for label, mk, sw, n_steps in (("10y_swap", Market(vol=vol), Swap(), 1000), ("driver_25y_swap", own, drv, 2500)):
+        eng.set_market(mk)
+        eng.set_swap(sw)
+        cfg = RunConfig(n_paths=n, n_steps=n_steps, dt=DT, seed=SEED)
+        res = {"n_paths": n, "n_steps": n_steps, "dates": n_steps // 50, "vol_form": eng.vol_form()}
+        for form, steps in (("auto", args.steps), ("convect", 2)):
+            eng.set_remainder_form(form)
+            for _ in range(2 if form == "convect" else args.warmup):
+                eng.enqueue(cfg, "fp64", pfe=False)
+                flush.zero_()
+            torch.cuda.synchronize()
+            for _ in range(steps):
+                eng.enqueue(cfg, "fp64", pfe=False)
+                flush.zero_()
+            torch.cuda.synchronize()
+            hist = eng.timing_history(steps)
+            r = eng.fetch()
+            key = "response_form" if form == "auto" else "convected_table_step"
+            res[key] = {"remainder": eng.remainder_form(), "path_kernel_ms": float(hist[:, 0].mean()),
+                        "device_ms_per_step": float(hist[:, 3].mean()),
+                        "path_steps_per_s": n * n_steps / (float(hist[:, 3].mean()) * 1e-3), "cva": r.cva,
+                        "ee": [float(x) for x in r.ee[: n_steps // 50]]}
+        eng.set_remainder_form("auto")
+        a, b = np.array(res["response_form"]["ee"]), np.array(res["convected_table_step"]["ee"])
+        res["ee_max_rel_diff"] = float(np.max(np.abs(a - b) / np.abs(b)))
+        res["speedup"] = res["response_form"]["path_steps_per_s"] / res["convected_table_step"]["path_steps_per_s"]
+        out[label] = res
+    return out
 
 
 def mixed_vs_fp64(eng, mk, sw, args, stream, flush, fp64_value, peak32=None) -> dict:

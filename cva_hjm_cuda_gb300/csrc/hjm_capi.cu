@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "../../include/hjm_cva.h"
+#include "hjm_eresp.h"
 #include "hjm_kernels.h"
 
 using namespace hjm;
@@ -84,6 +85,12 @@ struct hjm_ctx {
     bool have_poly = false;       // coefficients given by hjm_set_market_poly (sensitivities)
     bool poly_path = false;       // the kernels run the polynomial decomposition (coef)
     bool allow_poly_path = true;  // hjm_ctx_set_vol_decomposition
+    // cubic factors up to a small residual table (a PCA table printed to a
+    // few decimals): the FP64 Euler response form's decomposition
+    bool cubic_path = false;
+    double cubic[HJM_N_FACTOR][4] = {};  // coefficients of (T - T_L)^d
+    int cubic_degs[HJM_N_FACTOR] = {};
+    std::vector<double> resid;            // [3][nt] sigma_k - cubic_k (unscaled)
     int scheme = HJM_SCHEME_EULER;  // hjm_ctx_set_scheme
     int remainder = HJM_REMAINDER_AUTO;  // hjm_ctx_set_remainder_form
     int nt = 0;
@@ -98,16 +105,17 @@ struct hjm_ctx {
     bool keep_exposures = false;
 
     // device buffers
-    DevBuf partials, sums, result, estore, sel, hist, ext, ext_raw, wide, scratch, ck_h, ck_a, resp, vresp;
+    DevBuf partials, sums, result, estore, sel, hist, ext, ext_raw, wide, scratch, ck_h, ck_a, resp, vresp, eresp,
+        carry;
     MemBudget budget;
     hjm_ctx()
     {
         for (DevBuf* b : buffers()) b->budget = &budget;
     }
-    std::array<DevBuf*, 14> buffers()
+    std::array<DevBuf*, 16> buffers()
     {
         return {&partials, &sums, &result, &estore, &sel, &hist, &ext, &ext_raw, &wide, &scratch, &ck_h, &ck_a,
-                &resp, &vresp};
+                &resp, &vresp, &eresp, &carry};
     }
     // the response table in resp holds the run shape of resp_key; resp_used
     // is recorded after the last kernel that reads it
@@ -117,6 +125,13 @@ struct hjm_ctx {
         double c = 0, dtau = 0;
         PartsFrame frame = {};
     } resp_key;
+    struct ErespKey {  // the Euler response form's table in eresp
+        bool valid = false;
+        int nt = 0, stride = 0, B = 0, np = 0, nres = 0;
+        double c = 0, dtau = 0;
+        std::vector<EulerRespFrame> frames;  // one per window
+        std::vector<double> resid;  // sqrt(dt)-scaled, empty without a residual
+    } eresp_key;
     struct VrespKey {  // the volatility-table response table in vresp
         bool valid = false;
         int nt = 0, stride = 0, B = 0, scheme = 0;
@@ -285,10 +300,16 @@ hjm_status hjm_ctx_keep_exposures(hjm_ctx* ctx, int32_t keep)
 
 static bool use_poly_path(const hjm_ctx* ctx) { return ctx->poly_path && ctx->allow_poly_path; }
 
-// 0: table step, 1: quadratic factors, 2: factor k of degree <= k
+static bool use_cubic_path(const hjm_ctx* ctx) { return !ctx->poly_path && ctx->cubic_path && ctx->allow_poly_path; }
+
+// 0: table step, 1: quadratic factors, 2: factor k of degree <= k, 3: cubic
+// factors with a residual table (FP64 Euler valuations; the other modes run
+// the table step on such a market)
 static int vol_form_code(const hjm_ctx* ctx)
 {
-    if (!(ctx->have_market && use_poly_path(ctx))) return 0;
+    if (!ctx->have_market) return 0;
+    if (use_cubic_path(ctx)) return 3;
+    if (!use_poly_path(ctx)) return 0;
     return (ctx->coef[1] == 0.0 && ctx->coef[2] == 0.0 && ctx->coef[5] == 0.0) ? 2 : 1;
 }
 
@@ -374,6 +395,84 @@ __attribute__((visibility("hidden"))) bool fit_quadratic_vols(const double* vol,
     }
     return true;
 }
+
+// Cubic factors up to a residual table.  Each factor row is fitted by least
+// squares (modified Gram-Schmidt on 1, u, u^2, u^3 with u = (T - T_L) / T_L in
+// [-1, 0], then scaled to powers of t = T - T_L) with the lowest degree <= 3
+// whose largest residual is at most 2^-20 of the row's largest magnitude;
+// coef[k * 4 + d] multiplies t^d, degs[k] is the degree, resid[k * nt + t] =
+// sigma_k(T_t) - poly_k(T_t) in FP64.  False when some row needs more than a
+// cubic.  A PCA table printed to a fixed number of decimals (the reference's,
+// simulation_gpu_testing.cpp:47-63: its factors 2 and 3 are cubics to the
+// 9-decimal rounding, 1.1e-7 of their scale) fits with a residual of that
+// rounding's size.  Internal to the library.
+__attribute__((visibility("hidden"))) bool fit_cubic_resid(const double* vol, int nt, double dtau, double* coef,
+                                                            int* degs, double* resid)
+{
+    if (nt < 5) return false;
+    if (nt > HJM_MAX_TENOR) return false;
+    const double TL = dtau * (nt - 1);
+    const double tol = 0x1p-20;
+    double u[HJM_MAX_TENOR], q[4 * HJM_MAX_TENOR], r[HJM_MAX_TENOR];  // no heap use (hjm_run_static calls this)
+    for (int t = 0; t < nt; ++t) u[t] = (dtau * t - TL) / TL;
+    for (int k = 0; k < HJM_N_FACTOR; ++k) {
+        const double* v = vol + (size_t)k * nt;
+        double scale = 0.0;
+        for (int t = 0; t < nt; ++t) scale = std::max(scale, std::fabs(v[t]));
+        bool found = false;
+        for (int d = 0; d <= 3 && !found; ++d) {
+            // Q R of the columns u^0 .. u^d, then R b = Q^T v
+            double R[4][4] = {};
+            for (int j = 0; j <= d; ++j) {
+                double* qj = &q[(size_t)j * nt];
+                for (int t = 0; t < nt; ++t) qj[t] = std::pow(u[t], j);
+                for (int i = 0; i < j; ++i) {
+                    const double* qi = &q[(size_t)i * nt];
+                    double dot = 0.0;
+                    for (int t = 0; t < nt; ++t) dot += qi[t] * qj[t];
+                    R[i][j] = dot;
+                    for (int t = 0; t < nt; ++t) qj[t] -= dot * qi[t];
+                }
+                double nrm = 0.0;
+                for (int t = 0; t < nt; ++t) nrm += qj[t] * qj[t];
+                nrm = std::sqrt(nrm);
+                R[j][j] = nrm;
+                for (int t = 0; t < nt; ++t) qj[t] /= nrm;
+            }
+            double z[4] = {}, b[4] = {};
+            for (int t = 0; t < nt; ++t) r[t] = v[t];
+            for (int i = 0; i <= d; ++i) {
+                const double* qi = &q[(size_t)i * nt];
+                double dot = 0.0;
+                for (int t = 0; t < nt; ++t) dot += qi[t] * r[t];
+                z[i] = dot;
+                for (int t = 0; t < nt; ++t) r[t] -= dot * qi[t];
+            }
+            for (int i = d; i >= 0; --i) {
+                double acc = z[i];
+                for (int j = i + 1; j <= d; ++j) acc -= R[i][j] * b[j];
+                b[i] = acc / R[i][i];
+            }
+            double a[4] = {0.0, 0.0, 0.0, 0.0}, sc = 1.0;
+            for (int i = 0; i <= d; ++i, sc *= TL) a[i] = b[i] / sc;
+            double worst = 0.0;
+            for (int t = 0; t < nt; ++t) {
+                const double x = dtau * t - TL;
+                const double pv = ((a[3] * x + a[2]) * x + a[1]) * x + a[0];
+                r[t] = v[t] - pv;
+                worst = std::max(worst, std::fabs(r[t]));
+            }
+            if (worst <= tol * scale) {
+                found = true;
+                degs[k] = d;
+                for (int i = 0; i < 4; ++i) coef[k * 4 + i] = a[i];
+                for (int t = 0; t < nt; ++t) resid[(size_t)k * nt + t] = r[t];
+            }
+        }
+        if (!found) return false;
+    }
+    return true;
+}
 }  // namespace hjm
 
 static void trapezoid_drift(const std::vector<double>& vol, int nt, double dtau, std::vector<double>& drift)
@@ -415,6 +514,10 @@ hjm_status hjm_set_market(hjm_ctx* ctx, int32_t n_tenor, double dtau, const doub
     ctx->have_market = true;
     ctx->have_poly = false;
     ctx->poly_path = fit_quadratic_vols(ctx->vol.data(), n_tenor, dtau, ctx->coef);
+    ctx->resid.assign((size_t)HJM_N_FACTOR * n_tenor, 0.0);
+    ctx->cubic_path = !ctx->poly_path &&
+                      fit_cubic_resid(ctx->vol.data(), n_tenor, dtau, &ctx->cubic[0][0], ctx->cubic_degs,
+                                      ctx->resid.data());
     if (ctx->have_product && (int)ctx->payA.size() != n_tenor) ctx->have_product = false;
     return HJM_OK;
 }
@@ -440,6 +543,7 @@ hjm_status hjm_set_market_poly(hjm_ctx* ctx, int32_t n_tenor, double dtau, const
     std::memcpy(ctx->coef, vol_coef_host, sizeof(ctx->coef));
     ctx->have_poly = true;
     ctx->poly_path = true;
+    ctx->cubic_path = false;
     return HJM_OK;
 }
 
@@ -699,11 +803,18 @@ static void fill_pc(const hjm_ctx* ctx, const RunShape& sh, double dt, const Pat
 // impulse responses, six FP64 FMAs per date still to be sampled per step,
 // against four FMAs per live tenor (five for the predictor-corrector) and ~10
 // per step.
+//
+// Euler step with a decomposition (quadratic, or cubic with a residual
+// table): the response form of hjm_eresp.cu, whose per-step work is on the
+// FP32 pipe and which takes any number of dates (in windows); measured 6.9x
+// the convected form at 20 dates, and the convected cubic has no form but the
+// table step, so AUTO always takes it.
 static bool use_response_form(const hjm_ctx* ctx, const RunShape& sh)
 {
+    const bool pc = ctx->scheme == HJM_SCHEME_PREDICTOR_CORRECTOR;
+    if (!pc && (use_poly_path(ctx) || use_cubic_path(ctx))) return ctx->remainder != HJM_REMAINDER_CONVECT;
     if (sh.B > response_max_dates()) return false;
     if (ctx->remainder != HJM_REMAINDER_AUTO) return ctx->remainder == HJM_REMAINDER_RESPONSE;
-    const bool pc = ctx->scheme == HJM_SCHEME_PREDICTOR_CORRECTOR;
     const bool poly = use_poly_path(ctx);
     long conv = 0, resp = 0;
     for (int b = 1; b < sh.B; ++b) {
@@ -754,26 +865,17 @@ static hjm_status ensure_vol_response_table(hjm_ctx* ctx, const RunShape& sh, do
     return HJM_OK;
 }
 
-// The response table of the run shape and scheme, on the stream: recomputed
-// only when they changed, after the kernels of earlier valuations that read
-// it.  Euler: the source -2 c dtau^2 W at the last tenor (fill_params' k2);
-// predictor-corrector: the sources of fill_pc (wL1 at L-1; wL, gL at L);
-// then the moving-frame coefficients of the scheme's parts step f.
+// The predictor-corrector response table of the run shape, on the stream:
+// recomputed only when it changed, after the kernels of earlier valuations
+// that read it: the sources of fill_pc (wL1 at L-1; wL, gL at L), then the
+// moving-frame coefficients of the scheme's parts step f.
 static hjm_status ensure_response_table(hjm_ctx* ctx, const RunShape& sh, double dt, const PartsFrame& f,
                                         cudaStream_t s)
 {
     const double dtau = ctx->dtau;
     const double c = dt / dtau;
-    const bool pc = ctx->scheme == HJM_SCHEME_PREDICTOR_CORRECTOR;
-    double w0 = 0.0, w1, w2 = 0.0;
-    if (pc) {
-        const double wL1 = -c * c * dtau * dtau, wL = -(2.0 * c + c * c) * dtau * dtau, gL = -c * dtau * dtau;
-        w0 = wL1;
-        w1 = wL - gL;
-        w2 = gL;
-    } else {
-        w1 = -2.0 * ((dt / dtau) * dtau * dtau);
-    }
+    const double wL1 = -c * c * dtau * dtau, wL = -(2.0 * c + c * c) * dtau * dtau, gL = -c * dtau * dtau;
+    const double w0 = wL1, w1 = wL - gL, w2 = gL;
     hjm_ctx::RespKey& k = ctx->resp_key;
     if (!ctx->resp_used) HJM_CUDA(ctx, cudaEventCreateWithFlags(&ctx->resp_used, cudaEventDisableTiming));
     if (k.valid && k.nt == ctx->nt && k.stride == sh.stride && k.B == sh.B && k.c == c && k.dtau == dtau &&
@@ -786,7 +888,7 @@ static hjm_status ensure_response_table(hjm_ctx* ctx, const RunShape& sh, double
     else
         HJM_CUDA(ctx, cudaStreamWaitEvent(s, ctx->resp_used, 0));
     HJM_CUDA(ctx, cudaMemsetAsync(ctx->resp.p, 0, bytes, s));  // entries the kernel reads as exact zeros
-    HJM_CUDA(ctx, launch_response_table(ctx->nt, c, sh.stride, sh.B, pc, w0, w1, w2, (float4*)ctx->resp.p, s));
+    HJM_CUDA(ctx, launch_response_table_pc(ctx->nt, c, sh.stride, sh.B, w0, w1, w2, (float4*)ctx->resp.p, s));
     HJM_CUDA(ctx, launch_response_active(sh.stride, sh.B, (float4*)ctx->resp.p, s));
     HJM_CUDA(ctx, launch_state_coefs(f, sh.stride, sh.B, (float4*)ctx->resp.p, s));
     ctx->stat_launches += 3;
@@ -801,6 +903,91 @@ static hjm_status ensure_response_table(hjm_ctx* ctx, const RunShape& sh, double
     return HJM_OK;
 }
 
+// The Euler response form's table (remainder and residual responses, frame
+// coefficients, active prefixes) for the run shape and decomposition, on the
+// stream: rebuilt only when they changed, after the kernels of earlier
+// valuations that read it.
+static hjm_status ensure_eresp_table(hjm_ctx* ctx, const RunShape& sh, double dt,
+                                     const std::vector<EulerRespFrame>& frames, const std::vector<double>& resid,
+                                     int nres, cudaStream_t s)
+{
+    const EulerRespFrame& fr = frames[0];
+    const double c = dt / ctx->dtau;
+    hjm_ctx::ErespKey& k = ctx->eresp_key;
+    if (!ctx->resp_used) HJM_CUDA(ctx, cudaEventCreateWithFlags(&ctx->resp_used, cudaEventDisableTiming));
+    if (k.valid && k.nt == ctx->nt && k.stride == sh.stride && k.B == sh.B && k.np == fr.np && k.c == c &&
+        k.dtau == ctx->dtau && k.nres == nres && k.frames.size() == frames.size() &&
+        std::memcmp(k.frames.data(), frames.data(), sizeof(EulerRespFrame) * frames.size()) == 0 && k.resid == resid)
+        return HJM_OK;
+    k.valid = false;
+    const size_t bytes = sizeof(float4) * eresp_table_elems(sh.stride, sh.B, fr.np, nres, (int)frames.size());
+    if (bytes > ctx->eresp.bytes)
+        HJM_CUDA(ctx, ctx->eresp.ensure(bytes));  // cudaFree waits for the device
+    else
+        HJM_CUDA(ctx, cudaStreamWaitEvent(s, ctx->resp_used, 0));
+    HJM_CUDA(ctx, launch_eresp_tables(ctx->nt, c, ctx->dtau, sh.stride, sh.B, frames.data(), (int)frames.size(),
+                                      resid.empty() ? nullptr : resid.data(), nres, (float4*)ctx->eresp.p, s));
+    ctx->stat_launches += 3;
+    k.nt = ctx->nt;
+    k.stride = sh.stride;
+    k.B = sh.B;
+    k.np = fr.np;
+    k.nres = nres;
+    k.c = c;
+    k.dtau = ctx->dtau;
+    k.frames = frames;
+    k.resid = resid;
+    k.valid = true;
+    return HJM_OK;
+}
+
+// An FP64 Euler valuation in the response form (hjm_eresp.cu): the parts'
+// frame and loadings of the market's decomposition, the table, the carry of
+// a windowed run, and one launch per window.
+static hjm_status enqueue_eresp(hjm_ctx* ctx, const RunShape& sh, double dt, const PathParams<double>& P,
+                                const double* ext_dev, double* estore, cudaStream_t s)
+{
+    const bool cubic = use_cubic_path(ctx);
+    int lo[kMaxTenor], hi[kMaxTenor];
+    const int n_windows = eresp_windows(sh.B, lo, hi);
+    std::vector<EulerRespFrame> frames(n_windows);
+    int degs = 0;
+    for (int w = 0; w < n_windows; ++w)
+        eresp_make_frame(dt, ctx->dtau, ctx->nt, P.svc, cubic ? &ctx->cubic[0][0] : nullptr, ctx->cubic_degs,
+                         eresp_window_centre(ctx->dtau, lo[w], hi[w]), frames[w], degs);
+    const EulerRespFrame& fr = frames[0];
+    std::vector<double> resid;
+    int nres = 0;
+    if (cubic) {
+        const double sq = std::sqrt(dt);
+        resid.resize(ctx->resid.size());
+        for (size_t i = 0; i < resid.size(); ++i) resid[i] = sq * ctx->resid[i];
+        nres = eresp_residual_factors(ctx->resid.data(), ctx->vol.data(), ctx->nt);
+    }
+    const size_t smem = eresp_max_smem(sh.B, fr.np, sh.stride);
+    if (smem > 227 * 1024) return fail(ctx, HJM_ERR_UNSUPPORTED, "shared memory %zu B exceeds 227 KB", smem);
+    hjm_status st = ensure_eresp_table(ctx, sh, dt, frames, resid, nres, s);
+    if (st != HJM_OK) return st;
+    EulerRespParams E;
+    std::memset(&E, 0, sizeof(E));
+    E.P = P;
+    E.frame = block_frame_n(fr.n, sh.stride);
+    E.row = eresp_row(sh.B);
+    // the pairs are renormalised for the residual's terms and for windowed
+    // (long) runs, whose dates near the last tenor carry large remainders
+    E.renorm = (cubic || n_windows > 1) ? 1 : 0;
+    double* carry = nullptr;
+    if (n_windows > 1) {
+        HJM_CUDA(ctx, ctx->carry.ensure(sizeof(double) * 2 * (size_t)P.n_paths));
+        carry = (double*)ctx->carry.p;
+    }
+    int launches = 0;
+    HJM_CUDA(ctx, launch_path_fp64_eresp(E, frames.data(), degs, nres, (const float4*)ctx->eresp.p, ext_dev,
+                                         (double*)ctx->partials.p, estore, carry, s, &launches));
+    ctx->stat_launches += launches - 1;
+    return HJM_OK;
+}
+
 static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, double dt, uint64_t seed,
                                uint64_t path_offset, int32_t precision, double hazard, double recovery, double pfe_q,
                                const double* ext_dev)
@@ -810,8 +997,10 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
     if (st != HJM_OK) return st;
     HJM_CUDA(ctx, cudaSetDevice(ctx->device));
     const bool mixed = precision == HJM_PRECISION_MIXED;
-    if (!mixed && ctx->remainder == HJM_REMAINDER_RESPONSE && sh.B > response_max_dates())
-        return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "the response form holds at most %d dates (run has %d)",
+    const bool windows_ok = ctx->scheme == HJM_SCHEME_EULER && (use_poly_path(ctx) || use_cubic_path(ctx));
+    if (!mixed && ctx->remainder == HJM_REMAINDER_RESPONSE && sh.B > response_max_dates() && !windows_ok)
+        return fail(ctx, HJM_ERR_INVALID_ARGUMENT,
+                    "the response form of this market and scheme holds at most %d dates (run has %d)",
                     response_max_dates(), sh.B);
     const bool want_pfe = pfe_q > 0.0;
     const bool store = want_pfe || ctx->keep_exposures;
@@ -843,6 +1032,9 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
     ctx->stat_d2h = 0;
     HJM_CUDA(ctx, cudaEventRecord(ctx->ev[0], s));
     bool resp = false;
+    // the volatility form this run takes (vol_form_code's values): a cubic
+    // market runs its decomposition in the FP64 Euler response form only
+    int run_form = use_poly_path(ctx) ? vol_form_code(ctx) : 0;
     if (pc && mixed) {
         PathParams<float> P;
         fill_params<float>(ctx, sh, n_paths, dt, seed, path_offset, hazard, recovery, ld, store, P, F);
@@ -885,19 +1077,19 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
         PathParams<double> P;
         fill_params<double>(ctx, sh, n_paths, dt, seed, path_offset, hazard, recovery, ld, store, P, F);
         resp = use_response_form(ctx, sh);
-        if (resp && !use_poly_path(ctx)) {
+        if (resp && (use_poly_path(ctx) || use_cubic_path(ctx))) {
+            st = enqueue_eresp(ctx, sh, dt, P, ext_dev, store ? (double*)ctx->estore.p : nullptr, s);
+            if (st != HJM_OK) return st;
+            run_form = vol_form_code(ctx);
+        } else if (resp) {
             st = ensure_vol_response_table(ctx, sh, dt, &P.sv[0][0], s);
             if (st != HJM_OK) return st;
             HJM_CUDA(ctx, launch_path_fp64_vresp(ctx->nt, P, (const double2*)ctx->vresp.p, ext_dev,
                                                  (double*)ctx->partials.p, store ? (double*)ctx->estore.p : nullptr,
                                                  s));
         } else {
-            if (resp) {
-                st = ensure_response_table(ctx, sh, dt, euler_parts_frame(P), s);
-                if (st != HJM_OK) return st;
-            }
-            HJM_CUDA(ctx, launch_path_fp64(ctx->nt, P, use_poly_path(ctx),
-                                           resp ? (const float4*)ctx->resp.p : nullptr, ext_dev,
+            // convected: the quadratic decomposition, else the table step
+            HJM_CUDA(ctx, launch_path_fp64(ctx->nt, P, use_poly_path(ctx), ext_dev,
                                            (double*)ctx->partials.p, store ? (double*)ctx->estore.p : nullptr, s));
         }
         if (resp) HJM_CUDA(ctx, cudaEventRecord(ctx->resp_used, s));
@@ -923,7 +1115,7 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
         r.n_dates = n_dates;
         r.nt = ctx->nt;
         r.precision = precision;
-        r.vol_form = vol_form_code(ctx);
+        r.vol_form = run_form;
         r.dt = dt;
         r.dtau = ctx->dtau;
         r.hazard = hazard;
@@ -1279,7 +1471,7 @@ hjm_status hjm_run_adjoint(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, doubl
     r.n_dates = B + 1;
     r.nt = nt;
     r.precision = HJM_PRECISION_MIXED;
-    r.vol_form = vol_form_code(ctx);
+    r.vol_form = use_poly_path(ctx) ? vol_form_code(ctx) : 0;  // a cubic market runs the table step here
     r.remainder = 1;
     r.scheme = ctx->scheme;
     r.ckpt = K;
@@ -1452,7 +1644,7 @@ hjm_status hjm_run_mlmc(hjm_ctx* ctx, int32_t n_levels, const int64_t* n_paths, 
         r.n_dates = shapes[0].B + 1;
         r.nt = nt;
         r.precision = HJM_PRECISION_MIXED;
-        r.vol_form = vol_form_code(ctx);
+        r.vol_form = use_poly_path(ctx) ? vol_form_code(ctx) : 0;  // a cubic market runs the table step here
         r.remainder = 1;
         r.scheme = ctx->scheme;
         r.dtau = ctx->dtau;
@@ -1497,7 +1689,7 @@ hjm_status hjm_write_report(hjm_ctx* ctx, const char* path, int32_t format)
         return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "unknown report format %d", format);
     FILE* f = std::fopen(path, "w");
     if (!f) return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "cannot open %s for writing", path);
-    static const char* kForms[] = {"table", "poly", "poly_tri"};
+    static const char* kForms[] = {"table", "poly", "poly_tri", "cubic_resid"};
     static const char* kRemainders[] = {"none", "convect", "response"};
     std::vector<double> dates(r.nt);
     for (int j = 0; j < r.nt; ++j) dates[j] = r.dtau * j;

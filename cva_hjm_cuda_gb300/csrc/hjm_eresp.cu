@@ -1,0 +1,666 @@
+// hjm_eresp.cu -- the FP64 response form of the Euler step: polynomial parts
+// of degree <= 3, a residual volatility table, and runs of any number of
+// dates in windows of at most kRespSlots.
+//
+// The stochastic curve h (f = p + h, p the deterministic curve) is split as
+//     h = sum_d x_d t^d + hc,   t = T - tau0,
+// the parts x_d advancing by x <- M x + B phi (hjm_resp.cuh states M and the
+// moving frame), and the remainder hc by hc <- A hc + kappa w e_L + r phi,
+// where A is the upwind step (backward difference at the last tenor,
+// simulation_cpu.h:96-108), kappa w e_L the polynomial's error at L (kappa =
+// -2 c dtau^2, w = x_2 + 3 (T_L - tau0) x_3 before the step), and r the
+// residual loadings sqrt(dt) (sigma_k - poly_k) of a volatility table that
+// is a cubic only to its printed precision (the reference's own PCA table,
+// simulation_gpu_testing.cpp:47-63: factors 2 and 3 are cubics to 1.1e-7 of
+// their scale).  The pricing reads hc only at date j's tenor at its sampling
+// step, so per date still to be sampled the kernel keeps hc[j] and its
+// running sum, adding per step
+//     kappa G_j(lag) W            (double-FP32, the W terms: A, Al)
+//   + sum_k R_jk(lag) phi_k        (FP32 into the low lanes Al: the residual)
+// with G_j(m) = (A^m e_L)[j], R_jk(m) = (A^m r_k)[j] and their running sums
+// (eresp_table_kernel).  Exact in exact arithmetic, for any centre tau0; each
+// window takes the middle of its dates, where the polynomial's terms cancel
+// least (the parts carry 48 bits each, so their rounding scales with the
+// terms, not with the net curve).  The residual's response is ~1e-7 of the
+// curve's stochastic part, so its FP32 rounding stays below 1e-14 of the
+// curve.
+//
+// Windows.  The slots live in registers (kRespSlots of them).  A run with
+// more dates is priced in launches over windows of dates [lo, hi], the latest
+// window first: every launch evolves the parts and its window's slots from
+// the first evolved step to date hi (the parts are cheap to repeat, the
+// normals are counter-based), prices its dates, and passes to the next
+// (earlier) window, per path, the sum of its cash flows and its part of the
+// path's CVA contribution (carry [2][n_paths]); the earliest window (lo = 1)
+// completes the path's CVA statistics.  Each window writes the EE partial
+// sums and the exposure rows of its own dates.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "hjm_eresp.h"
+#include "hjm_resp.cuh"
+
+namespace hjm {
+
+namespace {
+
+// Shared memory of one launch over window [lo, hi] (dates with a cash flow):
+// cf_s [hi - lo + 3][kCta] (the epilogue's exposures alias it one row up),
+// red_s, the parts' running sums z_s [NP][kCta], then the staged coefficient
+// rows.
+size_t eresp_smem(int lo, int hi, int np, int coef_floats4)
+{
+    return ((size_t)(hi - lo + 3) * kFp64Cta + 2 * (kFp64Cta / 32) + (size_t)np * kFp64Cta) * 8 +
+           (size_t)coef_floats4 * 16;
+}
+
+// Epilogue of a window: exposures E_j = max(sum_{i > j} cf_i, 0) of dates
+// j in [lo - 1, hi - 1] (and E_B = 0 for the latest window), the cash flows of
+// later dates arriving in carry; the CTA's EE partial sums of those dates;
+// the CVA statistics (sum c, sum c^2 of the per-path contributions) from the
+// earliest window; the exposure rows by the bulk-copy engine.
+template <int kCta>
+__device__ __forceinline__ void window_epilogue(const PathParams<double>& P, int lo, int hi, double* cf_s,
+                                                double* red_s, double* __restrict__ partials,
+                                                double* __restrict__ estore, double* __restrict__ carry,
+                                                int64_t cta_base, int64_t lp, bool active)
+{
+    const int tid = threadIdx.x;
+    const int B = P.n_blocks;
+    const bool top = hi == B, bottom = lo == 1;
+    double* e_s = cf_s + kCta;  // exposure row of date j: j - lo + 1 (the cash-flow row of date j + 1)
+    double v = 0.0, cva_c = 0.0;
+    if (!top && active) {
+        v = carry[lp];
+        cva_c = carry[P.n_paths + lp];
+    }
+    if (top) e_s[(size_t)(B - lo + 1) * kCta + tid] = 0.0;
+    for (int j = hi - 1; j >= lo - 1; --j) {
+        v += cf_s[(size_t)(j - lo + 2) * kCta + tid];
+        double e = (v > 0.0) ? v : 0.0;
+        if (!active) e = 0.0;
+        e_s[(size_t)(j - lo + 1) * kCta + tid] = e;
+        cva_c = fma(P.cvaw[j], e, cva_c);
+    }
+    if (!bottom && active) {
+        carry[lp] = v;
+        carry[P.n_paths + lp] = cva_c;
+    }
+    __syncthreads();
+
+    const int warp = tid >> 5, lane = tid & 31;
+    const int R = B + 3;
+    const int j0 = lo - 1, j1 = top ? B : hi - 1;
+    for (int j = j0 + warp; j <= j1; j += kCta / 32) {
+        double sum = 0.0;
+#pragma unroll
+        for (int q = 0; q < kCta / 32; ++q) sum += e_s[(size_t)(j - lo + 1) * kCta + lane + 32 * q];
+        sum = warp_sum(sum);
+        if (lane == 0) partials[(size_t)blockIdx.x * R + j] = sum;
+    }
+    if (bottom) {
+        const double s1 = warp_sum(cva_c), s2 = warp_sum(cva_c * cva_c);
+        if (lane == 0) {
+            red_s[warp] = s1;
+            red_s[kCta / 32 + warp] = s2;
+        }
+    }
+    if (P.store_exposures) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+        if (bottom) {
+            double s1 = 0.0, s2 = 0.0;
+            for (int w = 0; w < kCta / 32; ++w) {
+                s1 += red_s[w];
+                s2 += red_s[kCta / 32 + w];
+            }
+            partials[(size_t)blockIdx.x * R + B + 1] = s1;
+            partials[(size_t)blockIdx.x * R + B + 2] = s2;
+        }
+        if (P.store_exposures) {
+            // date rows of this CTA's paths, smem -> HBM with the bulk-copy (TMA) engine
+            const int64_t cnt = (P.n_paths - cta_base < kCta) ? (P.n_paths - cta_base) : kCta;
+            const uint32_t bytes = (uint32_t)(((cnt + 1) / 2) * 2 * sizeof(double));
+            for (int j = j0; j <= j1; ++j) {
+                double* dst = estore + (size_t)j * (size_t)P.ld + (size_t)cta_base;
+                const uint32_t src = (uint32_t)__cvta_generic_to_shared(e_s + (size_t)(j - lo + 1) * kCta);
+                asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
+                             :: "l"(dst), "r"(src), "r"(bytes) : "memory");
+            }
+            asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+            asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+        }
+    }
+}
+
+// w = y_W + s n23 y_X in double-FP32 (the remainder's source W before step s
+// of the block, NP = 4): the product's leading term exact by FMA, Knuth's
+// two-sum for the addition, then renormalised.  The _rn intrinsics keep the
+// compiler from fusing a product into a later addition, which would void the
+// error-free transformations.
+__device__ __forceinline__ void source_w(float sh, float sl, float xh, float xl, float wh, float wl, float& oh,
+                                         float& ol)
+{
+    const float p = __fmul_rn(sh, xh);
+    float e = fmaf(sh, xh, -p);
+    e = fmaf(sh, xl, e);
+    e = fmaf(sl, xh, e);
+    const float s = __fadd_rn(wh, p);
+    const float bp = __fsub_rn(s, wh);
+    const float ap = __fsub_rn(s, bp);
+    const float err = __fadd_rn(__fsub_rn(wh, ap), __fsub_rn(p, bp));
+    const float l = __fadd_rn(wl, __fadd_rn(err, e));
+    oh = __fadd_rn(s, l);
+    ol = __fsub_rn(l, __fsub_rn(oh, s));
+}
+
+}  // namespace
+
+// DEGS: the factors' polynomial degrees (degs_pack); NRES: the factors
+// whose residual responses are in the table (0: none, one float4 per slot; 2:
+// factors 2 and 3, two float4; 3: all three, three float4); SC: the frame's
+// coefficient rows staged in shared memory.
+template <bool EXT, int DEGS, int NRES, bool SC>
+__global__ void __launch_bounds__(kFp64Cta, 6)
+    path_kernel_fp64_eresp(const __grid_constant__ EulerRespParams E, const float4* __restrict__ resp,
+                           const double* __restrict__ ext, double* __restrict__ partials,
+                           double* __restrict__ estore, double* __restrict__ carry)
+{
+    constexpr int kCta = kFp64Cta;
+    constexpr int NP = degs_parts(DEGS);
+    constexpr int SR = frame_row(NP);
+    constexpr int ENT = NRES == 3 ? 3 : (NRES == 2 ? 2 : 1);
+    const PathParams<double>& P = E.P;
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int tid = threadIdx.x;
+    const int B = P.n_blocks;
+    const int lo = E.win_lo, hi = E.win_hi;
+    double* cf_s = reinterpret_cast<double*>(smem);
+    double* red_s = cf_s + (size_t)(hi - lo + 3) * kCta;
+    double* z_s = red_s + 2 * (kCta / 32);
+
+    const int64_t cta_base = (int64_t)blockIdx.x * kCta;
+    const int64_t lp = cta_base + tid;
+    const bool active = lp < P.n_paths;
+    const uint64_t gpath = P.path_offset + (uint64_t)lp;
+
+    // {remainder at tenor j, its running sum} as hi + lo pairs, slot hi - j
+    float2 A[kRespSlots], Al[kRespSlots];
+#pragma unroll
+    for (int r = 0; r < kRespSlots; ++r) A[r] = Al[r] = make_float2(0.0f, 0.0f);
+    float2 Y[NP], Yl[NP];  // the parts in the block's moving frame, {y_c, v_c} hi + lo
+#pragma unroll
+    for (int c = 0; c < NP; ++c) Y[c] = Yl[c] = make_float2(0.0f, 0.0f);
+    const float4* coef_all = resp + (size_t)B * P.stride * E.row * ENT;
+    const float4* coef_g = coef_all + (size_t)E.frame_index * P.stride * SR;
+    const int* nact = reinterpret_cast<const int*>(coef_all + (size_t)E.n_frames * P.stride * SR);
+    const float4* coef = coef_g;
+    if constexpr (SC) {
+        float4* c_s = reinterpret_cast<float4*>(z_s + NP * kCta);
+        for (int i = tid; i < P.stride * SR; i += kCta) c_s[i] = coef_g[i];
+        __syncthreads();
+        coef = c_s;
+    }
+#pragma unroll
+    for (int c = 0; c < NP; ++c) z_s[c * kCta + tid] = 0.0;
+
+    const int roff = B - hi;                              // global slot of slot 0
+    const int nslot = hi - (lo > 2 ? lo : 2) + 1;         // slots of this window's dates
+
+    // price date i from its stochastic value xs and running sum zs
+    auto price = [&](int i, double xs, double zs) {
+        const double x = P.psamp[i] + xs;
+        const double D = exp(-(P.psum[i] + zs) * P.dt);
+        const double Lb = P.m * (exp(x * P.inv_m) - 1.0);
+        cf_s[(size_t)(i - lo + 1) * kCta + tid] = D * (P.payA[i] * Lb - P.payB[i]);
+    };
+
+    if (lo == 1) price(1, 0.0, 0.0);  // the first block holds the curve at spot
+    for (int b = 1; b < hi; ++b) {
+        const float4* row = resp + ((size_t)b * P.stride * E.row + roff) * ENT;
+        for (int s = 0; s < P.stride; ++s) {
+            const int n = b * P.stride + s;
+            float ph[3], pl[3];  // the normals as hi + lo (lo = 0 for the generator's FP32 draws)
+            if constexpr (EXT) {
+                double d0, d1, d2;
+                draw_phi<double, true>(ext, gpath, active ? lp : 0, P.n_paths, n, P.rk0, P.rk1, d0, d1, d2);
+                split_f64(d0, ph[0], pl[0]);
+                split_f64(d1, ph[1], pl[1]);
+                split_f64(d2, ph[2], pl[2]);
+            } else {
+                draw_phi<float, false>(ext, gpath, lp, P.n_paths, n, P.rk0, P.rk1, ph[0], ph[1], ph[2]);
+                pl[0] = pl[1] = pl[2] = 0.0f;
+            }
+            int n_act = __ldg(nact + n) - roff;  // uniform: the row's active prefix in this window
+            n_act = n_act < 0 ? 0 : (n_act > nslot ? nslot : n_act);
+            const float4* rr = row + (size_t)s * E.row * ENT;
+            // the remainder's source: W before this step's update
+            float wh, wl;
+            if constexpr (NP == 4) {
+                const float4 sg = coef[(size_t)s * SR + 12];
+                source_w(sg.x, sg.y, Y[3].x, Yl[3].x, Y[2].x, Yl[2].x, wh, wl);
+            } else {
+                wh = Y[2].x;
+                wl = Yl[2].x;
+            }
+            const float2 wh2 = make_float2(wh, wh), wl2 = make_float2(wl, wl), nwh2 = make_float2(-wh, -wh);
+            resp_groups(n_act, [&](auto gc) {
+                constexpr int G = decltype(gc)::value;
+                float4 k[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) k[u] = __ldg(rr + (4 * G + u) * ENT);
+                if constexpr (NRES == 3) {
+                    float4 r1[4], r2[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        r1[u] = __ldg(rr + (4 * G + u) * ENT + 1);
+                        r2[u] = __ldg(rr + (4 * G + u) * ENT + 2);
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        float2& lo2 = Al[4 * G + u];
+                        lo2 = __ffma2_rn(make_float2(r1[u].x, r1[u].y), make_float2(ph[0], ph[0]), lo2);
+                        lo2 = __ffma2_rn(make_float2(r1[u].z, r1[u].w), make_float2(ph[1], ph[1]), lo2);
+                        lo2 = __ffma2_rn(make_float2(r2[u].x, r2[u].y), make_float2(ph[2], ph[2]), lo2);
+                    }
+                } else if constexpr (NRES == 2) {
+                    float4 r1[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) r1[u] = __ldg(rr + (4 * G + u) * ENT + 1);
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        float2& lo2 = Al[4 * G + u];
+                        lo2 = __ffma2_rn(make_float2(r1[u].x, r1[u].y), make_float2(ph[1], ph[1]), lo2);
+                        lo2 = __ffma2_rn(make_float2(r1[u].z, r1[u].w), make_float2(ph[2], ph[2]), lo2);
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    df_acc(A[4 * G + u], Al[4 * G + u], make_float2(k[u].x, k[u].y), make_float2(k[u].z, k[u].w),
+                           wh2, wl2, nwh2);
+            });
+            // every fourth step, the active pairs renormalised (see renorm)
+            if (E.renorm && (s & 3) == 3)
+                resp_groups(n_act, [&](auto gc) {
+                    constexpr int G = decltype(gc)::value;
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) df_renorm(A[4 * G + u], Al[4 * G + u]);
+                });
+            // y += C(s) phi, v += G(s) phi for the (part, factor) terms of the degrees
+            frame_step_n<DEGS, EXT, SC>(Y, Yl, coef + (size_t)s * SR, ph, pl);
+        }
+        // the end of block b: the parts at date b + 1, priced when it is this window's
+        double x[NP], Z[NP];
+        frame_block_end_n<NP>(Y, Yl, E.frame, z_s + tid, kCta, x, Z);
+        const int i = b + 1;
+        if (i >= lo) {
+            const double t = P.tau[i] - E.tau0;
+            const float2 h = select_reg<kRespSlots, float2>(A, hi - i), l = select_reg<kRespSlots, float2>(Al, hi - i);
+            const double hc = widen_f32(h.x) + widen_f32(l.x);
+            const double hcs = widen_f32(h.y) + widen_f32(l.y);
+            double px = x[NP - 1], pz = Z[NP - 1];
+#pragma unroll
+            for (int c = NP - 2; c >= 0; --c) {
+                px = fma(t, px, x[c]);
+                pz = fma(t, pz, Z[c]);
+            }
+            price(i, px + hc, pz + hcs);
+        }
+    }
+    window_epilogue<kCta>(P, lo, hi, cf_s, red_s, partials, estore, carry, cta_base, lp, active);
+}
+
+// ---------------------------------------------------------------------------
+// Tables
+// ---------------------------------------------------------------------------
+// Residual loadings r_k[t] of the table kernel, by value.
+struct ResidLoadings {
+    double r[kFactors][kMaxTenor];
+};
+
+// The responses of the remainder's source and of the residual loadings at the
+// sampled tenors: entry (row b stride + s, slot r = B - j) holds, at lag
+// l = (j - b) stride - 1 - s (the distance to date j's sampling step), the
+// float4 {kappa G hi, kappa CG hi, kappa G lo, kappa CG lo} (each FP64 value
+// split into the nearest float and the float nearest the rest) and, with the
+// residual of all three factors (nres = 3), {R_j0, CR_j0, R_j1, CR_j1} and
+// {R_j2, CR_j2, 0, 0} in FP32, or of factors 2 and 3 only (nres = 2, the
+// first being an exact polynomial), {R_j1, CR_j1, R_j2, CR_j2}, for
+// 1 <= b < j <= B.  Every lag of date j maps to one entry (q = j - b
+// = l / stride + 1, s = q stride - 1 - l); the rest of the table stays zero.
+// G and R by repeated upwind steps in FP64 (backward difference at the last
+// tenor), one CTA, thread t holding tenor t.
+__global__ void __launch_bounds__(kMaxTenor)
+    eresp_table_kernel(int nt, double c, int stride, int B, int row, int nres, double kappa, ResidLoadings RL,
+                       float4* __restrict__ resp)
+{
+    __shared__ double v_s[4][kMaxTenor];
+    const int t = threadIdx.x;
+    const int L = nt - 1;
+    const int M = (B - 1) * stride - 1;  // the longest lag read
+    double v[4], cum[4];                 // [0]: G (e_L), [1..3]: R_k (r_k)
+    v[0] = (t == L) ? 1.0 : 0.0;
+    const int ent = nres == 3 ? 3 : (nres == 2 ? 2 : 1);
+    for (int k = 0; k < kFactors; ++k) v[1 + k] = (t < nt && nres > 0) ? RL.r[k][t] : 0.0;
+    for (int q = 0; q < 4; ++q) cum[q] = 0.0;
+    for (int m = 0; m <= M; ++m) {
+        for (int q = 0; q < 4; ++q) cum[q] += v[q];
+        if (t >= 2 && t <= B) {
+            const int qd = m / stride + 1;
+            const int b = t - qd;
+            if (b >= 1) {
+                float4* e = resp + (((size_t)b * stride + (size_t)(qd * stride - 1 - m)) * row + (B - t)) * ent;
+                const double g = kappa * v[0], cg = kappa * cum[0];
+                const float gh = __double2float_rn(g), cgh = __double2float_rn(cg);
+                e[0] = make_float4(gh, cgh, __double2float_rn(g - (double)gh), __double2float_rn(cg - (double)cgh));
+                if (nres == 3) {
+                    e[1] = make_float4(__double2float_rn(v[1]), __double2float_rn(cum[1]), __double2float_rn(v[2]),
+                                       __double2float_rn(cum[2]));
+                    e[2] = make_float4(__double2float_rn(v[3]), __double2float_rn(cum[3]), 0.0f, 0.0f);
+                } else if (nres == 2) {
+                    e[1] = make_float4(__double2float_rn(v[2]), __double2float_rn(cum[2]), __double2float_rn(v[3]),
+                                       __double2float_rn(cum[3]));
+                }
+            }
+        }
+        for (int q = 0; q < 4; ++q) v_s[q][t] = v[q];
+        __syncthreads();
+        for (int q = 0; q < 4; ++q) {
+            if (t < L)
+                v[q] += c * (v_s[q][t + 1] - v[q]);
+            else if (t == L)
+                v[q] += c * (v[q] - v_s[q][L - 1]);
+        }
+        __syncthreads();
+    }
+}
+
+// Per row of the table (rows x row slots), the active prefix n_act[row] in
+// global slot numbering: the slots up to the last one with a component that
+// is nonzero and at least 2^-70 of that component's largest magnitude in its
+// slot over all rows (a slot is one date).  The slots after it hold only terms
+// near the transport front, where the responses are vanishingly small (each
+// below 2^-70 of the date's largest coefficient); the kernels skip them.
+// n_act[rows] = 0 (read ahead).  One CTA.
+__global__ void __launch_bounds__(1024)
+    eresp_active_kernel(int rows, int row, int ent, const float4* __restrict__ resp, int* __restrict__ n_act)
+{
+    __shared__ unsigned int mx[kMaxTenor + 4][8];
+    for (int i = threadIdx.x; i < (kMaxTenor + 4) * 8; i += blockDim.x) (&mx[0][0])[i] = 0u;
+    __syncthreads();
+    const int ncomp = ent == 3 ? 8 : (ent == 2 ? 6 : 2);
+    auto comp = [&](size_t slot_base, int q) -> float {
+        if (q < 2) {
+            const float4 e = resp[slot_base];
+            return q == 0 ? e.x : e.y;
+        }
+        const float4 e = resp[slot_base + (q < 6 ? 1 : 2)];
+        switch (q) {
+            case 2: return e.x;
+            case 3: return e.y;
+            case 4: return e.z;
+            case 5: return e.w;
+            case 6: return e.x;
+            default: return e.y;
+        }
+    };
+    const int64_t total = (int64_t)rows * row;
+    for (int64_t i = threadIdx.x; i < total; i += blockDim.x) {
+        const int r = (int)(i % row);
+        for (int q = 0; q < ncomp; ++q)
+            atomicMax(&mx[r][q], __float_as_uint(fabsf(comp((size_t)i * ent, q))));  // non-negative floats order as their bits
+    }
+    __syncthreads();
+    for (int rw = threadIdx.x; rw <= rows; rw += blockDim.x) {
+        int n = 0;
+        if (rw < rows)
+            for (int r = 0; r < row; ++r)
+                for (int q = 0; q < ncomp; ++q) {
+                    const float a = fabsf(comp(((size_t)rw * row + r) * ent, q));
+                    if (a != 0.0f && a >= __uint_as_float(mx[r][q]) * 0x1p-70f) n = r + 1;
+                }
+        n_act[rw] = n;
+    }
+}
+
+// The moving-frame coefficients (hjm_resp.cuh): row s < stride, entry 3 c + k
+// = {C hi, G hi, C lo, G lo} of C(s) = M^-(s+1) B and G(s) = Q(s) C(s), FP64
+// split into the nearest float and the float nearest the rest; for NP = 4
+// entry 12 = {sigma hi, sigma lo, 0, 0}, sigma = s n23 + sig0, the coefficient
+// of y_X in the remainder's source before step s (W = y_W + s n23 y_X, plus
+// the cubic's own share sig0 X).
+struct FrameLoadings {
+    PartsN n;
+    double bm[4][kFactors];  // B[c][k]: loading of part c on factor k
+    double sig0;
+};
+
+__global__ void eresp_coef_kernel(FrameLoadings f, int np, int stride, float4* __restrict__ coef)
+{
+    const int sr = frame_row(np);
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)stride * sr) return;
+    const int64_t s = idx / sr;
+    const int e = (int)(idx % sr);
+    if (e == 12) {
+        const double sg = fma((double)s, f.n.n23, f.sig0);
+        const float h = __double2float_rn(sg);
+        coef[idx] = make_float4(h, __double2float_rn(sg - (double)h), 0.0f, 0.0f);
+        return;
+    }
+    const int c = e / 3, k = e % 3;
+    if (c >= np) return;
+    const double kk = (double)(s + 1), q = (double)s;
+    // M^-k: c1 = -k, c2 = C(k+1, 2), c3 = -C(k+2, 3); Q(q): q I + C(q+1, 2) N + C(q+1, 3) N^2 + C(q+1, 4) N^3
+    const PolyN minv(f.n, 1.0, -kk, 0.5 * kk * (kk + 1.0), -(kk + 2.0) * (kk + 1.0) * kk / 6.0);
+    const PolyN Q(f.n, q, 0.5 * q * (q + 1.0), (q + 1.0) * q * (q - 1.0) / 6.0,
+                  (q + 1.0) * q * (q - 1.0) * (q - 2.0) / 24.0);
+    double b[4] = {0.0, 0.0, 0.0, 0.0}, C[4];
+    for (int r = 0; r < np; ++r) b[r] = f.bm[r][k];
+    for (int r = 0; r < 4; ++r) C[r] = minv.row(r, b);
+    const double cv = C[c], gv = Q.row(c, C);
+    const float ch = __double2float_rn(cv), gh = __double2float_rn(gv);
+    coef[idx] = make_float4(ch, gh, __double2float_rn(cv - (double)ch), __double2float_rn(gv - (double)gh));
+}
+
+// ---------------------------------------------------------------------------
+// Host
+// ---------------------------------------------------------------------------
+int eresp_row(int n_blocks) { return (n_blocks + 2 + 3) / 4 * 4; }
+
+void eresp_make_frame(double dt, double dtau, int nt, const double (*svc)[3], const double* cubic,
+                      const int* cubic_degs, double tau0, EulerRespFrame& fr, int& degs)
+{
+    std::memset(&fr, 0, sizeof(fr));
+    const double c = dt / dtau, sq = std::sqrt(dt);
+    const double k1 = c * dtau, k2 = c * dtau * dtau;
+    const double TL = dtau * (nt - 1);
+    fr.tau0 = tau0;
+    int dg[kFactors];
+    if (cubic) {
+        fr.np = 4;
+        fr.n = PartsN{k1, k2, c * dtau * dtau * dtau, 2.0 * k1, 3.0 * k2, 3.0 * k1};
+        fr.sig0 = 3.0 * (TL - tau0);
+        // sum_e a_e (T - T_L)^e = sum_d a'_d (T - tau0)^d, a'_d = sum_{e>=d} C(e,d) a_e (tau0 - T_L)^(e-d)
+        const double dl = tau0 - TL;
+        for (int k = 0; k < kFactors; ++k) {
+            const double* a = cubic + k * 4;
+            const double sh[4] = {a[0] + dl * (a[1] + dl * (a[2] + dl * a[3])), a[1] + dl * (2.0 * a[2] + 3.0 * dl * a[3]),
+                                  a[2] + 3.0 * dl * a[3], a[3]};
+            for (int cc = 0; cc < 4; ++cc) fr.bm[cc][k] = sq * sh[cc];
+            dg[k] = cubic_degs[k];
+        }
+    } else {
+        fr.np = 3;
+        fr.n = PartsN{k1, k2, 0.0, 2.0 * k1, 0.0, 0.0};
+        fr.sig0 = 0.0;
+        // sum_d s_d T^d = s'_0 + s'_1 t + s'_2 t^2 with t = T - tau0
+        for (int k = 0; k < kFactors; ++k) {
+            const double* a = svc[k];
+            const double sh[3] = {a[0] + tau0 * (a[1] + tau0 * a[2]), a[1] + 2.0 * tau0 * a[2], a[2]};
+            for (int cc = 0; cc < 3; ++cc) fr.bm[cc][k] = sh[cc];
+            dg[k] = a[2] != 0.0 ? 2 : (a[1] != 0.0 ? 1 : 0);
+        }
+    }
+    degs = degs_pack(dg[0], dg[1], dg[2]);
+}
+
+double eresp_window_centre(double dtau, int lo, int hi) { return 0.5 * dtau * (double)(lo + hi); }
+
+int eresp_residual_factors(const double* resid, const double* vol, int nt)
+{
+    if (!resid) return 0;
+    double r0 = 0.0, s0 = 0.0;
+    for (int t = 0; t < nt; ++t) {
+        r0 = std::max(r0, std::fabs(resid[t]));
+        s0 = std::max(s0, std::fabs(vol[t]));
+    }
+    return r0 <= 0x1p-44 * s0 ? 2 : 3;
+}
+
+static int entries_per_slot(int nres) { return nres == 3 ? 3 : (nres == 2 ? 2 : 1); }
+
+size_t eresp_table_elems(int stride, int n_blocks, int np, int nres, int n_frames)
+{
+    const size_t rows = (size_t)n_blocks * stride;
+    return rows * eresp_row(n_blocks) * entries_per_slot(nres) + (size_t)n_frames * stride * frame_row(np) +
+           (rows + 4) / 4;
+}
+
+cudaError_t launch_eresp_tables(int nt, double c, double dtau, int stride, int n_blocks, const EulerRespFrame* frames,
+                                int n_frames, const double* resid /* [3][nt] sqrt(dt)-scaled, or null */, int nres,
+                                float4* table, cudaStream_t s)
+{
+    if (n_frames < 1) return cudaErrorInvalidValue;
+    const EulerRespFrame& fr = frames[0];
+    if (nt < 3 || nt > kMaxTenor || n_blocks < 1 || n_blocks >= nt || stride < 1) return cudaErrorInvalidValue;
+    const int row = eresp_row(n_blocks);
+    if (!resid) nres = 0;
+    const int ent = entries_per_slot(nres);
+    const size_t rows = (size_t)n_blocks * stride;
+    cudaError_t e =
+        cudaMemsetAsync(table, 0, sizeof(float4) * eresp_table_elems(stride, n_blocks, fr.np, nres, n_frames), s);
+    if (e != cudaSuccess) return e;
+    ResidLoadings RL;
+    std::memset(&RL, 0, sizeof(RL));
+    if (resid)
+        for (int k = 0; k < kFactors; ++k)
+            for (int t = 0; t < nt; ++t) RL.r[k][t] = resid[k * nt + t];
+    const double kappa = -2.0 * (c * dtau * dtau);
+    eresp_table_kernel<<<1, kMaxTenor, 0, s>>>(nt, c, stride, n_blocks, row, nres, kappa, RL, table);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    float4* coef = table + rows * row * ent;
+    const int64_t per_frame = (int64_t)stride * frame_row(fr.np);
+    for (int w = 0; w < n_frames; ++w) {
+        FrameLoadings f;
+        std::memset(&f, 0, sizeof(f));
+        f.n = frames[w].n;
+        f.sig0 = frames[w].sig0;
+        for (int cc = 0; cc < 4; ++cc)
+            for (int k = 0; k < kFactors; ++k) f.bm[cc][k] = frames[w].bm[cc][k];
+        eresp_coef_kernel<<<(unsigned)((per_frame + 127) / 128), 128, 0, s>>>(f, fr.np, stride, coef + w * per_frame);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    eresp_active_kernel<<<1, 1024, 0, s>>>((int)rows, row, ent, table,
+                                            reinterpret_cast<int*>(coef + (size_t)n_frames * per_frame));
+    return cudaGetLastError();
+}
+
+namespace {
+
+template <bool EXT, int DEGS, int NRES>
+cudaError_t launch_window(const EulerRespParams& E, const float4* table, const double* ext, double* partials,
+                          double* estore, double* carry, cudaStream_t s)
+{
+    constexpr int NP = degs_parts(DEGS);
+    const int sr = frame_row(NP);
+    const bool sc = (size_t)E.P.stride * sr <= (size_t)kFrameSmemRows * kStateRow;
+    const size_t smem = eresp_smem(E.win_lo, E.win_hi, NP, sc ? E.P.stride * sr : 0);
+    auto k = sc ? path_kernel_fp64_eresp<EXT, DEGS, NRES, true> : path_kernel_fp64_eresp<EXT, DEGS, NRES, false>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const int64_t grid = (E.P.n_paths + kFp64Cta - 1) / kFp64Cta;
+    k<<<(unsigned)grid, kFp64Cta, smem, s>>>(E, table, ext, partials, estore, carry);
+    return cudaGetLastError();
+}
+
+template <int DEGS, int NRES>
+cudaError_t launch_window_ext(const EulerRespParams& E, const float4* table, const double* ext, double* partials,
+                              double* estore, double* carry, cudaStream_t s)
+{
+    return ext ? launch_window<true, DEGS, NRES>(E, table, ext, partials, estore, carry, s)
+               : launch_window<false, DEGS, NRES>(E, table, ext, partials, estore, carry, s);
+}
+
+}  // namespace
+
+int eresp_windows(int n_blocks, int* lo, int* hi)
+{
+    // from the latest date down: each window holds kRespSlots dates with a
+    // slot; a window reaching date 2 takes date 1 (which needs no slot) too
+    int n = 0, h = n_blocks;
+    while (h >= 1) {
+        int l = h - kRespSlots + 1;
+        if (l <= 2) l = 1;
+        if (lo) lo[n] = l;
+        if (hi) hi[n] = h;
+        ++n;
+        h = l - 1;
+    }
+    return n;
+}
+
+cudaError_t launch_path_fp64_eresp(const EulerRespParams& base, const EulerRespFrame* frames, int degs, int nres,
+                                   const float4* table, const double* ext, double* partials, double* estore,
+                                   double* carry, cudaStream_t s, int* launches)
+{
+    int lo[kMaxTenor], hi[kMaxTenor];
+    const int nw = eresp_windows(base.P.n_blocks, lo, hi);
+    if (nw > 1 && !carry) return cudaErrorInvalidValue;
+    if (launches) *launches = 0;
+    for (int w = 0; w < nw; ++w) {
+        EulerRespParams E = base;
+        E.win_lo = lo[w];
+        E.win_hi = hi[w];
+        E.frame_index = w;
+        E.n_frames = nw;
+        E.tau0 = frames[w].tau0;
+        cudaError_t e;
+        if (nres == 2 && degs_of(degs, 0) == 0) {
+            e = launch_window_ext<degs_pack(0, 3, 3), 2>(E, table, ext, partials, estore, carry, s);
+        } else if (nres > 0) {
+            // (a residual table of factors 2 and 3 only is laid out as nres = 2)
+            if (nres == 2) return cudaErrorInvalidValue;
+            if (degs_of(degs, 0) == 0)
+                e = launch_window_ext<degs_pack(0, 3, 3), 3>(E, table, ext, partials, estore, carry, s);
+            else
+                e = launch_window_ext<degs_pack(3, 3, 3), 3>(E, table, ext, partials, estore, carry, s);
+        } else if (degs == degs_pack(0, 1, 2) || degs == degs_pack(0, 1, 1) || degs == degs_pack(0, 0, 2) ||
+                   degs == degs_pack(0, 1, 0) || degs == degs_pack(0, 0, 1) || degs == degs_pack(0, 0, 0)) {
+            e = launch_window_ext<degs_pack(0, 1, 2), 0>(E, table, ext, partials, estore, carry, s);
+        } else {
+            e = launch_window_ext<degs_pack(2, 2, 2), 0>(E, table, ext, partials, estore, carry, s);
+        }
+        if (e != cudaSuccess) return e;
+        if (launches) ++*launches;
+    }
+    return cudaSuccess;
+}
+
+size_t eresp_max_smem(int n_blocks, int np, int stride)
+{
+    int lo[kMaxTenor], hi[kMaxTenor];
+    const int nw = eresp_windows(n_blocks, lo, hi);
+    const int sr = frame_row(np);
+    const bool sc = (size_t)stride * sr <= (size_t)kFrameSmemRows * kStateRow;
+    size_t m = 0;
+    for (int w = 0; w < nw; ++w) m = std::max(m, eresp_smem(lo[w], hi[w], np, sc ? stride * sr : 0));
+    return m;
+}
+
+}  // namespace hjm

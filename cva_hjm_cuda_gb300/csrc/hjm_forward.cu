@@ -35,7 +35,6 @@ namespace hjm {
 //   acc_s  [B+1] double   FP64 discount sums of the stochastic part per tenor
 //   work_s [2(B+2)] double  curve at block start / end, then exposures
 //   red_s  [2 * kFp64Cta/32] double  CVA statistics
-constexpr int kFp64Cta = 64;
 
 __host__ __device__ inline size_t path_smem_bytes(int nt, int n_blocks, bool mixed)
 {
@@ -240,145 +239,31 @@ __global__ void __launch_bounds__(kFp64Cta, 4)
     fp64_epilogue<kCta>(P, cf_s, work_s, red_s, partials, estore, cta_base, active);
 }
 
-// The FP64 response form (hjm_resp.cuh): the polynomial parts S, U, W as
-// double-FP32 sums in a moving frame anchored at each block, the remainder as
-// double-FP32 impulse-response sums per date slot, FP64 at the sampled dates.
+// Shared memory of the response-form kernels: cf_s [B+2][kCta] (the
+// epilogue's exposures alias it one row up), red_s.
 __host__ __device__ inline size_t resp_smem_bytes(int n_blocks)
 {
-    // cf_s [B+2][kCta] (the epilogue's exposures alias it one row up), red_s
     return ((size_t)n_blocks + 2) * kFp64Cta * 8 + 2 * (kFp64Cta / 32) * 8;
 }
 
-// the Euler response kernel: and the running sums of the parts [3][kCta]
-// (the frame's coefficient rows follow when staged)
-__host__ __device__ inline size_t resp_smem_bytes_parts(int n_blocks)
-{
-    return resp_smem_bytes(n_blocks) + 3 * kFp64Cta * 8;
-}
-
-// SC: the frame's coefficient rows staged in shared memory (stride at most
-// kFrameSmemRows), else read through L1.
-template <int NT, bool EXT, bool TRI, bool SC>
-__global__ void __launch_bounds__(kFp64Cta, 6)
-    path_kernel_fp64_resp(const __grid_constant__ PathParams<double> P, const float4* __restrict__ resp,
-                          const double* __restrict__ ext, double* __restrict__ partials,
-                          double* __restrict__ estore)
-{
-    constexpr int kCta = kFp64Cta;
-    extern __shared__ __align__(128) unsigned char smem[];
-    const int tid = threadIdx.x;
-    const int B = P.n_blocks;
-    double* cf_s = reinterpret_cast<double*>(smem);
-    double* red_s = cf_s + (size_t)(B + 2) * kCta;
-
-    const int64_t cta_base = (int64_t)blockIdx.x * kCta;
-    const int64_t lp = cta_base + tid;  // path index within this launch
-    const bool active = lp < P.n_paths;
-    const uint64_t gpath = P.path_offset + (uint64_t)lp;
-
-    // {remainder at tenor j, its running sum} as hi + lo pairs, slot B - j,
-    // for the dates j not yet sampled
-    float2 A[kRespSlots], Al[kRespSlots];
-#pragma unroll
-    for (int r = 0; r < kRespSlots; ++r) A[r] = Al[r] = make_float2(0.0f, 0.0f);
-    // the parallel, tilt and curvature parts in the block's moving frame,
-    // {y_c, v_c} as hi + lo pairs (c = S, U, W), anchored at the block's start
-    float2 Y[3], Yl[3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) Y[c] = Yl[c] = make_float2(0.0f, 0.0f);
-    // the frame's coefficient rows (one block's), staged in shared memory for SC
-    const float4* coef = resp + resp_coef_offset(P.stride, B);
-    if constexpr (SC) {
-        float4* c_s = reinterpret_cast<float4*>(red_s + 2 * (kCta / 32) + 3 * kCta);
-        for (int i = tid; i < P.stride * kStateRow; i += kCta) c_s[i] = coef[i];
-        __syncthreads();
-        coef = c_s;
-    }
-    const int* nact = reinterpret_cast<const int*>(resp + resp_nact_offset(P.stride, B));
-    // the running sums Z of the parts over the evolved steps, FP64, between blocks
-    double* z_s = red_s + 2 * (kCta / 32);
-#pragma unroll
-    for (int c = 0; c < 3; ++c) z_s[c * kCta + tid] = 0.0;
-    const BlockFrame F(P.k1, P.k2, 2.0 * P.k1, (double)P.stride);  // the Euler step on a quadratic
-
-    // price date i from the sampled numeraire (x_i, D_i); for i >= 2 the
-    // block just ended: x = M^a y, Z += Q(a) y - v, then y re-anchored on x
-    auto sample = [&](int i) {
-        const double tau = P.tau[i];
-        double hc = 0.0, hcs = 0.0;
-        double S = 0.0, U = 0.0, W = 0.0, ZS = 0.0, ZU = 0.0, ZW = 0.0;
-        if (i >= 2) {
-            const float2 h = select_reg<kRespSlots, float2>(A, B - i), l = select_reg<kRespSlots, float2>(Al, B - i);
-            hc = widen_f32(h.x) + widen_f32(l.x);
-            hcs = widen_f32(h.y) + widen_f32(l.y);
-            frame_block_end(Y, Yl, F, z_s + tid, kCta, S, U, W, ZS, ZU, ZW);
-        }
-        const double x = P.psamp[i] + (fma(tau, fma(tau, W, U), S) + hc);
-        const double acc = fma(tau, fma(tau, ZW, ZU), ZS) + hcs;
-        const double D = exp(-(P.psum[i] + acc) * P.dt);
-        const double Lb = P.m * (exp(x * P.inv_m) - 1.0);
-        cf_s[i * kCta + tid] = D * (P.payA[i] * Lb - P.payB[i]);
-    };
-
-    sample(1);
-    for (int b = 1; b < B; ++b) {
-        const float4* row = resp + (size_t)b * P.stride * kRespRow;
-        for (int s = 0; s < P.stride; ++s) {
-            const int n = b * P.stride + s;
-            float ph[3], pl[3];  // the normals as hi + lo (lo = 0 for the generator's FP32 draws)
-            if constexpr (EXT) {
-                double d0, d1, d2;
-                draw_phi<double, true>(ext, gpath, active ? lp : 0, P.n_paths, n, P.rk0, P.rk1, d0, d1, d2);
-                split_f64(d0, ph[0], pl[0]);
-                split_f64(d1, ph[1], pl[1]);
-                split_f64(d2, ph[2], pl[2]);
-            } else {
-                draw_phi<float, false>(ext, gpath, lp, P.n_paths, n, P.rk0, P.rk1, ph[0], ph[1], ph[2]);
-            }
-            const int n_act = __ldg(nact + n);  // uniform: the row's active prefix
-            const float4* rr = row + (size_t)s * kRespRow;
-            // the remainder's source: W before this step's update
-            const float2 wh2 = make_float2(Y[2].x, Y[2].x), wl2 = make_float2(Yl[2].x, Yl[2].x);
-            const float2 nwh2 = make_float2(-Y[2].x, -Y[2].x);
-            resp_groups(n_act, [&](auto gc) {
-                constexpr int G = decltype(gc)::value;
-                float4 k[4];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) k[u] = __ldg(rr + 4 * G + u);
-#pragma unroll
-                for (int u = 0; u < 4; ++u)
-                    df_acc(A[4 * G + u], Al[4 * G + u], make_float2(k[u].x, k[u].y), make_float2(k[u].z, k[u].w),
-                           wh2, wl2, nwh2);
-            });
-            // y += C(s) phi, v += G(s) phi (factor k of degree <= k loads parts c <= k only)
-            frame_step<EXT, TRI, SC>(Y, Yl, coef + (size_t)s * kStateRow, ph, pl);
-        }
-        sample(b + 1);
-    }
-    fp64_epilogue<kCta>(P, cf_s, cf_s + kCta, red_s, partials, estore, cta_base, active);
-}
-
-// Impulse responses of the convection at the sampled tenors, for the response
-// form: entry (row b stride + s, column r = B - j) of resp holds, as FP32 pairs
-// {coef hi, sum hi, coef lo, sum lo}, the coefficient of the old W at step s of
-// block b in date j's remainder and in its running sum, at lag l = (j - b)
-// stride - 1 - s (the distance to date j's sampling step), for 1 <= b < j <=
-// B <= kRespDates.  Every lag l in [0, (j-1) stride - 1] of date j maps to
-// exactly one entry (q = j - b = l / stride + 1, s = q stride - 1 - l); the
-// rest of the table stays zero.  One CTA of kMaxTenor threads, thread t
-// holding tenor t of the responses.
-//  * Euler (pc = 0): coef = kappa G_j(l), G_j(m) = (A^m e_L)[j] by m
-//    applications of the upwind step (backward difference at the last tenor,
-//    simulation_cpu.h:96-108), sum = kappa CG_j(l), CG_j(m) = sum_{r<=m} G_j(r);
-//    kappa = w1.
-//  * predictor-corrector (pc = 1): the remainder is driven at L-1 by w0' W_old
-//    and at L by wL W_old + gL gamma, gamma = W_new - W_old; grouping the terms
-//    by W, the coefficient of the old W at lag l is H1(l) + H2(l+1) with
-//    H1 = w0 G1 + w1 G2 (w0 = wL1, w1 = wL - gL) and H2 = w2 G2 (w2 = gL), G1,
-//    G2 the responses of A2 (three-point stencil a0, a1, a2; Euler rows at
-//    L-1, L) to e_{L-1}, e_L, and the sum likewise with the running sums.
+// Impulse responses of the predictor-corrector step at the sampled tenors,
+// for its response form (path_kernel_pc_resp): entry (row b stride + s,
+// column r = B - j) of resp holds, as FP32 pairs {coef hi, sum hi, coef lo,
+// sum lo}, the coefficient of the old W at step s of block b in date j's
+// remainder and in its running sum, at lag l = (j - b) stride - 1 - s (the
+// distance to date j's sampling step), for 1 <= b < j <= B <= kRespDates.
+// Every lag l in [0, (j-1) stride - 1] of date j maps to exactly one entry
+// (q = j - b = l / stride + 1, s = q stride - 1 - l); the rest of the table
+// stays zero.  One CTA of kMaxTenor threads, thread t holding tenor t of the
+// responses.  The remainder is driven at L-1 by w0' W_old and at L by
+// wL W_old + gL gamma, gamma = W_new - W_old; grouping the terms by W, the
+// coefficient of the old W at lag l is H1(l) + H2(l+1) with H1 = w0 G1 + w1 G2
+// (w0 = wL1, w1 = wL - gL) and H2 = w2 G2 (w2 = gL), G1, G2 the responses of
+// A2 (three-point stencil a0, a1, a2; Euler rows at L-1, L) to e_{L-1}, e_L,
+// and the sum likewise with the running sums.  (The Euler step's table is
+// eresp_table_kernel in hjm_eresp.cu.)
 __global__ void __launch_bounds__(kMaxTenor)
-    response_table_kernel(int nt, double c, int stride, int B, int pc, double w0, double w1, double w2,
+    response_table_kernel(int nt, double c, int stride, int B, double w0, double w1, double w2,
                           float4* __restrict__ resp)
 {
     __shared__ double v_s[kMaxTenor], u_s[kMaxTenor];
@@ -394,22 +279,6 @@ __global__ void __launch_bounds__(kMaxTenor)
         resp[((size_t)b * stride + (size_t)(q * stride - 1 - l)) * kRespRow + (B - t)] =
             make_float4(ch, sh, __double2float_rn(coef - (double)ch), __double2float_rn(sum - (double)sh));
     };
-    if (!pc) {
-        double v = (t == L) ? 1.0 : 0.0;
-        double cum = 0.0;
-        for (int m = 0; m <= M; ++m) {
-            cum += v;
-            put(m, w1 * v, w1 * cum);
-            v_s[t] = v;
-            __syncthreads();
-            if (t < L)
-                v += c * (v_s[t + 1] - v);
-            else if (t == L)
-                v += c * (v - v_s[L - 1]);
-            __syncthreads();
-        }
-        return;
-    }
     const double a0 = 1.0 - c + 0.5 * c * c, a1 = c - c * c, a2 = 0.5 * c * c;
     double g1 = (t == L - 1) ? 1.0 : 0.0, g2 = (t == L) ? 1.0 : 0.0;
     double cg1 = 0.0, cg2 = 0.0, h1p = 0.0, ch1p = 0.0;  // H1, CH1 at the previous lag
@@ -1045,32 +914,11 @@ static cudaError_t launch_fp64_t(const PathParams<double>& P, const double* ext,
     return cudaGetLastError();
 }
 
-template <int NT, bool EXT, bool TRI>
-static cudaError_t launch_fp64_resp_t(const PathParams<double>& P, const float4* resp, const double* ext,
-                                      double* partials, double* estore, cudaStream_t s)
-{
-    const bool sc = P.stride <= kFrameSmemRows;
-    const size_t smem = resp_smem_bytes_parts(P.n_blocks) + (sc ? (size_t)P.stride * kStateRow * 16 : 0);
-    auto k = sc ? path_kernel_fp64_resp<NT, EXT, TRI, true> : path_kernel_fp64_resp<NT, EXT, TRI, false>;
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    const int64_t grid = (P.n_paths + kFp64Cta - 1) / kFp64Cta;
-    k<<<(unsigned)grid, kFp64Cta, smem, s>>>(P, resp, ext, partials, estore);
-    return cudaGetLastError();
-}
-
 template <int NT>
-static cudaError_t launch_fp64_nt(const PathParams<double>& P, bool poly, const float4* resp, const double* ext,
-                                  double* partials, double* estore, cudaStream_t s)
+static cudaError_t launch_fp64_nt(const PathParams<double>& P, bool poly, const double* ext, double* partials,
+                                  double* estore, cudaStream_t s)
 {
     const bool tri = poly && P.svc[0][1] == 0.0 && P.svc[0][2] == 0.0 && P.svc[1][2] == 0.0;
-    if (resp) {
-        if (!poly || P.n_blocks > kRespDates) return cudaErrorInvalidValue;
-        if (ext) return tri ? launch_fp64_resp_t<NT, true, true>(P, resp, ext, partials, estore, s)
-                            : launch_fp64_resp_t<NT, true, false>(P, resp, ext, partials, estore, s);
-        return tri ? launch_fp64_resp_t<NT, false, true>(P, resp, ext, partials, estore, s)
-                   : launch_fp64_resp_t<NT, false, false>(P, resp, ext, partials, estore, s);
-    }
     if (ext) return tri    ? launch_fp64_t<NT, true, kFormPolyTri>(P, ext, partials, estore, s)
                     : poly ? launch_fp64_t<NT, true, kFormPoly>(P, ext, partials, estore, s)
                            : launch_fp64_t<NT, true, kFormTable>(P, ext, partials, estore, s);
@@ -1079,11 +927,11 @@ static cudaError_t launch_fp64_nt(const PathParams<double>& P, bool poly, const 
                   : launch_fp64_t<NT, false, kFormTable>(P, ext, partials, estore, s);
 }
 
-cudaError_t launch_path_fp64(int nt, const PathParams<double>& P, bool poly, const float4* resp, const double* ext,
-                             double* partials, double* estore, cudaStream_t s)
+cudaError_t launch_path_fp64(int nt, const PathParams<double>& P, bool poly, const double* ext, double* partials,
+                             double* estore, cudaStream_t s)
 {
-    if (nt == 51) return launch_fp64_nt<51>(P, poly, resp, ext, partials, estore, s);
-    if (nt == 61) return launch_fp64_nt<61>(P, poly, resp, ext, partials, estore, s);
+    if (nt == 51) return launch_fp64_nt<51>(P, poly, ext, partials, estore, s);
+    if (nt == 61) return launch_fp64_nt<61>(P, poly, ext, partials, estore, s);
     return cudaErrorInvalidValue;
 }
 
@@ -1151,11 +999,11 @@ cudaError_t launch_state_coefs(const PartsFrame& f, int stride, int n_blocks, fl
     return cudaGetLastError();
 }
 
-cudaError_t launch_response_table(int nt, double c, int stride, int n_blocks, bool pc, double w0, double w1,
-                                  double w2, float4* resp, cudaStream_t s)
+cudaError_t launch_response_table_pc(int nt, double c, int stride, int n_blocks, double w0, double w1, double w2,
+                                     float4* resp, cudaStream_t s)
 {
     if (nt < 3 || nt > kMaxTenor || n_blocks > kRespDates || n_blocks >= nt || stride < 1) return cudaErrorInvalidValue;
-    response_table_kernel<<<1, kMaxTenor, 0, s>>>(nt, c, stride, n_blocks, pc ? 1 : 0, w0, w1, w2, resp);
+    response_table_kernel<<<1, kMaxTenor, 0, s>>>(nt, c, stride, n_blocks, w0, w1, w2, resp);
     return cudaGetLastError();
 }
 

@@ -10,6 +10,9 @@
 
 namespace hjm {
 
+// Threads (paths) per CTA of the FP64 path kernels
+constexpr int kFp64Cta = 64;
+
 // Device result block (doubles)
 constexpr int kResEE = 0;                       // [kMaxTenor]
 constexpr int kResPFE = kMaxTenor;              // [kMaxTenor]
@@ -48,12 +51,11 @@ constexpr int kFormTable = 0;    // volatility table PathParams::sv
 constexpr int kFormPoly = 1;     // factors quadratic in T, PathParams::svc
 constexpr int kFormPolyTri = 2;  // ... with factor k of degree <= k
 
-// poly: the volatility factors are polynomials of degree <= 2 in T (PathParams::svc);
-// resp: the response table of the polynomial form's remainder (the response
-// form, at most response_max_dates() dates) followed by the moving-frame
-// coefficients of its parts (launch_state_coefs), or null for the convected form
-cudaError_t launch_path_fp64(int nt, const PathParams<double>& P, bool poly, const float4* resp, const double* ext,
-                             double* partials, double* estore, cudaStream_t s);
+// The convected FP64 path kernel.  poly: the volatility factors are
+// polynomials of degree <= 2 in T (PathParams::svc), else the table step.
+// (The response forms of the Euler step are in hjm_eresp.h.)
+cudaError_t launch_path_fp64(int nt, const PathParams<double>& P, bool poly, const double* ext, double* partials,
+                             double* estore, cudaStream_t s);
 int response_max_dates();
 // The response form of the volatility-table step (FP64, either scheme: the
 // table carries the scheme): vresp from launch_response_table_vol with the
@@ -64,10 +66,10 @@ size_t response_table_vol_elems(int stride, int n_blocks);  // double2 entries
 cudaError_t launch_response_table_vol(int nt, double c, int stride, int n_blocks, bool pc, const double* sv,
                                       double2* vresp, cudaStream_t s);
 size_t response_table_elems(int stride, int n_blocks);  // float4 entries: responses, coefficients, prefixes
-// Euler: w1 = kappa = -2 c dtau^2 (w0, w2 unused); predictor-corrector: w0 =
-// wL1, w1 = wL - gL, w2 = gL (PcParams)
-cudaError_t launch_response_table(int nt, double c, int stride, int n_blocks, bool pc, double w0, double w1,
-                                  double w2, float4* resp, cudaStream_t s);
+// The predictor-corrector response form's table: w0 = wL1, w1 = wL - gL,
+// w2 = gL (PcParams)
+cudaError_t launch_response_table_pc(int nt, double c, int stride, int n_blocks, double w0, double w1, double w2,
+                                     float4* resp, cudaStream_t s);
 // The active prefix of each row of the response table in resp (after the
 // table and the coefficient rows), from the table's values
 cudaError_t launch_response_active(int stride, int n_blocks, float4* resp, cudaStream_t s);
@@ -119,17 +121,7 @@ struct PcParams {
     T wL1, wL, gL;         // sources: -c^2 dtau^2 W at L-1; -(2c + c^2) dtau^2 W - c dtau^2 gamma at L
 };
 
-// The frames of the two schemes' polynomial steps on (S, U, W)
-inline PartsFrame euler_parts_frame(const PathParams<double>& P)
-{
-    PartsFrame f{};
-    f.n01 = P.k1;
-    f.n02 = P.k2;
-    f.n12 = 2.0 * P.k1;
-    for (int k = 0; k < kFactors; ++k)
-        for (int c = 0; c < 3; ++c) f.bm[c][k] = P.svc[k][c];
-    return f;
-}
+// The frame of the predictor-corrector's polynomial step on (S, U, W)
 inline PartsFrame pc_parts_frame(const PcParams<double>& Q)
 {
     PartsFrame f{};

@@ -294,3 +294,155 @@ __device__ __forceinline__ void resp_groups(int n_act, Fn&& fn)
 }
 
 }  // namespace hjm
+
+namespace hjm {
+
+// ---------------------------------------------------------------------------
+// The polynomial parts with NP = 3 or 4 components (degree <= 3), for the
+// generalised Euler response kernel (hjm_eresp.cu).  The parts are the
+// coefficients x_d of the stochastic curve's polynomial sum_d x_d t^d in
+// t = T - tau0 (tau0 = 0 for the quadratic forms, the last tenor T_L for the
+// cubic one).  The upwind step takes t^d to t^d + c ((t + dtau)^d - t^d) at
+// every tenor below L (a translation, so the centre does not matter), i.e.
+// x <- M x + B phi with M = I + N,
+//     N[i][d] = c C(d, i) dtau^(d - i)   (i < d):
+//     n01 = c dtau, n02 = c dtau^2, n03 = c dtau^3, n12 = 2 c dtau,
+//     n13 = 3 c dtau^2, n23 = 3 c dtau,
+// and at L, where the scheme takes the backward difference, the polynomial
+// is off by -c (P(T_L + dtau) - 2 P(T_L) + P(T_L - dtau)) e_L: the remainder's
+// source.  With tau0 = T_L that second difference vanishes for t^3 (and for
+// 1, t), so the source stays -2 c dtau^2 x_2 e_L, one term in W = x_2.
+// N is nilpotent (N^NP = 0), so every power series in N is a cubic in N:
+//     M^a   = sum_i C(a, i) N^i,
+//     M^-k  = sum_i (-1)^i C(k + i - 1, i) N^i,
+//     Q(a)  = sum_{e=1..a} M^e = a I + sum_{i>=1} C(a + 1, i + 1) N^i.
+// A matrix c0 I + c1 N + c2 N^2 + c3 N^3 has the entries of PolyN below.
+// ---------------------------------------------------------------------------
+struct PartsN {
+    double n01, n02, n03, n12, n13, n23;
+};
+
+// Entries of c0 I + c1 N + c2 N^2 + c3 N^3 above the diagonal (the diagonal is c0).
+struct PolyN {
+    double d, e01, e02, e03, e12, e13, e23;
+    __host__ __device__ PolyN() : d(0), e01(0), e02(0), e03(0), e12(0), e13(0), e23(0) {}
+    __host__ __device__ PolyN(const PartsN& n, double c0, double c1, double c2, double c3)
+    {
+        d = c0;
+        e01 = c1 * n.n01;
+        e12 = c1 * n.n12;
+        e23 = c1 * n.n23;
+        e02 = c1 * n.n02 + c2 * (n.n01 * n.n12);
+        e13 = c1 * n.n13 + c2 * (n.n12 * n.n23);
+        e03 = c1 * n.n03 + c2 * (n.n01 * n.n13 + n.n02 * n.n23) + c3 * (n.n01 * n.n12 * n.n23);
+    }
+    // row r of the matrix times x (NP = 4 entries, unused ones zero)
+    __host__ __device__ double row(int r, const double* x) const
+    {
+        switch (r) {
+            case 0: return d * x[0] + e01 * x[1] + e02 * x[2] + e03 * x[3];
+            case 1: return d * x[1] + e12 * x[2] + e13 * x[3];
+            case 2: return d * x[2] + e23 * x[3];
+            default: return d * x[3];
+        }
+    }
+};
+
+// M^a and Q(a) of a block of a steps, FP64, formed once on the host.
+struct BlockFrameN {
+    PolyN Ma, Qa;
+};
+
+inline double binom(double a, int i)
+{
+    double r = 1.0;
+    for (int j = 0; j < i; ++j) r = r * (a - j) / (double)(j + 1);
+    return r;
+}
+
+inline BlockFrameN block_frame_n(const PartsN& n, int a)
+{
+    const double da = (double)a;
+    BlockFrameN f;
+    f.Ma = PolyN(n, 1.0, binom(da, 1), binom(da, 2), binom(da, 3));
+    f.Qa = PolyN(n, da, binom(da + 1.0, 2), binom(da + 1.0, 3), binom(da + 1.0, 4));
+    return f;
+}
+
+// The degrees of the three factors packed in one template constant.
+__host__ __device__ constexpr int degs_pack(int d0, int d1, int d2) { return d0 | (d1 << 2) | (d2 << 4); }
+__host__ __device__ constexpr int degs_of(int pack, int k) { return (pack >> (2 * k)) & 3; }
+__host__ __device__ constexpr int degs_parts(int pack)
+{
+    return 1 + (degs_of(pack, 0) > degs_of(pack, 1) ? (degs_of(pack, 0) > degs_of(pack, 2) ? degs_of(pack, 0)
+                                                                                          : degs_of(pack, 2))
+                                                    : (degs_of(pack, 1) > degs_of(pack, 2) ? degs_of(pack, 1)
+                                                                                          : degs_of(pack, 2)));
+}
+// Coefficient-row length of NP parts: entry 3 c + k for part c and factor k,
+// then (NP = 4) the source coefficient s n23 of the step.
+__host__ __device__ constexpr int frame_row(int np) { return np == 4 ? 13 : 9; }
+
+// One step of the NP parts in the moving frame: y_c += C(s)[c][k] phi_k and
+// v_c += G(s)[c][k] phi_k for the terms (c, k) with c <= deg_k (part c of
+// M^-(s+1) B is zero for factors of lower degree), each part renormalised
+// after its last term.  cr: the step's coefficient row (shared memory or L1).
+template <int DEGS, bool EXT, bool SHARED>
+__device__ __forceinline__ void frame_step_n(float2 (&Y)[degs_parts(DEGS)], float2 (&Yl)[degs_parts(DEGS)],
+                                             const float4* __restrict__ cr, const float (&ph)[3],
+                                             const float (&pl)[3])
+{
+    constexpr int NP = degs_parts(DEGS);
+    float4 q[3 * NP];
+#pragma unroll
+    for (int t = 0; t < 3 * NP; ++t)
+        if (t / 3 <= degs_of(DEGS, t % 3)) {
+            if constexpr (SHARED)
+                q[t] = cr[t];
+            else
+                q[t] = __ldg(cr + t);
+        }
+#pragma unroll
+    for (int c = 0; c < NP; ++c) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            if (c > degs_of(DEGS, k)) continue;
+            const float4 e = q[3 * c + k];
+            const float2 kh = make_float2(e.x, e.y), kl = make_float2(e.z, e.w);
+            if constexpr (EXT)
+                df_acc(Y[c], Yl[c], kh, kl, make_float2(ph[k], ph[k]), make_float2(pl[k], pl[k]),
+                       make_float2(-ph[k], -ph[k]));
+            else
+                df_acc_w(Y[c], Yl[c], kh, kl, make_float2(ph[k], ph[k]), make_float2(-ph[k], -ph[k]));
+        }
+        df_renorm(Y[c], Yl[c]);
+    }
+}
+
+// The end of a block of the NP parts: x = M^a y, Z += Q(a) y - v (z[c *
+// stride_z], FP64 in shared memory), then y re-anchored on x (v = 0).
+template <int NP>
+__device__ __forceinline__ void frame_block_end_n(float2 (&Y)[NP], float2 (&Yl)[NP], const BlockFrameN& F, double* z,
+                                                  int stride_z, double (&x)[NP], double (&Z)[NP])
+{
+    double y[4] = {0.0, 0.0, 0.0, 0.0}, v[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+    for (int c = 0; c < NP; ++c) {
+        y[c] = widen_f32(Y[c].x) + widen_f32(Yl[c].x);
+        v[c] = widen_f32(Y[c].y) + widen_f32(Yl[c].y);
+    }
+#pragma unroll
+    for (int c = 0; c < NP; ++c) {
+        x[c] = F.Ma.row(c, y);
+        Z[c] = z[c * stride_z] + (F.Qa.row(c, y) - v[c]);
+        z[c * stride_z] = Z[c];
+    }
+#pragma unroll
+    for (int c = 0; c < NP; ++c) {
+        const float xh = __double2float_rn(x[c]);
+        Y[c] = make_float2(xh, 0.0f);
+        Yl[c] = make_float2(__double2float_rn(x[c] - (double)xh), 0.0f);
+    }
+}
+
+}  // namespace hjm

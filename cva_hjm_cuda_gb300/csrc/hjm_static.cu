@@ -46,6 +46,7 @@
 #include <string>
 
 #include "../../include/hjm_cva.h"
+#include "hjm_eresp.h"
 #include "hjm_kernels.h"
 
 using namespace hjm;
@@ -53,6 +54,7 @@ using namespace hjm;
 namespace hjm {
 void set_thread_error(const char* msg);  // hjm_capi.cu: the message hjm_last_error(NULL) returns
 bool fit_quadratic_vols(const double* vol, int nt, double dtau, double* coef);  // hjm_capi.cu
+bool fit_cubic_resid(const double* vol, int nt, double dtau, double* coef, int* degs, double* resid);  // hjm_capi.cu
 }
 
 namespace {
@@ -307,24 +309,38 @@ hjm_status hjm_run_static(void* cuda_stream, int32_t n_tenor, double dtau, const
             for (int k = 0; k < kFactors; ++k)
                 for (int d = 0; d < 3; ++d) P.svc[k][d] = sq * coef[k * 3 + d];
         const size_t entries = response_table_vol_elems((int)stride, B);
-        if (poly && B >= 2 && B <= response_max_dates() && response_table_elems((int)stride, B) <= kStaticRespEntries) {
-            // the decomposition: the remainder's table and the coefficients of
-            // S, U, W (FP32 pairs, 16 bytes per entry like the double2 array)
-            // in the static array
-            const double c = dt / dtau;
+        // a table that is a cubic up to a small residual (the reference's own PCA table)
+        double cubic[HJM_N_FACTOR * 4], resid[HJM_N_FACTOR * HJM_MAX_TENOR];
+        int cdegs[HJM_N_FACTOR];
+        const bool cub = !poly && fit_cubic_resid(vol_host, n_tenor, dtau, cubic, cdegs, resid);
+        const int nres = cub ? eresp_residual_factors(resid, vol_host, n_tenor) : 0;
+        if ((poly || cub) && eresp_windows(B, nullptr, nullptr) == 1 &&
+            eresp_table_elems((int)stride, B, cub ? 4 : 3, nres, 1) <= kStaticRespEntries) {
+            // the decomposition's response form in one window: its table (FP32
+            // pairs, 16 bytes per entry like the double2 array) in the static array
+            EulerRespFrame fr;
+            int degs;
+            eresp_make_frame(dt, dtau, n_tenor, P.svc, cub ? cubic : nullptr, cdegs, eresp_window_centre(dtau, 1, B), fr,
+                             degs);
+            for (int i = 0; i < HJM_N_FACTOR * n_tenor; ++i) resid[i] *= sq;
             float4* table = reinterpret_cast<float4*>(resp_table);
-            STATIC_CUDA(cudaMemsetAsync(table, 0, sizeof(float4) * response_table_elems((int)stride, B), s));
-            STATIC_CUDA(launch_response_table(n_tenor, c, (int)stride, B, false, 0.0, -2.0 * P.k2, 0.0, table, s));
-            STATIC_CUDA(launch_response_active((int)stride, B, table, s));
-            STATIC_CUDA(launch_state_coefs(euler_parts_frame(P), (int)stride, B, table, s));
-            STATIC_CUDA(launch_path_fp64(n_tenor, P, true, table, nullptr, partials, nullptr, s));
+            STATIC_CUDA(launch_eresp_tables(n_tenor, dt / dtau, dtau, (int)stride, B, &fr, 1, cub ? resid : nullptr, nres,
+                                            table, s));
+            EulerRespParams E;
+            std::memset(&E, 0, sizeof(E));
+            E.P = P;
+            E.frame = block_frame_n(fr.n, (int)stride);
+            E.row = eresp_row(B);
+            E.renorm = cub ? 1 : 0;  // one window: the residual's terms only (as hjm_run)
+            STATIC_CUDA(
+                launch_path_fp64_eresp(E, &fr, degs, nres, table, nullptr, partials, nullptr, nullptr, s, nullptr));
         } else if (B >= 2 && B <= response_max_dates() && entries <= kStaticRespEntries) {
             // the response form: its table (zero outside the live entries) into the static array
             STATIC_CUDA(cudaMemsetAsync(resp_table, 0, sizeof(double2) * entries, s));
             STATIC_CUDA(launch_response_table_vol(n_tenor, dt / dtau, (int)stride, B, false, &P.sv[0][0], resp_table, s));
             STATIC_CUDA(launch_path_fp64_vresp(n_tenor, P, resp_table, nullptr, partials, nullptr, s));
         } else {
-            STATIC_CUDA(launch_path_fp64(n_tenor, P, poly, nullptr, nullptr, partials, nullptr, s));
+            STATIC_CUDA(launch_path_fp64(n_tenor, P, poly, nullptr, partials, nullptr, s));
         }
     }
     STATIC_CUDA(launch_reduce(partials, n_ctas, R, sums, F, result, s));

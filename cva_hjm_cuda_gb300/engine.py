@@ -144,10 +144,12 @@ class HJMEngine:
         return self.vol_form() != "table"
 
     def vol_form(self) -> str:
-        """The step the current market runs: "table", "poly" or "poly_tri"."""
+        """The step the current market runs: "table", "poly" (quadratic factors),
+        "poly_tri" (factor k of degree <= k) or "cubic_resid" (cubic factors up to a
+        residual table: the FP64 Euler valuations; other modes run the table step)."""
         active = C.c_int32(0)
         self._check(self.lib.hjm_ctx_vol_decomposition(self.ctx, C.byref(active)))
-        return ("table", "poly", "poly_tri")[active.value]
+        return ("table", "poly", "poly_tri", "cubic_resid")[active.value]
 
     def set_market(self, market: Market, drift: bool = True) -> None:
         spot, vol = _f64(market.spot), _f64(market.vol).ravel()

@@ -109,9 +109,17 @@ hjm_status hjm_ctx_set_scheme(hjm_ctx* ctx, int32_t scheme);
  * carry the stochastic curve as S + U T + W T^2 plus a remainder driven only at
  * the last tenor, instead of adding the three factor columns to every tenor
  * each step (simulation_gpu.cu:153-180).  enable = 0 forces the generic
- * table-driven step; default 1.  hjm_ctx_vol_decomposition reports what the
- * current market runs: 0 the table step, 1 the decomposition, 2 the
- * decomposition with factor k of degree <= k (three zero coefficients). */
+ * table-driven step; default 1.  A table that is no quadratic but a cubic in
+ * each factor up to a residual of at most 2^-20 of the factor's scale (a PCA
+ * table printed to a fixed number of decimals, as the reference's own
+ * simulation_gpu_testing.cpp:47-63, whose factors 2 and 3 are cubics to
+ * 1.1e-7) runs, in FP64 Euler valuations, the cubic decomposition in the
+ * basis (T - T_L)^d with the residual's impulse responses carried beside the
+ * remainder's (other modes run the table step on it).
+ * hjm_ctx_vol_decomposition reports what the current market runs: 0 the
+ * table step, 1 the decomposition, 2 the decomposition with factor k of
+ * degree <= k (three zero coefficients), 3 the cubic decomposition with a
+ * residual table. */
 hjm_status hjm_ctx_set_vol_decomposition(hjm_ctx* ctx, int32_t enable);
 hjm_status hjm_ctx_vol_decomposition(hjm_ctx* ctx, int32_t* active);
 
@@ -123,15 +131,20 @@ hjm_status hjm_ctx_vol_decomposition(hjm_ctx* ctx, int32_t* active);
  * responses of the convection (HJM_REMAINDER_RESPONSE: one double-FP32 term
  * per such date per step, on the FP32 pipe; the remainder is ~1e-5 of the
  * curve; the polynomial parts S, U, W then advance as double-FP32 sums in a
- * moving frame, with FP64 only at the sampled dates).  With a volatility table of any shape (no decomposition) the whole
- * stochastic curve is either convected with the noise injected at every tenor,
- * or carried in the response form as sums of the three factors' impulse
- * responses (six FP64 FMAs per date per step).  The response form holds at
- * most HJM_RESPONSE_MAX_DATES dates (a run with more fails with
- * HJM_ERR_INVALID_ARGUMENT when it is forced).  HJM_REMAINDER_AUTO (default)
- * takes the form with fewer FP64 operations for the run.  Both time schemes;
- * the forms agree to rounding; mixed precision always convects.  The report
- * names the form a valuation ran ("remainder"). */
+ * moving frame, with FP64 only at the sampled dates).  The Euler step's
+ * response form takes any number of dates: a run with more than
+ * HJM_RESPONSE_MAX_DATES is priced in windows of at most that many dates, one
+ * launch each, the later windows passing each path's later cash flows to the
+ * earlier ones.  With a volatility table of any shape (no decomposition) the
+ * whole stochastic curve is either convected with the noise injected at every
+ * tenor, or carried in the response form as sums of the three factors'
+ * impulse responses (six FP64 FMAs per date per step); that form, and the
+ * predictor-corrector's, hold at most HJM_RESPONSE_MAX_DATES dates (a run with
+ * more fails with HJM_ERR_INVALID_ARGUMENT when it is forced).
+ * HJM_REMAINDER_AUTO (default) takes the response form for the Euler step
+ * with a decomposition, else the form with fewer FP64 operations for the run.
+ * Both time schemes; the forms agree to rounding; mixed precision always
+ * convects.  The report names the form a valuation ran ("remainder"). */
 #define HJM_REMAINDER_AUTO 0
 #define HJM_REMAINDER_CONVECT 1
 #define HJM_REMAINDER_RESPONSE 2

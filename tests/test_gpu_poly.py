@@ -110,13 +110,14 @@ def generic_path(engine):
         engine.vol_decomposition(True)
 
 
-def test_reference_table_is_detected_as_polynomial(engine, golden_10y):
+def test_quadratic_table_is_detected_as_polynomial(engine, golden_10y):
     from conftest import market_from_golden
 
-    mk, sw = market_from_golden(golden_10y)
+    mk, sw = market_from_golden(golden_10y)  # the configured workloads' synthetic factors
     engine.set_market(mk)
     assert engine.vol_decomposition()
     assert engine.vol_form() == "poly_tri"  # factor k of degree k, as fitted from the table
+    # a bump of 1.6e-4 of the scale is neither a quadratic nor a cubic up to 2^-20
     bumped = Market(vol=mk.vol + 1e-6 * np.sin(np.arange(51))[None, :])
     engine.set_market(bumped)
     assert not engine.vol_decomposition()
@@ -332,11 +333,19 @@ def test_remainder_form_choice_and_limits(engine, remainder_form, tmp_path):
     engine.set_swap(Swap(n_tenor=61, n_periods=60))
     cfg30 = RunConfig(n_paths=256, n_steps=3000)
     engine.run(cfg30, "fp64")
-    assert engine.remainder_form() == "convect"  # 60 dates
+    assert engine.remainder_form() == "response"  # 60 dates: three windows
+    remainder_form("convect")
+    engine.run(cfg30, "fp64")
+    assert engine.remainder_form() == "convect"
+    # the volatility-table response form holds at most 24 dates
+    engine.set_market(_bumpy_market(61))
     remainder_form("response")
     with pytest.raises(_lib.HJMError) as ei:
         engine.run(cfg30, "fp64")
     assert "24 dates" in str(ei.value)
+    remainder_form("auto")
+    engine.run(cfg30, "fp64")
+    assert engine.remainder_form() == "convect"
     engine.set_market(Market(vol=Market().vol * (1.0 + 0.1 * np.cos(np.arange(51) / 7.0))[None, :]))
     engine.set_swap(Swap())
     remainder_form("auto")
