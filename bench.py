@@ -52,6 +52,15 @@ WORKLOADS = {
     # 64-swap netting set on a 61-tenor curve, mixed precision
     "netting": {"precision": "mixed", "n_paths": 2_097_152, "dtype": "f32+f64", "n_tenor": 61, "n_steps": 3000,
                 "name": "hjm-3f-61tenor-netting64-30y-mixed-2097152paths-3000steps"},
+    # the reference driver's own PCA volatility table (cubic factors to its
+    # rounding) on the 10y payer swap, FP64
+    "reftable": {"precision": "fp64", "n_paths": 1_048_576, "dtype": "f64", "n_tenor": 51, "n_steps": 1000,
+                 "market": "reference", "name": "hjm-3f-51tenor-reference-pca-table-irs-10y-fp64-1048576paths"},
+    # the reference driver's own workload: its curve, table, drift, accruals,
+    # the 25y swap N = 10, K = 6.7% (50 dates), FP64
+    "driver25y": {"precision": "fp64", "n_paths": 1_048_576, "dtype": "f64", "n_tenor": 51, "n_steps": 2500,
+                  "market": "reference", "swap": "driver",
+                  "name": "hjm-3f-51tenor-reference-driver-workload-25y-fp64-1048576paths"},
 }
 FLUSH_BYTES = 256 << 20
 
@@ -168,6 +177,39 @@ def response_fp32_flops_per_path(n_tenor: int, n_steps: int, stride: int, form: 
     slots = int((4 * ((pre + 3) // 4)).sum())
     terms = 6 if form == "poly_tri" else 9
     return 30 * slots + (26 * terms + 18) * (B - 1) * stride
+
+
+def eresp_windows(n_blocks: int) -> list[tuple[int, int]]:
+    """The Euler response form's windows of dates, latest first (eresp_windows)."""
+    out, h = [], n_blocks
+    while h >= 1:
+        lo = h - 23
+        if lo <= 2:
+            lo = 1
+        out.append((lo, h))
+        h = lo - 1
+    return out
+
+
+def cubic_fp32_flops_per_path(n_tenor: int, n_steps: int, stride: int, nres: int = 2) -> int:
+    """FP32 flops per path of the Euler response form with cubic factors (factor 1
+    constant, factors 2 and 3 cubic) and a residual table, counted as
+    response_fp32_flops_per_path counts the quadratic form: per window, per
+    evolved step up to its last date, each live date slot of the window in
+    groups of four (the residual reaches every tenor, so every date still to be
+    sampled is active): the remainder's double-FP32 term (30 flops), the
+    residual's packed FMAs (4 flops per residual factor) and the renormalisation
+    every fourth step (6 flops / 4); the parts' moving frame, 9 terms of 26
+    flops, 4 renormalisations of 6, and the source w = y_W + sigma y_X in
+    double-FP32 (14 flops)."""
+    B = n_steps // stride
+    total = 0
+    for lo, hi in eresp_windows(B):
+        for b in range(1, hi):
+            live = sum(1 for j in range(max(lo, 2), hi + 1) if j > b)
+            slots = 4 * ((live + 3) // 4)
+            total += stride * (slots * (30 + 4 * nres + 1.5) + 9 * 26 + 4 * 6 + 14)
+    return int(total)
 
 
 class ClockSampler:
@@ -315,6 +357,15 @@ def run_ours(args) -> None:
     prec = wl["precision"]
     n_steps = wl["n_steps"]
     mk, sw = Market(n_tenor=wl["n_tenor"]), Swap(n_tenor=wl["n_tenor"])
+    if wl.get("market") == "reference":
+        # the reference driver's inputs, from the committed golden fixture
+        g = json.loads((ROOT / "tests" / "golden" / "ref_driver_own_market.json").read_text())
+        vol = np.array(g["vol"]).reshape(3, 51)
+        if wl.get("swap") == "driver":
+            mk = Market(n_tenor=51, dtau=0.5, spot=np.array(g["spot"]), vol=vol, drift=np.array(g["drift"]))
+            sw = Swap(notional=g["notional"], strike=g["strike"], n_tenor=51, dtau=0.5, accrual=np.array(g["accrual"]))
+        else:
+            mk = Market(vol=vol)
     stride = int(round(mk.dtau / DT))
     eng = HJMEngine(local_rank)
     # a dedicated (non-default) stream: the engine and the timing events share it
@@ -446,7 +497,14 @@ def run_ours(args) -> None:
     traffic = profiled_traffic(f"{prec}-table-{n_paths}" if args.table_step else f"{prec}-{n_paths}")
     side = None
     bound = "fp64_pipe" if prec == "fp64" else "fp32_pipe"
-    if prec == "fp64" and remainder == "response" and form != "table" and not is_adjoint:
+    if prec == "fp64" and remainder == "response" and form == "cubic_resid":
+        flops = cubic_fp32_flops_per_path(mk.n_tenor, n_steps, stride) * n_paths
+        achieved = flops / (path_ms * 1e-3) / 1e12
+        peak = extras.get("measured_fma_peak_tflops", {}).get("fp32")
+        bound = "fp32_pipe (double-FP32)"
+        fma_busy = profiled_value("fma_pipe_cycles_active", f"{args.workload}-{n_paths}")
+        side = {"pipe": "fp64 (parts at the sampled dates)", "note": "see the headline workload"}
+    elif prec == "fp64" and remainder == "response" and form != "table" and not is_adjoint:
         # the per-step work is double-FP32 on the FP32 pipe: that is the
         # roofline; the FP64 pipe only forms the parts at the sampled dates
         side = {"pipe": "fp64 (parts at the sampled dates)", "algorithmic_flops_per_launch": flops,
@@ -461,9 +519,11 @@ def run_ours(args) -> None:
     roofline = {"bound": bound, "achieved": achieved, "peak": peak,
                 "unit": "TFLOP/s", "frac": (achieved / peak) if peak else None, "traffic": traffic,
                 "kernel": (f"adjoint_kernel<{mk.n_tenor},ckpt,{form}>" if is_adjoint else
+                           "path_kernel_fp64_eresp<philox,degs(0,3,3),residual2>"
+                           if prec == "fp64" and remainder == "response" and form == "cubic_resid" else
                            f"path_kernel_fp64_vresp<{mk.n_tenor},philox>"
                            if prec == "fp64" and remainder == "response" and form == "table" else
-                           f"path_kernel_fp64_resp<{mk.n_tenor},philox,{form}>"
+                           "path_kernel_fp64_eresp<philox,degs(0,1,2)>"
                            if prec == "fp64" and remainder == "response" else
                            f"path_kernel_fp64<{mk.n_tenor},philox,{form}>" if prec == "fp64" else
                            f"path_kernel_mixed<{mk.n_tenor},philox,{form}>"),
@@ -514,7 +574,9 @@ def run_ours(args) -> None:
                    "n_tenor": mk.n_tenor, "factors": 3, "sampled_dates": n_steps // stride,
                    "pfe_quantile": None if is_adjoint else 0.975, "hazard": 0.02,
                    "recovery": 0.4, "seed": SEED,
-                   "vol_form": ("quadratic factors (detected in the volatility table): decomposed step" if vol_form_poly
+                   "vol_form": ("cubic factors with a residual table (the reference driver's PCA table): "
+                                "decomposed step" if vol_form == "cubic_resid" else
+                                "quadratic factors (detected in the volatility table): decomposed step" if vol_form_poly
                                 else "volatility table: generic step"),
                    "remainder": remainder,
                    "arithmetic": (("FP64 deterministic curve, parts at the sampled dates, pricing, discounting "
