@@ -293,6 +293,54 @@ __device__ __forceinline__ void resp_groups(int n_act, Fn&& fn)
     }
 }
 
+// resp_groups with the step's other work, tail(), in one basic block with
+// the last M groups (groups M-1 .. 0; all active groups when fewer are): the
+// tail's instructions and those groups' chains interleave instead of
+// following one another.  Groups above them keep their own blocks.
+template <int M, typename Fn, typename Tail>
+__device__ __forceinline__ void resp_groups_tail(int n_act, Fn&& fn, Tail&& tail)
+{
+    static_assert(kRespSlots == 24 && M >= 1 && M <= 3, "six groups of four slots; 1 to 3 merged");
+    using I0 = std::integral_constant<int, 0>;
+    using I1 = std::integral_constant<int, 1>;
+    using I2 = std::integral_constant<int, 2>;
+    switch ((n_act + 3) >> 2) {
+        case 6:
+            fn(std::integral_constant<int, 5>{});
+            [[fallthrough]];
+        case 5:
+            fn(std::integral_constant<int, 4>{});
+            [[fallthrough]];
+        case 4:
+            fn(std::integral_constant<int, 3>{});
+            [[fallthrough]];
+        case 3:
+            fn(I2{});
+            if constexpr (M >= 3) {
+                fn(I1{});
+                fn(I0{});
+                tail();
+                break;
+            }
+            [[fallthrough]];
+        case 2:
+            fn(I1{});
+            if constexpr (M >= 2) {
+                fn(I0{});
+                tail();
+                break;
+            }
+            [[fallthrough]];
+        case 1:
+            fn(I0{});
+            tail();
+            break;
+        default:
+            tail();
+            break;
+    }
+}
+
 }  // namespace hjm
 
 namespace hjm {
