@@ -494,7 +494,8 @@ def run_ours(args) -> None:
                                              "how": "hjm_measure_fma_peak: 8 independent FMA chains per thread, "
                                                     "8 CTAs x 256 threads per SM, best of 3 (2 flops per FMA)"}
     achieved = flops / (path_ms * 1e-3) / 1e12
-    traffic = profiled_traffic(f"{prec}-table-{n_paths}" if args.table_step else f"{prec}-{n_paths}")
+    traffic = profiled_traffic(f"{prec}-table-{n_paths}" if args.table_step else
+                               f"{args.workload}-{n_paths}" if wl.get("market") == "reference" else f"{prec}-{n_paths}")
     side = None
     bound = "fp64_pipe" if prec == "fp64" else "fp32_pipe"
     if prec == "fp64" and remainder == "response" and form == "cubic_resid":
