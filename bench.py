@@ -485,14 +485,13 @@ def run_ours(args) -> None:
              * (2 if is_adjoint else 1))
     extras = {}
     peak_key = "fp64" if prec == "fp64" else "mixed"
-    peak = None
-    if not args.no_extras:
-        peak64 = max(eng.fma_peak_tflops("fp64") for _ in range(2))
-        peak32 = max(eng.fma_peak_tflops("mixed") for _ in range(2))
-        peak = peak64 if peak_key == "fp64" else peak32
-        extras["measured_fma_peak_tflops"] = {"fp64": peak64, "fp32": peak32,
-                                             "how": "hjm_measure_fma_peak: 8 independent FMA chains per thread, "
-                                                    "8 CTAs x 256 threads per SM, best of 3 (2 flops per FMA)"}
+    # the roofline denominators, measured on this GPU (a fraction of a second)
+    peak64 = max(eng.fma_peak_tflops("fp64") for _ in range(2))
+    peak32 = max(eng.fma_peak_tflops("mixed") for _ in range(2))
+    peak = peak64 if peak_key == "fp64" else peak32
+    extras["measured_fma_peak_tflops"] = {"fp64": peak64, "fp32": peak32,
+                                         "how": "hjm_measure_fma_peak: 8 independent FMA chains per thread, "
+                                                "8 CTAs x 256 threads per SM, best of 3 (2 flops per FMA)"}
     achieved = flops / (path_ms * 1e-3) / 1e12
     traffic = profiled_traffic(f"{prec}-table-{n_paths}" if args.table_step else
                                f"{args.workload}-{n_paths}" if wl.get("market") == "reference" else f"{prec}-{n_paths}")
