@@ -13,6 +13,8 @@ that straddle two CTAs.
 * config 2: 1,048,576 paths x 1,000 steps, FP64: per-path exposures within
   1e-10 relative (1e-13 of the exposure scale for values near zero);
 * config 3: 4,194,304 paths, mixed precision: within 1e-4 of the exposure scale;
+* the reference driver's PCA table at 1,048,576 paths, FP64 (the cubic form
+  with its residual): as config 2;
 * config 4: 1,048,576 paths, the adjoint: checkpoints every 32 steps against
   the store-the-seeds mode (1e-4), and the gradient of the whole run equal to
   the mean of the gradients of its 16 path ranges (the estimator is a path
@@ -24,6 +26,7 @@ import numpy as np
 import pytest
 
 import oracle_lib as O
+from conftest import load_golden
 from cva_hjm_cuda_gb300.market import DEFAULT_VOL_COEFFS, Market, RunConfig, Swap, nelson_siegel_curve, tenor_grid
 
 pytestmark = pytest.mark.gpu
@@ -75,6 +78,30 @@ def test_config2_fp64_sampled_paths_vs_oracle(engine):
     bad = (err > 1e-10 * np.abs(want)) & (err > 1e-13 * scale)
     assert not np.any(bad), f"max rel err {np.max(err / np.maximum(np.abs(want), 1e-300)):.3e}"
     # the EE of the full run is the mean of its exposures (reduction of 16,384 CTA rows)
+    np.testing.assert_allclose(v.ee[:21], x[:21].mean(axis=1), rtol=1e-12, atol=1e-12 * np.max(v.ee))
+
+
+def test_reference_table_1m_sampled_paths_vs_oracle(engine):
+    """The reference driver's PCA table (cubic factors with a residual) at 1,048,576 paths,
+    FP64, the 10y swap: the cubic response form's launch re-priced on 4,096 paths."""
+    g = load_golden("ref_driver_own_market.json")
+    mk, sw = Market(vol=np.array(g["vol"]).reshape(3, 51)), Swap()
+    cfg = RunConfig(n_paths=1_048_576, n_steps=1000, dt=0.01, seed=1234)
+    engine.set_market(mk)
+    engine.set_swap(sw)
+    assert engine.vol_form() == "cubic_resid"
+    engine.keep_exposures(True)
+    try:
+        v = engine.run(cfg, "fp64", pfe=False)
+        x = engine.exposures()
+    finally:
+        engine.keep_exposures(False)
+    assert engine.remainder_form() == "response"
+    got, want = _resample(engine, mk, sw, cfg, x, _sample_starts(cfg.n_paths, 64), 21)
+    scale = np.max(np.abs(want))
+    err = np.abs(got - want)
+    bad = (err > 1e-10 * np.abs(want)) & (err > 1e-13 * scale)
+    assert not np.any(bad), f"max rel err {np.max(err / np.maximum(np.abs(want), 1e-300)):.3e}"
     np.testing.assert_allclose(v.ee[:21], x[:21].mean(axis=1), rtol=1e-12, atol=1e-12 * np.max(v.ee))
 
 

@@ -72,10 +72,11 @@ def test_static_entry_matches_hjm_run_twice(precision, rtol):
 
 
 @pytest.mark.skipif(not _have_gpu(), reason="no CUDA device")
-@pytest.mark.parametrize("case", ["bumpy-table", "table-beyond-static"])
+@pytest.mark.parametrize("case", ["bumpy-table", "table-beyond-static", "reference-pca-table"])
 def test_static_fp64_response_and_fallback_match_hjm_run(case):
     """FP64 static runs take a response form when its table fits the static
-    array: the polynomial one for quadratic factors (the test above), the
+    array: the polynomial one for quadratic factors (the test above) and for
+    cubic factors with a residual table (the reference's PCA table), the
     volatility-table one for any other table (bumpy-table), the convected step
     when neither fits (1,000 steps per date); all equal hjm_run within 1e-10."""
     from cva_hjm_cuda_gb300.engine import HJMEngine
@@ -83,6 +84,14 @@ def test_static_fp64_response_and_fallback_match_hjm_run(case):
     lib = _lib.load()
     if case == "bumpy-table":
         mk = Market(vol=Market().vol * (1.0 + 0.1 * np.cos(np.arange(51) / 7.0))[None, :])
+        cfg = RunConfig(n_paths=20_000, seed=8)
+    elif case == "reference-pca-table":
+        # cubic factors with a residual table: the cubic response form in the static array
+        import json
+        from pathlib import Path
+
+        g = json.loads((Path(__file__).parent / "golden" / "ref_driver_own_market.json").read_text())
+        mk = Market(vol=np.array(g["vol"]).reshape(3, 51))
         cfg = RunConfig(n_paths=20_000, seed=8)
     else:
         mk = Market()
