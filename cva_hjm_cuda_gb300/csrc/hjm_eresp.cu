@@ -168,9 +168,10 @@ __device__ __forceinline__ void source_w(float sh, float sl, float xh, float xl,
 // DEGS: the factors' polynomial degrees (degs_pack); NRES: the factors
 // whose residual responses are in the table (0: none, one float4 per slot; 2:
 // factors 2 and 3, two float4; 3: all three, three float4); SC: the frame's
-// coefficient rows staged in shared memory.
-template <bool EXT, int DEGS, int NRES, bool SC>
-__global__ void __launch_bounds__(kFp64Cta, 6)
+// coefficient rows staged in shared memory; NS: date slots in registers (24,
+// or 20 for windows of at most 20 slotted dates, at 8 CTAs per SM).
+template <bool EXT, int DEGS, int NRES, bool SC, int NS = kRespSlots>
+__global__ void __launch_bounds__(kFp64Cta, NS == kRespSlots ? 6 : 8)
     path_kernel_fp64_eresp(const __grid_constant__ EulerRespParams E, const float4* __restrict__ resp,
                            const double* __restrict__ ext, double* __restrict__ partials,
                            double* __restrict__ estore, double* __restrict__ carry)
@@ -194,9 +195,9 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
     const uint64_t gpath = P.path_offset + (uint64_t)lp;
 
     // {remainder at tenor j, its running sum} as hi + lo pairs, slot hi - j
-    float2 A[kRespSlots], Al[kRespSlots];
+    float2 A[NS], Al[NS];
 #pragma unroll
-    for (int r = 0; r < kRespSlots; ++r) A[r] = Al[r] = make_float2(0.0f, 0.0f);
+    for (int r = 0; r < NS; ++r) A[r] = Al[r] = make_float2(0.0f, 0.0f);
     float2 Y[NP], Yl[NP];  // the parts in the block's moving frame, {y_c, v_c} hi + lo
 #pragma unroll
     for (int c = 0; c < NP; ++c) Y[c] = Yl[c] = make_float2(0.0f, 0.0f);
@@ -268,6 +269,7 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
             float nh[3], nl[3];
             resp_groups_tail<kMergedGroups>(n_act, [&](auto gc) {
                 constexpr int G = decltype(gc)::value;
+                if constexpr (4 * G < NS) {
                 float4 k[4];
 #pragma unroll
                 for (int u = 0; u < 4; ++u) k[u] = __ldg(rr + (4 * G + u) * ENT);
@@ -300,6 +302,7 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
                 for (int u = 0; u < 4; ++u)
                     df_acc(A[4 * G + u], Al[4 * G + u], make_float2(k[u].x, k[u].y), make_float2(k[u].z, k[u].w),
                            wh2, wl2, nwh2);
+                }
             }, [&]() {
                 draw(n < n_last ? n + 1 : n_last, nh, nl);
                 // y += C(s) phi, v += G(s) phi for the (part, factor) terms of the degrees
@@ -314,8 +317,10 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
             if (E.renorm && (s & 3) == 3)
                 resp_groups(n_act, [&](auto gc) {
                     constexpr int G = decltype(gc)::value;
+                    if constexpr (4 * G < NS) {
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) df_renorm(A[4 * G + u], Al[4 * G + u]);
+                        for (int u = 0; u < 4; ++u) df_renorm(A[4 * G + u], Al[4 * G + u]);
+                    }
                 });
         }
         // the end of block b: the parts at date b + 1, priced when it is this window's
@@ -324,7 +329,7 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
         const int i = b + 1;
         if (i >= lo) {
             const double t = P.tau[i] - E.tau0;
-            const float2 h = select_reg<kRespSlots, float2>(A, hi - i), l = select_reg<kRespSlots, float2>(Al, hi - i);
+            const float2 h = select_reg<NS, float2>(A, hi - i), l = select_reg<NS, float2>(Al, hi - i);
             const double hc = widen_f32(h.x) + widen_f32(l.x);
             const double hcs = widen_f32(h.y) + widen_f32(l.y);
             double px = x[NP - 1], pz = Z[NP - 1];
@@ -607,7 +612,15 @@ cudaError_t launch_window(const EulerRespParams& E, const float4* table, const d
     const int sr = frame_row(NP);
     const bool sc = (size_t)E.P.stride * sr <= (size_t)kFrameSmemRows * kStateRow;
     const size_t smem = eresp_smem(E.win_lo, E.win_hi, NP, sc ? E.P.stride * sr : 0);
+    const int nslot = E.win_hi - (E.win_lo > 2 ? E.win_lo : 2) + 1;
     auto k = sc ? path_kernel_fp64_eresp<EXT, DEGS, NRES, true> : path_kernel_fp64_eresp<EXT, DEGS, NRES, false>;
+    // a window of at most 20 slotted dates (the 10y swap: 19), quadratic
+    // factors, the generator's normals: 20 slots in 128 registers, 8 CTAs per
+    // SM instead of 6 (15.9 ms against 16.4 for the headline; the cubic form
+    // with its residual spills at 128 registers and runs slower, 27.0 against
+    // 25.9 ms, so it keeps 24 slots)
+    if constexpr (!EXT && NRES == 0)
+        if (nslot <= 20 && sc) k = path_kernel_fp64_eresp<EXT, DEGS, NRES, true, 20>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const int64_t grid = (E.P.n_paths + kFp64Cta - 1) / kFp64Cta;
