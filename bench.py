@@ -544,6 +544,7 @@ def run_ours(args) -> None:
             extras["fp64_convected_form"] = convected_form_run(eng, mk, sw, args, flush, stride, peak64, res)
         extras["generic_table_step"] = generic_step_run(eng, mk, sw, args, flush, stride, peak64, peak32)
         extras["reference_table"] = reference_table_run(eng, args, flush)
+        extras["dropin_call"] = dropin_run(args)
         eng.set_market(mk)
         eng.set_swap(sw)
         extras["predictor_corrector"] = predictor_corrector_run(eng, mk, sw, args, flush)
@@ -683,6 +684,44 @@ def reference_table_run(eng, args, flush) -> dict:
         res["ee_max_rel_diff"] = float(np.max(np.abs(a - b) / np.abs(b)))
         res["speedup"] = res["response_form"]["path_steps_per_s"] / res["convected_table_step"]["path_steps_per_s"]
         out[label] = res
+    return out
+
+
+def dropin_run(args) -> dict:
+    """The reference's own entry point, calculateExposureMultiGPU (double
+    overload, simulation_gpu.h:12), through the C++ drop-in of the library:
+    host arrays in, the 51-point EE out, timed end to end on the host (the
+    drop-in's process-wide context is warm after the first call).  On the
+    headline market and swap (1,048,576 paths, 10y) and on the reference
+    driver's own call (its curve, PCA table, drift, accruals, N = 10, K = 6.7%,
+    25y; 1,048,576 paths instead of the driver's default 100,000)."""
+    import numpy as np
+
+    from cva_hjm_cuda_gb300.engine import calculate_exposure_gpu
+    from cva_hjm_cuda_gb300.market import Market, Swap
+
+    g = json.loads((ROOT / "tests" / "golden" / "ref_driver_own_market.json").read_text())
+    mk, sw = Market(), Swap()
+    cases = {
+        "headline_10y": (sw.notional, sw.strike, 10.0, sw.accrual, mk.spot, mk.drift, mk.vol.ravel()),
+        "reference_driver_25y": (g["notional"], g["strike"], g["expiry"], np.array(g["accrual"]), np.array(g["spot"]),
+                                 np.array(g["drift"]), np.array(g["vol"])),
+    }
+    out = {}
+    n = WORKLOADS["fp64"]["n_paths"]
+    for label, (notional, strike, expiry, acc, spot, drift, vol) in cases.items():
+        ee = np.zeros(51)
+        steps = int(round(expiry / DT))
+        for _ in range(args.warmup):
+            calculate_exposure_gpu(ee, notional, strike, expiry, 0.5, acc, spot, drift, vol, 0.0, 1, n, DT)
+        times = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            calculate_exposure_gpu(ee, notional, strike, expiry, 0.5, acc, spot, drift, vol, 0.0, 1, n, DT)
+            times.append(time.perf_counter() - t0)
+        t = statistics.median(times)
+        out[label] = {"n_paths": n, "n_steps": steps, "ms_per_call": 1e3 * t, "path_steps_per_s": n * steps / t,
+                      "ee_0": float(ee[0])}
     return out
 
 

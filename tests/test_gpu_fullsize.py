@@ -18,7 +18,8 @@ that straddle two CTAs.
 * config 4: 1,048,576 paths, the adjoint: checkpoints every 32 steps against
   the store-the-seeds mode (1e-4), and the gradient of the whole run equal to
   the mean of the gradients of its 16 path ranges (the estimator is a path
-  mean; 1e-12 relative).
+  mean; 1e-12 relative), and one range deep inside the launch against central
+  finite differences of the FP64 valuation of its paths (2e-3).
 """
 from __future__ import annotations
 
@@ -138,3 +139,24 @@ def test_config4_adjoint_full_size(engine):
         mean = np.mean([getattr(p, name) for p in parts], axis=0)
         np.testing.assert_allclose(whole, mean, rtol=1e-12, atol=1e-12 * np.max(np.abs(whole)), err_msg=name)
     assert abs(a32.cva - np.mean([p.cva for p in parts])) <= 1e-12 * a32.cva
+    # one of those ranges, deep inside the launch, against central finite
+    # differences of the FP64 valuation of the same paths (bump 1e-5, within
+    # 2e-3 of the difference or 1 % of the largest forward sensitivity)
+    k = 11
+    part = parts[k]
+    spot = nelson_siegel_curve(tau)
+
+    def val(sp, hz=0.02):
+        engine.set_market_poly(51, 0.5, sp, DEFAULT_VOL_COEFFS)
+        c = RunConfig(n_paths=n // 16, seed=1234, path_offset=k * (n // 16), hazard=hz)
+        return engine.run(c, "fp64", pfe=False).cva
+
+    gmax = np.max(np.abs(part.dcva_dspot))
+    for t in (5, 15, 19):
+        up, dn = spot.copy(), spot.copy()
+        up[t] += 1e-5
+        dn[t] -= 1e-5
+        fd = (val(up) - val(dn)) / 2e-5
+        assert abs(part.dcva_dspot[t] - fd) <= 2e-3 * max(abs(fd), 0.01 * gmax), (t, part.dcva_dspot[t], fd)
+    fd = (val(spot, 0.02 + 1e-5) - val(spot, 0.02 - 1e-5)) / 2e-5
+    assert abs(part.dcva_dhazard - fd) <= 1e-6 * abs(fd)
