@@ -129,18 +129,19 @@ def algorithmic_flops_per_path(n_tenor: int, n_steps: int, stride: int, form: st
 
 def response_active_prefix(n_tenor: int, n_steps: int, stride: int, dtau: float = 0.5):
     """Per row b stride + s of the Euler response table, the active prefix the
-    kernel reads (response_active_kernel): the slots up to the last whose
-    coefficient kappa G_j(lag) or running-sum coefficient kappa CG_j(lag), in
-    FP32, is nonzero and at least 2^-70 of its slot's largest; lag = (j - b)
-    stride - 1 - s for date j = B - slot, G_j(m) = (A^m e_L)[j] by m upwind
-    steps with c = 1 / stride."""
+    kernel reads (eresp_active_kernel, no residual): the slots up to the last
+    whose coefficient kappa G_j(lag), in FP32, is nonzero and at least 2^-53
+    |kappa|, or whose running-sum coefficient kappa CG_j(lag) is at least
+    2^-53 |kappa| j stride; lag = (j - b) stride - 1 - s for date j = B - slot,
+    G_j(m) = (A^m e_L)[j] by m upwind steps with c = 1 / stride."""
     import numpy as np
 
     B, L = n_steps // stride, n_tenor - 1
     c = 1.0 / stride
     kappa = -2.0 * c * dtau * dtau
     rows = B * stride
-    tab = np.zeros((rows, 24, 2))
+    width = max(24, B)
+    tab = np.zeros((rows, width, 2))
     v = np.zeros(n_tenor)
     v[L] = 1.0
     cum = np.zeros(n_tenor)
@@ -153,11 +154,11 @@ def response_active_prefix(n_tenor: int, n_steps: int, stride: int, dtau: float 
         vn[:L] = v[:L] + c * (v[1:] - v[:L])
         vn[L] = v[L] + c * (v[L] - v[L - 1])
         v = vn
-    t32 = tab.astype(np.float32)
-    a = np.abs(t32)
-    thr = (a.max(axis=0) * np.float32(2.0 ** -70)).astype(np.float32)
-    sig = ((t32 != 0) & (a >= thr)).any(axis=2)
-    return np.where(sig.any(axis=1), 24 - np.argmax(sig[:, ::-1], axis=1), 0)
+    a = np.abs(tab.astype(np.float32))
+    tg = np.float32(abs(kappa)) * np.float32(2.0 ** -53)
+    tcg = (tg * (np.maximum(B - np.arange(width), 1) * stride).astype(np.float32)).astype(np.float32)
+    sig = ((a[:, :, 0] != 0) & (a[:, :, 0] >= tg)) | ((a[:, :, 1] != 0) & (a[:, :, 1] >= tcg[None, :]))
+    return np.where(sig.any(axis=1), width - np.argmax(sig[:, ::-1], axis=1), 0)
 
 
 def response_fp32_flops_per_path(n_tenor: int, n_steps: int, stride: int, form: str = "poly_tri") -> int:
@@ -197,18 +198,24 @@ def cubic_fp32_flops_per_path(n_tenor: int, n_steps: int, stride: int, nres: int
     response_fp32_flops_per_path counts the quadratic form: per window, per
     evolved step up to its last date, each live date slot of the window in
     groups of four (the residual reaches every tenor, so every date still to be
-    sampled is active): the remainder's double-FP32 term (30 flops), the
-    residual's packed FMAs (4 flops per residual factor) and the renormalisation
-    every fourth step (6 flops / 4); the parts' moving frame, 9 terms of 26
-    flops, 4 renormalisations of 6, and the source w = y_W + sigma y_X in
-    double-FP32 (14 flops)."""
+    sampled is active): the residual's packed FMAs (4 flops per residual
+    factor) and the renormalisation every fourth step (6 flops / 4), and in the
+    groups that reach the remainder's own prefix (``response_active_prefix``;
+    the first two groups always) its double-FP32 term (30 flops); the parts'
+    moving frame, 9 terms of 26 flops, 4 renormalisations of 6, and the source
+    w = y_W + sigma y_X in double-FP32 (14 flops)."""
     B = n_steps // stride
+    pre_w = response_active_prefix(n_tenor, n_steps, stride)
     total = 0
     for lo, hi in eresp_windows(B):
+        roff, nslot = B - hi, hi - max(lo, 2) + 1
         for b in range(1, hi):
             live = sum(1 for j in range(max(lo, 2), hi + 1) if j > b)
-            slots = 4 * ((live + 3) // 4)
-            total += stride * (slots * (30 + 4 * nres + 1.5) + 9 * 26 + 4 * 6 + 14)
+            groups = (live + 3) // 4
+            for s_ in range(stride):
+                n_w = min(max(int(pre_w[b * stride + s_]) - roff, 0), nslot)
+                w_groups = min(groups, max(2, (n_w + 3) // 4))
+                total += 4 * groups * (4 * nres + 1.5) + 4 * w_groups * 30 + 9 * 26 + 4 * 6 + 14
     return int(total)
 
 

@@ -132,6 +132,12 @@ struct hjm_ctx {
         std::vector<EulerRespFrame> frames;  // one per window
         std::vector<double> resid;  // sqrt(dt)-scaled, empty without a residual
     } eresp_key;
+    struct ErespFirst {  // eresp_first_active_date of the last run shape
+        bool valid = false;
+        int nt = 0, stride = 0, B = 0, nres = 0;
+        double c = 0;
+        int first = 2;
+    } eresp_first;
     struct VrespKey {  // the volatility-table response table in vresp
         bool valid = false;
         int nt = 0, stride = 0, B = 0, scheme = 0;
@@ -948,14 +954,6 @@ static hjm_status enqueue_eresp(hjm_ctx* ctx, const RunShape& sh, double dt, con
                                 const double* ext_dev, double* estore, cudaStream_t s)
 {
     const bool cubic = use_cubic_path(ctx);
-    int lo[kMaxTenor], hi[kMaxTenor];
-    const int n_windows = eresp_windows(sh.B, lo, hi);
-    std::vector<EulerRespFrame> frames(n_windows);
-    int degs = 0;
-    for (int w = 0; w < n_windows; ++w)
-        eresp_make_frame(dt, ctx->dtau, ctx->nt, P.svc, cubic ? &ctx->cubic[0][0] : nullptr, ctx->cubic_degs,
-                         eresp_window_centre(ctx->dtau, lo[w], hi[w]), frames[w], degs);
-    const EulerRespFrame& fr = frames[0];
     std::vector<double> resid;
     int nres = 0;
     if (cubic) {
@@ -964,7 +962,27 @@ static hjm_status enqueue_eresp(hjm_ctx* ctx, const RunShape& sh, double dt, con
         for (size_t i = 0; i < resid.size(); ++i) resid[i] = sq * ctx->resid[i];
         nres = eresp_residual_factors(ctx->resid.data(), ctx->vol.data(), ctx->nt);
     }
-    const size_t smem = eresp_max_smem(sh.B, fr.np, sh.stride);
+    // the earliest date the remainder reaches (the windows hold slots from it on)
+    const double c = dt / ctx->dtau;
+    hjm_ctx::ErespFirst& fa = ctx->eresp_first;
+    if (!(fa.valid && fa.nt == ctx->nt && fa.stride == sh.stride && fa.B == sh.B && fa.nres == nres && fa.c == c)) {
+        fa.first = eresp_first_active_date(ctx->nt, c, sh.stride, sh.B, nres);
+        fa.nt = ctx->nt;
+        fa.stride = sh.stride;
+        fa.B = sh.B;
+        fa.nres = nres;
+        fa.c = c;
+        fa.valid = true;
+    }
+    int lo[kMaxTenor], hi[kMaxTenor];
+    const int n_windows = eresp_windows(sh.B, fa.first, lo, hi, nullptr);
+    std::vector<EulerRespFrame> frames(n_windows);
+    int degs = 0;
+    for (int w = 0; w < n_windows; ++w)
+        eresp_make_frame(dt, ctx->dtau, ctx->nt, P.svc, cubic ? &ctx->cubic[0][0] : nullptr, ctx->cubic_degs,
+                         eresp_window_centre(ctx->dtau, lo[w], hi[w]), frames[w], degs);
+    const EulerRespFrame& fr = frames[0];
+    const size_t smem = eresp_max_smem(sh.B, fr.np, sh.stride, fa.first);
     if (smem > 227 * 1024) return fail(ctx, HJM_ERR_UNSUPPORTED, "shared memory %zu B exceeds 227 KB", smem);
     hjm_status st = ensure_eresp_table(ctx, sh, dt, frames, resid, nres, s);
     if (st != HJM_OK) return st;
@@ -973,16 +991,16 @@ static hjm_status enqueue_eresp(hjm_ctx* ctx, const RunShape& sh, double dt, con
     E.P = P;
     E.frame = block_frame_n(fr.n, sh.stride);
     E.row = eresp_row(sh.B);
-    // the pairs are renormalised for the residual's terms and for windowed
-    // (long) runs, whose dates near the last tenor carry large remainders
-    E.renorm = (cubic || n_windows > 1) ? 1 : 0;
+    // the pairs are renormalised for the residual's terms and for runs of more
+    // than 25 dates, whose dates near the last tenor carry large remainders
+    E.renorm = (cubic || sh.B > kRespSlots + 1) ? 1 : 0;
     double* carry = nullptr;
     if (n_windows > 1) {
         HJM_CUDA(ctx, ctx->carry.ensure(sizeof(double) * 2 * (size_t)P.n_paths));
         carry = (double*)ctx->carry.p;
     }
     int launches = 0;
-    HJM_CUDA(ctx, launch_path_fp64_eresp(E, frames.data(), degs, nres, (const float4*)ctx->eresp.p, ext_dev,
+    HJM_CUDA(ctx, launch_path_fp64_eresp(E, frames.data(), degs, nres, (const float4*)ctx->eresp.p, fa.first, ext_dev,
                                          (double*)ctx->partials.p, estore, carry, s, &launches));
     ctx->stat_launches += launches - 1;
     return HJM_OK;

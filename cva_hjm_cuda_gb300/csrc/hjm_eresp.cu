@@ -165,13 +165,20 @@ __device__ __forceinline__ void source_w(float sh, float sl, float xh, float xl,
 
 }  // namespace
 
+// CTAs per SM of a kernel holding ns date slots: register-limited (24 slots
+// in 168 registers, 16 or 20 in 128, 12 in 96, at 64 threads; 16 slots at 9
+// CTAs per SM spill).
+constexpr int eresp_min_ctas(int ns) { return ns >= 24 ? 6 : (ns >= 16 ? 8 : 10); }
+
 // DEGS: the factors' polynomial degrees (degs_pack); NRES: the factors
 // whose residual responses are in the table (0: none, one float4 per slot; 2:
 // factors 2 and 3, two float4; 3: all three, three float4); SC: the frame's
 // coefficient rows staged in shared memory; NS: date slots in registers (24,
-// or 20 for windows of at most 20 slotted dates, at 8 CTAs per SM).
+// or 20, 16, 12 for windows with at most that many active slots: more CTAs
+// per SM).  A date whose window slot is NS or beyond is never active (the
+// host chose NS from the table's prefixes): its remainder is zero.
 template <bool EXT, int DEGS, int NRES, bool SC, int NS = kRespSlots>
-__global__ void __launch_bounds__(kFp64Cta, NS == kRespSlots ? 6 : 8)
+__global__ void __launch_bounds__(kFp64Cta, eresp_min_ctas(NS))
     path_kernel_fp64_eresp(const __grid_constant__ EulerRespParams E, const float4* __restrict__ resp,
                            const double* __restrict__ ext, double* __restrict__ partials,
                            double* __restrict__ estore, double* __restrict__ carry)
@@ -201,9 +208,9 @@ __global__ void __launch_bounds__(kFp64Cta, NS == kRespSlots ? 6 : 8)
     float2 Y[NP], Yl[NP];  // the parts in the block's moving frame, {y_c, v_c} hi + lo
 #pragma unroll
     for (int c = 0; c < NP; ++c) Y[c] = Yl[c] = make_float2(0.0f, 0.0f);
-    const float4* coef_all = resp + (size_t)B * P.stride * E.row * ENT;
-    const float4* coef_g = coef_all + (size_t)E.frame_index * P.stride * SR;
-    const int* nact = reinterpret_cast<const int*>(coef_all + (size_t)E.n_frames * P.stride * SR);
+    const size_t rows = (size_t)B * P.stride;
+    const int* nact = reinterpret_cast<const int*>(resp + rows * E.row * ENT);
+    const float4* coef_g = resp + rows * E.row * ENT + (2 * rows + 5) / 4 + (size_t)E.frame_index * P.stride * SR;
     const float4* coef = coef_g;
     if constexpr (SC) {
         float4* c_s = reinterpret_cast<float4*>(z_s + NP * kCta);
@@ -215,7 +222,8 @@ __global__ void __launch_bounds__(kFp64Cta, NS == kRespSlots ? 6 : 8)
     for (int c = 0; c < NP; ++c) z_s[c * kCta + tid] = 0.0;
 
     const int roff = B - hi;                              // global slot of slot 0
-    const int nslot = hi - (lo > 2 ? lo : 2) + 1;         // slots of this window's dates
+    const int nslot0 = hi - (lo > 2 ? lo : 2) + 1;        // slots of this window's dates
+    const int nslot = nslot0 < NS ? nslot0 : NS;          // those that can be active
 
     // price date i from its stochastic value xs and running sum zs
     auto price = [&](int i, double xs, double zs) {
@@ -255,6 +263,12 @@ __global__ void __launch_bounds__(kFp64Cta, NS == kRespSlots ? 6 : 8)
             const int n = b * P.stride + s;
             int n_act = __ldg(nact + n) - roff;  // uniform: the row's active prefix in this window
             n_act = n_act < 0 ? 0 : (n_act > nslot ? nslot : n_act);
+            // the prefix of the remainder's W terms (the residual's reaches further)
+            int n_w = n_act;
+            if constexpr (NRES > 0) {
+                n_w = __ldg(nact + rows + 1 + n) - roff;
+                n_w = n_w < 0 ? 0 : (n_w > nslot ? nslot : n_w);
+            }
             const float4* rr = row + (size_t)s * E.row * ENT;
             // the remainder's source: W before this step's update
             float wh, wl;
@@ -298,10 +312,13 @@ __global__ void __launch_bounds__(kFp64Cta, NS == kRespSlots ? 6 : 8)
                         lo2 = __ffma2_rn(make_float2(r1[u].z, r1[u].w), make_float2(ph[2], ph[2]), lo2);
                     }
                 }
+                // (the merged groups, the latest dates, always: their W terms count)
+                if (NRES == 0 || G < kMergedGroups || 4 * G < n_w) {
 #pragma unroll
-                for (int u = 0; u < 4; ++u)
-                    df_acc(A[4 * G + u], Al[4 * G + u], make_float2(k[u].x, k[u].y), make_float2(k[u].z, k[u].w),
-                           wh2, wl2, nwh2);
+                    for (int u = 0; u < 4; ++u)
+                        df_acc(A[4 * G + u], Al[4 * G + u], make_float2(k[u].x, k[u].y),
+                               make_float2(k[u].z, k[u].w), wh2, wl2, nwh2);
+                }
                 }
             }, [&]() {
                 draw(n < n_last ? n + 1 : n_last, nh, nl);
@@ -329,7 +346,12 @@ __global__ void __launch_bounds__(kFp64Cta, NS == kRespSlots ? 6 : 8)
         const int i = b + 1;
         if (i >= lo) {
             const double t = P.tau[i] - E.tau0;
-            const float2 h = select_reg<NS, float2>(A, hi - i), l = select_reg<NS, float2>(Al, hi - i);
+            // (a slot beyond NS is never active: zero)
+            float2 h = make_float2(0.0f, 0.0f), l = h;
+            if (hi - i < NS) {
+                h = select_reg<NS, float2>(A, hi - i);
+                l = select_reg<NS, float2>(Al, hi - i);
+            }
             const double hc = widen_f32(h.x) + widen_f32(l.x);
             const double hcs = widen_f32(h.y) + widen_f32(l.y);
             double px = x[NP - 1], pz = Z[NP - 1];
@@ -409,18 +431,28 @@ __global__ void __launch_bounds__(kMaxTenor)
     }
 }
 
-// Per row of the table (rows x row slots), the active prefix n_act[row] in
-// global slot numbering: the slots up to the last one with a component that
-// is nonzero and at least 2^-70 of that component's largest magnitude in its
-// slot over all rows (a slot is one date).  The slots after it hold only terms
-// near the transport front, where the responses are vanishingly small (each
-// below 2^-70 of the date's largest coefficient); the kernels skip them.
-// n_act[rows] = 0 (read ahead).  One CTA.
+// Per row of the table (rows x row slots), two active prefixes in global
+// slot numbering (slot r: date B - r): n_act[row], the slots up to the last
+// one with any term that counts, and n_act[rows + 1 + row], up to the last
+// one with a remainder term (kappa G, kappa CG) that counts.  A remainder
+// term counts while it is at least 2^-53 |kappa| (for CG: 2^-53 |kappa|
+// times the date's sampling step, the running sum's own unit): FP64's unit
+// roundoff of the response G_L(0) = 1 of the last tenor to its own source.
+// Away from the transport front the responses fall off faster than
+// geometrically (binomial tails), so the terms one date drops sum to about
+// ten times the threshold, ~1e-15 |kappa| max|W| (per running-sum unit): far
+// under the slot's own double-FP32 rounding (2^-48 of the accumulator per
+// addition), and 25% to 30% of the terms of a 10y or 12y run.  A residual
+// term (R_jk, CR_jk) counts while it is at least 2^-60 of that component's
+// largest magnitude anywhere in the table; the residual loadings reach every
+// tenor, so its prefix covers nearly every date still to be sampled.  Zeros
+// never count.  n_act[rows] = n_act[2 rows + 1] = 0 (read ahead).  One CTA.
 __global__ void __launch_bounds__(1024)
-    eresp_active_kernel(int rows, int row, int ent, const float4* __restrict__ resp, int* __restrict__ n_act)
+    eresp_active_kernel(int rows, int row, int ent, int stride, int B, float kappa, const float4* __restrict__ resp,
+                        int* __restrict__ n_act)
 {
-    __shared__ unsigned int mx[kMaxTenor + 4][8];
-    for (int i = threadIdx.x; i < (kMaxTenor + 4) * 8; i += blockDim.x) (&mx[0][0])[i] = 0u;
+    __shared__ unsigned int mx[8];
+    if (threadIdx.x < 8) mx[threadIdx.x] = 0u;
     __syncthreads();
     const int ncomp = ent == 3 ? 8 : (ent == 2 ? 6 : 2);
     auto comp = [&](size_t slot_base, int q) -> float {
@@ -439,21 +471,31 @@ __global__ void __launch_bounds__(1024)
         }
     };
     const int64_t total = (int64_t)rows * row;
-    for (int64_t i = threadIdx.x; i < total; i += blockDim.x) {
-        const int r = (int)(i % row);
-        for (int q = 0; q < ncomp; ++q)
-            atomicMax(&mx[r][q], __float_as_uint(fabsf(comp((size_t)i * ent, q))));  // non-negative floats order as their bits
+    if (ncomp > 2) {
+        unsigned int m[6] = {0u, 0u, 0u, 0u, 0u, 0u};
+        for (int64_t i = threadIdx.x; i < total; i += blockDim.x)
+            for (int q = 2; q < ncomp; ++q)  // non-negative floats order as their bits
+                m[q - 2] = max(m[q - 2], __float_as_uint(fabsf(comp((size_t)i * ent, q))));
+        for (int q = 2; q < ncomp; ++q) atomicMax(&mx[q], m[q - 2]);
     }
     __syncthreads();
+    const float tg = fabsf(kappa) * 0x1p-53f;
     for (int rw = threadIdx.x; rw <= rows; rw += blockDim.x) {
-        int n = 0;
+        int n = 0, ng = 0;
         if (rw < rows)
-            for (int r = 0; r < row; ++r)
+            for (int r = 0; r < row; ++r) {
+                const float tcg = tg * (float)(max(B - r, 1) * stride);
                 for (int q = 0; q < ncomp; ++q) {
                     const float a = fabsf(comp(((size_t)rw * row + r) * ent, q));
-                    if (a != 0.0f && a >= __uint_as_float(mx[r][q]) * 0x1p-70f) n = r + 1;
+                    const float t = q == 0 ? tg : (q == 1 ? tcg : __uint_as_float(mx[q]) * 0x1p-60f);
+                    if (a != 0.0f && a >= t) {
+                        n = r + 1;
+                        if (q < 2) ng = r + 1;
+                    }
                 }
+            }
         n_act[rw] = n;
+        n_act[rows + 1 + rw] = ng;
     }
 }
 
@@ -554,26 +596,30 @@ int eresp_residual_factors(const double* resid, const double* vol, int nt)
 
 static int entries_per_slot(int nres) { return nres == 3 ? 3 : (nres == 2 ? 2 : 1); }
 
-size_t eresp_table_elems(int stride, int n_blocks, int np, int nres, int n_frames)
+static size_t eresp_prefix_ints(int stride, int n_blocks) { return 2 * ((size_t)n_blocks * stride + 1); }
+
+static size_t eresp_prefix_offset(int stride, int n_blocks, int nres)
 {
-    const size_t rows = (size_t)n_blocks * stride;
-    return rows * eresp_row(n_blocks) * entries_per_slot(nres) + (size_t)n_frames * stride * frame_row(np) +
-           (rows + 4) / 4;
+    return (size_t)n_blocks * stride * eresp_row(n_blocks) * entries_per_slot(nres);
 }
 
-cudaError_t launch_eresp_tables(int nt, double c, double dtau, int stride, int n_blocks, const EulerRespFrame* frames,
-                                int n_frames, const double* resid /* [3][nt] sqrt(dt)-scaled, or null */, int nres,
-                                float4* table, cudaStream_t s)
+// (the kernel's coefficient rows start (2 rows + 5) / 4 float4 after the prefixes)
+size_t eresp_table_elems(int stride, int n_blocks, int np, int nres, int n_frames)
 {
-    if (n_frames < 1) return cudaErrorInvalidValue;
-    const EulerRespFrame& fr = frames[0];
+    return eresp_prefix_offset(stride, n_blocks, nres) + (eresp_prefix_ints(stride, n_blocks) + 3) / 4 +
+           (size_t)n_frames * stride * frame_row(np);
+}
+
+static cudaError_t launch_eresp_responses(int nt, double c, double dtau, int stride, int n_blocks, const double* resid,
+                                   int nres, float4* table, cudaStream_t s)
+{
     if (nt < 3 || nt > kMaxTenor || n_blocks < 1 || n_blocks >= nt || stride < 1) return cudaErrorInvalidValue;
     const int row = eresp_row(n_blocks);
     if (!resid) nres = 0;
     const int ent = entries_per_slot(nres);
     const size_t rows = (size_t)n_blocks * stride;
-    cudaError_t e =
-        cudaMemsetAsync(table, 0, sizeof(float4) * eresp_table_elems(stride, n_blocks, fr.np, nres, n_frames), s);
+    const size_t pre = eresp_prefix_offset(stride, n_blocks, nres);
+    cudaError_t e = cudaMemsetAsync(table, 0, sizeof(float4) * (pre + (eresp_prefix_ints(stride, n_blocks) + 3) / 4), s);
     if (e != cudaSuccess) return e;
     ResidLoadings RL;
     std::memset(&RL, 0, sizeof(RL));
@@ -584,8 +630,17 @@ cudaError_t launch_eresp_tables(int nt, double c, double dtau, int stride, int n
     eresp_table_kernel<<<1, kMaxTenor, 0, s>>>(nt, c, stride, n_blocks, row, nres, kappa, RL, table);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    float4* coef = table + rows * row * ent;
-    const int64_t per_frame = (int64_t)stride * frame_row(fr.np);
+    eresp_active_kernel<<<1, 1024, 0, s>>>((int)rows, row, ent, stride, n_blocks, (float)kappa, table,
+                                            reinterpret_cast<int*>(table + pre));
+    return cudaGetLastError();
+}
+
+static cudaError_t launch_eresp_frames(int stride, int n_blocks, int nres, const EulerRespFrame* frames, int n_frames,
+                                float4* table, cudaStream_t s)
+{
+    if (n_frames < 1 || stride < 1) return cudaErrorInvalidValue;
+    float4* coef = table + eresp_prefix_offset(stride, n_blocks, nres) + (eresp_prefix_ints(stride, n_blocks) + 3) / 4;
+    const int64_t per_frame = (int64_t)stride * frame_row(frames[0].np);
     for (int w = 0; w < n_frames; ++w) {
         FrameLoadings f;
         std::memset(&f, 0, sizeof(f));
@@ -593,34 +648,48 @@ cudaError_t launch_eresp_tables(int nt, double c, double dtau, int stride, int n
         f.sig0 = frames[w].sig0;
         for (int cc = 0; cc < 4; ++cc)
             for (int k = 0; k < kFactors; ++k) f.bm[cc][k] = frames[w].bm[cc][k];
-        eresp_coef_kernel<<<(unsigned)((per_frame + 127) / 128), 128, 0, s>>>(f, fr.np, stride, coef + w * per_frame);
-        e = cudaGetLastError();
+        eresp_coef_kernel<<<(unsigned)((per_frame + 127) / 128), 128, 0, s>>>(f, frames[0].np, stride,
+                                                                               coef + w * per_frame);
+        const cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
-    eresp_active_kernel<<<1, 1024, 0, s>>>((int)rows, row, ent, table,
-                                            reinterpret_cast<int*>(coef + (size_t)n_frames * per_frame));
-    return cudaGetLastError();
+    return cudaSuccess;
+}
+
+cudaError_t launch_eresp_tables(int nt, double c, double dtau, int stride, int n_blocks, const EulerRespFrame* frames,
+                                int n_frames, const double* resid, int nres, float4* table, cudaStream_t s)
+{
+    if (!resid) nres = 0;
+    const cudaError_t e = launch_eresp_responses(nt, c, dtau, stride, n_blocks, resid, nres, table, s);
+    if (e != cudaSuccess) return e;
+    return launch_eresp_frames(stride, n_blocks, nres, frames, n_frames, table, s);
 }
 
 namespace {
 
 template <bool EXT, int DEGS, int NRES>
-cudaError_t launch_window(const EulerRespParams& E, const float4* table, const double* ext, double* partials,
+cudaError_t launch_window(const EulerRespParams& E, int ns, const float4* table, const double* ext, double* partials,
                           double* estore, double* carry, cudaStream_t s)
 {
     constexpr int NP = degs_parts(DEGS);
     const int sr = frame_row(NP);
     const bool sc = (size_t)E.P.stride * sr <= (size_t)kFrameSmemRows * kStateRow;
     const size_t smem = eresp_smem(E.win_lo, E.win_hi, NP, sc ? E.P.stride * sr : 0);
-    const int nslot = E.win_hi - (E.win_lo > 2 ? E.win_lo : 2) + 1;
     auto k = sc ? path_kernel_fp64_eresp<EXT, DEGS, NRES, true> : path_kernel_fp64_eresp<EXT, DEGS, NRES, false>;
-    // a window of at most 20 slotted dates (the 10y swap: 19), quadratic
-    // factors, the generator's normals: 20 slots in 128 registers, 8 CTAs per
-    // SM instead of 6 (15.9 ms against 16.4 for the headline; the cubic form
-    // with its residual spills at 128 registers and runs slower, 27.0 against
-    // 25.9 ms, so it keeps 24 slots)
-    if constexpr (!EXT && NRES == 0)
-        if (nslot <= 20 && sc) k = path_kernel_fp64_eresp<EXT, DEGS, NRES, true, 20>;
+    // a window with at most 20, 16 or 12 active slots, quadratic factors, the
+    // generator's normals: fewer slots in fewer registers, more CTAs per SM
+    // (20 slots: 8 CTAs instead of 6, 15.9 ms against 16.4 for the 10y
+    // headline; the cubic form with its residual spills at 128 registers and
+    // runs slower, 27.0 against 25.9 ms, and its residual keeps every date
+    // still to be sampled active, so it keeps 24)
+    if constexpr (!EXT && NRES == 0) {
+        if (sc && ns <= 12)
+            k = path_kernel_fp64_eresp<EXT, DEGS, NRES, true, 12>;
+        else if (sc && ns <= 16)
+            k = path_kernel_fp64_eresp<EXT, DEGS, NRES, true, 16>;
+        else if (sc && ns <= 20)
+            k = path_kernel_fp64_eresp<EXT, DEGS, NRES, true, 20>;
+    }
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const int64_t grid = (E.P.n_paths + kFp64Cta - 1) / kFp64Cta;
@@ -629,25 +698,56 @@ cudaError_t launch_window(const EulerRespParams& E, const float4* table, const d
 }
 
 template <int DEGS, int NRES>
-cudaError_t launch_window_ext(const EulerRespParams& E, const float4* table, const double* ext, double* partials,
-                              double* estore, double* carry, cudaStream_t s)
+cudaError_t launch_window_ext(const EulerRespParams& E, int ns, const float4* table, const double* ext,
+                              double* partials, double* estore, double* carry, cudaStream_t s)
 {
-    return ext ? launch_window<true, DEGS, NRES>(E, table, ext, partials, estore, carry, s)
-               : launch_window<false, DEGS, NRES>(E, table, ext, partials, estore, carry, s);
+    return ext ? launch_window<true, DEGS, NRES>(E, ns, table, ext, partials, estore, carry, s)
+               : launch_window<false, DEGS, NRES>(E, ns, table, ext, partials, estore, carry, s);
 }
 
 }  // namespace
 
-int eresp_windows(int n_blocks, int* lo, int* hi)
+int eresp_first_active_date(int nt, double c, int stride, int n_blocks, int nres)
 {
-    // from the latest date down: each window holds kRespSlots dates with a
-    // slot; a window reaching date 2 takes date 1 (which needs no slot) too
+    if (nres > 0) return 2;
+    if (nt < 3 || nt > kMaxTenor || n_blocks < 2 || n_blocks >= nt || stride < 1) return 2;
+    const int L = nt - 1, B = n_blocks;
+    double v[kMaxTenor] = {}, w[kMaxTenor], cum[kMaxTenor] = {};
+    bool sig[kMaxTenor] = {};
+    v[L] = 1.0;
+    const int M = (B - 1) * stride - 1;  // the longest lag in the table
+    for (int m = 0; m <= M; ++m) {
+        for (int t = 0; t <= L; ++t) cum[t] += v[t];
+        // date t's entries hold lags up to (t - 1) stride - 1; the device
+        // counts kappa G >= 2^-53 |kappa|, kappa CG >= 2^-53 |kappa| t stride
+        for (int t = 2; t <= B; ++t)
+            if (!sig[t] && m <= (t - 1) * stride - 1 &&
+                (std::fabs(v[t]) >= 0x1p-54 || std::fabs(cum[t]) >= 0x1p-54 * (double)t * stride))
+                sig[t] = true;
+        for (int t = 0; t < L; ++t) w[t] = v[t] + c * (v[t + 1] - v[t]);
+        w[L] = v[L] + c * (v[L] - v[L - 1]);
+        for (int t = 0; t <= L; ++t) v[t] = w[t];
+    }
+    for (int t = 2; t <= B; ++t)
+        if (sig[t]) return t;
+    return B + 1;
+}
+
+int eresp_windows(int n_blocks, int first_active, int* lo, int* hi, int* ns)
+{
+    const int f = std::max(first_active, 2);
     int n = 0, h = n_blocks;
     while (h >= 1) {
-        int l = h - kRespSlots + 1;
-        if (l <= 2) l = 1;
+        // dates of a window [1, h] that can be active: f .. h
+        int l = 1;
+        if (h - f + 1 > kRespSlots) {
+            l = h - kRespSlots + 1;
+            if (l <= 2) l = 1;
+        }
+        const int act = std::max(h - std::max(l, f) + 1, 0);
         if (lo) lo[n] = l;
         if (hi) hi[n] = h;
+        if (ns) ns[n] = act <= 12 ? 12 : (act <= 16 ? 16 : (act <= 20 ? 20 : kRespSlots));
         ++n;
         h = l - 1;
     }
@@ -655,11 +755,11 @@ int eresp_windows(int n_blocks, int* lo, int* hi)
 }
 
 cudaError_t launch_path_fp64_eresp(const EulerRespParams& base, const EulerRespFrame* frames, int degs, int nres,
-                                   const float4* table, const double* ext, double* partials, double* estore,
-                                   double* carry, cudaStream_t s, int* launches)
+                                   const float4* table, int first_active, const double* ext, double* partials,
+                                   double* estore, double* carry, cudaStream_t s, int* launches)
 {
-    int lo[kMaxTenor], hi[kMaxTenor];
-    const int nw = eresp_windows(base.P.n_blocks, lo, hi);
+    int lo[kMaxTenor], hi[kMaxTenor], ns[kMaxTenor];
+    const int nw = eresp_windows(base.P.n_blocks, first_active, lo, hi, ns);
     if (nw > 1 && !carry) return cudaErrorInvalidValue;
     if (launches) *launches = 0;
     for (int w = 0; w < nw; ++w) {
@@ -671,19 +771,19 @@ cudaError_t launch_path_fp64_eresp(const EulerRespParams& base, const EulerRespF
         E.tau0 = frames[w].tau0;
         cudaError_t e;
         if (nres == 2 && degs_of(degs, 0) == 0) {
-            e = launch_window_ext<degs_pack(0, 3, 3), 2>(E, table, ext, partials, estore, carry, s);
+            e = launch_window_ext<degs_pack(0, 3, 3), 2>(E, ns[w], table, ext, partials, estore, carry, s);
         } else if (nres > 0) {
             // (a residual table of factors 2 and 3 only is laid out as nres = 2)
             if (nres == 2) return cudaErrorInvalidValue;
             if (degs_of(degs, 0) == 0)
-                e = launch_window_ext<degs_pack(0, 3, 3), 3>(E, table, ext, partials, estore, carry, s);
+                e = launch_window_ext<degs_pack(0, 3, 3), 3>(E, ns[w], table, ext, partials, estore, carry, s);
             else
-                e = launch_window_ext<degs_pack(3, 3, 3), 3>(E, table, ext, partials, estore, carry, s);
+                e = launch_window_ext<degs_pack(3, 3, 3), 3>(E, ns[w], table, ext, partials, estore, carry, s);
         } else if (degs == degs_pack(0, 1, 2) || degs == degs_pack(0, 1, 1) || degs == degs_pack(0, 0, 2) ||
                    degs == degs_pack(0, 1, 0) || degs == degs_pack(0, 0, 1) || degs == degs_pack(0, 0, 0)) {
-            e = launch_window_ext<degs_pack(0, 1, 2), 0>(E, table, ext, partials, estore, carry, s);
+            e = launch_window_ext<degs_pack(0, 1, 2), 0>(E, ns[w], table, ext, partials, estore, carry, s);
         } else {
-            e = launch_window_ext<degs_pack(2, 2, 2), 0>(E, table, ext, partials, estore, carry, s);
+            e = launch_window_ext<degs_pack(2, 2, 2), 0>(E, ns[w], table, ext, partials, estore, carry, s);
         }
         if (e != cudaSuccess) return e;
         if (launches) ++*launches;
@@ -691,10 +791,10 @@ cudaError_t launch_path_fp64_eresp(const EulerRespParams& base, const EulerRespF
     return cudaSuccess;
 }
 
-size_t eresp_max_smem(int n_blocks, int np, int stride)
+size_t eresp_max_smem(int n_blocks, int np, int stride, int first_active)
 {
     int lo[kMaxTenor], hi[kMaxTenor];
-    const int nw = eresp_windows(n_blocks, lo, hi);
+    const int nw = eresp_windows(n_blocks, first_active, lo, hi, nullptr);
     const int sr = frame_row(np);
     const bool sc = (size_t)stride * sr <= (size_t)kFrameSmemRows * kStateRow;
     size_t m = 0;

@@ -9,9 +9,8 @@ namespace hjm {
 // run), the block's moving-frame matrices, the basis centre, the window of
 // dates this launch prices, and the table's slots per row (eresp_row).
 // frame: the window's coefficient rows (launch_eresp_tables writes one set
-// per window, frame_index picks it; n_frames of them before the active
-// prefixes).  renorm: renormalise the date slots' double-FP32 pairs every
-// fourth step.
+// per window after the active prefixes, frame_index picks it).  renorm:
+// renormalise the date slots' double-FP32 pairs every fourth step.
 // Without it the low part of a pair gathers every rounding error of the high
 // part, so that after n additions it is ~sqrt(n) ulps of the sum and rounds
 // at ~n 2^-49 of the sum; that is negligible for the small remainder of a
@@ -56,30 +55,44 @@ void eresp_make_frame(double dt, double dtau, int nt, const double (*svc)[3], co
 // tenors are ~30 times the net loading, and so are their rounding errors).
 double eresp_window_centre(double dtau, int lo, int hi);
 int eresp_row(int n_blocks);
-// float4 entries of the table buffer: responses, frame coefficients, active
-// prefixes.  nres: factors with a residual (0; 2: factors 2 and 3; 3: all).
+// float4 entries of the table buffer: responses, active prefixes, then the
+// frame coefficients of n_frames windows.  nres: factors with a residual (0;
+// 2: factors 2 and 3; 3: all).
 size_t eresp_table_elems(int stride, int n_blocks, int np, int nres, int n_frames);
 // Build the table on the stream (clears the buffer first).  resid: the
 // residual loadings sqrt(dt) (sigma_k - poly_k) [3][nt], or null; nres as
 // above (with nres = 2 the first factor's residual is left out).
 cudaError_t launch_eresp_tables(int nt, double c, double dtau, int stride, int n_blocks, const EulerRespFrame* frames,
                                 int n_frames, const double* resid, int nres, float4* table, cudaStream_t s);
+// The earliest date whose remainder terms the table's active prefixes can
+// ever hold (n_blocks + 1 when none): the host's FP64 restatement of
+// eresp_active_kernel's test at half its thresholds, so that it never
+// misses a date the device counts.  With a residual (nres > 0), 2: the
+// residual loadings reach every tenor.
+int eresp_first_active_date(int nt, double c, int stride, int n_blocks, int nres);
 // The residual factors a table needs: 0 without a residual, 2 when the first
 // factor's residual is at most 2^-44 of its scale (an exact constant, as the
 // reference table's first factor), else 3.
 int eresp_residual_factors(const double* resid, const double* vol, int nt);
-// The windows of a run of n_blocks dates, latest first (lo, hi may be null):
-// their number.
-int eresp_windows(int n_blocks, int* lo, int* hi);
+// The windows of a run of n_blocks dates, latest first (lo, hi, ns may be
+// null): their number.  A window needs a register slot only for its dates
+// that can be active, from first_active (eresp_first_active_date; 2 for
+// every date) on; earlier dates, never reached by the remainder, are priced
+// with no slot.  From the latest date down, a window takes every remaining
+// date when those that can be active number at most kRespSlots, else the
+// kRespSlots latest (a window reaching date 2 takes date 1 too).  ns: the
+// slots the window's kernel holds, 12, 16, 20 or 24, at least its active ones.
+int eresp_windows(int n_blocks, int first_active, int* lo, int* hi, int* ns);
 // One launch per window, latest first, window w with frame w (its centre in
 // frames[w].tau0).  degs: the factors' degrees
-// (degs_pack); nres: the table's residual factors; carry [2][n_paths]
-// doubles when the run has more than one window.  *launches: kernels enqueued.
+// (degs_pack); nres: the table's residual factors; first_active: as
+// eresp_windows (the frames' windows); carry [2][n_paths] doubles when the
+// run has more than one window.  *launches: kernels enqueued.
 cudaError_t launch_path_fp64_eresp(const EulerRespParams& base, const EulerRespFrame* frames, int degs, int nres,
-                                   const float4* table,
+                                   const float4* table, int first_active,
                                    const double* ext, double* partials, double* estore, double* carry,
                                    cudaStream_t s, int* launches);
 // The largest dynamic shared memory of the run's launches.
-size_t eresp_max_smem(int n_blocks, int np, int stride);
+size_t eresp_max_smem(int n_blocks, int np, int stride, int first_active);
 
 }  // namespace hjm

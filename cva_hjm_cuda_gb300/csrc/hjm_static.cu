@@ -314,7 +314,8 @@ hjm_status hjm_run_static(void* cuda_stream, int32_t n_tenor, double dtau, const
         int cdegs[HJM_N_FACTOR];
         const bool cub = !poly && fit_cubic_resid(vol_host, n_tenor, dtau, cubic, cdegs, resid);
         const int nres = cub ? eresp_residual_factors(resid, vol_host, n_tenor) : 0;
-        if ((poly || cub) && eresp_windows(B, nullptr, nullptr) == 1 &&
+        const int first = (poly || cub) ? eresp_first_active_date(n_tenor, dt / dtau, (int)stride, B, nres) : 2;
+        if ((poly || cub) && eresp_windows(B, first, nullptr, nullptr, nullptr) == 1 &&
             eresp_table_elems((int)stride, B, cub ? 4 : 3, nres, 1) <= kStaticRespEntries) {
             // the decomposition's response form in one window: its table (FP32
             // pairs, 16 bytes per entry like the double2 array) in the static array
@@ -331,9 +332,9 @@ hjm_status hjm_run_static(void* cuda_stream, int32_t n_tenor, double dtau, const
             E.P = P;
             E.frame = block_frame_n(fr.n, (int)stride);
             E.row = eresp_row(B);
-            E.renorm = cub ? 1 : 0;  // one window: the residual's terms only (as hjm_run)
-            STATIC_CUDA(
-                launch_path_fp64_eresp(E, &fr, degs, nres, table, nullptr, partials, nullptr, nullptr, s, nullptr));
+            E.renorm = (cub || B > kRespSlots + 1) ? 1 : 0;  // as hjm_run
+            STATIC_CUDA(launch_path_fp64_eresp(E, &fr, degs, nres, table, first, nullptr, partials, nullptr, nullptr, s,
+                                               nullptr));
         } else if (B >= 2 && B <= response_max_dates() && entries <= kStaticRespEntries) {
             // the response form: its table (zero outside the live entries) into the static array
             STATIC_CUDA(cudaMemsetAsync(resp_table, 0, sizeof(double2) * entries, s));

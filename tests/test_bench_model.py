@@ -10,7 +10,7 @@ import numpy as np
 import bench
 
 sys.path.insert(0, str(Path(__file__).parent))
-import test_response_form as R  # noqa: E402
+import test_cubic_windows as W  # noqa: E402
 
 
 def test_response_forms_count_the_kernels_operations():
@@ -42,5 +42,6 @@ def test_convected_forms_exceed_the_response_forms():
 def test_response_slots_follow_the_kernels_value_prefix():
     for nt, n_steps, stride in ((51, 1000, 50), (61, 1000, 50), (51, 600, 25)):
         B = n_steps // stride
-        tab, _, _ = R.response_table(nt, stride, B, 1.0 / stride, 0.5)
-        np.testing.assert_array_equal(bench.response_active_prefix(nt, n_steps, stride), R.active_prefix(tab, B, stride))
+        tab, kappa = W.eresp_table(nt, stride, B, 1.0 / stride)
+        np.testing.assert_array_equal(bench.response_active_prefix(nt, n_steps, stride),
+                                      W.eresp_prefix(tab, kappa, B, stride))

@@ -16,7 +16,11 @@
   block, x = M^a y and sum = Q(a) y - v at its end, and W before step s =
   y_W + s n23 y_X, against the direct recursion of the parts.
 * The windows: every date is priced by exactly one window, every window holds
-  at most 24 dates with a slot, the latest window is run first.
+  at most 24 dates that can be active (from the first date the remainder
+  reaches, eresp_first_active_date, on), the latest window is run first.
+* The active prefix of the response table (eresp_active_kernel): the terms it
+  skips sum, per date, to less than 32 x 2^-53 |kappa| per unit |W|, and the
+  sums over it equal the convected remainder.
 """
 from __future__ import annotations
 
@@ -237,26 +241,163 @@ def test_four_part_moving_frame_equals_the_parts_recursion(stride):
     assert np.allclose(Qa @ y - v, xs, rtol=1e-12, atol=1e-15)
 
 
-def windows(B):
-    """Restatement of eresp_windows: latest first."""
+def windows(B, first=2):
+    """Restatement of eresp_windows: latest first, (lo, hi, ns); dates before
+    first never need a slot."""
+    f = max(first, 2)
     out, h = [], B
     while h >= 1:
-        lo = h - SLOTS + 1
-        if lo <= 2:
-            lo = 1
-        out.append((lo, h))
+        lo = 1
+        if h - f + 1 > SLOTS:
+            lo = h - SLOTS + 1
+            if lo <= 2:
+                lo = 1
+        act = max(h - max(lo, f) + 1, 0)
+        ns = 12 if act <= 12 else (16 if act <= 16 else (20 if act <= 20 else 24))
+        out.append((lo, h, ns))
         h = lo - 1
     return out
 
 
+@pytest.mark.parametrize("first", [2, 10, 13])
 @pytest.mark.parametrize("B", list(range(1, 61)))
-def test_windows_partition_the_dates(B):
-    w = windows(B)
-    dates = sorted(d for lo, hi in w for d in range(lo, hi + 1))
+def test_windows_partition_the_dates(B, first):
+    w = windows(B, first)
+    dates = sorted(d for lo, hi, _ in w for d in range(lo, hi + 1))
     assert dates == list(range(1, B + 1))
-    for lo, hi in w:
-        assert hi - max(lo, 2) + 1 <= SLOTS
+    for lo, hi, ns in w:
+        active = max(hi - max(lo, first, 2) + 1, 0)
+        assert active <= ns <= SLOTS
+        assert hi - max(lo, 2) + 1 <= SLOTS or lo == 1
     assert w[0][1] == B and w[-1][0] == 1
-    assert [hi for _, hi in w] == sorted((hi for _, hi in w), reverse=True)
-    if B <= 25:
-        assert w == [(1, B)]
+    assert [hi for _, hi, _ in w] == sorted((hi for _, hi, _ in w), reverse=True)
+    if B <= 25 or B - max(first, 2) + 1 <= SLOTS:
+        assert [(lo, hi) for lo, hi, _ in w] == [(1, B)]
+    if first == 2:
+        # every date with a slot: the windows of 24 slotted dates
+        h = B
+        for lo, hi, _ in w:
+            assert hi == h and lo == (1 if h - 23 <= 2 else h - 23)
+            h = lo - 1
+
+
+# --- the active prefixes of the Euler response table (eresp_active_kernel) ---
+def eresp_table(nt, stride, B, c, dtau=0.5):
+    """kappa G_j(lag) and kappa CG_j(lag) per (row n = b stride + s, global slot
+    B - j), lag = j stride - 1 - n, as eresp_table_kernel writes them (FP64)."""
+    L = nt - 1
+    kappa = -2.0 * c * dtau * dtau
+    rows = B * stride
+    tab = np.zeros((rows, B + 1, 2))
+    v = np.zeros(nt)
+    v[L] = 1.0
+    cum = np.zeros(nt)
+    for m in range((B - 1) * stride):
+        cum = cum + v
+        for t in range(2, B + 1):
+            n = t * stride - 1 - m
+            if n >= stride:
+                tab[n, B - t] = (kappa * v[t], kappa * cum[t])
+        v = upwind(v, c)
+    return tab, kappa
+
+
+def eresp_prefix(tab, kappa, B, stride):
+    """As eresp_active_kernel without a residual: per row, the slots up to the
+    last whose FP32 kappa G reaches 2^-53 |kappa| or kappa CG reaches 2^-53
+    |kappa| times the date's sampling step."""
+    a = np.abs(tab.astype(np.float32))
+    tg = np.float32(abs(kappa)) * np.float32(2.0 ** -53)
+    dates = np.maximum(B - np.arange(tab.shape[1]), 1)
+    tcg = (tg * (dates * stride).astype(np.float32)).astype(np.float32)
+    sig = ((a[:, :, 0] != 0) & (a[:, :, 0] >= tg)) | ((a[:, :, 1] != 0) & (a[:, :, 1] >= tcg[None, :]))
+    return np.where(sig.any(axis=1), tab.shape[1] - np.argmax(sig[:, ::-1], axis=1), 0)
+
+
+ERESP_SHAPES = [(51, 50, 20), (51, 50, 24), (61, 50, 24), (51, 25, 20), (51, 100, 10), (51, 10, 5)]
+
+
+@pytest.mark.parametrize("nt,stride,B", ERESP_SHAPES)
+def test_eresp_prefix_drops_only_terms_below_the_unit_roundoff(nt, stride, B):
+    """The prefix skips, per date, terms that sum to less than 32 x 2^-53 |kappa|
+    per unit |W| (and per sampling step for the running sum), and at the 10y
+    shape a quarter of the terms the nonzero prefix would keep."""
+    c = (0.5 / stride) / 0.5
+    tab, kappa = eresp_table(nt, stride, B, c)
+    pre = eresp_prefix(tab, kappa, B, stride)
+    nz = np.where((tab != 0).any(axis=2).any(axis=1),
+                  tab.shape[1] - np.argmax((tab != 0).any(axis=2)[:, ::-1], axis=1), 0)
+    assert np.all(pre <= nz)
+    for t in range(2, B + 1):
+        r = B - t
+        rows = np.arange(stride, t * stride)
+        dropped = rows[pre[rows] <= r]
+        dg = np.abs(tab[dropped, r, 0]).sum()
+        dcg = np.abs(tab[dropped, r, 1]).sum()
+        assert dg <= 32 * 2.0 ** -53 * abs(kappa), (t, dg)
+        assert dcg <= 32 * 2.0 ** -53 * abs(kappa) * t * stride, (t, dcg)
+    if (nt, stride, B) == (51, 50, 20):
+        groups = lambda p: 4 * ((p[stride:] + 3) // 4)
+        assert groups(pre).mean() < 0.8 * groups(nz).mean()
+
+
+@pytest.mark.parametrize("nt,stride,B", ERESP_SHAPES[:4])
+def test_eresp_prefix_sums_equal_the_convected_remainder(nt, stride, B):
+    """The response sums over the prefix against hc <- A hc + kappa W e_L,
+    to 1e-12 of each sum plus the dropped terms' bound."""
+    c = (0.5 / stride) / 0.5
+    tab, kappa = eresp_table(nt, stride, B, c)
+    pre = eresp_prefix(tab, kappa, B, stride)
+    L = nt - 1
+    W = np.cumsum(np.random.default_rng(3).normal(size=B * stride)) * 1e-5
+    acc = np.zeros((B + 1, 2))
+    hc, hs = np.zeros(nt), np.zeros(nt)
+    for n in range(stride, B * stride):
+        w = W[n - 1]
+        acc[: pre[n]] += tab[n, : pre[n]] * w
+        hc = upwind(hc, c)
+        hc[L] += kappa * w
+        hs += hc
+        if (n + 1) % stride == 0:
+            j = (n + 1) // stride
+            if j >= 2:
+                floor = 32 * 2.0 ** -53 * abs(kappa) * np.abs(W).max()
+                assert abs(acc[B - j, 0] - hc[j]) <= 1e-12 * abs(hc[j]) + floor
+                assert abs(acc[B - j, 1] - hs[j]) <= 1e-12 * abs(hs[j]) + floor * j * stride
+
+
+def first_active_date(nt, stride, B):
+    """Restatement of eresp_first_active_date (no residual): the earliest date
+    whose kappa G or kappa CG reaches half the device's threshold at some lag
+    its entries hold."""
+    c = (0.5 / stride) / 0.5
+    L = nt - 1
+    v = np.zeros(nt)
+    v[L] = 1.0
+    cum = np.zeros(nt)
+    sig = np.zeros(B + 1, bool)
+    for m in range((B - 1) * stride):
+        cum = cum + v
+        for t in range(2, B + 1):
+            if m <= (t - 1) * stride - 1 and (abs(v[t]) >= 2.0 ** -54 or abs(cum[t]) >= 2.0 ** -54 * t * stride):
+                sig[t] = True
+        v = upwind(v, c)
+    hits = np.nonzero(sig)[0]
+    return int(hits[0]) if hits.size else B + 1
+
+
+@pytest.mark.parametrize("nt,stride,B", ERESP_SHAPES + [(51, 50, 30), (61, 50, 36)])
+def test_first_active_date_bounds_the_device_prefix(nt, stride, B):
+    """No row's active prefix reaches a date before the first active date, so
+    the windows' slots from it on (eresp_windows) hold every active term; at
+    the 10y shape the remainder never reaches dates 2 to 9."""
+    c = (0.5 / stride) / 0.5
+    tab, kappa = eresp_table(nt, stride, B, c)
+    pre = eresp_prefix(tab, kappa, B, stride)
+    f = first_active_date(nt, stride, B)
+    assert pre.max() <= max(B - f + 1, 0)
+    if (nt, stride, B) == (51, 50, 20):
+        assert f == 10 and pre.max() == 11
+        assert windows(B, f) == [(1, 20, 12)]
+    if (nt, stride, B) == (51, 50, 30):
+        assert [(lo, hi) for lo, hi, _ in windows(B, f)] == [(1, 30)]

@@ -294,14 +294,21 @@ def test_remainder_forms_agree_and_match_oracle(engine, remainder_form, nt, coef
 
 @pytest.mark.parametrize("n_paths,n_steps,dt", [(1, 1000, 0.01), (63, 500, 0.02), (257, 1200, 0.01),
                                                 (100, 250, 0.01), (64, 1000, 0.005), (100, 50, 0.05),
-                                                (65, 1000, 0.004)],
+                                                (65, 1000, 0.004), (129, 1050, 0.01), (130, 1250, 0.01),
+                                                (131, 1300, 0.01), (67, 1800, 0.01)],
                          ids=["1-path", "stride25", "24-dates", "5-dates", "stride100", "stride10-all-zero",
-                              "stride125-coefficients-via-L1"])
+                              "stride125-coefficients-via-L1", "21-dates", "25-dates", "26-dates-one-window",
+                              "36-dates-two-windows"])
 def test_response_form_shapes_vs_oracle(engine, remainder_form, n_paths, n_steps, dt):
-    """Ragged path counts, strides 10 to 125, 5 to 24 dates (the form's maximum);
-    with stride 10 the remainder never reaches a sampled tenor (all responses
-    zero); beyond 112 steps per block the frame's coefficients are read
-    through L1 instead of shared memory."""
+    """Ragged path counts, strides 10 to 125, 5 to 36 dates.  The remainder
+    reaches dates 10 and later only (stride 50), so the windows hold slots
+    from date 10 on: 20 and 21 dates in the 12-slot kernel, 24 and 25 in the
+    16-slot one, 26 in one window of the 20-slot one, 36 in two windows
+    (dates 13 to 36 in the 24-slot kernel, then 1 to 12 in the 12-slot one);
+    with stride 10 the
+    remainder never reaches a sampled tenor (all responses zero); beyond 112
+    steps per block the frame's coefficients are read through L1 instead of
+    shared memory."""
     mk = _poly_market(engine)
     stride = int(round(mk.dtau / dt))
     sw = Swap(n_periods=max(n_steps // stride, 1))
