@@ -812,7 +812,7 @@ static void fill_pc(const hjm_ctx* ctx, const RunShape& sh, double dt, const Pat
 //
 // Euler step with a decomposition (quadratic, or cubic with a residual
 // table): the response form of hjm_eresp.cu, whose per-step work is on the
-// FP32 pipe and which takes any number of dates (in windows); measured 6.9x
+// FP32 pipe and which takes any number of dates (in windows); measured 9.0x
 // the convected form at 20 dates, and the convected cubic has no form but the
 // table step, so AUTO always takes it.
 static bool use_response_form(const hjm_ctx* ctx, const RunShape& sh)

@@ -385,48 +385,48 @@ struct ResidLoadings {
 // 1 <= b < j <= B.  Every lag of date j maps to one entry (q = j - b
 // = l / stride + 1, s = q stride - 1 - l); the rest of the table stays zero.
 // G and R by repeated upwind steps in FP64 (backward difference at the last
-// tenor), one CTA, thread t holding tenor t.
+// tenor), one CTA per component (G, each residual factor), thread t holding
+// tenor t.
 __global__ void __launch_bounds__(kMaxTenor)
     eresp_table_kernel(int nt, double c, int stride, int B, int row, int nres, double kappa, ResidLoadings RL,
                        float4* __restrict__ resp)
 {
-    __shared__ double v_s[4][kMaxTenor];
+    // CTA q: component 0 (kappa G, from e_L) or a residual factor's R_k (k = 0
+    // with nres = 3; then 1 and 2), each with its running sum; the components
+    // are independent, so they run on separate SMs (the recursion is FP64)
+    const int k = nres == 3 ? (int)blockIdx.x - 1 : (int)blockIdx.x;  // residual factor of CTA q > 0
+    __shared__ double v_s[kMaxTenor];
     const int t = threadIdx.x;
     const int L = nt - 1;
     const int M = (B - 1) * stride - 1;  // the longest lag read
-    double v[4], cum[4];                 // [0]: G (e_L), [1..3]: R_k (r_k)
-    v[0] = (t == L) ? 1.0 : 0.0;
     const int ent = nres == 3 ? 3 : (nres == 2 ? 2 : 1);
-    for (int k = 0; k < kFactors; ++k) v[1 + k] = (t < nt && nres > 0) ? RL.r[k][t] : 0.0;
-    for (int q = 0; q < 4; ++q) cum[q] = 0.0;
+    double v = blockIdx.x == 0 ? ((t == L) ? 1.0 : 0.0) : (t < nt ? RL.r[k][t] : 0.0);
+    double cum = 0.0;
+    // the float2 of a residual factor: nres = 3: R_0 e[1].xy, R_1 e[1].zw,
+    // R_2 e[2].xy; nres = 2: R_1 e[1].xy, R_2 e[1].zw
+    const int f2 = nres == 3 ? k : k - 1;  // float2 index within the slot's entries after e[0]
     for (int m = 0; m <= M; ++m) {
-        for (int q = 0; q < 4; ++q) cum[q] += v[q];
+        cum += v;
         if (t >= 2 && t <= B) {
             const int qd = m / stride + 1;
             const int b = t - qd;
             if (b >= 1) {
                 float4* e = resp + (((size_t)b * stride + (size_t)(qd * stride - 1 - m)) * row + (B - t)) * ent;
-                const double g = kappa * v[0], cg = kappa * cum[0];
-                const float gh = __double2float_rn(g), cgh = __double2float_rn(cg);
-                e[0] = make_float4(gh, cgh, __double2float_rn(g - (double)gh), __double2float_rn(cg - (double)cgh));
-                if (nres == 3) {
-                    e[1] = make_float4(__double2float_rn(v[1]), __double2float_rn(cum[1]), __double2float_rn(v[2]),
-                                       __double2float_rn(cum[2]));
-                    e[2] = make_float4(__double2float_rn(v[3]), __double2float_rn(cum[3]), 0.0f, 0.0f);
-                } else if (nres == 2) {
-                    e[1] = make_float4(__double2float_rn(v[2]), __double2float_rn(cum[2]), __double2float_rn(v[3]),
-                                       __double2float_rn(cum[3]));
+                if (blockIdx.x == 0) {
+                    const double g = kappa * v, cg = kappa * cum;
+                    const float gh = __double2float_rn(g), cgh = __double2float_rn(cg);
+                    e[0] = make_float4(gh, cgh, __double2float_rn(g - (double)gh), __double2float_rn(cg - (double)cgh));
+                } else {
+                    reinterpret_cast<float2*>(e + 1)[f2] = make_float2(__double2float_rn(v), __double2float_rn(cum));
                 }
             }
         }
-        for (int q = 0; q < 4; ++q) v_s[q][t] = v[q];
+        v_s[t] = v;
         __syncthreads();
-        for (int q = 0; q < 4; ++q) {
-            if (t < L)
-                v[q] += c * (v_s[q][t + 1] - v[q]);
-            else if (t == L)
-                v[q] += c * (v[q] - v_s[q][L - 1]);
-        }
+        if (t < L)
+            v += c * (v_s[t + 1] - v);
+        else if (t == L)
+            v += c * (v - v_s[L - 1]);
         __syncthreads();
     }
 }
@@ -627,7 +627,8 @@ static cudaError_t launch_eresp_responses(int nt, double c, double dtau, int str
         for (int k = 0; k < kFactors; ++k)
             for (int t = 0; t < nt; ++t) RL.r[k][t] = resid[k * nt + t];
     const double kappa = -2.0 * (c * dtau * dtau);
-    eresp_table_kernel<<<1, kMaxTenor, 0, s>>>(nt, c, stride, n_blocks, row, nres, kappa, RL, table);
+    // one CTA for the remainder's responses, one per residual factor
+    eresp_table_kernel<<<1 + nres, kMaxTenor, 0, s>>>(nt, c, stride, n_blocks, row, nres, kappa, RL, table);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     eresp_active_kernel<<<1, 1024, 0, s>>>((int)rows, row, ent, stride, n_blocks, (float)kappa, table,
@@ -676,12 +677,12 @@ cudaError_t launch_window(const EulerRespParams& E, int ns, const float4* table,
     const bool sc = (size_t)E.P.stride * sr <= (size_t)kFrameSmemRows * kStateRow;
     const size_t smem = eresp_smem(E.win_lo, E.win_hi, NP, sc ? E.P.stride * sr : 0);
     auto k = sc ? path_kernel_fp64_eresp<EXT, DEGS, NRES, true> : path_kernel_fp64_eresp<EXT, DEGS, NRES, false>;
-    // a window with at most 20, 16 or 12 active slots, quadratic factors, the
-    // generator's normals: fewer slots in fewer registers, more CTAs per SM
-    // (20 slots: 8 CTAs instead of 6, 15.9 ms against 16.4 for the 10y
-    // headline; the cubic form with its residual spills at 128 registers and
-    // runs slower, 27.0 against 25.9 ms, and its residual keeps every date
-    // still to be sampled active, so it keeps 24)
+    // a window with at most 20, 16 or 12 dates that can be active, quadratic
+    // factors, the generator's normals: fewer slots in fewer registers, more
+    // CTAs per SM (the 10y headline: 12 slots, 10 CTAs, 12.9 ms against 13.6
+    // with 20 slots at 8 CTAs; the cubic form with its residual spills at 128
+    // registers and runs slower, 27.0 against 25.9 ms, and its residual keeps
+    // every date still to be sampled active, so it keeps 24)
     if constexpr (!EXT && NRES == 0) {
         if (sc && ns <= 12)
             k = path_kernel_fp64_eresp<EXT, DEGS, NRES, true, 12>;
