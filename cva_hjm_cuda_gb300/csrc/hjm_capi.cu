@@ -1036,7 +1036,7 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
     if (store) HJM_CUDA(ctx, ctx->estore.ensure(esize * (size_t)n_dates * (size_t)ld));
     if (want_pfe) {
         HJM_CUDA(ctx, ctx->sel.ensure(sizeof(SelState) * kMaxTenor));
-        HJM_CUDA(ctx, ctx->hist.ensure(sizeof(uint32_t) * 256 * kMaxTenor));
+        HJM_CUDA(ctx, ctx->hist.ensure(pfe_scratch_bytes()));
     }
     cudaStream_t s = ctx->stream;
     ctx->have_result = false;
@@ -1120,7 +1120,7 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
         const int64_t k = std::min<int64_t>(std::max<int64_t>((int64_t)std::ceil(pfe_q * (double)n_paths - 1e-7), 1),
                                             n_paths);
         HJM_CUDA(ctx, launch_pfe(ctx->estore.p, !mixed, ld, n_paths, n_dates, (uint64_t)(k - 1),
-                                 (SelState*)ctx->sel.p, (uint32_t*)ctx->hist.p, (double*)ctx->result.p, ctx->n_sms,
+                                 (SelState*)ctx->sel.p, ctx->hist.p, (double*)ctx->result.p, ctx->n_sms,
                                  s));
         ctx->stat_launches += 2 + 2 * (mixed ? 4 : 8);  // init, 8-bit digit passes (histogram + scan), write
     }

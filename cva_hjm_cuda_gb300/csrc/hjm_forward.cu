@@ -764,16 +764,27 @@ __global__ void finalize_results(const double* __restrict__ sums, FinalParams F,
 // ---------------------------------------------------------------------------
 // PFE: exact k-th smallest exposure of every date column by most-significant-
 // digit radix selection on the IEEE bit patterns (exposures are >= +0, so the
-// unsigned order of the bits is the numeric order).  8-bit digits; each pass
-// histograms the candidates that match the prefix found so far.
+// unsigned order of the bits is the numeric order).  11-bit digits; each pass
+// histograms the candidates that match the prefix found so far.  Once a
+// date's candidates number at most kPfeCap (two digits in, for a continuous
+// distribution: 1/2048 of an octave), one more pass copies them to a buffer
+// and one CTA ranks them in shared memory; the date's later passes exit at
+// once.  A date whose candidates stay many (ties: e.g. most exposures zero)
+// finishes by the global passes alone.  Three reads of the store instead of
+// eight (FP64) or four (FP32) with 8-bit digits.
 // ---------------------------------------------------------------------------
+constexpr int kPfeDigit = 11;
+constexpr int kPfeBins = 1 << kPfeDigit;
+
 template <typename K>
 __global__ void pfe_hist(const K* __restrict__ keys, int64_t ld, int64_t n, const SelState* __restrict__ st,
-                         uint32_t* __restrict__ hist, int shift)
+                         uint32_t* __restrict__ hist, int shift, int bits)
 {
-    __shared__ uint32_t h[256];
+    __shared__ uint32_t h[kPfeBins];
     const int date = blockIdx.y;
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) h[i] = 0;
+    if (st[date].stage != 0) return;  // compacted: ranked in shared memory
+    const int nb = 1 << bits;
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) h[i] = 0;
     __syncthreads();
     const uint64_t prefix = st[date].prefix, mask = st[date].mask;
     const K* col = keys + (size_t)date * (size_t)ld;
@@ -785,7 +796,7 @@ __global__ void pfe_hist(const K* __restrict__ keys, int64_t ld, int64_t n, cons
         if (i < n) {
             const uint64_t k = (uint64_t)col[i];
             take = (k & mask) == prefix;
-            digit = (uint32_t)(k >> shift) & 0xFFu;
+            digit = (uint32_t)(k >> shift) & (uint32_t)(nb - 1);
         }
         // warp-aggregated increments: one atomic per distinct digit per warp
         const uint32_t active = __ballot_sync(0xffffffffu, take);
@@ -795,27 +806,127 @@ __global__ void pfe_hist(const K* __restrict__ keys, int64_t ld, int64_t n, cons
         }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < 256; i += blockDim.x)
-        if (h[i]) atomicAdd(&hist[date * 256 + i], h[i]);
+    for (int i = threadIdx.x; i < nb; i += blockDim.x)
+        if (h[i]) atomicAdd(&hist[(size_t)date * kPfeBins + i], h[i]);
 }
 
-__global__ void pfe_scan(SelState* __restrict__ st, uint32_t* __restrict__ hist, int shift)
+// One CTA per date (256 threads): the digit whose cumulative count passes k,
+// by a block-wide prefix sum over the bins (8 per thread); the histogram is
+// cleared for the next pass.  A date left with at most kPfeCap candidates is
+// marked for compaction (stage 1).
+__global__ void __launch_bounds__(256) pfe_scan(SelState* __restrict__ st, uint32_t* __restrict__ hist, int shift,
+                                                int bits)
 {
+    __shared__ uint32_t wsum[8];
+    __shared__ int found;
     const int date = blockIdx.x;
-    if (threadIdx.x == 0) {
-        uint64_t k = st[date].k;
-        uint32_t* hd = hist + date * 256;
-        int d = 0;
-        for (; d < 255; ++d) {
-            if (k < hd[d]) break;
-            k -= hd[d];
+    if (st[date].stage != 0) return;
+    const int nb = 1 << bits;
+    const int per = (nb + 255) / 256;  // bins per thread (8 at 11 bits)
+    uint32_t* hd = hist + (size_t)date * kPfeBins;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    uint32_t mine = 0;
+    for (int b = 0; b < per; ++b) {
+        const int bin = t * per + b;
+        if (bin < nb) mine += hd[bin];
+    }
+    // exclusive prefix of the threads' sums
+    uint32_t incl = mine;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    if (lane == 31) wsum[warp] = incl;
+    if (t == 0) found = 0;
+    __syncthreads();
+    uint32_t before = incl - mine;
+    for (int w = 0; w < warp; ++w) before += wsum[w];
+    const uint64_t k = st[date].k;
+    if ((uint64_t)before <= k && k < (uint64_t)before + mine) {
+        uint64_t r = k - before;
+        int d = t * per;
+        for (;; ++d) {
+            const uint32_t c = hd[d];
+            if (r < c) break;
+            r -= c;
         }
+        const uint32_t cnt = hd[d];
         st[date].prefix |= (uint64_t)d << shift;
-        st[date].mask |= (uint64_t)0xFF << shift;
-        st[date].k = k;
+        st[date].mask |= (uint64_t)(nb - 1) << shift;
+        st[date].k = r;
+        st[date].count = cnt;
+        if (cnt <= (uint32_t)kPfeCap && shift > 0) st[date].stage = 1;
+        found = 1;
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) hist[date * 256 + i] = 0;
+    for (int b = 0; b < per; ++b) {
+        const int bin = t * per + b;
+        if (bin < nb) hd[bin] = 0;
+    }
+}
+
+// Copies the candidates of the dates marked for compaction (stage 1) to their
+// buffers, warp-aggregated appends.
+template <typename K>
+__global__ void pfe_compact(const K* __restrict__ keys, int64_t ld, int64_t n, const SelState* __restrict__ st,
+                            uint64_t* __restrict__ buf, uint32_t* __restrict__ cnt)
+{
+    const int date = blockIdx.y;
+    if (st[date].stage != 1) return;
+    const uint64_t prefix = st[date].prefix, mask = st[date].mask;
+    const K* col = keys + (size_t)date * (size_t)ld;
+    uint64_t* out = buf + (size_t)date * kPfeCap;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int lane = threadIdx.x & 31;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
+        const int64_t i = base + threadIdx.x;
+        uint64_t k = 0;
+        bool take = false;
+        if (i < n) {
+            k = (uint64_t)col[i];
+            take = (k & mask) == prefix;
+        }
+        const uint32_t ballot = __ballot_sync(0xffffffffu, take);
+        if (ballot) {
+            uint32_t at = 0;
+            if (lane == __ffs(ballot) - 1) at = atomicAdd(&cnt[date], (uint32_t)__popc(ballot));
+            at = __shfl_sync(0xffffffffu, at, __ffs(ballot) - 1);
+            if (take) {
+                const uint32_t pos = at + __popc(ballot & ((1u << lane) - 1u));
+                if (pos < (uint32_t)kPfeCap) out[pos] = k;  // (the scan counted them: at most kPfeCap)
+            }
+        }
+    }
+}
+
+// One CTA per compacted date: the candidate of rank k (ties by buffer
+// position, so exactly one has it) becomes the date's key; stage 2.
+__global__ void __launch_bounds__(256) pfe_finish(SelState* __restrict__ st, const uint64_t* __restrict__ buf,
+                                                  uint32_t* __restrict__ cnt)
+{
+    __shared__ uint64_t c_s[kPfeCap];
+    const int date = blockIdx.x;
+    if (st[date].stage != 1) return;
+    const uint32_t m = min(cnt[date], (uint32_t)kPfeCap);
+    for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) c_s[i] = buf[(size_t)date * kPfeCap + i];
+    __syncthreads();
+    const uint64_t k = st[date].k;
+    for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
+        const uint64_t v = c_s[i];
+        uint32_t rank = 0;
+        for (uint32_t j = 0; j < m; ++j) {
+            const uint64_t w = c_s[j];
+            rank += (w < v) || (w == v && j < i);
+        }
+        if (rank == k) st[date].prefix = v;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        st[date].mask = ~0ull;
+        st[date].k = 0;
+        st[date].stage = 2;
+        cnt[date] = 0;
+    }
 }
 
 template <typename K>
@@ -842,6 +953,8 @@ __global__ void pfe_init(SelState* __restrict__ st, int n_dates, uint64_t k0)
         st[j].prefix = 0;
         st[j].mask = 0;
         st[j].k = k0;
+        st[j].count = 0;
+        st[j].stage = 0;
     }
 }
 
@@ -1056,23 +1169,41 @@ cudaError_t launch_reduce(const double* partials, int64_t n_rows, int R, double*
     return cudaGetLastError();
 }
 
-cudaError_t launch_pfe(const void* estore, bool fp64_keys, int64_t ld, int64_t n_paths, int n_dates, uint64_t k0,
-                       SelState* st, uint32_t* hist, double* result, int n_sms, cudaStream_t s)
+size_t pfe_scratch_bytes()
 {
+    return sizeof(uint32_t) * ((size_t)kPfeBins * kMaxTenor + kMaxTenor) + sizeof(uint64_t) * (size_t)kPfeCap * kMaxTenor;
+}
+
+cudaError_t launch_pfe(const void* estore, bool fp64_keys, int64_t ld, int64_t n_paths, int n_dates, uint64_t k0,
+                       SelState* st, void* scratch, double* result, int n_sms, cudaStream_t s)
+{
+    uint32_t* hist = (uint32_t*)scratch;
+    uint32_t* cnt = hist + (size_t)kPfeBins * kMaxTenor;
+    uint64_t* buf = (uint64_t*)(cnt + kMaxTenor);  // 8-byte aligned: kPfeBins * kMaxTenor + kMaxTenor is even
     pfe_init<<<1, kMaxTenor, 0, s>>>(st, n_dates, k0);
-    cudaMemsetAsync(hist, 0, sizeof(uint32_t) * 256 * (size_t)n_dates, s);
+    cudaError_t e = cudaMemsetAsync(scratch, 0, sizeof(uint32_t) * ((size_t)kPfeBins * kMaxTenor + kMaxTenor), s);
+    if (e != cudaSuccess) return e;
     int64_t gx = (n_paths + 1023) / 1024;
     const int64_t cap = (int64_t)n_sms * 8;
     if (gx > cap) gx = cap;
     if (gx < 1) gx = 1;
     const dim3 grid((unsigned)gx, (unsigned)n_dates);
-    const int bits = fp64_keys ? 64 : 32;
-    for (int shift = bits - 8; shift >= 0; shift -= 8) {
+    const int total = fp64_keys ? 64 : 32;
+    for (int top = total; top > 0; top -= kPfeDigit) {
+        const int bits = top < kPfeDigit ? top : kPfeDigit;
+        const int shift = top - bits;
+        if (fp64_keys) {
+            pfe_hist<uint64_t><<<grid, 256, 0, s>>>((const uint64_t*)estore, ld, n_paths, st, hist, shift, bits);
+        } else {
+            pfe_hist<uint32_t><<<grid, 256, 0, s>>>((const uint32_t*)estore, ld, n_paths, st, hist, shift, bits);
+        }
+        pfe_scan<<<n_dates, 256, 0, s>>>(st, hist, shift, bits);
+        if (shift == 0) break;
         if (fp64_keys)
-            pfe_hist<uint64_t><<<grid, 256, 0, s>>>((const uint64_t*)estore, ld, n_paths, st, hist, shift);
+            pfe_compact<uint64_t><<<grid, 256, 0, s>>>((const uint64_t*)estore, ld, n_paths, st, buf, cnt);
         else
-            pfe_hist<uint32_t><<<grid, 256, 0, s>>>((const uint32_t*)estore, ld, n_paths, st, hist, shift);
-        pfe_scan<<<n_dates, 256, 0, s>>>(st, hist, shift);
+            pfe_compact<uint32_t><<<grid, 256, 0, s>>>((const uint32_t*)estore, ld, n_paths, st, buf, cnt);
+        pfe_finish<<<n_dates, 256, 0, s>>>(st, buf, cnt);
     }
     if (fp64_keys)
         pfe_write<uint64_t><<<1, kMaxTenor, 0, s>>>(st, n_dates, result);

@@ -31,7 +31,11 @@ struct FinalParams {
 
 struct SelState {
     uint64_t prefix, mask, k;
+    uint32_t count;  // candidates matching the prefix after the last pass
+    uint32_t stage;  // 0: global passes; 1: to compact and rank; 2: done
 };
+// Candidates of a date ranked in shared memory by the PFE selection.
+constexpr int kPfeCap = 2048;
 
 // Mixed-precision path kernel parameters: the FP32 parameter block plus the
 // volatility coefficients packed in tenor pairs {tenor p, tenor p + ceil(NT/2)}
@@ -93,8 +97,11 @@ int path_cta(bool mixed);  // paths per CTA of the path kernel (one partial-sum 
 
 cudaError_t launch_reduce(const double* partials, int64_t n_rows, int R, double* sums, const FinalParams& F,
                           double* result, cudaStream_t s);
+// scratch: pfe_scratch_bytes() of device memory (histograms, counters,
+// candidate buffers).
+size_t pfe_scratch_bytes();
 cudaError_t launch_pfe(const void* estore, bool fp64_keys, int64_t ld, int64_t n_paths, int n_dates, uint64_t k0,
-                       SelState* st, uint32_t* hist, double* result, int n_sms, cudaStream_t s);
+                       SelState* st, void* scratch, double* result, int n_sms, cudaStream_t s);
 cudaError_t launch_dump_normals(int64_t n_paths, uint64_t path_offset, int n_steps, uint32_t k0, uint32_t k1,
                                 double* out, cudaStream_t s);
 cudaError_t launch_philox_words(int64_t n_paths, uint64_t path_offset, uint32_t step, uint32_t k0, uint32_t k1,
