@@ -1,6 +1,7 @@
-// hjm_epilogue.cuh -- the end of the FP64 path kernels (Euler in
-// hjm_forward.cu, predictor-corrector in hjm_pc.cu): exposures, the CTA's
-// partial sums and the exposure store.
+// hjm_epilogue.cuh -- the end of the path kernels (FP64: Euler in
+// hjm_forward.cu, predictor-corrector in hjm_pc.cu; mixed precision: the
+// convected pairs in hjm_forward.cu, the response form in hjm_mresp.cu):
+// exposures, the CTA's partial sums and the exposure store.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -68,6 +69,68 @@ __device__ __forceinline__ void fp64_epilogue(const PathParams<double>& P, const
             const uint32_t bytes = (uint32_t)(((cnt + 1) / 2) * 2 * sizeof(double));
             for (int j = 0; j <= B; ++j) {
                 double* dst = estore + (size_t)j * (size_t)P.ld + (size_t)cta_base;
+                const uint32_t src = (uint32_t)__cvta_generic_to_shared(e_s + (size_t)j * kCta);
+                asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
+                             :: "l"(dst), "r"(src), "r"(bytes) : "memory");
+            }
+            asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+            asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+        }
+    }
+}
+
+// Epilogue of the mixed-precision path kernels (as fp64_epilogue, exposures
+// and their store in FP32): acc_s rows 1..B hold the cash flows (FP64), e_s
+// B+1 FP32 rows (free for this use).
+template <typename CF, int kCta = hjm::kCta>
+__device__ __forceinline__ void mixed_epilogue(const PathParams<float>& P, const CF* acc_s, float* e_s,
+                                               double* red_s, double* __restrict__ partials,
+                                               float* __restrict__ estore, int64_t cta_base, bool active)
+{
+    const int tid = threadIdx.x;
+    const int B = P.n_blocks;
+    double v = 0.0, cva_c = 0.0;
+    e_s[B * kCta + tid] = 0.f;
+    for (int j = B - 1; j >= 0; --j) {
+        v += as_f64(acc_s[(j + 1) * kCta + tid]);
+        double e = (v > 0.0) ? v : 0.0;
+        if (!active) e = 0.0;
+        e_s[j * kCta + tid] = (float)e;
+        cva_c = fma(P.cvaw[j], e, cva_c);
+    }
+    __syncthreads();
+
+    const int warp = tid >> 5, lane = tid & 31;
+    const int R = B + 3;
+    for (int j = warp; j <= B; j += kCta / 32) {
+        double sum = 0.0;
+#pragma unroll
+        for (int q = 0; q < kCta / 32; ++q) sum += (double)e_s[j * kCta + lane + 32 * q];
+        sum = warp_sum(sum);
+        if (lane == 0) partials[(size_t)blockIdx.x * R + j] = sum;
+    }
+    {
+        const double s1 = warp_sum(cva_c), s2 = warp_sum(cva_c * cva_c);
+        if (lane == 0) {
+            red_s[warp] = s1;
+            red_s[kCta / 32 + warp] = s2;
+        }
+    }
+    if (P.store_exposures) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+        double s1 = 0.0, s2 = 0.0;
+        for (int w = 0; w < kCta / 32; ++w) {
+            s1 += red_s[w];
+            s2 += red_s[kCta / 32 + w];
+        }
+        partials[(size_t)blockIdx.x * R + B + 1] = s1;
+        partials[(size_t)blockIdx.x * R + B + 2] = s2;
+        if (P.store_exposures) {
+            const int64_t cnt = (P.n_paths - cta_base < kCta) ? (P.n_paths - cta_base) : kCta;
+            const uint32_t bytes = (uint32_t)(((cnt + 3) / 4) * 4 * sizeof(float));
+            for (int j = 0; j <= B; ++j) {
+                float* dst = estore + (size_t)j * (size_t)P.ld + (size_t)cta_base;
                 const uint32_t src = (uint32_t)__cvta_generic_to_shared(e_s + (size_t)j * kCta);
                 asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
                              :: "l"(dst), "r"(src), "r"(bytes) : "memory");
