@@ -1122,7 +1122,9 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
         HJM_CUDA(ctx, launch_pfe(ctx->estore.p, !mixed, ld, n_paths, n_dates, (uint64_t)(k - 1),
                                  (SelState*)ctx->sel.p, ctx->hist.p, (double*)ctx->result.p, ctx->n_sms,
                                  s));
-        ctx->stat_launches += 2 + 2 * (mixed ? 4 : 8);  // init, 8-bit digit passes (histogram + scan), write
+        // init, write, per 11-bit digit a histogram and a scan, and between
+        // digits the compaction and ranking (6 digits of FP64 keys, 3 of FP32)
+        ctx->stat_launches += 2 + (mixed ? 3 * 2 + 2 * 2 : 6 * 2 + 5 * 2);
     }
     HJM_CUDA(ctx, cudaEventRecord(ctx->ev[3], s));
     {
