@@ -31,7 +31,7 @@ EXPORTED = [
     "hjm_version", "hjm_last_error", "hjm_ctx_create", "hjm_ctx_destroy", "hjm_ctx_set_stream",
     "hjm_ctx_keep_exposures", "hjm_ctx_set_memory_limit", "hjm_ctx_memory_in_use", "hjm_ctx_set_vol_decomposition", "hjm_ctx_set_scheme", "hjm_ctx_vol_decomposition",
     "hjm_ctx_set_remainder_form", "hjm_ctx_remainder_form", "hjm_set_market", "hjm_set_swap", "hjm_set_netting_set", "hjm_run",
-    "hjm_enqueue", "hjm_fetch_results", "hjm_run_with_normals", "hjm_get_exposures", "hjm_set_market_poly", "hjm_calibrate_pca", "hjm_write_report", "hjm_run_mlmc",
+    "hjm_enqueue", "hjm_fetch_results", "hjm_run_with_normals", "hjm_get_exposures", "hjm_get_exposure_paths", "hjm_set_market_poly", "hjm_calibrate_pca", "hjm_write_report", "hjm_run_mlmc",
     "hjm_run_adjoint", "hjm_dump_normals", "hjm_philox_words", "hjm_last_timings", "hjm_timing_history", "hjm_last_stats", "hjm_measure_fma_peak",
     "hjm_dropin_calculate_exposure_fp64", "hjm_dropin_calculate_exposure_fp32", "hjm_run_static",
 ]
@@ -78,6 +78,7 @@ def _declare(lib: C.CDLL) -> None:
         "hjm_run_with_normals": (st, [_vp, C.c_int64, C.c_int32, C.c_double, _dp, C.c_int32, C.c_double, C.c_double,
                                       C.c_double, _dp, _dp, _dp]),
         "hjm_get_exposures": (st, [_vp, _dp, C.c_int64]),
+        "hjm_get_exposure_paths": (st, [_vp, C.c_int64, C.c_int64, _dp]),
         "hjm_run_adjoint": (st, [_vp, C.c_int64, C.c_int32, C.c_double, C.c_uint64, C.c_uint64, C.c_double,
                                  C.c_double, C.c_int32, _dp, _dp, _dp, _dp]),
         "hjm_dump_normals": (st, [_vp, C.c_int64, C.c_uint64, C.c_int32, C.c_uint64, _dp]),

@@ -1254,6 +1254,33 @@ hjm_status hjm_get_exposures(hjm_ctx* ctx, double* out_host, int64_t capacity)
     return HJM_OK;
 }
 
+hjm_status hjm_get_exposure_paths(hjm_ctx* ctx, int64_t path_begin, int64_t n, double* out_host)
+{
+    HJM_CHECK_CTX(ctx);
+    if (!ctx->have_result || !ctx->last_stored)
+        return fail(ctx, HJM_ERR_NOT_CONFIGURED,
+                    "no stored exposures: run with a PFE quantile or after hjm_ctx_keep_exposures(ctx, 1)");
+    if (!out_host || n <= 0 || path_begin < 0 || path_begin > ctx->last_n_paths - n)
+        return fail(ctx, HJM_ERR_INVALID_ARGUMENT, "paths [%lld, %lld + %lld) outside the run's %lld paths",
+                    (long long)path_begin, (long long)path_begin, (long long)n, (long long)ctx->last_n_paths);
+    HJM_CUDA(ctx, cudaSetDevice(ctx->device));
+    const size_t rows = (size_t)ctx->last_n_dates, cols = (size_t)n;
+    const size_t es = ctx->last_mixed ? sizeof(float) : sizeof(double);
+    const char* src = (const char*)ctx->estore.p + (size_t)path_begin * es;
+    if (!ctx->last_mixed) {
+        HJM_CUDA(ctx, cudaMemcpy2DAsync(out_host, cols * sizeof(double), src, (size_t)ctx->last_ld * es,
+                                        cols * es, rows, cudaMemcpyDeviceToHost, ctx->stream));
+        HJM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    } else {
+        std::vector<float> tmp(rows * cols);
+        HJM_CUDA(ctx, cudaMemcpy2DAsync(tmp.data(), cols * sizeof(float), src, (size_t)ctx->last_ld * es,
+                                        cols * es, rows, cudaMemcpyDeviceToHost, ctx->stream));
+        HJM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        for (size_t i = 0; i < rows * cols; ++i) out_host[i] = (double)tmp[i];
+    }
+    return HJM_OK;
+}
+
 // ---------------------------------------------------------------------------
 // diagnostics
 // ---------------------------------------------------------------------------

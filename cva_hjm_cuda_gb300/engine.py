@@ -226,6 +226,13 @@ class HJMEngine:
         self._check(self.lib.hjm_get_exposures(self.ctx, _dptr(out), out.size))
         return out
 
+    def exposure_paths(self, path_begin: int, n: int) -> np.ndarray:
+        """Per-path exposures of the paths [path_begin, path_begin + n) of the
+        last valuation, [n_dates][n]: only that slice leaves the device."""
+        out = np.zeros((self._last_dates, n))
+        self._check(self.lib.hjm_get_exposure_paths(self.ctx, path_begin, n, _dptr(out)))
+        return out
+
     # ---------------------------------------------------------- sensitivities
     def run_adjoint(self, cfg: RunConfig, checkpoint_every: int = 32) -> Sensitivities:
         nt = self.n_tenor

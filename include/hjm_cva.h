@@ -212,6 +212,14 @@ hjm_status hjm_run_with_normals(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, 
  * matrix of simulation_gpu.cu:1003 / simulation_cpu.h:362, transposed). */
 hjm_status hjm_get_exposures(hjm_ctx* ctx, double* out_host, int64_t capacity);
 
+/* Exposures of the paths [path_begin, path_begin + n) of the last valuation,
+ * date-major as hjm_get_exposures: out[j * n + p] for path path_begin + p.
+ * Copies only that slice (one strided device-to-host copy; the FP32 store of
+ * a mixed-precision run is widened on the host), so a caller can inspect a
+ * few paths of a run whose whole store would not fit in host memory.  No
+ * counterpart in the reference, which returns the expected exposure only. */
+hjm_status hjm_get_exposure_paths(hjm_ctx* ctx, int64_t path_begin, int64_t n, double* out_host);
+
 /* ---- multi-level Monte Carlo --------------------------------------------------- */
 /* EE and CVA by multi-level Monte Carlo (the reference's doc/TODO:15): level l
  * runs the context's time scheme with dt / 2^l and n_steps 2^l; level 0 is the plain
