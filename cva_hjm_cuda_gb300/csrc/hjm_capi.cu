@@ -1025,7 +1025,7 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
     const int n_dates = sh.B + 1;
     const int R = sh.B + 3;
     const bool pc = ctx->scheme == HJM_SCHEME_PREDICTOR_CORRECTOR;
-    const int cta = pc ? pc_cta() : path_cta(mixed);
+    const int cta = pc ? pc_cta() : path_cta(mixed, ctx->nt, sh.B, use_poly_path(ctx));
     const int64_t n_ctas = (n_paths + cta - 1) / cta;
     const int64_t ld = (n_paths + 3) / 4 * 4;
     const size_t esize = mixed ? 4 : 8;

@@ -522,8 +522,12 @@ __global__ void __launch_bounds__(kMaxTenor)
 // otherwise; the remainder is a small fraction of the curve), and the FP64
 // running sums of the scalar parts S, U, W stay in registers, so that the
 // shared memory of a CTA (the occupancy limit with 60 dates) shrinks by a third.
-template <int NT, bool EXT, bool POLY, bool CMP>
-__global__ void __launch_bounds__(kCta, 4)
+// Occupancy: with polynomial factors the kernel fits 96 registers without
+// spills, 640 threads per SM (5 CTAs of 128, 20 warps); the table step needs
+// more registers (it spills at 96) and keeps 512, and so do the compact sums,
+// whose 64-thread CTAs shared memory bounds first (7 per SM).
+template <int NT, bool EXT, bool POLY, bool CMP, int C>
+__global__ void __launch_bounds__(C, (POLY && !CMP ? 640 : 512) / C)
     path_kernel_mixed(const __grid_constant__ MixedParams M, const double* __restrict__ ext,
                       double* __restrict__ partials, float* __restrict__ estore)
 {
@@ -535,25 +539,25 @@ __global__ void __launch_bounds__(kCta, 4)
     const int B = P.n_blocks;
     const int rows = B + 1;
     constexpr size_t ka = sizeof(Acc);
-    Acc* acc_s = reinterpret_cast<Acc*>(smem);                                // [B+1][kCta]
-    float* hs_s = reinterpret_cast<float*>(smem + (size_t)rows * kCta * ka);  // [B+2][kCta]
+    Acc* acc_s = reinterpret_cast<Acc*>(smem);                                // [B+1][C]
+    float* hs_s = reinterpret_cast<float*>(smem + (size_t)rows * C * ka);  // [B+2][C]
     double* red_s = reinterpret_cast<double*>(
-        smem + (((size_t)rows * kCta * ka + (size_t)(rows + 1) * kCta * 4 + 7) & ~(size_t)7));
+        smem + (((size_t)rows * C * ka + (size_t)(rows + 1) * C * 4 + 7) & ~(size_t)7));
     double zS = 0.0, zU = 0.0, zW = 0.0;  // CMP: FP64 running sums of the parts over the evolved steps
 
-    const int64_t cta_base = (int64_t)blockIdx.x * kCta;
+    const int64_t cta_base = (int64_t)blockIdx.x * C;
     const int64_t lp = cta_base + tid;
     const bool active = lp < P.n_paths;
     const uint64_t gpath = P.path_offset + (uint64_t)lp;
 
     MixedPath<NT, POLY> x;
     x.reset();
-    for (int i = 0; i < rows; ++i) acc_s[i * kCta + tid] = Acc(0);
-    for (int t = 0; t <= B + 1; ++t) hs_s[t * kCta + tid] = 0.f;
+    for (int i = 0; i < rows; ++i) acc_s[i * C + tid] = Acc(0);
+    for (int t = 0; t <= B + 1; ++t) hs_s[t * C + tid] = 0.f;
 
     auto sample = [&](int i) {
         const double xv = P.psamp[i] + (double)x.value(P, i);
-        double a = P.psum[i] + as_f64(acc_s[i * kCta + tid]);
+        double a = P.psum[i] + as_f64(acc_s[i * C + tid]);
         if constexpr (CMP) {
             const double ti = (double)P.tau[i];
             a += fma(ti, fma(ti, zW, zU), zS);
@@ -562,7 +566,7 @@ __global__ void __launch_bounds__(kCta, 4)
         const float mm = (float)P.m;
         const float L = mm * expm1f((float)xv / mm);
         const float cf = D * ((float)P.payA[i] * L - (float)P.payB[i]);
-        acc_s[i * kCta + tid] = (Acc)cf;  // cash flow of date i
+        acc_s[i * C + tid] = (Acc)cf;  // cash flow of date i
     };
 
     sample(1);
@@ -587,33 +591,33 @@ __global__ void __launch_bounds__(kCta, 4)
         // block sums of tenors 2 .. B; fold (b, B] into FP64 (CMP: the
         // remainder's in FP32, the parts' into their FP64 running sums)
         if constexpr (CMP) {
-            recover_sums_up<NT>(x.h, hs_s, tid, kCta, P, x.g, 0.f, 0.f, 0.f, bs.H1, B, [&](int t, float Ht) {
-                if (t > b) acc_s[t * kCta + tid] += Ht;
+            recover_sums_up<NT>(x.h, hs_s, tid, C, P, x.g, 0.f, 0.f, 0.f, bs.H1, B, [&](int t, float Ht) {
+                if (t > b) acc_s[t * C + tid] += Ht;
             });
             zS += as_f64(bs.sS);
             zU += as_f64(bs.sU);
             zW += as_f64(bs.sW);
         } else {
-            block_sums_up<NT, POLY>(x, hs_s, tid, kCta, P, bs, B, [&](int t, float Ht) {
-                if (t > b) acc_s[t * kCta + tid] += as_f64(Ht);
+            block_sums_up<NT, POLY>(x, hs_s, tid, C, P, bs, B, [&](int t, float Ht) {
+                if (t > b) acc_s[t * C + tid] += as_f64(Ht);
             });
         }
         // the block-end curve (POLY: its convected part) is the next block's start
 #pragma unroll
         for (int t = 1; t < NT; ++t)
-            if (t <= B + 1) hs_s[t * kCta + tid] = x.rem(t);
+            if (t <= B + 1) hs_s[t * C + tid] = x.rem(t);
         sample(b + 1);
     }
 
-    mixed_epilogue(P, acc_s, hs_s, red_s, partials, estore, cta_base, active);
+    mixed_epilogue<Acc, C>(P, acc_s, hs_s, red_s, partials, estore, cta_base, active);
 }
 
-__host__ __device__ inline size_t mixed_smem_bytes(int nt, int n_blocks, bool cmp = false)
+__host__ __device__ inline size_t mixed_smem_bytes(int nt, int n_blocks, bool cmp = false, int cta = kCta)
 {
     (void)nt;
     const size_t rows = (size_t)n_blocks + 1;
-    const size_t head = rows * kCta * (cmp ? 4 : 8) + (rows + 1) * kCta * 4;
-    return ((head + 7) & ~(size_t)7) + 2 * (kCta / 32) * 8;
+    const size_t head = rows * cta * (cmp ? 4 : 8) + (rows + 1) * cta * 4;
+    return ((head + 7) & ~(size_t)7) + 2 * (cta / 32) * 8;
 }
 
 // The compact sums when the FP64 ones would hold a CTA's shared memory above a
@@ -622,6 +626,15 @@ inline bool mixed_compact(int nt, int n_blocks, bool poly)
 {
     return poly && mixed_smem_bytes(nt, n_blocks, false) > (size_t)228 * 1024 / 4;
 }
+
+// Paths per CTA of the mixed kernel.  With the compact sums shared memory
+// bounds the occupancy (~0.5 KB per path with 60 dates), and 64-thread CTAs
+// pack an SM more finely: 7 of them (14 warps) where 3 of 128 threads fit
+// (12 warps) for the 61-tenor netting set, 8 (16 warps) instead of 4 for a
+// 25y swap on 51 tenors.  Otherwise the registers bound it (5 CTAs of 128
+// threads, 20 warps), whatever the CTA size.
+constexpr int kMixedCompactCta = 64;
+inline int mixed_cta(bool cmp) { return cmp ? kMixedCompactCta : kCta; }
 
 void pack_mixed_params(int nt, const PathParams<float>& P, MixedParams& M)
 {
@@ -1063,12 +1076,16 @@ static cudaError_t launch_mixed_t(const MixedParams& M, const double* ext, doubl
                                   cudaStream_t s)
 {
     const bool cmp = mixed_compact(NT, M.P.n_blocks, POLY);
-    const size_t smem = mixed_smem_bytes(NT, M.P.n_blocks, cmp);
-    auto k = cmp ? path_kernel_mixed<NT, EXT, POLY, POLY> : path_kernel_mixed<NT, EXT, POLY, false>;
+    const int cta = mixed_cta(cmp);
+    const size_t smem = mixed_smem_bytes(NT, M.P.n_blocks, cmp, cta);
+    auto k = path_kernel_mixed<NT, EXT, POLY, false, kCta>;
+    if constexpr (POLY) {
+        if (cmp) k = path_kernel_mixed<NT, EXT, true, true, kMixedCompactCta>;
+    }
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    const int64_t grid = (M.P.n_paths + kCta - 1) / kCta;
-    k<<<(unsigned)grid, kCta, smem, s>>>(M, ext, partials, estore);
+    const int64_t grid = (M.P.n_paths + cta - 1) / cta;
+    k<<<(unsigned)grid, cta, smem, s>>>(M, ext, partials, estore);
     return cudaGetLastError();
 }
 
@@ -1097,7 +1114,10 @@ size_t path_smem(int nt, int n_blocks, bool mixed)
     return mixed ? mixed_smem_bytes(nt, n_blocks) : path_smem_bytes(nt, n_blocks, false);  // the larger form
 }
 
-int path_cta(bool mixed) { return mixed ? kCta : kFp64Cta; }
+int path_cta(bool mixed, int nt, int n_blocks, bool poly)
+{
+    return mixed ? mixed_cta(mixed_compact(nt, n_blocks, poly)) : kFp64Cta;
+}
 
 cudaError_t launch_reduce(const double* partials, int64_t n_rows, int R, double* sums, const FinalParams& F,
                           double* result, cudaStream_t s)

@@ -93,7 +93,9 @@ cudaError_t launch_path_mixed(int nt, const MixedParams& M, bool poly, const dou
 void pack_mixed_params(int nt, const PathParams<float>& P, MixedParams& M);
 bool path_tenor_supported(int nt);
 size_t path_smem(int nt, int n_blocks, bool mixed);
-int path_cta(bool mixed);  // paths per CTA of the path kernel (one partial-sum row each)
+// paths per CTA of the Euler path kernel of a run (one partial-sum row each):
+// FP64 64; mixed 128, or 64 with the compact sums (polynomial factors, many dates)
+int path_cta(bool mixed, int nt, int n_blocks, bool poly);
 
 cudaError_t launch_reduce(const double* partials, int64_t n_rows, int R, double* sums, const FinalParams& F,
                           double* result, cudaStream_t s);

@@ -249,7 +249,11 @@ hjm_status hjm_run_static(void* cuda_stream, int32_t n_tenor, double dtau, const
         return static_fail(HJM_ERR_INVALID_ARGUMENT, "%d sampled dates need %d tenors; the grid has %d", B, B + 1,
                            n_tenor);
     const int R = B + 3;
-    const int cta = path_cta(precision == HJM_PRECISION_MIXED);
+    // quadratic factors: the polynomial decomposition's coefficients
+    // sqrt(dt) c_{k,d}, as hjm_run's fill_params
+    double coef[HJM_N_VOL_COEF];
+    const bool poly = fit_quadratic_vols(vol_host, n_tenor, dtau, coef);
+    const int cta = path_cta(precision == HJM_PRECISION_MIXED, n_tenor, B, poly);
     const int64_t n_ctas = (n_paths + cta - 1) / cta;
     if (R > kStaticCols || n_ctas > kStaticCtas)
         return static_fail(HJM_ERR_INVALID_ARGUMENT, "run exceeds the static scratch");
@@ -286,10 +290,6 @@ hjm_status hjm_run_static(void* cuda_stream, int32_t n_tenor, double dtau, const
 
     STATIC_CUDA(cudaMemsetAsync(result, 0, sizeof(double) * kResLen, s));
     FinalParams F;
-    // quadratic factors: the polynomial decomposition's coefficients
-    // sqrt(dt) c_{k,d}, as hjm_run's fill_params
-    double coef[HJM_N_VOL_COEF];
-    const bool poly = fit_quadratic_vols(vol_host, n_tenor, dtau, coef);
     const double sq = std::sqrt(dt);
     if (precision == HJM_PRECISION_MIXED) {
         PathParams<float> P;
