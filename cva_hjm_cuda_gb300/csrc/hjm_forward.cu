@@ -522,12 +522,13 @@ __global__ void __launch_bounds__(kMaxTenor)
 // otherwise; the remainder is a small fraction of the curve), and the FP64
 // running sums of the scalar parts S, U, W stay in registers, so that the
 // shared memory of a CTA (the occupancy limit with 60 dates) shrinks by a third.
-// Occupancy: with polynomial factors the kernel fits 96 registers without
-// spills, 640 threads per SM (5 CTAs of 128, 20 warps); the table step needs
-// more registers (it spills at 96) and keeps 512, and so do the compact sums,
-// whose 64-thread CTAs shared memory bounds first (7 per SM).
+// Occupancy: 512 threads per SM by the registers (<= 128 per thread; 112 with
+// polynomial factors, 4 CTAs of 128).  Capped at 96 registers (5 CTAs, 20
+// warps) the polynomial form does not spill but ran slower (20.8 ms against
+// 20.5 at 4,194,304 paths); the compact sums' 64-thread CTAs are bounded by
+// shared memory first (7 per SM for the netting set).
 template <int NT, bool EXT, bool POLY, bool CMP, int C>
-__global__ void __launch_bounds__(C, (POLY && !CMP ? 640 : 512) / C)
+__global__ void __launch_bounds__(C, 512 / C)
     path_kernel_mixed(const __grid_constant__ MixedParams M, const double* __restrict__ ext,
                       double* __restrict__ partials, float* __restrict__ estore)
 {
@@ -630,9 +631,9 @@ inline bool mixed_compact(int nt, int n_blocks, bool poly)
 // Paths per CTA of the mixed kernel.  With the compact sums shared memory
 // bounds the occupancy (~0.5 KB per path with 60 dates), and 64-thread CTAs
 // pack an SM more finely: 7 of them (14 warps) where 3 of 128 threads fit
-// (12 warps) for the 61-tenor netting set, 8 (16 warps) instead of 4 for a
-// 25y swap on 51 tenors.  Otherwise the registers bound it (5 CTAs of 128
-// threads, 20 warps), whatever the CTA size.
+// (12 warps) for the 61-tenor netting set (36.5 ms from 37.1); a 25y swap on
+// 51 tenors keeps 16 warps either way.  Otherwise the registers bound it,
+// whatever the CTA size.
 constexpr int kMixedCompactCta = 64;
 inline int mixed_cta(bool cmp) { return cmp ? kMixedCompactCta : kCta; }
 
