@@ -702,7 +702,8 @@ def reference_table_run(eng, args, flush) -> dict:
 
 def dropin_run(args) -> dict:
     """The reference's own entry point, calculateExposureMultiGPU (double
-    overload, simulation_gpu.h:12), through the C++ drop-in of the library:
+    overload, simulation_gpu.h:12; the float overload, :14, on the driver's
+    call as well), through the C++ drop-in of the library:
     host arrays in, the 51-point EE out, timed end to end on the host (the
     drop-in's process-wide context is warm after the first call).  On the
     headline market and swap (1,048,576 paths, 10y) and on the reference
@@ -710,7 +711,7 @@ def dropin_run(args) -> dict:
     25y; 1,048,576 paths instead of the driver's default 100,000)."""
     import numpy as np
 
-    from cva_hjm_cuda_gb300.engine import calculate_exposure_gpu
+    from cva_hjm_cuda_gb300.engine import calculate_exposure_gpu, calculate_exposure_gpu_fp32
     from cva_hjm_cuda_gb300.market import Market, Swap
 
     g = json.loads((ROOT / "tests" / "golden" / "ref_driver_own_market.json").read_text())
@@ -735,6 +736,23 @@ def dropin_run(args) -> dict:
         t = statistics.median(times)
         out[label] = {"n_paths": n, "n_steps": steps, "ms_per_call": 1e3 * t, "path_steps_per_s": n * steps / t,
                       "ee_0": float(ee[0])}
+    # the float overload (simulation_gpu.h:14: the library's mixed precision)
+    # on the reference driver's own call, the same paths
+    notional, strike, expiry, acc, spot, drift, vol = cases["reference_driver_25y"]
+    ee32 = np.zeros(51, dtype=np.float32)
+    steps = int(round(expiry / DT))
+    for _ in range(args.warmup):
+        calculate_exposure_gpu_fp32(ee32, notional, strike, expiry, 0.5, acc, spot, drift, vol, 0.0, 1, n, DT)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        calculate_exposure_gpu_fp32(ee32, notional, strike, expiry, 0.5, acc, spot, drift, vol, 0.0, 1, n, DT)
+        times.append(time.perf_counter() - t0)
+    t = statistics.median(times)
+    ee64 = out["reference_driver_25y"]["ee_0"]
+    out["reference_driver_25y_float"] = {"n_paths": n, "n_steps": steps, "ms_per_call": 1e3 * t,
+                                         "path_steps_per_s": n * steps / t, "ee_0": float(ee32[0]),
+                                         "ee_0_rel_diff_vs_double_overload": abs(float(ee32[0]) - ee64) / abs(ee64)}
     return out
 
 

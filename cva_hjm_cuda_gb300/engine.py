@@ -332,3 +332,18 @@ def calculate_exposure_gpu(expected_exposure: np.ndarray, notional: float, K: fl
     a, s, d, v = (_f64(x) for x in (accrual, spot_rates, drift, volatilities))
     lib.hjm_dropin_calculate_exposure_fp64(_dptr(expected_exposure), notional, K, expiry, dtau, _dptr(a), _dptr(s),
                                            _dptr(d), _dptr(v), num_gpus, simN, dt)
+
+
+def calculate_exposure_gpu_fp32(expected_exposure: np.ndarray, notional: float, K: float, expiry: float, dtau: float,
+                                accrual, spot_rates, drift, volatilities, scale: float, num_gpus: int, simN: int,
+                                dt: float) -> None:
+    """The float overload of calculateExposureMultiGPU (simulation_gpu.h:14, the
+    library's mixed precision) through the C++ drop-in; float32 arrays in, the
+    51-point EE written into expected_exposure (float32)."""
+    lib = _lib.load()
+    if expected_exposure.dtype != np.float32 or expected_exposure.size < 51:
+        raise ValueError("expected_exposure must be a float32 array of 51 values")
+    a, s, d, v = (np.ascontiguousarray(x, dtype=np.float32) for x in (accrual, spot_rates, drift, volatilities))
+    fp = lambda x: x.ctypes.data_as(C.POINTER(C.c_float))  # noqa: E731
+    lib.hjm_dropin_calculate_exposure_fp32(fp(expected_exposure), notional, K, expiry, dtau, fp(a), fp(s), fp(d),
+                                           fp(v), num_gpus, simN, dt)
