@@ -105,35 +105,28 @@ struct hjm_ctx {
     bool keep_exposures = false;
 
     // device buffers
-    DevBuf partials, sums, result, estore, sel, hist, ext, ext_raw, wide, scratch, ck_h, ck_a, resp, vresp, eresp,
-        carry;
+    DevBuf partials, sums, result, estore, sel, hist, ext, ext_raw, wide, scratch, ck_h, ck_a, vresp, eresp, carry;
     MemBudget budget;
     hjm_ctx()
     {
         for (DevBuf* b : buffers()) b->budget = &budget;
     }
-    std::array<DevBuf*, 16> buffers()
+    std::array<DevBuf*, 15> buffers()
     {
         return {&partials, &sums, &result, &estore, &sel, &hist, &ext, &ext_raw, &wide, &scratch, &ck_h, &ck_a,
-                &resp, &vresp, &eresp, &carry};
+                &vresp, &eresp, &carry};
     }
-    // the response table in resp holds the run shape of resp_key; resp_used
-    // is recorded after the last kernel that reads it
-    struct RespKey {  // the response table in resp, with the parts' frame coefficients
-        bool valid = false;
-        int nt = 0, stride = 0, B = 0, scheme = 0;
-        double c = 0, dtau = 0;
-        PartsFrame frame = {};
-    } resp_key;
-    struct ErespKey {  // the Euler response form's table in eresp
-        bool valid = false;
+    // the response tables in eresp and vresp hold the run shapes of their
+    // keys; resp_used is recorded after the last kernel that reads either
+    struct ErespKey {  // the response form's table in eresp (Euler or predictor-corrector)
+        bool valid = false, pc = false;
         int nt = 0, stride = 0, B = 0, np = 0, nres = 0;
         double c = 0, dtau = 0;
         std::vector<EulerRespFrame> frames;  // one per window
         std::vector<double> resid;  // sqrt(dt)-scaled, empty without a residual
     } eresp_key;
     struct ErespFirst {  // eresp_first_active_date of the last run shape
-        bool valid = false;
+        bool valid = false, pc = false;
         int nt = 0, stride = 0, B = 0, nres = 0;
         double c = 0;
         int first = 2;
@@ -798,46 +791,36 @@ static void fill_pc(const hjm_ctx* ctx, const RunShape& sh, double dt, const Pat
     Q.gL = (T)(-c * dtau * dtau);
 }
 
-// FP64 valuation with the decomposition (Euler or predictor-corrector): the
-// remainder in impulse responses (its terms on the FP32 pipe, ~12 FP64
-// operations per step for the polynomial parts) when that is cheaper than its
-// convection (one FMA per live tenor and ~17 per step for Euler, two and ~20
-// for the predictor-corrector), summed over the evolved blocks; the response
-// terms count as two FMAs per date still to be sampled.
+// FP64 valuation with a decomposition (quadratic factors under either
+// scheme, or cubic ones with a residual table under the Euler step): the
+// response form of hjm_eresp.cu, whose per-step work is on the FP32 pipe and
+// which takes any number of dates (in windows); measured 9.0x the convected
+// form at 20 dates (Euler), and the convected cubic has no form but the table
+// step, so AUTO always takes it.
 //
-// Volatility-table step (no decomposition): the whole stochastic curve in
-// impulse responses, six FP64 FMAs per date still to be sampled per step,
-// against four FMAs per live tenor (five for the predictor-corrector) and ~10
-// per step.
-//
-// Euler step with a decomposition (quadratic, or cubic with a residual
-// table): the response form of hjm_eresp.cu, whose per-step work is on the
-// FP32 pipe and which takes any number of dates (in windows); measured 9.0x
-// the convected form at 20 dates, and the convected cubic has no form but the
-// table step, so AUTO always takes it.
+// Volatility-table step (no decomposition, at most 24 dates): the whole
+// stochastic curve in impulse responses, six FP64 FMAs per date still to be
+// sampled per step, against four FMAs per live tenor (five for the
+// predictor-corrector) and ~10 per step when convected; AUTO takes the
+// cheaper, summed over the evolved blocks.
 static bool use_response_form(const hjm_ctx* ctx, const RunShape& sh)
 {
     const bool pc = ctx->scheme == HJM_SCHEME_PREDICTOR_CORRECTOR;
-    if (!pc && (use_poly_path(ctx) || use_cubic_path(ctx))) return ctx->remainder != HJM_REMAINDER_CONVECT;
+    if (use_poly_path(ctx) || (!pc && use_cubic_path(ctx))) return ctx->remainder != HJM_REMAINDER_CONVECT;
     if (sh.B > response_max_dates()) return false;
     if (ctx->remainder != HJM_REMAINDER_AUTO) return ctx->remainder == HJM_REMAINDER_RESPONSE;
-    const bool poly = use_poly_path(ctx);
     long conv = 0, resp = 0;
     for (int b = 1; b < sh.B; ++b) {
         const int live = ctx->nt - 1 - b;
-        if (poly) {
-            conv += pc ? 2 * live + 20 : live + 17;
-            resp += 2 * (sh.B - b) + 12;
-        } else {
-            conv += pc ? 5 * live + 12 : 4 * live + 10;
-            resp += 6 * (sh.B - b);
-        }
+        conv += pc ? 5 * live + 12 : 4 * live + 10;
+        resp += 6 * (sh.B - b);
     }
     return resp < conv;
 }
 
 // The volatility-table response table of the run shape, scheme and loadings
-// sv [kFactors][kMaxTenor] (the path parameters'), as ensure_response_table.
+// sv [kFactors][kMaxTenor] (the path parameters'), on the stream: rebuilt
+// only when it changed, after the kernels of earlier valuations that read it.
 static hjm_status ensure_vol_response_table(hjm_ctx* ctx, const RunShape& sh, double dt, const double* sv,
                                             cudaStream_t s)
 {
@@ -871,57 +854,19 @@ static hjm_status ensure_vol_response_table(hjm_ctx* ctx, const RunShape& sh, do
     return HJM_OK;
 }
 
-// The predictor-corrector response table of the run shape, on the stream:
-// recomputed only when it changed, after the kernels of earlier valuations
-// that read it: the sources of fill_pc (wL1 at L-1; wL, gL at L), then the
-// moving-frame coefficients of the scheme's parts step f.
-static hjm_status ensure_response_table(hjm_ctx* ctx, const RunShape& sh, double dt, const PartsFrame& f,
-                                        cudaStream_t s)
-{
-    const double dtau = ctx->dtau;
-    const double c = dt / dtau;
-    const double wL1 = -c * c * dtau * dtau, wL = -(2.0 * c + c * c) * dtau * dtau, gL = -c * dtau * dtau;
-    const double w0 = wL1, w1 = wL - gL, w2 = gL;
-    hjm_ctx::RespKey& k = ctx->resp_key;
-    if (!ctx->resp_used) HJM_CUDA(ctx, cudaEventCreateWithFlags(&ctx->resp_used, cudaEventDisableTiming));
-    if (k.valid && k.nt == ctx->nt && k.stride == sh.stride && k.B == sh.B && k.c == c && k.dtau == dtau &&
-        k.scheme == ctx->scheme && std::memcmp(&k.frame, &f, sizeof(f)) == 0)
-        return HJM_OK;
-    k.valid = false;
-    const size_t bytes = sizeof(float4) * response_table_elems(sh.stride, sh.B);
-    if (bytes > ctx->resp.bytes)
-        HJM_CUDA(ctx, ctx->resp.ensure(bytes));  // cudaFree waits for the device
-    else
-        HJM_CUDA(ctx, cudaStreamWaitEvent(s, ctx->resp_used, 0));
-    HJM_CUDA(ctx, cudaMemsetAsync(ctx->resp.p, 0, bytes, s));  // entries the kernel reads as exact zeros
-    HJM_CUDA(ctx, launch_response_table_pc(ctx->nt, c, sh.stride, sh.B, w0, w1, w2, (float4*)ctx->resp.p, s));
-    HJM_CUDA(ctx, launch_response_active(sh.stride, sh.B, (float4*)ctx->resp.p, s));
-    HJM_CUDA(ctx, launch_state_coefs(f, sh.stride, sh.B, (float4*)ctx->resp.p, s));
-    ctx->stat_launches += 3;
-    std::memcpy(&k.frame, &f, sizeof(f));
-    k.nt = ctx->nt;
-    k.stride = sh.stride;
-    k.B = sh.B;
-    k.c = c;
-    k.dtau = dtau;
-    k.scheme = ctx->scheme;
-    k.valid = true;
-    return HJM_OK;
-}
-
-// The Euler response form's table (remainder and residual responses, frame
+// The response form's table (remainder and residual responses, frame
 // coefficients, active prefixes) for the run shape and decomposition, on the
 // stream: rebuilt only when they changed, after the kernels of earlier
 // valuations that read it.
 static hjm_status ensure_eresp_table(hjm_ctx* ctx, const RunShape& sh, double dt,
                                      const std::vector<EulerRespFrame>& frames, const std::vector<double>& resid,
-                                     int nres, cudaStream_t s)
+                                     int nres, bool pc, cudaStream_t s)
 {
     const EulerRespFrame& fr = frames[0];
     const double c = dt / ctx->dtau;
     hjm_ctx::ErespKey& k = ctx->eresp_key;
     if (!ctx->resp_used) HJM_CUDA(ctx, cudaEventCreateWithFlags(&ctx->resp_used, cudaEventDisableTiming));
-    if (k.valid && k.nt == ctx->nt && k.stride == sh.stride && k.B == sh.B && k.np == fr.np && k.c == c &&
+    if (k.valid && k.pc == pc && k.nt == ctx->nt && k.stride == sh.stride && k.B == sh.B && k.np == fr.np && k.c == c &&
         k.dtau == ctx->dtau && k.nres == nres && k.frames.size() == frames.size() &&
         std::memcmp(k.frames.data(), frames.data(), sizeof(EulerRespFrame) * frames.size()) == 0 && k.resid == resid)
         return HJM_OK;
@@ -932,8 +877,9 @@ static hjm_status ensure_eresp_table(hjm_ctx* ctx, const RunShape& sh, double dt
     else
         HJM_CUDA(ctx, cudaStreamWaitEvent(s, ctx->resp_used, 0));
     HJM_CUDA(ctx, launch_eresp_tables(ctx->nt, c, ctx->dtau, sh.stride, sh.B, frames.data(), (int)frames.size(),
-                                      resid.empty() ? nullptr : resid.data(), nres, (float4*)ctx->eresp.p, s));
+                                      resid.empty() ? nullptr : resid.data(), nres, pc, (float4*)ctx->eresp.p, s));
     ctx->stat_launches += 3;
+    k.pc = pc;
     k.nt = ctx->nt;
     k.stride = sh.stride;
     k.B = sh.B;
@@ -947,13 +893,17 @@ static hjm_status ensure_eresp_table(hjm_ctx* ctx, const RunShape& sh, double dt
     return HJM_OK;
 }
 
-// An FP64 Euler valuation in the response form (hjm_eresp.cu): the parts'
-// frame and loadings of the market's decomposition, the table, the carry of
-// a windowed run, and one launch per window.
+// An FP64 valuation in the response form (hjm_eresp.cu): the parts' frame
+// and loadings of the market's decomposition, the table, the carry of a
+// windowed run, and one launch per window.  Q: the predictor-corrector's
+// parameters (its parts' step, N-projected loadings and deterministic
+// curve; quadratic factors), or null for the Euler step.
 static hjm_status enqueue_eresp(hjm_ctx* ctx, const RunShape& sh, double dt, const PathParams<double>& P,
-                                const double* ext_dev, double* estore, cudaStream_t s)
+                                const double* ext_dev, double* estore, cudaStream_t s,
+                                const PcParams<double>* Q = nullptr)
 {
-    const bool cubic = use_cubic_path(ctx);
+    const bool pc = Q != nullptr;
+    const bool cubic = !pc && use_cubic_path(ctx);
     std::vector<double> resid;
     int nres = 0;
     if (cubic) {
@@ -965,8 +915,10 @@ static hjm_status enqueue_eresp(hjm_ctx* ctx, const RunShape& sh, double dt, con
     // the earliest date the remainder reaches (the windows hold slots from it on)
     const double c = dt / ctx->dtau;
     hjm_ctx::ErespFirst& fa = ctx->eresp_first;
-    if (!(fa.valid && fa.nt == ctx->nt && fa.stride == sh.stride && fa.B == sh.B && fa.nres == nres && fa.c == c)) {
-        fa.first = eresp_first_active_date(ctx->nt, c, sh.stride, sh.B, nres);
+    if (!(fa.valid && fa.pc == pc && fa.nt == ctx->nt && fa.stride == sh.stride && fa.B == sh.B && fa.nres == nres &&
+          fa.c == c)) {
+        fa.first = eresp_first_active_date(ctx->nt, c, sh.stride, sh.B, nres, pc);
+        fa.pc = pc;
         fa.nt = ctx->nt;
         fa.stride = sh.stride;
         fa.B = sh.B;
@@ -978,17 +930,26 @@ static hjm_status enqueue_eresp(hjm_ctx* ctx, const RunShape& sh, double dt, con
     const int n_windows = eresp_windows(sh.B, fa.first, lo, hi, nullptr);
     std::vector<EulerRespFrame> frames(n_windows);
     int degs = 0;
+    double svc_pc[kFactors][3];  // the predictor-corrector's N-projected loadings of 1, T, T^2
+    if (pc)
+        for (int k = 0; k < kFactors; ++k) {
+            svc_pc[k][0] = Q->aS[k];
+            svc_pc[k][1] = Q->aU[k];
+            svc_pc[k][2] = Q->aW[k];
+        }
     for (int w = 0; w < n_windows; ++w)
-        eresp_make_frame(dt, ctx->dtau, ctx->nt, P.svc, cubic ? &ctx->cubic[0][0] : nullptr, ctx->cubic_degs,
-                         eresp_window_centre(ctx->dtau, lo[w], hi[w]), frames[w], degs);
+        eresp_make_frame(dt, ctx->dtau, ctx->nt, pc ? svc_pc : P.svc, cubic ? &ctx->cubic[0][0] : nullptr,
+                         ctx->cubic_degs, eresp_window_centre(ctx->dtau, lo[w], hi[w]), frames[w], degs, pc);
     const EulerRespFrame& fr = frames[0];
     const size_t smem = eresp_max_smem(sh.B, fr.np, sh.stride, fa.first);
     if (smem > 227 * 1024) return fail(ctx, HJM_ERR_UNSUPPORTED, "shared memory %zu B exceeds 227 KB", smem);
-    hjm_status st = ensure_eresp_table(ctx, sh, dt, frames, resid, nres, s);
+    hjm_status st = ensure_eresp_table(ctx, sh, dt, frames, resid, nres, pc, s);
     if (st != HJM_OK) return st;
     EulerRespParams E;
     std::memset(&E, 0, sizeof(E));
     E.P = P;
+    E.wnew_L = pc ? Q->gL : 0.0;
+    E.tenor_L = ctx->nt - 1;
     E.frame = block_frame_n(fr.n, sh.stride);
     E.row = eresp_row(sh.B);
     // the pairs are renormalised for the residual's terms and for runs of more
@@ -1015,7 +976,7 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
     if (st != HJM_OK) return st;
     HJM_CUDA(ctx, cudaSetDevice(ctx->device));
     const bool mixed = precision == HJM_PRECISION_MIXED;
-    const bool windows_ok = ctx->scheme == HJM_SCHEME_EULER && (use_poly_path(ctx) || use_cubic_path(ctx));
+    const bool windows_ok = use_poly_path(ctx) || (ctx->scheme == HJM_SCHEME_EULER && use_cubic_path(ctx));
     if (!mixed && ctx->remainder == HJM_REMAINDER_RESPONSE && sh.B > response_max_dates() && !windows_ok)
         return fail(ctx, HJM_ERR_INVALID_ARGUMENT,
                     "the response form of this market and scheme holds at most %d dates (run has %d)",
@@ -1068,19 +1029,19 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
         fill_pc<double>(ctx, sh, dt, P, Q);
         ctx->stat_h2d = sizeof(Q) + sizeof(FinalParams);
         resp = use_response_form(ctx, sh);
-        if (resp && !use_poly_path(ctx)) {
+        if (resp && use_poly_path(ctx)) {
+            // the decomposition in the response form of hjm_eresp.cu, with the
+            // two-stage step's parts frame and remainder table (any number of dates)
+            st = enqueue_eresp(ctx, sh, dt, Q.P, ext_dev, store ? (double*)ctx->estore.p : nullptr, s, &Q);
+            if (st != HJM_OK) return st;
+        } else if (resp) {
             st = ensure_vol_response_table(ctx, sh, dt, &Q.P.sv[0][0], s);
             if (st != HJM_OK) return st;
             HJM_CUDA(ctx, launch_path_fp64_vresp(ctx->nt, Q.P, (const double2*)ctx->vresp.p, ext_dev,
                                                  (double*)ctx->partials.p, store ? (double*)ctx->estore.p : nullptr,
                                                  s));
         } else {
-            if (resp) {
-                st = ensure_response_table(ctx, sh, dt, pc_parts_frame(Q), s);
-                if (st != HJM_OK) return st;
-            }
-            HJM_CUDA(ctx, launch_path_pc(ctx->nt, Q, use_poly_path(ctx), resp ? (const float4*)ctx->resp.p : nullptr,
-                                         ext_dev, (double*)ctx->partials.p,
+            HJM_CUDA(ctx, launch_path_pc(ctx->nt, Q, use_poly_path(ctx), ext_dev, (double*)ctx->partials.p,
                                          store ? (double*)ctx->estore.p : nullptr, s));
         }
         if (resp) HJM_CUDA(ctx, cudaEventRecord(ctx->resp_used, s));

@@ -352,8 +352,12 @@ __global__ void __launch_bounds__(kFp64Cta, eresp_min_ctas(NS))
                 h = select_reg<NS, float2>(A, hi - i);
                 l = select_reg<NS, float2>(Al, hi - i);
             }
-            const double hc = widen_f32(h.x) + widen_f32(l.x);
-            const double hcs = widen_f32(h.y) + widen_f32(l.y);
+            double hc = widen_f32(h.x) + widen_f32(l.x);
+            double hcs = widen_f32(h.y) + widen_f32(l.y);
+            if (i == E.tenor_L) {  // (the basis-independent W = x[2] after the date's sampling step)
+                hc = fma(E.wnew_L, x[2], hc);
+                hcs = fma(E.wnew_L, x[2], hcs);
+            }
             double px = x[NP - 1], pz = Z[NP - 1];
 #pragma unroll
             for (int c = NP - 2; c >= 0; --c) {
@@ -427,6 +431,63 @@ __global__ void __launch_bounds__(kMaxTenor)
             v += c * (v_s[t + 1] - v);
         else if (t == L)
             v += c * (v - v_s[L - 1]);
+        __syncthreads();
+    }
+}
+
+// The remainder's responses under the predictor-corrector step (no residual:
+// one float4 per slot, laid out as eresp_table_kernel's).  The two-stage
+// step f' = A2 f + N (mu dt + xi) drives the remainder at L - 1 and L by W
+// (the quadratic's boundary terms of A2 T^2 and N T^2): w0 W_old e_{L-1} +
+// w1 W_old e_L + w2 W_new e_L with w0 = -c^2 dtau^2, w1 = wL - gL, w2 = gL
+// (wL = -(2c + c^2) dtau^2, gL = -c dtau^2).  W_new of one step is W_old of
+// the next, so the coefficient of the old W at lag l is H(l) = w0 G1(l) +
+// w1 G2(l) + w2 G2(l + 1), with G1, G2 the responses of A2 to e_{L-1}, e_L
+// (the three-point upwind stencil a0 = 1 - c + c^2/2, a1 = c - c^2,
+// a2 = c^2/2, Euler rows at L - 1 and L), and its running sum likewise from
+// the running sums of G1, G2.  FP64 recursion, thread t holding tenor t.
+__global__ void __launch_bounds__(kMaxTenor)
+    eresp_table_pc_kernel(int nt, double c, int stride, int B, int row, double w0, double w1, double w2,
+                          float4* __restrict__ resp)
+{
+    __shared__ double v_s[kMaxTenor + 2], u_s[kMaxTenor + 2];
+    const int t = threadIdx.x;
+    const int L = nt - 1;
+    const int M = (B - 1) * stride - 1;  // the longest lag read
+    const double a0 = 1.0 - c + 0.5 * c * c, a1 = c - c * c, a2 = 0.5 * c * c;
+    double g1 = (t == L - 1) ? 1.0 : 0.0, g2 = (t == L) ? 1.0 : 0.0;
+    double cg1 = 0.0, cg2 = 0.0, hp = 0.0, chp = 0.0;  // H's first two terms at the previous lag
+    for (int m = 0; m <= M + 1; ++m) {
+        cg1 += g1;
+        cg2 += g2;
+        const int l = m - 1;  // the lag whose entry this iteration completes
+        if (l >= 0 && t >= 2 && t <= B) {
+            const int qd = l / stride + 1;
+            const int b = t - qd;
+            if (b >= 1) {
+                const double g = hp + w2 * g2, cg = chp + w2 * cg2;
+                const float gh = __double2float_rn(g), cgh = __double2float_rn(cg);
+                resp[((size_t)b * stride + (size_t)(qd * stride - 1 - l)) * row + (B - t)] =
+                    make_float4(gh, cgh, __double2float_rn(g - (double)gh), __double2float_rn(cg - (double)cgh));
+            }
+        }
+        hp = w0 * g1 + w1 * g2;
+        chp = w0 * cg1 + w1 * cg2;
+        if (t < nt) {
+            v_s[t] = g1;
+            u_s[t] = g2;
+        }
+        __syncthreads();
+        if (t < L - 1) {
+            g1 = a0 * g1 + a1 * v_s[t + 1] + a2 * v_s[t + 2];
+            g2 = a0 * g2 + a1 * u_s[t + 1] + a2 * u_s[t + 2];
+        } else if (t == L - 1) {
+            g1 += c * (v_s[L] - g1);
+            g2 += c * (u_s[L] - g2);
+        } else if (t == L) {
+            g1 += c * (g1 - v_s[L - 1]);
+            g2 += c * (g2 - u_s[L - 1]);
+        }
         __syncthreads();
     }
 }
@@ -544,8 +605,12 @@ __global__ void eresp_coef_kernel(FrameLoadings f, int np, int stride, float4* _
 // ---------------------------------------------------------------------------
 int eresp_row(int n_blocks) { return (n_blocks + 2 + 3) / 4 * 4; }
 
+// The predictor-corrector's remainder source per unit W and step, w0 + w1 +
+// w2 = -(2c + 2c^2) dtau^2 (the Euler step's kappa = -2 c dtau^2 to first order)
+double eresp_kappa_pc(double c, double dtau) { return -(2.0 * c + 2.0 * c * c) * dtau * dtau; }
+
 void eresp_make_frame(double dt, double dtau, int nt, const double (*svc)[3], const double* cubic,
-                      const int* cubic_degs, double tau0, EulerRespFrame& fr, int& degs)
+                      const int* cubic_degs, double tau0, EulerRespFrame& fr, int& degs, bool pc)
 {
     std::memset(&fr, 0, sizeof(fr));
     const double c = dt / dtau, sq = std::sqrt(dt);
@@ -568,7 +633,7 @@ void eresp_make_frame(double dt, double dtau, int nt, const double (*svc)[3], co
         }
     } else {
         fr.np = 3;
-        fr.n = PartsN{k1, k2, 0.0, 2.0 * k1, 0.0, 0.0};
+        fr.n = PartsN{k1, pc ? (c + c * c) * dtau * dtau : k2, 0.0, 2.0 * k1, 0.0, 0.0};
         fr.sig0 = 0.0;
         // sum_d s_d T^d = s'_0 + s'_1 t + s'_2 t^2 with t = T - tau0
         for (int k = 0; k < kFactors; ++k) {
@@ -611,7 +676,7 @@ size_t eresp_table_elems(int stride, int n_blocks, int np, int nres, int n_frame
 }
 
 static cudaError_t launch_eresp_responses(int nt, double c, double dtau, int stride, int n_blocks, const double* resid,
-                                   int nres, float4* table, cudaStream_t s)
+                                   int nres, bool pc, float4* table, cudaStream_t s)
 {
     if (nt < 3 || nt > kMaxTenor || n_blocks < 1 || n_blocks >= nt || stride < 1) return cudaErrorInvalidValue;
     const int row = eresp_row(n_blocks);
@@ -626,9 +691,18 @@ static cudaError_t launch_eresp_responses(int nt, double c, double dtau, int str
     if (resid)
         for (int k = 0; k < kFactors; ++k)
             for (int t = 0; t < nt; ++t) RL.r[k][t] = resid[k * nt + t];
-    const double kappa = -2.0 * (c * dtau * dtau);
-    // one CTA for the remainder's responses, one per residual factor
-    eresp_table_kernel<<<1 + nres, kMaxTenor, 0, s>>>(nt, c, stride, n_blocks, row, nres, kappa, RL, table);
+    // kappa: the remainder's source per unit W and step, the scale of its
+    // responses (the predictor-corrector's sources at L - 1 and L together)
+    const double kappa = pc ? eresp_kappa_pc(c, dtau) : -2.0 * (c * dtau * dtau);
+    if (pc) {
+        if (nres != 0) return cudaErrorInvalidValue;
+        const double d2 = dtau * dtau;
+        eresp_table_pc_kernel<<<1, kMaxTenor, 0, s>>>(nt, c, stride, n_blocks, row, -c * c * d2, -(c + c * c) * d2,
+                                                      -c * d2, table);
+    } else {
+        // one CTA for the remainder's responses, one per residual factor
+        eresp_table_kernel<<<1 + nres, kMaxTenor, 0, s>>>(nt, c, stride, n_blocks, row, nres, kappa, RL, table);
+    }
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     eresp_active_kernel<<<1, 1024, 0, s>>>((int)rows, row, ent, stride, n_blocks, (float)kappa, table,
@@ -658,10 +732,10 @@ static cudaError_t launch_eresp_frames(int stride, int n_blocks, int nres, const
 }
 
 cudaError_t launch_eresp_tables(int nt, double c, double dtau, int stride, int n_blocks, const EulerRespFrame* frames,
-                                int n_frames, const double* resid, int nres, float4* table, cudaStream_t s)
+                                int n_frames, const double* resid, int nres, bool pc, float4* table, cudaStream_t s)
 {
     if (!resid) nres = 0;
-    const cudaError_t e = launch_eresp_responses(nt, c, dtau, stride, n_blocks, resid, nres, table, s);
+    const cudaError_t e = launch_eresp_responses(nt, c, dtau, stride, n_blocks, resid, nres, pc, table, s);
     if (e != cudaSuccess) return e;
     return launch_eresp_frames(stride, n_blocks, nres, frames, n_frames, table, s);
 }
@@ -708,10 +782,59 @@ cudaError_t launch_window_ext(const EulerRespParams& E, int ns, const float4* ta
 
 }  // namespace
 
-int eresp_first_active_date(int nt, double c, int stride, int n_blocks, int nres)
+// The predictor-corrector's table (eresp_table_pc_kernel) restated in FP64
+// on a unit grid (dtau = 1: every coefficient scales with dtau^2, as kappa).
+static int eresp_first_active_date_pc(int nt, double c, int stride, int n_blocks)
+{
+    const int L = nt - 1, B = n_blocks;
+    const double w0 = -c * c, w1 = -(c + c * c), w2 = -c, kap = std::fabs(eresp_kappa_pc(c, 1.0));
+    const double a0 = 1.0 - c + 0.5 * c * c, a1 = c - c * c, a2 = 0.5 * c * c;
+    double g1[kMaxTenor] = {}, g2[kMaxTenor] = {}, cg1[kMaxTenor] = {}, cg2[kMaxTenor] = {};
+    double hp[kMaxTenor] = {}, chp[kMaxTenor] = {}, n1[kMaxTenor], n2[kMaxTenor];
+    bool sig[kMaxTenor] = {};
+    g1[L - 1] = 1.0;
+    g2[L] = 1.0;
+    const int M = (B - 1) * stride - 1;  // the longest lag in the table
+    for (int m = 0; m <= M + 1; ++m) {
+        for (int t = 0; t <= L; ++t) {
+            cg1[t] += g1[t];
+            cg2[t] += g2[t];
+        }
+        const int l = m - 1;
+        // at half the device's thresholds (2^-53 |kappa|, times t stride for the running sum)
+        if (l >= 0)
+            for (int t = 2; t <= B; ++t)
+                if (!sig[t] && l <= (t - 1) * stride - 1 &&
+                    (std::fabs(hp[t] + w2 * g2[t]) >= 0x1p-54 * kap ||
+                     std::fabs(chp[t] + w2 * cg2[t]) >= 0x1p-54 * kap * (double)t * stride))
+                    sig[t] = true;
+        for (int t = 0; t <= L; ++t) {
+            hp[t] = w0 * g1[t] + w1 * g2[t];
+            chp[t] = w0 * cg1[t] + w1 * cg2[t];
+        }
+        for (int t = 0; t < L - 1; ++t) {
+            n1[t] = a0 * g1[t] + a1 * g1[t + 1] + a2 * g1[t + 2];
+            n2[t] = a0 * g2[t] + a1 * g2[t + 1] + a2 * g2[t + 2];
+        }
+        n1[L - 1] = g1[L - 1] + c * (g1[L] - g1[L - 1]);
+        n2[L - 1] = g2[L - 1] + c * (g2[L] - g2[L - 1]);
+        n1[L] = g1[L] + c * (g1[L] - g1[L - 1]);
+        n2[L] = g2[L] + c * (g2[L] - g2[L - 1]);
+        for (int t = 0; t <= L; ++t) {
+            g1[t] = n1[t];
+            g2[t] = n2[t];
+        }
+    }
+    for (int t = 2; t <= B; ++t)
+        if (sig[t]) return t;
+    return B + 1;
+}
+
+int eresp_first_active_date(int nt, double c, int stride, int n_blocks, int nres, bool pc)
 {
     if (nres > 0) return 2;
     if (nt < 3 || nt > kMaxTenor || n_blocks < 2 || n_blocks >= nt || stride < 1) return 2;
+    if (pc) return eresp_first_active_date_pc(nt, c, stride, n_blocks);
     const int L = nt - 1, B = n_blocks;
     double v[kMaxTenor] = {}, w[kMaxTenor], cum[kMaxTenor] = {};
     bool sig[kMaxTenor] = {};

@@ -19,10 +19,17 @@ namespace hjm {
 // the residual terms, which the low parts accumulate (their running total
 // sets the low parts' rounding unless it is moved into the high parts).
 // Every fourth step keeps the low part within about two ulps of the sum.
+// wnew_L: the predictor-corrector's source at the last tenor per unit of W
+// after the step (gL = -c dtau^2; 0 for Euler).  Its term of a step enters
+// the remainder after the step, so for the one date that samples the last
+// tenor (tenor_L; with nt - 1 dates) the term of its own sampling step has
+// lag -1, outside the table: the kernel adds it when it prices that date.
 struct EulerRespParams {
     PathParams<double> P;
     BlockFrameN frame;
     double tau0;
+    double wnew_L;
+    int tenor_L;
     int win_lo, win_hi;
     int row;
     int renorm;
@@ -48,8 +55,11 @@ struct EulerRespFrame {
 // (coefficients of (T - T_L)^d, unscaled) and their degrees, from the cubic;
 // the polynomials re-expanded in powers of T - tau0 (a Taylor shift in FP64).
 // degs: degs_pack of the factors' degrees.
+// pc: the predictor-corrector's two-stage step on the parts (N's entry
+// n02 = (c + c^2) dtau^2 instead of c dtau^2; svc then holds its N-projected
+// loadings, quadratic only).
 void eresp_make_frame(double dt, double dtau, int nt, const double (*svc)[3], const double* cubic,
-                      const int* cubic_degs, double tau0, EulerRespFrame& fr, int& degs);
+                      const int* cubic_degs, double tau0, EulerRespFrame& fr, int& degs, bool pc = false);
 // The basis centre of a window: the middle of its sampled tenors, where the
 // polynomial's terms cancel least (at T_L the cubic's terms at the early
 // tenors are ~30 times the net loading, and so are their rounding errors).
@@ -62,14 +72,19 @@ size_t eresp_table_elems(int stride, int n_blocks, int np, int nres, int n_frame
 // Build the table on the stream (clears the buffer first).  resid: the
 // residual loadings sqrt(dt) (sigma_k - poly_k) [3][nt], or null; nres as
 // above (with nres = 2 the first factor's residual is left out).
+// pc: the predictor-corrector step's remainder responses (no residual).
 cudaError_t launch_eresp_tables(int nt, double c, double dtau, int stride, int n_blocks, const EulerRespFrame* frames,
-                                int n_frames, const double* resid, int nres, float4* table, cudaStream_t s);
+                                int n_frames, const double* resid, int nres, bool pc, float4* table, cudaStream_t s);
 // The earliest date whose remainder terms the table's active prefixes can
 // ever hold (n_blocks + 1 when none): the host's FP64 restatement of
 // eresp_active_kernel's test at half its thresholds, so that it never
 // misses a date the device counts.  With a residual (nres > 0), 2: the
 // residual loadings reach every tenor.
-int eresp_first_active_date(int nt, double c, int stride, int n_blocks, int nres);
+// pc: the predictor-corrector step's table (eresp_table_pc_kernel).
+int eresp_first_active_date(int nt, double c, int stride, int n_blocks, int nres, bool pc = false);
+// The predictor-corrector's remainder source per unit W and step (the scale
+// of its table's entries, as kappa = -2 c dtau^2 is the Euler step's).
+double eresp_kappa_pc(double c, double dtau);
 // The residual factors a table needs: 0 without a residual, 2 when the first
 // factor's residual is at most 2^-44 of its scale (an exact constant, as the
 // reference table's first factor), else 3.

@@ -246,126 +246,6 @@ __host__ __device__ inline size_t resp_smem_bytes(int n_blocks)
     return ((size_t)n_blocks + 2) * kFp64Cta * 8 + 2 * (kFp64Cta / 32) * 8;
 }
 
-// Impulse responses of the predictor-corrector step at the sampled tenors,
-// for its response form (path_kernel_pc_resp): entry (row b stride + s,
-// column r = B - j) of resp holds, as FP32 pairs {coef hi, sum hi, coef lo,
-// sum lo}, the coefficient of the old W at step s of block b in date j's
-// remainder and in its running sum, at lag l = (j - b) stride - 1 - s (the
-// distance to date j's sampling step), for 1 <= b < j <= B <= kRespDates.
-// Every lag l in [0, (j-1) stride - 1] of date j maps to exactly one entry
-// (q = j - b = l / stride + 1, s = q stride - 1 - l); the rest of the table
-// stays zero.  One CTA of kMaxTenor threads, thread t holding tenor t of the
-// responses.  The remainder is driven at L-1 by w0' W_old and at L by
-// wL W_old + gL gamma, gamma = W_new - W_old; grouping the terms by W, the
-// coefficient of the old W at lag l is H1(l) + H2(l+1) with H1 = w0 G1 + w1 G2
-// (w0 = wL1, w1 = wL - gL) and H2 = w2 G2 (w2 = gL), G1, G2 the responses of
-// A2 (three-point stencil a0, a1, a2; Euler rows at L-1, L) to e_{L-1}, e_L,
-// and the sum likewise with the running sums.  (The Euler step's table is
-// eresp_table_kernel in hjm_eresp.cu.)
-__global__ void __launch_bounds__(kMaxTenor)
-    response_table_kernel(int nt, double c, int stride, int B, double w0, double w1, double w2,
-                          float4* __restrict__ resp)
-{
-    __shared__ double v_s[kMaxTenor], u_s[kMaxTenor];
-    const int t = threadIdx.x;
-    const int L = nt - 1;
-    const int M = (B - 1) * stride - 1;  // the longest lag read
-    auto put = [&](int l, double coef, double sum) {
-        if (t < 2 || t > B) return;
-        const int q = l / stride + 1;
-        const int b = t - q;
-        if (b < 1) return;
-        const float ch = __double2float_rn(coef), sh = __double2float_rn(sum);
-        resp[((size_t)b * stride + (size_t)(q * stride - 1 - l)) * kRespRow + (B - t)] =
-            make_float4(ch, sh, __double2float_rn(coef - (double)ch), __double2float_rn(sum - (double)sh));
-    };
-    const double a0 = 1.0 - c + 0.5 * c * c, a1 = c - c * c, a2 = 0.5 * c * c;
-    double g1 = (t == L - 1) ? 1.0 : 0.0, g2 = (t == L) ? 1.0 : 0.0;
-    double cg1 = 0.0, cg2 = 0.0, h1p = 0.0, ch1p = 0.0;  // H1, CH1 at the previous lag
-    for (int m = 0; m <= M + 1; ++m) {
-        cg1 += g1;
-        cg2 += g2;
-        if (m >= 1) put(m - 1, h1p + w2 * g2, ch1p + w2 * cg2);
-        h1p = w0 * g1 + w1 * g2;
-        ch1p = w0 * cg1 + w1 * cg2;
-        v_s[t] = g1;
-        u_s[t] = g2;
-        __syncthreads();
-        if (t < L - 1) {
-            g1 = a0 * g1 + a1 * v_s[t + 1] + a2 * v_s[t + 2];
-            g2 = a0 * g2 + a1 * u_s[t + 1] + a2 * u_s[t + 2];
-        } else if (t == L - 1) {
-            g1 += c * (v_s[L] - g1);
-            g2 += c * (u_s[L] - g2);
-        } else if (t == L) {
-            g1 += c * (g1 - v_s[L - 1]);
-            g2 += c * (g2 - u_s[L - 1]);
-        }
-        __syncthreads();
-    }
-}
-
-// Per row of the response table (rows * kRespRow entries), the active
-// prefix n_act[row]: the slots up to the last one whose coefficient or
-// running-sum coefficient reaches 2^-70 of the largest of its slot over all
-// rows (slot r is one date, so the largest is that date's largest response).
-// The slots after it hold only terms near the transport front, where the
-// response is vanishingly small (at most ~1e3 terms, each below 2^-70 of the
-// date's largest coefficient, times W); the kernels skip them.  Zero slots
-// never count.  n_act[rows] = 0 (read ahead by the kernels).  One CTA.
-__global__ void __launch_bounds__(1024) response_active_kernel(int rows, const float4* __restrict__ resp,
-                                                               int* __restrict__ n_act)
-{
-    __shared__ unsigned int mc[kRespRow], ms[kRespRow];
-    if (threadIdx.x < kRespRow) mc[threadIdx.x] = ms[threadIdx.x] = 0u;
-    __syncthreads();
-    const int64_t total = (int64_t)rows * kRespRow;
-    for (int64_t i = threadIdx.x; i < total; i += blockDim.x) {
-        const float4 e = resp[i];
-        const int r = (int)(i % kRespRow);
-        atomicMax(&mc[r], __float_as_uint(fabsf(e.x)));  // non-negative floats order as their bits
-        atomicMax(&ms[r], __float_as_uint(fabsf(e.y)));
-    }
-    __syncthreads();
-    for (int row = threadIdx.x; row <= rows; row += blockDim.x) {
-        int n = 0;
-        if (row < rows)
-            for (int r = 0; r < kRespRow; ++r) {
-                const float4 e = resp[(size_t)row * kRespRow + r];
-                const float tc = __uint_as_float(mc[r]) * 0x1p-70f, ts = __uint_as_float(ms[r]) * 0x1p-70f;
-                if ((e.x != 0.0f && fabsf(e.x) >= tc) || (e.y != 0.0f && fabsf(e.y) >= ts)) n = r + 1;
-            }
-        n_act[row] = n;
-    }
-}
-
-// The moving-frame coefficients of the response forms' parts (the frame,
-// M^-k and Q(a) are stated with kStateRow): row s < stride (the step within a
-// block), entry 3 c + k = {C hi, G hi, C lo, G lo} of C(s) = M^-(s+1) B and
-// G(s) = Q(s) C(s); FP64, each split into the nearest float and the float
-// nearest the rest.
-__global__ void state_coef_kernel(PartsFrame f, int stride, float4* __restrict__ coef)
-{
-    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (int64_t)stride * kStateRow) return;
-    const int64_t m = idx / kStateRow;
-    const int c = (int)(idx % kStateRow) / 3, k = (int)(idx % kStateRow) % 3;
-    const double kk = (double)(m + 1), q = (double)m, nn = f.n01 * f.n12;
-    const double minv[3][3] = {{1.0, -kk * f.n01, -kk * f.n02 + 0.5 * kk * (kk + 1.0) * nn},
-                               {0.0, 1.0, -kk * f.n12},
-                               {0.0, 0.0, 1.0}};
-    const double h = 0.5 * q * (q + 1.0);
-    const double Q[3][3] = {{q, h * f.n01, h * f.n02 + (q + 1.0) * q * (q - 1.0) / 6.0 * nn},
-                            {0.0, q, h * f.n12},
-                            {0.0, 0.0, q}};
-    double C[3];  // column k of C(m)
-    for (int r = 0; r < 3; ++r) C[r] = minv[r][0] * f.bm[0][k] + minv[r][1] * f.bm[1][k] + minv[r][2] * f.bm[2][k];
-    const double cv = C[c], gv = Q[c][0] * C[0] + Q[c][1] * C[1] + Q[c][2] * C[2];
-    const float ch = __double2float_rn(cv), gh = __double2float_rn(gv);
-    coef[(size_t)m * kStateRow + 3 * c + k] =
-        make_float4(ch, gh, __double2float_rn(cv - (double)ch), __double2float_rn(gv - (double)gh));
-}
-
 // Response form of the volatility-table step (FP64, any factor shapes, at most
 // kRespDates dates, both time schemes).  Without a polynomial part the whole
 // stochastic curve is driven by the injected noise: h_n = A h_{n-1} + S phi_n
@@ -1039,38 +919,6 @@ cudaError_t launch_response_table_vol(int nt, double c, int stride, int n_blocks
 }
 
 int response_max_dates() { return kRespDates; }
-
-size_t response_table_elems(int stride, int n_blocks)
-{
-    const size_t rows = (size_t)n_blocks * stride;
-    return resp_nact_offset(stride, n_blocks) + (rows + 4) / 4;  // the active counts (and one more), 4 ints per entry
-}
-
-cudaError_t launch_response_active(int stride, int n_blocks, float4* resp, cudaStream_t s)
-{
-    if (n_blocks < 1 || n_blocks > kRespDates || stride < 1) return cudaErrorInvalidValue;
-    response_active_kernel<<<1, 1024, 0, s>>>(n_blocks * stride, resp,
-                                             reinterpret_cast<int*>(resp + resp_nact_offset(stride, n_blocks)));
-    return cudaGetLastError();
-}
-
-cudaError_t launch_state_coefs(const PartsFrame& f, int stride, int n_blocks, float4* resp, cudaStream_t s)
-{
-    if (n_blocks < 2 || n_blocks > kRespDates || stride < 1) return cudaErrorInvalidValue;
-    const int64_t total = (int64_t)stride * kStateRow;
-    const int threads = 256;
-    state_coef_kernel<<<(unsigned)((total + threads - 1) / threads), threads, 0, s>>>(
-        f, stride, resp + resp_coef_offset(stride, n_blocks));
-    return cudaGetLastError();
-}
-
-cudaError_t launch_response_table_pc(int nt, double c, int stride, int n_blocks, double w0, double w1, double w2,
-                                     float4* resp, cudaStream_t s)
-{
-    if (nt < 3 || nt > kMaxTenor || n_blocks > kRespDates || n_blocks >= nt || stride < 1) return cudaErrorInvalidValue;
-    response_table_kernel<<<1, kMaxTenor, 0, s>>>(nt, c, stride, n_blocks, w0, w1, w2, resp);
-    return cudaGetLastError();
-}
 
 template <int NT, bool EXT, bool POLY>
 static cudaError_t launch_mixed_t(const MixedParams& M, const double* ext, double* partials, float* estore,

@@ -69,25 +69,6 @@ cudaError_t launch_path_fp64_vresp(int nt, const PathParams<double>& P, const do
 size_t response_table_vol_elems(int stride, int n_blocks);  // double2 entries
 cudaError_t launch_response_table_vol(int nt, double c, int stride, int n_blocks, bool pc, const double* sv,
                                       double2* vresp, cudaStream_t s);
-size_t response_table_elems(int stride, int n_blocks);  // float4 entries: responses, coefficients, prefixes
-// The predictor-corrector response form's table: w0 = wL1, w1 = wL - gL,
-// w2 = gL (PcParams)
-cudaError_t launch_response_table_pc(int nt, double c, int stride, int n_blocks, double w0, double w1, double w2,
-                                     float4* resp, cudaStream_t s);
-// The active prefix of each row of the response table in resp (after the
-// table and the coefficient rows), from the table's values
-cudaError_t launch_response_active(int stride, int n_blocks, float4* resp, cudaStream_t s);
-// The moving frame of the response forms' polynomial parts: the step
-// x <- M x + B phi on x = (S, U, W), M = I + N with N's entries n01 (S from
-// U), n02 (S from W), n12 (U from W), and bm[c][k] = B, the loading of part c
-// on factor k.
-struct PartsFrame {
-    double n01, n02, n12;
-    double bm[3][3];
-};
-// Its coefficients (one block's rows), into the rows after the response
-// table in resp (whose size response_table_elems counts)
-cudaError_t launch_state_coefs(const PartsFrame& f, int stride, int n_blocks, float4* resp, cudaStream_t s);
 cudaError_t launch_path_mixed(int nt, const MixedParams& M, bool poly, const double* ext, double* partials,
                               float* estore, cudaStream_t s);
 void pack_mixed_params(int nt, const PathParams<float>& P, MixedParams& M);
@@ -130,24 +111,10 @@ struct PcParams {
     T wL1, wL, gL;         // sources: -c^2 dtau^2 W at L-1; -(2c + c^2) dtau^2 W - c dtau^2 gamma at L
 };
 
-// The frame of the predictor-corrector's polynomial step on (S, U, W)
-inline PartsFrame pc_parts_frame(const PcParams<double>& Q)
-{
-    PartsFrame f{};
-    f.n01 = Q.k1;
-    f.n02 = Q.k2p;
-    f.n12 = Q.k1x2;
-    for (int k = 0; k < kFactors; ++k) {
-        f.bm[0][k] = Q.aS[k];
-        f.bm[1][k] = Q.aU[k];
-        f.bm[2][k] = Q.aW[k];
-    }
-    return f;
-}
-// resp (FP64 only): the predictor-corrector response table (the response
-// form, polynomial volatility, at most response_max_dates() dates) or null
-cudaError_t launch_path_pc(int nt, const PcParams<double>& Q, bool poly, const float4* resp, const double* ext,
-                           double* partials, double* estore, cudaStream_t s);
+// The predictor-corrector's convected kernels (the FP64 response form of its
+// decomposition runs in hjm_eresp.cu)
+cudaError_t launch_path_pc(int nt, const PcParams<double>& Q, bool poly, const double* ext, double* partials,
+                           double* estore, cudaStream_t s);
 cudaError_t launch_path_pc(int nt, const PcParams<float>& Q, bool poly, const double* ext, double* partials,
                            float* estore, cudaStream_t s);
 size_t pc_smem(int nt, int n_blocks, bool mixed);

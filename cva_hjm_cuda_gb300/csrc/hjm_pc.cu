@@ -155,134 +155,6 @@ __global__ void __launch_bounds__(kPcCta, 4)
     }
 }
 
-// Response form of the FP64 predictor-corrector path (polynomial volatility,
-// at most kRespDates dates), as path_kernel_fp64_resp in hjm_forward.cu: the
-// polynomial parts, whose step with the N-projected loadings is
-//     S' = S + c dtau U + (c + c^2) dtau^2 W + aS.phi,  U' = U + 2 c dtau W + aU.phi,
-//     W' = W + aW.phi   (old values on the right),
-// as double-FP32 sums in the block's moving frame of that step (frame_step,
-// frame_block_end in hjm_resp.cuh), and the remainder, driven at L-1 and L by W and by the step's curvature
-// noise, as double-FP32 sums of the predictor-corrector response table (the
-// coefficient of the old W per date slot and lag; response_table_kernel with
-// pc = 1) over the active prefix of slots.  TRI: factor k of degree <= k
-// (aU[0] = aW[0] = aW[1] = 0).
-template <int NT, bool EXT, bool TRI, bool SC>
-__global__ void __launch_bounds__(kPcCta, 6)
-    path_kernel_pc_resp(const __grid_constant__ PcParams<double> Q, const float4* __restrict__ resp,
-                        const double* __restrict__ ext, double* __restrict__ partials, double* __restrict__ estore)
-{
-    const PathParams<double>& P = Q.P;
-    extern __shared__ __align__(128) unsigned char smem[];
-    const int tid = threadIdx.x;
-    const int B = P.n_blocks;
-    double* cf_s = reinterpret_cast<double*>(smem);  // [B+2][kPcCta]; exposures alias it one row up
-    double* red_s = cf_s + (size_t)(B + 2) * kPcCta;
-
-    const int64_t cta_base = (int64_t)blockIdx.x * kPcCta;
-    const int64_t lp = cta_base + tid;
-    const bool active = lp < P.n_paths;
-    const uint64_t gpath = P.path_offset + (uint64_t)lp;
-
-    float2 A[kRespSlots], Al[kRespSlots];  // {remainder at tenor j, its running sum}, slot B - j, hi + lo
-#pragma unroll
-    for (int r = 0; r < kRespSlots; ++r) A[r] = Al[r] = make_float2(0.0f, 0.0f);
-    // the parts S, U, W in the block's moving frame, {y_c, v_c} as hi + lo
-    // pairs, and their FP64 running sums between blocks (shared memory)
-    float2 Y[3], Yl[3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) Y[c] = Yl[c] = make_float2(0.0f, 0.0f);
-    double* z_s = red_s + 2 * (kPcCta / 32);
-#pragma unroll
-    for (int c = 0; c < 3; ++c) z_s[c * kPcCta + tid] = 0.0;
-    const BlockFrame F(Q.k1, Q.k2p, Q.k1x2, (double)P.stride);  // the two-stage step on a quadratic
-    // the frame's coefficient rows (one block's), staged in shared memory for SC
-    const float4* coef = resp + resp_coef_offset(P.stride, B);
-    if constexpr (SC) {
-        float4* c_s = reinterpret_cast<float4*>(z_s + 3 * kPcCta);
-        for (int i = tid; i < P.stride * kStateRow; i += kPcCta) c_s[i] = coef[i];
-        __syncthreads();
-        coef = c_s;
-    }
-    // the active prefix of each row, after the table's response and coefficient rows
-    const int* nact = reinterpret_cast<const int*>(resp + resp_nact_offset(P.stride, B));
-
-    auto sample = [&](int i) {
-        const double tau = P.tau[i];
-        const float2 h = select_reg<kRespSlots, float2>(A, B - i), l = select_reg<kRespSlots, float2>(Al, B - i);
-        const double hc = widen_f32(h.x) + widen_f32(l.x), hcs = widen_f32(h.y) + widen_f32(l.y);
-        double S = 0.0, U = 0.0, W = 0.0, ZS = 0.0, ZU = 0.0, ZW = 0.0;
-        if (i >= 2) frame_block_end(Y, Yl, F, z_s + tid, kPcCta, S, U, W, ZS, ZU, ZW);
-        const double x = P.psamp[i] + (fma(tau, fma(tau, W, U), S) + hc);
-        const double acc = fma(tau, fma(tau, ZW, ZU), ZS) + hcs;
-        const double D = exp(-(P.psum[i] + acc) * P.dt);
-        const double Lb = P.m * (exp(x * P.inv_m) - 1.0);
-        cf_s[i * kPcCta + tid] = D * (P.payA[i] * Lb - P.payB[i]);
-    };
-
-    sample(1);
-    for (int b = 1; b < B; ++b) {
-        const float4* row = resp + (size_t)b * P.stride * kRespRow;
-        for (int s = 0; s < P.stride; ++s) {
-            const int n = b * P.stride + s;
-            float ph[3], pl[3];  // the normals as hi + lo (lo = 0 for the generator's FP32 draws)
-            if constexpr (EXT) {
-                double d0, d1, d2;
-                draw_phi<double, true>(ext, gpath, active ? lp : 0, P.n_paths, n, P.rk0, P.rk1, d0, d1, d2);
-                split_f64(d0, ph[0], pl[0]);
-                split_f64(d1, ph[1], pl[1]);
-                split_f64(d2, ph[2], pl[2]);
-            } else {
-                draw_phi<float, false>(ext, gpath, lp, P.n_paths, n, P.rk0, P.rk1, ph[0], ph[1], ph[2]);
-            }
-            const int n_act = __ldg(nact + n);  // uniform: the row's active prefix
-            const float4* rr = row + (size_t)s * kRespRow;
-            // the remainder's sources read W before this step's update
-            const float2 wh2 = make_float2(Y[2].x, Y[2].x), wl2 = make_float2(Yl[2].x, Yl[2].x);
-            const float2 nwh2 = make_float2(-Y[2].x, -Y[2].x);
-            resp_groups(n_act, [&](auto gc) {
-                constexpr int G = decltype(gc)::value;
-                float4 k[4];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) k[u] = __ldg(rr + 4 * G + u);
-#pragma unroll
-                for (int u = 0; u < 4; ++u)
-                    df_acc(A[4 * G + u], Al[4 * G + u], make_float2(k[u].x, k[u].y), make_float2(k[u].z, k[u].w),
-                           wh2, wl2, nwh2);
-            });
-            frame_step<EXT, TRI, SC>(Y, Yl, coef + (size_t)s * kStateRow, ph, pl);
-        }
-        sample(b + 1);
-    }
-    fp64_epilogue<kPcCta>(P, cf_s, cf_s + kPcCta, red_s, partials, estore, cta_base, active);
-}
-
-template <int NT, bool EXT, bool TRI>
-static cudaError_t launch_pc_resp_t(const PcParams<double>& Q, const float4* resp, const double* ext,
-                                    double* partials, double* estore, cudaStream_t s)
-{
-    // cf_s [B+2][kCta], red_s, the parts' running sums [3][kCta], the frame's coefficients
-    const bool sc = Q.P.stride <= kFrameSmemRows;
-    const size_t smem = ((size_t)Q.P.n_blocks + 2) * kPcCta * 8 + 2 * (kPcCta / 32) * 8 + 3 * kPcCta * 8 +
-                        (sc ? (size_t)Q.P.stride * kStateRow * 16 : 0);
-    auto k = sc ? path_kernel_pc_resp<NT, EXT, TRI, true> : path_kernel_pc_resp<NT, EXT, TRI, false>;
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    const int64_t grid = (Q.P.n_paths + kPcCta - 1) / kPcCta;
-    k<<<(unsigned)grid, kPcCta, smem, s>>>(Q, resp, ext, partials, estore);
-    return cudaGetLastError();
-}
-
-template <int NT>
-static cudaError_t launch_pc_resp_nt(const PcParams<double>& Q, const float4* resp, const double* ext,
-                                     double* partials, double* estore, cudaStream_t s)
-{
-    const bool tri = Q.aU[0] == 0.0 && Q.aW[0] == 0.0 && Q.aW[1] == 0.0;
-    if (ext) return tri ? launch_pc_resp_t<NT, true, true>(Q, resp, ext, partials, estore, s)
-                        : launch_pc_resp_t<NT, true, false>(Q, resp, ext, partials, estore, s);
-    return tri ? launch_pc_resp_t<NT, false, true>(Q, resp, ext, partials, estore, s)
-               : launch_pc_resp_t<NT, false, false>(Q, resp, ext, partials, estore, s);
-}
-
 template <int NT, typename T, bool EXT, bool POLY>
 static cudaError_t launch_pc_t(const PcParams<T>& Q, const double* ext, double* partials, T* estore, cudaStream_t s)
 {
@@ -314,15 +186,9 @@ static cudaError_t launch_pc_any(int nt, const PcParams<T>& Q, bool poly, const 
     return cudaErrorInvalidValue;
 }
 
-cudaError_t launch_path_pc(int nt, const PcParams<double>& Q, bool poly, const float4* resp, const double* ext,
-                           double* partials, double* estore, cudaStream_t s)
+cudaError_t launch_path_pc(int nt, const PcParams<double>& Q, bool poly, const double* ext, double* partials,
+                           double* estore, cudaStream_t s)
 {
-    if (resp) {
-        if (!poly || Q.P.n_blocks > kRespDates) return cudaErrorInvalidValue;
-        if (nt == 51) return launch_pc_resp_nt<51>(Q, resp, ext, partials, estore, s);
-        if (nt == 61) return launch_pc_resp_nt<61>(Q, resp, ext, partials, estore, s);
-        return cudaErrorInvalidValue;
-    }
     return launch_pc_any<double>(nt, Q, poly, ext, partials, estore, s);
 }
 

@@ -1,9 +1,10 @@
-// hjm_resp.cuh -- the response form of the polynomial decomposition's remainder.
+// hjm_resp.cuh -- device helpers of the FP64 response forms.
 //
-// The impulse-response table layout, the active prefix of date slots per
-// step, the fall-through dispatch over groups of four slots and the
-// double-FP32 helpers of the FP64 response form (path_kernel_fp64_resp in
-// hjm_forward.cu).
+// The date-slot dispatch (groups of four slots, Duff's device), the
+// double-FP32 helpers and the polynomial parts' moving frame shared by the
+// Euler and predictor-corrector response form (path_kernel_fp64_eresp in
+// hjm_eresp.cu), and the slot constants of the volatility-table response form
+// (path_kernel_fp64_vresp in hjm_forward.cu).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -15,49 +16,44 @@
 
 namespace hjm {
 
-// Response form (polynomial volatility, at most kRespDates sampled dates).  The remainder hc of the polynomial decomposition starts at
-// zero, is driven only at the last tenor, by kappa W_{n-1} at step n (kappa =
-// -2 c dtau^2, W before the step's update), and is otherwise convected by A.
-// So after step K its value at tenor j and its running sum are
-//     hc_K[j]               = sum_{n<=K} G_j(K - n)  kappa W_{n-1},  G_j(m) = (A^m e_L)[j],
-//     sum_{K'<=K} hc_K'[j]  = sum_{n<=K} CG_j(K - n) kappa W_{n-1},  CG_j(m) = sum_{r<=m} G_j(r),
-// exact in exact arithmetic.  The pricing reads hc only at tenor j at date
-// j's sampling step K_j = j stride - 1 (its value and, for the discount, its
-// running sum), so the kernel keeps those two numbers per date still to be
-// sampled and adds one term to each per step: 2 (B - b) FMAs in block b, in
-// place of the convection of every live tenor and the block-end discount
-// recovery.  G_j(m) vanishes for m < L - j (the remainder's support reaches
-// one tenor further down per step), so a date takes no term while its lag is
-// that short.
+// Response form.  The remainder hc of the polynomial decomposition starts at
+// zero, is driven only at the last tenor (Euler: by kappa W_{n-1} at step n,
+// kappa = -2 c dtau^2, W before the step's update; the predictor-corrector
+// step drives it at L - 1 and L by W before and after the step) and is
+// otherwise convected by the scheme's A.  So after step K its value at tenor
+// j and its running sum are fixed linear functionals of the W history,
+//     hc_K[j]               = sum_{n<=K} H_j(K - n)  W_{n-1},
+//     sum_{K'<=K} hc_K'[j]  = sum_{n<=K} CH_j(K - n) W_{n-1},
+// (Euler: H_j(m) = kappa (A^m e_L)[j]), exact in exact arithmetic.  The
+// pricing reads hc only at tenor j at date j's sampling step K_j = j stride
+// - 1 (its value and, for the discount, its running sum), so the kernel keeps
+// those two numbers per date still to be sampled and adds one term to each
+// per step, in place of the convection of every live tenor and the block-end
+// discount recovery.  H_j(m) vanishes while the lag m is too short for the
+// transport from the last tenor to reach tenor j (one tenor per step under
+// Euler, two under the predictor-corrector's stencil).
 //
 // Both sums are carried in double-FP32 arithmetic on the FP32 pipe (76 times
 // the FP64 pipe's rate on GB300): the table holds each coefficient as a pair
-// of floats hi + lo (48 significant bits), W comes as W_hi + W_lo (the Euler
-// kernel's own double-FP32 accumulator of W; the predictor-corrector kernel
-// splits its FP64 W with integer operations), the product's leading term is
-// made exact by an FMA and the accumulation by Knuth's two-sum, packed
-// {value, running sum} in FP32x2 instructions.  The relative error of a
-// date's sum stays below ~1e-12 of its magnitude (checked against FP64 sums
-// of the same terms), and the remainder at a sampled tenor is small: |hc| <=
-// 7e-5 for 24 dates, the most this form takes, against a curve of ~0.03 (the
-// far tail of the transport from the last tenor; below 1e-6 for the 10y swap
-// on 51 tenors), so its rounding stays within an ulp of the FP64 curve.
+// of floats hi + lo (48 significant bits), W is the parts' own double-FP32
+// accumulator, the product's leading term is made exact by an FMA and the
+// accumulation by Knuth's two-sum (df_acc), packed {value, running sum} in
+// FP32x2 instructions.  The relative error of a date's sum stays below ~1e-12
+// of its magnitude (checked against FP64 sums of the same terms), and the
+// remainder at a sampled tenor is a small part of the curve (the far tail of
+// the transport from the last tenor), so its rounding stays within an ulp of
+// the FP64 curve.
 //
-// The accumulators of date j sit in slot r = B - j.  At step s of block b the
-// dates with a nonzero term are j = b + q for q_min <= q <= B - b, q_min the
-// least q whose lag q stride - 1 - s reaches the date's tenor (Euler: one
-// tenor per step from L, lag >= L - j; predictor-corrector: the stencil
-// reaches two tenors per step, 2 lag >= L - 2 - j): slots 0 .. n_act - 1, a
-// prefix.  The kernels read each row's prefix from the table
-// (response_active_kernel), which also drops the trailing slots whose terms
-// are vanishingly small.  A switch on the number of groups of four slots
-// covering it enters a fall-through chain of groups (Duff's device): the
-// skipped groups issue nothing (a predicated loop would issue them all), and
-// the four terms of a group form one basic block, their loads in flight
+// The accumulators of date j sit in slot r = B - j (of the window).  At step
+// s of block b the dates with a term that counts form a prefix of the slots,
+// n_act of them, which the kernels read per row from the table (its active
+// prefix, eresp_active_kernel).  A switch on the number of groups of four
+// slots covering it enters a fall-through chain of groups (Duff's device):
+// the skipped groups issue nothing (a predicated loop would issue them all),
+// and the four terms of a group form one basic block, their loads in flight
 // together and their FP32 chains interleaved.  The table is zero outside the
 // live nonzero entries, so the slots a group adds beyond n_act add exact
-// zeros (dead or not yet reached dates).  The impulse responses come from
-// response_table_kernel.
+// zeros (dead or not yet reached dates).
 constexpr int kRespDates = 24;   // dates the response form holds (slots 0 .. 22 for dates 2 .. B)
 constexpr int kRespSlots = 24;   // accumulator slots, a multiple of the group of 4 (slot 23 stays zero)
 constexpr int kRespRow = 24;     // response-table row: one float4 per slot
@@ -165,101 +161,16 @@ __device__ __forceinline__ void df_renorm(float2& A, float2& Al)
 // double-FP32 on the FP32 pipe, and renormalise the pairs (df_renorm); at
 // each block's end (a sampling date) they widen them, form x_end, add the
 // block's sum to the running sums Z in FP64, and re-anchor y on x_end
-// (rounded to FP32 pairs) with v = 0 (frame_block_end).  The coefficients
+// (rounded to FP32 pairs) with v = 0.  The coefficients
 // are the same in every block: row s (< stride) of the coefficient table
 // holds kStateRow float4 {C hi, G hi, C lo, G lo}, entry 3 c + k for part c
-// and factor k (state_coef_kernel).  W = y_W in every frame, so the
+// and factor k (eresp_coef_kernel; frame_step_n, frame_block_end_n below
+// generalise the step to cubic parts).  W = y_W in every frame, so the
 // remainder's source reads its accumulator directly.  The rounding: 2^-48 of
 // the accumulator per double-FP32 addition over one block's ~150 additions
 // (~5e-14 of the parts' terms), the rest FP64.
 constexpr int kStateRow = 9;
 constexpr int kFrameSmemRows = 112;  // rows staged in shared memory (15.75 KB per CTA at most)
-
-// M^a and Q(a) of a block of a steps (uniform across the CTA).
-struct BlockFrame {
-    double a, m01, m02, m12, q01, q02, q12;
-    __device__ BlockFrame(double n01, double n02, double n12, double steps)
-    {
-        a = steps;
-        const double ha = 0.5 * a * (a + 1.0), nn = n01 * n12;
-        m01 = a * n01;
-        m02 = fma(0.5 * a * (a - 1.0), nn, a * n02);
-        m12 = a * n12;
-        q01 = ha * n01;
-        q02 = fma((a + 1.0) * a * (a - 1.0) / 6.0, nn, ha * n02);
-        q12 = ha * n12;
-    }
-};
-
-// One step of the parts: y += C(s) phi, v += G(s) phi from the coefficient
-// row cr (in shared memory for SHARED, else read through L1), then the pairs
-// renormalised.  ph, pl: the normals as hi + lo (pl unused for FP32 draws,
-// EXT = false).
-template <bool EXT, bool TRI, bool SHARED = false>
-__device__ __forceinline__ void frame_step(float2 (&Y)[3], float2 (&Yl)[3], const float4* __restrict__ cr,
-                                           const float (&ph)[3], const float (&pl)[3])
-{
-    float4 q[kStateRow];
-#pragma unroll
-    for (int t = 0; t < kStateRow; ++t)
-        if (!TRI || t / 3 <= t % 3) {
-            if constexpr (SHARED)
-                q[t] = cr[t];
-            else
-                q[t] = __ldg(cr + t);
-        }
-#pragma unroll
-    for (int t = 0; t < kStateRow; ++t) {
-        const int c = t / 3, k = t % 3;
-        if (TRI && c > k) continue;
-        const float2 kh = make_float2(q[t].x, q[t].y), kl = make_float2(q[t].z, q[t].w);
-        if constexpr (EXT)
-            df_acc(Y[c], Yl[c], kh, kl, make_float2(ph[k], ph[k]), make_float2(pl[k], pl[k]),
-                   make_float2(-ph[k], -ph[k]));
-        else
-            df_acc_w(Y[c], Yl[c], kh, kl, make_float2(ph[k], ph[k]), make_float2(-ph[k], -ph[k]));
-        if (k == 2) df_renorm(Y[c], Yl[c]);  // the part's last term of the step
-    }
-}
-
-// The end of a block: x = M^a y (S, U, W out), Z += Q(a) y - v (z[c *
-// stride_z] in shared memory, out as ZS, ZU, ZW), then y re-anchored on x.
-__device__ __forceinline__ void frame_block_end(float2 (&Y)[3], float2 (&Yl)[3], const BlockFrame& F, double* z,
-                                                int stride_z, double& S, double& U, double& W, double& ZS,
-                                                double& ZU, double& ZW)
-{
-    double y[3], v[3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        y[c] = (double)Y[c].x + (double)Yl[c].x;
-        v[c] = (double)Y[c].y + (double)Yl[c].y;
-    }
-    W = y[2];
-    U = fma(F.m12, y[2], y[1]);
-    S = fma(F.m01, y[1], fma(F.m02, y[2], y[0]));
-    ZW = z[2 * stride_z] + fma(F.a, y[2], -v[2]);
-    ZU = z[stride_z] + fma(F.a, y[1], fma(F.q12, y[2], -v[1]));
-    ZS = z[0] + fma(F.a, y[0], fma(F.q01, y[1], fma(F.q02, y[2], -v[0])));
-    z[0] = ZS;
-    z[stride_z] = ZU;
-    z[2 * stride_z] = ZW;
-    const double x3[3] = {S, U, W};
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        const float xh = __double2float_rn(x3[c]);
-        Y[c] = make_float2(xh, 0.0f);
-        Yl[c] = make_float2(__double2float_rn(x3[c] - (double)xh), 0.0f);
-    }
-}
-
-// Offsets (in float4) within the Euler or predictor-corrector response
-// table buffer: the response rows [B stride][kRespRow], the coefficient rows
-// [stride][kStateRow], the active prefixes [B stride + 1] (int).
-__host__ __device__ inline size_t resp_coef_offset(int stride, int B) { return (size_t)B * stride * kRespRow; }
-__host__ __device__ inline size_t resp_nact_offset(int stride, int B)
-{
-    return (size_t)B * stride * kRespRow + (size_t)stride * kStateRow;
-}
 
 // fn(std::integral_constant<int, G>) for the groups G = ceil(n_act/4) - 1 .. 0
 // of four slots each, by a switch that enters a fall-through chain (Duff's

@@ -326,7 +326,7 @@ hjm_status hjm_run_static(void* cuda_stream, int32_t n_tenor, double dtau, const
             for (int i = 0; i < HJM_N_FACTOR * n_tenor; ++i) resid[i] *= sq;
             float4* table = reinterpret_cast<float4*>(resp_table);
             STATIC_CUDA(launch_eresp_tables(n_tenor, dt / dtau, dtau, (int)stride, B, &fr, 1, cub ? resid : nullptr, nres,
-                                            table, s));
+                                            false, table, s));
             EulerRespParams E;
             std::memset(&E, 0, sizeof(E));
             E.P = P;

@@ -239,8 +239,10 @@ def test_pc_response_form_vs_convected_and_oracle(pc, case, general):
 
 
 @pytest.mark.parametrize("nt,n_paths,n_steps,dt", [(51, 1, 1000, 0.01), (51, 257, 1200, 0.01), (51, 63, 500, 0.02),
-                                                   (51, 65, 1000, 0.004), (61, 257, 1000, 0.01)],
-                         ids=["1-path", "24-dates", "stride25", "stride125-coefficients-via-L1", "61-tenors"])
+                                                   (51, 65, 1000, 0.004), (61, 257, 1000, 0.01),
+                                                   (51, 129, 2500, 0.01), (61, 65, 3000, 0.01)],
+                         ids=["1-path", "24-dates", "stride25", "stride125-coefficients-via-L1", "61-tenors",
+                              "50-dates-in-windows", "61-tenors-60-dates-in-windows"])
 def test_pc_response_form_shapes_vs_oracle(pc, nt, n_paths, n_steps, dt):
     mk = Market(n_tenor=nt)
     pc.set_market(mk)
@@ -258,3 +260,40 @@ def test_pc_response_form_shapes_vs_oracle(pc, nt, n_paths, n_steps, dt):
     ee = O.expected_exposure(O.exposure_paths_pc(mk, sw, cfg.n_steps, cfg.dt, normals))
     nd = n_steps // stride
     _assert_rel(v.ee[:nd + 1], ee[:nd + 1], FP64_RTOL, "EE")
+
+
+@pytest.mark.parametrize("nt,n_steps", [(51, 2500), (61, 3000)], ids=["25y-51-tenors", "30y-61-tenors"])
+def test_pc_response_windows_vs_convected_and_oracle(pc, nt, n_steps):
+    """More than 24 dates: the predictor-corrector's response form prices
+    them in windows (hjm_eresp.cu); per-path exposures against its all-FP64
+    convected form on the same paths (1e-11 relative) and against the oracle
+    (1e-10).  Exposures near zero are compared absolutely, below 5e-13 of the
+    scale: over 50 or 60 dates the two FP64 forms and the oracle order their
+    operations differently by ~1e-13 of the scale (the Euler tests' floor for
+    runs of more than 24 dates).  The last date samples the last tenor, where
+    the step's curvature noise enters after the step (a lag -1 term)."""
+    mk = Market(n_tenor=nt)
+    pc.set_market(mk)
+    sw = Swap(n_tenor=nt, n_periods=n_steps // 50)
+    pc.set_swap(sw)
+    cfg = RunConfig(n_paths=193, n_steps=n_steps, dt=0.01, seed=17)
+    out = {}
+    pc.keep_exposures(True)
+    try:
+        for form in ("convect", "response"):
+            pc.set_remainder_form(form)
+            out[form] = (pc.run(cfg, "fp64"), pc.exposures())
+            assert pc.remainder_form() == form
+        pc.set_remainder_form("auto")
+        pc.run(cfg, "fp64")
+        assert pc.remainder_form() == "response"
+    finally:
+        pc.keep_exposures(False)
+        pc.set_remainder_form("auto")
+    (vc, xc), (vr, xr) = out["convect"], out["response"]
+    nd = n_steps // 50 + 1
+    _assert_rel(xr[:nd], xc[:nd], 1e-11, "exposures response vs convect", floor=5e-13)
+    normals = pc.dump_normals(cfg.n_paths, cfg.n_steps, cfg.seed)
+    x = O.exposure_paths_pc(mk, sw, cfg.n_steps, cfg.dt, normals)
+    _assert_rel(xr[:nd], x[:, :nd].T, FP64_RTOL, "exposures vs oracle", floor=5e-13)
+    _assert_rel(vr.ee[:nd], O.expected_exposure(x)[:nd], FP64_RTOL, "EE vs oracle")
