@@ -324,7 +324,7 @@ struct VolLoadings {
 // The table of path_kernel_fp64_vresp: R_jk(m) = (A^m S_k)[j] by m applications
 // of the upwind step (Euler: backward difference at L, simulation_cpu.h:96-108)
 // or of A2 (predictor-corrector: three-point stencil, Euler rows at L-1, L),
-// and their running sums; the lag -> entry map of response_table_kernel.  One
+// and their running sums; the lag -> entry map of eresp_table_kernel.  One
 // CTA of kMaxTenor threads, thread t holding tenor t of the three responses.
 __global__ void __launch_bounds__(kMaxTenor)
     response_table_vol_kernel(int nt, double c, int stride, int B, int pc, const __grid_constant__ VolLoadings S,

@@ -4,7 +4,9 @@ The response form carries the remainder hc of the polynomial decomposition,
 driven by kappa W at the last tenor and convected upwind, as impulse-response
 sums at the sampled tenors: for date j, hc at its sampling step and the
 running sum of hc, both sum_n coef(lag) W_{n-1}.  Restated here in numpy, as
-response_table_kernel and path_kernel_fp64_resp compute them:
+eresp_table_kernel (eresp_table_pc_kernel for the predictor-corrector) and
+path_kernel_fp64_eresp compute them (the Euler prefix rule of
+eresp_active_kernel is in test_cubic_windows.py):
 
 * the table: entry (row b*stride + s, slot B - j) holds kappa G_j(lag) and
   kappa CG_j(lag), lag = (j - b) stride - 1 - s, every lag of every date in
@@ -101,9 +103,10 @@ def test_value_prefix_drops_only_vanishing_terms(nt, stride, B, c):
 
 
 def active_prefix(tab, B, stride):
-    """As response_active_kernel: per row, the slots up to the last whose
-    coefficient or running-sum coefficient (FP32 hi part) is nonzero and at
-    least 2^-70 of its slot's largest over all rows."""
+    """An earlier, stricter prefix rule: per row, the slots up to the last
+    whose coefficient or running-sum coefficient (FP32 hi part) is nonzero
+    and at least 2^-70 of its slot's largest over all rows (the kernels now
+    cut at FP64's unit roundoff of the unit response, eresp_active_kernel)."""
     T = tab.reshape(B * stride, ROW, 2).astype(np.float32)
     a = np.abs(T)
     thr = (a.max(axis=0) * np.float32(2.0 ** -70)).astype(np.float32)
@@ -265,8 +268,8 @@ def pc_sources(c, dtau):
 
 
 def response_table_pc(nt, stride, B, c, dtau):
-    """As response_table_kernel with pc = 1: the coefficient of the old W at
-    lag l is H1(l) + H2(l+1), H1 = wL1 G1 + (wL - gL) G2, H2 = gL G2."""
+    """As eresp_table_pc_kernel: the coefficient of the old W at lag l is
+    H1(l) + H2(l+1), H1 = wL1 G1 + (wL - gL) G2, H2 = gL G2."""
     L = nt - 1
     wL1, wL, gL = pc_sources(c, dtau)
     w0, w1, w2 = wL1, wL - gL, gL
@@ -345,6 +348,70 @@ def test_pc_response_sums_equal_the_convected_remainder(nt, stride, B, c):
             assert abs(got - want) <= 1e-12 * abs(want) + 1e-300, (j, got, want)
 
 
+def test_pc_date_at_the_last_tenor_takes_the_lag_minus_one_term():
+    """With as many dates as tenors after the first (B = L), the date that
+    samples the last tenor also takes gL times W after its own sampling step
+    (the step's curvature noise enters at L after the step, a lag -1 term the
+    table cannot hold); path_kernel_fp64_eresp adds it when it prices that
+    date.  Value and running sum against the direct recursion."""
+    nt, stride, c, dtau = 11, 10, 0.1, 0.5
+    L = B = nt - 1
+    tab, _ = response_table_pc(nt, stride, B, c, dtau)
+    wL1, wL, gL = pc_sources(c, dtau)
+    rng = np.random.default_rng(11)
+    acc = np.zeros((ROW, 2))
+    hc, hsum = np.zeros(nt), np.zeros(nt)
+    W = 0.0
+    for b in range(1, B):
+        for s in range(stride):
+            for r in range(B - b):
+                acc[r] += tab[(b * stride + s) * ROW + r] * W
+            gam = rng.normal() * 1e-5
+            hn = pc_step(hc, c)
+            hn[L - 1] += wL1 * W
+            hn[L] += wL * W + gL * gam
+            hc = hn
+            hsum += hc
+            W += gam
+        j = b + 1
+        got_v, got_s = acc[B - j, 0], acc[B - j, 1]
+        if j == L:
+            got_v, got_s = got_v + gL * W, got_s + gL * W
+        for got, want in ((got_v, hc[j]), (got_s, hsum[j])):
+            assert abs(got - want) <= 1e-12 * abs(want) + 1e-300, (j, got, want)
+
+
+def eresp_prefix_pc(tab, B, stride, c, dtau):
+    """As eresp_active_kernel on the predictor-corrector's table: the slots up
+    to the last whose FP32 coefficient reaches 2^-53 |kappa_pc| or running-sum
+    coefficient 2^-53 |kappa_pc| times the date's sampling step, kappa_pc =
+    -(2c + 2c^2) dtau^2 (the step's source per unit W)."""
+    kappa = -(2 * c + 2 * c * c) * dtau * dtau
+    T = tab.reshape(B * stride, ROW, 2)
+    a = np.abs(T.astype(np.float32))
+    tg = np.float32(abs(kappa)) * np.float32(2.0 ** -53)
+    dates = np.maximum(B - np.arange(ROW), 1)
+    tcg = (tg * (dates * stride).astype(np.float32)).astype(np.float32)
+    sig = ((a[:, :, 0] != 0) & (a[:, :, 0] >= tg)) | ((a[:, :, 1] != 0) & (a[:, :, 1] >= tcg[None, :]))
+    return np.where(sig.any(axis=1), ROW - np.argmax(sig[:, ::-1], axis=1), 0), kappa
+
+
+@pytest.mark.parametrize("nt,stride,B,c", SHAPES)
+def test_pc_eresp_prefix_drops_only_terms_below_the_unit_roundoff(nt, stride, B, c):
+    """The response kernel's prefix on the predictor-corrector's table skips,
+    per date, terms that sum to less than 32 x 2^-53 |kappa_pc| per unit |W|
+    (per sampling step for the running sum), as on the Euler step's."""
+    tab, _ = response_table_pc(nt, stride, B, c, 0.5)
+    pre, kappa = eresp_prefix_pc(tab, B, stride, c, 0.5)
+    T = tab.reshape(B * stride, ROW, 2)
+    for t in range(2, B + 1):
+        r = B - t
+        rows = np.arange(stride, t * stride)
+        dropped = rows[pre[rows] <= r]
+        assert np.abs(T[dropped, r, 0]).sum() <= 32 * 2.0 ** -53 * abs(kappa), t
+        assert np.abs(T[dropped, r, 1]).sum() <= 32 * 2.0 ** -53 * abs(kappa) * t * stride, t
+
+
 # --- volatility-table step: the whole stochastic curve in factor responses ---
 def euler_step(v, c):
     L = v.size - 1
@@ -390,13 +457,13 @@ def test_vol_table_response_sums_equal_the_direct_recursion(scheme, nt, stride, 
             assert abs(got - want) <= 1e-12 * abs(want) + 1e-300, (j, got, want)
 
 
-# --- the parts S, U, W in the moving frame (path_kernel_fp64_resp, Euler) ---
+# --- the parts S, U, W in the moving frame (path_kernel_fp64_eresp) ---
 SVC_TRI = np.sqrt(0.01) * np.array([[0.0064, 0.0, 0.0], [-0.0036, 0.0004, 0.0], [0.0020, -0.0006, 0.00002]])
 SVC_GEN = SVC_TRI + np.sqrt(0.01) * np.array([[0.0, 1e-4, 2e-6], [0.0, 0.0, -3e-6], [0.0, 0.0, 0.0]])
 
 
 def state_coefs(stride, n01, n02, n12, svc):
-    """As state_coef_kernel: row s < stride (the step within a block) holds
+    """As eresp_coef_kernel: row s < stride (the step within a block) holds
     C(s) = M^-(s+1) B and G(s) = Q(s) C(s), B[c][k] = svc[k][c], M = I + N,
     N = [[0, n01, n02], [0, 0, n12], [0, 0, 0]]."""
     Bm = np.asarray(svc, dtype=np.float64).T
