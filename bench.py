@@ -97,23 +97,18 @@ def algorithmic_flops_per_path(n_tenor: int, n_steps: int, stride: int, form: st
     ADD or MUL issues like an FMA, so the fraction is a lower bound on the
     FP64 pipe's use (ncu's pipe utilisation is the direct measure).
 
-    ``remainder="response"`` (FP64, at most 24 dates): polynomial forms, the
-    FP64 pipe forms the parts and their running sums from the moving-frame
-    sums only at the sampled dates (41 flops per date: widening the six sums
-    (6), x = M^a y (6), Z += Q(a) y - v (15), the two quadratics at the date's
-    tenor (11) and the re-anchoring's rests (3)); the per-step work runs in
-    double-FP32 on the FP32 pipe
-    (``response_fp32_flops_per_path``); ``table``, six FP64 FMAs per date still
-    to be sampled per step (the three factors' responses, value and running
-    sum); no block recovery."""
+    ``remainder="response"`` (FP64): polynomial forms, the FP64 pipe forms the
+    parts and their running sums from the moving-frame sums only at the
+    sampled dates (41 flops per date: widening the six sums (6), x = M^a y
+    (6), Z += Q(a) y - v (15), the two quadratics at the date's tenor (11) and
+    the re-anchoring's rests (3)); the per-step work runs in double-FP32 on the
+    FP32 pipe (``response_fp32_flops_per_path``); ``table`` (at most 24 dates),
+    the same: the whole per-step work in double-FP32 on the FP32 pipe
+    (``table_response_fp32_flops_per_path``), nothing per step in FP64."""
     B = n_steps // stride
     L = n_tenor - 1
-    if remainder == "response" and form != "table":
-        return 41 * B
     if remainder == "response":
-        # volatility table in the response form: per step and date still to be
-        # sampled, three FMAs for the value and three for the running sum
-        return 12 * stride * sum(B - b for b in range(1, B))
+        return 41 * B if form != "table" else 0
 
     def per_step(b: int, k: int) -> int:
         # polynomial forms: the remainder is still zero below tenor L - 1 - k
@@ -178,6 +173,18 @@ def response_fp32_flops_per_path(n_tenor: int, n_steps: int, stride: int, form: 
     slots = int((4 * ((pre + 3) // 4)).sum())
     terms = 6 if form == "poly_tri" else 9
     return 30 * slots + (26 * terms + 18) * (B - 1) * stride
+
+
+def table_response_fp32_flops_per_path(n_tenor: int, n_steps: int, stride: int) -> int:
+    """FP32 flops per path of the volatility-table step's response form
+    (path_kernel_fp64_vresp): per step and date still to be sampled, three
+    double-FP32 terms into {value, running sum} (13 flops per lane each: the
+    negated product, two FMAs for its error, Knuth's two-sum and the low
+    part's update; 26 for the two lanes) and the pairs' renormalisation (3 per
+    lane), 84 flops; an add counted as one flop though it occupies the FMA
+    pipe like an FMA."""
+    B = n_steps // stride
+    return 84 * stride * sum(B - b for b in range(1, B))
 
 
 def eresp_windows(n_blocks: int) -> list[tuple[int, int]]:
@@ -831,6 +838,8 @@ def generic_step_run(eng, mk, sw, args, flush, stride, peak64, peak32) -> dict:
             res = eng.fetch()
             form = eng.remainder_form() if prec == "fp64" else "convect"
             fl = algorithmic_flops_per_path(mk.n_tenor, N_STEPS, stride, "table", form) * n
+            if form == "response":  # the double-FP32 response sums, on the FP32 pipe
+                fl, peak = table_response_fp32_flops_per_path(mk.n_tenor, N_STEPS, stride) * n, peak32
             out[prec] = {"n_paths": n, "remainder": form,
                          "path_steps_per_s": n * N_STEPS / (step_ms * 1e-3), "device_ms_per_step": step_ms,
                          "path_kernel_ms": kern_ms, "achieved_tflops": fl / (kern_ms * 1e-3) / 1e12,

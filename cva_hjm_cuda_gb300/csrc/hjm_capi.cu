@@ -799,23 +799,16 @@ static void fill_pc(const hjm_ctx* ctx, const RunShape& sh, double dt, const Pat
 // step, so AUTO always takes it.
 //
 // Volatility-table step (no decomposition, at most 24 dates): the whole
-// stochastic curve in impulse responses, six FP64 FMAs per date still to be
-// sampled per step, against four FMAs per live tenor (five for the
-// predictor-corrector) and ~10 per step when convected; AUTO takes the
-// cheaper, summed over the evolved blocks.
+// stochastic curve in impulse responses, per step and date still to be
+// sampled three double-FP32 terms on the FP32 pipe, against four FP64 FMAs
+// per live tenor (five for the predictor-corrector) when convected: the
+// response form whenever it holds the run's dates.
 static bool use_response_form(const hjm_ctx* ctx, const RunShape& sh)
 {
     const bool pc = ctx->scheme == HJM_SCHEME_PREDICTOR_CORRECTOR;
     if (use_poly_path(ctx) || (!pc && use_cubic_path(ctx))) return ctx->remainder != HJM_REMAINDER_CONVECT;
     if (sh.B > response_max_dates()) return false;
-    if (ctx->remainder != HJM_REMAINDER_AUTO) return ctx->remainder == HJM_REMAINDER_RESPONSE;
-    long conv = 0, resp = 0;
-    for (int b = 1; b < sh.B; ++b) {
-        const int live = ctx->nt - 1 - b;
-        conv += pc ? 5 * live + 12 : 4 * live + 10;
-        resp += 6 * (sh.B - b);
-    }
-    return resp < conv;
+    return ctx->remainder != HJM_REMAINDER_CONVECT;
 }
 
 // The volatility-table response table of the run shape, scheme and loadings
@@ -835,14 +828,14 @@ static hjm_status ensure_vol_response_table(hjm_ctx* ctx, const RunShape& sh, do
         k.sv == key)
         return HJM_OK;
     k.valid = false;
-    const size_t bytes = sizeof(double2) * response_table_vol_elems(sh.stride, sh.B);
+    const size_t bytes = sizeof(float4) * response_table_vol_elems(sh.stride, sh.B);
     if (bytes > ctx->vresp.bytes)
         HJM_CUDA(ctx, ctx->vresp.ensure(bytes));  // cudaFree waits for the device
     else
         HJM_CUDA(ctx, cudaStreamWaitEvent(s, ctx->resp_used, 0));
     HJM_CUDA(ctx, cudaMemsetAsync(ctx->vresp.p, 0, bytes, s));  // entries the kernel reads as exact zeros
     HJM_CUDA(ctx, launch_response_table_vol(nt, c, sh.stride, sh.B, ctx->scheme == HJM_SCHEME_PREDICTOR_CORRECTOR, sv,
-                                            (double2*)ctx->vresp.p, s));
+                                            (float4*)ctx->vresp.p, s));
     ctx->stat_launches += 1;
     k.nt = nt;
     k.stride = sh.stride;
@@ -1037,7 +1030,7 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
         } else if (resp) {
             st = ensure_vol_response_table(ctx, sh, dt, &Q.P.sv[0][0], s);
             if (st != HJM_OK) return st;
-            HJM_CUDA(ctx, launch_path_fp64_vresp(ctx->nt, Q.P, (const double2*)ctx->vresp.p, ext_dev,
+            HJM_CUDA(ctx, launch_path_fp64_vresp(ctx->nt, Q.P, (const float4*)ctx->vresp.p, ext_dev,
                                                  (double*)ctx->partials.p, store ? (double*)ctx->estore.p : nullptr,
                                                  s));
         } else {
@@ -1063,7 +1056,7 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
         } else if (resp) {
             st = ensure_vol_response_table(ctx, sh, dt, &P.sv[0][0], s);
             if (st != HJM_OK) return st;
-            HJM_CUDA(ctx, launch_path_fp64_vresp(ctx->nt, P, (const double2*)ctx->vresp.p, ext_dev,
+            HJM_CUDA(ctx, launch_path_fp64_vresp(ctx->nt, P, (const float4*)ctx->vresp.p, ext_dev,
                                                  (double*)ctx->partials.p, store ? (double*)ctx->estore.p : nullptr,
                                                  s));
         } else {

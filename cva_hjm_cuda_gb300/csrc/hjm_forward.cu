@@ -246,22 +246,28 @@ __host__ __device__ inline size_t resp_smem_bytes(int n_blocks)
     return ((size_t)n_blocks + 2) * kFp64Cta * 8 + 2 * (kFp64Cta / 32) * 8;
 }
 
-// Response form of the volatility-table step (FP64, any factor shapes, at most
-// kRespDates dates, both time schemes).  Without a polynomial part the whole
-// stochastic curve is driven by the injected noise: h_n = A h_{n-1} + S phi_n
-// (A the upwind step, or the predictor-corrector's A2 with the loadings S
-// N-projected), so at date j's tenor after step K
+// Response form of the volatility-table step (FP64 accuracy, any factor
+// shapes, at most kRespDates dates, both time schemes).  Without a polynomial
+// part the whole stochastic curve is driven by the injected noise: h_n =
+// A h_{n-1} + S phi_n (A the upwind step, or the predictor-corrector's A2
+// with the loadings S N-projected), so at date j's tenor after step K
 //     h_K[j] = sum_{n<=K} sum_k phi_{n,k} R_jk(K - n),   R_jk(l) = (A^l S_k)[j],
 // and its running sum likewise with CR_jk(l) = sum_{r<=l} R_jk(r).  Per step
-// and date still to be sampled: six FP64 FMAs (three factors, value and sum)
-// on coefficients read from the table (response_table_vol_kernel), in place of
-// four FMAs per live tenor and the block-end recovery.  FP64 throughout: here
-// the response sums are the curve's whole stochastic part, so no double-FP32
-// shortcut keeps FP64 accuracy.  Entry (row b stride + s, slot B - j) holds
-// three double2 {R_jk, CR_jk} at lag (j - b) stride - 1 - s.
+// and date still to be sampled, three terms (the factors) into {value,
+// running sum}, on coefficients read from the table (response_table_vol_kernel),
+// in place of four FMAs per live tenor and the block-end recovery.  The sums
+// run in double-FP32 on the FP32 pipe: the table holds each coefficient as
+// FP32 hi + lo (48 bits), a generator normal is exact in FP32 (an external
+// FP64 normal is split hi + lo), the product's leading term is exact by FMA
+// and Knuth's two-sum adds it (df_acc_w / df_acc), and the pairs are
+// renormalised after every step's three terms, so each addition rounds at
+// 2^-48 of the date's sum (the sums are the curve's whole stochastic part,
+// ~1e-2, over at most ~1,200 steps: ~1e-15 of the curve, random-walk-like).
+// Entry (row b stride + s, slot B - j) holds three float4 {R_jk hi, CR_jk hi,
+// R_jk lo, CR_jk lo} at lag (j - b) stride - 1 - s.
 template <int NT, bool EXT>
 __global__ void __launch_bounds__(kFp64Cta, 6)
-    path_kernel_fp64_vresp(const __grid_constant__ PathParams<double> P, const double2* __restrict__ vresp,
+    path_kernel_fp64_vresp(const __grid_constant__ PathParams<double> P, const float4* __restrict__ vresp,
                            const double* __restrict__ ext, double* __restrict__ partials,
                            double* __restrict__ estore)
 {
@@ -277,13 +283,18 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
     const bool active = lp < P.n_paths;
     const uint64_t gpath = P.path_offset + (uint64_t)lp;
 
-    double a[kRespSlots], ai[kRespSlots];  // h at tenor j and its running sum, slot B - j
+    // {h at tenor j, its running sum} as hi + lo pairs, slot B - j
+    float2 A[kRespSlots], Al[kRespSlots];
 #pragma unroll
-    for (int r = 0; r < kRespSlots; ++r) a[r] = ai[r] = 0.0;
+    for (int r = 0; r < kRespSlots; ++r) A[r] = Al[r] = make_float2(0.0f, 0.0f);
 
     auto sample = [&](int i) {
-        const double h = i >= 2 ? select_reg<kRespSlots, double>(a, B - i) : 0.0;
-        const double hs = i >= 2 ? select_reg<kRespSlots, double>(ai, B - i) : 0.0;
+        double h = 0.0, hs = 0.0;
+        if (i >= 2) {
+            const float2 a = select_reg<kRespSlots, float2>(A, B - i), l = select_reg<kRespSlots, float2>(Al, B - i);
+            h = widen_f32(a.x) + widen_f32(l.x);
+            hs = widen_f32(a.y) + widen_f32(l.y);
+        }
         const double x = P.psamp[i] + h;
         const double D = exp(-(P.psum[i] + hs) * P.dt);
         const double Lb = P.m * (exp(x * P.inv_m) - 1.0);
@@ -292,21 +303,40 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
 
     sample(1);
     for (int b = 1; b < B; ++b) {
-        const double2* row = vresp + (size_t)b * P.stride * kRespRow * 3;
+        const float4* row = vresp + (size_t)b * P.stride * kRespRow * 3;
         const int n_act = B - b;  // every date still to be sampled (the factors reach every tenor)
         for (int s = 0; s < P.stride; ++s) {
             const int n = b * P.stride + s;
-            double phi0, phi1, phi2;
-            draw_phi<double, EXT>(ext, gpath, active ? lp : 0, P.n_paths, n, P.rk0, P.rk1, phi0, phi1, phi2);
-            const double2* rr = row + (size_t)s * kRespRow * 3;
+            float ph[3], pl[3];  // the normals as hi + lo (lo = 0 for the generator's FP32 draws)
+            if constexpr (EXT) {
+                double d0, d1, d2;
+                draw_phi<double, true>(ext, gpath, active ? lp : 0, P.n_paths, n, P.rk0, P.rk1, d0, d1, d2);
+                split_f64(d0, ph[0], pl[0]);
+                split_f64(d1, ph[1], pl[1]);
+                split_f64(d2, ph[2], pl[2]);
+            } else {
+                draw_phi<float, false>(ext, gpath, lp, P.n_paths, n, P.rk0, P.rk1, ph[0], ph[1], ph[2]);
+            }
+            const float4* rr = row + (size_t)s * kRespRow * 3;
             resp_groups(n_act, [&](auto gc) {
                 constexpr int G = decltype(gc)::value;
+                float4 q[4][3];
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+#pragma unroll
+                    for (int k = 0; k < kFactors; ++k) q[u][k] = __ldg(rr + (4 * G + u) * 3 + k);
 #pragma unroll
                 for (int u = 0; u < 4; ++u) {
-                    const double2* e = rr + (4 * G + u) * 3;
-                    const double2 k0 = __ldg(e), k1 = __ldg(e + 1), k2 = __ldg(e + 2);
-                    a[4 * G + u] = fma(k2.x, phi2, fma(k1.x, phi1, fma(k0.x, phi0, a[4 * G + u])));
-                    ai[4 * G + u] = fma(k2.y, phi2, fma(k1.y, phi1, fma(k0.y, phi0, ai[4 * G + u])));
+#pragma unroll
+                    for (int k = 0; k < kFactors; ++k) {
+                        const float2 kh = make_float2(q[u][k].x, q[u][k].y), kl = make_float2(q[u][k].z, q[u][k].w);
+                        const float2 w = make_float2(ph[k], ph[k]), nw = make_float2(-ph[k], -ph[k]);
+                        if constexpr (EXT)
+                            df_acc(A[4 * G + u], Al[4 * G + u], kh, kl, w, make_float2(pl[k], pl[k]), nw);
+                        else
+                            df_acc_w(A[4 * G + u], Al[4 * G + u], kh, kl, w, nw);
+                    }
+                    df_renorm(A[4 * G + u], Al[4 * G + u]);
                 }
             });
         }
@@ -328,7 +358,7 @@ struct VolLoadings {
 // CTA of kMaxTenor threads, thread t holding tenor t of the three responses.
 __global__ void __launch_bounds__(kMaxTenor)
     response_table_vol_kernel(int nt, double c, int stride, int B, int pc, const __grid_constant__ VolLoadings S,
-                              double2* __restrict__ vresp)
+                              float4* __restrict__ vresp)
 {
     __shared__ double v_s[kFactors][kMaxTenor];
     const int t = threadIdx.x;
@@ -348,9 +378,13 @@ __global__ void __launch_bounds__(kMaxTenor)
             const int q = m / stride + 1;
             const int b = t - q;
             if (b >= 1) {
-                double2* e = vresp + (((size_t)b * stride + (size_t)(q * stride - 1 - m)) * kRespRow + (B - t)) * 3;
+                float4* e = vresp + (((size_t)b * stride + (size_t)(q * stride - 1 - m)) * kRespRow + (B - t)) * 3;
 #pragma unroll
-                for (int k = 0; k < kFactors; ++k) e[k] = make_double2(v[k], cum[k]);
+                for (int k = 0; k < kFactors; ++k) {
+                    const float vh = __double2float_rn(v[k]), ch = __double2float_rn(cum[k]);
+                    e[k] = make_float4(vh, ch, __double2float_rn(v[k] - (double)vh),
+                                       __double2float_rn(cum[k] - (double)ch));
+                }
             }
         }
 #pragma unroll
@@ -881,7 +915,7 @@ cudaError_t launch_path_fp64(int nt, const PathParams<double>& P, bool poly, con
 }
 
 template <int NT, bool EXT>
-static cudaError_t launch_fp64_vresp_t(const PathParams<double>& P, const double2* vresp, const double* ext,
+static cudaError_t launch_fp64_vresp_t(const PathParams<double>& P, const float4* vresp, const double* ext,
                                        double* partials, double* estore, cudaStream_t s)
 {
     const size_t smem = resp_smem_bytes(P.n_blocks);
@@ -893,7 +927,7 @@ static cudaError_t launch_fp64_vresp_t(const PathParams<double>& P, const double
     return cudaGetLastError();
 }
 
-cudaError_t launch_path_fp64_vresp(int nt, const PathParams<double>& P, const double2* vresp, const double* ext,
+cudaError_t launch_path_fp64_vresp(int nt, const PathParams<double>& P, const float4* vresp, const double* ext,
                                    double* partials, double* estore, cudaStream_t s)
 {
     if (!vresp || P.n_blocks > kRespDates) return cudaErrorInvalidValue;
@@ -907,7 +941,7 @@ cudaError_t launch_path_fp64_vresp(int nt, const PathParams<double>& P, const do
 size_t response_table_vol_elems(int stride, int n_blocks) { return (size_t)n_blocks * stride * kRespRow * 3; }
 
 cudaError_t launch_response_table_vol(int nt, double c, int stride, int n_blocks, bool pc, const double* sv,
-                                      double2* vresp, cudaStream_t s)
+                                      float4* vresp, cudaStream_t s)
 {
     if (nt < 3 || nt > kMaxTenor || n_blocks > kRespDates || n_blocks >= nt || stride < 1) return cudaErrorInvalidValue;
     VolLoadings S;

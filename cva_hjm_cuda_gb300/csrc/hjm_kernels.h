@@ -64,11 +64,11 @@ int response_max_dates();
 // The response form of the volatility-table step (FP64, either scheme: the
 // table carries the scheme): vresp from launch_response_table_vol with the
 // kernel's loadings sv [kFactors][kMaxTenor] (PathParams::sv)
-cudaError_t launch_path_fp64_vresp(int nt, const PathParams<double>& P, const double2* vresp, const double* ext,
+cudaError_t launch_path_fp64_vresp(int nt, const PathParams<double>& P, const float4* vresp, const double* ext,
                                    double* partials, double* estore, cudaStream_t s);
-size_t response_table_vol_elems(int stride, int n_blocks);  // double2 entries
+size_t response_table_vol_elems(int stride, int n_blocks);  // float4 entries
 cudaError_t launch_response_table_vol(int nt, double c, int stride, int n_blocks, bool pc, const double* sv,
-                                      double2* vresp, cudaStream_t s);
+                                      float4* vresp, cudaStream_t s);
 cudaError_t launch_path_mixed(int nt, const MixedParams& M, bool poly, const double* ext, double* partials,
                               float* estore, cudaStream_t s);
 void pack_mixed_params(int nt, const PathParams<float>& P, MixedParams& M);

@@ -338,8 +338,9 @@ hjm_status hjm_run_static(void* cuda_stream, int32_t n_tenor, double dtau, const
         } else if (B >= 2 && B <= response_max_dates() && entries <= kStaticRespEntries) {
             // the response form: its table (zero outside the live entries) into the static array
             STATIC_CUDA(cudaMemsetAsync(resp_table, 0, sizeof(double2) * entries, s));
-            STATIC_CUDA(launch_response_table_vol(n_tenor, dt / dtau, (int)stride, B, false, &P.sv[0][0], resp_table, s));
-            STATIC_CUDA(launch_path_fp64_vresp(n_tenor, P, resp_table, nullptr, partials, nullptr, s));
+            float4* vtable = reinterpret_cast<float4*>(resp_table);
+            STATIC_CUDA(launch_response_table_vol(n_tenor, dt / dtau, (int)stride, B, false, &P.sv[0][0], vtable, s));
+            STATIC_CUDA(launch_path_fp64_vresp(n_tenor, P, vtable, nullptr, partials, nullptr, s));
         } else {
             STATIC_CUDA(launch_path_fp64(n_tenor, P, poly, nullptr, partials, nullptr, s));
         }

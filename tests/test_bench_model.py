@@ -19,9 +19,12 @@ def test_response_forms_count_the_kernels_operations():
     # polynomial response form: the FP64 pipe forms the parts at the B dates only
     assert bench.algorithmic_flops_per_path(nt, n_steps, stride, "poly_tri", "response") == 41 * B
     assert bench.algorithmic_flops_per_path(nt, n_steps, stride, "poly", "response") == 41 * B
-    # volatility table in the response form: six FMAs per date still to be sampled per step
+    # volatility table in the response form: no FP64 work per step; on the
+    # FP32 pipe three double-FP32 terms (26 flops for both lanes each) and the
+    # renormalisation (6) per date still to be sampled per step
     live = sum(B - b for b in range(1, B)) * stride
-    assert bench.algorithmic_flops_per_path(nt, n_steps, stride, "table", "response") == 12 * live
+    assert bench.algorithmic_flops_per_path(nt, n_steps, stride, "table", "response") == 0
+    assert bench.table_response_fp32_flops_per_path(nt, n_steps, stride) == (3 * 26 + 6) * live
     # the double-FP32 side: 30 flops per slot (slots in groups of four over the
     # active prefix), 26 per moving-frame term (6 or 9 per step), 18 per step
     # for the renormalisation
@@ -33,7 +36,7 @@ def test_response_forms_count_the_kernels_operations():
 
 
 def test_convected_forms_exceed_the_response_forms():
-    for form in ("poly_tri", "poly", "table"):
+    for form in ("poly_tri", "poly"):
         conv = bench.algorithmic_flops_per_path(51, 1000, 50, form)
         resp = bench.algorithmic_flops_per_path(51, 1000, 50, form, "response")
         assert resp < conv, form

@@ -367,7 +367,8 @@ def test_remainder_form_choice_and_limits(engine, remainder_form, tmp_path):
 
 # ---------------------------------------------------------------------------
 # the volatility-table step (a table of any shape) in the response form: the
-# whole stochastic curve as FP64 sums of the three factors' impulse responses
+# whole stochastic curve as double-FP32 sums of the three factors' impulse
+# responses
 # ---------------------------------------------------------------------------
 def _bumpy_market(nt=51):
     mk = Market(n_tenor=nt)
@@ -399,7 +400,10 @@ def test_table_step_response_vs_convected_and_oracle(engine, remainder_form, sch
         engine.keep_exposures(False)
         engine.set_scheme("euler")
     (vc, xc), (vr, xr) = out["convect"], out["response"]
-    _assert_rel(xr, xc, 1e-11, "exposures response vs convect")
+    # the response sums run in double-FP32 (2^-48 per addition, random-walk
+    # over the run): exposures near zero compared absolutely below 1e-13 of
+    # the scale, as for the decomposition's response form
+    _assert_rel(xr, xc, 1e-11, "exposures response vs convect", floor=EXPOSURE_FLOOR)
     paths = O.exposure_paths_pc if scheme == "predictor_corrector" else O.exposure_paths
     x = paths(mk, sw, cfg.n_steps, cfg.dt, normals)
     ee = O.expected_exposure(x)
