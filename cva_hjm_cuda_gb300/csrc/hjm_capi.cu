@@ -798,16 +798,14 @@ static void fill_pc(const hjm_ctx* ctx, const RunShape& sh, double dt, const Pat
 // form at 20 dates (Euler), and the convected cubic has no form but the table
 // step, so AUTO always takes it.
 //
-// Volatility-table step (no decomposition, at most 24 dates): the whole
-// stochastic curve in impulse responses, per step and date still to be
-// sampled three double-FP32 terms on the FP32 pipe, against four FP64 FMAs
-// per live tenor (five for the predictor-corrector) when convected: the
-// response form whenever it holds the run's dates.
+// Volatility-table step (no decomposition): the whole stochastic curve in
+// impulse responses, per step and date still to be sampled three
+// double-FP32 terms on the FP32 pipe (in windows of at most 24 dates),
+// against four FP64 FMAs per live tenor (five for the predictor-corrector)
+// when convected.
 static bool use_response_form(const hjm_ctx* ctx, const RunShape& sh)
 {
-    const bool pc = ctx->scheme == HJM_SCHEME_PREDICTOR_CORRECTOR;
-    if (use_poly_path(ctx) || (!pc && use_cubic_path(ctx))) return ctx->remainder != HJM_REMAINDER_CONVECT;
-    if (sh.B > response_max_dates()) return false;
+    (void)sh;
     return ctx->remainder != HJM_REMAINDER_CONVECT;
 }
 
@@ -960,6 +958,23 @@ static hjm_status enqueue_eresp(hjm_ctx* ctx, const RunShape& sh, double dt, con
     return HJM_OK;
 }
 
+// The volatility-table step in the response form (its table already on the
+// stream): the carry of a windowed run, one launch per window.
+static hjm_status enqueue_vresp(hjm_ctx* ctx, const RunShape& sh, const PathParams<double>& P, const double* ext_dev,
+                                double* estore, cudaStream_t s)
+{
+    double* carry = nullptr;
+    if (vresp_windows(sh.B) > 1) {
+        HJM_CUDA(ctx, ctx->carry.ensure(sizeof(double) * 2 * (size_t)P.n_paths));
+        carry = (double*)ctx->carry.p;
+    }
+    int launches = 0;
+    HJM_CUDA(ctx, launch_path_fp64_vresp(ctx->nt, P, (const float4*)ctx->vresp.p, ext_dev, (double*)ctx->partials.p,
+                                         estore, carry, s, &launches));
+    ctx->stat_launches += launches - 1;
+    return HJM_OK;
+}
+
 static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, double dt, uint64_t seed,
                                uint64_t path_offset, int32_t precision, double hazard, double recovery, double pfe_q,
                                const double* ext_dev)
@@ -969,11 +984,6 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
     if (st != HJM_OK) return st;
     HJM_CUDA(ctx, cudaSetDevice(ctx->device));
     const bool mixed = precision == HJM_PRECISION_MIXED;
-    const bool windows_ok = use_poly_path(ctx) || (ctx->scheme == HJM_SCHEME_EULER && use_cubic_path(ctx));
-    if (!mixed && ctx->remainder == HJM_REMAINDER_RESPONSE && sh.B > response_max_dates() && !windows_ok)
-        return fail(ctx, HJM_ERR_INVALID_ARGUMENT,
-                    "the response form of this market and scheme holds at most %d dates (run has %d)",
-                    response_max_dates(), sh.B);
     const bool want_pfe = pfe_q > 0.0;
     const bool store = want_pfe || ctx->keep_exposures;
     const int n_dates = sh.B + 1;
@@ -1030,9 +1040,8 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
         } else if (resp) {
             st = ensure_vol_response_table(ctx, sh, dt, &Q.P.sv[0][0], s);
             if (st != HJM_OK) return st;
-            HJM_CUDA(ctx, launch_path_fp64_vresp(ctx->nt, Q.P, (const float4*)ctx->vresp.p, ext_dev,
-                                                 (double*)ctx->partials.p, store ? (double*)ctx->estore.p : nullptr,
-                                                 s));
+            st = enqueue_vresp(ctx, sh, Q.P, ext_dev, store ? (double*)ctx->estore.p : nullptr, s);
+            if (st != HJM_OK) return st;
         } else {
             HJM_CUDA(ctx, launch_path_pc(ctx->nt, Q, use_poly_path(ctx), ext_dev, (double*)ctx->partials.p,
                                          store ? (double*)ctx->estore.p : nullptr, s));
@@ -1056,9 +1065,8 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
         } else if (resp) {
             st = ensure_vol_response_table(ctx, sh, dt, &P.sv[0][0], s);
             if (st != HJM_OK) return st;
-            HJM_CUDA(ctx, launch_path_fp64_vresp(ctx->nt, P, (const float4*)ctx->vresp.p, ext_dev,
-                                                 (double*)ctx->partials.p, store ? (double*)ctx->estore.p : nullptr,
-                                                 s));
+            st = enqueue_vresp(ctx, sh, P, ext_dev, store ? (double*)ctx->estore.p : nullptr, s);
+            if (st != HJM_OK) return st;
         } else {
             // convected: the quadratic decomposition, else the table step
             HJM_CUDA(ctx, launch_path_fp64(ctx->nt, P, use_poly_path(ctx), ext_dev,

@@ -40,6 +40,7 @@
 #include <cmath>
 #include <cstring>
 
+#include "hjm_epilogue.cuh"
 #include "hjm_eresp.h"
 #include "hjm_resp.cuh"
 
@@ -61,85 +62,6 @@ size_t eresp_smem(int lo, int hi, int np, int coef_floats4)
 {
     return ((size_t)(hi - lo + 3) * kFp64Cta + 2 * (kFp64Cta / 32) + (size_t)np * kFp64Cta) * 8 +
            (size_t)coef_floats4 * 16;
-}
-
-// Epilogue of a window: exposures E_j = max(sum_{i > j} cf_i, 0) of dates
-// j in [lo - 1, hi - 1] (and E_B = 0 for the latest window), the cash flows of
-// later dates arriving in carry; the CTA's EE partial sums of those dates;
-// the CVA statistics (sum c, sum c^2 of the per-path contributions) from the
-// earliest window; the exposure rows by the bulk-copy engine.
-template <int kCta>
-__device__ __forceinline__ void window_epilogue(const PathParams<double>& P, int lo, int hi, double* cf_s,
-                                                double* red_s, double* __restrict__ partials,
-                                                double* __restrict__ estore, double* __restrict__ carry,
-                                                int64_t cta_base, int64_t lp, bool active)
-{
-    const int tid = threadIdx.x;
-    const int B = P.n_blocks;
-    const bool top = hi == B, bottom = lo == 1;
-    double* e_s = cf_s + kCta;  // exposure row of date j: j - lo + 1 (the cash-flow row of date j + 1)
-    double v = 0.0, cva_c = 0.0;
-    if (!top && active) {
-        v = carry[lp];
-        cva_c = carry[P.n_paths + lp];
-    }
-    if (top) e_s[(size_t)(B - lo + 1) * kCta + tid] = 0.0;
-    for (int j = hi - 1; j >= lo - 1; --j) {
-        v += cf_s[(size_t)(j - lo + 2) * kCta + tid];
-        double e = (v > 0.0) ? v : 0.0;
-        if (!active) e = 0.0;
-        e_s[(size_t)(j - lo + 1) * kCta + tid] = e;
-        cva_c = fma(P.cvaw[j], e, cva_c);
-    }
-    if (!bottom && active) {
-        carry[lp] = v;
-        carry[P.n_paths + lp] = cva_c;
-    }
-    __syncthreads();
-
-    const int warp = tid >> 5, lane = tid & 31;
-    const int R = B + 3;
-    const int j0 = lo - 1, j1 = top ? B : hi - 1;
-    for (int j = j0 + warp; j <= j1; j += kCta / 32) {
-        double sum = 0.0;
-#pragma unroll
-        for (int q = 0; q < kCta / 32; ++q) sum += e_s[(size_t)(j - lo + 1) * kCta + lane + 32 * q];
-        sum = warp_sum(sum);
-        if (lane == 0) partials[(size_t)blockIdx.x * R + j] = sum;
-    }
-    if (bottom) {
-        const double s1 = warp_sum(cva_c), s2 = warp_sum(cva_c * cva_c);
-        if (lane == 0) {
-            red_s[warp] = s1;
-            red_s[kCta / 32 + warp] = s2;
-        }
-    }
-    if (P.store_exposures) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    __syncthreads();
-    if (tid == 0) {
-        if (bottom) {
-            double s1 = 0.0, s2 = 0.0;
-            for (int w = 0; w < kCta / 32; ++w) {
-                s1 += red_s[w];
-                s2 += red_s[kCta / 32 + w];
-            }
-            partials[(size_t)blockIdx.x * R + B + 1] = s1;
-            partials[(size_t)blockIdx.x * R + B + 2] = s2;
-        }
-        if (P.store_exposures) {
-            // date rows of this CTA's paths, smem -> HBM with the bulk-copy (TMA) engine
-            const int64_t cnt = (P.n_paths - cta_base < kCta) ? (P.n_paths - cta_base) : kCta;
-            const uint32_t bytes = (uint32_t)(((cnt + 1) / 2) * 2 * sizeof(double));
-            for (int j = j0; j <= j1; ++j) {
-                double* dst = estore + (size_t)j * (size_t)P.ld + (size_t)cta_base;
-                const uint32_t src = (uint32_t)__cvta_generic_to_shared(e_s + (size_t)(j - lo + 1) * kCta);
-                asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
-                             :: "l"(dst), "r"(src), "r"(bytes) : "memory");
-            }
-            asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-            asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
-        }
-    }
 }
 
 // w = y_W + s n23 y_X in double-FP32 (the remainder's source W before step s

@@ -22,6 +22,7 @@
 #include <cstring>
 
 #include "hjm_device.cuh"
+#include "hjm_eresp.h"
 #include "hjm_kernels.h"
 #include "hjm_pairs.cuh"
 #include "hjm_resp.cuh"
@@ -239,18 +240,11 @@ __global__ void __launch_bounds__(kFp64Cta, 4)
     fp64_epilogue<kCta>(P, cf_s, work_s, red_s, partials, estore, cta_base, active);
 }
 
-// Shared memory of the response-form kernels: cf_s [B+2][kCta] (the
-// epilogue's exposures alias it one row up), red_s.
-__host__ __device__ inline size_t resp_smem_bytes(int n_blocks)
-{
-    return ((size_t)n_blocks + 2) * kFp64Cta * 8 + 2 * (kFp64Cta / 32) * 8;
-}
-
 // Response form of the volatility-table step (FP64 accuracy, any factor
-// shapes, at most kRespDates dates, both time schemes).  Without a polynomial
-// part the whole stochastic curve is driven by the injected noise: h_n =
-// A h_{n-1} + S phi_n (A the upwind step, or the predictor-corrector's A2
-// with the loadings S N-projected), so at date j's tenor after step K
+// shapes, both time schemes).  Without a polynomial part the whole
+// stochastic curve is driven by the injected noise: h_n = A h_{n-1} + S phi_n
+// (A the upwind step, or the predictor-corrector's A2 with the loadings S
+// N-projected), so at date j's tenor after step K
 //     h_K[j] = sum_{n<=K} sum_k phi_{n,k} R_jk(K - n),   R_jk(l) = (A^l S_k)[j],
 // and its running sum likewise with CR_jk(l) = sum_{r<=l} R_jk(r).  Per step
 // and date still to be sampled, three terms (the factors) into {value,
@@ -262,49 +256,65 @@ __host__ __device__ inline size_t resp_smem_bytes(int n_blocks)
 // and Knuth's two-sum adds it (df_acc_w / df_acc), and the pairs are
 // renormalised after every step's three terms, so each addition rounds at
 // 2^-48 of the date's sum (the sums are the curve's whole stochastic part,
-// ~1e-2, over at most ~1,200 steps: ~1e-15 of the curve, random-walk-like).
-// Entry (row b stride + s, slot B - j) holds three float4 {R_jk hi, CR_jk hi,
-// R_jk lo, CR_jk lo} at lag (j - b) stride - 1 - s.
+// ~1e-2: ~1e-15 of the curve, random-walk-like over the run).  Entry (row
+// b stride + s, slot B - j) holds three float4 {R_jk hi, CR_jk hi, R_jk lo,
+// CR_jk lo} at lag (j - b) stride - 1 - s; rows are W.row slots wide.
+//
+// Windows, as the decomposition's response form (hjm_eresp.cu): the
+// kRespSlots register slots hold the dates of one window [lo, hi] (dates
+// 2 .. hi from max(lo, 2), slot r for date hi - r); a run with more dates is
+// priced in launches over windows, the latest first, each re-running the
+// normals from the first evolved step to date hi and passing the earlier
+// windows its cash flows' sum and CVA share per path (carry).
+struct VrespWindow {
+    int lo, hi;  // the window's dates
+    int row;     // slots per table row (global slot numbering, slot B - j for date j)
+};
+
 template <int NT, bool EXT>
 __global__ void __launch_bounds__(kFp64Cta, 6)
-    path_kernel_fp64_vresp(const __grid_constant__ PathParams<double> P, const float4* __restrict__ vresp,
-                           const double* __restrict__ ext, double* __restrict__ partials,
-                           double* __restrict__ estore)
+    path_kernel_fp64_vresp(const __grid_constant__ PathParams<double> P, const VrespWindow W,
+                           const float4* __restrict__ vresp, const double* __restrict__ ext,
+                           double* __restrict__ partials, double* __restrict__ estore, double* __restrict__ carry)
 {
     constexpr int kCta = kFp64Cta;
     extern __shared__ __align__(128) unsigned char smem[];
     const int tid = threadIdx.x;
     const int B = P.n_blocks;
-    double* cf_s = reinterpret_cast<double*>(smem);
-    double* red_s = cf_s + (size_t)(B + 2) * kCta;
+    const int lo = W.lo, hi = W.hi;
+    double* cf_s = reinterpret_cast<double*>(smem);  // [hi - lo + 3][kCta]: date i's cash flow in row i - lo + 1
+    double* red_s = cf_s + (size_t)(hi - lo + 3) * kCta;
 
     const int64_t cta_base = (int64_t)blockIdx.x * kCta;
     const int64_t lp = cta_base + tid;
     const bool active = lp < P.n_paths;
     const uint64_t gpath = P.path_offset + (uint64_t)lp;
 
-    // {h at tenor j, its running sum} as hi + lo pairs, slot B - j
+    // {h at tenor j, its running sum} as hi + lo pairs, slot hi - j
     float2 A[kRespSlots], Al[kRespSlots];
 #pragma unroll
     for (int r = 0; r < kRespSlots; ++r) A[r] = Al[r] = make_float2(0.0f, 0.0f);
+    const int roff = B - hi;  // global slot of slot 0
+    const int first = lo > 2 ? lo : 2;
 
-    auto sample = [&](int i) {
+    auto price = [&](int i) {
         double h = 0.0, hs = 0.0;
         if (i >= 2) {
-            const float2 a = select_reg<kRespSlots, float2>(A, B - i), l = select_reg<kRespSlots, float2>(Al, B - i);
+            const float2 a = select_reg<kRespSlots, float2>(A, hi - i), l = select_reg<kRespSlots, float2>(Al, hi - i);
             h = widen_f32(a.x) + widen_f32(l.x);
             hs = widen_f32(a.y) + widen_f32(l.y);
         }
         const double x = P.psamp[i] + h;
         const double D = exp(-(P.psum[i] + hs) * P.dt);
         const double Lb = P.m * (exp(x * P.inv_m) - 1.0);
-        cf_s[i * kCta + tid] = D * (P.payA[i] * Lb - P.payB[i]);
+        cf_s[(size_t)(i - lo + 1) * kCta + tid] = D * (P.payA[i] * Lb - P.payB[i]);
     };
 
-    sample(1);
-    for (int b = 1; b < B; ++b) {
-        const float4* row = vresp + (size_t)b * P.stride * kRespRow * 3;
-        const int n_act = B - b;  // every date still to be sampled (the factors reach every tenor)
+    if (lo == 1) price(1);
+    for (int b = 1; b < hi; ++b) {
+        const float4* row = vresp + ((size_t)b * P.stride * W.row + roff) * 3;
+        // the window's dates still to be sampled: max(b + 1, first) .. hi
+        const int n_act = hi - (b + 1 > first ? b + 1 : first) + 1;
         for (int s = 0; s < P.stride; ++s) {
             const int n = b * P.stride + s;
             float ph[3], pl[3];  // the normals as hi + lo (lo = 0 for the generator's FP32 draws)
@@ -317,7 +327,7 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
             } else {
                 draw_phi<float, false>(ext, gpath, lp, P.n_paths, n, P.rk0, P.rk1, ph[0], ph[1], ph[2]);
             }
-            const float4* rr = row + (size_t)s * kRespRow * 3;
+            const float4* rr = row + (size_t)s * W.row * 3;
             resp_groups(n_act, [&](auto gc) {
                 constexpr int G = decltype(gc)::value;
                 float4 q[4][3];
@@ -340,9 +350,9 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
                 }
             });
         }
-        sample(b + 1);
+        if (b + 1 >= lo) price(b + 1);
     }
-    fp64_epilogue<kCta>(P, cf_s, cf_s + kCta, red_s, partials, estore, cta_base, active);
+    window_epilogue<kCta>(P, lo, hi, cf_s, red_s, partials, estore, carry, cta_base, lp, active);
 }
 
 // Loadings of the three factors on the tenor grid (sqrt(dt) sigma_k, the
@@ -357,8 +367,8 @@ struct VolLoadings {
 // and their running sums; the lag -> entry map of eresp_table_kernel.  One
 // CTA of kMaxTenor threads, thread t holding tenor t of the three responses.
 __global__ void __launch_bounds__(kMaxTenor)
-    response_table_vol_kernel(int nt, double c, int stride, int B, int pc, const __grid_constant__ VolLoadings S,
-                              float4* __restrict__ vresp)
+    response_table_vol_kernel(int nt, double c, int stride, int B, int row, int pc,
+                              const __grid_constant__ VolLoadings S, float4* __restrict__ vresp)
 {
     __shared__ double v_s[kFactors][kMaxTenor];
     const int t = threadIdx.x;
@@ -378,7 +388,7 @@ __global__ void __launch_bounds__(kMaxTenor)
             const int q = m / stride + 1;
             const int b = t - q;
             if (b >= 1) {
-                float4* e = vresp + (((size_t)b * stride + (size_t)(q * stride - 1 - m)) * kRespRow + (B - t)) * 3;
+                float4* e = vresp + (((size_t)b * stride + (size_t)(q * stride - 1 - m)) * row + (B - t)) * 3;
 #pragma unroll
                 for (int k = 0; k < kFactors; ++k) {
                     const float vh = __double2float_rn(v[k]), ch = __double2float_rn(cum[k]);
@@ -915,40 +925,68 @@ cudaError_t launch_path_fp64(int nt, const PathParams<double>& P, bool poly, con
 }
 
 template <int NT, bool EXT>
-static cudaError_t launch_fp64_vresp_t(const PathParams<double>& P, const float4* vresp, const double* ext,
-                                       double* partials, double* estore, cudaStream_t s)
+static cudaError_t launch_fp64_vresp_t(const PathParams<double>& P, const VrespWindow& W, const float4* vresp,
+                                       const double* ext, double* partials, double* estore, double* carry,
+                                       cudaStream_t s)
 {
-    const size_t smem = resp_smem_bytes(P.n_blocks);
+    // cf_s [hi - lo + 3][kCta] (the epilogue's exposures alias it one row up), red_s
+    const size_t smem = ((size_t)(W.hi - W.lo + 3) * kFp64Cta + 2 * (kFp64Cta / 32)) * 8;
     auto k = path_kernel_fp64_vresp<NT, EXT>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const int64_t grid = (P.n_paths + kFp64Cta - 1) / kFp64Cta;
-    k<<<(unsigned)grid, kFp64Cta, smem, s>>>(P, vresp, ext, partials, estore);
+    k<<<(unsigned)grid, kFp64Cta, smem, s>>>(P, W, vresp, ext, partials, estore, carry);
     return cudaGetLastError();
 }
 
+int vresp_windows(int n_blocks) { return eresp_windows(n_blocks, 2, nullptr, nullptr, nullptr); }
+
 cudaError_t launch_path_fp64_vresp(int nt, const PathParams<double>& P, const float4* vresp, const double* ext,
-                                   double* partials, double* estore, cudaStream_t s)
+                                   double* partials, double* estore, double* carry, cudaStream_t s, int* launches)
 {
-    if (!vresp || P.n_blocks > kRespDates) return cudaErrorInvalidValue;
-    if (nt == 51) return ext ? launch_fp64_vresp_t<51, true>(P, vresp, ext, partials, estore, s)
-                             : launch_fp64_vresp_t<51, false>(P, vresp, ext, partials, estore, s);
-    if (nt == 61) return ext ? launch_fp64_vresp_t<61, true>(P, vresp, ext, partials, estore, s)
-                             : launch_fp64_vresp_t<61, false>(P, vresp, ext, partials, estore, s);
-    return cudaErrorInvalidValue;
+    int lo[kMaxTenor], hi[kMaxTenor];
+    // every date is reached at once (the factors load every tenor): windows
+    // of kRespSlots dates from date 2, the latest first
+    const int nw = eresp_windows(P.n_blocks, 2, lo, hi, nullptr);
+    if (!vresp || (nw > 1 && !carry)) return cudaErrorInvalidValue;
+    if (launches) *launches = 0;
+    for (int w = 0; w < nw; ++w) {
+        const VrespWindow W{lo[w], hi[w], vresp_row(P.n_blocks)};
+        cudaError_t e;
+        if (nt == 51)
+            e = ext ? launch_fp64_vresp_t<51, true>(P, W, vresp, ext, partials, estore, carry, s)
+                    : launch_fp64_vresp_t<51, false>(P, W, vresp, ext, partials, estore, carry, s);
+        else if (nt == 61)
+            e = ext ? launch_fp64_vresp_t<61, true>(P, W, vresp, ext, partials, estore, carry, s)
+                    : launch_fp64_vresp_t<61, false>(P, W, vresp, ext, partials, estore, carry, s);
+        else
+            return cudaErrorInvalidValue;
+        if (e != cudaSuccess) return e;
+        if (launches) ++*launches;
+    }
+    return cudaSuccess;
 }
 
-size_t response_table_vol_elems(int stride, int n_blocks) { return (size_t)n_blocks * stride * kRespRow * 3; }
+// Slots per row of the volatility-table response table: every date 2 .. B in
+// its global slot B - j, and the last group of four a window reads (up to
+// slot B + 1) within the row.
+int vresp_row(int n_blocks) { return n_blocks + 2 <= kRespRow ? kRespRow : (n_blocks + 2 + 3) / 4 * 4; }
+
+size_t response_table_vol_elems(int stride, int n_blocks)
+{
+    return (size_t)n_blocks * stride * vresp_row(n_blocks) * 3;
+}
 
 cudaError_t launch_response_table_vol(int nt, double c, int stride, int n_blocks, bool pc, const double* sv,
                                       float4* vresp, cudaStream_t s)
 {
-    if (nt < 3 || nt > kMaxTenor || n_blocks > kRespDates || n_blocks >= nt || stride < 1) return cudaErrorInvalidValue;
+    if (nt < 3 || nt > kMaxTenor || n_blocks >= nt || stride < 1) return cudaErrorInvalidValue;
     VolLoadings S;
     std::memset(&S, 0, sizeof(S));
     for (int k = 0; k < kFactors; ++k)
         for (int t = 0; t < nt; ++t) S.sv[k][t] = sv[k * kMaxTenor + t];
-    response_table_vol_kernel<<<1, kMaxTenor, 0, s>>>(nt, c, stride, n_blocks, pc ? 1 : 0, S, vresp);
+    response_table_vol_kernel<<<1, kMaxTenor, 0, s>>>(nt, c, stride, n_blocks, vresp_row(n_blocks), pc ? 1 : 0, S,
+                                                      vresp);
     return cudaGetLastError();
 }
 

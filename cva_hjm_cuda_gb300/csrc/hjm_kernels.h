@@ -61,11 +61,17 @@ constexpr int kFormPolyTri = 2;  // ... with factor k of degree <= k
 cudaError_t launch_path_fp64(int nt, const PathParams<double>& P, bool poly, const double* ext, double* partials,
                              double* estore, cudaStream_t s);
 int response_max_dates();
-// The response form of the volatility-table step (FP64, either scheme: the
-// table carries the scheme): vresp from launch_response_table_vol with the
-// kernel's loadings sv [kFactors][kMaxTenor] (PathParams::sv)
+// The response form of the volatility-table step (FP64 accuracy, either
+// scheme: the table carries the scheme): vresp from launch_response_table_vol
+// with the kernel's loadings sv [kFactors][kMaxTenor] (PathParams::sv); one
+// launch per window of at most kRespSlots dates (vresp_windows of them),
+// carry [2][n_paths] doubles when there is more than one; *launches: kernels
+// enqueued.
 cudaError_t launch_path_fp64_vresp(int nt, const PathParams<double>& P, const float4* vresp, const double* ext,
-                                   double* partials, double* estore, cudaStream_t s);
+                                   double* partials, double* estore, double* carry, cudaStream_t s,
+                                   int* launches = nullptr);
+int vresp_windows(int n_blocks);
+int vresp_row(int n_blocks);                                // slots per table row
 size_t response_table_vol_elems(int stride, int n_blocks);  // float4 entries
 cudaError_t launch_response_table_vol(int nt, double c, int stride, int n_blocks, bool pc, const double* sv,
                                       float4* vresp, cudaStream_t s);

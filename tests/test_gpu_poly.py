@@ -344,15 +344,14 @@ def test_remainder_form_choice_and_limits(engine, remainder_form, tmp_path):
     remainder_form("convect")
     engine.run(cfg30, "fp64")
     assert engine.remainder_form() == "convect"
-    # the volatility-table response form holds at most 24 dates
+    # the volatility-table response form: 60 dates in windows as well
     engine.set_market(_bumpy_market(61))
     remainder_form("response")
-    with pytest.raises(_lib.HJMError) as ei:
-        engine.run(cfg30, "fp64")
-    assert "24 dates" in str(ei.value)
+    engine.run(cfg30, "fp64")
+    assert engine.remainder_form() == "response"
     remainder_form("auto")
     engine.run(cfg30, "fp64")
-    assert engine.remainder_form() == "convect"
+    assert engine.remainder_form() == "response"
     engine.set_market(Market(vol=Market().vol * (1.0 + 0.1 * np.cos(np.arange(51) / 7.0))[None, :]))
     engine.set_swap(Swap())
     remainder_form("auto")
@@ -434,6 +433,48 @@ def test_table_step_response_shapes_vs_oracle(engine, remainder_form, n_paths, n
     cva, _ = O.cva(ee, nd + 1, mk.dtau, cfg.hazard, cfg.recovery)
     _assert_rel(v.ee[:nd + 1], ee[:nd + 1], FP64_RTOL, "EE")
     _assert_rel(v.cva, cva, FP64_RTOL, "CVA")
+
+
+@pytest.mark.parametrize("scheme", ["euler", "predictor_corrector"])
+@pytest.mark.parametrize("nt,n_steps", [(51, 2500), (61, 3000)], ids=["25y-51-tenors", "30y-61-tenors"])
+def test_table_step_response_windows_vs_convected_and_oracle(engine, remainder_form, scheme, nt, n_steps):
+    """More than 24 dates on a table of any shape: the response form prices
+    them in windows of 24 (the latest first, the earlier ones taking the later
+    cash flows per path); per-path exposures against the all-FP64 convected
+    table step (1e-11) and the oracle (1e-10), both absolutely below 5e-13 of
+    the scale (over 50 or 60 dates the FP64 forms themselves differ by ~1e-13
+    of it)."""
+    mk = _bumpy_market(nt)
+    sw = Swap(n_tenor=nt, n_periods=n_steps // 50)
+    engine.set_scheme(scheme)
+    try:
+        engine.set_market(mk)
+        engine.set_swap(sw)
+        assert engine.vol_form() == "table"
+        cfg = RunConfig(n_paths=129, n_steps=n_steps, seed=41)
+        out = {}
+        engine.keep_exposures(True)
+        for form in ("convect", "response"):
+            remainder_form(form)
+            out[form] = (engine.run(cfg, "fp64"), engine.exposures())
+            assert engine.remainder_form() == form
+        remainder_form("auto")
+        normals = engine.dump_normals(cfg.n_paths, cfg.n_steps, cfg.seed)
+        ext = engine.run_with_normals(normals, cfg.n_steps, cfg.dt, "fp64")
+    finally:
+        engine.keep_exposures(False)
+        engine.set_scheme("euler")
+    (vc, xc), (vr, xr) = out["convect"], out["response"]
+    nd = n_steps // 50 + 1
+    _assert_rel(xr[:nd], xc[:nd], 1e-11, "exposures response vs convect", floor=5e-13)
+    paths = O.exposure_paths_pc if scheme == "predictor_corrector" else O.exposure_paths
+    x = paths(mk, sw, cfg.n_steps, cfg.dt, normals)
+    ee = O.expected_exposure(x)
+    cva, _ = O.cva(ee, nd, mk.dtau, cfg.hazard, cfg.recovery)
+    _assert_rel(xr[:nd], x[:, :nd].T, FP64_RTOL, "exposures vs oracle", floor=5e-13)
+    _assert_rel(vr.ee[:nd], ee[:nd], FP64_RTOL, "EE vs oracle")
+    _assert_rel(vr.cva, cva, FP64_RTOL, "CVA vs oracle")
+    np.testing.assert_array_equal(ext.ee, vr.ee)
 
 
 def test_response_tables_follow_shape_market_and_scheme(engine):
