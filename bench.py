@@ -522,6 +522,12 @@ def run_ours(args) -> None:
         bound = "fp32_pipe (double-FP32)"
         fma_busy = profiled_value("fma_pipe_cycles_active", f"{args.workload}-{n_paths}")
         side = {"pipe": "fp64 (parts at the sampled dates)", "note": "see the headline workload"}
+    elif prec == "fp64" and remainder == "response" and form == "table":
+        # the table step's response sums, double-FP32 on the FP32 pipe
+        flops = table_response_fp32_flops_per_path(mk.n_tenor, n_steps, stride) * n_paths
+        achieved = flops / (path_ms * 1e-3) / 1e12
+        peak = extras.get("measured_fma_peak_tflops", {}).get("fp32")
+        bound = "fp32_pipe (double-FP32)"
     elif prec == "fp64" and remainder == "response" and form != "table" and not is_adjoint:
         # the per-step work is double-FP32 on the FP32 pipe: that is the
         # roofline; the FP64 pipe only forms the parts at the sampled dates
@@ -604,7 +610,9 @@ def run_ours(args) -> None:
                                    "exposures within ~2e-13 of the exposure scale of the all-FP64 step "
                                    "(fp64_convected_form), EE and CVA within 1e-10 of the FP64 oracle"
                                    if form != "table" else
-                                   "FP64 (the factors' impulse responses, value and running sum, per date)")
+                                   "FP64 deterministic curve, pricing, discounting and reductions; per step the "
+                                   "three factors' impulse-response sums (value and running sum per date) in "
+                                   "double-FP32 (48-bit) on the FP32 pipe")
                                   if remainder == "response" and prec == "fp64" else None),
                    "path_step": ("one Euler step of one path's whole tenor curve, the reference's unit; the "
                                  "response form computes the same values by exact algebra without evolving every "
