@@ -131,20 +131,18 @@ hjm_status hjm_ctx_vol_decomposition(hjm_ctx* ctx, int32_t* active);
  * responses of the convection (HJM_REMAINDER_RESPONSE: one double-FP32 term
  * per such date per step, on the FP32 pipe; the remainder is ~1e-5 of the
  * curve; the polynomial parts S, U, W then advance as double-FP32 sums in a
- * moving frame, with FP64 only at the sampled dates).  The Euler step's
- * response form takes any number of dates: a run with more than
+ * moving frame, with FP64 only at the sampled dates).  With a volatility
+ * table of any shape (no decomposition) the whole stochastic curve is either
+ * convected with the noise injected at every tenor (four FP64 FMAs per live
+ * tenor per step), or carried in the response form as double-FP32 sums of
+ * the three factors' impulse responses (three terms per date per step).
+ * Every response form takes any number of dates: a run with more than
  * HJM_RESPONSE_MAX_DATES is priced in windows of at most that many dates, one
  * launch each, the later windows passing each path's later cash flows to the
- * earlier ones.  With a volatility table of any shape (no decomposition) the
- * whole stochastic curve is either convected with the noise injected at every
- * tenor, or carried in the response form as sums of the three factors'
- * impulse responses (six FP64 FMAs per date per step); that form, and the
- * predictor-corrector's, hold at most HJM_RESPONSE_MAX_DATES dates (a run with
- * more fails with HJM_ERR_INVALID_ARGUMENT when it is forced).
- * HJM_REMAINDER_AUTO (default) takes the response form for the Euler step
- * with a decomposition, else the form with fewer FP64 operations for the run.
- * Both time schemes; the forms agree to rounding; mixed precision always
- * convects.  The report names the form a valuation ran ("remainder"). */
+ * earlier ones.  HJM_REMAINDER_AUTO (default) takes the response form for
+ * every FP64 valuation.  Both time schemes; the forms agree to rounding
+ * (per-path exposures within ~1e-13 of the exposure scale); mixed precision
+ * always convects.  The report names the form a valuation ran ("remainder"). */
 #define HJM_REMAINDER_AUTO 0
 #define HJM_REMAINDER_CONVECT 1
 #define HJM_REMAINDER_RESPONSE 2
