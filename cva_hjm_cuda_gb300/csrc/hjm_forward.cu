@@ -558,8 +558,15 @@ inline bool mixed_compact(int nt, int n_blocks, bool poly)
 // (12 warps) for the 61-tenor netting set (36.5 ms from 37.1); a 25y swap on
 // 51 tenors keeps 16 warps either way.  Otherwise the registers bound it,
 // whatever the CTA size.
+// The table step keeps FP64 sums per tenor (no compact form without the
+// parts), so with many dates its shared memory binds the same way (25y on 51
+// tenors: 79 KB per CTA of 128, 2 per SM; 5 of 64, 10 warps instead of 8).
 constexpr int kMixedCompactCta = 64;
-inline int mixed_cta(bool cmp) { return cmp ? kMixedCompactCta : kCta; }
+inline int mixed_cta(int nt, int n_blocks, bool poly)
+{
+    if (mixed_compact(nt, n_blocks, poly)) return kMixedCompactCta;
+    return mixed_smem_bytes(nt, n_blocks, false) > (size_t)228 * 1024 / 4 ? kMixedCompactCta : kCta;
+}
 
 void pack_mixed_params(int nt, const PathParams<float>& P, MixedParams& M)
 {
@@ -997,11 +1004,13 @@ static cudaError_t launch_mixed_t(const MixedParams& M, const double* ext, doubl
                                   cudaStream_t s)
 {
     const bool cmp = mixed_compact(NT, M.P.n_blocks, POLY);
-    const int cta = mixed_cta(cmp);
+    const int cta = mixed_cta(NT, M.P.n_blocks, POLY);
     const size_t smem = mixed_smem_bytes(NT, M.P.n_blocks, cmp, cta);
     auto k = path_kernel_mixed<NT, EXT, POLY, false, kCta>;
     if constexpr (POLY) {
         if (cmp) k = path_kernel_mixed<NT, EXT, true, true, kMixedCompactCta>;
+    } else {
+        if (cta == kMixedCompactCta) k = path_kernel_mixed<NT, EXT, false, false, kMixedCompactCta>;
     }
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -1037,7 +1046,7 @@ size_t path_smem(int nt, int n_blocks, bool mixed)
 
 int path_cta(bool mixed, int nt, int n_blocks, bool poly)
 {
-    return mixed ? mixed_cta(mixed_compact(nt, n_blocks, poly)) : kFp64Cta;
+    return mixed ? mixed_cta(nt, n_blocks, poly) : kFp64Cta;
 }
 
 cudaError_t launch_reduce(const double* partials, int64_t n_rows, int R, double* sums, const FinalParams& F,
