@@ -958,6 +958,32 @@ static hjm_status enqueue_eresp(hjm_ctx* ctx, const RunShape& sh, double dt, con
     return HJM_OK;
 }
 
+// Mixed precision on a market whose factors are cubics up to a residual
+// (hjm_set_market's fit): the cubic polynomial form of the mixed kernel, in
+// powers of t = T - tau0 about the middle of the sampled tenors (the cubic's
+// terms cancel least there), the fit re-expanded on the host in FP64 and
+// rounded to FP32.  The residual, at most 2^-20 of each factor's scale by the
+// fit's rule (1.1e-7 for the reference driver's PCA table: two FP32 ulps of
+// the loadings, which the table step rounds to half an ulp), is left out: an
+// input perturbation of that size, far inside the mixed precision's 1e-4.
+static void fill_mixed_cubic(const hjm_ctx* ctx, const RunShape& sh, double dt, MixedParams& M)
+{
+    const double dtau = ctx->dtau, c = dt / dtau, sq = std::sqrt(dt);
+    const double TL = dtau * (ctx->nt - 1);
+    const double tau0 = eresp_window_centre(dtau, 1, sh.B);
+    const double dl = tau0 - TL;  // sum_e a_e (T - T_L)^e = sum_d a'_d (T - tau0)^d
+    for (int k = 0; k < kFactors; ++k) {
+        const double* a = ctx->cubic[k];
+        const double sh4[4] = {a[0] + dl * (a[1] + dl * (a[2] + dl * a[3])), a[1] + dl * (2.0 * a[2] + 3.0 * dl * a[3]),
+                               a[2] + 3.0 * dl * a[3], a[3]};
+        for (int d = 0; d < 3; ++d) M.svcf[k][d] = (float)(sq * sh4[d]);
+        M.svcx[k] = (float)(sq * sh4[3]);
+    }
+    M.k3f = (float)(c * dtau * dtau * dtau);
+    M.src3f = (float)(3.0 * (TL - tau0));
+    for (int t = 0; t < ctx->nt; ++t) M.P.tau[t] = (float)(dtau * t - tau0);
+}
+
 // The volatility-table step in the response form (its table already on the
 // stream): the carry of a windowed run, one launch per window.
 static hjm_status enqueue_vresp(hjm_ctx* ctx, const RunShape& sh, const PathParams<double>& P, const double* ext_dev,
@@ -989,7 +1015,9 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
     const int n_dates = sh.B + 1;
     const int R = sh.B + 3;
     const bool pc = ctx->scheme == HJM_SCHEME_PREDICTOR_CORRECTOR;
-    const int cta = pc ? pc_cta() : path_cta(mixed, ctx->nt, sh.B, use_poly_path(ctx));
+    // a cubic market in mixed precision (Euler): the cubic polynomial form
+    const bool mixed_cubic = mixed && !pc && use_cubic_path(ctx);
+    const int cta = pc ? pc_cta() : path_cta(mixed, ctx->nt, sh.B, use_poly_path(ctx) || mixed_cubic);
     const int64_t n_ctas = (n_paths + cta - 1) / cta;
     const int64_t ld = (n_paths + 3) / 4 * 4;
     const size_t esize = mixed ? 4 : 8;
@@ -1015,7 +1043,8 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
     HJM_CUDA(ctx, cudaEventRecord(ctx->ev[0], s));
     bool resp = false;
     // the volatility form this run takes (vol_form_code's values): a cubic
-    // market runs its decomposition in the FP64 Euler response form only
+    // market runs its decomposition in the Euler step only (FP64: the response
+    // form with the residual; mixed precision: the cubic polynomial form)
     int run_form = use_poly_path(ctx) ? vol_form_code(ctx) : 0;
     if (pc && mixed) {
         PathParams<float> P;
@@ -1052,8 +1081,12 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
         fill_params<float>(ctx, sh, n_paths, dt, seed, path_offset, hazard, recovery, ld, store, P, F);
         MixedParams M;
         pack_mixed_params(ctx->nt, P, M);
+        if (mixed_cubic) {
+            fill_mixed_cubic(ctx, sh, dt, M);
+            run_form = vol_form_code(ctx);
+        }
         HJM_CUDA(ctx, launch_path_mixed(ctx->nt, M, use_poly_path(ctx), ext_dev, (double*)ctx->partials.p,
-                                        store ? (float*)ctx->estore.p : nullptr, s));
+                                        store ? (float*)ctx->estore.p : nullptr, s, mixed_cubic));
     } else {
         PathParams<double> P;
         fill_params<double>(ctx, sh, n_paths, dt, seed, path_offset, hazard, recovery, ld, store, P, F);

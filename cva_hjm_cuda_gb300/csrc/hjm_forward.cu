@@ -451,12 +451,13 @@ __global__ void __launch_bounds__(kMaxTenor)
 // warps) the polynomial form does not spill but ran slower (20.8 ms against
 // 20.5 at 4,194,304 paths); the compact sums' 64-thread CTAs are bounded by
 // shared memory first (7 per SM for the netting set).
-template <int NT, bool EXT, bool POLY, bool CMP, int C>
+template <int NT, bool EXT, bool POLY, bool CMP, int C, bool CUB = false>
 __global__ void __launch_bounds__(C, 512 / C)
     path_kernel_mixed(const __grid_constant__ MixedParams M, const double* __restrict__ ext,
                       double* __restrict__ partials, float* __restrict__ estore)
 {
     static_assert(!CMP || POLY, "the compact sums need the polynomial parts");
+    static_assert(!CUB || POLY, "the cubic part extends the polynomial form");
     using Acc = typename std::conditional<CMP, float, double>::type;
     const PathParams<float>& P = M.P;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -468,14 +469,14 @@ __global__ void __launch_bounds__(C, 512 / C)
     float* hs_s = reinterpret_cast<float*>(smem + (size_t)rows * C * ka);  // [B+2][C]
     double* red_s = reinterpret_cast<double*>(
         smem + (((size_t)rows * C * ka + (size_t)(rows + 1) * C * 4 + 7) & ~(size_t)7));
-    double zS = 0.0, zU = 0.0, zW = 0.0;  // CMP: FP64 running sums of the parts over the evolved steps
+    double zS = 0.0, zU = 0.0, zW = 0.0, zX = 0.0;  // CMP: FP64 running sums of the parts over the evolved steps
 
     const int64_t cta_base = (int64_t)blockIdx.x * C;
     const int64_t lp = cta_base + tid;
     const bool active = lp < P.n_paths;
     const uint64_t gpath = P.path_offset + (uint64_t)lp;
 
-    MixedPath<NT, POLY> x;
+    MixedPath<NT, POLY, CUB> x;
     x.reset();
     for (int i = 0; i < rows; ++i) acc_s[i * C + tid] = Acc(0);
     for (int t = 0; t <= B + 1; ++t) hs_s[t * C + tid] = 0.f;
@@ -485,7 +486,7 @@ __global__ void __launch_bounds__(C, 512 / C)
         double a = P.psum[i] + as_f64(acc_s[i * C + tid]);
         if constexpr (CMP) {
             const double ti = (double)P.tau[i];
-            a += fma(ti, fma(ti, zW, zU), zS);
+            a += CUB ? fma(ti, fma(ti, fma(ti, zX, zW), zU), zS) : fma(ti, fma(ti, zW, zU), zS);
         }
         const float D = expf((float)(-a * P.dt));
         const float mm = (float)P.m;
@@ -522,6 +523,7 @@ __global__ void __launch_bounds__(C, 512 / C)
             zS += as_f64(bs.sS);
             zU += as_f64(bs.sU);
             zW += as_f64(bs.sW);
+            if constexpr (CUB) zX += as_f64(bs.sX);
         } else {
             block_sums_up<NT, POLY>(x, hs_s, tid, C, P, bs, B, [&](int t, float Ht) {
                 if (t > b) acc_s[t * C + tid] += as_f64(Ht);
@@ -999,16 +1001,16 @@ cudaError_t launch_response_table_vol(int nt, double c, int stride, int n_blocks
 
 int response_max_dates() { return kRespDates; }
 
-template <int NT, bool EXT, bool POLY>
+template <int NT, bool EXT, bool POLY, bool CUB = false>
 static cudaError_t launch_mixed_t(const MixedParams& M, const double* ext, double* partials, float* estore,
                                   cudaStream_t s)
 {
     const bool cmp = mixed_compact(NT, M.P.n_blocks, POLY);
     const int cta = mixed_cta(NT, M.P.n_blocks, POLY);
     const size_t smem = mixed_smem_bytes(NT, M.P.n_blocks, cmp, cta);
-    auto k = path_kernel_mixed<NT, EXT, POLY, false, kCta>;
+    auto k = path_kernel_mixed<NT, EXT, POLY, false, kCta, CUB>;
     if constexpr (POLY) {
-        if (cmp) k = path_kernel_mixed<NT, EXT, true, true, kMixedCompactCta>;
+        if (cmp) k = path_kernel_mixed<NT, EXT, true, true, kMixedCompactCta, CUB>;
     } else {
         if (cta == kMixedCompactCta) k = path_kernel_mixed<NT, EXT, false, false, kMixedCompactCta>;
     }
@@ -1020,9 +1022,11 @@ static cudaError_t launch_mixed_t(const MixedParams& M, const double* ext, doubl
 }
 
 template <int NT>
-static cudaError_t launch_mixed_nt(const MixedParams& M, bool poly, const double* ext, double* partials,
+static cudaError_t launch_mixed_nt(const MixedParams& M, bool poly, bool cub, const double* ext, double* partials,
                                    float* estore, cudaStream_t s)
 {
+    if (cub) return ext ? launch_mixed_t<NT, true, true, true>(M, ext, partials, estore, s)
+                        : launch_mixed_t<NT, false, true, true>(M, ext, partials, estore, s);
     if (ext) return poly ? launch_mixed_t<NT, true, true>(M, ext, partials, estore, s)
                          : launch_mixed_t<NT, true, false>(M, ext, partials, estore, s);
     return poly ? launch_mixed_t<NT, false, true>(M, ext, partials, estore, s)
@@ -1030,10 +1034,10 @@ static cudaError_t launch_mixed_nt(const MixedParams& M, bool poly, const double
 }
 
 cudaError_t launch_path_mixed(int nt, const MixedParams& M, bool poly, const double* ext, double* partials,
-                              float* estore, cudaStream_t s)
+                              float* estore, cudaStream_t s, bool cub)
 {
-    if (nt == 51) return launch_mixed_nt<51>(M, poly, ext, partials, estore, s);
-    if (nt == 61) return launch_mixed_nt<61>(M, poly, ext, partials, estore, s);
+    if (nt == 51) return launch_mixed_nt<51>(M, poly || cub, cub, ext, partials, estore, s);
+    if (nt == 61) return launch_mixed_nt<61>(M, poly || cub, cub, ext, partials, estore, s);
     return cudaErrorInvalidValue;
 }
 

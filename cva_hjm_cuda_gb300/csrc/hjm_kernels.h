@@ -45,8 +45,12 @@ struct MixedParams {
     float2 svp[kFactors][kMaxTenor / 2];
     float2 rp;  // {rr, rr}: the growth-scaled upwind coefficient
     // polynomial volatility in FP32: sqrt(dt) sigma_k(T) = sum_d svcf[k][d] T^d
+    // (+ svcx[k] T^3 for a cubic, T then the tenor minus the basis centre)
     float svcf[kFactors][3];
     float k1f, k2f;  // c dtau, c dtau^2
+    float svcx[kFactors];
+    float k3f;       // c dtau^3
+    float src3f;     // 3 (T_L - centre): the cubic's share of the remainder's source
 };
 
 
@@ -75,8 +79,10 @@ int vresp_row(int n_blocks);                                // slots per table r
 size_t response_table_vol_elems(int stride, int n_blocks);  // float4 entries
 cudaError_t launch_response_table_vol(int nt, double c, int stride, int n_blocks, bool pc, const double* sv,
                                       float4* vresp, cudaStream_t s);
+// cub: the cubic polynomial form (MixedParams::svcx, k3f, src3f; P.tau the
+// tenors minus the basis centre), which implies poly
 cudaError_t launch_path_mixed(int nt, const MixedParams& M, bool poly, const double* ext, double* partials,
-                              float* estore, cudaStream_t s);
+                              float* estore, cudaStream_t s, bool cub = false);
 void pack_mixed_params(int nt, const PathParams<float>& P, MixedParams& M);
 bool path_tenor_supported(int nt);
 size_t path_smem(int nt, int n_blocks, bool mixed);

@@ -140,12 +140,17 @@ __device__ __forceinline__ void convect_pairs(float2 (&h)[PairGrid<NT>::H], cons
 // curve h itself.  Polynomial volatility (POLY, degree <= 2): h = S 1 + U T +
 // W T^2 + hc, with the packed hc only convected (see the FP64 kernel for the
 // algebra: A 1 = 1, A T = T + c dtau 1, A T^2 = T^2 + 2 c dtau T + c dtau^2 1
-// - 2 c dtau^2 e_L).
-template <int NT, bool POLY>
+// - 2 c dtau^2 e_L).  CUB (a table that is a cubic up to a residual below
+// FP32's resolution of it, such as the reference driver's own PCA table): a
+// fourth part X of T^3, with T the tenor minus the basis centre (P.tau holds
+// it), A T^3 = T^3 + 3 c dtau T^2 + 3 c dtau^2 T + c dtau^3 1 in the interior,
+// and the remainder's source at the last tenor -2 c dtau^2 (W + 3 T_L X).
+template <int NT, bool POLY, bool CUB = false>
 struct MixedPath {
+    static_assert(!CUB || POLY, "the cubic part extends the polynomial form");
     static constexpr int H = PairGrid<NT>::H;
     float2 h[H];  // v = h / g (POLY: the convected remainder hc, scaled alike)
-    float S, U, W;
+    float S, U, W, X;
     float g;      // (1 + rr)^-n', n' = steps evolved so far
     float ig;     // (1 + rr)^n' (POLY: times -2 c dtau^2, the source per unit W)
 
@@ -153,7 +158,7 @@ struct MixedPath {
     {
 #pragma unroll
         for (int p = 0; p < H; ++p) h[p] = make_float2(0.f, 0.f);
-        S = U = W = 0.f;
+        S = U = W = X = 0.f;
         g = ig = 1.f;
     }
     // the scales at the start of block b, from the table (no drift across blocks)
@@ -166,13 +171,19 @@ struct MixedPath {
     {
         ig *= M.P.ip;
         if constexpr (POLY) {
-            convect_pairs<NT>(h, M, ig * W);
-            // the noise projection folded into the updates (old U, W on the right)
+            convect_pairs<NT>(h, M, ig * (CUB ? fmaf(M.src3f, X, W) : W));
+            // the noise projection folded into the updates (old U, W, X on the right)
             float Sn = fmaf(M.svcf[0][0], phi0, fmaf(M.k2f, W, fmaf(M.k1f, U, S)));
+            if constexpr (CUB) Sn = fmaf(M.k3f, X, Sn);
             Sn = fmaf(M.svcf[2][0], phi2, fmaf(M.svcf[1][0], phi1, Sn));
             float Un = fmaf(M.svcf[1][1], phi1, fmaf(M.svcf[0][1], phi0, fmaf(2.0f * M.k1f, W, U)));
+            if constexpr (CUB) Un = fmaf(3.0f * M.k2f, X, Un);
             Un = fmaf(M.svcf[2][1], phi2, Un);
-            const float Wn = fmaf(M.svcf[2][2], phi2, fmaf(M.svcf[1][2], phi1, fmaf(M.svcf[0][2], phi0, W)));
+            float Wn = fmaf(M.svcf[2][2], phi2, fmaf(M.svcf[1][2], phi1, fmaf(M.svcf[0][2], phi0, W)));
+            if constexpr (CUB) {
+                Wn = fmaf(3.0f * M.k1f, X, Wn);
+                X = fmaf(M.svcx[2], phi2, fmaf(M.svcx[1], phi1, fmaf(M.svcx[0], phi0, X)));
+            }
             S = Sn;
             U = Un;
             W = Wn;
@@ -181,11 +192,16 @@ struct MixedPath {
         }
         g *= M.P.qm;
     }
+    // the polynomial part at basis coordinate t
+    __device__ __forceinline__ float poly(float t) const
+    {
+        return CUB ? fmaf(t, fmaf(t, fmaf(t, X, W), U), S) : fmaf(t, fmaf(t, W, U), S);
+    }
     // tenor i (runtime) of the stochastic curve
     __device__ __forceinline__ float value(const PathParams<float>& P, int i) const
     {
         float v = g * select_pair<NT>(h, i);
-        if (POLY) v += fmaf(P.tau[i], fmaf(P.tau[i], W, U), S);
+        if (POLY) v += poly(P.tau[i]);
         return v;
     }
     // tenor t (compile-time after unrolling) of the stochastic curve without
@@ -195,15 +211,16 @@ struct MixedPath {
 
 // Running sums over a block (or a partial block) of steps for the recovery.
 struct BlockSums {
-    float F0, F1, F2, H1, sS, sU, sW;
-    __device__ __forceinline__ void reset() { F0 = F1 = F2 = H1 = sS = sU = sW = 0.f; }
-    template <int NT, bool POLY>
-    __device__ __forceinline__ void add(const MixedPath<NT, POLY>& x, float phi0, float phi1, float phi2)
+    float F0, F1, F2, H1, sS, sU, sW, sX;
+    __device__ __forceinline__ void reset() { F0 = F1 = F2 = H1 = sS = sU = sW = sX = 0.f; }
+    template <int NT, bool POLY, bool CUB>
+    __device__ __forceinline__ void add(const MixedPath<NT, POLY, CUB>& x, float phi0, float phi1, float phi2)
     {
         if constexpr (POLY) {
             sS += x.S;
             sU += x.U;
             sW += x.W;
+            if constexpr (CUB) sX += x.X;
         } else {
             F0 += phi0;
             F1 += phi1;
@@ -211,18 +228,24 @@ struct BlockSums {
         }
         H1 = fmaf(x.g, x.h[1].x, H1);
     }
+    // the block sums of the polynomial part at basis coordinate t
+    template <bool CUB>
+    __device__ __forceinline__ float poly(float t) const
+    {
+        return CUB ? fmaf(t, fmaf(t, fmaf(t, sX, sW), sU), sS) : fmaf(t, fmaf(t, sW, sU), sS);
+    }
 };
 
 // Block sums of tenors 2 .. tmax of the stochastic curve over the steps the
 // sums cover (upward recovery from tenor 1 plus, POLY, the scalar parts);
 // fold(t, sum) is called for t = 2 .. tmax.
-template <int NT, bool POLY, typename Fold>
-__device__ __forceinline__ void block_sums_up(const MixedPath<NT, POLY>& x, const float* hs_s, int tid, int cta,
+template <int NT, bool POLY, bool CUB, typename Fold>
+__device__ __forceinline__ void block_sums_up(const MixedPath<NT, POLY, CUB>& x, const float* hs_s, int tid, int cta,
                                               const PathParams<float>& P, const BlockSums& bs, int tmax, Fold fold)
 {
     if constexpr (POLY) {
         recover_sums_up<NT>(x.h, hs_s, tid, cta, P, x.g, 0.f, 0.f, 0.f, bs.H1, tmax, [&](int t, float Ht) {
-            fold(t, Ht + fmaf(P.tau[t], fmaf(P.tau[t], bs.sW, bs.sU), bs.sS));
+            fold(t, Ht + bs.poly<CUB>(P.tau[t]));
         });
     } else {
         recover_sums_up<NT>(x.h, hs_s, tid, cta, P, x.g, bs.F0, bs.F1, bs.F2, bs.H1, tmax, fold);

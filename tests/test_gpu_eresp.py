@@ -170,15 +170,40 @@ def test_windows_on_external_double_normals(engine):
     _assert_rel(v.ee, ee, FP64_RTOL, "EE")
 
 
-def test_cubic_market_other_modes_run_the_table_step(engine):
-    """Mixed precision and the predictor-corrector scheme take the table step on the
-    driver's table, at their own tolerances."""
-    mk, sw = _own_market()
+@pytest.mark.parametrize("shape", ["10y-synthetic-swap", "25y-driver-swap"])
+def test_cubic_market_mixed_precision_vs_fp64_and_oracle(engine, shape, tmp_path):
+    """Mixed precision on the driver's table runs the cubic polynomial form (its
+    residual, 1.1e-7 of the factors' scale, left out): EE and CVA within 1e-4 of
+    the FP64 run on the same paths, per-path exposures within 1e-4 of the
+    exposure scale from the oracle on the full table.  The predictor-corrector
+    scheme takes the table step on such a market."""
+    import json
+
+    mk, drv = _own_market()
+    sw, n_steps = (Swap(), 1000) if shape.startswith("10y") else (drv, 2500)
     engine.set_market(mk)
     engine.set_swap(sw)
-    cfg = RunConfig(n_paths=2000, n_steps=2500, dt=0.01, seed=4)
+    cfg = RunConfig(n_paths=2000, n_steps=n_steps, dt=0.01, seed=4)
+    nd = n_steps // 50
     f64 = engine.run(cfg, "fp64")
-    mx = engine.run(cfg, "mixed")
+    engine.keep_exposures(True)
+    try:
+        mx = engine.run(cfg, "mixed")
+        x = engine.exposures()
+    finally:
+        engine.keep_exposures(False)
     assert engine.remainder_form() == "convect"
-    np.testing.assert_allclose(mx.ee[:50], f64.ee[:50], rtol=1e-4)
+    engine.write_report(tmp_path / "r.json")
+    assert json.loads((tmp_path / "r.json").read_text())["run"]["vol_form"] == "cubic_resid"
+    np.testing.assert_allclose(mx.ee[:nd], f64.ee[:nd], rtol=1e-4)
     assert abs(mx.cva - f64.cva) <= 1e-4 * f64.cva
+    normals = engine.dump_normals(cfg.n_paths, cfg.n_steps, cfg.seed)
+    xo = O.exposure_paths(mk, sw, cfg.n_steps, cfg.dt, normals)[:, :nd + 1].T
+    assert np.max(np.abs(x - xo)) <= 1e-4 * np.max(np.abs(xo))
+    engine.set_scheme("predictor_corrector")
+    try:
+        engine.run(cfg, "mixed")
+        engine.write_report(tmp_path / "p.json")
+        assert json.loads((tmp_path / "p.json").read_text())["run"]["vol_form"] == "table"
+    finally:
+        engine.set_scheme("euler")
