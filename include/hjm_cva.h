@@ -113,9 +113,11 @@ hjm_status hjm_ctx_set_scheme(hjm_ctx* ctx, int32_t scheme);
  * each factor up to a residual of at most 2^-20 of the factor's scale (a PCA
  * table printed to a fixed number of decimals, as the reference's own
  * simulation_gpu_testing.cpp:47-63, whose factors 2 and 3 are cubics to
- * 1.1e-7) runs, in FP64 Euler valuations, the cubic decomposition in the
- * basis (T - T_L)^d with the residual's impulse responses carried beside the
- * remainder's (other modes run the table step on it).
+ * 1.1e-7) runs, in Euler valuations, the cubic decomposition: in FP64 with
+ * the residual's impulse responses carried beside the remainder's, in mixed
+ * precision without the residual (below FP32's resolution of the loadings);
+ * the predictor-corrector scheme, the adjoint, MLMC and hjm_run_static run
+ * the table step on it.
  * hjm_ctx_vol_decomposition reports what the current market runs: 0 the
  * table step, 1 the decomposition, 2 the decomposition with factor k of
  * degree <= k (three zero coefficients), 3 the cubic decomposition with a
