@@ -54,7 +54,7 @@ namespace hjm {
 // together and their FP32 chains interleaved.  The table is zero outside the
 // live nonzero entries, so the slots a group adds beyond n_act add exact
 // zeros (dead or not yet reached dates).
-constexpr int kRespDates = 24;   // dates the response form holds (slots 0 .. 22 for dates 2 .. B)
+constexpr int kRespDates = 24;   // dates a response-form window holds (one launch of hjm_run_static)
 constexpr int kRespSlots = 24;   // accumulator slots, a multiple of the group of 4 (slot 23 stays zero)
 constexpr int kRespRow = 24;     // response-table row: one float4 per slot
 

@@ -119,9 +119,11 @@ class HJMEngine:
         self._check(self.lib.hjm_ctx_set_scheme(self.ctx, {"euler": 0, "predictor_corrector": 1}[scheme]))
 
     def set_remainder_form(self, form: str = "auto") -> None:
-        """FP64 form of the decomposition's remainder: "convect" (over the live
-        tenors every step), "response" (impulse responses at the sampled tenors,
-        at most 24 dates) or "auto" (the cheaper one for the run)."""
+        """FP64 transport form: "convect" (the remainder, or with a table of
+        any shape the whole stochastic curve, over the live tenors every step
+        in FP64), "response" (impulse-response sums at the sampled tenors in
+        double-FP32, in windows of at most 24 dates) or "auto" (the response
+        form)."""
         self._check(self.lib.hjm_ctx_set_remainder_form(self.ctx, {"auto": 0, "convect": 1, "response": 2}[form]))
 
     def remainder_form(self) -> str:
