@@ -779,15 +779,15 @@ int eresp_first_active_date(int nt, double c, int stride, int n_blocks, int nres
     return B + 1;
 }
 
-int eresp_windows(int n_blocks, int first_active, int* lo, int* hi, int* ns)
+int eresp_windows(int n_blocks, int first_active, int* lo, int* hi, int* ns, int max_slots)
 {
     const int f = std::max(first_active, 2);
     int n = 0, h = n_blocks;
     while (h >= 1) {
         // dates of a window [1, h] that can be active: f .. h
         int l = 1;
-        if (h - f + 1 > kRespSlots) {
-            l = h - kRespSlots + 1;
+        if (h - f + 1 > max_slots) {
+            l = h - max_slots + 1;
             if (l <= 2) l = 1;
         }
         const int act = std::max(h - std::max(l, f) + 1, 0);

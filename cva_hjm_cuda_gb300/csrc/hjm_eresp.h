@@ -97,7 +97,9 @@ int eresp_residual_factors(const double* resid, const double* vol, int nt);
 // date when those that can be active number at most kRespSlots, else the
 // kRespSlots latest (a window reaching date 2 takes date 1 too).  ns: the
 // slots the window's kernel holds, 12, 16, 20 or 24, at least its active ones.
-int eresp_windows(int n_blocks, int first_active, int* lo, int* hi, int* ns);
+// max_slots: the dates a window holds (kRespSlots; the volatility-table
+// response form takes 16).
+int eresp_windows(int n_blocks, int first_active, int* lo, int* hi, int* ns, int max_slots = kRespSlots);
 // One launch per window, latest first, window w with frame w (its centre in
 // frames[w].tau0).  degs: the factors' degrees
 // (degs_pack); nres: the table's residual factors; first_active: as

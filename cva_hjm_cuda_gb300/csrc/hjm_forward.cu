@@ -260,8 +260,8 @@ __global__ void __launch_bounds__(kFp64Cta, 4)
 // b stride + s, slot B - j) holds three float4 {R_jk hi, CR_jk hi, R_jk lo,
 // CR_jk lo} at lag (j - b) stride - 1 - s; rows are W.row slots wide.
 //
-// Windows, as the decomposition's response form (hjm_eresp.cu): the
-// kRespSlots register slots hold the dates of one window [lo, hi] (dates
+// Windows, as the decomposition's response form (hjm_eresp.cu): the NS
+// register slots hold the dates of one window [lo, hi] (dates
 // 2 .. hi from max(lo, 2), slot r for date hi - r); a run with more dates is
 // priced in launches over windows, the latest first, each re-running the
 // normals from the first evolved step to date hi and passing the earlier
@@ -271,8 +271,11 @@ struct VrespWindow {
     int row;     // slots per table row (global slot numbering, slot B - j for date j)
 };
 
-template <int NT, bool EXT>
-__global__ void __launch_bounds__(kFp64Cta, 6)
+// NS register slots: 16 (128 registers, 8 CTAs per SM; windows of 16 dates,
+// 6-7% faster than 24 slots at 6 CTAs per SM for 20 to 60 dates) or 24 (one
+// launch for up to 24 dates: hjm_run_static, which has no carry).
+template <int NT, bool EXT, int NS>
+__global__ void __launch_bounds__(kFp64Cta, NS <= 16 ? 8 : 6)
     path_kernel_fp64_vresp(const __grid_constant__ PathParams<double> P, const VrespWindow W,
                            const float4* __restrict__ vresp, const double* __restrict__ ext,
                            double* __restrict__ partials, double* __restrict__ estore, double* __restrict__ carry)
@@ -291,16 +294,16 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
     const uint64_t gpath = P.path_offset + (uint64_t)lp;
 
     // {h at tenor j, its running sum} as hi + lo pairs, slot hi - j
-    float2 A[kRespSlots], Al[kRespSlots];
+    float2 A[NS], Al[NS];
 #pragma unroll
-    for (int r = 0; r < kRespSlots; ++r) A[r] = Al[r] = make_float2(0.0f, 0.0f);
+    for (int r = 0; r < NS; ++r) A[r] = Al[r] = make_float2(0.0f, 0.0f);
     const int roff = B - hi;  // global slot of slot 0
     const int first = lo > 2 ? lo : 2;
 
     auto price = [&](int i) {
         double h = 0.0, hs = 0.0;
         if (i >= 2) {
-            const float2 a = select_reg<kRespSlots, float2>(A, hi - i), l = select_reg<kRespSlots, float2>(Al, hi - i);
+            const float2 a = select_reg<NS, float2>(A, hi - i), l = select_reg<NS, float2>(Al, hi - i);
             h = widen_f32(a.x) + widen_f32(l.x);
             hs = widen_f32(a.y) + widen_f32(l.y);
         }
@@ -330,6 +333,7 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
             const float4* rr = row + (size_t)s * W.row * 3;
             resp_groups(n_act, [&](auto gc) {
                 constexpr int G = decltype(gc)::value;
+                if constexpr (4 * G < NS) {
                 float4 q[4][3];
 #pragma unroll
                 for (int u = 0; u < 4; ++u)
@@ -347,6 +351,7 @@ __global__ void __launch_bounds__(kFp64Cta, 6)
                             df_acc_w(A[4 * G + u], Al[4 * G + u], kh, kl, w, nw);
                     }
                     df_renorm(A[4 * G + u], Al[4 * G + u]);
+                }
                 }
             });
         }
@@ -933,14 +938,14 @@ cudaError_t launch_path_fp64(int nt, const PathParams<double>& P, bool poly, con
     return cudaErrorInvalidValue;
 }
 
-template <int NT, bool EXT>
+template <int NT, bool EXT, int NS>
 static cudaError_t launch_fp64_vresp_t(const PathParams<double>& P, const VrespWindow& W, const float4* vresp,
                                        const double* ext, double* partials, double* estore, double* carry,
                                        cudaStream_t s)
 {
     // cf_s [hi - lo + 3][kCta] (the epilogue's exposures alias it one row up), red_s
     const size_t smem = ((size_t)(W.hi - W.lo + 3) * kFp64Cta + 2 * (kFp64Cta / 32)) * 8;
-    auto k = path_kernel_fp64_vresp<NT, EXT>;
+    auto k = path_kernel_fp64_vresp<NT, EXT, NS>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const int64_t grid = (P.n_paths + kFp64Cta - 1) / kFp64Cta;
@@ -948,28 +953,41 @@ static cudaError_t launch_fp64_vresp_t(const PathParams<double>& P, const VrespW
     return cudaGetLastError();
 }
 
-int vresp_windows(int n_blocks) { return eresp_windows(n_blocks, 2, nullptr, nullptr, nullptr); }
+template <int NS>
+static cudaError_t launch_fp64_vresp_ns(int nt, const PathParams<double>& P, const VrespWindow& W,
+                                        const float4* vresp, const double* ext, double* partials, double* estore,
+                                        double* carry, cudaStream_t s)
+{
+    if (nt == 51)
+        return ext ? launch_fp64_vresp_t<51, true, NS>(P, W, vresp, ext, partials, estore, carry, s)
+                   : launch_fp64_vresp_t<51, false, NS>(P, W, vresp, ext, partials, estore, carry, s);
+    if (nt == 61)
+        return ext ? launch_fp64_vresp_t<61, true, NS>(P, W, vresp, ext, partials, estore, carry, s)
+                   : launch_fp64_vresp_t<61, false, NS>(P, W, vresp, ext, partials, estore, carry, s);
+    return cudaErrorInvalidValue;
+}
+
+int vresp_windows(int n_blocks, int max_slots)
+{
+    return eresp_windows(n_blocks, 2, nullptr, nullptr, nullptr, max_slots);
+}
 
 cudaError_t launch_path_fp64_vresp(int nt, const PathParams<double>& P, const float4* vresp, const double* ext,
-                                   double* partials, double* estore, double* carry, cudaStream_t s, int* launches)
+                                   double* partials, double* estore, double* carry, cudaStream_t s, int* launches,
+                                   int max_slots)
 {
+    if (max_slots != 16 && max_slots != 24) return cudaErrorInvalidValue;
     int lo[kMaxTenor], hi[kMaxTenor];
     // every date is reached at once (the factors load every tenor): windows
-    // of kRespSlots dates from date 2, the latest first
-    const int nw = eresp_windows(P.n_blocks, 2, lo, hi, nullptr);
+    // of max_slots dates from date 2, the latest first
+    const int nw = eresp_windows(P.n_blocks, 2, lo, hi, nullptr, max_slots);
     if (!vresp || (nw > 1 && !carry)) return cudaErrorInvalidValue;
     if (launches) *launches = 0;
     for (int w = 0; w < nw; ++w) {
         const VrespWindow W{lo[w], hi[w], vresp_row(P.n_blocks)};
-        cudaError_t e;
-        if (nt == 51)
-            e = ext ? launch_fp64_vresp_t<51, true>(P, W, vresp, ext, partials, estore, carry, s)
-                    : launch_fp64_vresp_t<51, false>(P, W, vresp, ext, partials, estore, carry, s);
-        else if (nt == 61)
-            e = ext ? launch_fp64_vresp_t<61, true>(P, W, vresp, ext, partials, estore, carry, s)
-                    : launch_fp64_vresp_t<61, false>(P, W, vresp, ext, partials, estore, carry, s);
-        else
-            return cudaErrorInvalidValue;
+        const cudaError_t e = max_slots == 16
+                                  ? launch_fp64_vresp_ns<16>(nt, P, W, vresp, ext, partials, estore, carry, s)
+                                  : launch_fp64_vresp_ns<24>(nt, P, W, vresp, ext, partials, estore, carry, s);
         if (e != cudaSuccess) return e;
         if (launches) ++*launches;
     }

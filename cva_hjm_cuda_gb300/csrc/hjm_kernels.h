@@ -68,13 +68,13 @@ int response_max_dates();
 // The response form of the volatility-table step (FP64 accuracy, either
 // scheme: the table carries the scheme): vresp from launch_response_table_vol
 // with the kernel's loadings sv [kFactors][kMaxTenor] (PathParams::sv); one
-// launch per window of at most kRespSlots dates (vresp_windows of them),
-// carry [2][n_paths] doubles when there is more than one; *launches: kernels
-// enqueued.
+// launch per window of at most max_slots dates (16, or 24 for one launch up
+// to 24 dates; vresp_windows of them), carry [2][n_paths] doubles when there
+// is more than one; *launches: kernels enqueued.
 cudaError_t launch_path_fp64_vresp(int nt, const PathParams<double>& P, const float4* vresp, const double* ext,
                                    double* partials, double* estore, double* carry, cudaStream_t s,
-                                   int* launches = nullptr);
-int vresp_windows(int n_blocks);
+                                   int* launches = nullptr, int max_slots = 16);
+int vresp_windows(int n_blocks, int max_slots = 16);
 int vresp_row(int n_blocks);                                // slots per table row
 size_t response_table_vol_elems(int stride, int n_blocks);  // float4 entries
 cudaError_t launch_response_table_vol(int nt, double c, int stride, int n_blocks, bool pc, const double* sv,

@@ -340,7 +340,8 @@ hjm_status hjm_run_static(void* cuda_stream, int32_t n_tenor, double dtau, const
             STATIC_CUDA(cudaMemsetAsync(resp_table, 0, sizeof(double2) * entries, s));
             float4* vtable = reinterpret_cast<float4*>(resp_table);
             STATIC_CUDA(launch_response_table_vol(n_tenor, dt / dtau, (int)stride, B, false, &P.sv[0][0], vtable, s));
-            STATIC_CUDA(launch_path_fp64_vresp(n_tenor, P, vtable, nullptr, partials, nullptr, nullptr, s));
+            // one launch of 24 slots (the static scratch holds no carry)
+            STATIC_CUDA(launch_path_fp64_vresp(n_tenor, P, vtable, nullptr, partials, nullptr, nullptr, s, nullptr, 24));
         } else {
             STATIC_CUDA(launch_path_fp64(n_tenor, P, poly, nullptr, partials, nullptr, s));
         }
