@@ -187,11 +187,12 @@ def table_response_fp32_flops_per_path(n_tenor: int, n_steps: int, stride: int) 
     return 84 * stride * sum(B - b for b in range(1, B))
 
 
-def eresp_windows(n_blocks: int) -> list[tuple[int, int]]:
-    """The Euler response form's windows of dates, latest first (eresp_windows)."""
+def eresp_windows(n_blocks: int, dates: int = 24) -> list[tuple[int, int]]:
+    """The Euler response form's windows of dates, latest first (eresp_windows,
+    every date from 2 on active: ``dates`` of them per window)."""
     out, h = [], n_blocks
     while h >= 1:
-        lo = h - 23
+        lo = h - dates + 1
         if lo <= 2:
             lo = 1
         out.append((lo, h))
@@ -214,7 +215,7 @@ def cubic_fp32_flops_per_path(n_tenor: int, n_steps: int, stride: int, nres: int
     B = n_steps // stride
     pre_w = response_active_prefix(n_tenor, n_steps, stride)
     total = 0
-    for lo, hi in eresp_windows(B):
+    for lo, hi in eresp_windows(B, 16):  # with a residual table the windows hold 16 dates
         roff, nslot = B - hi, hi - max(lo, 2) + 1
         for b in range(1, hi):
             live = sum(1 for j in range(max(lo, 2), hi + 1) if j > b)

@@ -918,7 +918,7 @@ static hjm_status enqueue_eresp(hjm_ctx* ctx, const RunShape& sh, double dt, con
         fa.valid = true;
     }
     int lo[kMaxTenor], hi[kMaxTenor];
-    const int n_windows = eresp_windows(sh.B, fa.first, lo, hi, nullptr);
+    const int n_windows = eresp_windows(sh.B, fa.first, lo, hi, nullptr, eresp_window_dates(nres));
     std::vector<EulerRespFrame> frames(n_windows);
     int degs = 0;
     double svc_pc[kFactors][3];  // the predictor-corrector's N-projected loadings of 1, T, T^2
@@ -932,7 +932,7 @@ static hjm_status enqueue_eresp(hjm_ctx* ctx, const RunShape& sh, double dt, con
         eresp_make_frame(dt, ctx->dtau, ctx->nt, pc ? svc_pc : P.svc, cubic ? &ctx->cubic[0][0] : nullptr,
                          ctx->cubic_degs, eresp_window_centre(ctx->dtau, lo[w], hi[w]), frames[w], degs, pc);
     const EulerRespFrame& fr = frames[0];
-    const size_t smem = eresp_max_smem(sh.B, fr.np, sh.stride, fa.first);
+    const size_t smem = eresp_max_smem(sh.B, fr.np, sh.stride, fa.first, nres);
     if (smem > 227 * 1024) return fail(ctx, HJM_ERR_UNSUPPORTED, "shared memory %zu B exceeds 227 KB", smem);
     hjm_status st = ensure_eresp_table(ctx, sh, dt, frames, resid, nres, pc, s);
     if (st != HJM_OK) return st;

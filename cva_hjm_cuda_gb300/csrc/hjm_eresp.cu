@@ -679,6 +679,12 @@ cudaError_t launch_window(const EulerRespParams& E, int ns, const float4* table,
     // with 20 slots at 8 CTAs; the cubic form with its residual spills at 128
     // registers and runs slower, 27.0 against 25.9 ms, and its residual keeps
     // every date still to be sampled active, so it keeps 24)
+    // (with a residual table the windows hold 16 dates, eresp_window_dates: 16
+    // slots in 126 registers, no spills, 8 CTAs per SM; the external-normals
+    // variant spills there and keeps 24)
+    if constexpr (!EXT && NRES > 0) {
+        if (sc) k = path_kernel_fp64_eresp<EXT, DEGS, NRES, true, 16>;
+    }
     if constexpr (!EXT && NRES == 0) {
         if (sc && ns <= 12)
             k = path_kernel_fp64_eresp<EXT, DEGS, NRES, true, 12>;
@@ -805,7 +811,7 @@ cudaError_t launch_path_fp64_eresp(const EulerRespParams& base, const EulerRespF
                                    double* estore, double* carry, cudaStream_t s, int* launches)
 {
     int lo[kMaxTenor], hi[kMaxTenor], ns[kMaxTenor];
-    const int nw = eresp_windows(base.P.n_blocks, first_active, lo, hi, ns);
+    const int nw = eresp_windows(base.P.n_blocks, first_active, lo, hi, ns, eresp_window_dates(nres));
     if (nw > 1 && !carry) return cudaErrorInvalidValue;
     if (launches) *launches = 0;
     for (int w = 0; w < nw; ++w) {
@@ -837,10 +843,10 @@ cudaError_t launch_path_fp64_eresp(const EulerRespParams& base, const EulerRespF
     return cudaSuccess;
 }
 
-size_t eresp_max_smem(int n_blocks, int np, int stride, int first_active)
+size_t eresp_max_smem(int n_blocks, int np, int stride, int first_active, int nres)
 {
     int lo[kMaxTenor], hi[kMaxTenor];
-    const int nw = eresp_windows(n_blocks, first_active, lo, hi, nullptr);
+    const int nw = eresp_windows(n_blocks, first_active, lo, hi, nullptr, eresp_window_dates(nres));
     const int sr = frame_row(np);
     const bool sc = (size_t)stride * sr <= (size_t)kFrameSmemRows * kStateRow;
     size_t m = 0;

@@ -97,9 +97,13 @@ int eresp_residual_factors(const double* resid, const double* vol, int nt);
 // date when those that can be active number at most kRespSlots, else the
 // kRespSlots latest (a window reaching date 2 takes date 1 too).  ns: the
 // slots the window's kernel holds, 12, 16, 20 or 24, at least its active ones.
-// max_slots: the dates a window holds (kRespSlots; the volatility-table
-// response form takes 16).
+// max_slots: the dates a window holds (eresp_window_dates; the
+// volatility-table response form takes 16).
 int eresp_windows(int n_blocks, int first_active, int* lo, int* hi, int* ns, int max_slots = kRespSlots);
+// The dates a window of the response form holds: kRespSlots, or 16 with a
+// residual table (every date still to be sampled is active; 16 register slots
+// fit 128 registers without spills, 8 CTAs per SM).
+inline int eresp_window_dates(int nres) { return nres > 0 ? 16 : kRespSlots; }
 // One launch per window, latest first, window w with frame w (its centre in
 // frames[w].tau0).  degs: the factors' degrees
 // (degs_pack); nres: the table's residual factors; first_active: as
@@ -110,6 +114,6 @@ cudaError_t launch_path_fp64_eresp(const EulerRespParams& base, const EulerRespF
                                    const double* ext, double* partials, double* estore, double* carry,
                                    cudaStream_t s, int* launches);
 // The largest dynamic shared memory of the run's launches.
-size_t eresp_max_smem(int n_blocks, int np, int stride, int first_active);
+size_t eresp_max_smem(int n_blocks, int np, int stride, int first_active, int nres);
 
 }  // namespace hjm

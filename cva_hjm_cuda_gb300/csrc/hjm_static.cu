@@ -315,7 +315,7 @@ hjm_status hjm_run_static(void* cuda_stream, int32_t n_tenor, double dtau, const
         const bool cub = !poly && fit_cubic_resid(vol_host, n_tenor, dtau, cubic, cdegs, resid);
         const int nres = cub ? eresp_residual_factors(resid, vol_host, n_tenor) : 0;
         const int first = (poly || cub) ? eresp_first_active_date(n_tenor, dt / dtau, (int)stride, B, nres) : 2;
-        if ((poly || cub) && eresp_windows(B, first, nullptr, nullptr, nullptr) == 1 &&
+        if ((poly || cub) && eresp_windows(B, first, nullptr, nullptr, nullptr, eresp_window_dates(nres)) == 1 &&
             eresp_table_elems((int)stride, B, cub ? 4 : 3, nres, 1) <= kStaticRespEntries) {
             // the decomposition's response form in one window: its table (FP32
             // pairs, 16 bytes per entry like the double2 array) in the static array

@@ -241,15 +241,16 @@ def test_four_part_moving_frame_equals_the_parts_recursion(stride):
     assert np.allclose(Qa @ y - v, xs, rtol=1e-12, atol=1e-15)
 
 
-def windows(B, first=2):
+def windows(B, first=2, dates=SLOTS):
     """Restatement of eresp_windows: latest first, (lo, hi, ns); dates before
-    first never need a slot."""
+    first never need a slot; ``dates`` per window (24, or 16 with a residual
+    table, eresp_window_dates, and for the volatility-table response form)."""
     f = max(first, 2)
     out, h = [], B
     while h >= 1:
         lo = 1
-        if h - f + 1 > SLOTS:
-            lo = h - SLOTS + 1
+        if h - f + 1 > dates:
+            lo = h - dates + 1
             if lo <= 2:
                 lo = 1
         act = max(h - max(lo, f) + 1, 0)
@@ -262,6 +263,9 @@ def windows(B, first=2):
 @pytest.mark.parametrize("first", [2, 10, 13])
 @pytest.mark.parametrize("B", list(range(1, 61)))
 def test_windows_partition_the_dates(B, first):
+    w16 = windows(B, first, 16)
+    assert sorted(d for lo, hi, _ in w16 for d in range(lo, hi + 1)) == list(range(1, B + 1))
+    assert all(hi - max(lo, first, 2) + 1 <= 16 for lo, hi, _ in w16)
     w = windows(B, first)
     dates = sorted(d for lo, hi, _ in w for d in range(lo, hi + 1))
     assert dates == list(range(1, B + 1))
