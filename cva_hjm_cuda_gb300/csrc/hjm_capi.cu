@@ -966,14 +966,18 @@ static hjm_status enqueue_eresp(hjm_ctx* ctx, const RunShape& sh, double dt, con
 // fit's rule (1.1e-7 for the reference driver's PCA table: two FP32 ulps of
 // the loadings, which the table step rounds to half an ulp), is left out: an
 // input perturbation of that size, far inside the mixed precision's 1e-4.
-static void fill_mixed_cubic(const hjm_ctx* ctx, const RunShape& sh, double dt, MixedParams& M)
+namespace hjm {
+// (Shared with hjm_run_static; internal to the library.)  cubic: [3][4]
+// coefficients of (T - T_L)^d as fit_cubic_resid gives them.
+__attribute__((visibility("hidden"))) void mixed_cubic_params(int nt, double dtau, double dt, int n_blocks,
+                                                              const double* cubic, MixedParams& M)
 {
-    const double dtau = ctx->dtau, c = dt / dtau, sq = std::sqrt(dt);
-    const double TL = dtau * (ctx->nt - 1);
-    const double tau0 = eresp_window_centre(dtau, 1, sh.B);
+    const double c = dt / dtau, sq = std::sqrt(dt);
+    const double TL = dtau * (nt - 1);
+    const double tau0 = eresp_window_centre(dtau, 1, n_blocks);
     const double dl = tau0 - TL;  // sum_e a_e (T - T_L)^e = sum_d a'_d (T - tau0)^d
     for (int k = 0; k < kFactors; ++k) {
-        const double* a = ctx->cubic[k];
+        const double* a = cubic + 4 * k;
         const double sh4[4] = {a[0] + dl * (a[1] + dl * (a[2] + dl * a[3])), a[1] + dl * (2.0 * a[2] + 3.0 * dl * a[3]),
                                a[2] + 3.0 * dl * a[3], a[3]};
         for (int d = 0; d < 3; ++d) M.svcf[k][d] = (float)(sq * sh4[d]);
@@ -981,8 +985,9 @@ static void fill_mixed_cubic(const hjm_ctx* ctx, const RunShape& sh, double dt, 
     }
     M.k3f = (float)(c * dtau * dtau * dtau);
     M.src3f = (float)(3.0 * (TL - tau0));
-    for (int t = 0; t < ctx->nt; ++t) M.P.tau[t] = (float)(dtau * t - tau0);
+    for (int t = 0; t < nt; ++t) M.P.tau[t] = (float)(dtau * t - tau0);
 }
+}  // namespace hjm
 
 // The volatility-table step in the response form (its table already on the
 // stream): the carry of a windowed run, one launch per window.
@@ -1082,7 +1087,7 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
         MixedParams M;
         pack_mixed_params(ctx->nt, P, M);
         if (mixed_cubic) {
-            fill_mixed_cubic(ctx, sh, dt, M);
+            mixed_cubic_params(ctx->nt, ctx->dtau, dt, sh.B, &ctx->cubic[0][0], M);
             run_form = vol_form_code(ctx);
         }
         HJM_CUDA(ctx, launch_path_mixed(ctx->nt, M, use_poly_path(ctx), ext_dev, (double*)ctx->partials.p,

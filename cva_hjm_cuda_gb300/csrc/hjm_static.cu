@@ -55,6 +55,7 @@ namespace hjm {
 void set_thread_error(const char* msg);  // hjm_capi.cu: the message hjm_last_error(NULL) returns
 bool fit_quadratic_vols(const double* vol, int nt, double dtau, double* coef);  // hjm_capi.cu
 bool fit_cubic_resid(const double* vol, int nt, double dtau, double* coef, int* degs, double* resid);  // hjm_capi.cu
+void mixed_cubic_params(int nt, double dtau, double dt, int n_blocks, const double* cubic, MixedParams& M);  // hjm_capi.cu
 }
 
 namespace {
@@ -253,7 +254,13 @@ hjm_status hjm_run_static(void* cuda_stream, int32_t n_tenor, double dtau, const
     // sqrt(dt) c_{k,d}, as hjm_run's fill_params
     double coef[HJM_N_VOL_COEF];
     const bool poly = fit_quadratic_vols(vol_host, n_tenor, dtau, coef);
-    const int cta = path_cta(precision == HJM_PRECISION_MIXED, n_tenor, B, poly);
+    // a table that is a cubic up to a small residual (the reference's own PCA
+    // table): FP64 the response form with the residual, mixed precision the
+    // cubic polynomial form, as hjm_run
+    double cubic[HJM_N_FACTOR * 4], resid[HJM_N_FACTOR * HJM_MAX_TENOR];
+    int cdegs[HJM_N_FACTOR];
+    const bool cub = !poly && fit_cubic_resid(vol_host, n_tenor, dtau, cubic, cdegs, resid);
+    const int cta = path_cta(precision == HJM_PRECISION_MIXED, n_tenor, B, poly || cub);
     const int64_t n_ctas = (n_paths + cta - 1) / cta;
     if (R > kStaticCols || n_ctas > kStaticCtas)
         return static_fail(HJM_ERR_INVALID_ARGUMENT, "run exceeds the static scratch");
@@ -300,7 +307,8 @@ hjm_status hjm_run_static(void* cuda_stream, int32_t n_tenor, double dtau, const
                 for (int d = 0; d < 3; ++d) P.svc[k][d] = sq * coef[k * 3 + d];
         MixedParams M;
         pack_mixed_params(n_tenor, P, M);
-        STATIC_CUDA(launch_path_mixed(n_tenor, M, poly, nullptr, partials, nullptr, s));
+        if (cub) mixed_cubic_params(n_tenor, dtau, dt, B, cubic, M);
+        STATIC_CUDA(launch_path_mixed(n_tenor, M, poly, nullptr, partials, nullptr, s, cub));
     } else {
         PathParams<double> P;
         static_params<double>(n_tenor, dtau, spot_host, vol_host, drift, payA, payB, (int)stride, B, n_paths, dt,
@@ -309,10 +317,6 @@ hjm_status hjm_run_static(void* cuda_stream, int32_t n_tenor, double dtau, const
             for (int k = 0; k < kFactors; ++k)
                 for (int d = 0; d < 3; ++d) P.svc[k][d] = sq * coef[k * 3 + d];
         const size_t entries = response_table_vol_elems((int)stride, B);
-        // a table that is a cubic up to a small residual (the reference's own PCA table)
-        double cubic[HJM_N_FACTOR * 4], resid[HJM_N_FACTOR * HJM_MAX_TENOR];
-        int cdegs[HJM_N_FACTOR];
-        const bool cub = !poly && fit_cubic_resid(vol_host, n_tenor, dtau, cubic, cdegs, resid);
         const int nres = cub ? eresp_residual_factors(resid, vol_host, n_tenor) : 0;
         const int first = (poly || cub) ? eresp_first_active_date(n_tenor, dt / dtau, (int)stride, B, nres) : 2;
         if ((poly || cub) && eresp_windows(B, first, nullptr, nullptr, nullptr, eresp_window_dates(nres)) == 1 &&

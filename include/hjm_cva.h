@@ -116,8 +116,8 @@ hjm_status hjm_ctx_set_scheme(hjm_ctx* ctx, int32_t scheme);
  * 1.1e-7) runs, in Euler valuations, the cubic decomposition: in FP64 with
  * the residual's impulse responses carried beside the remainder's, in mixed
  * precision without the residual (below FP32's resolution of the loadings);
- * the predictor-corrector scheme, the adjoint, MLMC and hjm_run_static run
- * the table step on it.
+ * the predictor-corrector scheme, the adjoint and MLMC run the table step on
+ * it.
  * hjm_ctx_vol_decomposition reports what the current market runs: 0 the
  * table step, 1 the decomposition, 2 the decomposition with factor k of
  * degree <= k (three zero coefficients), 3 the cubic decomposition with a

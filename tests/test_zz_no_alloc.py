@@ -132,13 +132,20 @@ def test_static_entry_matches_oracle(precision, rtol):
 
 
 @pytest.mark.skipif(not _have_gpu(), reason="no CUDA device")
-def test_static_mixed_runs_the_decomposition_like_hjm_run():
-    """With quadratic factors the static mixed run takes the polynomial decomposition, as
-    hjm_run does, and gives hjm_run's results to rounding."""
+@pytest.mark.parametrize("market", ["quadratic", "reference-pca-table"])
+def test_static_mixed_runs_the_decomposition_like_hjm_run(market):
+    """With quadratic factors, or the reference driver's PCA table (cubic up to
+    a residual), the static mixed run takes the same polynomial form as
+    hjm_run and gives hjm_run's results to rounding."""
+    from conftest import load_golden
     from cva_hjm_cuda_gb300.engine import HJMEngine
 
     lib = _lib.load()
-    mk, sw = Market(), Swap()
+    if market == "quadratic":
+        mk = Market()
+    else:
+        mk = Market(vol=np.array(load_golden("ref_driver_own_market.json")["vol"]).reshape(3, 51))
+    sw = Swap()
     cfg = RunConfig(n_paths=30_000, seed=99)
     with HJMEngine(0) as eng:
         eng.set_market(mk)
