@@ -22,13 +22,13 @@
 // factors of the configured workloads) runs the polynomial decomposition in
 // both precisions, as hjm_run does.  FP64 runs take a response form whenever
 // its table fits a second static array (4 MB; recomputed on the device at
-// every call; hjm_run weighs the response form against convection by the
-// run's operation counts, which favour it for these shapes anyway): with
-// quadratic factors the decomposition's remainder in double-FP32
-// impulse-response sums (12x the convected table step), else the whole
-// stochastic curve as FP64 sums of the three factors' responses (3x; with 20
-// dates up to ~180 steps per date).  Larger FP64 runs take the convected step
-// (decomposed or table), mixed precision always the convected pairs.
+// every call) and one launch covers the run's dates (hjm_run takes a response
+// form for every FP64 valuation, in as many windows as it needs, each after
+// the last with a carry): with polynomial factors the decomposition's
+// remainder in double-FP32 impulse-response sums, else the whole stochastic
+// curve as double-FP32 sums of the three factors' responses (12x the
+// convected table step on the 10y swap).  Other FP64 runs take the convected
+// step (decomposed or table); mixed precision always the convected pairs.
 //
 // Limits: at most HJM_STATIC_MAX_PATHS paths per call; EE and CVA only (the
 // per-path exposure store a PFE needs would not fit a modest static buffer).
@@ -90,8 +90,8 @@ hjm_status static_fail(hjm_status st, const char* fmt, ...)
 // The scratch: 8.4 MB of FP64 per device (HJM_STATIC_MAX_PATHS / 64 CTA rows
 // of 64 partial sums, plus column sums and the result block).
 static __device__ __align__(256) double g_hjm_static_scratch[kScratchDoubles];
-// ... and 4 MB for the FP64 response table (double2 entries of the
-// volatility-table form, or float4 entries of the polynomial form).
+// ... and 4 MB for the FP64 response table (the float4 entries of either
+// response form, in a double2 array for its 16-byte alignment).
 static __device__ __align__(256) double2 g_hjm_static_resp[kStaticRespEntries];
 static_assert(sizeof(float4) == sizeof(double2), "both response tables use 16-byte entries");
 
@@ -322,7 +322,7 @@ hjm_status hjm_run_static(void* cuda_stream, int32_t n_tenor, double dtau, const
         if ((poly || cub) && eresp_windows(B, first, nullptr, nullptr, nullptr, eresp_window_dates(nres)) == 1 &&
             eresp_table_elems((int)stride, B, cub ? 4 : 3, nres, 1) <= kStaticRespEntries) {
             // the decomposition's response form in one window: its table (FP32
-            // pairs, 16 bytes per entry like the double2 array) in the static array
+            // pairs, 16 bytes per entry) in the static array
             EulerRespFrame fr;
             int degs;
             eresp_make_frame(dt, dtau, n_tenor, P.svc, cub ? cubic : nullptr, cdegs, eresp_window_centre(dtau, 1, B), fr,
@@ -341,7 +341,7 @@ hjm_status hjm_run_static(void* cuda_stream, int32_t n_tenor, double dtau, const
                                                nullptr));
         } else if (B >= 2 && B <= response_max_dates() && entries <= kStaticRespEntries) {
             // the response form: its table (zero outside the live entries) into the static array
-            STATIC_CUDA(cudaMemsetAsync(resp_table, 0, sizeof(double2) * entries, s));
+            STATIC_CUDA(cudaMemsetAsync(resp_table, 0, sizeof(float4) * entries, s));
             float4* vtable = reinterpret_cast<float4*>(resp_table);
             STATIC_CUDA(launch_response_table_vol(n_tenor, dt / dtau, (int)stride, B, false, &P.sv[0][0], vtable, s));
             // one launch of 24 slots (the static scratch holds no carry)
