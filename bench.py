@@ -187,6 +187,48 @@ def table_response_fp32_flops_per_path(n_tenor: int, n_steps: int, stride: int) 
     return 84 * stride * sum(B - b for b in range(1, B))
 
 
+def mixed_response_slots(n_tenor: int, n_steps: int, stride: int, dtau: float = 0.5) -> int:
+    """The date slots of the mixed-precision response form (mresp_slots): 8 or
+    16 when every date whose response ever counts (a term kappa G_j(lag) of at
+    least 2^-30 |kappa|, or kappa CG_j(lag) of at least 2^-30 |kappa| j stride,
+    at the lags date j reads) fits them, else 0 (the run convects)."""
+    import numpy as np
+
+    B, L = n_steps // stride, n_tenor - 1
+    c = 1.0 / stride
+    thr = 2.0 ** -30
+    v = np.zeros(n_tenor)
+    v[L] = 1.0
+    cum = np.zeros(n_tenor)
+    need = 0
+    j = np.arange(2, B + 1)
+    for m in range((B - 1) * stride):
+        cum += v
+        ok = (m <= (j - 1) * stride - 1) & ((np.abs(v[j]) >= thr) | (np.abs(cum[j]) >= thr * j * stride))
+        if ok.any():
+            need = max(need, int(B - j[ok].min() + 1))
+        vn = v.copy()
+        vn[:L] = v[:L] + c * (v[1:] - v[:L])
+        vn[L] = v[L] + c * (v[L] - v[L - 1])
+        v = vn
+    return 8 if need <= 8 else (16 if need <= 16 else 0)
+
+
+def mixed_response_flops_per_path(n_tenor: int, n_steps: int, stride: int, form: str = "poly_tri") -> int:
+    """FP32 flops per path of the mixed-precision response form
+    (path_kernel_mixed_resp), counted from its formulas: per evolved step of
+    block b, the three scalar parts with the noise projection folded in (9
+    FMA for ``poly_tri``, 12 for ``poly``, 15 with the cubic part of
+    ``cubic_resid`` and its source), their block sums (3 ADD, 4 with the
+    cubic) and, for each slot of a date still to be sampled, one packed FMA
+    into {value, running sum} (4 flops).  Normals and pricing are not
+    counted."""
+    B = n_steps // stride
+    ns = mixed_response_slots(n_tenor, n_steps, stride)
+    parts = {"poly_tri": 2 * 9 + 3, "poly": 2 * 12 + 3, "cubic_resid": 2 * 16 + 4}[form]
+    return sum(stride * (parts + 4 * min(ns, B - b)) for b in range(1, B))
+
+
 def eresp_windows(n_blocks: int, dates: int = 24) -> list[tuple[int, int]]:
     """The Euler response form's windows of dates, latest first (eresp_windows,
     every date from 2 on active: ``dates`` of them per window)."""
@@ -499,9 +541,13 @@ def run_ours(args) -> None:
         return
 
     form = vol_form
-    remainder = "convect" if (is_adjoint or prec != "fp64") else eng.remainder_form()
-    flops = (algorithmic_flops_per_path(mk.n_tenor, n_steps, stride, form, remainder) * n_paths
-             * (2 if is_adjoint else 1))
+    remainder = "convect" if is_adjoint else eng.remainder_form()
+    if prec != "fp64" and remainder == "response":
+        flops = mixed_response_flops_per_path(mk.n_tenor, n_steps, stride, form) * n_paths
+    else:
+        flops = (algorithmic_flops_per_path(mk.n_tenor, n_steps, stride, form,
+                                            "convect" if prec != "fp64" else remainder) * n_paths
+                 * (2 if is_adjoint else 1))
     extras = {}
     peak_key = "fp64" if prec == "fp64" else "mixed"
     # the roofline denominators, measured on this GPU (a fraction of a second)
@@ -551,6 +597,8 @@ def run_ours(args) -> None:
                            "path_kernel_fp64_eresp<philox,degs(0,1,2)>"
                            if prec == "fp64" and remainder == "response" else
                            f"path_kernel_fp64<{mk.n_tenor},philox,{form}>" if prec == "fp64" else
+                           f"path_kernel_mixed_resp<philox,{form},{mixed_response_slots(mk.n_tenor, n_steps, stride)}>"
+                           if remainder == "response" else
                            f"path_kernel_mixed<{mk.n_tenor},philox,{form}>"),
                 "algorithmic_flops_per_launch": flops, "avg_launch_ms": path_ms,
                 "peak_source": "measured live by bench.py (FMA microkernel, this GPU)",
@@ -796,6 +844,7 @@ def mixed_vs_fp64(eng, mk, sw, args, stream, flush, fp64_value, peak32=None) -> 
     el = e0.elapsed_time(e1) / 1e3
     hist = eng.timing_history(min(args.steps, 64))
     mx = eng.fetch()
+    mx_form = eng.remainder_form()
     f64 = eng.run(cfg, "fp64")
     f64_ms = float(eng.timing_history(1)[0, 0])
     rel = np.abs(mx.ee[:20] - f64.ee[:20]) / f64.ee[:20]
@@ -803,12 +852,17 @@ def mixed_vs_fp64(eng, mk, sw, args, stream, flush, fp64_value, peak32=None) -> 
     stride = int(round(mk.dtau / DT))
     kern_ms = float(hist[:, 0].mean())
     form = eng.vol_form()
-    flops = algorithmic_flops_per_path(mk.n_tenor, N_STEPS, stride, form, "convect") * n
+    engine_form = mx_form
+    if engine_form == "response":
+        flops = mixed_response_flops_per_path(mk.n_tenor, N_STEPS, stride, form) * n
+        kname = f"path_kernel_mixed_resp<philox,{form},{mixed_response_slots(mk.n_tenor, N_STEPS, stride)}>"
+    else:
+        flops = algorithmic_flops_per_path(mk.n_tenor, N_STEPS, stride, form, "convect") * n
+        kname = f"path_kernel_mixed<{mk.n_tenor},philox,{form}>"
     return {
         "value": value, "unit": UNIT, "n_paths": n, "ms_per_step": 1e3 * el / args.steps,
-        "path_kernel_ms": kern_ms,
-        "roofline": fp32_roofline(f"path_kernel_mixed<{mk.n_tenor},philox,{form}>", flops, kern_ms, peak32,
-                                  f"mixed-{n}"),
+        "path_kernel_ms": kern_ms, "remainder": engine_form,
+        "roofline": fp32_roofline(kname, flops, kern_ms, peak32, f"mixed-{n}"),
         "speedup_vs_fp64_path_steps_per_s": value / fp64_value,
         "fp64_same_paths_path_kernel_ms": f64_ms,
         "ee_rel_err_vs_fp64_per_date": [float(x) for x in rel],

@@ -25,7 +25,7 @@ BUILD = PKG / "_build"
 LIB_DIR = PKG / "lib"
 LIB = LIB_DIR / "libhjmcva.so"
 
-CUDA_SOURCES = ["hjm_forward.cu", "hjm_eresp.cu", "hjm_adjoint.cu", "hjm_pc.cu", "hjm_mlmc.cu", "hjm_capi.cu", "hjm_static.cu", "peak_fma.cu"]
+CUDA_SOURCES = ["hjm_forward.cu", "hjm_eresp.cu", "hjm_mresp.cu", "hjm_adjoint.cu", "hjm_pc.cu", "hjm_mlmc.cu", "hjm_capi.cu", "hjm_static.cu", "peak_fma.cu"]
 CXX_SOURCES = ["hjm_dropin.cpp", "hjm_calib.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -105,19 +105,20 @@ struct hjm_ctx {
     bool keep_exposures = false;
 
     // device buffers
-    DevBuf partials, sums, result, estore, sel, hist, ext, ext_raw, wide, scratch, ck_h, ck_a, vresp, eresp, carry;
+    DevBuf partials, sums, result, estore, sel, hist, ext, ext_raw, wide, scratch, ck_h, ck_a, vresp, eresp, carry,
+        mresp;
     MemBudget budget;
     hjm_ctx()
     {
         for (DevBuf* b : buffers()) b->budget = &budget;
     }
-    std::array<DevBuf*, 15> buffers()
+    std::array<DevBuf*, 16> buffers()
     {
         return {&partials, &sums, &result, &estore, &sel, &hist, &ext, &ext_raw, &wide, &scratch, &ck_h, &ck_a,
-                &vresp, &eresp, &carry};
+                &vresp, &eresp, &carry, &mresp};
     }
-    // the response tables in eresp and vresp hold the run shapes of their
-    // keys; resp_used is recorded after the last kernel that reads either
+    // the response tables in eresp, vresp and mresp hold the run shapes of
+    // their keys; resp_used is recorded after the last kernel that reads one
     struct ErespKey {  // the response form's table in eresp (Euler or predictor-corrector)
         bool valid = false, pc = false;
         int nt = 0, stride = 0, B = 0, np = 0, nres = 0;
@@ -137,6 +138,11 @@ struct hjm_ctx {
         double c = 0;
         std::vector<double> sv;
     } vresp_key;
+    struct MrespKey {  // the mixed-precision response form's slots and its table in mresp
+        bool valid = false, on_device = false;
+        int nt = 0, stride = 0, B = 0, ns = 0;
+        double c = 0, dtau = 0;
+    } mresp_key;
     cudaEvent_t resp_used = nullptr;
 
     // last valuation
@@ -800,9 +806,12 @@ static void fill_pc(const hjm_ctx* ctx, const RunShape& sh, double dt, const Pat
 //
 // Volatility-table step (no decomposition): the whole stochastic curve in
 // impulse responses, per step and date still to be sampled three
-// double-FP32 terms on the FP32 pipe (in windows of at most 24 dates),
-// against four FP64 FMAs per live tenor (five for the predictor-corrector)
-// when convected.
+// double-FP32 terms on the FP32 pipe (in windows of 16 dates), against four
+// FP64 FMAs per live tenor (five for the predictor-corrector) when convected.
+//
+// Mixed precision with polynomial factors under the Euler step: the FP32
+// response form of hjm_mresp.cu when the dates whose responses count fit its
+// slots (mresp_slots: the 10y swap's 20 dates in 8), else the convected pairs.
 static bool use_response_form(const hjm_ctx* ctx, const RunShape& sh)
 {
     (void)sh;
@@ -989,6 +998,44 @@ __attribute__((visibility("hidden"))) void mixed_cubic_params(int nt, double dta
 }
 }  // namespace hjm
 
+// The date slots of the mixed-precision response form for the run shape (0:
+// the run convects), counted on the host once per shape.
+static int mresp_run_slots(hjm_ctx* ctx, const RunShape& sh, double dt)
+{
+    const double c = dt / ctx->dtau;
+    hjm_ctx::MrespKey& k = ctx->mresp_key;
+    if (!(k.valid && k.nt == ctx->nt && k.stride == sh.stride && k.B == sh.B && k.c == c && k.dtau == ctx->dtau)) {
+        k.ns = mresp_slots(ctx->nt, c, sh.stride, sh.B);
+        k.nt = ctx->nt;
+        k.stride = sh.stride;
+        k.B = sh.B;
+        k.c = c;
+        k.dtau = ctx->dtau;
+        k.valid = true;
+        k.on_device = false;
+    }
+    return k.ns;
+}
+
+// Its table on the stream (for the shape mresp_run_slots counted): built
+// only when the shape changed, after the kernels of earlier valuations that
+// read the old one.
+static hjm_status ensure_mresp_table(hjm_ctx* ctx, cudaStream_t s)
+{
+    hjm_ctx::MrespKey& k = ctx->mresp_key;
+    if (k.on_device) return HJM_OK;
+    if (!ctx->resp_used) HJM_CUDA(ctx, cudaEventCreateWithFlags(&ctx->resp_used, cudaEventDisableTiming));
+    const size_t bytes = sizeof(float4) * mresp_table_elems(k.stride, k.B, k.ns);
+    if (bytes > ctx->mresp.bytes)
+        HJM_CUDA(ctx, ctx->mresp.ensure(bytes));  // cudaFree waits for the device
+    else
+        HJM_CUDA(ctx, cudaStreamWaitEvent(s, ctx->resp_used, 0));
+    HJM_CUDA(ctx, launch_mresp_table(k.nt, k.c, k.dtau, k.stride, k.B, k.ns, (float4*)ctx->mresp.p, s));
+    ctx->stat_launches += 1;
+    k.on_device = true;
+    return HJM_OK;
+}
+
 // The volatility-table step in the response form (its table already on the
 // stream): the carry of a windowed run, one launch per window.
 static hjm_status enqueue_vresp(hjm_ctx* ctx, const RunShape& sh, const PathParams<double>& P, const double* ext_dev,
@@ -1022,7 +1069,13 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
     const bool pc = ctx->scheme == HJM_SCHEME_PREDICTOR_CORRECTOR;
     // a cubic market in mixed precision (Euler): the cubic polynomial form
     const bool mixed_cubic = mixed && !pc && use_cubic_path(ctx);
-    const int cta = pc ? pc_cta() : path_cta(mixed, ctx->nt, sh.B, use_poly_path(ctx) || mixed_cubic);
+    // mixed precision with polynomial factors: the response form when the
+    // dates its remainder reaches fit its slots (else the convected pairs)
+    const int mresp_ns = (mixed && !pc && (use_poly_path(ctx) || mixed_cubic) && use_response_form(ctx, sh))
+                             ? mresp_run_slots(ctx, sh, dt)
+                             : 0;
+    const int cta = pc ? pc_cta()
+                       : (mresp_ns ? kCta : path_cta(mixed, ctx->nt, sh.B, use_poly_path(ctx) || mixed_cubic));
     const int64_t n_ctas = (n_paths + cta - 1) / cta;
     const int64_t ld = (n_paths + 3) / 4 * 4;
     const size_t esize = mixed ? 4 : 8;
@@ -1090,8 +1143,18 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
             mixed_cubic_params(ctx->nt, ctx->dtau, dt, sh.B, &ctx->cubic[0][0], M);
             run_form = vol_form_code(ctx);
         }
-        HJM_CUDA(ctx, launch_path_mixed(ctx->nt, M, use_poly_path(ctx), ext_dev, (double*)ctx->partials.p,
-                                        store ? (float*)ctx->estore.p : nullptr, s, mixed_cubic));
+        if (mresp_ns) {
+            st = ensure_mresp_table(ctx, s);
+            if (st != HJM_OK) return st;
+            HJM_CUDA(ctx, launch_path_mixed_resp(M, mresp_ns, mixed_cubic, (const float4*)ctx->mresp.p, ext_dev,
+                                                 (double*)ctx->partials.p, store ? (float*)ctx->estore.p : nullptr,
+                                                 s));
+            HJM_CUDA(ctx, cudaEventRecord(ctx->resp_used, s));
+            resp = true;
+        } else {
+            HJM_CUDA(ctx, launch_path_mixed(ctx->nt, M, use_poly_path(ctx), ext_dev, (double*)ctx->partials.p,
+                                            store ? (float*)ctx->estore.p : nullptr, s, mixed_cubic));
+        }
     } else {
         PathParams<double> P;
         fill_params<double>(ctx, sh, n_paths, dt, seed, path_offset, hazard, recovery, ld, store, P, F);

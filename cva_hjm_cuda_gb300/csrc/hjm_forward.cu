@@ -506,7 +506,7 @@ __global__ void __launch_bounds__(C, 512 / C)
     const int n_last = B * P.stride - 1;
     const int64_t lpc = active ? lp : 0;
     float q0, q1, q2;
-    draw_phi<float, EXT>(ext, gpath, lpc, P.n_paths, P.stride, P.rk0, P.rk1, q0, q1, q2);
+    draw_phi<float, EXT>(ext, gpath, lpc, P.n_paths, min(P.stride, n_last), P.rk0, P.rk1, q0, q1, q2);
     for (int b = 1; b < B; ++b) {
         BlockSums bs;
         bs.reset();

@@ -84,6 +84,21 @@ cudaError_t launch_response_table_vol(int nt, double c, int stride, int n_blocks
 cudaError_t launch_path_mixed(int nt, const MixedParams& M, bool poly, const double* ext, double* partials,
                               float* estore, cudaStream_t s, bool cub = false);
 void pack_mixed_params(int nt, const PathParams<float>& P, MixedParams& M);
+// The response form of the mixed-precision Euler step (hjm_mresp.cu):
+// polynomial factors (cub: the cubic form), the remainder as FP32
+// impulse-response sums at the dates it reaches.  mresp_slots: the date
+// slots of the run shape, 8 or 16, or 0 when the dates whose responses count
+// do not fit 16 (the run then convects); launch_mresp_table: the table on
+// the stream (rows b stride + s of ns / 2 float4, each two {kappa G,
+// kappa CG} pairs; mresp_table_elems float4).
+int mresp_slots(int nt, double c, int stride, int n_blocks);
+size_t mresp_table_elems(int stride, int n_blocks, int ns);
+cudaError_t launch_mresp_table(int nt, double c, double dtau, int stride, int n_blocks, int ns, float4* table,
+                               cudaStream_t s);
+size_t mresp_smem_bytes(int n_blocks);
+// paths per CTA: kCta, as launch_path_mixed's table form (path_cta)
+cudaError_t launch_path_mixed_resp(const MixedParams& M, int ns, bool cub, const float4* table, const double* ext,
+                                   double* partials, float* estore, cudaStream_t s);
 bool path_tenor_supported(int nt);
 size_t path_smem(int nt, int n_blocks, bool mixed);
 // paths per CTA of the Euler path kernel of a run (one partial-sum row each):

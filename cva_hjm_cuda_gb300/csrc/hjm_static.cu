@@ -28,7 +28,9 @@
 // remainder in double-FP32 impulse-response sums, else the whole stochastic
 // curve as double-FP32 sums of the three factors' responses (12x the
 // convected table step on the 10y swap).  Other FP64 runs take the convected
-// step (decomposed or table); mixed precision always the convected pairs.
+// step (decomposed or table).  Mixed precision with polynomial factors takes
+// the FP32 response form where hjm_run does (its table, also rebuilt at every
+// call, in the same static array), else the convected pairs.
 //
 // Limits: at most HJM_STATIC_MAX_PATHS paths per call; EE and CVA only (the
 // per-path exposure store a PFE needs would not fit a modest static buffer).
@@ -260,7 +262,12 @@ hjm_status hjm_run_static(void* cuda_stream, int32_t n_tenor, double dtau, const
     double cubic[HJM_N_FACTOR * 4], resid[HJM_N_FACTOR * HJM_MAX_TENOR];
     int cdegs[HJM_N_FACTOR];
     const bool cub = !poly && fit_cubic_resid(vol_host, n_tenor, dtau, cubic, cdegs, resid);
-    const int cta = path_cta(precision == HJM_PRECISION_MIXED, n_tenor, B, poly || cub);
+    // mixed precision with polynomial factors: the response form when the
+    // dates its remainder reaches fit its slots and its table the static array
+    const int mresp_ns =
+        (precision == HJM_PRECISION_MIXED && (poly || cub)) ? mresp_slots(n_tenor, dt / dtau, (int)stride, B) : 0;
+    const bool mresp = mresp_ns > 0 && mresp_table_elems((int)stride, B, mresp_ns) <= kStaticRespEntries;
+    const int cta = mresp ? kCta : path_cta(precision == HJM_PRECISION_MIXED, n_tenor, B, poly || cub);
     const int64_t n_ctas = (n_paths + cta - 1) / cta;
     if (R > kStaticCols || n_ctas > kStaticCtas)
         return static_fail(HJM_ERR_INVALID_ARGUMENT, "run exceeds the static scratch");
@@ -308,7 +315,13 @@ hjm_status hjm_run_static(void* cuda_stream, int32_t n_tenor, double dtau, const
         MixedParams M;
         pack_mixed_params(n_tenor, P, M);
         if (cub) mixed_cubic_params(n_tenor, dtau, dt, B, cubic, M);
-        STATIC_CUDA(launch_path_mixed(n_tenor, M, poly, nullptr, partials, nullptr, s, cub));
+        if (mresp) {
+            float4* table = reinterpret_cast<float4*>(resp_table);
+            STATIC_CUDA(launch_mresp_table(n_tenor, dt / dtau, dtau, (int)stride, B, mresp_ns, table, s));
+            STATIC_CUDA(launch_path_mixed_resp(M, mresp_ns, cub, table, nullptr, partials, nullptr, s));
+        } else {
+            STATIC_CUDA(launch_path_mixed(n_tenor, M, poly, nullptr, partials, nullptr, s, cub));
+        }
     } else {
         PathParams<double> P;
         static_params<double>(n_tenor, dtau, spot_host, vol_host, drift, payA, payB, (int)stride, B, n_paths, dt,

@@ -48,3 +48,22 @@ def test_response_slots_follow_the_kernels_value_prefix():
         tab, kappa = W.eresp_table(nt, stride, B, 1.0 / stride)
         np.testing.assert_array_equal(bench.response_active_prefix(nt, n_steps, stride),
                                       W.eresp_prefix(tab, kappa, B, stride))
+
+
+def test_mixed_response_slots_and_count():
+    """The mixed-precision response form's slots (mresp_slots restated): the
+    10y swap's counting dates fit 8 slots, the 12y swap's 16; the 25y swap on
+    51 tenors and the 30y netting shape on 61 tenors convect.  Its count: the
+    parts (21 flops per step for factor k of degree <= k) and one packed FMA
+    per slot of a date still to be sampled."""
+    assert bench.mixed_response_slots(51, 1000, 50) == 8
+    assert bench.mixed_response_slots(51, 1200, 50) == 16
+    assert bench.mixed_response_slots(51, 2500, 50) == 0
+    assert bench.mixed_response_slots(61, 3000, 50) == 0
+    # one date: nothing evolves, every slot fits
+    assert bench.mixed_response_slots(51, 50, 50) == 8
+    B, stride = 20, 50
+    want = sum(stride * (21 + 4 * min(8, B - b)) for b in range(1, B))
+    assert bench.mixed_response_flops_per_path(51, 1000, 50, "poly_tri") == want
+    # far below the convected pairs' count on the same run
+    assert want < 0.6 * bench.algorithmic_flops_per_path(51, 1000, 50, "poly_tri")

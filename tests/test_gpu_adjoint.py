@@ -36,12 +36,21 @@ def _poly(engine, spot=None, coef=DEFAULT_VOL_COEFFS, nt=51):
 
 
 def test_adjoint_cva_equals_mixed_forward(engine):
-    """The adjoint launch runs the mixed-precision valuation's forward pass
-    unchanged (checkpoint writes only read the state), so its CVA, standard
-    error and dCVA/dhazard equal the valuation's bit for bit in both modes."""
+    """The adjoint launch runs the convected mixed-precision valuation's
+    forward pass unchanged (checkpoint writes only read the state), so its
+    CVA, standard error and dCVA/dhazard equal that valuation's bit for bit in
+    both modes (and the default valuation, the remainder's FP32 responses,
+    within FP32 rounding)."""
     _poly(engine)
     cfg = RunConfig(n_paths=40000, seed=77)
-    v = engine.run(cfg, "mixed", pfe=False)
+    engine.set_remainder_form("convect")
+    try:
+        v = engine.run(cfg, "mixed", pfe=False)
+    finally:
+        engine.set_remainder_form("auto")
+    r = engine.run(cfg, "mixed", pfe=False)
+    assert engine.remainder_form() == "response"
+    assert abs(r.cva - v.cva) <= 1e-6 * v.cva
     for k in (0, 32):
         a = engine.run_adjoint(cfg, checkpoint_every=k)
         assert a.cva == v.cva

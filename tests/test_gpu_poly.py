@@ -335,12 +335,14 @@ def test_remainder_form_choice_and_limits(engine, remainder_form, tmp_path):
     engine.write_report(tmp_path / "r.json")
     assert json.loads((tmp_path / "r.json").read_text())["run"]["remainder"] == "response"
     engine.run(RunConfig(n_paths=256), "mixed")
-    assert engine.remainder_form() == "convect"  # mixed precision convects (the FP32 pairs cost less)
+    assert engine.remainder_form() == "response"  # mixed precision: the 10y swap's counting dates fit 8 slots
     _poly_market(engine, nt=61)
     engine.set_swap(Swap(n_tenor=61, n_periods=60))
     cfg30 = RunConfig(n_paths=256, n_steps=3000)
     engine.run(cfg30, "fp64")
     assert engine.remainder_form() == "response"  # 60 dates: three windows
+    engine.run(cfg30, "mixed")
+    assert engine.remainder_form() == "convect"  # mixed precision: 44 counting dates do not fit 16 slots
     remainder_form("convect")
     engine.run(cfg30, "fp64")
     assert engine.remainder_form() == "convect"
