@@ -99,7 +99,11 @@ __global__ void __launch_bounds__(kCta, mresp_min_ctas(NS))
     for (int b = 1; b < B; ++b) {
         float sS = 0.f, sU = 0.f, sW = 0.f, sX = 0.f;
         const float4* row = resp + (size_t)b * P.stride * (NS / 2);
-#pragma unroll 2
+        // unrolled by 5 (a divisor of 50 steps per block; the generator's
+        // draws of five steps in flight): 15.65 ms at 4M paths on the 10y
+        // swap, against 15.77 by 4 and 16.67 by 2; the cubic, 16-slot and
+        // external-normals variants spill beyond 2
+#pragma unroll((EXT || CUB || NS > 8) ? 2 : 5)
         for (int s = 0; s < P.stride; ++s) {
             const int n = b * P.stride + s;
             const float phi0 = q0, phi1 = q1, phi2 = q2;
