@@ -125,7 +125,7 @@ hjm_status hjm_ctx_set_scheme(hjm_ctx* ctx, int32_t scheme);
 hjm_status hjm_ctx_set_vol_decomposition(hjm_ctx* ctx, int32_t enable);
 hjm_status hjm_ctx_vol_decomposition(hjm_ctx* ctx, int32_t* active);
 
-/* FP64 transport form.  The pricing reads the stochastic curve only at each
+/* Transport form of the remainder.  The pricing reads the stochastic curve only at each
  * date's own tenor.  With the polynomial decomposition the remainder, driven
  * only at the last tenor (the last two for the predictor-corrector), is either
  * convected over the live tenors every step (HJM_REMAINDER_CONVECT) or carried,
@@ -143,8 +143,15 @@ hjm_status hjm_ctx_vol_decomposition(hjm_ctx* ctx, int32_t* active);
  * launch each, the later windows passing each path's later cash flows to the
  * earlier ones.  HJM_REMAINDER_AUTO (default) takes the response form for
  * every FP64 valuation.  Both time schemes; the forms agree to rounding
- * (per-path exposures within ~1e-13 of the exposure scale); mixed precision
- * always convects.  The report names the form a valuation ran ("remainder"). */
+ * (per-path exposures within ~1e-13 of the exposure scale).  Mixed precision
+ * with the decomposition (Euler step) carries the remainder as FP32
+ * impulse-response sums (one packed FMA per date per step) when the dates
+ * whose responses ever reach 2^-30 of the source fit 16 slots (the 10y swap's
+ * 20 dates on 51 tenors: 8), else convects it in FP32 pairs (the 25y swap,
+ * the 30y netting set); the two agree to FP32 rounding (~1e-7 of the
+ * exposure scale).  AUTO and RESPONSE take it where it fits; mixed precision
+ * under the predictor-corrector scheme, the adjoint and MLMC convect.  The
+ * report names the form a valuation ran ("remainder"). */
 #define HJM_REMAINDER_AUTO 0
 #define HJM_REMAINDER_CONVECT 1
 #define HJM_REMAINDER_RESPONSE 2
@@ -296,8 +303,8 @@ hjm_status hjm_run_adjoint(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, doubl
  * stream) and the call is synchronous: it waits for cuda_stream and returns
  * when ee_out [n_tenor] and cva_out [HJM_CVA_OUT_LEN] hold the results.  Its
  * device memory is two fixed static arrays that each GPU loading the library
- * keeps until exit: 8.4 MB of scratch and 4 MB for the FP64 response table,
- * about 12.4 MB in all; it calls no cudaMalloc, cudaFree or allocating
+ * keeps until exit: 8.4 MB of scratch and 4 MB for a response form's table
+ * (FP64, or mixed precision's), about 12.4 MB in all; it calls no cudaMalloc, cudaFree or allocating
  * library routine.  Limits: at most
  * HJM_STATIC_MAX_PATHS paths per call (larger runs fail with
  * HJM_ERR_INVALID_ARGUMENT), EE and CVA only (no PFE).  The first call on a
