@@ -1088,8 +1088,26 @@ def adjoint_cost(eng, args, flush) -> dict:
         ms.append(float(eng.timing_history(1)[0, 3]))
     one = statistics.median(ms)
     out["one_cva_valuation_ms"] = one
+    out["one_cva_valuation_remainder"] = eng.remainder_form()
+    # the adjoint's forward pass convects the remainder: the valuation in that
+    # form as well (the default valuation carries it in FP32 responses)
+    eng.set_remainder_form("convect")
+    try:
+        for _ in range(args.warmup):
+            eng.run(cfg, "mixed", pfe=False)
+        ms = []
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            eng.run(cfg, "mixed", pfe=False)
+            ms.append(float(eng.timing_history(1)[0, 3]))
+    finally:
+        eng.set_remainder_form("auto")
+    conv = statistics.median(ms)
+    out["one_cva_valuation_convected_ms"] = conv
     for label in ("checkpoint_32", "no_checkpoint"):
         out[label]["cost_in_valuations"] = out[label]["ms"] / one
+        out[label]["cost_in_convected_valuations"] = out[label]["ms"] / conv
     # one-sided bump-and-revalue of the 51 forwards, 9 coefficients and the hazard
     out["bump_and_revalue_valuations"] = 1 + 51 + 9 + 1
     out["cva"] = sens.cva

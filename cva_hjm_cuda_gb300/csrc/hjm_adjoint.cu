@@ -709,6 +709,279 @@ cudaError_t launch_adjoint_pc(int nt, const PcParams<float>& Q, bool poly, doubl
     return cudaErrorInvalidValue;
 }
 
+// ---------------------------------------------------------------------------
+// The adjoint in the response form (Euler step, quadratic factors, the sampled
+// states kept: checkpoint_every = 0).  The forward pass is the mixed
+// valuation's response form (path_kernel_mixed_resp, hjm_mresp.cu: the parts
+// S, U, W as FP32 scalars, the remainder as FP32 impulse-response sums in NS
+// date slots, the same operations in the same order, so the path's cash
+// flows are the valuation's); it keeps each date's sampled forward and
+// discount factor.  The reverse sweep needs the per-tenor adjoint only for its
+// last tenor, the remainder's coupling to W in the moment recursion
+// (adjoint_kernel above): the adjoint of hc after step n at the last tenor is
+//     g_n[L] = sum_j xbar_j G_j(n_j - n) + abar_j CG_j(n_j - n),
+// G_j(m) = (A^m e_L)[j], CG_j its running sum, over the dates j still ahead
+// of step n -- the forward table's own entries, so with the slot dates' seeds
+// {xbar_j, abar_j} in registers the sweep's kappa g_n[L] is one packed FMA
+// per slot (table row n) instead of the transposed convection of every tenor.
+// Dates whose responses never count (no slot) contribute below 2^-30 of
+// kappa per seed, as in the valuation.
+struct AdjRespLayout {
+    size_t cf, xs, ds, cb, red, total;
+};
+
+__host__ __device__ inline AdjRespLayout adj_resp_layout(int B, int R)
+{
+    AdjRespLayout L;
+    const size_t rows = (size_t)B + 1;
+    L.cf = 0;
+    L.xs = align128((rows + 1) * kAdjCta * 4);
+    L.ds = align128(L.xs + rows * kAdjCta * 4);
+    L.cb = align128(L.ds + rows * kAdjCta * 4);
+    L.red = align128(L.cb + (size_t)9 * kAdjCta * 8);
+    L.total = align128(L.red + (size_t)(kAdjCta / 32) * R * 8);
+    return L;
+}
+
+// CTAs per SM: the registers' bound (8 slots in 80 per thread; 16 in 128)
+constexpr int adj_resp_min_ctas(int ns) { return ns <= 8 ? 12 : 8; }
+
+template <int NS>
+__global__ void __launch_bounds__(kAdjCta, adj_resp_min_ctas(NS))
+    adjoint_kernel_resp(const __grid_constant__ MixedParams M, const float4* __restrict__ resp,
+                        double* __restrict__ partials)
+{
+    constexpr int C = kAdjCta;
+    const PathParams<float>& P = M.P;
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int tid = threadIdx.x;
+    const int B = P.n_blocks;
+    const int R = 3 * B + 12;
+    const AdjRespLayout Ly = adj_resp_layout(B, R);
+    float* cf_s = reinterpret_cast<float*>(smem + Ly.cf);  // [B+2][C]: cash flows, then exposures one row up
+    float* xs_s = reinterpret_cast<float*>(smem + Ly.xs);  // [B+1][C]: x_i, then xbar_i
+    float* ds_s = reinterpret_cast<float*>(smem + Ly.ds);  // [B+1][C]: D_i, then abar_i
+    double* cb_s = reinterpret_cast<double*>(smem + Ly.cb);
+    double* red_s = reinterpret_cast<double*>(smem + Ly.red);
+
+    const int64_t lp = (int64_t)blockIdx.x * C + tid;
+    const bool active = lp < P.n_paths;
+    const uint64_t gpath = P.path_offset + (uint64_t)lp;
+    const int stride = P.stride;
+    const int n_steps = B * stride;
+
+    // ---------------------------------------------------------------- forward
+    float2 A[NS];  // {hc at date j's tenor, its running sum}, slot B - j
+#pragma unroll
+    for (int r = 0; r < NS; ++r) A[r] = make_float2(0.f, 0.f);
+    float S = 0.f, U = 0.f, W = 0.f;
+    double zS = 0.0, zU = 0.0, zW = 0.0;
+    auto price = [&](int i, float2 rc) {
+        const float ti = P.tau[i];
+        const float pv = fmaf(ti, fmaf(ti, W, U), S);
+        const double xv = P.psamp[i] + (double)(rc.x + pv);
+        const double td = (double)ti;
+        const double a = P.psum[i] + (double)rc.y + fma(td, fma(td, zW, zU), zS);
+        const float D = expf((float)(-a * P.dt));
+        const float mm = (float)P.m;
+        const float L = mm * expm1f((float)xv / mm);
+        cf_s[i * C + tid] = D * ((float)P.payA[i] * L - (float)P.payB[i]);
+        xs_s[i * C + tid] = (float)xv;
+        ds_s[i * C + tid] = D;
+    };
+    price(1, make_float2(0.f, 0.f));
+    const int n_last = n_steps - 1;
+    float q0, q1, q2;
+    draw_phi<float, false>(nullptr, gpath, lp, P.n_paths, min(stride, n_last), P.rk0, P.rk1, q0, q1, q2);
+    for (int b = 1; b < B; ++b) {
+        float sS = 0.f, sU = 0.f, sW = 0.f;
+        const float4* row = resp + (size_t)b * stride * (NS / 2);
+#pragma unroll 2
+        for (int s = 0; s < stride; ++s) {
+            const int n = b * stride + s;
+            const float phi0 = q0, phi1 = q1, phi2 = q2;
+            draw_phi<float, false>(nullptr, gpath, lp, P.n_paths, min(n + 1, n_last), P.rk0, P.rk1, q0, q1, q2);
+            const float2 w2 = make_float2(W, W);
+            const float4* rr = row + (size_t)s * (NS / 2);
+#pragma unroll
+            for (int u = 0; u < NS / 2; ++u) {
+                const float4 e = __ldg(rr + u);
+                A[2 * u] = __ffma2_rn(make_float2(e.x, e.y), w2, A[2 * u]);
+                A[2 * u + 1] = __ffma2_rn(make_float2(e.z, e.w), w2, A[2 * u + 1]);
+            }
+            float Sn = fmaf(M.svcf[0][0], phi0, fmaf(M.k2f, W, fmaf(M.k1f, U, S)));
+            Sn = fmaf(M.svcf[2][0], phi2, fmaf(M.svcf[1][0], phi1, Sn));
+            float Un = fmaf(M.svcf[1][1], phi1, fmaf(M.svcf[0][1], phi0, fmaf(2.0f * M.k1f, W, U)));
+            Un = fmaf(M.svcf[2][1], phi2, Un);
+            const float Wn = fmaf(M.svcf[2][2], phi2, fmaf(M.svcf[1][2], phi1, fmaf(M.svcf[0][2], phi0, W)));
+            S = Sn;
+            U = Un;
+            W = Wn;
+            sS += S;
+            sU += U;
+            sW += W;
+        }
+        zS += (double)sS;
+        zU += (double)sU;
+        zW += (double)sW;
+        const int r = B - (b + 1);
+        price(b + 1, r < NS ? select_reg<NS, float2>(A, r) : make_float2(0.f, 0.f));
+    }
+
+    // exposures, the path's CVA contribution, the CTA's EE and CVA partial sums
+    float* e_s = cf_s + C;
+    double v = 0.0, cva_c = 0.0;
+    e_s[B * C + tid] = 0.f;
+    for (int j = B - 1; j >= 0; --j) {
+        v += (double)cf_s[(j + 1) * C + tid];
+        double e = (v > 0.0) ? v : 0.0;
+        if (!active) e = 0.0;
+        e_s[j * C + tid] = (float)e;
+        cva_c = fma(P.cvaw[j], e, cva_c);
+    }
+    __syncthreads();
+    const int warp = tid >> 5, lane = tid & 31;
+    for (int j = warp; j <= B; j += C / 32) {
+        double sum = 0.0;
+#pragma unroll
+        for (int q = 0; q < C / 32; ++q) sum += (double)e_s[j * C + lane + 32 * q];
+        sum = warp_sum(sum);
+        if (lane == 0) partials[(size_t)blockIdx.x * R + j] = sum;
+    }
+    {
+        const double s1 = warp_sum(cva_c), s2 = warp_sum(cva_c * cva_c);
+        if (lane == 0) {
+            red_s[warp] = s1;
+            red_s[C / 32 + warp] = s2;
+        }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        double s1 = 0.0, s2 = 0.0;
+        for (int w = 0; w < C / 32; ++w) {
+            s1 += red_s[w];
+            s2 += red_s[C / 32 + w];
+        }
+        partials[(size_t)blockIdx.x * R + B + 1] = s1;
+        partials[(size_t)blockIdx.x * R + B + 2] = s2;
+    }
+    __syncthreads();  // (red_s is reused by the final reduction)
+
+    // per-date seeds from cfbar_i = sum_{j<i} w_j [E_j > 0]
+    {
+        float cfbar = 0.f;
+        for (int i = 1; i <= B; ++i) {
+            const int j = i - 1;
+            if (e_s[j * C + tid] > 0.f) cfbar += (float)P.cvaw[j];
+            if (!active) cfbar = 0.f;
+            float xbar, abar;
+            date_seeds(P, i, (double)xs_s[i * C + tid], ds_s[i * C + tid], cfbar, xbar, abar);
+            xs_s[i * C + tid] = xbar;
+            ds_s[i * C + tid] = abar;
+        }
+    }
+
+    // ---------------------------------------------------------------- reverse
+    for (int q = 0; q < 9; ++q) cb_s[q * C + tid] = 0.0;
+    float2 sd[NS];  // {xbar_j, abar_j} of slot r's date j = B - r once the sweep reaches it
+#pragma unroll
+    for (int r = 0; r < NS; ++r) sd[r] = make_float2(0.f, 0.f);
+    float M0 = 0.f, M1 = 0.f, M2 = 0.f, I0 = 0.f, I1 = 0.f, I2 = 0.f;
+    const float dtau = (float)(1.0 / P.m);
+    const float k1 = P.c * dtau, k2 = P.c * dtau * dtau;
+    float r0, r1, r2;
+    draw_phi<float, false>(nullptr, gpath, lp, P.n_paths, n_steps - 1, P.rk0, P.rk1, r0, r1, r2);
+    for (int i = B; i >= 2; --i) {
+        {
+            const float xb = xs_s[i * C + tid], ab = ds_s[i * C + tid];
+            const int rs = B - i;
+#pragma unroll
+            for (int r = 0; r < NS; ++r)
+                if (r == rs) sd[r] = make_float2(xb, ab);
+            const float ti = dtau * (float)i;
+            I0 += ab;
+            I1 = fmaf(ab, ti, I1);
+            I2 = fmaf(ab, ti * ti, I2);
+            M0 += xb;
+            M1 = fmaf(xb, ti, M1);
+            M2 = fmaf(xb, ti * ti, M2);
+        }
+        float cbb[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) cbb[q] = 0.f;
+#pragma unroll 2
+        for (int n = i * stride - 1; n >= (i - 1) * stride; --n) {
+            M0 += I0;
+            M1 += I1;
+            M2 += I2;
+            const float phi0 = r0, phi1 = r1, phi2 = r2;
+            draw_phi<float, false>(nullptr, gpath, lp, P.n_paths, max(n - 1, stride), P.rk0, P.rk1, r0, r1, r2);
+            cbb[0] = fmaf(phi0, M0, cbb[0]);
+            cbb[1] = fmaf(phi0, M1, cbb[1]);
+            cbb[2] = fmaf(phi0, M2, cbb[2]);
+            cbb[3] = fmaf(phi1, M0, cbb[3]);
+            cbb[4] = fmaf(phi1, M1, cbb[4]);
+            cbb[5] = fmaf(phi1, M2, cbb[5]);
+            cbb[6] = fmaf(phi2, M0, cbb[6]);
+            cbb[7] = fmaf(phi2, M1, cbb[7]);
+            cbb[8] = fmaf(phi2, M2, cbb[8]);
+            // kappa g_n[L] from the slot dates' seeds and table row n
+            float2 kg = make_float2(0.f, 0.f);
+            const float4* rr = resp + (size_t)n * (NS / 2);
+#pragma unroll
+            for (int u = 0; u < NS / 2; ++u) {
+                const float4 e = __ldg(rr + u);
+                kg = __ffma2_rn(make_float2(e.x, e.y), sd[2 * u], kg);
+                kg = __ffma2_rn(make_float2(e.z, e.w), sd[2 * u + 1], kg);
+            }
+            M2 = fmaf(k2, M0, fmaf(2.f * k1, M1, M2)) + (kg.x + kg.y);
+            M1 = fmaf(k1, M0, M1);
+        }
+#pragma unroll
+        for (int q = 0; q < 9; ++q) cb_s[q * C + tid] += (double)cbb[q];
+    }
+
+    // ---------------------------------------------------------------- CTA reduction
+    // columns as adjoint_kernel's: [0..B] EE, B+1/B+2 CVA stats, E xbar_i,
+    // E abar_i (i = 1..B), the 9 coefficient columns
+    const int cx = B + 3, ca = 2 * B + 3, cc = 3 * B + 3;
+    double* wred = red_s;  // [warp][R]
+    for (int i = 1; i <= B; ++i) {
+        const double sx_ = warp_sum(active ? (double)xs_s[i * C + tid] : 0.0);
+        const double sa_ = warp_sum(active ? (double)ds_s[i * C + tid] : 0.0);
+        if (lane == 0) {
+            wred[warp * R + cx + i - 1] = sx_;
+            wred[warp * R + ca + i - 1] = sa_;
+        }
+    }
+    for (int q = 0; q < 9; ++q) {
+        const double sum = warp_sum(active ? cb_s[q * C + tid] : 0.0);
+        if (lane == 0) wred[warp * R + cc + q] = sum;
+    }
+    __syncthreads();
+    for (int col = cx + tid; col < R; col += C) {
+        double sum = 0.0;
+        for (int w = 0; w < C / 32; ++w) sum += wred[w * R + col];
+        partials[(size_t)blockIdx.x * R + col] = sum;
+    }
+}
+
+size_t adjoint_resp_smem(int n_blocks) { return adj_resp_layout(n_blocks, 3 * n_blocks + 12).total; }
+
+cudaError_t launch_adjoint_resp(const AdjParams& A, int ns, const float4* table, double* partials, cudaStream_t s)
+{
+    if (ns != 8 && ns != 16) return cudaErrorInvalidValue;
+    const int B = A.M.P.n_blocks;
+    if (B < 1 || B >= kMaxTenor || A.M.P.stride < 1) return cudaErrorInvalidValue;
+    auto k = ns == 8 ? adjoint_kernel_resp<8> : adjoint_kernel_resp<16>;
+    const size_t smem = adjoint_resp_smem(B);
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const int64_t grid = (A.M.P.n_paths + kAdjCta - 1) / kAdjCta;
+    k<<<(unsigned)grid, kAdjCta, smem, s>>>(A.M, table, partials);
+    return cudaGetLastError();
+}
+
 size_t adjoint_smem(int nt, int n_blocks, bool ckpt) { return adj_layout(nt, n_blocks, 3 * n_blocks + 12, ckpt).total; }
 
 int adjoint_columns(int nt, int n_blocks)

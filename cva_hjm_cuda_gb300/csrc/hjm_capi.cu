@@ -1467,7 +1467,13 @@ hjm_status hjm_run_adjoint(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, doubl
                     "volatility-coefficient sensitivities need a polynomial market (hjm_set_market_poly)");
     const int nt = ctx->nt, B = sh.B;
     const int R = adjoint_columns(nt, B);
-    const size_t smem = pc ? adjoint_pc_smem(nt, B) : adjoint_smem(nt, B, checkpoint_every > 0);
+    // quadratic factors under the Euler step with the sampled states kept:
+    // the response form's adjoint where the valuation's response form fits
+    const int adj_ns = (!pc && checkpoint_every == 0 && use_poly_path(ctx) && ctx->remainder != HJM_REMAINDER_CONVECT)
+                           ? mresp_run_slots(ctx, sh, dt)
+                           : 0;
+    const size_t smem = pc ? adjoint_pc_smem(nt, B)
+                           : (adj_ns ? adjoint_resp_smem(B) : adjoint_smem(nt, B, checkpoint_every > 0));
     if (smem > 227 * 1024) return fail(ctx, HJM_ERR_UNSUPPORTED, "adjoint shared memory %zu B exceeds 227 KB", smem);
     HJM_CUDA(ctx, cudaSetDevice(ctx->device));
     const int64_t n_ctas = (n_paths + adjoint_cta() - 1) / adjoint_cta();
@@ -1501,11 +1507,17 @@ hjm_status hjm_run_adjoint(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, doubl
     ctx->n_enqueued++;
     HJM_CUDA(ctx, cudaMemsetAsync(ctx->result.p, 0, sizeof(double) * kResLen, s));
     HJM_CUDA(ctx, cudaEventRecord(ctx->ev[0], s));
-    if (pc)
+    if (pc) {
         HJM_CUDA(ctx, launch_adjoint_pc(nt, Qp, use_poly_path(ctx), (double*)ctx->partials.p, s));
-    else
+    } else if (adj_ns) {
+        st = ensure_mresp_table(ctx, s);
+        if (st != HJM_OK) return st;
+        HJM_CUDA(ctx, launch_adjoint_resp(A, adj_ns, (const float4*)ctx->mresp.p, (double*)ctx->partials.p, s));
+        HJM_CUDA(ctx, cudaEventRecord(ctx->resp_used, s));
+    } else {
         HJM_CUDA(ctx, launch_adjoint(nt, A, use_poly_path(ctx), (double*)ctx->partials.p,
                                      K > 0 ? (float*)ctx->ck_h.p : nullptr, K > 0 ? (double*)ctx->ck_a.p : nullptr, s));
+    }
     HJM_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
     HJM_CUDA(ctx, launch_reduce((const double*)ctx->partials.p, n_ctas, R, (double*)ctx->sums.p, F,
                                 (double*)ctx->result.p, s));
@@ -1582,7 +1594,7 @@ hjm_status hjm_run_adjoint(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, doubl
     r.nt = nt;
     r.precision = HJM_PRECISION_MIXED;
     r.vol_form = use_poly_path(ctx) ? vol_form_code(ctx) : 0;  // a cubic market runs the table step here
-    r.remainder = 1;
+    r.remainder = adj_ns ? 2 : 1;
     r.scheme = ctx->scheme;
     r.ckpt = K;
     r.dt = dt;

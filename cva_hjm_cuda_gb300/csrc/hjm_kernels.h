@@ -176,6 +176,11 @@ int adjoint_columns(int nt, int n_blocks);
 int adjoint_cta();  // paths per CTA of the adjoint kernel (one partial-sum row each)
 cudaError_t launch_adjoint(int nt, const AdjParams& A, bool poly, double* partials, float* ck_h, double* ck_a,
                            cudaStream_t s);
+// the adjoint in the response form (Euler, quadratic factors, sampled states
+// kept): the mixed response form's forward pass and table (mresp_slots'
+// ns slots), the same partial-sum columns as launch_adjoint
+size_t adjoint_resp_smem(int n_blocks);
+cudaError_t launch_adjoint_resp(const AdjParams& A, int ns, const float4* table, double* partials, cudaStream_t s);
 // the predictor-corrector adjoint (sampled states kept; same partial-sum columns
 // as launch_adjoint, the coefficient columns gather phi_k (M0, M1, M2 + gL g[L]))
 size_t adjoint_pc_smem(int nt, int n_blocks);

@@ -36,32 +36,43 @@ def _poly(engine, spot=None, coef=DEFAULT_VOL_COEFFS, nt=51):
 
 
 def test_adjoint_cva_equals_mixed_forward(engine):
-    """The adjoint launch runs the convected mixed-precision valuation's
-    forward pass unchanged (checkpoint writes only read the state), so its
-    CVA, standard error and dCVA/dhazard equal that valuation's bit for bit in
-    both modes (and the default valuation, the remainder's FP32 responses,
-    within FP32 rounding)."""
+    """Each adjoint launch runs its valuation's forward pass unchanged: the
+    convected adjoint (checkpoints, or the convected form requested) the
+    convected mixed valuation's, bit for bit in CVA, standard error and
+    dCVA/dhazard (checkpoint writes only read the state); the response form's
+    adjoint (no checkpoints, the default) the response valuation's, whose
+    per-path cash flows it reproduces (its CTAs sum them in other groups)."""
     _poly(engine)
     cfg = RunConfig(n_paths=40000, seed=77)
     engine.set_remainder_form("convect")
     try:
         v = engine.run(cfg, "mixed", pfe=False)
+        a0c = engine.run_adjoint(cfg, checkpoint_every=0)
     finally:
         engine.set_remainder_form("auto")
     r = engine.run(cfg, "mixed", pfe=False)
     assert engine.remainder_form() == "response"
     assert abs(r.cva - v.cva) <= 1e-6 * v.cva
-    for k in (0, 32):
-        a = engine.run_adjoint(cfg, checkpoint_every=k)
+    for a in (a0c, engine.run_adjoint(cfg, checkpoint_every=32)):
         assert a.cva == v.cva
         assert a.cva_stderr == v.cva_stderr
         assert a.dcva_dhazard == v.dcva_dhazard
+    a0 = engine.run_adjoint(cfg, checkpoint_every=0)
+    assert abs(a0.cva - r.cva) <= 1e-12 * r.cva
+    assert abs(a0.cva_stderr - r.cva_stderr) <= 1e-9 * r.cva_stderr
+    assert abs(a0.dcva_dhazard - r.dcva_dhazard) <= 1e-12 * abs(r.dcva_dhazard)
 
 
 def test_checkpoint_mode_matches_seed_mode(engine):
+    """The convected adjoint with checkpoints against the convected adjoint
+    that keeps the sampled states (the same forward pass: CVA bit for bit)."""
     _poly(engine)
     cfg = RunConfig(n_paths=20000, seed=5)
-    a = engine.run_adjoint(cfg, checkpoint_every=0)
+    engine.set_remainder_form("convect")
+    try:
+        a = engine.run_adjoint(cfg, checkpoint_every=0)
+    finally:
+        engine.set_remainder_form("auto")
     for k in (32, 50, 7):
         b = engine.run_adjoint(cfg, checkpoint_every=k)
         assert b.cva == a.cva

@@ -299,9 +299,9 @@ def test_one_and_two_dates_every_mode(engine, n_steps):
     engine.set_market_poly(51, 0.5, mk.spot, DEFAULT_VOL_COEFFS)
     engine.set_swap(sw)
     v = engine.run(cfg, "mixed", pfe=False)
-    for k in (0, 32):
+    for k in (0, 32):  # (the response form's adjoint, the convected one's)
         s = engine.run_adjoint(cfg, checkpoint_every=k)
-        assert s.cva == v.cva and np.all(np.isfinite(s.dcva_dspot))
+        assert abs(s.cva - v.cva) <= 1e-6 * abs(v.cva) and np.all(np.isfinite(s.dcva_dspot))
     m = engine.run_mlmc([777, 512], n_steps=n_steps // 2, dt=0.02, seed=2)
     assert np.isfinite(m["cva"]) and m["levels"][1]["n_paths"] == 512
 

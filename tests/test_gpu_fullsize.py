@@ -123,8 +123,8 @@ def test_config4_adjoint_full_size(engine):
     n = 1_048_576
     cfg = RunConfig(n_paths=n, seed=1234)
     a32 = engine.run_adjoint(cfg, checkpoint_every=32)
-    a0 = engine.run_adjoint(cfg, checkpoint_every=0)
-    assert a32.cva == a0.cva
+    a0 = engine.run_adjoint(cfg, checkpoint_every=0)  # the response form's adjoint
+    assert abs(a32.cva - a0.cva) <= 1e-6 * a0.cva
     for name in ("dcva_dspot", "dcva_ddrift"):
         g32, g0 = getattr(a32, name), getattr(a0, name)
         np.testing.assert_allclose(g32, g0, rtol=1e-4, atol=1e-4 * np.max(np.abs(g0)), err_msg=name)

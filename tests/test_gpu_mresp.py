@@ -134,3 +134,36 @@ def test_mixed_response_path_ranges_compose(engine):
     a = engine.run(RunConfig(n_paths=n // 2, seed=9), "mixed", pfe=False)
     b = engine.run(RunConfig(n_paths=n // 2, seed=9, path_offset=n // 2), "mixed", pfe=False)
     np.testing.assert_allclose(full.ee, 0.5 * (a.ee + b.ee), rtol=1e-12, atol=1e-12 * np.max(full.ee))
+
+
+@pytest.mark.parametrize("n_periods", [20, 24])
+def test_response_adjoint_vs_convected_adjoint(engine, n_periods, tmp_path):
+    """The adjoint in the response form (the sampled states kept, the sweep's
+    last-tenor adjoint from the table: 8 slots for 10y, 16 for 12y) against
+    the convected adjoint on the same paths: every sensitivity within 1e-4 of
+    its group's largest (FP32 rounding of two orderings), CVA within 1e-6."""
+    import json
+
+    from cva_hjm_cuda_gb300.market import DEFAULT_VOL_COEFFS, nelson_siegel_curve, tenor_grid
+
+    engine.set_market_poly(51, 0.5, nelson_siegel_curve(tenor_grid(51, 0.5)), DEFAULT_VOL_COEFFS)
+    engine.set_swap(Swap(n_periods=n_periods))
+    cfg = RunConfig(n_paths=30_011, n_steps=50 * n_periods, seed=21)
+    a = engine.run_adjoint(cfg, checkpoint_every=0)
+    engine.write_report(tmp_path / "a.json")
+    assert json.loads((tmp_path / "a.json").read_text())["run"]["remainder"] == "response"
+    engine.set_remainder_form("convect")
+    try:
+        c = engine.run_adjoint(cfg, checkpoint_every=0)
+        engine.write_report(tmp_path / "c.json")
+        assert json.loads((tmp_path / "c.json").read_text())["run"]["remainder"] == "convect"
+    finally:
+        engine.set_remainder_form("auto")
+    assert abs(a.cva - c.cva) <= 1e-6 * c.cva
+    assert abs(a.dcva_dhazard - c.dcva_dhazard) <= 1e-6 * abs(c.dcva_dhazard)
+    for name in ("dcva_dspot", "dcva_ddrift", "dcva_dvolcoef"):
+        ga, gc = np.ravel(getattr(a, name)), np.ravel(getattr(c, name))
+        if name == "dcva_dvolcoef":  # in units of a volatility change at T = 25y
+            w = np.array([25.0 ** (q % 3) for q in range(9)])
+            ga, gc = ga / w, gc / w
+        np.testing.assert_allclose(ga, gc, rtol=0, atol=1e-4 * np.max(np.abs(gc)), err_msg=name)
