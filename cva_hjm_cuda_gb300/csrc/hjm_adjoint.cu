@@ -796,7 +796,7 @@ __global__ void __launch_bounds__(kAdjCta, adj_resp_min_ctas(NS))
     for (int b = 1; b < B; ++b) {
         float sS = 0.f, sU = 0.f, sW = 0.f;
         const float4* row = resp + (size_t)b * stride * (NS / 2);
-#pragma unroll 2
+#pragma unroll 5  // (a divisor of 50 steps per block: 8.66 ms against 8.77 by 2 at 1M paths)
         for (int s = 0; s < stride; ++s) {
             const int n = b * stride + s;
             const float phi0 = q0, phi1 = q1, phi2 = q2;
