@@ -1068,6 +1068,9 @@ def adjoint_cost(eng, args, flush) -> dict:
     eng.set_swap(Swap())
     cfg = RunConfig(n_paths=n, n_steps=N_STEPS, dt=DT, seed=SEED)
     out = {"n_paths": n, "n_sensitivities": 51 + 51 + 9 + 1}
+    # checkpoints every 32 steps: the convected adjoint (curve states stored
+    # and recomputed); none: the response form's adjoint, which keeps each
+    # date's sampled state (the sweep needs no other forward state)
     for label, k in (("checkpoint_32", 32), ("no_checkpoint", 0)):
         for _ in range(args.warmup):
             eng.run_adjoint(cfg, checkpoint_every=k)
@@ -1077,7 +1080,7 @@ def adjoint_cost(eng, args, flush) -> dict:
             torch.cuda.synchronize()
             sens = eng.run_adjoint(cfg, checkpoint_every=k)
             ms.append(float(eng.timing_history(1)[0, 3]))
-        out[label] = {"ms": statistics.median(ms)}
+        out[label] = {"ms": statistics.median(ms), "remainder": "convect" if k else "response"}
     for _ in range(args.warmup):
         eng.run(cfg, "mixed", pfe=False)
     ms = []

@@ -119,11 +119,13 @@ class HJMEngine:
         self._check(self.lib.hjm_ctx_set_scheme(self.ctx, {"euler": 0, "predictor_corrector": 1}[scheme]))
 
     def set_remainder_form(self, form: str = "auto") -> None:
-        """FP64 transport form: "convect" (the remainder, or with a table of
-        any shape the whole stochastic curve, over the live tenors every step
-        in FP64), "response" (impulse-response sums at the sampled tenors in
-        double-FP32, in windows of at most 24 dates) or "auto" (the response
-        form)."""
+        """Transport form of the remainder: "convect" (the remainder, or with a
+        table of any shape the whole stochastic curve, over the live tenors
+        every step), "response" (impulse-response sums at the sampled tenors:
+        FP64 valuations in double-FP32, in windows of dates; mixed precision
+        and its adjoint without checkpoints in FP32 where the dates the
+        remainder reaches fit 16 slots) or "auto" (the response form where it
+        applies)."""
         self._check(self.lib.hjm_ctx_set_remainder_form(self.ctx, {"auto": 0, "convect": 1, "response": 2}[form]))
 
     def remainder_form(self) -> str:

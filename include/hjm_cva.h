@@ -284,8 +284,16 @@ hjm_status hjm_calibrate_pca(const double* curves, int32_t n_obs, int32_t n_teno
  * checkpointed every checkpoint_every steps (0 = none: the sampled states are
  * kept instead) and each date's state is recomputed from the last checkpoint
  * before it for the reverse sweep; the predictor-corrector scheme keeps the
- * sampled states (checkpoint_every must be 0).  The coefficient sensitivities
- * require a market set through hjm_set_market_poly. */
+ * sampled states (checkpoint_every must be 0).  With checkpoint_every = 0,
+ * quadratic factors and the Euler step, the adjoint runs in the response
+ * form where the mixed valuation does (the remainder's FP32 responses in the
+ * forward pass; in the reverse sweep the remainder's adjoint at the last
+ * tenor from the same table and the sampled dates' seeds): it needs no
+ * forward state but the sampled one, so there is nothing to checkpoint
+ * (8.7 ms at 1,048,576 paths on the 10y swap, against 16.3 ms with
+ * checkpoints every 32 steps); HJM_REMAINDER_CONVECT keeps the convected
+ * adjoint.  The coefficient sensitivities require a market set through
+ * hjm_set_market_poly. */
 hjm_status hjm_set_market_poly(hjm_ctx* ctx, int32_t n_tenor, double dtau, const double* spot_host,
                                const double* vol_coef_host /* [3][3] */);
 hjm_status hjm_run_adjoint(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, double dt, uint64_t seed,
