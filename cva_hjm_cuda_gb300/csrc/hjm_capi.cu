@@ -139,7 +139,7 @@ struct hjm_ctx {
         std::vector<double> sv;
     } vresp_key;
     struct MrespKey {  // the mixed-precision response form's slots and its table in mresp
-        bool valid = false, on_device = false;
+        bool valid = false, on_device = false, pc = false;
         int nt = 0, stride = 0, B = 0, ns = 0;
         double c = 0, dtau = 0;
     } mresp_key;
@@ -998,14 +998,16 @@ __attribute__((visibility("hidden"))) void mixed_cubic_params(int nt, double dta
 }
 }  // namespace hjm
 
-// The date slots of the mixed-precision response form for the run shape (0:
-// the run convects), counted on the host once per shape.
-static int mresp_run_slots(hjm_ctx* ctx, const RunShape& sh, double dt)
+// The date slots of the mixed-precision response form for the run shape and
+// scheme (0: the run convects), counted on the host once per shape.
+static int mresp_run_slots(hjm_ctx* ctx, const RunShape& sh, double dt, bool pc = false)
 {
     const double c = dt / ctx->dtau;
     hjm_ctx::MrespKey& k = ctx->mresp_key;
-    if (!(k.valid && k.nt == ctx->nt && k.stride == sh.stride && k.B == sh.B && k.c == c && k.dtau == ctx->dtau)) {
-        k.ns = mresp_slots(ctx->nt, c, sh.stride, sh.B);
+    if (!(k.valid && k.pc == pc && k.nt == ctx->nt && k.stride == sh.stride && k.B == sh.B && k.c == c &&
+          k.dtau == ctx->dtau)) {
+        k.ns = mresp_slots(ctx->nt, c, ctx->dtau, sh.stride, sh.B, pc);
+        k.pc = pc;
         k.nt = ctx->nt;
         k.stride = sh.stride;
         k.B = sh.B;
@@ -1030,7 +1032,7 @@ static hjm_status ensure_mresp_table(hjm_ctx* ctx, cudaStream_t s)
         HJM_CUDA(ctx, ctx->mresp.ensure(bytes));  // cudaFree waits for the device
     else
         HJM_CUDA(ctx, cudaStreamWaitEvent(s, ctx->resp_used, 0));
-    HJM_CUDA(ctx, launch_mresp_table(k.nt, k.c, k.dtau, k.stride, k.B, k.ns, (float4*)ctx->mresp.p, s));
+    HJM_CUDA(ctx, launch_mresp_table(k.nt, k.c, k.dtau, k.stride, k.B, k.ns, k.pc, (float4*)ctx->mresp.p, s));
     ctx->stat_launches += 1;
     k.on_device = true;
     return HJM_OK;
@@ -1071,11 +1073,12 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
     const bool mixed_cubic = mixed && !pc && use_cubic_path(ctx);
     // mixed precision with polynomial factors: the response form when the
     // dates its remainder reaches fit its slots (else the convected pairs)
-    const int mresp_ns = (mixed && !pc && (use_poly_path(ctx) || mixed_cubic) && use_response_form(ctx, sh))
-                             ? mresp_run_slots(ctx, sh, dt)
+    const int mresp_ns = (mixed && (pc ? use_poly_path(ctx) : (use_poly_path(ctx) || mixed_cubic)) &&
+                          use_response_form(ctx, sh))
+                             ? mresp_run_slots(ctx, sh, dt, pc)
                              : 0;
-    const int cta = pc ? pc_cta()
-                       : (mresp_ns ? kCta : path_cta(mixed, ctx->nt, sh.B, use_poly_path(ctx) || mixed_cubic));
+    const int cta = mresp_ns ? kCta
+                             : (pc ? pc_cta() : path_cta(mixed, ctx->nt, sh.B, use_poly_path(ctx) || mixed_cubic));
     const int64_t n_ctas = (n_paths + cta - 1) / cta;
     const int64_t ld = (n_paths + 3) / 4 * 4;
     const size_t esize = mixed ? 4 : 8;
@@ -1110,8 +1113,30 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
         PcParams<float> Q;
         fill_pc<float>(ctx, sh, dt, P, Q);
         ctx->stat_h2d = sizeof(Q) + sizeof(FinalParams);
-        HJM_CUDA(ctx, launch_path_pc(ctx->nt, Q, use_poly_path(ctx), ext_dev, (double*)ctx->partials.p,
-                                     store ? (float*)ctx->estore.p : nullptr, s));
+        if (mresp_ns) {
+            // the response form: the two-stage step's parts are the Euler
+            // kernel's update with the N-projected loadings and (c + c^2) dtau^2
+            MixedParams M;
+            std::memset(&M, 0, sizeof(M));
+            M.P = Q.P;
+            for (int k = 0; k < kFactors; ++k) {
+                M.svcf[k][0] = Q.aS[k];
+                M.svcf[k][1] = Q.aU[k];
+                M.svcf[k][2] = Q.aW[k];
+            }
+            M.k1f = Q.k1;
+            M.k2f = Q.k2p;
+            st = ensure_mresp_table(ctx, s);
+            if (st != HJM_OK) return st;
+            HJM_CUDA(ctx, launch_path_mixed_resp(M, mresp_ns, false, (const float4*)ctx->mresp.p, ext_dev,
+                                                 (double*)ctx->partials.p, store ? (float*)ctx->estore.p : nullptr,
+                                                 s));
+            HJM_CUDA(ctx, cudaEventRecord(ctx->resp_used, s));
+            resp = true;
+        } else {
+            HJM_CUDA(ctx, launch_path_pc(ctx->nt, Q, use_poly_path(ctx), ext_dev, (double*)ctx->partials.p,
+                                         store ? (float*)ctx->estore.p : nullptr, s));
+        }
     } else if (pc) {
         PathParams<double> P;
         fill_params<double>(ctx, sh, n_paths, dt, seed, path_offset, hazard, recovery, ld, store, P, F);

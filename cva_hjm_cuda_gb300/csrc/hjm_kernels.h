@@ -91,10 +91,14 @@ void pack_mixed_params(int nt, const PathParams<float>& P, MixedParams& M);
 // do not fit 16 (the run then convects); launch_mresp_table: the table on
 // the stream (rows b stride + s of ns / 2 float4, each two {kappa G,
 // kappa CG} pairs; mresp_table_elems float4).
-int mresp_slots(int nt, double c, int stride, int n_blocks);
+// pc: the predictor-corrector step's remainder (its parts then run the same
+// kernel with the N-projected loadings aS, aU, aW as the coefficients of 1,
+// T, T^2 and k2f = (c + c^2) dtau^2; not for a run whose last date samples
+// the last tenor)
+int mresp_slots(int nt, double c, double dtau, int stride, int n_blocks, bool pc = false);
 size_t mresp_table_elems(int stride, int n_blocks, int ns);
-cudaError_t launch_mresp_table(int nt, double c, double dtau, int stride, int n_blocks, int ns, float4* table,
-                               cudaStream_t s);
+cudaError_t launch_mresp_table(int nt, double c, double dtau, int stride, int n_blocks, int ns, bool pc,
+                               float4* table, cudaStream_t s);
 size_t mresp_smem_bytes(int n_blocks);
 // paths per CTA: kCta, as launch_path_mixed's table form (path_cta)
 cudaError_t launch_path_mixed_resp(const MixedParams& M, int ns, bool cub, const float4* table, const double* ext,

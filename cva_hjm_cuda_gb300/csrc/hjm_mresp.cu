@@ -154,25 +154,73 @@ __global__ void __launch_bounds__(kCta, mresp_min_ctas(NS))
 // ---------------------------------------------------------------------------
 size_t mresp_smem_bytes(int n_blocks) { return (size_t)(n_blocks + 2) * kCta * sizeof(float) + 2 * (kCta / 32) * 8; }
 
-int mresp_slots(int nt, double c, int stride, int n_blocks)
+// The predictor-corrector's remainder sources per unit W: w0 W_old at L - 1,
+// w1 W_old + w2 W_new at L (w0 = -c^2 dtau^2, w1 = -(c + c^2) dtau^2, w2 =
+// -c dtau^2; their sum is the step's kappa).
+static void pc_sources(double c, double dtau, double& w0, double& w1, double& w2)
+{
+    const double d2 = dtau * dtau;
+    w0 = -c * c * d2;
+    w1 = -(c + c * c) * d2;
+    w2 = -c * d2;
+}
+
+int mresp_slots(int nt, double c, double dtau, int stride, int n_blocks, bool pc)
 {
     const int B = n_blocks, L = nt - 1;
     if (nt < 3 || nt > kMaxTenor || B < 1 || B >= nt || stride < 1 || !(c > 0.0 && c < 1.0)) return 0;
+    // (the predictor-corrector's date at the last tenor takes a lag -1 term
+    // this kernel leaves out)
+    if (pc && B == L) return 0;
     const double thr = std::ldexp(1.0, -30);
     const int M = (B - 1) * stride - 1;  // the longest lag read
-    double v[kMaxTenor] = {}, vn[kMaxTenor], cum[kMaxTenor] = {};
+    // Euler: G = A^m e_L.  Predictor-corrector: H(l) = w0 G1(l) + w1 G2(l) +
+    // w2 G2(l + 1) per unit kappa, G1, G2 the three-point step's responses to
+    // e_{L-1}, e_L (the tables' recursions, eresp_table_pc_kernel)
+    double w0 = 0.0, w1 = 0.0, w2 = 0.0, kap = 1.0;
+    if (pc) {
+        pc_sources(c, dtau, w0, w1, w2);
+        kap = std::fabs(w0 + w1 + w2);
+    }
+    const double a0 = 1.0 - c + 0.5 * c * c, a1 = c - c * c, a2 = 0.5 * c * c;
+    double v[kMaxTenor] = {}, vn[kMaxTenor], cum[kMaxTenor] = {};   // Euler, or G2 for the predictor-corrector
+    double u[kMaxTenor] = {}, un[kMaxTenor], cu[kMaxTenor] = {};    // G1
+    double hp[kMaxTenor] = {}, chp[kMaxTenor] = {};                 // w0 G1 + w1 G2 at the previous lag
     v[L] = 1.0;
+    if (pc) u[L - 1] = 1.0;
     int need = 0;
-    for (int m = 0; m <= M; ++m) {
-        for (int t = 0; t < nt; ++t) cum[t] += v[t];
-        // date j reads lags up to K_j - stride = (j - 1) stride - 1; the
-        // latest dates' slots come first, so only dates below B - need matter
-        for (int j = 2; j < B + 1 - need; ++j)
-            if (m <= (j - 1) * stride - 1 &&
-                (std::fabs(v[j]) >= thr || std::fabs(cum[j]) >= thr * (double)(j * stride)))
-                need = B - j + 1;
-        for (int t = 0; t < L; ++t) vn[t] = v[t] + c * (v[t + 1] - v[t]);
-        vn[L] = v[L] + c * (v[L] - v[L - 1]);
+    for (int m = 0; m <= M + (pc ? 1 : 0); ++m) {
+        for (int t = 0; t < nt; ++t) {
+            cum[t] += v[t];
+            cu[t] += u[t];
+        }
+        const int l = pc ? m - 1 : m;  // the lag this iteration completes
+        if (l >= 0)
+            for (int j = 2; j < B + 1 - need; ++j) {
+                // date j reads lags up to K_j - stride = (j - 1) stride - 1
+                if (l > (j - 1) * stride - 1) continue;
+                const double h = pc ? (hp[j] + w2 * v[j]) / kap : v[j];
+                const double ch = pc ? (chp[j] + w2 * cum[j]) / kap : cum[j];
+                if (std::fabs(h) >= thr || std::fabs(ch) >= thr * (double)(j * stride)) need = B - j + 1;
+            }
+        if (pc) {
+            for (int t = 0; t < nt; ++t) {
+                hp[t] = w0 * u[t] + w1 * v[t];
+                chp[t] = w0 * cu[t] + w1 * cum[t];
+            }
+            for (int t = 0; t < L - 1; ++t) {
+                vn[t] = a0 * v[t] + a1 * v[t + 1] + a2 * v[t + 2];
+                un[t] = a0 * u[t] + a1 * u[t + 1] + a2 * u[t + 2];
+            }
+            vn[L - 1] = v[L - 1] + c * (v[L] - v[L - 1]);
+            un[L - 1] = u[L - 1] + c * (u[L] - u[L - 1]);
+            vn[L] = v[L] + c * (v[L] - v[L - 1]);
+            un[L] = u[L] + c * (u[L] - u[L - 1]);
+            for (int t = 0; t < nt; ++t) u[t] = un[t];
+        } else {
+            for (int t = 0; t < L; ++t) vn[t] = v[t] + c * (v[t + 1] - v[t]);
+            vn[L] = v[L] + c * (v[L] - v[L - 1]);
+        }
         for (int t = 0; t < nt; ++t) v[t] = vn[t];
     }
     return need <= 8 ? 8 : (need <= 16 ? 16 : 0);
@@ -211,14 +259,67 @@ __global__ void __launch_bounds__(kMaxTenor)
     }
 }
 
-cudaError_t launch_mresp_table(int nt, double c, double dtau, int stride, int n_blocks, int ns, float4* table,
-                               cudaStream_t s)
+// The predictor-corrector's table in the same layout: per old W at lag l,
+// {H(l), CH(l)} with H(l) = w0 G1(l) + w1 G2(l) + w2 G2(l + 1) (W_new of one
+// step is W_old of the next) and CH likewise from the running sums, the
+// recursions of eresp_table_pc_kernel (hjm_eresp.cu) rounded to FP32.
+__global__ void __launch_bounds__(kMaxTenor)
+    mresp_table_pc_kernel(int nt, double c, int stride, int B, int ns, double w0, double w1, double w2,
+                          float4* __restrict__ table)
+{
+    __shared__ double v_s[kMaxTenor + 2], u_s[kMaxTenor + 2];
+    const int t = threadIdx.x;
+    const int L = nt - 1;
+    const int M = (B - 1) * stride - 1;
+    const double a0 = 1.0 - c + 0.5 * c * c, a1 = c - c * c, a2 = 0.5 * c * c;
+    const int r = B - t;
+    const bool keep = t >= 2 && t <= B && r < ns;
+    double g1 = (t == L - 1) ? 1.0 : 0.0, g2 = (t == L) ? 1.0 : 0.0;
+    double cg1 = 0.0, cg2 = 0.0, hp = 0.0, chp = 0.0;
+    float2* row2 = reinterpret_cast<float2*>(table);
+    for (int m = 0; m <= M + 1; ++m) {
+        cg1 += g1;
+        cg2 += g2;
+        const int l = m - 1;  // the lag this iteration completes
+        if (keep && l >= 0 && l <= (t - 1) * stride - 1) {
+            const size_t n = (size_t)t * stride - 1 - (size_t)l;
+            row2[n * ns + r] = make_float2((float)(hp + w2 * g2), (float)(chp + w2 * cg2));
+        }
+        hp = w0 * g1 + w1 * g2;
+        chp = w0 * cg1 + w1 * cg2;
+        if (t < nt) {
+            v_s[t] = g1;
+            u_s[t] = g2;
+        }
+        __syncthreads();
+        if (t < L - 1) {
+            g1 = a0 * g1 + a1 * v_s[t + 1] + a2 * v_s[t + 2];
+            g2 = a0 * g2 + a1 * u_s[t + 1] + a2 * u_s[t + 2];
+        } else if (t == L - 1) {
+            g1 += c * (v_s[L] - g1);
+            g2 += c * (u_s[L] - g2);
+        } else if (t == L) {
+            g1 += c * (g1 - v_s[L - 1]);
+            g2 += c * (g2 - u_s[L - 1]);
+        }
+        __syncthreads();
+    }
+}
+
+cudaError_t launch_mresp_table(int nt, double c, double dtau, int stride, int n_blocks, int ns, bool pc,
+                               float4* table, cudaStream_t s)
 {
     if (nt < 3 || nt > kMaxTenor || n_blocks < 1 || n_blocks >= nt || stride < 1 || (ns != 8 && ns != 16))
         return cudaErrorInvalidValue;
     cudaError_t e = cudaMemsetAsync(table, 0, sizeof(float4) * mresp_table_elems(stride, n_blocks, ns), s);
     if (e != cudaSuccess) return e;
-    mresp_table_kernel<<<1, kMaxTenor, 0, s>>>(nt, c, stride, n_blocks, ns, -2.0 * c * dtau * dtau, table);
+    if (pc) {
+        double w0, w1, w2;
+        pc_sources(c, dtau, w0, w1, w2);
+        mresp_table_pc_kernel<<<1, kMaxTenor, 0, s>>>(nt, c, stride, n_blocks, ns, w0, w1, w2, table);
+    } else {
+        mresp_table_kernel<<<1, kMaxTenor, 0, s>>>(nt, c, stride, n_blocks, ns, -2.0 * c * dtau * dtau, table);
+    }
     return cudaGetLastError();
 }
 

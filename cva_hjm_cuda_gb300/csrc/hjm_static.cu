@@ -265,7 +265,7 @@ hjm_status hjm_run_static(void* cuda_stream, int32_t n_tenor, double dtau, const
     // mixed precision with polynomial factors: the response form when the
     // dates its remainder reaches fit its slots and its table the static array
     const int mresp_ns =
-        (precision == HJM_PRECISION_MIXED && (poly || cub)) ? mresp_slots(n_tenor, dt / dtau, (int)stride, B) : 0;
+        (precision == HJM_PRECISION_MIXED && (poly || cub)) ? mresp_slots(n_tenor, dt / dtau, dtau, (int)stride, B) : 0;
     const bool mresp = mresp_ns > 0 && mresp_table_elems((int)stride, B, mresp_ns) <= kStaticRespEntries;
     const int cta = mresp ? kCta : path_cta(precision == HJM_PRECISION_MIXED, n_tenor, B, poly || cub);
     const int64_t n_ctas = (n_paths + cta - 1) / cta;
@@ -317,7 +317,7 @@ hjm_status hjm_run_static(void* cuda_stream, int32_t n_tenor, double dtau, const
         if (cub) mixed_cubic_params(n_tenor, dtau, dt, B, cubic, M);
         if (mresp) {
             float4* table = reinterpret_cast<float4*>(resp_table);
-            STATIC_CUDA(launch_mresp_table(n_tenor, dt / dtau, dtau, (int)stride, B, mresp_ns, table, s));
+            STATIC_CUDA(launch_mresp_table(n_tenor, dt / dtau, dtau, (int)stride, B, mresp_ns, false, table, s));
             STATIC_CUDA(launch_path_mixed_resp(M, mresp_ns, cub, table, nullptr, partials, nullptr, s));
         } else {
             STATIC_CUDA(launch_path_mixed(n_tenor, M, poly, nullptr, partials, nullptr, s, cub));

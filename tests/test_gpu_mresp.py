@@ -167,3 +167,31 @@ def test_response_adjoint_vs_convected_adjoint(engine, n_periods, tmp_path):
             w = np.array([25.0 ** (q % 3) for q in range(9)])
             ga, gc = ga / w, gc / w
         np.testing.assert_allclose(ga, gc, rtol=0, atol=1e-4 * np.max(np.abs(gc)), err_msg=name)
+
+
+def test_pc_mixed_response_vs_convected_and_oracle(engine):
+    """The predictor-corrector step in mixed precision: its remainder (sources
+    at L - 1 and L from the old and new W) in FP32 responses of the
+    three-point step, the parts by the same kernel with the N-projected
+    loadings; against its convected kernel and the PC oracle."""
+    mk, sw = Market(), Swap()
+    engine.set_market(mk)
+    engine.set_swap(sw)
+    engine.set_scheme("predictor_corrector")
+    try:
+        cfg = RunConfig(n_paths=3001, seed=13)
+        (r, xr, fr), (c, xc, fc) = _both_forms(engine, cfg)
+        assert (fr, fc) == ("response", "convect")
+        scale = np.max(np.abs(xc))
+        assert np.max(np.abs(xr - xc)) <= FORM_TOL * scale
+        np.testing.assert_allclose(r.ee[:21], c.ee[:21], rtol=FORM_TOL, atol=FORM_TOL * np.max(c.ee))
+        assert abs(r.cva - c.cva) <= FORM_TOL * c.cva
+        normals = engine.dump_normals(cfg.n_paths, cfg.n_steps, cfg.seed)
+        xo = O.exposure_paths_pc(mk, sw, cfg.n_steps, cfg.dt, normals)[:, :21].T
+        assert np.max(np.abs(xr - xo)) <= MIXED_RTOL * np.max(np.abs(xo))
+        # the 25y swap (its last date samples the last tenor) convects
+        engine.set_swap(Swap(n_periods=50))
+        engine.run(RunConfig(n_paths=300, n_steps=2500, seed=13), "mixed")
+        assert engine.remainder_form() == "convect"
+    finally:
+        engine.set_scheme("euler")

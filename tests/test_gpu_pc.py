@@ -100,15 +100,23 @@ def test_pc_external_normals_and_61_tenors(pc, precision):
 
 
 def test_pc_adjoint_cva_equals_pc_mixed_valuation(pc):
-    """The predictor-corrector adjoint runs the mixed-precision valuation's
-    forward pass (the shared path state), so CVA, its standard error and
-    dCVA/dhazard are the valuation's bit for bit; it keeps the sampled states
-    (checkpoint_every = 0 only)."""
+    """The predictor-corrector adjoint runs the convected mixed-precision
+    valuation's forward pass (the shared path state), so CVA, its standard
+    error and dCVA/dhazard are that valuation's bit for bit (the default
+    valuation, the remainder's FP32 responses, within FP32 rounding); it keeps
+    the sampled states (checkpoint_every = 0 only)."""
     mk = Market()
     pc.set_market_poly(51, 0.5, mk.spot, DEFAULT_VOL_COEFFS)
     pc.set_swap(Swap())
     cfg = RunConfig(n_paths=40000, seed=77)
-    v = pc.run(cfg, "mixed", pfe=False)
+    r = pc.run(cfg, "mixed", pfe=False)
+    assert pc.remainder_form() == "response"
+    pc.set_remainder_form("convect")
+    try:
+        v = pc.run(cfg, "mixed", pfe=False)
+    finally:
+        pc.set_remainder_form("auto")
+    assert abs(r.cva - v.cva) <= 1e-6 * v.cva
     a = pc.run_adjoint(cfg, checkpoint_every=0)
     assert a.cva == v.cva
     assert a.cva_stderr == v.cva_stderr
