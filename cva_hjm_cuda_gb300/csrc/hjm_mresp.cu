@@ -25,6 +25,13 @@
 // resolution of the curve); runs whose counting dates fit 8 or 16 slots take
 // this kernel, the others (the 25y and 30y runs: 38 and 44 slots) the
 // convected form.
+//
+// The predictor-corrector step runs the same kernel: its parts advance by
+// the same update with the N-projected loadings and (c + c^2) dtau^2, and its
+// remainder, driven at L - 1 and L by the old and the new W, has per old W
+// the responses H(l) = w0 G1(l) + w1 G2(l) + w2 G2(l + 1) of the three-point
+// step (mresp_table_pc_kernel); a run whose last date samples the last tenor
+// (its own step's new W enters there with no lag) convects.
 #include <cuda_runtime.h>
 
 #include <algorithm>

@@ -149,9 +149,12 @@ hjm_status hjm_ctx_vol_decomposition(hjm_ctx* ctx, int32_t* active);
  * whose responses ever reach 2^-30 of the source fit 16 slots (the 10y swap's
  * 20 dates on 51 tenors: 8), else convects it in FP32 pairs (the 25y swap,
  * the 30y netting set); the two agree to FP32 rounding (~1e-7 of the
- * exposure scale).  AUTO and RESPONSE take it where it fits; mixed precision
- * under the predictor-corrector scheme, the adjoint and MLMC convect.  The
- * report names the form a valuation ran ("remainder"). */
+ * exposure scale).  AUTO and RESPONSE take it where it fits, under either
+ * scheme (the predictor-corrector's only when its last date does not sample
+ * the last tenor), and in hjm_run_adjoint without checkpoints (Euler); the
+ * adjoint with checkpoints, the predictor-corrector's adjoint and MLMC's
+ * coupled levels convect.  The report names the form a valuation ran
+ * ("remainder"). */
 #define HJM_REMAINDER_AUTO 0
 #define HJM_REMAINDER_CONVECT 1
 #define HJM_REMAINDER_RESPONSE 2
