@@ -144,7 +144,7 @@ hjm_status hjm_ctx_vol_decomposition(hjm_ctx* ctx, int32_t* active);
  * earlier ones.  HJM_REMAINDER_AUTO (default) takes the response form for
  * every FP64 valuation.  Both time schemes; the forms agree to rounding
  * (per-path exposures within ~1e-13 of the exposure scale).  Mixed precision
- * with the decomposition (Euler step) carries the remainder as FP32
+ * with the decomposition carries the remainder as FP32
  * impulse-response sums (one packed FMA per date per step) when the dates
  * whose responses ever reach 2^-30 of the source fit 16 slots (the 10y swap's
  * 20 dates on 51 tenors: 8), else convects it in FP32 pairs (the 25y swap,
