@@ -229,6 +229,19 @@ def mixed_response_flops_per_path(n_tenor: int, n_steps: int, stride: int, form:
     return sum(stride * (parts + 4 * min(ns, B - b)) for b in range(1, B))
 
 
+def adjoint_response_flops_per_path(n_tenor: int, n_steps: int, stride: int, form: str = "poly_tri") -> int:
+    """FP32 flops per path of the response form's adjoint
+    (adjoint_kernel_resp): its forward pass, the mixed response form's count
+    (``mixed_response_flops_per_path``), and per reverse step the discount
+    seeds into the three moments (3 ADD), the nine coefficient products (9
+    FMA), the moments' step (3 FMA + 1 ADD) and one packed FMA (4 flops) per
+    slot for the remainder's last-tenor adjoint."""
+    B = n_steps // stride
+    ns = mixed_response_slots(n_tenor, n_steps, stride)
+    reverse = (B - 1) * stride * (3 + 18 + 7 + 4 * ns)
+    return mixed_response_flops_per_path(n_tenor, n_steps, stride, form) + reverse
+
+
 def eresp_windows(n_blocks: int, dates: int = 24) -> list[tuple[int, int]]:
     """The Euler response form's windows of dates, latest first (eresp_windows,
     every date from 2 on active: ``dates`` of them per window)."""
@@ -385,7 +398,9 @@ def run_reference(args) -> None:
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": wl["name"], "sample_paths_per_step": n, "n_steps": N_STEPS, "dt": DT,
+        "config": {"workload": (wl["name"].replace("ckpt32", f"ckpt{args.checkpoint_every}"
+                                                   if args.checkpoint_every else "sampled-states")
+                                if is_adjoint else wl["name"]), "sample_paths_per_step": n, "n_steps": N_STEPS, "dt": DT,
                    "n_tenor": 51, "l2": "n/a (host CPU)"},
         "impl": "reference",
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": n_threads, "kind": "port",
@@ -452,7 +467,7 @@ def run_ours(args) -> None:
 
     def one_step():
         if is_adjoint:
-            eng.run_adjoint(cfg, checkpoint_every=32)  # synchronises: results are copied out
+            eng.run_adjoint(cfg, checkpoint_every=args.checkpoint_every)  # synchronises: results are copied out
         else:
             eng.enqueue(cfg, prec)
 
@@ -501,7 +516,7 @@ def run_ours(args) -> None:
         if is_adjoint:
             eng.set_market_poly(mk.n_tenor, mk.dtau, mk.spot, mk.vol_coeffs)
             set_product()
-            sens = eng.run_adjoint(cfg, checkpoint_every=32)
+            sens = eng.run_adjoint(cfg, checkpoint_every=args.checkpoint_every)
         else:
             eng.set_market(mk)
             set_product()
@@ -529,7 +544,7 @@ def run_ours(args) -> None:
         else:
             cold.set_swap(sw)
         if is_adjoint:
-            cold.run_adjoint(cfg, checkpoint_every=32)
+            cold.run_adjoint(cfg, checkpoint_every=args.checkpoint_every)
         else:
             cold.run(cfg, prec)
         cold_s = time.perf_counter() - t0
@@ -541,8 +556,11 @@ def run_ours(args) -> None:
         return
 
     form = vol_form
-    remainder = "convect" if is_adjoint else eng.remainder_form()
-    if prec != "fp64" and remainder == "response":
+    remainder = (("response" if args.checkpoint_every == 0 else "convect") if is_adjoint
+                 else eng.remainder_form())
+    if is_adjoint and remainder == "response":
+        flops = adjoint_response_flops_per_path(mk.n_tenor, n_steps, stride, form) * n_paths
+    elif prec != "fp64" and remainder == "response":
         flops = mixed_response_flops_per_path(mk.n_tenor, n_steps, stride, form) * n_paths
     else:
         flops = (algorithmic_flops_per_path(mk.n_tenor, n_steps, stride, form,
@@ -591,7 +609,9 @@ def run_ours(args) -> None:
         fma_busy = profiled_value("fma_pipe_cycles_active", f"{prec}-{n_paths}")
     roofline = {"bound": bound, "achieved": achieved, "peak": peak,
                 "unit": "TFLOP/s", "frac": (achieved / peak) if peak else None, "traffic": traffic,
-                "kernel": (f"adjoint_kernel<{mk.n_tenor},ckpt,{form}>" if is_adjoint else
+                "kernel": (f"adjoint_kernel_resp<{mixed_response_slots(mk.n_tenor, n_steps, stride)}>"
+                           if is_adjoint and remainder == "response" else
+                           f"adjoint_kernel<{mk.n_tenor},ckpt,{form}>" if is_adjoint else
                            "path_kernel_fp64_eresp<philox,degs(0,3,3),residual2>"
                            if prec == "fp64" and remainder == "response" and form == "cubic_resid" else
                            f"path_kernel_fp64_vresp<{mk.n_tenor},philox>"
@@ -646,7 +666,9 @@ def run_ours(args) -> None:
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": wl["dtype"], "data": "synthetic",
-        "config": {"workload": wl["name"], "n_paths_per_gpu": n_paths, "n_steps": n_steps, "dt": DT,
+        "config": {"workload": (wl["name"].replace("ckpt32", f"ckpt{args.checkpoint_every}"
+                                                   if args.checkpoint_every else "sampled-states")
+                                if is_adjoint else wl["name"]), "n_paths_per_gpu": n_paths, "n_steps": n_steps, "dt": DT,
                    "n_tenor": mk.n_tenor, "factors": 3, "sampled_dates": n_steps // stride,
                    "pfe_quantile": None if is_adjoint else 0.975, "hazard": 0.02,
                    "recovery": 0.4, "seed": SEED,
@@ -1171,6 +1193,9 @@ def main() -> None:
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="fp64")
     ap.add_argument("--paths", type=int, default=0, help="override the workload's path count (profiling only)")
+    ap.add_argument("--checkpoint-every", type=int, default=32,
+                    help="adjoint workload: curve checkpoints every K steps (0: the sampled states kept, "
+                         "the response form's adjoint)")
     ap.add_argument("--no-extras", action="store_true", help="only the headline workload")
     ap.add_argument("--table-step", action="store_true",
                     help="run the workload on the volatility-table step (no decomposition; profiling only)")

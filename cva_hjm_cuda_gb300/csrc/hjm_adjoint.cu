@@ -726,25 +726,31 @@ cudaError_t launch_adjoint_pc(int nt, const PcParams<float>& Q, bool poly, doubl
 // per slot (table row n) instead of the transposed convection of every tenor.
 // Dates whose responses never count (no slot) contribute below 2^-30 of
 // kappa per seed, as in the valuation.
+// Shared memory: the cash flows (then the exposures, one row up) share their
+// region with the sweep's coefficient sums, which start after the seeds have
+// read the exposures (17.1 KB per CTA at 20 dates: 12 CTAs per SM, as the
+// registers allow, instead of 10 with separate regions).
 struct AdjRespLayout {
-    size_t cf, xs, ds, cb, red, total;
+    size_t cf, cb, xs, ds, red, total;
 };
 
 __host__ __device__ inline AdjRespLayout adj_resp_layout(int B, int R)
 {
     AdjRespLayout L;
     const size_t rows = (size_t)B + 1;
-    L.cf = 0;
-    L.xs = align128((rows + 1) * kAdjCta * 4);
+    const size_t cf = (rows + 1) * kAdjCta * 4, cb = (size_t)9 * kAdjCta * 8;
+    L.cf = L.cb = 0;
+    L.xs = align128(cf > cb ? cf : cb);
     L.ds = align128(L.xs + rows * kAdjCta * 4);
-    L.cb = align128(L.ds + rows * kAdjCta * 4);
-    L.red = align128(L.cb + (size_t)9 * kAdjCta * 8);
+    L.red = align128(L.ds + rows * kAdjCta * 4);
     L.total = align128(L.red + (size_t)(kAdjCta / 32) * R * 8);
     return L;
 }
 
-// CTAs per SM: the registers' bound (8 slots in 80 per thread; 16 in 128)
-constexpr int adj_resp_min_ctas(int ns) { return ns <= 8 ? 12 : 8; }
+// CTAs per SM the launch bounds ask for (8 slots: at 11 the compiler keeps
+// 80 registers without spills, so 12 CTAs are resident, as the shared
+// memory allows; asked for 12 it spills; 16 slots in 128 registers, 8)
+constexpr int adj_resp_min_ctas(int ns) { return ns <= 8 ? 11 : 8; }
 
 template <int NS>
 __global__ void __launch_bounds__(kAdjCta, adj_resp_min_ctas(NS))
@@ -761,7 +767,7 @@ __global__ void __launch_bounds__(kAdjCta, adj_resp_min_ctas(NS))
     float* cf_s = reinterpret_cast<float*>(smem + Ly.cf);  // [B+2][C]: cash flows, then exposures one row up
     float* xs_s = reinterpret_cast<float*>(smem + Ly.xs);  // [B+1][C]: x_i, then xbar_i
     float* ds_s = reinterpret_cast<float*>(smem + Ly.ds);  // [B+1][C]: D_i, then abar_i
-    double* cb_s = reinterpret_cast<double*>(smem + Ly.cb);
+    double* cb_s = reinterpret_cast<double*>(smem + Ly.cb);  // [9][C], the sweep's (over cf_s)
     double* red_s = reinterpret_cast<double*>(smem + Ly.red);
 
     const int64_t lp = (int64_t)blockIdx.x * C + tid;
@@ -882,6 +888,7 @@ __global__ void __launch_bounds__(kAdjCta, adj_resp_min_ctas(NS))
     }
 
     // ---------------------------------------------------------------- reverse
+    __syncthreads();  // (cb_s overlays the exposures that the seeds just read)
     for (int q = 0; q < 9; ++q) cb_s[q * C + tid] = 0.0;
     float2 sd[NS];  // {xbar_j, abar_j} of slot r's date j = B - r once the sweep reaches it
 #pragma unroll
