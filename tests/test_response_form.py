@@ -586,3 +586,53 @@ def test_double_fp32_moving_frame_tracks_the_fp64_recursion(svc, seed, scheme):
     at the median date and path (2^-48 of the accumulator per addition over a
     block's ~150 additions; FP64 across blocks), < 7e-13 over 24 seeds."""
     assert _moving_frame_errors(svc, 50, 21, 0.01, 0.5, seed, df=True, scheme=scheme) < 1e-12
+
+
+# --- mixed precision's response form (hjm_mresp.cu) ---------------------------
+@pytest.mark.parametrize("nt,stride,B,c,ns", [(51, 50, 20, 0.02, 8), (51, 50, 24, 0.02, 16)])
+def test_mixed_slots_carry_every_counting_date_in_fp32(nt, stride, B, c, ns):
+    """The mixed kernel's FP32 sums over its ns slots (the latest dates; the
+    host's count, bench.mixed_response_slots) against the direct FP64
+    recursion of the remainder: the slotted dates within 4e-6 of their own
+    magnitude plus 1e-7 of the largest (FP32 accumulation of FP32-rounded
+    terms, one FMA per step: ~sqrt(steps) FP32 roundings, 2e-6 over 1,150
+    steps; the running sum's error is then ~1e-10 of the discount exponent,
+    far under its own FP32 evaluation), and the dates left without a slot below
+    1e-8 |kappa| max|W| per running-sum step (their terms never reach
+    2^-30 |kappa|)."""
+    import bench
+
+    assert bench.mixed_response_slots(nt, B * stride, stride) == ns
+    rng = np.random.default_rng(5)
+    W = np.cumsum(rng.normal(size=B * stride)) * 1e-5
+    tab, _, kappa = response_table(nt, stride, B, c, 0.5)
+    T = tab.reshape(B * stride, ROW, 2).astype(np.float32)
+    L = nt - 1
+    acc = np.zeros((ns, 2), dtype=np.float32)
+    hc = np.zeros(nt)
+    hsum = np.zeros(nt)
+    w = 0.0
+    got, want = {}, {}
+    for b in range(1, B):
+        for s in range(stride):
+            n = b * stride + s
+            wf = np.float32(w)
+            for r in range(ns):  # every slot every step, as the kernel
+                for q in range(2):
+                    acc[r, q] = _fma32(T[n, r, q], wf, acc[r, q])
+            hn = hc.copy()
+            hn[:L] = hc[:L] + c * (hc[1:] - hc[:L])
+            hn[L] = hc[L] + c * (hc[L] - hc[L - 1]) + kappa * w
+            hc = hn
+            hsum += hc
+            w = W[n]
+        j = b + 1
+        want[j] = (hc[j], hsum[j])
+        got[j] = (float(acc[B - j, 0]), float(acc[B - j, 1])) if B - j < ns else (0.0, 0.0)
+    big = [max(abs(want[j][q]) for j in want) for q in range(2)]
+    for j in want:
+        for q in range(2):
+            if B - j < ns:
+                assert abs(got[j][q] - want[j][q]) <= 4e-6 * abs(want[j][q]) + 1e-7 * big[q], (j, q)
+            else:
+                assert abs(want[j][q]) <= 1e-8 * abs(kappa) * np.max(np.abs(W)) * (j * stride if q else 1), (j, q)
