@@ -398,9 +398,7 @@ def run_reference(args) -> None:
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": (wl["name"].replace("ckpt32", f"ckpt{args.checkpoint_every}"
-                                                   if args.checkpoint_every else "sampled-states")
-                                if is_adjoint else wl["name"]), "sample_paths_per_step": n, "n_steps": N_STEPS, "dt": DT,
+        "config": {"workload": wl["name"], "sample_paths_per_step": n, "n_steps": N_STEPS, "dt": DT,
                    "n_tenor": 51, "l2": "n/a (host CPU)"},
         "impl": "reference",
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": n_threads, "kind": "port",

@@ -67,3 +67,18 @@ def test_mixed_response_slots_and_count():
     assert bench.mixed_response_flops_per_path(51, 1000, 50, "poly_tri") == want
     # far below the convected pairs' count on the same run
     assert want < 0.6 * bench.algorithmic_flops_per_path(51, 1000, 50, "poly_tri")
+
+
+def test_reference_arm_prints_its_line():
+    """bench.py --impl reference (the oracle port on the host cores) runs
+    without a GPU and prints one JSON line of the contract."""
+    import json
+    import subprocess
+
+    root = Path(__file__).resolve().parent.parent
+    r = subprocess.run([sys.executable, str(root / "bench.py"), "--impl", "reference", "--steps", "1",
+                        "--warmup", "0"], capture_output=True, text=True, timeout=600, cwd=root)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["value"] > 0
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["cpu_baseline"]["kind"] == "port"
