@@ -1,4 +1,4 @@
-// hjm_mresp.cu -- the response form of the mixed-precision Euler step.
+// hjm_mresp.cu -- the response form of the mixed-precision step (Euler and predictor-corrector).
 //
 // With polynomial volatility factors the stochastic curve splits as
 //     h = S + U t + W t^2 (+ X t^3) + hc,
