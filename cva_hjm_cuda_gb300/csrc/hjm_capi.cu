@@ -812,11 +812,7 @@ static void fill_pc(const hjm_ctx* ctx, const RunShape& sh, double dt, const Pat
 // Mixed precision with polynomial factors under the Euler step: the FP32
 // response form of hjm_mresp.cu when the dates whose responses count fit its
 // slots (mresp_slots: the 10y swap's 20 dates in 8), else the convected pairs.
-static bool use_response_form(const hjm_ctx* ctx, const RunShape& sh)
-{
-    (void)sh;
-    return ctx->remainder != HJM_REMAINDER_CONVECT;
-}
+static bool use_response_form(const hjm_ctx* ctx) { return ctx->remainder != HJM_REMAINDER_CONVECT; }
 
 // The volatility-table response table of the run shape, scheme and loadings
 // sv [kFactors][kMaxTenor] (the path parameters'), on the stream: rebuilt
@@ -1074,7 +1070,7 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
     // mixed precision with polynomial factors: the response form when the
     // dates its remainder reaches fit its slots (else the convected pairs)
     const int mresp_ns = (mixed && (pc ? use_poly_path(ctx) : (use_poly_path(ctx) || mixed_cubic)) &&
-                          use_response_form(ctx, sh))
+                          use_response_form(ctx))
                              ? mresp_run_slots(ctx, sh, dt, pc)
                              : 0;
     const int cta = mresp_ns ? kCta
@@ -1143,7 +1139,7 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
         PcParams<double> Q;
         fill_pc<double>(ctx, sh, dt, P, Q);
         ctx->stat_h2d = sizeof(Q) + sizeof(FinalParams);
-        resp = use_response_form(ctx, sh);
+        resp = use_response_form(ctx);
         if (resp && use_poly_path(ctx)) {
             // the decomposition in the response form of hjm_eresp.cu, with the
             // two-stage step's parts frame and remainder table (any number of dates)
@@ -1183,7 +1179,7 @@ static hjm_status enqueue_impl(hjm_ctx* ctx, int64_t n_paths, int32_t n_steps, d
     } else {
         PathParams<double> P;
         fill_params<double>(ctx, sh, n_paths, dt, seed, path_offset, hazard, recovery, ld, store, P, F);
-        resp = use_response_form(ctx, sh);
+        resp = use_response_form(ctx);
         if (resp && (use_poly_path(ctx) || use_cubic_path(ctx))) {
             st = enqueue_eresp(ctx, sh, dt, P, ext_dev, store ? (double*)ctx->estore.p : nullptr, s);
             if (st != HJM_OK) return st;
