@@ -809,9 +809,10 @@ static void fill_pc(const hjm_ctx* ctx, const RunShape& sh, double dt, const Pat
 // double-FP32 terms on the FP32 pipe (in windows of 16 dates), against four
 // FP64 FMAs per live tenor (five for the predictor-corrector) when convected.
 //
-// Mixed precision with polynomial factors under the Euler step: the FP32
-// response form of hjm_mresp.cu when the dates whose responses count fit its
-// slots (mresp_slots: the 10y swap's 20 dates in 8), else the convected pairs.
+// Mixed precision with polynomial factors (either scheme) and the adjoint
+// without checkpoints (Euler): the FP32 response form of hjm_mresp.cu when
+// the dates whose responses count fit its slots (mresp_slots: the 10y swap's
+// 20 dates in 8), else the convected pairs.
 static bool use_response_form(const hjm_ctx* ctx) { return ctx->remainder != HJM_REMAINDER_CONVECT; }
 
 // The volatility-table response table of the run shape, scheme and loadings
